@@ -1,0 +1,998 @@
+// CPU restatement of HOBAK's implicit tet-FEM timestep (the oracle).
+//
+// TEST INFRASTRUCTURE.  Only tests/, __graft_entry__.smoke() and bench.py's
+// CPU-baseline leg load this library, and only as the checker or the timed CPU
+// baseline -- never as the product path.  It is an independent FP64
+// restatement of the reference algorithm (no Eigen, no shared code with the
+// CUDA library), pinned against the reference build's golden vectors in
+// tests/golden/.  Each function cites the reference file:line it follows.
+//
+// Layouts: vectors are interleaved xyz (3V doubles); 3x3 matrices are column
+// major (a[i + 3*j] = A(i,j)), like the reference's flatten()
+// (util/MATRIX_UTIL.cpp:33-43); 9x9 and 12x12 matrices are column major.
+// Sparse matrices are 3x3-block CSR (BSR) with blocks stored column major.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+enum Material { SNH = 0, ARAP = 1, STVK = 2, LINEAR = 3, NHBW = 4, SNHB = 5 };
+
+inline double det3(const double* A) {
+  return A[0] * (A[4] * A[8] - A[7] * A[5]) - A[3] * (A[1] * A[8] - A[7] * A[2]) +
+         A[6] * (A[1] * A[5] - A[4] * A[2]);
+}
+
+// C = A * B (3x3, column major)
+inline void mul3(const double* A, const double* B, double* C) {
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) {
+      double s = 0;
+      for (int k = 0; k < 3; k++) s += A[i + 3 * k] * B[k + 3 * j];
+      C[i + 3 * j] = s;
+    }
+}
+
+// C = A * B^T
+inline void mul3t(const double* A, const double* B, double* C) {
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) {
+      double s = 0;
+      for (int k = 0; k < 3; k++) s += A[i + 3 * k] * B[j + 3 * k];
+      C[i + 3 * j] = s;
+    }
+}
+
+// 3x3 inverse by cofactors (TET_MESH.cpp:178-191 uses Eigen's Dm.inverse())
+inline void inv3(const double* A, double* Ai) {
+  const double d = det3(A);
+  const double id = 1.0 / d;
+  Ai[0] = (A[4] * A[8] - A[5] * A[7]) * id;
+  Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  Ai[3] = (A[5] * A[6] - A[3] * A[8]) * id;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+  Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  Ai[6] = (A[3] * A[7] - A[4] * A[6]) * id;
+  Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+}
+
+// Rotation-variant SVD, F = U diag(S) V^T with S sorted by magnitude, U and V
+// rotations, and any reflection carried by the sign of S[2] -- the convention
+// of svd_rv (util/MATRIX_UTIL.cpp:76-95).  Computed by one-sided (Hestenes)
+// Jacobi orthogonalisation of F's columns, a different route from the
+// reference's two-sided JacobiSVD; the factors agree up to the usual
+// non-uniqueness, and everything downstream is invariant to that.
+void svd_rv(const double* F, double* U, double* S, double* V) {
+  double A[9];
+  std::memcpy(A, F, sizeof(A));
+  double W[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+  for (int sweep = 0; sweep < 40; sweep++) {
+    bool rotated = false;
+    for (int r = 0; r < 3; r++) {
+      const int p = pq[r][0], q = pq[r][1];
+      double* ap = A + 3 * p;
+      double* aq = A + 3 * q;
+      const double alpha = ap[0] * ap[0] + ap[1] * ap[1] + ap[2] * ap[2];
+      const double beta = aq[0] * aq[0] + aq[1] * aq[1] + aq[2] * aq[2];
+      const double gamma = ap[0] * aq[0] + ap[1] * aq[1] + ap[2] * aq[2];
+      if (gamma == 0.0 || std::fabs(gamma) <= 1e-17 * std::sqrt(alpha * beta)) continue;
+      rotated = true;
+      const double zeta = (beta - alpha) / (2.0 * gamma);
+      const double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+      const double c = 1.0 / std::sqrt(1.0 + t * t), s = c * t;
+      for (int i = 0; i < 3; i++) {
+        const double x = ap[i], y = aq[i];
+        ap[i] = c * x - s * y;
+        aq[i] = s * x + c * y;
+        const double vx = W[i + 3 * p], vy = W[i + 3 * q];
+        W[i + 3 * p] = c * vx - s * vy;
+        W[i + 3 * q] = s * vx + c * vy;
+      }
+    }
+    if (!rotated) break;
+  }
+  double sig[3];
+  for (int k = 0; k < 3; k++)
+    sig[k] = std::sqrt(A[3 * k] * A[3 * k] + A[3 * k + 1] * A[3 * k + 1] + A[3 * k + 2] * A[3 * k + 2]);
+  int order[3] = {0, 1, 2};
+  std::sort(order, order + 3, [&](int a, int b) { return sig[a] > sig[b]; });
+  for (int k = 0; k < 3; k++) {
+    const int o = order[k];
+    S[k] = sig[o];
+    for (int i = 0; i < 3; i++) {
+      V[i + 3 * k] = W[i + 3 * o];
+      U[i + 3 * k] = S[k] > 0 ? A[i + 3 * o] / S[k] : 0.0;
+    }
+  }
+  // complete U where columns vanished (rank-deficient F)
+  const double tiny = 1e-300;
+  if (S[0] <= tiny) {
+    const double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    std::memcpy(U, I, sizeof(I));
+  } else if (S[1] <= tiny) {
+    // any unit vector orthogonal to u0
+    const double* u0 = U;
+    double e[3] = {0, 0, 0};
+    int m = 0;
+    for (int i = 1; i < 3; i++)
+      if (std::fabs(u0[i]) < std::fabs(u0[m])) m = i;
+    e[m] = 1;
+    double d = e[0] * u0[0] + e[1] * u0[1] + e[2] * u0[2];
+    double u1[3] = {e[0] - d * u0[0], e[1] - d * u0[1], e[2] - d * u0[2]};
+    double n = std::sqrt(u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]);
+    for (int i = 0; i < 3; i++) U[3 + i] = u1[i] / n;
+  }
+  if (S[2] <= tiny || S[1] <= tiny || S[0] <= tiny) {
+    U[6] = U[1] * U[5] - U[2] * U[4];
+    U[7] = U[2] * U[3] - U[0] * U[5];
+    U[8] = U[0] * U[4] - U[1] * U[3];
+  }
+  // fold reflections into S[2]
+  if (det3(U) < 0) {
+    for (int i = 0; i < 3; i++) U[6 + i] = -U[6 + i];
+    S[2] = -S[2];
+  }
+  if (det3(V) < 0) {
+    for (int i = 0; i < 3; i++) V[6 + i] = -V[6 + i];
+    S[2] = -S[2];
+  }
+}
+
+// Symmetric 3x3 eigensystem by cyclic Jacobi rotations; A = Q diag(L) Q^T.
+// Stands in for Eigen::SelfAdjointEigenSolver<MATRIX3> (SNH.cpp:130).
+void eig3sym(const double* Ain, double* Q, double* L) {
+  double a[3][3];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) a[i][j] = Ain[i + 3 * j];
+  double q[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+  for (int sweep = 0; sweep < 50; sweep++) {
+    double off = std::fabs(a[0][1]) + std::fabs(a[0][2]) + std::fabs(a[1][2]);
+    double diag = std::fabs(a[0][0]) + std::fabs(a[1][1]) + std::fabs(a[2][2]);
+    if (off == 0.0 || off <= 1e-18 * diag) break;
+    for (int r = 0; r < 3; r++) {
+      const int p = pq[r][0], k = pq[r][1];
+      if (a[p][k] == 0.0) continue;
+      const double theta = (a[k][k] - a[p][p]) / (2.0 * a[p][k]);
+      const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+      const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+      // a <- J^T a J, J = rotation in the (p,k) plane
+      for (int m = 0; m < 3; m++) {
+        const double amp = a[m][p], amk = a[m][k];
+        a[m][p] = c * amp - s * amk;
+        a[m][k] = s * amp + c * amk;
+      }
+      for (int m = 0; m < 3; m++) {
+        const double apm = a[p][m], akm = a[k][m];
+        a[p][m] = c * apm - s * akm;
+        a[k][m] = s * apm + c * akm;
+      }
+      for (int m = 0; m < 3; m++) {
+        const double qmp = q[m][p], qmk = q[m][k];
+        q[m][p] = c * qmp - s * qmk;
+        q[m][k] = s * qmp + c * qmk;
+      }
+    }
+  }
+  for (int i = 0; i < 3; i++) {
+    L[i] = a[i][i];
+    for (int m = 0; m < 3; m++) Q[m + 3 * i] = q[m][i];
+  }
+}
+
+struct MaterialParams {
+  int kind;
+  double mu, lambda, alpha;
+};
+
+MaterialParams makeMaterial(int kind, double mu, double lambda) {
+  MaterialParams m{kind, mu, lambda, 0.0};
+  if (kind == SNH) {  // SNH.cpp:23-32
+    m.lambda = lambda + mu;
+    m.alpha = 1.0 + m.mu / m.lambda;
+  } else if (kind == NHBW) {  // NEO_HOOKEAN_BW.cpp:23-29
+    m.alpha = 1.0 + mu / lambda;
+  } else if (kind == SNHB) {  // SNH_WITH_BARRIER.cpp:26-35
+    m.mu = (4.0 / 3.0) * mu;
+    m.lambda = lambda + (5.0 / 6.0) * mu;
+    m.alpha = 1.0 + m.mu / m.lambda - m.mu / (4.0 * m.lambda);
+  }
+  return m;
+}
+
+// pJ/pF = [f1 x f2, f2 x f0, f0 x f1] (util/MATRIX_UTIL.cpp:561-568)
+inline void pJpF(const double* F, double* G) {
+  const double* f0 = F;
+  const double* f1 = F + 3;
+  const double* f2 = F + 6;
+  G[0] = f1[1] * f2[2] - f1[2] * f2[1];
+  G[1] = f1[2] * f2[0] - f1[0] * f2[2];
+  G[2] = f1[0] * f2[1] - f1[1] * f2[0];
+  G[3] = f2[1] * f0[2] - f2[2] * f0[1];
+  G[4] = f2[2] * f0[0] - f2[0] * f0[2];
+  G[5] = f2[0] * f0[1] - f2[1] * f0[0];
+  G[6] = f0[1] * f1[2] - f0[2] * f1[1];
+  G[7] = f0[2] * f1[0] - f0[0] * f1[2];
+  G[8] = f0[0] * f1[1] - f0[1] * f1[0];
+}
+
+inline double sqnorm9(const double* A) {
+  double s = 0;
+  for (int k = 0; k < 9; k++) s += A[k] * A[k];
+  return s;
+}
+
+// Strain energy density psi(F): SNH.cpp:34-43, ARAP.cpp:39-43 (through
+// HYPERELASTIC.cpp:41-47), STVK.cpp psi, LINEAR.cpp psi, NEO_HOOKEAN_BW.cpp psi,
+// SNH_WITH_BARRIER.cpp psi.
+double psi(const MaterialParams& m, const double* F) {
+  switch (m.kind) {
+    case SNH: {
+      const double Ic = sqnorm9(F), Jm = det3(F) - m.alpha;
+      return 0.5 * (m.mu * (Ic - 3.0) + m.lambda * Jm * Jm);
+    }
+    case ARAP: {
+      double U[9], S[3], V[9], R[9];
+      svd_rv(F, U, S, V);
+      mul3t(U, V, R);
+      double d = 0;
+      for (int k = 0; k < 9; k++) d += (F[k] - R[k]) * (F[k] - R[k]);
+      return m.mu * d;
+    }
+    case STVK: {
+      double FtF[9], E[9];
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) {
+          double s = 0;
+          for (int k = 0; k < 3; k++) s += F[k + 3 * i] * F[k + 3 * j];
+          FtF[i + 3 * j] = s;
+        }
+      for (int k = 0; k < 9; k++) E[k] = 0.5 * (FtF[k] - (k % 4 == 0 ? 1.0 : 0.0));
+      const double tr = E[0] + E[4] + E[8];
+      return m.mu * sqnorm9(E) + m.lambda * 0.5 * tr * tr;
+    }
+    case LINEAR: {
+      double e[9];
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) e[i + 3 * j] = 0.5 * (F[i + 3 * j] + F[j + 3 * i]) - (i == j ? 1.0 : 0.0);
+      const double tr = e[0] + e[4] + e[8];
+      return m.mu * sqnorm9(e) + 0.5 * m.lambda * tr * tr;
+    }
+    case NHBW: {
+      const double Ic = sqnorm9(F), lj = std::log(det3(F));
+      return m.mu * 0.5 * (Ic - 3.0) - m.mu * lj + m.lambda * 0.5 * lj * lj;
+    }
+    case SNHB: {
+      const double Ic = sqnorm9(F), Jm = det3(F) - m.alpha;
+      return 0.5 * (m.mu * (Ic - 3.0) + m.lambda * Jm * Jm - m.mu * std::log(Ic + 1.0));
+    }
+  }
+  return 0.0;
+}
+
+// First Piola-Kirchhoff stress P(F): SNH.cpp:45-50, ARAP.cpp:48-55 (through
+// HYPERELASTIC.cpp:61-67), STVK.cpp PK1, LINEAR.cpp PK1, NEO_HOOKEAN_BW.cpp PK1,
+// SNH_WITH_BARRIER.cpp PK1.
+void PK1(const MaterialParams& m, const double* F, double* P) {
+  switch (m.kind) {
+    case SNH: {
+      double G[9];
+      pJpF(F, G);
+      const double Jm = det3(F) - m.alpha;
+      for (int k = 0; k < 9; k++) P[k] = m.mu * F[k] + m.lambda * Jm * G[k];
+      return;
+    }
+    case ARAP: {
+      // R (2 mu (S - I)) with R = U V^T, S = V Sigma V^T
+      double U[9], S[3], V[9], R[9], Sm[9], T[9];
+      svd_rv(F, U, S, V);
+      mul3t(U, V, R);
+      double VS[9];
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) VS[i + 3 * j] = V[i + 3 * j] * S[j];
+      mul3t(VS, V, Sm);
+      for (int k = 0; k < 9; k++) T[k] = 2.0 * m.mu * (Sm[k] - (k % 4 == 0 ? 1.0 : 0.0));
+      mul3(R, T, P);
+      return;
+    }
+    case STVK: {
+      double FtF[9], E[9], Sg[9];
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) {
+          double s = 0;
+          for (int k = 0; k < 3; k++) s += F[k + 3 * i] * F[k + 3 * j];
+          FtF[i + 3 * j] = s;
+        }
+      for (int k = 0; k < 9; k++) E[k] = 0.5 * (FtF[k] - (k % 4 == 0 ? 1.0 : 0.0));
+      const double tr = E[0] + E[4] + E[8];
+      for (int k = 0; k < 9; k++) Sg[k] = (k % 4 == 0 ? m.lambda * tr : 0.0) + 2.0 * m.mu * E[k];
+      mul3(F, Sg, P);
+      return;
+    }
+    case LINEAR: {
+      double e[9];
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) e[i + 3 * j] = 0.5 * (F[i + 3 * j] + F[j + 3 * i]) - (i == j ? 1.0 : 0.0);
+      const double tr = e[0] + e[4] + e[8];
+      for (int k = 0; k < 9; k++) P[k] = 2.0 * m.mu * e[k] + (k % 4 == 0 ? m.lambda * tr : 0.0);
+      return;
+    }
+    case NHBW: {
+      double G[9];
+      pJpF(F, G);
+      const double J = det3(F);
+      for (int k = 0; k < 9; k++) P[k] = m.mu * (F[k] - (1.0 / J) * G[k]) + m.lambda * std::log(J) * (1.0 / J) * G[k];
+      return;
+    }
+    case SNHB: {
+      double G[9];
+      pJpF(F, G);
+      const double Ic = sqnorm9(F), Jm = det3(F) - m.alpha;
+      for (int k = 0; k < 9; k++) P[k] = m.mu * F[k] + m.lambda * Jm * G[k] - m.mu / (Ic + 1) * F[k];
+      return;
+    }
+  }
+}
+
+// Q9 columns 0-5: twist and flip modes (util/MATRIX_UTIL.cpp:420-460)
+void twistFlip(const double* U, const double* V, double* Q9) {
+  const double r = 1.0 / std::sqrt(2.0);
+  // twist k is U T_k V^T with T_k = e_j e_i^T - e_i e_j^T for (i, j) =
+  // (1,2), (2,0), (1,0): the x-, y- and z-twists of MATRIX_UTIL.cpp:424-433
+  const int ij[3][2] = {{1, 2}, {2, 0}, {1, 0}};
+  for (int k = 0; k < 3; k++) {
+    const int i = ij[k][0], j = ij[k][1];
+    for (int c = 0; c < 3; c++)
+      for (int rr = 0; rr < 3; rr++) {
+        // (U T V^T)(rr,c) = U(rr,j) V(c,i) - U(rr,i) V(c,j)
+        const double tw = U[rr + 3 * j] * V[c + 3 * i] - U[rr + 3 * i] * V[c + 3 * j];
+        const double fl = U[rr + 3 * j] * V[c + 3 * i] + U[rr + 3 * i] * V[c + 3 * j];
+        Q9[9 * k + rr + 3 * c] = r * tw;
+        Q9[9 * (k + 3) + rr + 3 * c] = r * fl;
+      }
+  }
+}
+
+// Q9 columns 6-8: scaling modes U diag(q_k) V^T (util/MATRIX_UTIL.cpp:465-497)
+void scaling(const double* U, const double* Q3, const double* V, double* Q9) {
+  for (int k = 0; k < 3; k++)
+    for (int c = 0; c < 3; c++)
+      for (int rr = 0; rr < 3; rr++) {
+        double s = 0;
+        for (int m = 0; m < 3; m++) s += U[rr + 3 * m] * Q3[m + 3 * k] * V[c + 3 * m];
+        Q9[9 * (6 + k) + rr + 3 * c] = s;
+      }
+}
+
+// H9 = Q diag(max(L, 0)) Q^T
+void assembleClamped(const double* Q9, double* L, double* H9) {
+  for (int k = 0; k < 9; k++)
+    if (L[k] < 0.0) L[k] = 0.0;
+  for (int c = 0; c < 9; c++)
+    for (int r = 0; r < 9; r++) {
+      double s = 0;
+      for (int k = 0; k < 9; k++) s += Q9[9 * k + r] * L[k] * Q9[9 * k + c];
+      H9[r + 9 * c] = s;
+    }
+}
+
+// Clamped 9x9 Hessian d2psi/dF2 projected to PSD, as a function of
+// (U, Sigma, V): SNH.cpp:94-144, ARAP.cpp:113-135, STVK.cpp buildEigensystem
+// (Appendix F.1 eigensystem), LINEAR.cpp hessian (no clamp),
+// NEO_HOOKEAN_BW.cpp clampedHessian, SNH_WITH_BARRIER.cpp clampedHessian.
+void clampedHessian(const MaterialParams& m, const double* U, const double* S, const double* V, double* H9) {
+  double Q9[81], L[9];
+  const double s0 = S[0], s1 = S[1], s2 = S[2];
+  if (m.kind == LINEAR) {
+    std::memset(H9, 0, 81 * sizeof(double));
+    for (int k = 0; k < 9; k++) H9[k + 9 * k] = m.mu;
+    const double d = m.mu + m.lambda;
+    H9[0 + 9 * 0] += d;
+    H9[4 + 9 * 4] += d;
+    H9[8 + 9 * 8] += d;
+    H9[1 + 9 * 3] = H9[3 + 9 * 1] = m.mu;
+    H9[2 + 9 * 6] = H9[6 + 9 * 2] = m.mu;
+    H9[5 + 9 * 7] = H9[7 + 9 * 5] = m.mu;
+    H9[0 + 9 * 4] = H9[0 + 9 * 8] = H9[4 + 9 * 8] = m.lambda;
+    H9[4 + 9 * 0] = H9[8 + 9 * 0] = H9[8 + 9 * 4] = m.lambda;
+    return;
+  }
+  twistFlip(U, V, Q9);
+  if (m.kind == ARAP) {
+    for (int k = 0; k < 9; k++) L[k] = 2.0 * m.mu;
+    L[0] = m.mu * (2.0 - 4.0 / (s1 + s2));
+    L[1] = m.mu * (2.0 - 4.0 / (s0 + s2));
+    L[2] = m.mu * (2.0 - 4.0 / (s0 + s1));
+    const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    scaling(U, I3, V, Q9);
+    assembleClamped(Q9, L, H9);
+    return;
+  }
+  double A[9];
+  if (m.kind == SNH) {
+    const double J = s0 * s1 * s2;
+    const double front = m.lambda * (J - 1.0) - m.mu;
+    L[0] = front * s0 + m.mu;
+    L[1] = front * s1 + m.mu;
+    L[2] = front * s2 + m.mu;
+    L[3] = -front * s0 + m.mu;
+    L[4] = -front * s1 + m.mu;
+    L[5] = -front * s2 + m.mu;
+    A[0] = m.mu + m.lambda * s1 * s1 * s2 * s2;
+    A[4] = m.mu + m.lambda * s0 * s0 * s2 * s2;
+    A[8] = m.mu + m.lambda * s0 * s0 * s1 * s1;
+    const double od = m.lambda * (2.0 * J - 1.0) - m.mu;
+    A[3] = A[1] = od * s2;
+    A[6] = A[2] = od * s1;
+    A[7] = A[5] = od * s0;
+  } else if (m.kind == STVK) {
+    const double I2 = s0 * s0 + s1 * s1 + s2 * s2;
+    const double front = -m.mu + m.lambda * 0.5 * (I2 - 3.0);
+    L[0] = front + m.mu * (s1 * s1 + s2 * s2 - s1 * s2);
+    L[1] = front + m.mu * (s0 * s0 + s2 * s2 - s0 * s2);
+    L[2] = front + m.mu * (s0 * s0 + s1 * s1 - s0 * s1);
+    L[3] = front + m.mu * (s1 * s1 + s2 * s2 + s1 * s2);
+    L[4] = front + m.mu * (s0 * s0 + s2 * s2 + s0 * s2);
+    L[5] = front + m.mu * (s0 * s0 + s1 * s1 + s0 * s1);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        A[i + 3 * j] = (i == j) ? front + (m.lambda + 3.0 * m.mu) * S[i] * S[i] : m.lambda * S[i] * S[j];
+  } else if (m.kind == NHBW) {
+    const double J = s0 * s1 * s2, lj = std::log(J);
+    const double i01 = 1.0 / (s0 * s1), i02 = 1.0 / (s0 * s2), i12 = 1.0 / (s1 * s2);
+    const double front = m.lambda * lj - m.mu;
+    L[0] = front * i12 + m.mu;
+    L[1] = front * i02 + m.mu;
+    L[2] = front * i01 + m.mu;
+    L[3] = -front * i12 + m.mu;
+    L[4] = -front * i02 + m.mu;
+    L[5] = -front * i01 + m.mu;
+    const double fd = m.lambda * (1.0 - lj) + m.mu;
+    A[0] = fd / (s0 * s0) + m.mu;
+    A[4] = fd / (s1 * s1) + m.mu;
+    A[8] = fd / (s2 * s2) + m.mu;
+    A[3] = A[1] = m.lambda * i01;
+    A[6] = A[2] = m.lambda * i02;
+    A[7] = A[5] = m.lambda * i12;
+  } else {  // SNHB
+    const double J = s0 * s1 * s2, I2 = s0 * s0 + s1 * s1 + s2 * s2;
+    const double front = -m.mu / (I2 + 1.0) + m.mu;
+    const double back = m.lambda * (J - m.alpha);
+    for (int i = 0; i < 3; i++) {
+      L[i] = front + back * S[i];
+      L[i + 3] = front - back * S[i];
+    }
+    const double sq = (I2 + 1.0) * (I2 + 1.0), isq = 1.0 / sq, tm = 2.0 * m.mu;
+    const double fd = (-m.mu * (I2 + 1.0)) * isq + m.mu;
+    const double fo = (2.0 * J - m.alpha) * m.lambda;
+    A[0] = fd + tm * s0 * s0 * isq + m.lambda * s1 * s1 * s2 * s2;
+    A[4] = fd + tm * s1 * s1 * isq + m.lambda * s0 * s0 * s2 * s2;
+    A[8] = fd + tm * s2 * s2 * isq + m.lambda * s0 * s0 * s1 * s1;
+    A[3] = A[1] = fo * s2 + (tm * s0 * s1) * isq;
+    A[6] = A[2] = fo * s1 + (tm * s0 * s2) * isq;
+    A[7] = A[5] = fo * s0 + (tm * s1 * s2) * isq;
+  }
+  double Q3[9], L3[3];
+  eig3sym(A, Q3, L3);
+  for (int k = 0; k < 3; k++) L[6 + k] = L3[k];
+  scaling(U, Q3, V, Q9);
+  assembleClamped(Q9, L, H9);
+}
+
+// pFpx (9x12) from DmInv (TET_MESH.cpp:197-252): column 3*a+i, row i+3*j.
+void pFpx(const double* Dinv, double* P) {
+  std::memset(P, 0, 108 * sizeof(double));
+  for (int j = 0; j < 3; j++) {
+    const double t = -(Dinv[0 + 3 * j] + Dinv[1 + 3 * j] + Dinv[2 + 3 * j]);
+    for (int i = 0; i < 3; i++) {
+      const int row = i + 3 * j;
+      P[row + 9 * (0 + i)] = t;
+      for (int a = 1; a < 4; a++) P[row + 9 * (3 * a + i)] = Dinv[(a - 1) + 3 * j];
+    }
+  }
+}
+
+struct Mesh {
+  int nv = 0, nt = 0;
+  std::vector<double> rest;     // 3V
+  std::vector<int> tets;        // 4T
+  std::vector<double> vol;      // T
+  std::vector<double> oneRing;  // V
+  std::vector<double> DmInv;    // 9T
+  // BSR pattern: row u -> sorted neighbour vertices
+  std::vector<int> rowptr, cols;
+  std::vector<int> diag;        // block index of (u,u)
+  // vertex -> incident (tet, local slot), ascending tet
+  std::vector<int> vtxptr, vtxinc;
+  // per tet: block index of (tet[a], tet[b]) for a,b in 0..3
+  std::vector<int> tetBlocks;   // 16T
+};
+
+// Rest volumes, one-ring volumes, DmInv (TET_MESH.cpp:121-191) and the
+// block sparsity of the stiffness matrix (TET_MESH_FASTER.cpp:30-73).
+void buildMesh(Mesh& M, int nv, int nt, const double* rest, const int* tets) {
+  M.nv = nv;
+  M.nt = nt;
+  M.rest.assign(rest, rest + 3 * nv);
+  M.tets.assign(tets, tets + 4 * nt);
+  M.vol.resize(nt);
+  M.oneRing.assign(nv, 0.0);
+  M.DmInv.resize(9 * (size_t)nt);
+  for (int t = 0; t < nt; t++) {
+    const int* v = tets + 4 * t;
+    double Dm[9];
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < 3; i++) Dm[i + 3 * a] = rest[3 * v[a + 1] + i] - rest[3 * v[0] + i];
+    const double* d1 = Dm;
+    const double* d2 = Dm + 3;
+    const double* d3 = Dm + 6;
+    const double cr[3] = {d1[1] * d2[2] - d1[2] * d2[1], d1[2] * d2[0] - d1[0] * d2[2], d1[0] * d2[1] - d1[1] * d2[0]};
+    M.vol[t] = (d3[0] * cr[0] + d3[1] * cr[1] + d3[2] * cr[2]) / 6.0;
+    inv3(Dm, &M.DmInv[9 * (size_t)t]);
+  }
+  for (int t = 0; t < nt; t++) {
+    const double q = 0.25 * M.vol[t];
+    for (int a = 0; a < 4; a++) M.oneRing[tets[4 * t + a]] += q;
+  }
+  // vertex incidence, ascending tet order
+  M.vtxptr.assign(nv + 1, 0);
+  for (int k = 0; k < 4 * nt; k++) M.vtxptr[tets[k] + 1]++;
+  for (int v = 0; v < nv; v++) M.vtxptr[v + 1] += M.vtxptr[v];
+  M.vtxinc.resize(4 * (size_t)nt);
+  std::vector<int> fill(M.vtxptr.begin(), M.vtxptr.end() - 1);
+  for (int t = 0; t < nt; t++)
+    for (int a = 0; a < 4; a++) M.vtxinc[fill[tets[4 * t + a]]++] = 4 * t + a;
+  // block pattern
+  M.rowptr.assign(nv + 1, 0);
+  std::vector<std::vector<int>> nb(nv);
+  for (int v = 0; v < nv; v++) {
+    auto& n = nb[v];
+    for (int k = M.vtxptr[v]; k < M.vtxptr[v + 1]; k++) {
+      const int t = M.vtxinc[k] / 4;
+      for (int b = 0; b < 4; b++) n.push_back(tets[4 * t + b]);
+    }
+    std::sort(n.begin(), n.end());
+    n.erase(std::unique(n.begin(), n.end()), n.end());
+    M.rowptr[v + 1] = M.rowptr[v] + (int)n.size();
+  }
+  M.cols.resize(M.rowptr[nv]);
+  M.diag.resize(nv);
+  for (int v = 0; v < nv; v++) {
+    std::copy(nb[v].begin(), nb[v].end(), M.cols.begin() + M.rowptr[v]);
+    M.diag[v] = M.rowptr[v] + int(std::lower_bound(nb[v].begin(), nb[v].end(), v) - nb[v].begin());
+  }
+  M.tetBlocks.resize(16 * (size_t)nt);
+  for (int t = 0; t < nt; t++)
+    for (int a = 0; a < 4; a++)
+      for (int b = 0; b < 4; b++) {
+        const int u = tets[4 * t + a], w = tets[4 * t + b];
+        const int* beg = &M.cols[M.rowptr[u]];
+        const int* end = &M.cols[M.rowptr[u + 1]];
+        M.tetBlocks[16 * (size_t)t + 4 * a + b] = M.rowptr[u] + int(std::lower_bound(beg, end, w) - beg);
+      }
+}
+
+// Per-tet F = Ds DmInv (TET_MESH.cpp:706-714), force
+// -vol pFpx^T vec(P) (TET_MESH.cpp:736-747) and element Hessian
+// pFpx^T (-vol clampedHessian) pFpx (TET_MESH_FASTER.cpp:95-103).
+void elementTerms(const Mesh& M, const MaterialParams& mat, const double* disp, int t, double* F, double* U,
+                  double* S, double* V, double* fe, double* He) {
+  const int* v = &M.tets[4 * (size_t)t];
+  double x[4][3];
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++) x[a][i] = M.rest[3 * v[a] + i] + disp[3 * v[a] + i];
+  double Ds[9];
+  for (int a = 0; a < 3; a++)
+    for (int i = 0; i < 3; i++) Ds[i + 3 * a] = x[a + 1][i] - x[0][i];
+  mul3(Ds, &M.DmInv[9 * (size_t)t], F);
+  svd_rv(F, U, S, V);
+  double P9[108];
+  pFpx(&M.DmInv[9 * (size_t)t], P9);
+  const double vol = M.vol[t];
+  if (fe) {
+    double P[9];
+    PK1(mat, F, P);
+    for (int c = 0; c < 12; c++) {
+      double s = 0;
+      for (int r = 0; r < 9; r++) s += P9[r + 9 * c] * P[r];
+      fe[c] = -vol * s;
+    }
+  }
+  if (He) {
+    double H9[81], T[108];
+    clampedHessian(mat, U, S, V, H9);
+    for (int k = 0; k < 81; k++) H9[k] *= -vol;
+    for (int c = 0; c < 12; c++)
+      for (int r = 0; r < 9; r++) {
+        double s = 0;
+        for (int k = 0; k < 9; k++) s += H9[r + 9 * k] * P9[k + 9 * c];
+        T[r + 9 * c] = s;
+      }
+    for (int c = 0; c < 12; c++)
+      for (int r = 0; r < 12; r++) {
+        double s = 0;
+        for (int k = 0; k < 9; k++) s += P9[k + 9 * r] * T[k + 9 * c];
+        He[r + 12 * c] = s;
+      }
+  }
+}
+
+// Deterministic chunked dot product (fixed summation tree, any thread count).
+double dot(const std::vector<double>& a, const std::vector<double>& b) {
+  const long n = (long)a.size();
+  const long chunk = 4096;
+  const long nc = (n + chunk - 1) / chunk;
+  std::vector<double> part(nc);
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < nc; c++) {
+    double s = 0;
+    const long e = std::min(n, (c + 1) * chunk);
+    for (long i = c * chunk; i < e; i++) s += a[i] * b[i];
+    part[c] = s;
+  }
+  double s = 0;
+  for (long c = 0; c < nc; c++) s += part[c];
+  return s;
+}
+
+struct Sim {
+  Mesh M;
+  MaterialParams mat;
+  std::vector<int> pinned;
+  std::vector<double> pinTarget;  // 3 per pinned vertex
+  std::vector<unsigned char> free;  // per vertex: 1 = free, 0 = pinned (S block = I or 0)
+  double density = 1.0, dt = 1.0 / 60.0;
+  double gravity[3] = {0, 0, 0};
+  double tol = 1e-8;
+  int maxit = 1000;
+  int precond = 0;  // 0 = scalar Jacobi (Eigen DiagonalPreconditioner), 1 = 3x3 block Jacobi
+  std::vector<double> x, v, fext;
+  std::vector<double> K, A, R, He, fe;
+  int lastIters = 0;
+  double lastErr = 0;
+};
+
+// K = sum of element Hessians per block, gathered per row in ascending tet
+// order like TET_MESH_FASTER's _hessianGathers (TET_MESH_FASTER.cpp:113-131);
+// R = sum of element forces per vertex in ascending tet order
+// (TET_MESH.cpp:756-767).
+void assemble(Sim& s) {
+  const Mesh& M = s.M;
+  const int nt = M.nt, nv = M.nv;
+  s.He.resize(144 * (size_t)nt);
+  s.fe.resize(12 * (size_t)nt);
+#pragma omp parallel for schedule(static)
+  for (int t = 0; t < nt; t++) {
+    double F[9], U[9], S[3], V[9];
+    elementTerms(M, s.mat, s.x.data(), t, F, U, S, V, &s.fe[12 * (size_t)t], &s.He[144 * (size_t)t]);
+  }
+  s.K.assign(9 * (size_t)M.rowptr[nv], 0.0);
+  s.R.assign(3 * (size_t)nv, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int u = 0; u < nv; u++) {
+    for (int k = M.vtxptr[u]; k < M.vtxptr[u + 1]; k++) {
+      const int t = M.vtxinc[k] / 4, a = M.vtxinc[k] % 4;
+      const double* H = &s.He[144 * (size_t)t];
+      for (int i = 0; i < 3; i++) s.R[3 * u + i] += s.fe[12 * (size_t)t + 3 * a + i];
+      for (int b = 0; b < 4; b++) {
+        double* blk = &s.K[9 * (size_t)M.tetBlocks[16 * (size_t)t + 4 * a + b]];
+        for (int c = 0; c < 3; c++)
+          for (int r = 0; r < 3; r++) blk[r + 3 * c] += H[(3 * a + r) + 12 * (3 * b + c)];
+      }
+    }
+  }
+}
+
+// y = LHS x with LHS = S A S + (I - S), S = diag(free) per vertex
+// (BACKWARD_EULER_VELOCITY.cpp:170); A's blocks in `A`.
+void applyLHS(const Sim& s, const std::vector<double>& A, const std::vector<double>& x, std::vector<double>& y) {
+  const Mesh& M = s.M;
+#pragma omp parallel for schedule(static)
+  for (int u = 0; u < M.nv; u++) {
+    if (!s.free[u]) {
+      for (int i = 0; i < 3; i++) y[3 * u + i] = x[3 * u + i];
+      continue;
+    }
+    for (int i = 0; i < 3; i++) {
+      double acc = 0;
+      for (int k = M.rowptr[u]; k < M.rowptr[u + 1]; k++) {
+        const int w = M.cols[k];
+        if (!s.free[w]) continue;
+        const double* blk = &A[9 * (size_t)k];
+        for (int c = 0; c < 3; c++) acc += blk[i + 3 * c] * x[3 * w + c];
+      }
+      y[3 * u + i] = acc;
+    }
+  }
+}
+
+// Preconditioned CG restating Eigen's conjugate_gradient
+// (ext/eigen-3.3.7/Eigen/src/IterativeLinearSolvers/ConjugateGradient.h:28-90)
+// with x0 = 0 (ConjugateGradient.h:236) and the Jacobi preconditioner
+// (BasicPreconditioners.h:67-75); precond = 1 swaps in 3x3 block Jacobi.
+void pcg(Sim& s, const std::vector<double>& A, const std::vector<double>& rhs, std::vector<double>& x) {
+  const Mesh& M = s.M;
+  const size_t n = 3 * (size_t)M.nv;
+  x.assign(n, 0.0);
+  std::vector<double> r(rhs), p(n), z(n), tmp(n), inv(9 * (size_t)M.nv, 0.0);
+  // preconditioner from LHS's diagonal (pinned blocks are identity)
+  for (int u = 0; u < M.nv; u++) {
+    double* B = &inv[9 * (size_t)u];
+    if (!s.free[u]) {
+      B[0] = B[4] = B[8] = 1.0;
+      continue;
+    }
+    const double* D = &A[9 * (size_t)M.diag[u]];
+    if (s.precond == 1) {
+      inv3(D, B);
+    } else {
+      for (int i = 0; i < 3; i++) B[4 * i] = D[4 * i] != 0.0 ? 1.0 / D[4 * i] : 1.0;
+    }
+  }
+  auto applyPrec = [&](const std::vector<double>& in, std::vector<double>& out) {
+#pragma omp parallel for schedule(static)
+    for (int u = 0; u < M.nv; u++) {
+      const double* B = &inv[9 * (size_t)u];
+      for (int i = 0; i < 3; i++) {
+        if (s.precond == 1)
+          out[3 * u + i] = B[i] * in[3 * u] + B[i + 3] * in[3 * u + 1] + B[i + 6] * in[3 * u + 2];
+        else
+          out[3 * u + i] = B[4 * i] * in[3 * u + i];
+      }
+    }
+  };
+  const double rhsNorm2 = dot(rhs, rhs);
+  s.lastIters = 0;
+  if (rhsNorm2 == 0) {
+    s.lastErr = 0;
+    return;
+  }
+  const double threshold = std::max(s.tol * s.tol * rhsNorm2, std::numeric_limits<double>::min());
+  double rn2 = dot(r, r);
+  if (rn2 < threshold) {
+    s.lastErr = std::sqrt(rn2 / rhsNorm2);
+    return;
+  }
+  applyPrec(r, p);
+  double absNew = dot(r, p);
+  int i = 0;
+  while (i < s.maxit) {
+    applyLHS(s, A, p, tmp);
+    const double alpha = absNew / dot(p, tmp);
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < (long)n; k++) {
+      x[k] += alpha * p[k];
+      r[k] -= alpha * tmp[k];
+    }
+    rn2 = dot(r, r);
+    if (rn2 < threshold) break;
+    applyPrec(r, z);
+    const double absOld = absNew;
+    absNew = dot(r, z);
+    const double beta = absNew / absOld;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < (long)n; k++) p[k] = z[k] + beta * p[k];
+    i++;
+  }
+  s.lastErr = std::sqrt(rn2 / rhsNorm2);
+  s.lastIters = i;
+}
+
+// One BACKWARD_EULER_VELOCITY::solveRayleighDamped step with collisions off
+// (BACKWARD_EULER_VELOCITY.cpp:107-235).  The Rayleigh C built at line 118 is
+// zeroed by computeCollisionResponse (TIMESTEPPER.cpp:657) before use, so it
+// is not formed here; with no plane constraints z = 0 (BEV.cpp:52-81).
+void step(Sim& s) {
+  const Mesh& M = s.M;
+  const int nv = M.nv;
+  // applyKinematicConstraints (TIMESTEPPER.cpp:105-122)
+  for (size_t k = 0; k < s.pinned.size(); k++)
+    for (int i = 0; i < 3; i++) s.x[3 * s.pinned[k] + i] = s.pinTarget[3 * k + i];
+  assemble(s);
+  const double dt = s.dt;
+  // K v
+  std::vector<double> Kv(3 * (size_t)nv);
+#pragma omp parallel for schedule(static)
+  for (int u = 0; u < nv; u++)
+    for (int i = 0; i < 3; i++) {
+      double acc = 0;
+      for (int k = M.rowptr[u]; k < M.rowptr[u + 1]; k++) {
+        const double* blk = &s.K[9 * (size_t)k];
+        const int w = M.cols[k];
+        for (int c = 0; c < 3; c++) acc += blk[i + 3 * c] * s.v[3 * w + c];
+      }
+      Kv[3 * u + i] = acc;
+    }
+  // b = dt (R + dt K v + f); rhs = S b; A = M - dt^2 K (BEV.cpp:157-170)
+  std::vector<double> rhs(3 * (size_t)nv);
+  for (int u = 0; u < nv; u++)
+    for (int i = 0; i < 3; i++) {
+      const size_t k = 3 * (size_t)u + i;
+      const double b = dt * (s.R[k] + dt * Kv[k] + s.fext[k]);
+      rhs[k] = s.free[u] ? b : 0.0;
+    }
+  s.A.resize(s.K.size());
+  const double dt2 = dt * dt;
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < (long)s.K.size(); k++) s.A[k] = -dt2 * s.K[k];
+  for (int u = 0; u < nv; u++) {
+    double* D = &s.A[9 * (size_t)M.diag[u]];
+    const double m = s.density * M.oneRing[u];
+    for (int i = 0; i < 3; i++) D[4 * i] = m + D[4 * i];
+  }
+  std::vector<double> y;
+  pcg(s, s.A, rhs, y);
+  // v += y; x += dt v; v = S v (BEV.cpp:191-201)
+  for (int u = 0; u < nv; u++)
+    for (int i = 0; i < 3; i++) {
+      const size_t k = 3 * (size_t)u + i;
+      s.v[k] = s.v[k] + y[k];
+      s.x[k] = s.x[k] + dt * s.v[k];
+      if (!s.free[u]) s.v[k] = 0.0;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// Per-tet quantities at displacement `disp`; any output pointer may be null.
+int oracle_elements(int nv, int nt, const double* rest, const int* tets, const double* disp, int material, double mu,
+                    double lambda, double* F, double* Sigma, double* psiOut, double* P, double* H9, double* fe,
+                    double* He) {
+  if (nv <= 0 || nt <= 0 || !rest || !tets || !disp) return -1;
+  Mesh M;
+  buildMesh(M, nv, nt, rest, tets);
+  const MaterialParams mat = makeMaterial(material, mu, lambda);
+#pragma omp parallel for schedule(static)
+  for (int t = 0; t < nt; t++) {
+    double f[9], U[9], S[3], V[9], fl[12], H[144];
+    elementTerms(M, mat, disp, t, f, U, S, V, fl, H);
+    if (F) std::memcpy(F + 9 * (size_t)t, f, sizeof(f));
+    if (Sigma) std::memcpy(Sigma + 3 * (size_t)t, S, sizeof(S));
+    if (psiOut) psiOut[t] = psi(mat, f);
+    if (P) PK1(mat, f, P + 9 * (size_t)t);
+    if (H9) clampedHessian(mat, U, S, V, H9 + 81 * (size_t)t);
+    if (fe) std::memcpy(fe + 12 * (size_t)t, fl, sizeof(fl));
+    if (He) std::memcpy(He + 144 * (size_t)t, H, sizeof(H));
+  }
+  return 0;
+}
+
+// Rotation-variant SVD of n matrices (column major).
+int oracle_svd(int n, const double* F, double* U, double* S, double* V) {
+  for (int k = 0; k < n; k++) svd_rv(F + 9 * (size_t)k, U + 9 * (size_t)k, S + 3 * (size_t)k, V + 9 * (size_t)k);
+  return 0;
+}
+
+void* oracle_create(int nv, int nt, const double* rest, const int* tets, int material, double mu, double lambda,
+                    double density, const double* gravity, double dt) {
+  if (nv <= 0 || nt <= 0 || !rest || !tets) return nullptr;
+  Sim* s = new Sim;
+  buildMesh(s->M, nv, nt, rest, tets);
+  s->mat = makeMaterial(material, mu, lambda);
+  s->density = density;
+  s->dt = dt;
+  for (int i = 0; i < 3; i++) s->gravity[i] = gravity ? gravity[i] : 0.0;
+  s->x.assign(3 * (size_t)nv, 0.0);
+  s->v.assign(3 * (size_t)nv, 0.0);
+  s->free.assign(nv, 1);
+  // externalForces = oneRingVolume * density * g (TIMESTEPPER.cpp:334-345)
+  s->fext.resize(3 * (size_t)nv);
+  for (int u = 0; u < nv; u++)
+    for (int i = 0; i < 3; i++) s->fext[3 * u + i] = s->M.oneRing[u] * (density * s->gravity[i]);
+  return s;
+}
+
+void oracle_destroy(void* h) { delete static_cast<Sim*>(h); }
+
+int oracle_set_state(void* h, const double* x, const double* v) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  const size_t n = 3 * (size_t)s->M.nv;
+  if (x) s->x.assign(x, x + n);
+  if (v) s->v.assign(v, v + n);
+  return 0;
+}
+
+int oracle_get_state(void* h, double* x, double* v) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  if (x) std::copy(s->x.begin(), s->x.end(), x);
+  if (v) std::copy(s->v.begin(), s->v.end(), v);
+  return 0;
+}
+
+// Pin vertices at their current world position (attachKinematicConstraints,
+// TIMESTEPPER.cpp:380-403): target displacement = (rest + x) - rest.
+int oracle_attach_pins(void* h, int n, const int* ids) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  for (int k = 0; k < n; k++) {
+    const int u = ids[k];
+    if (u < 0 || u >= s->M.nv) return -2;
+    s->pinned.push_back(u);
+    for (int i = 0; i < 3; i++) {
+      const double world = s->M.rest[3 * u + i] + s->x[3 * u + i];
+      s->pinTarget.push_back(world - s->M.rest[3 * u + i]);
+    }
+    s->free[u] = 0;
+  }
+  return 0;
+}
+
+int oracle_set_solver(void* h, double tol, int maxit, int precond) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  s->tol = tol;
+  s->maxit = maxit;
+  s->precond = precond;
+  return 0;
+}
+
+int oracle_set_external_forces(void* h, const double* f) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s || !f) return -1;
+  s->fext.assign(f, f + 3 * (size_t)s->M.nv);
+  return 0;
+}
+
+int oracle_step(void* h, int nsteps, int* iters, double* errs) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  for (int k = 0; k < nsteps; k++) {
+    step(*s);
+    if (iters) iters[k] = s->lastIters;
+    if (errs) errs[k] = s->lastErr;
+  }
+  return 0;
+}
+
+int oracle_nblocks(void* h) { return static_cast<Sim*>(h)->M.rowptr.back(); }
+
+// BSR pattern (rowptr V+1, cols nblocks) and, at the current displacement,
+// the assembled stiffness K (9 per block, column major) and forces R (3V).
+int oracle_assemble(void* h, int* rowptr, int* cols, double* K, double* R) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  if (rowptr) std::copy(s->M.rowptr.begin(), s->M.rowptr.end(), rowptr);
+  if (cols) std::copy(s->M.cols.begin(), s->M.cols.end(), cols);
+  if (K || R) {
+    assemble(*s);
+    if (K) std::copy(s->K.begin(), s->K.end(), K);
+    if (R) std::copy(s->R.begin(), s->R.end(), R);
+  }
+  return 0;
+}
+
+double oracle_energy(void* h) {
+  Sim* s = static_cast<Sim*>(h);
+  double e = 0;
+  for (int t = 0; t < s->M.nt; t++) {
+    double F[9], U[9], S[3], V[9];
+    elementTerms(s->M, s->mat, s->x.data(), t, F, U, S, V, nullptr, nullptr);
+    e += s->M.vol[t] * psi(s->mat, F);
+  }
+  return e;
+}
+
+int oracle_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

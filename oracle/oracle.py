@@ -1,0 +1,155 @@
+"""ctypes wrapper of the CPU oracle (oracle/hobak_oracle.cpp).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, as the checker or the timed CPU baseline.  The
+product library (hobakv1_gb300) never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libhobak_oracle.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lib = None
+
+MATERIALS = {"snh": 0, "arap": 1, "stvk": 2, "linear": 3, "neo_hookean_bw": 4, "snh_barrier": 5}
+
+
+def build(quiet: bool = True) -> str:
+    """Compile the oracle with make (portable flags; works on x86 and aarch64)."""
+    subprocess.run(["make", "-C", HERE, "-s"], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.oracle_elements.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oracle_svd.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp]
+        L.oracle_create.restype = ctypes.c_void_p
+        L.oracle_create.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _ip, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_double, _dp, ctypes.c_double]
+        L.oracle_destroy.argtypes = [ctypes.c_void_p]
+        L.oracle_set_state.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.oracle_get_state.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.oracle_attach_pins.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip]
+        L.oracle_set_solver.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.oracle_set_external_forces.argtypes = [ctypes.c_void_p, _dp]
+        L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp]
+        L.oracle_nblocks.argtypes = [ctypes.c_void_p]
+        L.oracle_assemble.argtypes = [ctypes.c_void_p, _ip, _ip, _dp, _dp]
+        L.oracle_energy.argtypes = [ctypes.c_void_p]
+        L.oracle_energy.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def elements(rest, tets, x, material, mu, lam):
+    rest = np.ascontiguousarray(rest, dtype=np.float64)
+    tets = np.ascontiguousarray(tets, dtype=np.int32)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    nv, nt = rest.shape[0], tets.shape[0]
+    out = {k: np.zeros((nt, n)) for k, n in
+           [("F", 9), ("Sigma", 3), ("P", 9), ("H9", 81), ("fe", 12), ("He", 144)]}
+    out["psi"] = np.zeros(nt)
+    rc = lib().oracle_elements(nv, nt, _d(rest), _i(tets), _d(x), MATERIALS[material], mu, lam,
+                               _d(out["F"]), _d(out["Sigma"]), _d(out["psi"]), _d(out["P"]),
+                               _d(out["H9"]), _d(out["fe"]), _d(out["He"]))
+    assert rc == 0
+    return out
+
+
+def svd(F):
+    F = np.ascontiguousarray(F, dtype=np.float64).reshape(-1, 9)
+    n = F.shape[0]
+    U, S, V = np.zeros((n, 9)), np.zeros((n, 3)), np.zeros((n, 9))
+    lib().oracle_svd(n, _d(F), _d(U), _d(S), _d(V))
+    return U, S, V
+
+
+class Sim:
+    """CPU oracle BACKWARD_EULER_VELOCITY on one scene (collisions off)."""
+
+    def __init__(self, scene, tol=1e-8, maxit=1000, precond=0):
+        L = lib()
+        self.scene = scene
+        self._rest = np.ascontiguousarray(scene.rest, dtype=np.float64)
+        self._tets = np.ascontiguousarray(scene.tets, dtype=np.int32)
+        g = np.array(scene.gravity, dtype=np.float64)
+        self.h = L.oracle_create(scene.nv, scene.nt, _d(self._rest), _i(self._tets),
+                                 MATERIALS[scene.material], scene.mu, scene.lam, scene.density,
+                                 _d(g), scene.dt)
+        assert self.h
+        x0 = np.ascontiguousarray(scene.x0.reshape(-1), dtype=np.float64)
+        v0 = np.ascontiguousarray(scene.v0.reshape(-1), dtype=np.float64)
+        L.oracle_set_state(self.h, _d(x0), _d(v0))
+        pins = np.ascontiguousarray(scene.pinned, dtype=np.int32)
+        assert L.oracle_attach_pins(self.h, len(pins), _i(pins)) == 0
+        L.oracle_set_solver(self.h, tol, maxit, precond)
+
+    def step(self, n=1):
+        iters = np.zeros(n, dtype=np.int32)
+        errs = np.zeros(n)
+        assert lib().oracle_step(self.h, n, _i(iters), _d(errs)) == 0
+        return iters, errs
+
+    def state(self):
+        x = np.zeros(3 * self.scene.nv)
+        v = np.zeros(3 * self.scene.nv)
+        lib().oracle_get_state(self.h, _d(x), _d(v))
+        return x, v
+
+    def assemble(self):
+        nb = lib().oracle_nblocks(self.h)
+        rowptr = np.zeros(self.scene.nv + 1, dtype=np.int32)
+        cols = np.zeros(nb, dtype=np.int32)
+        K = np.zeros(9 * nb)
+        R = np.zeros(3 * self.scene.nv)
+        lib().oracle_assemble(self.h, _i(rowptr), _i(cols), _d(K), _d(R))
+        return rowptr, cols, K.reshape(nb, 9), R
+
+    def energy(self):
+        return lib().oracle_energy(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_destroy(self.h)
+            self.h = None
+
+
+def bsr_to_dense(rowptr, cols, blocks, nv):
+    """Dense 3V x 3V matrix from BSR (blocks column major)."""
+    A = np.zeros((3 * nv, 3 * nv))
+    for u in range(nv):
+        for k in range(rowptr[u], rowptr[u + 1]):
+            w = cols[k]
+            A[3 * u:3 * u + 3, 3 * w:3 * w + 3] = blocks[k].reshape(3, 3, order="F")
+    return A
+
+
+def csc_to_dense(colptr, rowidx, values, n):
+    A = np.zeros((n, n))
+    for c in range(n):
+        for k in range(colptr[c], colptr[c + 1]):
+            A[rowidx[k], c] = values[k]
+    return A

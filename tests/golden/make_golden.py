@@ -1,0 +1,72 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs the UNMODIFIED reference (HOBAK) through the harness built by
+oracle/ref/Makefile (binary oracle/_ref/hobak_ref; needs the reference sources,
+so this only runs where they are).  Inputs come from hobakv1_gb300.scenes, so
+they are regenerated bit-identically anywhere.  Usage:
+
+    make -C oracle/ref REF=<reference checkout> -j8
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from hobakv1_gb300 import scenes  # noqa: E402
+from oracle import refrun  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def element_states(N):
+    """Named displacement fields on the N^3 Kuhn cube: rest (F = I up to
+    jitter), compressed+twisted, and a seeded large perturbation that inverts
+    some tets."""
+    rest, tets = scenes.kuhn_cube(N)
+    h = 1.0 / N
+    twisted = scenes.compress_and_twist(rest, N) - rest
+    rng = np.random.default_rng(scenes.BASE_SEED + 77)
+    wild = rng.uniform(-0.6 * h, 0.6 * h, size=rest.shape)
+    return rest, tets, {"rest": np.zeros_like(rest), "twist": twisted, "wild": wild}
+
+
+def make_elements():
+    for mat in scenes.MATERIALS:
+        N = 3 if mat in ("snh", "arap") else 2
+        rest, tets, states = element_states(N)
+        mu, lam = scenes.lame(1e4, 0.45)
+        for name, x in states.items():
+            if mat == "neo_hookean_bw" and name == "wild":
+                continue  # log(J) of inverted tets is undefined for this energy
+            r = refrun.elements(rest, tets, x, mat, mu, lam)
+            np.savez_compressed(os.path.join(OUT, f"elements_{mat}_{name}.npz"),
+                                rest=rest, tets=tets, x=x, mu=mu, lam=lam,
+                                **{k: r[k] for k in ["F", "Sigma", "psi", "P", "H9", "fe", "He", "R",
+                                                     "K_colptr", "K_rowidx", "K_values", "energy",
+                                                     "restVolume", "oneRingVolume"]})
+            print("elements", mat, name, len(tets))
+
+
+def make_trajectories():
+    cases = [(scenes.config1_scene(10), 100, 25),
+             (scenes.config2_scene(6, "snh"), 100, 25),
+             (scenes.config2_scene(6, "arap"), 100, 25)]
+    for s, steps, stride in cases:
+        r = refrun.run(s, steps, stride=stride)
+        np.savez_compressed(os.path.join(OUT, f"traj_{s.name}.npz"), x=r["x"], v=r["v"],
+                            iters=r["iters"], cg_error=r["cg_error"], energy=r["energy"],
+                            steps=steps, stride=stride)
+        print("trajectory", s.name, r["iters"].sum())
+
+
+if __name__ == "__main__":
+    if not refrun.available():
+        sys.exit("reference build missing: make -C oracle/ref REF=<reference checkout>")
+    make_elements()
+    make_trajectories()

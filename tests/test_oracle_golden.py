@@ -1,0 +1,86 @@
+"""Pins the CPU oracle against golden vectors produced by the reference build
+(tests/golden/make_golden.py).  CPU only."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from hobakv1_gb300 import scenes
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def relmax(a, b, floor=1e-300):
+    """max |a - b| over max(max |b|, floor): relative error with an absolute
+    floor for quantities that vanish (stress and energy at rest)."""
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), floor))
+
+
+def natural_floors(g):
+    """Scales below which a stress/energy/force is roundoff: mu for psi and P,
+    mu * (tet size)^2 for element forces."""
+    mu = float(g["mu"])
+    area = float(np.mean(g["restVolume"])) ** (2.0 / 3.0)
+    return {"psi": mu, "P": mu, "fe": mu * area, "R": mu * area}
+
+
+ELEMENT_FILES = sorted(glob.glob(os.path.join(GOLDEN, "elements_*.npz")))
+
+
+@pytest.mark.parametrize("path", ELEMENT_FILES, ids=[os.path.basename(p)[9:-4] for p in ELEMENT_FILES])
+def test_oracle_elements_match_reference(path):
+    g = np.load(path)
+    mat = os.path.basename(path)[len("elements_"):].rsplit("_", 1)[0]
+    o = oracle.elements(g["rest"], g["tets"], g["x"], mat, float(g["mu"]), float(g["lam"]))
+    # per-element forces and Hessians within 1e-10 relative (FP64)
+    floors = natural_floors(g)
+    for k in ["F", "psi", "P", "H9", "fe", "He"]:
+        err = relmax(o[k], g[k], floors.get(k, 1e-300))
+        assert err < 1e-10, (k, err)
+    # singular values with the svd_rv sign convention
+    assert relmax(o["Sigma"], g["Sigma"]) < 1e-10
+
+
+@pytest.mark.parametrize("path", ELEMENT_FILES[:3], ids=lambda p: os.path.basename(p))
+def test_oracle_assembly_matches_reference_csc(path):
+    g = np.load(path)
+    mat = os.path.basename(path)[len("elements_"):].rsplit("_", 1)[0]
+    s = scenes.Scene("g", g["rest"], g["tets"], mat, float(g["mu"]), float(g["lam"]),
+                     np.zeros(0, np.int32), g["x"].reshape(-1, 3), np.zeros_like(g["x"]).reshape(-1, 3))
+    sim = oracle.Sim(s)
+    rowptr, cols, K, R = sim.assemble()
+    nv = s.nv
+    # sparsity: the scalar CSC pattern implied by the 3x3 blocks is bit-exact
+    A = oracle.bsr_to_dense(rowptr, cols, K, nv)
+    pattern = np.zeros((3 * nv, 3 * nv), bool)
+    for u in range(nv):
+        for k in range(rowptr[u], rowptr[u + 1]):
+            w = cols[k]
+            pattern[3 * u:3 * u + 3, 3 * w:3 * w + 3] = True
+    ref_pattern = np.zeros_like(pattern)
+    cp, ri = g["K_colptr"], g["K_rowidx"]
+    for c in range(3 * nv):
+        ref_pattern[ri[cp[c]:cp[c + 1]], c] = True
+    assert np.array_equal(pattern, ref_pattern)
+    Kref = oracle.csc_to_dense(cp, ri, g["K_values"], 3 * nv)
+    assert relmax(A, Kref) < 1e-10
+    assert relmax(R, g["R"], natural_floors(g)["R"]) < 1e-10
+
+
+@pytest.mark.parametrize("name,scene_fn", [
+    ("kuhn10_snh", lambda: scenes.config1_scene(10)),
+    ("kuhn6_snh_twist", lambda: scenes.config2_scene(6, "snh")),
+    ("kuhn6_arap_twist", lambda: scenes.config2_scene(6, "arap")),
+])
+def test_oracle_trajectory_matches_reference(name, scene_fn):
+    g = np.load(os.path.join(GOLDEN, f"traj_{name}.npz"))
+    s = scene_fn()
+    sim = oracle.Sim(s)
+    stride = int(g["stride"])
+    for k in range(1, g["x"].shape[0]):
+        sim.step(stride)
+        x, v = sim.state()
+        err = np.linalg.norm(x - g["x"][k]) / np.linalg.norm(g["x"][k])
+        assert err < 1e-8, (k, err)
