@@ -1,0 +1,112 @@
+"""Loads libhobak_gpu.so (the sm_103a CUDA library) and declares its C ABI.
+
+There is no CPU fallback: if the library is missing or cannot find a GB300,
+every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class HobakMaterial(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("mu", ctypes.c_double), ("lambda_", ctypes.c_double)]
+
+
+class HobakSceneDesc(ctypes.Structure):
+    _fields_ = [("nv", ctypes.c_int), ("nt", ctypes.c_int), ("rest", _dp), ("tets", _ip),
+                ("material", HobakMaterial), ("density", ctypes.c_double),
+                ("gravity", ctypes.c_double * 3), ("dt", ctypes.c_double),
+                ("npinned", ctypes.c_int), ("pinned", _ip), ("x0", _dp), ("v0", _dp)]
+
+
+class HobakSolverOpts(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("max_iters", ctypes.c_int), ("precision", ctypes.c_int),
+                ("preconditioner", ctypes.c_int), ("max_refinements", ctypes.c_int),
+                ("use_graph", ctypes.c_int)]
+
+
+class HobakStepStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int),
+                ("rel_residual", ctypes.c_double), ("refinements", ctypes.c_int)]
+
+
+# name -> (restype, argtypes); mirrors include/hobak_gpu.h
+SIGNATURES = {
+    "hobak_version": (ctypes.c_char_p, []),
+    "hobak_last_error": (ctypes.c_char_p, []),
+    "hobak_device_check": (ctypes.c_int, [_ip, _ip, _ip]),
+    "hobak_default_solver_opts": (None, [ctypes.POINTER(HobakSolverOpts)]),
+    "hobak_batch_create": (ctypes.c_int, [ctypes.POINTER(HobakSceneDesc), ctypes.c_int,
+                                          ctypes.POINTER(HobakSolverOpts), ctypes.POINTER(ctypes.c_void_p)]),
+    "hobak_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "hobak_batch_num_scenes": (ctypes.c_int, [ctypes.c_void_p, _ip]),
+    "hobak_batch_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(HobakStepStats)]),
+    "hobak_batch_set_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
+    "hobak_batch_get_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
+    "hobak_batch_set_external_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    "hobak_batch_set_solver": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakSolverOpts)]),
+    "hobak_batch_device_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "hobak_batch_energy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    "hobak_gpu_create": (ctypes.c_int, [ctypes.POINTER(HobakSceneDesc), ctypes.POINTER(HobakSolverOpts),
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "hobak_gpu_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(HobakStepStats)]),
+    "hobak_gpu_set_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    "hobak_gpu_get_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    "hobak_gpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "hobak_material_eval": (ctypes.c_int, [ctypes.POINTER(HobakMaterial), ctypes.c_int, _dp, _dp, _dp, _dp]),
+    "hobak_element_eval": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp,
+                                          ctypes.POINTER(HobakMaterial), _dp, _dp, _dp, _dp]),
+    "hobak_batch_assemble": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _ip, _dp, _dp]),
+}
+
+_lib = None
+
+
+class HobakError(RuntimeError):
+    def __init__(self, code, where, msg):
+        super().__init__(f"{where} failed with status {code}: {msg}")
+        self.code = code
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the CUDA library (building it with nvcc if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing; build it with hobakv1_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc: int, where: str) -> int:
+    """Raise on a negative status; return warnings (positive) to the caller."""
+    if rc < 0:
+        raise HobakError(rc, where, load().hobak_last_error().decode())
+    return rc
+
+
+def dptr(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def iptr(a):
+    return a.ctypes.data_as(_ip) if a is not None else None

@@ -1,0 +1,763 @@
+// Host side of the C ABI (include/hobak_gpu.h): batch set-up (rest-shape
+// precompute, block sparsity, element->block maps, tiles), device memory, the
+// step driver and the element-level entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/hobak_gpu.h"
+#include "element_math.cuh"
+#include "kernels.cuh"
+
+using namespace hobak;
+
+namespace {
+
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg) {
+  g_lastError = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                          \
+  do {                                                                                          \
+    cudaError_t _e = (expr);                                                                    \
+    if (_e != cudaSuccess)                                                                      \
+      return fail(_e == cudaErrorMemoryAllocation ? HOBAK_ERR_NO_MEMORY : HOBAK_ERR_CUDA,       \
+                  std::string(#expr) + ": " + cudaGetErrorString(_e));                          \
+  } while (0)
+
+// One device allocation carved into aligned sub-buffers.
+struct Arena {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  std::vector<std::pair<size_t, size_t>> plan;  // (offset, bytes)
+  size_t reserve(size_t bytes) {
+    used = (used + 255) & ~size_t(255);
+    const size_t off = used;
+    used += bytes;
+    return off;
+  }
+};
+
+struct SceneHost {
+  int nv, nt;
+  int v0, t0, b0, tile0, ntiles;
+  hobak_material mat;
+  double density, dt;
+  double gravity[3];
+};
+
+}  // namespace
+
+struct hobak_batch_t {
+  std::vector<SceneHost> scenes;
+  hobak_solver_opts opts{};
+  int nv = 0, nt = 0, nblocks = 0, ntiles = 0;
+  std::vector<double> oneRing;   // per vertex
+  std::vector<unsigned char> freeMask;
+  std::vector<int> tetsHost;     // global ids
+  DeviceBatch d{};
+  void* arena = nullptr;
+  size_t arenaBytes = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t chunkGraph = nullptr;
+  int chunkIters = 0;
+  int lastStatus = HOBAK_OK;
+  std::vector<SolveState> lastSolve;
+  std::vector<int> hostRowptr, hostCols;
+};
+
+namespace {
+
+constexpr int kChunk = 16;  // PCG iterations between host convergence checks (even)
+
+double tet_volume(const double* x0, const double* x1, const double* x2, const double* x3) {
+  const double d1[3] = {x1[0] - x0[0], x1[1] - x0[1], x1[2] - x0[2]};
+  const double d2[3] = {x2[0] - x0[0], x2[1] - x0[1], x2[2] - x0[2]};
+  const double d3[3] = {x3[0] - x0[0], x3[1] - x0[1], x3[2] - x0[2]};
+  const double c[3] = {d1[1] * d2[2] - d1[2] * d2[1], d1[2] * d2[0] - d1[0] * d2[2], d1[0] * d2[1] - d1[1] * d2[0]};
+  return (d3[0] * c[0] + d3[1] * c[1] + d3[2] * c[2]) / 6.0;
+}
+
+// DmInv by cofactors (TET_MESH.cpp:178-191 inverts Dm with Eigen).
+void dm_inverse(const double* x0, const double* x1, const double* x2, const double* x3, double* Ai) {
+  double A[9];
+  for (int i = 0; i < 3; i++) {
+    A[i] = x1[i] - x0[i];
+    A[3 + i] = x2[i] - x0[i];
+    A[6 + i] = x3[i] - x0[i];
+  }
+  const double det = A[0] * (A[4] * A[8] - A[7] * A[5]) - A[3] * (A[1] * A[8] - A[7] * A[2]) +
+                     A[6] * (A[1] * A[5] - A[4] * A[2]);
+  const double id = 1.0 / det;
+  Ai[0] = (A[4] * A[8] - A[5] * A[7]) * id;
+  Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  Ai[3] = (A[5] * A[6] - A[3] * A[8]) * id;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+  Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  Ai[6] = (A[3] * A[7] - A[4] * A[6]) * id;
+  Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+}
+
+int validate_scene(const hobak_scene_desc& s, int idx) {
+  char buf[160];
+  if (s.nv <= 0 || s.nt <= 0 || !s.rest || !s.tets) {
+    std::snprintf(buf, sizeof(buf), "scene %d: empty mesh or null rest/tets", idx);
+    return fail(HOBAK_ERR_INVALID, buf);
+  }
+  if (s.material.kind < 0 || s.material.kind > 5) {
+    std::snprintf(buf, sizeof(buf), "scene %d: unknown material kind %d", idx, s.material.kind);
+    return fail(HOBAK_ERR_INVALID, buf);
+  }
+  if (!(s.dt > 0.0) || !(s.density > 0.0)) {
+    std::snprintf(buf, sizeof(buf), "scene %d: dt and density must be positive", idx);
+    return fail(HOBAK_ERR_INVALID, buf);
+  }
+  if (s.npinned < 0 || (s.npinned > 0 && !s.pinned)) {
+    std::snprintf(buf, sizeof(buf), "scene %d: bad pin list", idx);
+    return fail(HOBAK_ERR_INVALID, buf);
+  }
+  for (long k = 0; k < 4L * s.nt; k++)
+    if (s.tets[k] < 0 || s.tets[k] >= s.nv) {
+      std::snprintf(buf, sizeof(buf), "scene %d: tet vertex id out of range at %ld", idx, k);
+      return fail(HOBAK_ERR_INVALID, buf);
+    }
+  for (int k = 0; k < s.npinned; k++)
+    if (s.pinned[k] < 0 || s.pinned[k] >= s.nv) {
+      std::snprintf(buf, sizeof(buf), "scene %d: pinned id out of range", idx);
+      return fail(HOBAK_ERR_INVALID, buf);
+    }
+  return HOBAK_OK;
+}
+
+template <typename T>
+T* carve(void* base, size_t off) {
+  return reinterpret_cast<T*>(static_cast<char*>(base) + off);
+}
+
+int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
+  // ---- host precompute ----
+  std::vector<int> vtxptr, vtxinc, rowptr, cols, blkRow, blkptr, blksrc, tileScene, tileV0, tileV1;
+  std::vector<int> tetScene, vertexScene;
+  std::vector<double> rest, x, v, fext, mass, pinTarget, DmInv, vol;
+  std::vector<SceneParams> sparams;
+  B->scenes.resize(n);
+  int nv = 0, nt = 0;
+  for (int s = 0; s < n; s++) {
+    B->scenes[s].v0 = nv;
+    B->scenes[s].t0 = nt;
+    nv += descs[s].nv;
+    nt += descs[s].nt;
+  }
+  B->nv = nv;
+  B->nt = nt;
+  rest.resize(3 * (size_t)nv);
+  x.assign(3 * (size_t)nv, 0.0);
+  v.assign(3 * (size_t)nv, 0.0);
+  fext.resize(3 * (size_t)nv);
+  mass.resize(nv);
+  pinTarget.assign(3 * (size_t)nv, 0.0);
+  B->freeMask.assign(nv, 1);
+  B->oneRing.assign(nv, 0.0);
+  vertexScene.resize(nv);
+  B->tetsHost.resize(4 * (size_t)nt);
+  tetScene.resize(nt);
+  DmInv.resize(9 * (size_t)nt);
+  vol.resize(nt);
+  vtxptr.assign(nv + 1, 0);
+  rowptr.assign(nv + 1, 0);
+
+  for (int s = 0; s < n; s++) {
+    const hobak_scene_desc& D = descs[s];
+    SceneHost& H = B->scenes[s];
+    H.nv = D.nv;
+    H.nt = D.nt;
+    H.mat = D.material;
+    H.density = D.density;
+    H.dt = D.dt;
+    for (int i = 0; i < 3; i++) H.gravity[i] = D.gravity[i];
+    const int v0 = H.v0, t0 = H.t0;
+    std::memcpy(&rest[3 * (size_t)v0], D.rest, 3 * sizeof(double) * D.nv);
+    if (D.x0) std::memcpy(&x[3 * (size_t)v0], D.x0, 3 * sizeof(double) * D.nv);
+    if (D.v0) std::memcpy(&v[3 * (size_t)v0], D.v0, 3 * sizeof(double) * D.nv);
+    for (int u = 0; u < D.nv; u++) vertexScene[v0 + u] = s;
+    // per-tet rest data (TET_MESH.cpp:121-191)
+    for (int t = 0; t < D.nt; t++) {
+      const int* tv = D.tets + 4 * (size_t)t;
+      const double* p[4];
+      for (int a = 0; a < 4; a++) {
+        B->tetsHost[4 * (size_t)(t0 + t) + a] = v0 + tv[a];
+        p[a] = D.rest + 3 * (size_t)tv[a];
+      }
+      vol[t0 + t] = tet_volume(p[0], p[1], p[2], p[3]);
+      if (!(vol[t0 + t] > 0.0)) {
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "scene %d: tet %d has non-positive rest volume", s, t);
+        return fail(HOBAK_ERR_INVALID, buf);
+      }
+      dm_inverse(p[0], p[1], p[2], p[3], &DmInv[9 * (size_t)(t0 + t)]);
+      tetScene[t0 + t] = s;
+    }
+    // one-ring volumes: quarter of each incident tet, in tet order (TET_MESH.cpp:156-173)
+    for (int t = 0; t < D.nt; t++) {
+      const double q = 0.25 * vol[t0 + t];
+      for (int a = 0; a < 4; a++) B->oneRing[v0 + D.tets[4 * (size_t)t + a]] += q;
+    }
+    for (int u = 0; u < D.nv; u++) {
+      const double orv = B->oneRing[v0 + u];
+      mass[v0 + u] = orv * D.density;  // scaleMass(density) (TIMESTEPPER.h:100)
+      for (int i = 0; i < 3; i++)  // addGravity(density * g) (TIMESTEPPER.cpp:334-345)
+        fext[3 * (size_t)(v0 + u) + i] = orv * (D.density * D.gravity[i]);
+    }
+    // pins keep the displacement they have when attached: (rest + x) - rest
+    for (int k = 0; k < D.npinned; k++) {
+      const int u = v0 + D.pinned[k];
+      B->freeMask[u] = 0;
+      for (int i = 0; i < 3; i++) {
+        const double world = rest[3 * (size_t)u + i] + x[3 * (size_t)u + i];
+        pinTarget[3 * (size_t)u + i] = world - rest[3 * (size_t)u + i];
+      }
+    }
+  }
+  // vertex -> (tet, a) incidences, ascending tet
+  for (long k = 0; k < 4L * nt; k++) vtxptr[B->tetsHost[k] + 1]++;
+  for (int u = 0; u < nv; u++) vtxptr[u + 1] += vtxptr[u];
+  vtxinc.resize(4 * (size_t)nt);
+  {
+    std::vector<int> fill(vtxptr.begin(), vtxptr.end() - 1);
+    for (int t = 0; t < nt; t++)
+      for (int a = 0; a < 4; a++) vtxinc[fill[B->tetsHost[4 * (size_t)t + a]]++] = 4 * t + a;
+  }
+  // block rows: sorted unique neighbours through shared tets
+  {
+    std::vector<int> nb;
+    for (int u = 0; u < nv; u++) {
+      nb.clear();
+      for (int k = vtxptr[u]; k < vtxptr[u + 1]; k++) {
+        const int t = vtxinc[k] >> 2;
+        for (int a = 0; a < 4; a++) nb.push_back(B->tetsHost[4 * (size_t)t + a]);
+      }
+      std::sort(nb.begin(), nb.end());
+      nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+      rowptr[u + 1] = rowptr[u] + (int)nb.size();
+      cols.insert(cols.end(), nb.begin(), nb.end());
+    }
+  }
+  const int nblocks = rowptr[nv];
+  B->nblocks = nblocks;
+  blkRow.resize(nblocks);
+  for (int u = 0; u < nv; u++)
+    for (int k = rowptr[u]; k < rowptr[u + 1]; k++) blkRow[k] = u;
+  // block <- (tet, a, b) contributions in ascending tet order
+  {
+    std::vector<int> where(16 * (size_t)nt);
+    blkptr.assign(nblocks + 1, 0);
+    for (int t = 0; t < nt; t++)
+      for (int a = 0; a < 4; a++)
+        for (int bb = 0; bb < 4; bb++) {
+          const int u = B->tetsHost[4 * (size_t)t + a], w = B->tetsHost[4 * (size_t)t + bb];
+          const int* beg = cols.data() + rowptr[u];
+          const int* end = cols.data() + rowptr[u + 1];
+          const int k = rowptr[u] + int(std::lower_bound(beg, end, w) - beg);
+          where[16 * (size_t)t + 4 * a + bb] = k;
+          blkptr[k + 1]++;
+        }
+    for (int k = 0; k < nblocks; k++) blkptr[k + 1] += blkptr[k];
+    blksrc.resize(16 * (size_t)nt);
+    std::vector<int> fill(blkptr.begin(), blkptr.end() - 1);
+    for (int t = 0; t < nt; t++)
+      for (int e = 0; e < 16; e++) blksrc[fill[where[16 * (size_t)t + e]]++] = 16 * t + e;
+  }
+  // tiles: kTileV consecutive vertices of one scene
+  for (int s = 0; s < n; s++) {
+    SceneHost& H = B->scenes[s];
+    H.tile0 = (int)tileScene.size();
+    for (int u = 0; u < H.nv; u += kTileV) {
+      tileScene.push_back(s);
+      tileV0.push_back(H.v0 + u);
+      tileV1.push_back(H.v0 + std::min(H.nv, u + kTileV));
+    }
+    H.ntiles = (int)tileScene.size() - H.tile0;
+    H.b0 = rowptr[H.v0];
+    const MatParams mp = make_material(H.mat.kind, H.mat.mu, H.mat.lambda);
+    SceneParams p{};
+    p.v0 = H.v0;
+    p.nv = H.nv;
+    p.t0 = H.t0;
+    p.nt = H.nt;
+    p.tile0 = H.tile0;
+    p.ntiles = H.ntiles;
+    p.kind = mp.kind;
+    p.mu = mp.mu;
+    p.lambda = mp.lambda;
+    p.alpha = mp.alpha;
+    p.dt = H.dt;
+    sparams.push_back(p);
+  }
+  const int ntiles = (int)tileScene.size();
+  B->ntiles = ntiles;
+
+  // ---- device arena ----
+  Arena A;
+  const size_t V3 = 3 * (size_t)nv * sizeof(double);
+  struct Slot {
+    size_t off;
+  };
+  const size_t oScenes = A.reserve(sizeof(SceneParams) * n);
+  const size_t oSolve = A.reserve(sizeof(SolveState) * n);
+  const size_t oActive = A.reserve(sizeof(int));
+  const size_t oRest = A.reserve(V3), oX = A.reserve(V3), oV = A.reserve(V3), oF = A.reserve(V3);
+  const size_t oMass = A.reserve(sizeof(double) * nv), oFree = A.reserve(nv), oPin = A.reserve(V3);
+  const size_t oVS = A.reserve(sizeof(int) * nv);
+  const size_t oTets = A.reserve(sizeof(int4) * nt), oDm = A.reserve(sizeof(double) * 9 * (size_t)nt);
+  const size_t oVol = A.reserve(sizeof(double) * nt), oTS = A.reserve(sizeof(int) * nt);
+  const size_t oRowptr = A.reserve(sizeof(int) * (nv + 1)), oCols = A.reserve(sizeof(int) * nblocks);
+  const size_t oBlkRow = A.reserve(sizeof(int) * nblocks), oBlkptr = A.reserve(sizeof(int) * (nblocks + 1));
+  const size_t oBlksrc = A.reserve(sizeof(int) * 16 * (size_t)nt);
+  const size_t oVtxptr = A.reserve(sizeof(int) * (nv + 1)), oVtxinc = A.reserve(sizeof(int) * 4 * (size_t)nt);
+  const size_t oTileS = A.reserve(sizeof(int) * ntiles), oTile0 = A.reserve(sizeof(int) * ntiles);
+  const size_t oTile1 = A.reserve(sizeof(int) * ntiles);
+  const size_t oEH = A.reserve(sizeof(double) * kElemHess * (size_t)nt);
+  const size_t oEG = A.reserve(sizeof(double) * 12 * (size_t)nt);
+  const size_t oLhs = A.reserve(sizeof(double) * 9 * (size_t)nblocks);
+  const size_t oMinv = A.reserve(sizeof(double) * 9 * (size_t)nv);
+  const size_t oRhs = A.reserve(V3), oY = A.reserve(V3), oR = A.reserve(V3), oZ = A.reserve(V3);
+  const size_t oP0 = A.reserve(V3), oP1 = A.reserve(V3), oAp = A.reserve(V3);
+  const size_t oPart = A.reserve(sizeof(double) * 2 * (size_t)ntiles);
+  const size_t oPsi = A.reserve(sizeof(double) * nt);
+  void* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, A.used);
+  if (e != cudaSuccess)
+    return fail(e == cudaErrorMemoryAllocation ? HOBAK_ERR_NO_MEMORY : HOBAK_ERR_CUDA,
+                std::string("cudaMalloc of batch arena: ") + cudaGetErrorString(e));
+  B->arena = base;
+  B->arenaBytes = A.used;
+  CUDA_TRY(cudaMemset(base, 0, A.used));
+
+  DeviceBatch& d = B->d;
+  d.nscenes = n;
+  d.nv = nv;
+  d.nt = nt;
+  d.nblocks = nblocks;
+  d.ntiles = ntiles;
+  d.scenes = carve<SceneParams>(base, oScenes);
+  d.solve = carve<SolveState>(base, oSolve);
+  d.active = carve<int>(base, oActive);
+  d.rest = carve<double>(base, oRest);
+  d.x = carve<double>(base, oX);
+  d.v = carve<double>(base, oV);
+  d.fext = carve<double>(base, oF);
+  d.mass = carve<double>(base, oMass);
+  d.freeMask = carve<unsigned char>(base, oFree);
+  d.pinTarget = carve<double>(base, oPin);
+  d.vertexScene = carve<int>(base, oVS);
+  d.tets = carve<int4>(base, oTets);
+  d.DmInv = carve<double>(base, oDm);
+  d.vol = carve<double>(base, oVol);
+  d.tetScene = carve<int>(base, oTS);
+  d.rowptr = carve<int>(base, oRowptr);
+  d.cols = carve<int>(base, oCols);
+  d.blkRow = carve<int>(base, oBlkRow);
+  d.blkptr = carve<int>(base, oBlkptr);
+  d.blksrc = carve<int>(base, oBlksrc);
+  d.vtxptr = carve<int>(base, oVtxptr);
+  d.vtxinc = carve<int>(base, oVtxinc);
+  d.tileScene = carve<int>(base, oTileS);
+  d.tileV0 = carve<int>(base, oTile0);
+  d.tileV1 = carve<int>(base, oTile1);
+  d.elemH = carve<double>(base, oEH);
+  d.elemG = carve<double>(base, oEG);
+  d.lhs = carve<double>(base, oLhs);
+  d.minv = carve<double>(base, oMinv);
+  d.rhs = carve<double>(base, oRhs);
+  d.y = carve<double>(base, oY);
+  d.r = carve<double>(base, oR);
+  d.z = carve<double>(base, oZ);
+  d.p0 = carve<double>(base, oP0);
+  d.p1 = carve<double>(base, oP1);
+  d.Ap = carve<double>(base, oAp);
+  d.partial = carve<double>(base, oPart);
+  d.psi = carve<double>(base, oPsi);
+
+  auto up = [&](const void* dst, const void* src, size_t bytes) {
+    return cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice);
+  };
+  CUDA_TRY(up(d.scenes, sparams.data(), sizeof(SceneParams) * n));
+  CUDA_TRY(up(d.rest, rest.data(), V3));
+  CUDA_TRY(up(d.x, x.data(), V3));
+  CUDA_TRY(up(d.v, v.data(), V3));
+  CUDA_TRY(up(d.fext, fext.data(), V3));
+  CUDA_TRY(up(d.mass, mass.data(), sizeof(double) * nv));
+  CUDA_TRY(up(d.freeMask, B->freeMask.data(), nv));
+  CUDA_TRY(up(d.pinTarget, pinTarget.data(), V3));
+  CUDA_TRY(up(d.vertexScene, vertexScene.data(), sizeof(int) * nv));
+  CUDA_TRY(up(d.tets, B->tetsHost.data(), sizeof(int4) * nt));
+  CUDA_TRY(up(d.DmInv, DmInv.data(), sizeof(double) * 9 * (size_t)nt));
+  CUDA_TRY(up(d.vol, vol.data(), sizeof(double) * nt));
+  CUDA_TRY(up(d.tetScene, tetScene.data(), sizeof(int) * nt));
+  CUDA_TRY(up(d.rowptr, rowptr.data(), sizeof(int) * (nv + 1)));
+  CUDA_TRY(up(d.cols, cols.data(), sizeof(int) * nblocks));
+  CUDA_TRY(up(d.blkRow, blkRow.data(), sizeof(int) * nblocks));
+  CUDA_TRY(up(d.blkptr, blkptr.data(), sizeof(int) * (nblocks + 1)));
+  CUDA_TRY(up(d.blksrc, blksrc.data(), sizeof(int) * 16 * (size_t)nt));
+  CUDA_TRY(up(d.vtxptr, vtxptr.data(), sizeof(int) * (nv + 1)));
+  CUDA_TRY(up(d.vtxinc, vtxinc.data(), sizeof(int) * 4 * (size_t)nt));
+  CUDA_TRY(up(d.tileScene, tileScene.data(), sizeof(int) * ntiles));
+  CUDA_TRY(up(d.tileV0, tileV0.data(), sizeof(int) * ntiles));
+  CUDA_TRY(up(d.tileV1, tileV1.data(), sizeof(int) * ntiles));
+  B->hostRowptr = rowptr;
+  B->hostCols = cols;
+  return HOBAK_OK;
+}
+
+int upload_solver_opts(hobak_batch_t* B) {
+  std::vector<SolveState> st(B->scenes.size());
+  for (auto& s : st) {
+    std::memset(&s, 0, sizeof(s));
+    s.tol = B->opts.tol;
+    s.maxit = B->opts.max_iters;
+  }
+  CUDA_TRY(cudaMemcpy(B->d.solve, st.data(), sizeof(SolveState) * st.size(), cudaMemcpyHostToDevice));
+  return HOBAK_OK;
+}
+
+int check_opts(const hobak_solver_opts* o) {
+  if (!o) return HOBAK_OK;
+  if (!(o->tol > 0.0) || o->max_iters <= 0) return fail(HOBAK_ERR_INVALID, "solver tol and max_iters must be > 0");
+  if (o->precision != HOBAK_PRECISION_FP64 && o->precision != HOBAK_PRECISION_MIXED)
+    return fail(HOBAK_ERR_INVALID, "unknown precision mode");
+  if (o->preconditioner != HOBAK_PRECOND_JACOBI && o->preconditioner != HOBAK_PRECOND_BLOCK_JACOBI)
+    return fail(HOBAK_ERR_INVALID, "unknown preconditioner");
+  if (o->max_refinements < 0 || o->max_refinements > 3) return fail(HOBAK_ERR_INVALID, "max_refinements in 0..3");
+  return HOBAK_OK;
+}
+
+// Capture kChunk PCG iterations (p ping-pong fixed) as one graph.
+int ensure_chunk_graph(hobak_batch_t* B) {
+  if (B->chunkGraph) return HOBAK_OK;
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+  for (int c = 0; c < kChunk; c += 2) {
+    launch_pcg_iteration(B->d, B->d.p0, B->d.p1, B->stream);
+    launch_pcg_iteration(B->d, B->d.p1, B->d.p0, B->stream);
+  }
+  CUDA_TRY(cudaStreamEndCapture(B->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&B->chunkGraph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(HOBAK_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return HOBAK_OK;
+}
+
+int run_step(hobak_batch_t* B) {
+  DeviceBatch& d = B->d;
+  cudaStream_t s = B->stream;
+  launch_begin_step(d, s);
+  launch_element(d, s);
+  launch_assemble(d, s);
+  launch_diag_inverse(d, B->opts.preconditioner, s);
+  const int n = (int)B->scenes.size();
+  CUDA_TRY(cudaMemcpyAsync(d.active, &n, sizeof(int), cudaMemcpyHostToDevice, s));
+  launch_pcg_init(d, s);
+  int h_active = n;
+  int iters = 0;
+  if (B->opts.use_graph) {
+    int rc = ensure_chunk_graph(B);
+    if (rc) return rc;
+  }
+  int* pinnedActive = nullptr;
+  CUDA_TRY(cudaMallocHost(&pinnedActive, sizeof(int)));
+  while (true) {
+    CUDA_TRY(cudaMemcpyAsync(pinnedActive, d.active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    h_active = *pinnedActive;
+    if (h_active <= 0 || iters >= B->opts.max_iters) break;
+    if (B->opts.use_graph) {
+      CUDA_TRY(cudaGraphLaunch(B->chunkGraph, s));
+    } else {
+      for (int c = 0; c < kChunk; c += 2) {
+        launch_pcg_iteration(d, d.p0, d.p1, s);
+        launch_pcg_iteration(d, d.p1, d.p0, s);
+      }
+    }
+    iters += kChunk;
+  }
+  cudaFreeHost(pinnedActive);
+  launch_finish_step(d, s);
+  CUDA_TRY(cudaGetLastError());
+  return HOBAK_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* hobak_version(void) { return "hobak-gb300 0.1 (sm_103a)"; }
+
+const char* hobak_last_error(void) { return g_lastError.c_str(); }
+
+int hobak_device_check(int* major, int* minor, int* sms) {
+  int dev = 0;
+  cudaDeviceProp p;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(HOBAK_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  e = cudaGetDeviceProperties(&p, dev);
+  if (e != cudaSuccess) return fail(HOBAK_ERR_NO_DEVICE, cudaGetErrorString(e));
+  if (major) *major = p.major;
+  if (minor) *minor = p.minor;
+  if (sms) *sms = p.multiProcessorCount;
+  if (p.major != 10) return fail(HOBAK_ERR_NO_DEVICE, "this build targets sm_103a (Blackwell Ultra) only");
+  return HOBAK_OK;
+}
+
+void hobak_default_solver_opts(hobak_solver_opts* o) {
+  if (!o) return;
+  o->tol = 1e-8;
+  o->max_iters = 1000;
+  o->precision = HOBAK_PRECISION_FP64;
+  o->preconditioner = HOBAK_PRECOND_BLOCK_JACOBI;
+  o->max_refinements = 3;
+  o->use_graph = 1;
+}
+
+int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_solver_opts* opts,
+                       hobak_batch* out) {
+  if (!out) return fail(HOBAK_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!scenes || nscenes <= 0) return fail(HOBAK_ERR_INVALID, "no scenes");
+  int rc = check_opts(opts);
+  if (rc) return rc;
+  for (int s = 0; s < nscenes; s++)
+    if ((rc = validate_scene(scenes[s], s))) return rc;
+  if ((rc = hobak_device_check(nullptr, nullptr, nullptr))) return rc;
+  std::unique_ptr<hobak_batch_t> B(new hobak_batch_t);
+  if (opts)
+    B->opts = *opts;
+  else
+    hobak_default_solver_opts(&B->opts);
+  CUDA_TRY(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+  if ((rc = build_batch(B.get(), scenes, nscenes))) {
+    hobak_batch_destroy(B.release());
+    return rc;
+  }
+  if ((rc = upload_solver_opts(B.get()))) {
+    hobak_batch_destroy(B.release());
+    return rc;
+  }
+  *out = B.release();
+  return HOBAK_OK;
+}
+
+int hobak_batch_destroy(hobak_batch b) {
+  if (!b) return HOBAK_OK;
+  if (b->chunkGraph) cudaGraphExecDestroy(b->chunkGraph);
+  if (b->arena) cudaFree(b->arena);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return HOBAK_OK;
+}
+
+int hobak_batch_num_scenes(hobak_batch b, int* n) {
+  if (!b || !n) return fail(HOBAK_ERR_INVALID, "null handle");
+  *n = (int)b->scenes.size();
+  return HOBAK_OK;
+}
+
+int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats) {
+  if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
+  if (nsteps < 0) return fail(HOBAK_ERR_INVALID, "nsteps < 0");
+  for (int k = 0; k < nsteps; k++) {
+    int rc = run_step(b);
+    if (rc) return rc;
+  }
+  const int n = (int)b->scenes.size();
+  b->lastSolve.resize(n);
+  CUDA_TRY(cudaMemcpyAsync(b->lastSolve.data(), b->d.solve, sizeof(SolveState) * n, cudaMemcpyDeviceToHost,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  int status = HOBAK_OK;
+  for (int s = 0; s < n; s++) {
+    const SolveState& st = b->lastSolve[s];
+    if (st.converged < 0) status = HOBAK_ERR_NAN;
+    else if (st.converged == 0 && status == HOBAK_OK) status = HOBAK_WARN_NOT_CONVERGED;
+    if (stats) {
+      stats[s].iterations = st.iters;
+      stats[s].converged = st.converged > 0 ? 1 : 0;
+      stats[s].rel_residual = st.rhsNorm2 > 0 ? std::sqrt(st.rr / st.rhsNorm2) : 0.0;
+      stats[s].refinements = st.refinements;
+    }
+  }
+  if (status == HOBAK_ERR_NAN) return fail(status, "non-finite residual in PCG");
+  return status;
+}
+
+int hobak_batch_set_state(hobak_batch b, int scene, const double* x, const double* v) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  const SceneHost& H = b->scenes[scene];
+  const size_t bytes = 3 * sizeof(double) * H.nv;
+  if (x) CUDA_TRY(cudaMemcpyAsync(b->d.x + 3 * (size_t)H.v0, x, bytes, cudaMemcpyHostToDevice, b->stream));
+  if (v) CUDA_TRY(cudaMemcpyAsync(b->d.v + 3 * (size_t)H.v0, v, bytes, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  const SceneHost& H = b->scenes[scene];
+  const size_t bytes = 3 * sizeof(double) * H.nv;
+  if (x) CUDA_TRY(cudaMemcpyAsync(x, b->d.x + 3 * (size_t)H.v0, bytes, cudaMemcpyDeviceToHost, b->stream));
+  if (v) CUDA_TRY(cudaMemcpyAsync(v, b->d.v + 3 * (size_t)H.v0, bytes, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_external_forces(hobak_batch b, int scene, const double* f) {
+  if (!b || !f || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  const SceneHost& H = b->scenes[scene];
+  CUDA_TRY(cudaMemcpyAsync(const_cast<double*>(b->d.fext) + 3 * (size_t)H.v0, f, 3 * sizeof(double) * H.nv,
+                           cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
+  if (!b || !opts) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  int rc = check_opts(opts);
+  if (rc) return rc;
+  b->opts = *opts;
+  return upload_solver_opts(b);
+}
+
+int hobak_batch_device_bytes(hobak_batch b, long long* bytes) {
+  if (!b || !bytes) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  *bytes = (long long)b->arenaBytes;
+  return HOBAK_OK;
+}
+
+int hobak_batch_energy(hobak_batch b, int scene, double* energy) {
+  if (!b || !energy || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  const SceneHost& H = b->scenes[scene];
+  launch_energy(b->d, b->stream);
+  std::vector<double> psi(H.nt);
+  CUDA_TRY(cudaMemcpyAsync(psi.data(), b->d.psi + H.t0, sizeof(double) * H.nt, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  double e = 0;
+  for (double p : psi) e += p;
+  *energy = e;
+  return HOBAK_OK;
+}
+
+int hobak_gpu_create(const hobak_scene_desc* scene, const hobak_solver_opts* opts, hobak_batch* out) {
+  return hobak_batch_create(scene, 1, opts, out);
+}
+int hobak_gpu_step(hobak_batch b, int nsteps, hobak_step_stats* stats) { return hobak_batch_step(b, nsteps, stats); }
+int hobak_gpu_set_state(hobak_batch b, const double* x, const double* v) { return hobak_batch_set_state(b, 0, x, v); }
+int hobak_gpu_get_state(hobak_batch b, double* x, double* v) { return hobak_batch_get_state(b, 0, x, v); }
+int hobak_gpu_destroy(hobak_batch b) { return hobak_batch_destroy(b); }
+
+int hobak_material_eval(const hobak_material* m, int n, const double* F, double* psi, double* P, double* H) {
+  if (!m || n <= 0 || !F) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  if (m->kind < 0 || m->kind > 5) return fail(HOBAK_ERR_INVALID, "unknown material");
+  int rc = hobak_device_check(nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  double *dF = nullptr, *dPsi = nullptr, *dP = nullptr, *dH = nullptr;
+  const size_t N = (size_t)n;
+  CUDA_TRY(cudaMalloc(&dF, 9 * N * sizeof(double)));
+  if (psi) CUDA_TRY(cudaMalloc(&dPsi, N * sizeof(double)));
+  if (P) CUDA_TRY(cudaMalloc(&dP, 9 * N * sizeof(double)));
+  if (H) CUDA_TRY(cudaMalloc(&dH, 81 * N * sizeof(double)));
+  CUDA_TRY(cudaMemcpy(dF, F, 9 * N * sizeof(double), cudaMemcpyHostToDevice));
+  launch_material_eval(m->kind, m->mu, m->lambda, n, dF, dPsi, dP, dH, 0);
+  CUDA_TRY(cudaGetLastError());
+  if (psi) CUDA_TRY(cudaMemcpy(psi, dPsi, N * sizeof(double), cudaMemcpyDeviceToHost));
+  if (P) CUDA_TRY(cudaMemcpy(P, dP, 9 * N * sizeof(double), cudaMemcpyDeviceToHost));
+  if (H) CUDA_TRY(cudaMemcpy(H, dH, 81 * N * sizeof(double), cudaMemcpyDeviceToHost));
+  cudaFree(dF);
+  cudaFree(dPsi);
+  cudaFree(dP);
+  cudaFree(dH);
+  return HOBAK_OK;
+}
+
+int hobak_element_eval(int nv, int nt, const double* rest, const int* tets, const double* x, const hobak_material* m,
+                       double* F, double* sigma, double* force, double* hessian) {
+  if (nv <= 0 || nt <= 0 || !rest || !tets || !x || !m) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  if (m->kind < 0 || m->kind > 5) return fail(HOBAK_ERR_INVALID, "unknown material");
+  for (long k = 0; k < 4L * nt; k++)
+    if (tets[k] < 0 || tets[k] >= nv) return fail(HOBAK_ERR_INVALID, "tet vertex id out of range");
+  int rc = hobak_device_check(nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  std::vector<double> Dm(9 * (size_t)nt), vol(nt);
+  for (int t = 0; t < nt; t++) {
+    const double* p[4];
+    for (int a = 0; a < 4; a++) p[a] = rest + 3 * (size_t)tets[4 * (size_t)t + a];
+    vol[t] = tet_volume(p[0], p[1], p[2], p[3]);
+    dm_inverse(p[0], p[1], p[2], p[3], &Dm[9 * (size_t)t]);
+  }
+  const size_t T = (size_t)nt, V = (size_t)nv;
+  double *dRest, *dX, *dDm, *dVol, *dF = nullptr, *dS = nullptr, *dFo = nullptr, *dH = nullptr;
+  int4* dTets;
+  CUDA_TRY(cudaMalloc(&dRest, 3 * V * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&dX, 3 * V * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&dDm, 9 * T * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&dVol, T * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&dTets, T * sizeof(int4)));
+  if (F) CUDA_TRY(cudaMalloc(&dF, 9 * T * sizeof(double)));
+  if (sigma) CUDA_TRY(cudaMalloc(&dS, 3 * T * sizeof(double)));
+  if (force) CUDA_TRY(cudaMalloc(&dFo, 12 * T * sizeof(double)));
+  if (hessian) CUDA_TRY(cudaMalloc(&dH, 144 * T * sizeof(double)));
+  CUDA_TRY(cudaMemcpy(dRest, rest, 3 * V * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(dX, x, 3 * V * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(dDm, Dm.data(), 9 * T * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(dVol, vol.data(), T * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(dTets, tets, T * sizeof(int4), cudaMemcpyHostToDevice));
+  launch_element_eval(nt, dTets, dRest, dX, dDm, dVol, m->kind, m->mu, m->lambda, dF, dS, dFo, dH, 0);
+  CUDA_TRY(cudaGetLastError());
+  if (F) CUDA_TRY(cudaMemcpy(F, dF, 9 * T * sizeof(double), cudaMemcpyDeviceToHost));
+  if (sigma) CUDA_TRY(cudaMemcpy(sigma, dS, 3 * T * sizeof(double), cudaMemcpyDeviceToHost));
+  if (force) CUDA_TRY(cudaMemcpy(force, dFo, 12 * T * sizeof(double), cudaMemcpyDeviceToHost));
+  if (hessian) CUDA_TRY(cudaMemcpy(hessian, dH, 144 * T * sizeof(double), cudaMemcpyDeviceToHost));
+  for (void* p : {(void*)dRest, (void*)dX, (void*)dDm, (void*)dVol, (void*)dTets, (void*)dF, (void*)dS,
+                  (void*)dFo, (void*)dH})
+    cudaFree(p);
+  return HOBAK_OK;
+}
+
+int hobak_batch_assemble(hobak_batch b, int scene, int* nblocks, int* rowptr, int* cols, double* K, double* R) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  const SceneHost& H = b->scenes[scene];
+  const int rb0 = b->hostRowptr[H.v0], rb1 = b->hostRowptr[H.v0 + H.nv];
+  if (nblocks) *nblocks = rb1 - rb0;
+  if (rowptr)
+    for (int u = 0; u <= H.nv; u++) rowptr[u] = b->hostRowptr[H.v0 + u] - rb0;
+  if (cols)
+    for (int k = rb0; k < rb1; k++) cols[k - rb0] = b->hostCols[k] - H.v0;
+  if (!K && !R) return HOBAK_OK;
+  // element terms at the current state with raw forces, then the device
+  // gathers K and R into the (per-step scratch) LHS and rhs buffers
+  DeviceBatch d = b->d;
+  launch_begin_step(d, b->stream);
+  launch_element(d, b->stream, 1);
+  launch_assemble_raw(d, d.lhs, d.rhs, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  if (K)
+    CUDA_TRY(cudaMemcpyAsync(K, d.lhs + 9 * (size_t)rb0, 9 * sizeof(double) * (rb1 - rb0), cudaMemcpyDeviceToHost,
+                             b->stream));
+  if (R)
+    CUDA_TRY(cudaMemcpyAsync(R, d.rhs + 3 * (size_t)H.v0, 3 * sizeof(double) * H.nv, cudaMemcpyDeviceToHost,
+                             b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+// Shared device-side layout of a packed batch of scenes.
+//
+// HBM layout (one contiguous region per array, scenes packed back to back):
+//   vertices  [V]  rest, displacement x, velocity v, external force, mass,
+//                  free mask (0 = pinned), pin target          (interleaved xyz)
+//   tets      [T]  int4 global vertex ids, DmInv (9, column major), rest volume,
+//                  scene id
+//   blocks    [B]  3x3-block CSR of the system matrix: rowptr [V+1] (global),
+//                  cols [B] (global vertex ids), values 9 per block ROW major
+//   element   [T]  10 upper-triangle 3x3 blocks of the 12x12 element Hessian
+//                  (90 values) + 12 right-hand-side contributions
+//   maps           block <- (tet, a, b) contributions (CSR by block, ascending
+//                  tet), vertex <- (tet, a) incidences (CSR by vertex)
+//   tiles          PCG work units: kTileV consecutive vertices of one scene
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hobak {
+
+enum MaterialKind : int { MAT_SNH = 0, MAT_ARAP = 1, MAT_STVK = 2, MAT_LINEAR = 3, MAT_NHBW = 4, MAT_SNHB = 5 };
+
+constexpr int kTileV = 128;       // vertices per PCG tile (one CTA)
+constexpr int kElemHess = 90;     // 10 upper blocks x 9
+constexpr int kElemStride = 102;  // 90 Hessian + 12 rhs values per tet
+
+// Index of block (a, b), a <= b, in the 10-block upper triangle of a 4x4
+// block matrix: (0,0)(0,1)(0,2)(0,3)(1,1)(1,2)(1,3)(2,2)(2,3)(3,3).
+__host__ __device__ __forceinline__ int upper_block(int a, int b) {
+  return a * 4 - (a * (a - 1)) / 2 + (b - a);
+}
+
+struct SceneParams {
+  int v0, nv;          // vertex range
+  int t0, nt;          // tet range
+  int tile0, ntiles;   // PCG tile range
+  int kind;            // material
+  double mu, lambda, alpha;  // reparameterised material constants
+  double dt;
+};
+
+// Per-scene solver scalars, written by the last CTA of each reduction.
+struct SolveState {
+  double rhsNorm2, threshold;
+  double rz, pAp, alpha, beta, rr;
+  double tol;
+  int iters, maxit;
+  int done;        // 1 when this scene's PCG has finished
+  int converged;
+  unsigned ticketA, ticketB;
+  int totalIters;  // summed over refinement sweeps
+  int refinements;
+  int pad;
+};
+
+}  // namespace hobak

@@ -1,0 +1,354 @@
+// Per-tet element kernels for sm_103a.
+//
+// One thread per tet: gather the 4 vertices, F = Ds DmInv, rotation-variant
+// SVD, PK1 and the analytic-eigensystem clamped Hessian, then the element
+// force and the 12x12 element Hessian.  The Hessian is never formed as 9x9:
+// every eigenmode q_k (a 3x3 matrix U M_k V^T) is pushed through
+// pFpx^T first, w_k = pFpx^T vec(q_k), which only needs B = DmInv V, and the
+// element matrix is accumulated as -vol D^T (sum_k lambda_k w_k w_k^T) D with
+// D the 9x12 difference operator dx_a = x_{a+1} - x_0.  This is the same
+// matrix as the reference's pFpx^T (-V clampedHessian) pFpx
+// (TET_MESH_FASTER.cpp:95-103) with far fewer FP64 operations.
+#include "element_math.cuh"
+#include "kernels.cuh"
+
+namespace hobak {
+
+namespace {
+
+constexpr double kInvSqrt2 = 0.70710678118654752440;
+
+// 9x9 symmetric accumulator over (vertex a = 1..3, component i), packed
+// upper triangle, index of (r, c) with r <= c.
+__host__ __device__ __forceinline__ constexpr int sym9(int r, int c) { return r * 9 - (r * (r - 1)) / 2 + (c - r); }
+
+// Hr = sum_k L_k w_k w_k^T over the 9 eigenmodes (reduced 9x9, vertices 1..3).
+// Returns in Hr[45].  U, B are the SVD's U and B = DmInv V.
+template <typename T>
+__device__ __forceinline__ void reduced_hessian(const MatParams& m, const double* Ud, const double* Sd,
+                                                const double* Vd, const double* Dinv, T* Hr) {
+#pragma unroll
+  for (int k = 0; k < 45; k++) Hr[k] = T(0);
+  if (m.kind == MAT_LINEAR) {
+    // H9 = mu (I + transpose swap) + lambda vec(I) vec(I)^T (LINEAR.cpp hessian):
+    // Hr[(a,i),(b,k)] = mu delta_ik (d_a . d_b) + mu d_a[k] d_b[i] + lambda d_a[i] d_b[k]
+    const T mu = T(m.mu), la = T(m.lambda);
+#pragma unroll
+    for (int r = 0; r < 9; r++)
+#pragma unroll
+      for (int c = r; c < 9; c++) {
+        const int a = r / 3, i = r % 3, b = c / 3, k = c % 3;
+        T dd = T(0);
+#pragma unroll
+        for (int j = 0; j < 3; j++) dd += T(Dinv[a + 3 * j]) * T(Dinv[b + 3 * j]);
+        T val = mu * T(Dinv[a + 3 * k]) * T(Dinv[b + 3 * i]) + la * T(Dinv[a + 3 * i]) * T(Dinv[b + 3 * k]);
+        if (i == k) val += mu * dd;
+        Hr[sym9(r, c)] = val;
+      }
+    return;
+  }
+  T L[9], A3[9], Q3[9];
+  const bool scalingMatrix = material_eigensystem<T>(m, Sd, L, A3);
+  if (scalingMatrix) {
+    T L3[3];
+    eig3sym<T>(A3, Q3, L3);
+    L[6] = L3[0];
+    L[7] = L3[1];
+    L[8] = L3[2];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) Q3[k] = (k % 4 == 0) ? T(1) : T(0);
+  }
+  // B(a, m) = sum_j DmInv(a, j) V(j, m); U in T
+  T U[9], B[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) U[k] = T(Ud[k]);
+#pragma unroll
+  for (int mm = 0; mm < 3; mm++)
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      double s = 0;
+#pragma unroll
+      for (int j = 0; j < 3; j++) s += Dinv[a + 3 * j] * Vd[j + 3 * mm];
+      B[a + 3 * mm] = T(s);
+    }
+  const T rs2 = T(kInvSqrt2);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const T lam = L[k] > T(0) ? L[k] : T(0);  // clamp (SNH.cpp:138-141)
+    if (lam == T(0)) continue;
+    T w[9];  // w[(a, comp)] = (U M_k B^T)(comp, a)
+    if (k < 6) {
+      // twist (k < 3) and flip (k >= 3) for column pair (i, j)
+      const int kk = k % 3;
+      const int i = (kk == 0) ? 1 : (kk == 1) ? 2 : 1;
+      const int j = (kk == 0) ? 2 : 0;
+      const T sgn = (k < 3) ? T(-1) : T(1);
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          w[3 * a + c] = rs2 * (U[c + 3 * j] * B[a + 3 * i] + sgn * U[c + 3 * i] * B[a + 3 * j]);
+    } else {
+      const int kk = k - 6;
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          T s = T(0);
+#pragma unroll
+          for (int mm = 0; mm < 3; mm++) s += Q3[mm + 3 * kk] * U[c + 3 * mm] * B[a + 3 * mm];
+          w[3 * a + c] = s;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 9; r++) {
+      const T lr = lam * w[r];
+#pragma unroll
+      for (int c = r; c < 9; c++) Hr[sym9(r, c)] += lr * w[c];
+    }
+  }
+}
+
+// Element force f = -vol pFpx^T vec(P) (TET_MESH.cpp:743-745):
+// f_{a+1} = -vol P DmInv^T(:, a), f_0 = -(f_1 + f_2 + f_3).
+__device__ __forceinline__ void element_force(const double* P, const double* Dinv, double vol, double* f) {
+#pragma unroll
+  for (int i = 0; i < 3; i++) f[i] = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const double g = P[i] * Dinv[a] + P[i + 3] * Dinv[a + 3] + P[i + 6] * Dinv[a + 6];
+      f[3 * (a + 1) + i] = -vol * g;
+      f[i] += vol * g;
+    }
+}
+
+// Expand -vol D^T Hr D into the 10 upper 3x3 blocks (row major in each block).
+template <typename T, typename OutT>
+__device__ __forceinline__ void expand_blocks(const T* Hr, double vol, OutT* out) {
+  const T nv = T(-vol);
+  // vertex-0 sums: colsum[b][i][k] = sum_a Hr[(a,i),(b,k)]
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = a; b < 3; b++)
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          const int r = 3 * a + i, c = 3 * b + k;
+          const T h = (r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)];
+          out[9 * upper_block(a + 1, b + 1) + 3 * i + k] = OutT(nv * h);
+        }
+  T s00[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) s00[k] = T(0);
+#pragma unroll
+  for (int b = 0; b < 3; b++)
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        T s = T(0);
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          const int r = 3 * a + i, c = 3 * b + k;
+          s += (r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)];
+        }
+        // block (0, b+1) entry (i, k) = -vol * (-(sum_a Hr[(a,i),(b,k)]))
+        out[9 * upper_block(0, b + 1) + 3 * i + k] = OutT(-nv * s);
+        s00[3 * i + k] += s;
+      }
+  // block (0,0) = -vol * sum_a sum_b Hr[a,b]: row sums of the column sums
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) out[3 * i + k] = OutT(nv * s00[3 * i + k]);
+}
+
+__device__ __forceinline__ void load_tet(const int4 tv, const double* rest, const double* x, double X[4][3]) {
+  const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) X[a][i] = rest[3 * vid[a] + i] + x[3 * vid[a] + i];
+}
+
+__device__ __forceinline__ void deformation_gradient(const double X[4][3], const double* Dinv, double* F) {
+  // F = Ds DmInv, Ds(:, a) = x_{a+1} - x_0 (TET_MESH.cpp:706-714)
+  double Ds[9];
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) Ds[i + 3 * a] = X[a + 1][i] - X[0][i];
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      F[i + 3 * j] = Ds[i] * Dinv[3 * j] + Ds[i + 3] * Dinv[1 + 3 * j] + Ds[i + 6] * Dinv[2 + 3 * j];
+}
+
+// Batched step kernel: element Hessian blocks and right-hand-side terms
+// g = dt (f + dt He v) for every tet of every scene.
+__global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.nt) return;
+  const int4 tv = b.tets[t];
+  const SceneParams& sp = b.scenes[b.tetScene[t]];
+  const MatParams m{sp.kind, sp.mu, sp.lambda, sp.alpha};
+  const double dt = rawForces ? 0.0 : sp.dt;
+  double Dinv[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) Dinv[k] = b.DmInv[9 * (size_t)t + k];
+  const double vol = b.vol[t];
+  double X[4][3];
+  load_tet(tv, b.rest, b.x, X);
+  double F[9], U[9], S[3], V[9], P[9], f[12];
+  deformation_gradient(X, Dinv, F);
+  svd3_rv(F, U, S, V);
+  material_pk1(m, F, U, V, P);
+  element_force(P, Dinv, vol, f);
+
+  double Hr[45];
+  reduced_hessian<double>(m, U, S, V, Dinv, Hr);
+
+  // He v = -vol D^T Hr (D v): D v = relative velocities of vertices 1..3
+  const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
+  double dv[9];
+  {
+    double v0[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) v0[i] = b.v[3 * vid[0] + i];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) dv[3 * a + i] = b.v[3 * vid[a + 1] + i] - v0[i];
+  }
+  double* g = b.elemG + 12 * (size_t)t;
+  double h0[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int r = 0; r < 9; r++) {
+    double s = 0;
+#pragma unroll
+    for (int c = 0; c < 9; c++) s += ((r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)]) * dv[c];
+    const double hv = -vol * s;
+    h0[r % 3] += hv;
+    g[3 + r] = rawForces ? f[3 + r] : dt * (f[3 + r] + dt * hv);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) g[i] = rawForces ? f[i] : dt * (f[i] - dt * h0[i]);
+
+  expand_blocks<double, double>(Hr, vol, b.elemH + kElemHess * (size_t)t);
+}
+
+// Standalone: clamped 9x9 Hessian, PK1 and psi of n deformation gradients.
+__global__ void k_material_eval(MatParams m, int n, const double* Fin, double* psi, double* Pout, double* Hout) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double F[9], U[9], S[3], V[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) F[k] = Fin[9 * (size_t)e + k];
+  svd3_rv(F, U, S, V);
+  if (psi) psi[e] = material_psi(m, F, S);
+  if (Pout) material_pk1(m, F, U, V, Pout + 9 * (size_t)e);
+  if (Hout) {
+    // H9 through the same reduced path with DmInv = I (pFpx then selects F itself)
+    const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    double Hr[45];
+    reduced_hessian<double>(m, U, S, V, I3, Hr);
+    // with DmInv = I, Hr[(a,i),(b,k)] = H9[(i + 3a), (k + 3b)] in flatten order
+    double* H = Hout + 81 * (size_t)e;
+#pragma unroll
+    for (int r = 0; r < 9; r++)
+#pragma unroll
+      for (int c = 0; c < 9; c++) {
+        const int rr = 3 * (r / 3) + r % 3, cc = 3 * (c / 3) + c % 3;
+        H[r + 9 * c] = (rr <= cc) ? Hr[sym9(rr, cc)] : Hr[sym9(cc, rr)];
+      }
+  }
+}
+
+// Standalone: per-tet F, sigma, element force and full 12x12 element Hessian.
+__global__ void k_element_eval(int nt, const int4* tets, const double* rest, const double* x, const double* DmInv,
+                               const double* volume, MatParams m, double* Fo, double* So, double* fo, double* Ho) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  double Dinv[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) Dinv[k] = DmInv[9 * (size_t)t + k];
+  const double vol = volume[t];
+  double X[4][3];
+  load_tet(tets[t], rest, x, X);
+  double F[9], U[9], S[3], V[9], P[9], f[12];
+  deformation_gradient(X, Dinv, F);
+  svd3_rv(F, U, S, V);
+  if (Fo)
+    for (int k = 0; k < 9; k++) Fo[9 * (size_t)t + k] = F[k];
+  if (So)
+    for (int k = 0; k < 3; k++) So[3 * (size_t)t + k] = S[k];
+  if (fo) {
+    material_pk1(m, F, U, V, P);
+    element_force(P, Dinv, vol, f);
+    for (int k = 0; k < 12; k++) fo[12 * (size_t)t + k] = f[k];
+  }
+  if (Ho) {
+    double Hr[45], blk[kElemHess];
+    reduced_hessian<double>(m, U, S, V, Dinv, Hr);
+    expand_blocks<double, double>(Hr, vol, blk);
+    double* H = Ho + 144 * (size_t)t;
+    for (int a = 0; a < 4; a++)
+      for (int bb = 0; bb < 4; bb++)
+        for (int i = 0; i < 3; i++)
+          for (int k = 0; k < 3; k++) {
+            const double val = (a <= bb) ? blk[9 * upper_block(a, bb) + 3 * i + k]
+                                         : blk[9 * upper_block(bb, a) + 3 * k + i];
+            H[(3 * a + i) + 12 * (3 * bb + k)] = val;
+          }
+  }
+}
+
+// Per-tet energy density times rest volume.
+__global__ void k_energy(DeviceBatch b) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.nt) return;
+  const SceneParams& sp = b.scenes[b.tetScene[t]];
+  const MatParams m{sp.kind, sp.mu, sp.lambda, sp.alpha};
+  double Dinv[9];
+  for (int k = 0; k < 9; k++) Dinv[k] = b.DmInv[9 * (size_t)t + k];
+  double X[4][3];
+  load_tet(b.tets[t], b.rest, b.x, X);
+  double F[9], U[9], S[3], V[9];
+  deformation_gradient(X, Dinv, F);
+  svd3_rv(F, U, S, V);
+  b.psi[t] = b.vol[t] * material_psi(m, F, S);
+}
+
+}  // namespace
+
+void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces) {
+  if (b.nt == 0) return;
+  k_element<<<(b.nt + 127) / 128, 128, 0, s>>>(b, rawForces);
+}
+
+void launch_energy(const DeviceBatch& b, cudaStream_t s) {
+  if (b.nt == 0) return;
+  k_energy<<<(b.nt + 127) / 128, 128, 0, s>>>(b);
+}
+
+void launch_material_eval(int kind, double mu, double lambda, int n, const double* F, double* psi, double* P,
+                          double* H, cudaStream_t s) {
+  if (n <= 0) return;
+  k_material_eval<<<(n + 127) / 128, 128, 0, s>>>(make_material(kind, mu, lambda), n, F, psi, P, H);
+}
+
+void launch_element_eval(int nt, const int4* tets, const double* rest, const double* x, const double* DmInv,
+                         const double* vol, int kind, double mu, double lambda, double* F, double* sigma,
+                         double* force, double* hessian, cudaStream_t s) {
+  if (nt <= 0) return;
+  k_element_eval<<<(nt + 127) / 128, 128, 0, s>>>(nt, tets, rest, x, DmInv, vol, make_material(kind, mu, lambda), F,
+                                                   sigma, force, hessian);
+}
+
+}  // namespace hobak

@@ -1,0 +1,427 @@
+// Per-tet constitutive math for the sm_103a element kernel.
+//
+// Everything here runs in registers of one thread (one tet).  3x3 matrices are
+// column major, a[i + 3*j] = A(i,j), matching the reference's flatten()
+// (util/MATRIX_UTIL.cpp:33-43).  The deformation gradient, its SVD and the
+// stress are FP64; the eigen-clamped Hessian is templated on the arithmetic
+// type so the mixed-precision path can build it in FP32.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace hobak {
+
+__device__ __forceinline__ double det3(const double* A) {
+  return A[0] * (A[4] * A[8] - A[7] * A[5]) - A[3] * (A[1] * A[8] - A[7] * A[2]) +
+         A[6] * (A[1] * A[5] - A[4] * A[2]);
+}
+
+// Rotation-variant SVD F = U diag(S) V^T (the svd_rv convention,
+// util/MATRIX_UTIL.cpp:76-95): S sorted by magnitude, U and V rotations, the
+// sign of det F carried by S[2].  One-sided Jacobi: plane rotations applied
+// on the right orthogonalise F's columns; V accumulates them.  Converges
+// quadratically; the loop stops when no pair needs a rotation.
+__device__ __forceinline__ void svd3_rv(const double* F, double* U, double* S, double* V) {
+  double A[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) A[k] = F[k];
+#pragma unroll
+  for (int k = 0; k < 9; k++) V[k] = (k % 4 == 0) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 12; sweep++) {
+    bool rotated = false;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const int p = (r == 2) ? 1 : 0;
+      const int q = (r == 0) ? 1 : 2;
+      const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
+      const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
+      const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
+      if (fabs(gamma) > 1e-17 * sqrt(alpha * beta)) {
+        rotated = true;
+        const double zeta = (beta - alpha) / (2.0 * gamma);
+        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = rsqrt(1.0 + t * t), s = c * t;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double x = A[3 * p + i], y = A[3 * q + i];
+          A[3 * p + i] = c * x - s * y;
+          A[3 * q + i] = s * x + c * y;
+          const double vx = V[3 * p + i], vy = V[3 * q + i];
+          V[3 * p + i] = c * vx - s * vy;
+          V[3 * q + i] = s * vx + c * vy;
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  double n[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) n[k] = A[3 * k] * A[3 * k] + A[3 * k + 1] * A[3 * k + 1] + A[3 * k + 2] * A[3 * k + 2];
+  // sort columns by norm, descending (3-element network, swaps A and V columns)
+  auto swapcols = [&](int a, int b) {
+    double tn = n[a];
+    n[a] = n[b];
+    n[b] = tn;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      double t = A[3 * a + i];
+      A[3 * a + i] = A[3 * b + i];
+      A[3 * b + i] = t;
+      t = V[3 * a + i];
+      V[3 * a + i] = V[3 * b + i];
+      V[3 * b + i] = t;
+    }
+  };
+  if (n[0] < n[1]) swapcols(0, 1);
+  if (n[0] < n[2]) swapcols(0, 2);
+  if (n[1] < n[2]) swapcols(1, 2);
+#pragma unroll
+  for (int k = 0; k < 3; k++) S[k] = sqrt(n[k]);
+  // U columns; complete vanishing columns with cross products
+  const double tiny = 1e-300;
+  if (S[0] > tiny) {
+    const double r0 = 1.0 / S[0];
+#pragma unroll
+    for (int i = 0; i < 3; i++) U[i] = A[i] * r0;
+  } else {
+    U[0] = 1.0; U[1] = 0.0; U[2] = 0.0;
+  }
+  if (S[1] > tiny) {
+    const double r1 = 1.0 / S[1];
+#pragma unroll
+    for (int i = 0; i < 3; i++) U[3 + i] = A[3 + i] * r1;
+  } else {
+    // unit vector orthogonal to u0: cross u0 with the axis it is least aligned with
+    const double ax = fabs(U[0]), ay = fabs(U[1]), az = fabs(U[2]);
+    double e0 = 0, e1 = 0, e2 = 0;
+    if (ax <= ay && ax <= az) e0 = 1; else if (ay <= az) e1 = 1; else e2 = 1;
+    double w0 = U[1] * e2 - U[2] * e1, w1 = U[2] * e0 - U[0] * e2, w2 = U[0] * e1 - U[1] * e0;
+    const double rn = rsqrt(w0 * w0 + w1 * w1 + w2 * w2);
+    U[3] = w0 * rn; U[4] = w1 * rn; U[5] = w2 * rn;
+  }
+  if (S[2] > tiny && S[1] > tiny) {
+    const double r2 = 1.0 / S[2];
+#pragma unroll
+    for (int i = 0; i < 3; i++) U[6 + i] = A[6 + i] * r2;
+  } else {
+    U[6] = U[1] * U[5] - U[2] * U[4];
+    U[7] = U[2] * U[3] - U[0] * U[5];
+    U[8] = U[0] * U[4] - U[1] * U[3];
+  }
+  if (det3(U) < 0.0) {
+    U[6] = -U[6]; U[7] = -U[7]; U[8] = -U[8];
+    S[2] = -S[2];
+  }
+  if (det3(V) < 0.0) {
+    V[6] = -V[6]; V[7] = -V[7]; V[8] = -V[8];
+    S[2] = -S[2];
+  }
+}
+
+// Symmetric 3x3 eigensystem by cyclic Jacobi: A = Q diag(L) Q^T.
+template <typename T>
+__device__ __forceinline__ void eig3sym(const T* Ain, T* Q, T* L) {
+  T a00 = Ain[0], a01 = Ain[3], a02 = Ain[6], a11 = Ain[4], a12 = Ain[7], a22 = Ain[8];
+#pragma unroll
+  for (int k = 0; k < 9; k++) Q[k] = (k % 4 == 0) ? T(1) : T(0);
+  const T eps = sizeof(T) == 8 ? T(1e-18) : T(1e-9);
+  for (int sweep = 0; sweep < 16; sweep++) {
+    const T off = fabs(a01) + fabs(a02) + fabs(a12);
+    const T dg = fabs(a00) + fabs(a11) + fabs(a22);
+    if (!(off > eps * dg)) break;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const int p = (r == 2) ? 1 : 0;
+      const int q = (r == 0) ? 1 : 2;
+      T apq = (r == 0) ? a01 : (r == 1) ? a02 : a12;
+      if (apq == T(0)) continue;
+      T app = (p == 0) ? a00 : a11;
+      T aqq = (q == 1) ? a11 : a22;
+      const T theta = (aqq - app) / (T(2) * apq);
+      const T t = copysign(T(1), theta) / (fabs(theta) + sqrt(theta * theta + T(1)));
+      const T c = T(1) / sqrt(t * t + T(1)), s = t * c;
+      // rotate: the remaining index m is the third one
+      if (r == 0) {  // (0,1), m = 2
+        const T n00 = a00 - t * a01, n11 = a11 + t * a01;
+        const T n02 = c * a02 - s * a12, n12 = s * a02 + c * a12;
+        a00 = n00; a11 = n11; a01 = T(0); a02 = n02; a12 = n12;
+      } else if (r == 1) {  // (0,2), m = 1
+        const T n00 = a00 - t * a02, n22 = a22 + t * a02;
+        const T n01 = c * a01 - s * a12, n21 = s * a01 + c * a12;
+        a00 = n00; a22 = n22; a02 = T(0); a01 = n01; a12 = n21;
+      } else {  // (1,2), m = 0
+        const T n11 = a11 - t * a12, n22 = a22 + t * a12;
+        const T n01 = c * a01 - s * a02, n02 = s * a01 + c * a02;
+        a11 = n11; a22 = n22; a12 = T(0); a01 = n01; a02 = n02;
+      }
+#pragma unroll
+      for (int m = 0; m < 3; m++) {
+        const T qp = Q[m + 3 * p], qq = Q[m + 3 * q];
+        Q[m + 3 * p] = c * qp - s * qq;
+        Q[m + 3 * q] = s * qp + c * qq;
+      }
+    }
+  }
+  L[0] = a00; L[1] = a11; L[2] = a22;
+}
+
+// Material parameters after each reference constructor's reparameterisation.
+struct MatParams {
+  int kind;
+  double mu, lambda, alpha;
+};
+
+__host__ __device__ inline MatParams make_material(int kind, double mu, double lambda) {
+  MatParams m{kind, mu, lambda, 0.0};
+  if (kind == MAT_SNH) {  // SNH.cpp:23-32
+    m.lambda = lambda + mu;
+    m.alpha = 1.0 + m.mu / m.lambda;
+  } else if (kind == MAT_NHBW) {  // NEO_HOOKEAN_BW.cpp:23-29
+    m.alpha = 1.0 + mu / lambda;
+  } else if (kind == MAT_SNHB) {  // SNH_WITH_BARRIER.cpp:26-35
+    m.mu = (4.0 / 3.0) * mu;
+    m.lambda = lambda + (5.0 / 6.0) * mu;
+    m.alpha = 1.0 + m.mu / m.lambda - m.mu / (4.0 * m.lambda);
+  }
+  return m;
+}
+
+// d det(F) / dF = [f1 x f2, f2 x f0, f0 x f1] (partialJpartialF, MATRIX_UTIL.cpp:561-568)
+__device__ __forceinline__ void cofactor(const double* F, double* G) {
+  G[0] = F[4] * F[8] - F[5] * F[7];
+  G[1] = F[5] * F[6] - F[3] * F[8];
+  G[2] = F[3] * F[7] - F[4] * F[6];
+  G[3] = F[7] * F[2] - F[8] * F[1];
+  G[4] = F[8] * F[0] - F[6] * F[2];
+  G[5] = F[6] * F[1] - F[7] * F[0];
+  G[6] = F[1] * F[5] - F[2] * F[4];
+  G[7] = F[2] * F[3] - F[0] * F[5];
+  G[8] = F[0] * F[4] - F[1] * F[3];
+}
+
+// psi(F): SNH.cpp:34-43, ARAP.cpp:39-43, STVK.cpp psi, LINEAR.cpp psi,
+// NEO_HOOKEAN_BW.cpp psi, SNH_WITH_BARRIER.cpp psi.  ARAP uses the SVD given.
+__device__ inline double material_psi(const MatParams& m, const double* F, const double* S) {
+  double Ic = 0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) Ic += F[k] * F[k];
+  switch (m.kind) {
+    case MAT_SNH: {
+      const double Jm = det3(F) - m.alpha;
+      return 0.5 * (m.mu * (Ic - 3.0) + m.lambda * Jm * Jm);
+    }
+    case MAT_ARAP:
+      return m.mu * ((S[0] - 1.0) * (S[0] - 1.0) + (S[1] - 1.0) * (S[1] - 1.0) + (S[2] - 1.0) * (S[2] - 1.0));
+    case MAT_STVK: {
+      double E[9], tr = 0, en = 0;
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double ftf = F[3 * i] * F[3 * j] + F[3 * i + 1] * F[3 * j + 1] + F[3 * i + 2] * F[3 * j + 2];
+          E[i + 3 * j] = 0.5 * (ftf - (i == j ? 1.0 : 0.0));
+        }
+      tr = E[0] + E[4] + E[8];
+#pragma unroll
+      for (int k = 0; k < 9; k++) en += E[k] * E[k];
+      return m.mu * en + m.lambda * 0.5 * tr * tr;
+    }
+    case MAT_LINEAR: {
+      double en = 0;
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double e = 0.5 * (F[i + 3 * j] + F[j + 3 * i]) - (i == j ? 1.0 : 0.0);
+          en += e * e;
+        }
+      const double tr = F[0] + F[4] + F[8] - 3.0;
+      return m.mu * en + 0.5 * m.lambda * tr * tr;
+    }
+    case MAT_NHBW: {
+      const double lj = log(det3(F));
+      return m.mu * 0.5 * (Ic - 3.0) - m.mu * lj + m.lambda * 0.5 * lj * lj;
+    }
+    default: {  // MAT_SNHB
+      const double Jm = det3(F) - m.alpha;
+      return 0.5 * (m.mu * (Ic - 3.0) + m.lambda * Jm * Jm - m.mu * log(Ic + 1.0));
+    }
+  }
+}
+
+// PK1(F): SNH.cpp:45-50, ARAP.cpp:48-55 (P = R 2mu (S - I) = 2mu (F - U V^T)),
+// STVK.cpp PK1, LINEAR.cpp PK1, NEO_HOOKEAN_BW.cpp PK1, SNH_WITH_BARRIER.cpp PK1.
+__device__ inline void material_pk1(const MatParams& m, const double* F, const double* U, const double* V,
+                                    double* P) {
+  switch (m.kind) {
+    case MAT_SNH: {
+      double G[9];
+      cofactor(F, G);
+      const double s = m.lambda * (det3(F) - m.alpha);
+#pragma unroll
+      for (int k = 0; k < 9; k++) P[k] = m.mu * F[k] + s * G[k];
+      return;
+    }
+    case MAT_ARAP: {
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double R = U[i] * V[j] + U[i + 3] * V[j + 3] + U[i + 6] * V[j + 6];
+          P[i + 3 * j] = 2.0 * m.mu * (F[i + 3 * j] - R);
+        }
+      return;
+    }
+    case MAT_STVK: {
+      double E[9];
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double ftf = F[3 * i] * F[3 * j] + F[3 * i + 1] * F[3 * j + 1] + F[3 * i + 2] * F[3 * j + 2];
+          E[i + 3 * j] = 0.5 * (ftf - (i == j ? 1.0 : 0.0));
+        }
+      const double tr = E[0] + E[4] + E[8];
+      double Sg[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) Sg[k] = (k % 4 == 0 ? m.lambda * tr : 0.0) + 2.0 * m.mu * E[k];
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+          P[i + 3 * j] = F[i] * Sg[3 * j] + F[i + 3] * Sg[3 * j + 1] + F[i + 6] * Sg[3 * j + 2];
+      return;
+    }
+    case MAT_LINEAR: {
+      const double tr = F[0] + F[4] + F[8] - 3.0;
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double e = 0.5 * (F[i + 3 * j] + F[j + 3 * i]) - (i == j ? 1.0 : 0.0);
+          P[i + 3 * j] = 2.0 * m.mu * e + (i == j ? m.lambda * tr : 0.0);
+        }
+      return;
+    }
+    case MAT_NHBW: {
+      double G[9];
+      cofactor(F, G);
+      const double J = det3(F), iJ = 1.0 / J, lj = log(J);
+#pragma unroll
+      for (int k = 0; k < 9; k++) P[k] = m.mu * (F[k] - iJ * G[k]) + m.lambda * lj * iJ * G[k];
+      return;
+    }
+    default: {  // MAT_SNHB
+      double G[9], Ic = 0;
+      cofactor(F, G);
+#pragma unroll
+      for (int k = 0; k < 9; k++) Ic += F[k] * F[k];
+      const double s = m.lambda * (det3(F) - m.alpha), b = m.mu / (Ic + 1.0);
+#pragma unroll
+      for (int k = 0; k < 9; k++) P[k] = m.mu * F[k] + s * G[k] - b * F[k];
+      return;
+    }
+  }
+}
+
+// Analytic eigensystem of the 9x9 Hessian d2psi/dF2 in the (twist, flip,
+// scaling) basis of "Analytic Eigensystems for Isotropic Distortion Energies":
+// L[0..2] twist, L[3..5] flip, L[6..8] scaling with 3x3 scaling-mode matrix A
+// (symmetric, column major).  Returns false when the scaling modes are the
+// coordinate axes (ARAP, MATRIX_UTIL.cpp:465-497 "jackpot" version).
+// SNH.cpp:94-144, ARAP.cpp:113-135, STVK.cpp buildEigensystem,
+// NEO_HOOKEAN_BW.cpp clampedHessian, SNH_WITH_BARRIER.cpp clampedHessian.
+template <typename T>
+__device__ inline bool material_eigensystem(const MatParams& mp, const double* Sd, T* L, T* A) {
+  const T mu = T(mp.mu), lambda = T(mp.lambda);
+  const T s0 = T(Sd[0]), s1 = T(Sd[1]), s2 = T(Sd[2]);
+  switch (mp.kind) {
+    case MAT_ARAP: {
+      L[0] = mu * (T(2) - T(4) / (s1 + s2));
+      L[1] = mu * (T(2) - T(4) / (s0 + s2));
+      L[2] = mu * (T(2) - T(4) / (s0 + s1));
+#pragma unroll
+      for (int k = 3; k < 9; k++) L[k] = T(2) * mu;
+      return false;
+    }
+    case MAT_SNH: {
+      const T J = s0 * s1 * s2;
+      const T front = lambda * (J - T(1)) - mu;
+      L[0] = front * s0 + mu;
+      L[1] = front * s1 + mu;
+      L[2] = front * s2 + mu;
+      L[3] = -front * s0 + mu;
+      L[4] = -front * s1 + mu;
+      L[5] = -front * s2 + mu;
+      A[0] = mu + lambda * s1 * s1 * s2 * s2;
+      A[4] = mu + lambda * s0 * s0 * s2 * s2;
+      A[8] = mu + lambda * s0 * s0 * s1 * s1;
+      const T od = lambda * (T(2) * J - T(1)) - mu;
+      A[1] = A[3] = od * s2;
+      A[2] = A[6] = od * s1;
+      A[5] = A[7] = od * s0;
+      return true;
+    }
+    case MAT_STVK: {
+      const T I2 = s0 * s0 + s1 * s1 + s2 * s2;
+      const T front = -mu + lambda * T(0.5) * (I2 - T(3));
+      L[0] = front + mu * (s1 * s1 + s2 * s2 - s1 * s2);
+      L[1] = front + mu * (s0 * s0 + s2 * s2 - s0 * s2);
+      L[2] = front + mu * (s0 * s0 + s1 * s1 - s0 * s1);
+      L[3] = front + mu * (s1 * s1 + s2 * s2 + s1 * s2);
+      L[4] = front + mu * (s0 * s0 + s2 * s2 + s0 * s2);
+      L[5] = front + mu * (s0 * s0 + s1 * s1 + s0 * s1);
+      const T sv[3] = {s0, s1, s2};
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+          A[i + 3 * j] = (i == j) ? front + (lambda + T(3) * mu) * sv[i] * sv[i] : lambda * sv[i] * sv[j];
+      return true;
+    }
+    case MAT_NHBW: {
+      const T J = s0 * s1 * s2, lj = log(J);
+      const T i01 = T(1) / (s0 * s1), i02 = T(1) / (s0 * s2), i12 = T(1) / (s1 * s2);
+      const T front = lambda * lj - mu;
+      L[0] = front * i12 + mu;
+      L[1] = front * i02 + mu;
+      L[2] = front * i01 + mu;
+      L[3] = -front * i12 + mu;
+      L[4] = -front * i02 + mu;
+      L[5] = -front * i01 + mu;
+      const T fd = lambda * (T(1) - lj) + mu;
+      A[0] = fd / (s0 * s0) + mu;
+      A[4] = fd / (s1 * s1) + mu;
+      A[8] = fd / (s2 * s2) + mu;
+      A[1] = A[3] = lambda * i01;
+      A[2] = A[6] = lambda * i02;
+      A[5] = A[7] = lambda * i12;
+      return true;
+    }
+    default: {  // MAT_SNHB
+      const T alpha = T(mp.alpha);
+      const T J = s0 * s1 * s2, I2 = s0 * s0 + s1 * s1 + s2 * s2;
+      const T front = -mu / (I2 + T(1)) + mu;
+      const T back = lambda * (J - alpha);
+      L[0] = front + back * s0;
+      L[1] = front + back * s1;
+      L[2] = front + back * s2;
+      L[3] = front - back * s0;
+      L[4] = front - back * s1;
+      L[5] = front - back * s2;
+      const T isq = T(1) / ((I2 + T(1)) * (I2 + T(1))), tm = T(2) * mu;
+      const T fd = (-mu * (I2 + T(1))) * isq + mu;
+      const T fo = (T(2) * J - alpha) * lambda;
+      A[0] = fd + tm * s0 * s0 * isq + lambda * s1 * s1 * s2 * s2;
+      A[4] = fd + tm * s1 * s1 * isq + lambda * s0 * s0 * s2 * s2;
+      A[8] = fd + tm * s2 * s2 * isq + lambda * s0 * s0 * s1 * s1;
+      A[1] = A[3] = fo * s2 + (tm * s0 * s1) * isq;
+      A[2] = A[6] = fo * s1 + (tm * s0 * s2) * isq;
+      A[5] = A[7] = fo * s0 + (tm * s1 * s2) * isq;
+      return true;
+    }
+  }
+}
+
+}  // namespace hobak

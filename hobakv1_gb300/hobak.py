@@ -1,0 +1,390 @@
+"""Python mirror of HOBAK's hot-path interfaces over the GB300 C ABI.
+
+Class and method names follow the reference so code written against it reads
+the same:
+
+  * VOLUME::HYPERELASTIC and its energies (Hyperelastic/Volume/HYPERELASTIC.h:31-64):
+    SNH, ARAP, STVK, LINEAR, NEO_HOOKEAN_BW, SNH_WITH_BARRIER with
+    psi / PK1 / clampedHessian, evaluated on the GPU in batches.
+  * TET_MESH (Geometry/TET_MESH.h): rest vertices, tets, displacement.
+  * TIMESTEPPER::BACKWARD_EULER_VELOCITY (Timestepper/BACKWARD_EULER_VELOCITY.h:35-58):
+    position() / velocity() / externalForces() host state, setDt, addGravity,
+    attachKinematicConstraints, scaleMass, solve(verbose).
+  * BATCH: many scenes stepped together (hobak_batch_*).
+
+Matrices use numpy's [i, j] indexing; the C ABI's column-major flatten order
+(util/MATRIX_UTIL.cpp:33-43) is applied at the boundary.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import HobakMaterial, HobakSceneDesc, HobakSolverOpts, HobakStepStats, check, dptr, iptr
+
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+PRECOND_JACOBI = 0
+PRECOND_BLOCK_JACOBI = 1
+
+
+def _colmajor(F: np.ndarray) -> np.ndarray:
+    F = np.asarray(F, dtype=np.float64)
+    single = F.ndim == 2
+    F = F.reshape(-1, 3, 3)
+    return np.ascontiguousarray(F.transpose(0, 2, 1).reshape(-1, 9)), single
+
+
+class HYPERELASTIC:
+    """Base of the isotropic volume energies; (mu, lambda) are the reference
+    constructor arguments (the SNH reparameterisation happens in the library)."""
+    KIND = -1
+    NAME = "HYPERELASTIC"
+
+    def __init__(self, mu: float, lam: float):
+        self.mu = float(mu)
+        self.lam = float(lam)
+
+    def name(self) -> str:
+        return self.NAME
+
+    def _c(self) -> HobakMaterial:
+        return HobakMaterial(self.KIND, self.mu, self.lam)
+
+    @staticmethod
+    def computeMu(E: float, nu: float) -> float:
+        """HYPERELASTIC::computeMu (HYPERELASTIC.cpp:111-115)."""
+        return E / (2.0 * (1.0 + nu))
+
+    @staticmethod
+    def computeLambda(E: float, nu: float) -> float:
+        """HYPERELASTIC::computeLambda (HYPERELASTIC.cpp:117-122)."""
+        return (E * nu) / ((1.0 + nu) * (1.0 - 2.0 * nu))
+
+    def _eval(self, F, want_psi=False, want_P=False, want_H=False):
+        Fc, single = _colmajor(F)
+        n = Fc.shape[0]
+        psi = np.zeros(n) if want_psi else None
+        P = np.zeros((n, 9)) if want_P else None
+        H = np.zeros((n, 81)) if want_H else None
+        mat = self._c()
+        check(_lib.load().hobak_material_eval(ctypes.byref(mat), n, dptr(Fc), dptr(psi), dptr(P), dptr(H)),
+              "hobak_material_eval")
+        return psi, P, H, single
+
+    def psi(self, F):
+        """Strain energy density psi(F)."""
+        psi, _, _, single = self._eval(F, want_psi=True)
+        return float(psi[0]) if single else psi
+
+    def PK1(self, F):
+        """First Piola-Kirchhoff stress, [..., 3, 3]."""
+        _, P, _, single = self._eval(F, want_P=True)
+        P = P.reshape(-1, 3, 3).transpose(0, 2, 1)
+        return P[0] if single else P
+
+    def clampedHessian(self, F):
+        """d2psi/dF2 projected to PSD, 9x9 in flatten() order, [..., 9, 9]."""
+        _, _, H, single = self._eval(F, want_H=True)
+        H = H.reshape(-1, 9, 9).transpose(0, 2, 1)
+        return H[0] if single else H
+
+
+class SNH(HYPERELASTIC):
+    KIND, NAME = 0, "SNH"
+
+
+class ARAP(HYPERELASTIC):
+    KIND, NAME = 1, "ARAP"
+
+
+class STVK(HYPERELASTIC):
+    KIND, NAME = 2, "STVK"
+
+
+class LINEAR(HYPERELASTIC):
+    KIND, NAME = 3, "LINEAR"
+
+
+class NEO_HOOKEAN_BW(HYPERELASTIC):
+    KIND, NAME = 4, "NEO_HOOKEAN_BW"
+
+
+class SNH_WITH_BARRIER(HYPERELASTIC):
+    KIND, NAME = 5, "SNH_WITH_BARRIER"
+
+
+MATERIAL_CLASSES = {"snh": SNH, "arap": ARAP, "stvk": STVK, "linear": LINEAR,
+                    "neo_hookean_bw": NEO_HOOKEAN_BW, "snh_barrier": SNH_WITH_BARRIER}
+
+
+def make_material(name: str, mu: float, lam: float) -> HYPERELASTIC:
+    return MATERIAL_CLASSES[name](mu, lam)
+
+
+class TET_MESH:
+    """Rest mesh plus current displacement (Geometry/TET_MESH.h)."""
+
+    def __init__(self, restVertices: np.ndarray, tets: np.ndarray):
+        self._rest = np.ascontiguousarray(restVertices, dtype=np.float64).reshape(-1, 3)
+        self._tets = np.ascontiguousarray(tets, dtype=np.int32).reshape(-1, 4)
+        self._disp = np.zeros_like(self._rest)
+        d1 = self._rest[self._tets[:, 1]] - self._rest[self._tets[:, 0]]
+        d2 = self._rest[self._tets[:, 2]] - self._rest[self._tets[:, 0]]
+        d3 = self._rest[self._tets[:, 3]] - self._rest[self._tets[:, 0]]
+        self._restVolumes = np.einsum("ij,ij->i", d3, np.cross(d1, d2)) / 6.0
+        if (self._restVolumes <= 0).any():
+            raise ValueError("TET_MESH: tets must have positive rest volume")
+        self._oneRing = np.zeros(len(self._rest))
+        np.add.at(self._oneRing, self._tets.reshape(-1), np.repeat(0.25 * self._restVolumes, 4))
+
+    def restVertices(self):
+        return self._rest
+
+    def tets(self):
+        return self._tets
+
+    def vertices(self):
+        return self._rest + self._disp
+
+    def totalVertices(self) -> int:
+        return len(self._rest)
+
+    def DOFs(self) -> int:
+        return 3 * len(self._rest)
+
+    def restOneRingVolumes(self):
+        return self._oneRing
+
+    def setDisplacement(self, delta):
+        self._disp = np.asarray(delta, dtype=np.float64).reshape(-1, 3).copy()
+
+    def getDisplacement(self):
+        return self._disp.reshape(-1).copy()
+
+    def computeElements(self, material: HYPERELASTIC):
+        """Per-tet F, Sigma, element force (12) and element Hessian (12x12) on
+        the GPU at the current displacement."""
+        nt, nv = len(self._tets), len(self._rest)
+        F, S = np.zeros((nt, 9)), np.zeros((nt, 3))
+        f, H = np.zeros((nt, 12)), np.zeros((nt, 144))
+        x = np.ascontiguousarray(self._disp.reshape(-1))
+        mat = material._c()
+        check(_lib.load().hobak_element_eval(nv, nt, dptr(self._rest), iptr(self._tets), dptr(x),
+                                             ctypes.byref(mat), dptr(F), dptr(S), dptr(f), dptr(H)),
+              "hobak_element_eval")
+        return {"F": F, "Sigma": S, "force": f, "hessian": H}
+
+
+def solver_opts(tol=1e-8, max_iters=1000, precision=PRECISION_FP64, preconditioner=PRECOND_BLOCK_JACOBI,
+                max_refinements=3, use_graph=True) -> HobakSolverOpts:
+    o = HobakSolverOpts()
+    o.tol, o.max_iters, o.precision = tol, max_iters, precision
+    o.preconditioner, o.max_refinements, o.use_graph = preconditioner, max_refinements, int(use_graph)
+    return o
+
+
+class _SceneArrays:
+    """Keeps the numpy buffers a HobakSceneDesc points into alive."""
+
+    def __init__(self, rest, tets, material, density, gravity, dt, pinned, x0, v0):
+        self.rest = np.ascontiguousarray(rest, dtype=np.float64).reshape(-1)
+        self.tets = np.ascontiguousarray(tets, dtype=np.int32).reshape(-1)
+        self.pinned = np.ascontiguousarray(pinned if pinned is not None else [], dtype=np.int32)
+        self.x0 = np.ascontiguousarray(x0, dtype=np.float64).reshape(-1) if x0 is not None else None
+        self.v0 = np.ascontiguousarray(v0, dtype=np.float64).reshape(-1) if v0 is not None else None
+        d = HobakSceneDesc()
+        d.nv, d.nt = len(self.rest) // 3, len(self.tets) // 4
+        d.rest, d.tets = dptr(self.rest), iptr(self.tets)
+        d.material = material._c()
+        d.density = float(density)
+        d.gravity = (ctypes.c_double * 3)(*[float(g) for g in gravity])
+        d.dt = float(dt)
+        d.npinned = len(self.pinned)
+        d.pinned = iptr(self.pinned) if len(self.pinned) else None
+        d.x0, d.v0 = dptr(self.x0), dptr(self.v0)
+        self.desc = d
+
+
+class BATCH:
+    """Many scenes packed into one device-resident batch (hobak_batch_*)."""
+
+    def __init__(self, scenes: Sequence, opts: Optional[HobakSolverOpts] = None):
+        L = _lib.load()
+        self._arrays = [_SceneArrays(s.rest, s.tets, make_material(s.material, s.mu, s.lam), s.density,
+                                     s.gravity, s.dt, s.pinned, s.x0, s.v0) for s in scenes]
+        descs = (HobakSceneDesc * len(self._arrays))(*[a.desc for a in self._arrays])
+        self.nv = [len(a.rest) // 3 for a in self._arrays]
+        self.opts = opts if opts is not None else solver_opts()
+        h = ctypes.c_void_p()
+        check(L.hobak_batch_create(descs, len(self._arrays), ctypes.byref(self.opts), ctypes.byref(h)),
+              "hobak_batch_create")
+        self.h = h
+        self.last_stats = None
+        self.last_status = 0
+
+    def __len__(self):
+        return len(self._arrays)
+
+    def step(self, nsteps: int = 1):
+        stats = (HobakStepStats * len(self))()
+        self.last_status = check(_lib.load().hobak_batch_step(self.h, nsteps, stats), "hobak_batch_step")
+        self.last_stats = [(s.iterations, s.converged, s.rel_residual, s.refinements) for s in stats]
+        return self.last_stats
+
+    def get_state(self, scene: int):
+        n = 3 * self.nv[scene]
+        x, v = np.zeros(n), np.zeros(n)
+        check(_lib.load().hobak_batch_get_state(self.h, scene, dptr(x), dptr(v)), "hobak_batch_get_state")
+        return x, v
+
+    def set_state(self, scene: int, x=None, v=None):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1) if x is not None else None
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1) if v is not None else None
+        check(_lib.load().hobak_batch_set_state(self.h, scene, dptr(x), dptr(v)), "hobak_batch_set_state")
+
+    def set_external_forces(self, scene: int, f):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        check(_lib.load().hobak_batch_set_external_forces(self.h, scene, dptr(f)), "hobak_batch_set_external_forces")
+
+    def set_solver(self, opts: HobakSolverOpts):
+        self.opts = opts
+        check(_lib.load().hobak_batch_set_solver(self.h, ctypes.byref(opts)), "hobak_batch_set_solver")
+
+    def device_bytes(self) -> int:
+        b = ctypes.c_longlong()
+        check(_lib.load().hobak_batch_device_bytes(self.h, ctypes.byref(b)), "hobak_batch_device_bytes")
+        return b.value
+
+    def energy(self, scene: int) -> float:
+        e = ctypes.c_double()
+        check(_lib.load().hobak_batch_energy(self.h, scene, ctypes.byref(e)), "hobak_batch_energy")
+        return e.value
+
+    def assemble(self, scene: int):
+        """BSR pattern, K blocks (column major) and R at the current state."""
+        L = _lib.load()
+        nb = ctypes.c_int()
+        check(L.hobak_batch_assemble(self.h, scene, ctypes.byref(nb), None, None, None, None), "hobak_batch_assemble")
+        rowptr = np.zeros(self.nv[scene] + 1, dtype=np.int32)
+        cols = np.zeros(nb.value, dtype=np.int32)
+        K = np.zeros(9 * nb.value)
+        R = np.zeros(3 * self.nv[scene])
+        check(L.hobak_batch_assemble(self.h, scene, None, iptr(rowptr), iptr(cols), dptr(K), dptr(R)),
+              "hobak_batch_assemble")
+        return rowptr, cols, K.reshape(-1, 9), R
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            _lib.load().hobak_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BACKWARD_EULER_VELOCITY:
+    """GPU drop-in for TIMESTEPPER::BACKWARD_EULER_VELOCITY.
+
+    Host-side position() (displacement), velocity() and externalForces() stay
+    the source of truth like the reference's mutable references
+    (TIMESTEPPER.h:44-58): solve() uploads them, takes one step on the GPU and
+    downloads the new state.  Settings (dt, pins, mass scale) are frozen at the
+    first solve()."""
+
+    def __init__(self, tetMesh: TET_MESH, hyperelastic: HYPERELASTIC, opts: Optional[HobakSolverOpts] = None):
+        self._mesh = tetMesh
+        self._material = hyperelastic
+        self._opts = opts if opts is not None else solver_opts()
+        n = tetMesh.DOFs()
+        self._position = tetMesh.getDisplacement()
+        self._velocity = np.zeros(n)
+        self._externalForces = np.zeros(n)
+        self._dt = 1.0 / 60.0  # BACKWARD_EULER_VELOCITY.cpp:37
+        self._massScale = 1.0
+        self._pinned: list = []
+        self._batch: Optional[BATCH] = None
+        self._currentTimestep = 0
+        self._lastStats = None
+
+    # ---- reference accessors ----
+    def position(self):
+        return self._position
+
+    def velocity(self):
+        return self._velocity
+
+    def externalForces(self):
+        return self._externalForces
+
+    def dt(self):
+        return self._dt
+
+    def setDt(self, dt: float):
+        self._require_unbuilt("setDt")
+        self._dt = float(dt)
+
+    def scaleMass(self, scalar: float):
+        """M *= scalar (TIMESTEPPER.h:100)."""
+        self._require_unbuilt("scaleMass")
+        self._massScale *= float(scalar)
+
+    def addGravity(self, bodyForce):
+        """f_ext += oneRingVolume * bodyForce (TIMESTEPPER.cpp:334-345)."""
+        g = np.asarray(bodyForce, dtype=np.float64).reshape(1, 3)
+        self._externalForces += (self._mesh.restOneRingVolumes()[:, None] * g).reshape(-1)
+
+    def attachKinematicConstraints(self, vertices: Iterable[int]):
+        """Pin vertices at their current positions (TIMESTEPPER.cpp:380-403).
+        Takes vertex ids, or any object with inside(point) like KINEMATIC_SHAPE."""
+        self._require_unbuilt("attachKinematicConstraints")
+        if hasattr(vertices, "inside"):
+            verts = self._mesh.restVertices() + self._position.reshape(-1, 3)
+            ids = [i for i, p in enumerate(verts) if vertices.inside(p)]
+        else:
+            ids = [int(i) for i in vertices]
+        self._pinned.extend(ids)
+
+    def constrainedNodes(self):
+        return sorted(set(self._pinned))
+
+    def _require_unbuilt(self, what):
+        if self._batch is not None:
+            raise RuntimeError(f"{what}: the GPU state is built at the first solve(); call it before")
+
+    def _build(self):
+        class _S:  # scene record for BATCH
+            pass
+        s = _S()
+        s.rest, s.tets = self._mesh.restVertices(), self._mesh.tets()
+        s.material = [k for k, c in MATERIAL_CLASSES.items() if c is type(self._material)][0]
+        s.mu, s.lam = self._material.mu, self._material.lam
+        s.density, s.gravity, s.dt = self._massScale, (0.0, 0.0, 0.0), self._dt
+        s.pinned = np.array(sorted(set(self._pinned)), dtype=np.int32)
+        s.x0, s.v0 = self._position, self._velocity
+        self._batch = BATCH([s], self._opts)
+
+    def solve(self, verbose: bool = False) -> bool:
+        if self._batch is None:
+            self._build()
+        b = self._batch
+        b.set_state(0, self._position, self._velocity)
+        b.set_external_forces(0, self._externalForces)
+        stats = b.step(1)
+        x, v = b.get_state(0)
+        self._position[:] = x
+        self._velocity[:] = v
+        self._currentTimestep += 1
+        self._lastStats = stats[0]
+        if verbose:
+            print(f"  PCG iters: {stats[0][0]:3d} err: {stats[0][2]:6.4e}")
+        return True
+
+    def lastSolveStats(self):
+        return self._lastStats

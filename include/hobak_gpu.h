@@ -1,0 +1,167 @@
+/*
+ * hobak_gpu.h -- C ABI of the GB300 (sm_103a) implicit tet-FEM timestep.
+ *
+ * A drop-in for HOBAK's BACKWARD_EULER_VELOCITY::solve hot path with its
+ * VOLUME::HYPERELASTIC energies.  Plain C types only: host buffers are
+ * caller-owned, device buffers are library-owned, handles are opaque.  Every
+ * call returns an int status (HOBAK_OK = 0; negative = error; positive =
+ * warning) and never throws.  The message of the last failing call on the
+ * calling thread is available from hobak_last_error().
+ *
+ * State conventions follow the reference:
+ *   - vectors are interleaved xyz, 3*nv doubles;
+ *   - the position state is the DISPLACEMENT from rest, like
+ *     TIMESTEPPER::_position (Timestepper/TIMESTEPPER.h:190);
+ *   - the mass matrix is diag(density * one-ring volume)
+ *     (TIMESTEPPER.cpp:176-208 with scaleMass, TIMESTEPPER.h:100);
+ *   - pinned vertices are held at the displacement they had when pinned
+ *     (attachKinematicConstraints, TIMESTEPPER.cpp:380-403 with
+ *     applyKinematicConstraints, TIMESTEPPER.cpp:105-122).
+ */
+#ifndef HOBAK_GPU_H
+#define HOBAK_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define HOBAK_OK 0
+#define HOBAK_WARN_NOT_CONVERGED 1   /* PCG hit max iterations in some scene */
+#define HOBAK_ERR_INVALID -1         /* bad argument, size or handle */
+#define HOBAK_ERR_CUDA -2            /* CUDA runtime error (message in hobak_last_error) */
+#define HOBAK_ERR_NAN -3             /* non-finite value detected in a solve */
+#define HOBAK_ERR_NO_MEMORY -4       /* device allocation failed */
+#define HOBAK_ERR_ADMISSION -5       /* serving: job does not fit the memory budget */
+#define HOBAK_ERR_TIMEOUT -6         /* a bounded device wait gave up */
+#define HOBAK_ERR_NO_DEVICE -7       /* no usable sm_103 device */
+
+/* ---- materials: the VOLUME::HYPERELASTIC family (Hyperelastic/Volume/) ---- */
+#define HOBAK_MATERIAL_SNH 0            /* SNH.cpp (Stable Neo-Hookean)        */
+#define HOBAK_MATERIAL_ARAP 1           /* ARAP.cpp                            */
+#define HOBAK_MATERIAL_STVK 2           /* STVK.cpp (St. Venant-Kirchhoff)     */
+#define HOBAK_MATERIAL_LINEAR 3         /* LINEAR.cpp                          */
+#define HOBAK_MATERIAL_NEO_HOOKEAN_BW 4 /* NEO_HOOKEAN_BW.cpp                  */
+#define HOBAK_MATERIAL_SNH_BARRIER 5    /* SNH_WITH_BARRIER.cpp                */
+
+/* ---- precision modes ---- */
+#define HOBAK_PRECISION_FP64 0   /* every kernel in FP64 */
+#define HOBAK_PRECISION_MIXED 1  /* FP32 Hessian/SpMV/inner PCG, FP64 SVD, residual and refinement */
+
+/* ---- preconditioners ---- */
+#define HOBAK_PRECOND_JACOBI 0        /* scalar 1/diag, Eigen DiagonalPreconditioner */
+#define HOBAK_PRECOND_BLOCK_JACOBI 1  /* inverse of each 3x3 diagonal block */
+
+/* Lame parameters as the reference materials take them: the constructor
+ * arguments (mu, lambda) of SNH(mu, lambda), ARAP(mu, lambda), ...  The SNH
+ * reparameterisation lambda' = lambda + mu (SNH.cpp:23-32) happens inside. */
+typedef struct hobak_material {
+  int kind;      /* HOBAK_MATERIAL_* */
+  double mu;
+  double lambda;
+} hobak_material;
+
+/* One scene (one tet mesh with its material and pins). */
+typedef struct hobak_scene_desc {
+  int nv;                  /* vertices */
+  int nt;                  /* tets */
+  const double* rest;      /* 3*nv rest positions */
+  const int* tets;         /* 4*nt vertex ids, positive rest volume */
+  hobak_material material;
+  double density;          /* mass scale: M = density * diag(one-ring volume) */
+  double gravity[3];       /* body force per unit mass; f_ext = M g per vertex */
+  double dt;               /* time step (reference default 1/60, BEV.cpp:37) */
+  int npinned;
+  const int* pinned;       /* pinned vertex ids (may be NULL if npinned == 0) */
+  const double* x0;        /* 3*nv initial displacement (NULL = zero); pins take x0 */
+  const double* v0;        /* 3*nv initial velocity (NULL = zero) */
+} hobak_scene_desc;
+
+/* Linear solver options (Eigen ConjugateGradient equivalents,
+ * ext/eigen-3.3.7/Eigen/src/IterativeLinearSolvers/ConjugateGradient.h). */
+typedef struct hobak_solver_opts {
+  double tol;              /* relative residual: stop when |r| < tol |rhs| */
+  int max_iters;           /* per solve */
+  int precision;           /* HOBAK_PRECISION_* */
+  int preconditioner;      /* HOBAK_PRECOND_* */
+  int max_refinements;     /* MIXED only: FP64 iterative-refinement sweeps (<= 3) */
+  int use_graph;           /* capture each step as a CUDA graph (1) or launch eagerly (0) */
+} hobak_solver_opts;
+
+/* Per-scene statistics of the last step. */
+typedef struct hobak_step_stats {
+  int iterations;          /* PCG iterations of the last step (summed over refinement sweeps) */
+  int converged;           /* 1 when the residual test passed */
+  double rel_residual;     /* sqrt(|r|^2 / |rhs|^2) at exit (Eigen's error()) */
+  int refinements;         /* MIXED: refinement sweeps used */
+} hobak_step_stats;
+
+typedef struct hobak_batch_t* hobak_batch;
+
+/* Library version and device check. */
+const char* hobak_version(void);
+const char* hobak_last_error(void);
+int hobak_device_check(int* sm_major, int* sm_minor, int* num_sms);
+
+/* Default options: tol 1e-8, 1000 iterations, FP64, block Jacobi, 3 refinements, graph on. */
+void hobak_default_solver_opts(hobak_solver_opts* opts);
+
+/* ---- batched API: many scenes packed into one device-resident batch ----
+ * Replaces one BACKWARD_EULER_VELOCITY per scene (BACKWARD_EULER_VELOCITY.cpp:31-46)
+ * with all scenes stepped together; each scene's result does not depend on
+ * the others (per-scene reductions, no cross-scene atomics). */
+int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_solver_opts* opts,
+                       hobak_batch* out);
+int hobak_batch_destroy(hobak_batch b);
+int hobak_batch_num_scenes(hobak_batch b, int* n);
+/* Advance every scene by nsteps BACKWARD_EULER_VELOCITY::solve steps
+ * (BACKWARD_EULER_VELOCITY.cpp:96-235).  State stays on the device.
+ * stats may be NULL or point at nscenes entries (stats of the last step). */
+int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats);
+/* Host <-> device state of one scene (3*nv doubles each; NULL skips). */
+int hobak_batch_set_state(hobak_batch b, int scene, const double* x, const double* v);
+int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v);
+/* Replace the external force vector (3*nv) of one scene; the default is M g. */
+int hobak_batch_set_external_forces(hobak_batch b, int scene, const double* f);
+int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts);
+/* Device memory held by the batch, in bytes. */
+int hobak_batch_device_bytes(hobak_batch b, long long* bytes);
+/* Mesh-wide hyperelastic energy sum(restVolume * psi(F)) of one scene
+ * (TET_MESH::computeHyperelasticEnergy, TET_MESH.cpp:719-731). */
+int hobak_batch_energy(hobak_batch b, int scene, double* energy);
+
+/* ---- single-scene API: the BACKWARD_EULER_VELOCITY drop-in ----
+ * A batch of one.  hobak_gpu_step uploads nothing and downloads nothing;
+ * pair it with set/get_state for host-side state like the reference's
+ * position()/velocity() references (TIMESTEPPER.h:53-58). */
+int hobak_gpu_create(const hobak_scene_desc* scene, const hobak_solver_opts* opts, hobak_batch* out);
+int hobak_gpu_step(hobak_batch b, int nsteps, hobak_step_stats* stats);
+int hobak_gpu_set_state(hobak_batch b, const double* x, const double* v);
+int hobak_gpu_get_state(hobak_batch b, double* x, double* v);
+int hobak_gpu_destroy(hobak_batch b);
+
+/* ---- element-level entry points (the VOLUME::HYPERELASTIC boundary) ----
+ * Batched, device-evaluated material and element terms for n deformation
+ * gradients / tets.  Host buffers in and out.  Any output may be NULL.
+ *   hobak_material_eval: psi(F) (HYPERELASTIC.h:36), PK1(F) (HYPERELASTIC.h:40),
+ *     clampedHessian (HYPERELASTIC.h:48), F column major (flatten,
+ *     MATRIX_UTIL.cpp:33-43), Hessians 81 per F, column major.
+ *   hobak_element_eval: per tet F = Ds DmInv (TET_MESH.cpp:706-714),
+ *     rotation-variant SVD (svd_rv, MATRIX_UTIL.cpp:76-95), element force
+ *     -V pFpx^T vec(P) (TET_MESH.cpp:736-747) and element Hessian
+ *     pFpx^T (-V clampedHessian) pFpx (TET_MESH_FASTER.cpp:95-103), 144 per
+ *     tet, column major. */
+int hobak_material_eval(const hobak_material* m, int n, const double* F, double* psi, double* P, double* H);
+int hobak_element_eval(int nv, int nt, const double* rest, const int* tets, const double* x,
+                       const hobak_material* m, double* F, double* sigma, double* force, double* hessian);
+/* Assembled stiffness of one scene at its current state: BSR pattern
+ * (rowptr nv+1, cols nblocks), K blocks (9 each, column major) and forces R
+ * (3*nv).  K and R follow TET_MESH_FASTER::computeHyperelasticClampedHessian
+ * (TET_MESH_FASTER.cpp:89-133) and TET_MESH::computeHyperelasticForces
+ * (TET_MESH.cpp:736-770).  Call with NULL outputs to query nblocks. */
+int hobak_batch_assemble(hobak_batch b, int scene, int* nblocks, int* rowptr, int* cols, double* K, double* R);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HOBAK_GPU_H */
