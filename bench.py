@@ -1,0 +1,314 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 implicit tet-FEM timestep (BACKWARD_EULER_VELOCITY).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+One "step" is one BACKWARD_EULER_VELOCITY::solve over the workload (all scenes
+of a batch).  Prints ONE JSON line (rank 0).  `value` is device-resident
+steps/s over the timed region (CUDA events on the library's stream, W warm-up
+steps first); `e2e` is the same metric through the public API with host
+buffers (pinned) copied in and out every step.  `--impl reference` times the
+CPU restatement of the reference algorithm (oracle/) on the host cores for the
+same workload.
+
+Workloads (synthetic, seeded; see hobakv1_gb300/scenes.py):
+  kuhn40_snh_twist   40^3 Kuhn cube, 384,000 tets, SNH E=1e4 nu=0.45, compressed 0.6 + twisted, FP64
+  kuhn40_arap_twist  same with ARAP
+  kuhn10_snh         10^3 Kuhn cube, 6,000 tets, SNH E=1e3 nu=0.45 (the CPU-runnable case)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "steps/s, p50/p99 step latency: batched mixed-precision vs plain FP64, same tol"
+WORKLOADS = {
+    "kuhn40_snh_twist": dict(kind="config2", N=40, material="snh", precision=0),
+    "kuhn40_arap_twist": dict(kind="config2", N=40, material="arap", precision=0),
+    "kuhn10_snh": dict(kind="config1", N=10, material="snh", precision=0),
+}
+DEFAULT_WORKLOAD = "kuhn40_snh_twist"
+
+
+def make_scenes(spec):
+    from hobakv1_gb300 import scenes
+    if spec["kind"] == "config2":
+        return [scenes.config2_scene(spec["N"], spec["material"])]
+    if spec["kind"] == "config1":
+        return [scenes.config1_scene(spec["N"], spec["material"])]
+    raise ValueError(spec)
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload):
+    """DRAM bytes per launch of each kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return json.load(f).get(workload, {})
+
+
+def cpu_baseline(scene_list, steps, warmup):
+    """The oracle (CPU restatement of the reference algorithm, OpenMP on all
+    host cores) on the same workload; bounded sample."""
+    from oracle import oracle
+    oracle.build()
+    sims = [oracle.Sim(s, precond=0) for s in scene_list]
+    for sim in sims:
+        sim.step(warmup) if warmup else None
+    t0 = time.perf_counter()
+    lat = []
+    for _ in range(steps):
+        ts = time.perf_counter()
+        for sim in sims:
+            sim.step(1)
+        lat.append(time.perf_counter() - ts)
+    dt = time.perf_counter() - t0
+    return steps / dt, lat, oracle.lib().oracle_threads()
+
+
+def run_reference(args, spec, scene_list):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    steps = max(1, min(args.steps, 5))
+    warm = 1 if args.warmup > 0 else 0
+    value, lat, cores = cpu_baseline(scene_list, steps, warm)
+    sample = f"{steps} timed steps after {warm} warm-up of {args.workload} ({len(scene_list)} scene(s))"
+    lat_ms = [1e3 * x for x in lat]
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": warm, "ms_per_step": 1e3 / value,
+            "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": args.workload,
+                                              **config_of(spec, scene_list, "jacobi (Eigen DiagonalPreconditioner)")},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(spec, scene_list, preconditioner="block_jacobi"):
+    return {"scenes": len(scene_list), "tets": int(sum(s.nt for s in scene_list)),
+            "verts": int(sum(s.nv for s in scene_list)),
+            "material": spec["material"], "precision": "fp64" if spec["precision"] == 0 else "mixed",
+            "pcg_tol": 1e-8, "pcg_max_iters": 1000, "preconditioner": preconditioner,
+            "l2": "per-step working set (element Hessians alone 276 MB at 40^3) exceeds the 129 MB L2; no flush"}
+
+
+def run_ours(args, spec, scene_list):
+    import torch
+    from hobakv1_gb300 import hobak
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    opts = hobak.solver_opts(precision=spec["precision"])
+    batch = hobak.BATCH(scene_list, opts)
+    stream = torch.cuda.ExternalStream(batch.stream_handle())
+
+    # ---- device-resident timed region ----
+    batch.step(args.warmup)
+    batch.enable_timing(True)
+    batch.phase_times()  # reset
+    launches0 = batch.launch_count()
+    iters = []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev[0].record(stream)
+    for k in range(args.steps):
+        st = batch.step(1)
+        iters.append(max(s[0] for s in st))
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    clock = clocks.stop()
+    gpu_launches = batch.launch_count() - launches0
+    phases = batch.phase_times()
+    lat = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[args.steps])
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1e3)
+
+    # ---- kernel rooflines: per-launch CUDA-event time of the hot kernels ----
+    kms = batch.time_kernels(reps=10)
+    kbytes = batch.kernel_bytes()
+    per_step_launches = {"element": 1, "assemble": 1, "spmv": float(np.mean(iters)) + 1,
+                         "pcg_update": float(np.mean(iters)) + 1}
+    share = {k: kms[k] * per_step_launches[k] for k in kms}
+    dominant = max(share, key=share.get)
+    peak, peak_kind = measured_peaks()
+    achieved = kbytes[dominant] / (kms[dominant] * 1e-3) / 1e9
+    traffic = ncu_traffic(args.workload).get(dominant)
+    roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes": kbytes[dominant], "launch_ms": kms[dominant],
+                "kernels": {k: {"launch_ms": kms[k], "GB/s": kbytes[k] / (kms[k] * 1e-3) / 1e9,
+                                "launches_per_step": per_step_launches[k]} for k in kms}}
+
+    # ---- e2e: public API with pinned host buffers in/out every step ----
+    nvs = [s.nv for s in scene_list]
+    host = [(torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy(),
+             torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy(),
+             torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy()) for n in nvs]
+    for i, (x, v, f) in enumerate(host):
+        xx, vv = batch.get_state(i)
+        x[:], v[:] = xx, vv
+        s = scene_list[i]
+        mass = np.zeros(s.nv)
+        np.add.at(mass, s.tets.reshape(-1), np.repeat(0.25 * np.abs(
+            np.einsum("ij,ij->i", s.rest[s.tets[:, 3]] - s.rest[s.tets[:, 0]],
+                      np.cross(s.rest[s.tets[:, 1]] - s.rest[s.tets[:, 0]],
+                               s.rest[s.tets[:, 2]] - s.rest[s.tets[:, 0]])) / 6.0), 4))
+        f[:] = (mass[:, None] * (s.density * np.array(s.gravity))[None, :]).reshape(-1)
+    e2e_steps = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        for i, (x, v, f) in enumerate(host):
+            batch.set_state(i, x, v)
+            batch.set_external_forces(i, f)
+        batch.step(1)
+        for i, (x, v, f) in enumerate(host):
+            xx, vv = batch.get_state(i)
+            x[:], v[:] = xx, vv
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    nbytes = sum(nvs) * 3 * 8
+    e2e = {"value": world * e2e_steps / (e2e_ms / 1e3), "unit": "steps/s",
+           "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": 2 * nbytes + 32 * len(nvs),
+           "api": "hobak_batch_set_state/set_external_forces/step/get_state"}
+
+    # ---- CPU baseline (rank 0, N = 1 only) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        steps = 3 if sum(s.nt for s in scene_list) > 100_000 else 20
+        cv, _, cores = cpu_baseline(scene_list, steps, 0)
+        cpu = {"value": cv, "unit": "steps/s", "cores": cores, "kind": "port",
+               "sample": f"{steps} steps of {args.workload} on the host cores (OpenMP), from the initial state"}
+
+    if rank == 0:
+        lat_sorted = sorted(lat)
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+                "p50_ms": float(np.percentile(lat_sorted, 50)), "p99_ms": float(np.percentile(lat_sorted, 99)),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if spec["precision"] == 0 else "f32+f64", "data": "synthetic",
+                "config": {"workload": args.workload, **config_of(spec, scene_list)},
+                "pcg_iters_per_step": float(np.mean(iters)),
+                "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(gpu_launches),
+                "clocks": clock}
+        print(json.dumps(line), flush=True)
+    batch.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    spec = WORKLOADS[args.workload]
+    scene_list = make_scenes(spec)
+    if args.impl == "reference":
+        run_reference(args, spec, scene_list)
+    else:
+        run_ours(args, spec, scene_list)
+
+
+if __name__ == "__main__":
+    main()

@@ -63,6 +63,12 @@ SIGNATURES = {
     "hobak_element_eval": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp,
                                           ctypes.POINTER(HobakMaterial), _dp, _dp, _dp, _dp]),
     "hobak_batch_assemble": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _ip, _dp, _dp]),
+    "hobak_batch_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "hobak_batch_enable_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "hobak_batch_phase_times": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_longlong)]),
+    "hobak_batch_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "hobak_batch_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    "hobak_batch_kernel_bytes": (ctypes.c_int, [ctypes.c_void_p, _dp]),
 }
 
 _lib = None

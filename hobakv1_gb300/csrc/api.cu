@@ -73,6 +73,12 @@ struct hobak_batch_t {
   int lastStatus = HOBAK_OK;
   std::vector<SolveState> lastSolve;
   std::vector<int> hostRowptr, hostCols;
+  int* pinnedActive = nullptr;   // pinned host word for the convergence poll
+  long long launches = 0;        // kernels launched by this batch
+  bool timing = false;
+  cudaEvent_t ev[6] = {};
+  double phaseMs[5] = {0, 0, 0, 0, 0};
+  long long phaseLaunches[5] = {0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -461,26 +467,28 @@ int ensure_chunk_graph(hobak_batch_t* B) {
 int run_step(hobak_batch_t* B) {
   DeviceBatch& d = B->d;
   cudaStream_t s = B->stream;
+  const bool T = B->timing;
+  if (T) CUDA_TRY(cudaEventRecord(B->ev[0], s));
   launch_begin_step(d, s);
   launch_element(d, s);
+  if (T) CUDA_TRY(cudaEventRecord(B->ev[1], s));
   launch_assemble(d, s);
   launch_diag_inverse(d, B->opts.preconditioner, s);
+  if (T) CUDA_TRY(cudaEventRecord(B->ev[2], s));
   const int n = (int)B->scenes.size();
-  CUDA_TRY(cudaMemcpyAsync(d.active, &n, sizeof(int), cudaMemcpyHostToDevice, s));
+  *B->pinnedActive = n;
+  CUDA_TRY(cudaMemcpyAsync(d.active, B->pinnedActive, sizeof(int), cudaMemcpyHostToDevice, s));
   launch_pcg_init(d, s);
-  int h_active = n;
+  if (T) CUDA_TRY(cudaEventRecord(B->ev[3], s));
   int iters = 0;
   if (B->opts.use_graph) {
     int rc = ensure_chunk_graph(B);
     if (rc) return rc;
   }
-  int* pinnedActive = nullptr;
-  CUDA_TRY(cudaMallocHost(&pinnedActive, sizeof(int)));
   while (true) {
-    CUDA_TRY(cudaMemcpyAsync(pinnedActive, d.active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(B->pinnedActive, d.active, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
-    h_active = *pinnedActive;
-    if (h_active <= 0 || iters >= B->opts.max_iters) break;
+    if (*B->pinnedActive <= 0 || iters >= B->opts.max_iters) break;
     if (B->opts.use_graph) {
       CUDA_TRY(cudaGraphLaunch(B->chunkGraph, s));
     } else {
@@ -491,9 +499,22 @@ int run_step(hobak_batch_t* B) {
     }
     iters += kChunk;
   }
-  cudaFreeHost(pinnedActive);
+  if (T) CUDA_TRY(cudaEventRecord(B->ev[4], s));
   launch_finish_step(d, s);
+  if (T) CUDA_TRY(cudaEventRecord(B->ev[5], s));
   CUDA_TRY(cudaGetLastError());
+  const long long pcgLaunches = 2LL * iters;
+  const long long phase[5] = {2, 2, 1, pcgLaunches, 1};
+  for (int k = 0; k < 5; k++) B->phaseLaunches[k] += phase[k];
+  B->launches += 6 + pcgLaunches;
+  if (T) {
+    CUDA_TRY(cudaEventSynchronize(B->ev[5]));
+    for (int k = 0; k < 5; k++) {
+      float ms = 0;
+      CUDA_TRY(cudaEventElapsedTime(&ms, B->ev[k], B->ev[k + 1]));
+      B->phaseMs[k] += ms;
+    }
+  }
   return HOBAK_OK;
 }
 
@@ -546,6 +567,8 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
   else
     hobak_default_solver_opts(&B->opts);
   CUDA_TRY(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaMallocHost(&B->pinnedActive, sizeof(int)));
+  for (auto& e : B->ev) CUDA_TRY(cudaEventCreate(&e));
   if ((rc = build_batch(B.get(), scenes, nscenes))) {
     hobak_batch_destroy(B.release());
     return rc;
@@ -561,6 +584,9 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
 int hobak_batch_destroy(hobak_batch b) {
   if (!b) return HOBAK_OK;
   if (b->chunkGraph) cudaGraphExecDestroy(b->chunkGraph);
+  for (auto& e : b->ev)
+    if (e) cudaEventDestroy(e);
+  if (b->pinnedActive) cudaFreeHost(b->pinnedActive);
   if (b->arena) cudaFree(b->arena);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -654,6 +680,85 @@ int hobak_batch_energy(hobak_batch b, int scene, double* energy) {
   double e = 0;
   for (double p : psi) e += p;
   *energy = e;
+  return HOBAK_OK;
+}
+
+int hobak_batch_get_stream(hobak_batch b, void** stream) {
+  if (!b || !stream) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  *stream = (void*)b->stream;
+  return HOBAK_OK;
+}
+
+int hobak_batch_enable_timing(hobak_batch b, int on) {
+  if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
+  b->timing = on != 0;
+  return HOBAK_OK;
+}
+
+int hobak_batch_phase_times(hobak_batch b, double* ms, long long* launches) {
+  if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
+  for (int k = 0; k < 5; k++) {
+    if (ms) ms[k] = b->phaseMs[k];
+    if (launches) launches[k] = b->phaseLaunches[k];
+    b->phaseMs[k] = 0;
+    b->phaseLaunches[k] = 0;
+  }
+  return HOBAK_OK;
+}
+
+int hobak_batch_launch_count(hobak_batch b, long long* launches) {
+  if (!b || !launches) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  *launches = b->launches;
+  return HOBAK_OK;
+}
+
+int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
+  if (!b || !ms || reps <= 0) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  const DeviceBatch& d = b->d;
+  cudaStream_t s = b->stream;
+  // keep every scene's PCG "running" so spmv/update do their full work
+  const int n = (int)b->scenes.size();
+  std::vector<SolveState> st(n);
+  CUDA_TRY(cudaMemcpy(st.data(), d.solve, sizeof(SolveState) * n, cudaMemcpyDeviceToHost));
+  for (auto& x : st) {
+    x.done = 0;
+    x.threshold = -1.0;
+    x.maxit = 0x7fffffff;
+    if (!(x.alpha == x.alpha)) x.alpha = 0.0;
+    if (!(x.beta == x.beta)) x.beta = 0.0;
+  }
+  CUDA_TRY(cudaMemcpy(d.solve, st.data(), sizeof(SolveState) * n, cudaMemcpyHostToDevice));
+  cudaEvent_t e0 = b->ev[0], e1 = b->ev[1];
+  for (int k = 0; k < 4; k++) {
+    CUDA_TRY(cudaEventRecord(e0, s));
+    for (int r = 0; r < reps; r++) {
+      if (k == 0) launch_element(d, s);
+      else if (k == 1) launch_assemble(d, s);
+      else if (k == 2) launch_spmv(d, d.p0, d.p1, s);
+      else launch_update(d, d.p1, s);
+    }
+    CUDA_TRY(cudaEventRecord(e1, s));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    float t = 0;
+    CUDA_TRY(cudaEventElapsedTime(&t, e0, e1));
+    ms[k] = t / reps;
+  }
+  b->launches += 4LL * reps;
+  CUDA_TRY(cudaGetLastError());
+  return upload_solver_opts(b);
+}
+
+int hobak_batch_kernel_bytes(hobak_batch b, double* bytes) {
+  if (!b || !bytes) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  const double T = b->nt, V = b->nv, B = b->nblocks, C = 16.0 * b->nt;
+  // element: tets 16, 4 x (rest, x, v) 288, DmInv 72, vol 8, scene id 4; writes 90 + 12 doubles
+  bytes[0] = T * (16 + 288 + 72 + 8 + 4 + 8.0 * (kElemHess + 12));
+  // assembly: element Hessians once, contribution map, block ids, LHS write; mask/mass per vertex
+  bytes[1] = T * 8.0 * kElemHess + C * 4 + B * (4 + 4 + 4 + 72) + V * (1 + 8 + 4);
+  // spmv: LHS 72 + col 4 per block; rowptr, z, pOld read and pNew, Ap written per vertex
+  bytes[2] = B * 76 + V * (4 + 24 * 4);
+  // update: y rw, p, r rw, Ap, Minv (72), z write per vertex
+  bytes[3] = V * (48 + 24 + 48 + 24 + 72 + 24);
   return HOBAK_OK;
 }
 

@@ -70,6 +70,8 @@ void launch_assemble(const DeviceBatch& b, cudaStream_t s);
 void launch_diag_inverse(const DeviceBatch& b, int precond, cudaStream_t s);
 void launch_pcg_init(const DeviceBatch& b, cudaStream_t s);
 void launch_pcg_iteration(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s);
+void launch_spmv(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s);
+void launch_update(const DeviceBatch& b, const double* p, cudaStream_t s);
 void launch_finish_step(const DeviceBatch& b, cudaStream_t s);
 void launch_energy(const DeviceBatch& b, cudaStream_t s);
 

@@ -386,9 +386,17 @@ void launch_diag_inverse(const DeviceBatch& b, int precond, cudaStream_t s) {
 
 void launch_pcg_init(const DeviceBatch& b, cudaStream_t s) { k_pcg_init<<<b.ntiles, kTileV, 0, s>>>(b); }
 
-void launch_pcg_iteration(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s) {
+void launch_spmv(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s) {
   k_spmv<<<b.ntiles, kSpmvThreads, 0, s>>>(b, pOld, pNew);
-  k_update<<<b.ntiles, kTileV, 0, s>>>(b, pNew);
+}
+
+void launch_update(const DeviceBatch& b, const double* p, cudaStream_t s) {
+  k_update<<<b.ntiles, kTileV, 0, s>>>(b, p);
+}
+
+void launch_pcg_iteration(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s) {
+  launch_spmv(b, pOld, pNew, s);
+  launch_update(b, pNew, s);
 }
 
 void launch_finish_step(const DeviceBatch& b, cudaStream_t s) {

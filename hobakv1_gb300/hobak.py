@@ -277,6 +277,39 @@ class BATCH:
               "hobak_batch_assemble")
         return rowptr, cols, K.reshape(-1, 9), R
 
+    # ---- measurement ----
+    KERNELS = ("element", "assemble", "spmv", "pcg_update")
+    PHASES = ("element", "assembly", "pcg_init", "pcg_iterations", "update")
+
+    def stream_handle(self) -> int:
+        p = ctypes.c_void_p()
+        check(_lib.load().hobak_batch_get_stream(self.h, ctypes.byref(p)), "hobak_batch_get_stream")
+        return p.value or 0
+
+    def enable_timing(self, on: bool = True):
+        check(_lib.load().hobak_batch_enable_timing(self.h, int(on)), "hobak_batch_enable_timing")
+
+    def phase_times(self):
+        ms = np.zeros(5)
+        n = (ctypes.c_longlong * 5)()
+        check(_lib.load().hobak_batch_phase_times(self.h, dptr(ms), n), "hobak_batch_phase_times")
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PHASES)}
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        check(_lib.load().hobak_batch_launch_count(self.h, ctypes.byref(n)), "hobak_batch_launch_count")
+        return n.value
+
+    def time_kernels(self, reps: int = 20):
+        ms = np.zeros(4)
+        check(_lib.load().hobak_batch_time_kernels(self.h, reps, dptr(ms)), "hobak_batch_time_kernels")
+        return dict(zip(self.KERNELS, ms.tolist()))
+
+    def kernel_bytes(self):
+        b = np.zeros(4)
+        check(_lib.load().hobak_batch_kernel_bytes(self.h, dptr(b)), "hobak_batch_kernel_bytes")
+        return dict(zip(self.KERNELS, b.tolist()))
+
     def close(self):
         if getattr(self, "h", None) and self.h.value:
             _lib.load().hobak_batch_destroy(self.h)

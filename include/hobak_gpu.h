@@ -161,6 +161,25 @@ int hobak_element_eval(int nv, int nt, const double* rest, const int* tets, cons
  * (TET_MESH.cpp:736-770).  Call with NULL outputs to query nblocks. */
 int hobak_batch_assemble(hobak_batch b, int scene, int* nblocks, int* rowptr, int* cols, double* K, double* R);
 
+/* ---- measurement (no reference counterpart; the reference's TIMER,
+ * util/TIMER.h:33-76, is replaced by CUDA events) ---- */
+/* The CUDA stream (a cudaStream_t) all work of the batch is issued on. */
+int hobak_batch_get_stream(hobak_batch b, void** stream);
+/* Phase timers: when on, every step records CUDA events around its phases.
+ * hobak_batch_phase_times returns, since the last call, the summed ms and the
+ * kernel launches of the 5 phases: [element, assembly+preconditioner,
+ * rhs+pcg init, pcg iterations, update], then resets them. */
+int hobak_batch_enable_timing(hobak_batch b, int on);
+int hobak_batch_phase_times(hobak_batch b, double* ms, long long* launches);
+/* Kernels launched by this batch since creation. */
+int hobak_batch_launch_count(hobak_batch b, long long* launches);
+/* Per-launch device time (ms, CUDA events, reps back-to-back launches on the
+ * batch stream, at the current state) of the hot kernels
+ * [element, assembly, spmv, pcg update], and their algorithmic bytes per
+ * launch (every array counted once). */
+int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms);
+int hobak_batch_kernel_bytes(hobak_batch b, double* bytes);
+
 #ifdef __cplusplus
 }
 #endif
