@@ -1,0 +1,64 @@
+// Drives the C++ mirror (hobakv1_gb300/cpp/HOBAK_GPU.h) the way a reference
+// scene drives BACKWARD_EULER_VELOCITY (SIMULATION_SCENE::stepSimulation,
+// Scenes/SIMULATION_SCENE.h:120-126): zero external forces, add gravity,
+// solve, read position().  Reads a mesh and state from raw binary files and
+// writes the final displacement, so a test can compare it with the oracle.
+//
+//   bev_gpu_example <in.bin> <out.bin> <steps>
+// in.bin: int nv, int nt, int npinned, int material, double mu, lambda,
+//         density, dt, rest[3nv], tets[4nt] (int), pinned[npinned] (int), x0[3nv]
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "../../hobakv1_gb300/cpp/HOBAK_GPU.h"
+
+using namespace HOBAK_GPU;
+
+int main(int argc, char** argv) {
+  if (argc != 4) {
+    std::fprintf(stderr, "usage: %s in.bin out.bin steps\n", argv[0]);
+    return 2;
+  }
+  FILE* f = std::fopen(argv[1], "rb");
+  if (!f) return 2;
+  int hdr[4];
+  double prm[4];
+  if (std::fread(hdr, sizeof(int), 4, f) != 4 || std::fread(prm, sizeof(double), 4, f) != 4) return 2;
+  const int nv = hdr[0], nt = hdr[1], np = hdr[2], kind = hdr[3];
+  std::vector<double> rest(3 * nv), x0(3 * nv);
+  std::vector<int> tets(4 * nt), pinned(np);
+  if (std::fread(rest.data(), 8, rest.size(), f) != rest.size() || std::fread(tets.data(), 4, tets.size(), f) != tets.size() ||
+      std::fread(pinned.data(), 4, pinned.size(), f) != pinned.size() || std::fread(x0.data(), 8, x0.size(), f) != x0.size())
+    return 2;
+  std::fclose(f);
+
+  std::vector<VECTOR3> restV(nv);
+  for (int i = 0; i < nv; i++) restV[i] = {rest[3 * i], rest[3 * i + 1], rest[3 * i + 2]};
+  std::vector<VECTOR4I> tetV(nt);
+  for (int t = 0; t < nt; t++) tetV[t] = {tets[4 * t], tets[4 * t + 1], tets[4 * t + 2], tets[4 * t + 3]};
+  TET_MESH mesh(restV, tetV);
+  VOLUME::SNH snh(prm[0], prm[1]);
+  VOLUME::ARAP arap(prm[0], prm[1]);
+  VOLUME::HYPERELASTIC& material = (kind == HOBAK_MATERIAL_ARAP) ? (VOLUME::HYPERELASTIC&)arap : snh;
+
+  TIMESTEPPER::BACKWARD_EULER_VELOCITY solver(mesh, material);
+  solver.setDt(prm[3]);
+  solver.scaleMass(prm[2]);
+  solver.position() = x0;
+  solver.attachKinematicConstraints(pinned);
+  const VECTOR3 gravity = {0.0, -9.8 * prm[2], 0.0};
+  for (int s = 0; s < std::atoi(argv[3]); s++) {
+    std::fill(solver.externalForces().begin(), solver.externalForces().end(), 0.0);
+    solver.addGravity(gravity);
+    if (!solver.solve(false)) {
+      std::fprintf(stderr, "solve failed: %s\n", solver.lastError().c_str());
+      return 1;
+    }
+  }
+  FILE* o = std::fopen(argv[2], "wb");
+  std::fwrite(solver.position().data(), 8, solver.position().size(), o);
+  std::fclose(o);
+  std::printf("steps %d last PCG iterations %d\n", solver.currentTimestep(), solver.lastSolveStats().iterations);
+  return 0;
+}
