@@ -69,6 +69,10 @@ SIGNATURES = {
     "hobak_batch_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "hobak_batch_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "hobak_batch_kernel_bytes": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "hobak_element_eval_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.POINTER(HobakMaterial), ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p]),
 }
 
 _lib = None

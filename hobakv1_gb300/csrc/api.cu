@@ -26,6 +26,14 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+}  // namespace
+
+namespace hobak {
+int record_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace hobak
+
+namespace {
+
 #define CUDA_TRY(expr)                                                                          \
   do {                                                                                          \
     cudaError_t _e = (expr);                                                                    \

@@ -161,6 +161,26 @@ int hobak_element_eval(int nv, int nt, const double* rest, const int* tets, cons
  * (TET_MESH.cpp:736-770).  Call with NULL outputs to query nblocks. */
 int hobak_batch_assemble(hobak_batch b, int scene, int* nblocks, int* rowptr, int* cols, double* K, double* R);
 
+/* ---- allocation-free element evaluation (no counterpart in the reference) ----
+ * For callers that cannot let a library call cudaMalloc/cudaFree: plugins in
+ * hosts that own the device-memory budget, or per-frame loops where an
+ * allocation would synchronise the device.  Same results as
+ * hobak_element_eval, but every array argument is a DEVICE pointer the caller
+ * owns (tets 16-byte aligned), `stream` is a cudaStream_t (NULL = default
+ * stream), and the call allocates nothing: its per-tet rest-shape scratch
+ * lives in one static device array of HOBAK_NOALLOC_MAX_TETS tets (10 MiB),
+ * held by every GPU that loads the library until the process exits.  Larger
+ * calls return HOBAK_ERR_INVALID.  The first call on a device looks up that
+ * array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array: calls whose work overlaps on the GPU
+ * race and must be serialised by the caller.  Returns once its work on
+ * `stream` is done; a tet naming a vertex outside [0, nv) is reported as
+ * HOBAK_ERR_INVALID before any element is evaluated. */
+#define HOBAK_NOALLOC_MAX_TETS 131072
+int hobak_element_eval_noalloc(int nv, int nt, const double* rest, const int* tets, const double* x,
+                               const hobak_material* m, double* F, double* sigma, double* force, double* hessian,
+                               void* stream);
+
 /* ---- measurement (no reference counterpart; the reference's TIMER,
  * util/TIMER.h:33-76, is replaced by CUDA events) ---- */
 /* The CUDA stream (a cudaStream_t) all work of the batch is issued on. */
