@@ -76,8 +76,9 @@ struct hobak_batch_t {
   void* arena = nullptr;
   size_t arenaBytes = 0;
   cudaStream_t stream = nullptr;
-  cudaGraphExec_t chunkGraph = nullptr;
-  int chunkIters = 0;
+  cudaStream_t captureStream = nullptr;  // fills the bodies of captured while loops
+  cudaGraphExec_t stepGraph[2] = {nullptr, nullptr};  // untimed, timed
+  long long eagerChunks = 0;
   int lastStatus = HOBAK_OK;
   std::vector<SolveState> lastSolve;
   std::vector<int> hostRowptr, hostCols;
@@ -91,7 +92,7 @@ struct hobak_batch_t {
 
 namespace {
 
-constexpr int kChunk = 16;  // PCG iterations between host convergence checks (even)
+constexpr int kChunk = 8;  // PCG iterations per loop body (graph) or per host poll (eager)
 
 double tet_volume(const double* x0, const double* x1, const double* x2, const double* x3) {
   const double d1[3] = {x1[0] - x0[0], x1[1] - x0[1], x1[2] - x0[2]};
@@ -330,6 +331,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oScenes = A.reserve(sizeof(SceneParams) * n);
   const size_t oSolve = A.reserve(sizeof(SolveState) * n);
   const size_t oActive = A.reserve(sizeof(int));
+  const size_t oBodyRuns = A.reserve(sizeof(unsigned long long));
   const size_t oRest = A.reserve(V3), oX = A.reserve(V3), oV = A.reserve(V3), oF = A.reserve(V3);
   const size_t oMass = A.reserve(sizeof(double) * nv), oFree = A.reserve(nv), oPin = A.reserve(V3);
   const size_t oVS = A.reserve(sizeof(int) * nv);
@@ -342,12 +344,20 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oTileS = A.reserve(sizeof(int) * ntiles), oTile0 = A.reserve(sizeof(int) * ntiles);
   const size_t oTile1 = A.reserve(sizeof(int) * ntiles);
   const size_t oEH = A.reserve(sizeof(double) * kElemHess * (size_t)nt);
+  const size_t oEHf = A.reserve(sizeof(float) * kElemHess * (size_t)nt);
   const size_t oEG = A.reserve(sizeof(double) * 12 * (size_t)nt);
+  const size_t oRhs = A.reserve(V3), oY = A.reserve(V3), oR64 = A.reserve(V3);
+  // FP64 inner solve (r = r64, d = y)
   const size_t oLhs = A.reserve(sizeof(double) * 9 * (size_t)nblocks);
   const size_t oMinv = A.reserve(sizeof(double) * 9 * (size_t)nv);
-  const size_t oRhs = A.reserve(V3), oY = A.reserve(V3), oR = A.reserve(V3), oZ = A.reserve(V3);
-  const size_t oP0 = A.reserve(V3), oP1 = A.reserve(V3), oAp = A.reserve(V3);
-  const size_t oPart = A.reserve(sizeof(double) * 2 * (size_t)ntiles);
+  const size_t oU = A.reserve(V3), oP = A.reserve(V3), oS = A.reserve(V3), oW = A.reserve(V3);
+  // FP32 inner solve (mixed precision)
+  const size_t F3 = 3 * (size_t)nv * sizeof(float);
+  const size_t oLhsF = A.reserve(sizeof(float) * 9 * (size_t)nblocks);
+  const size_t oMinvF = A.reserve(sizeof(float) * 9 * (size_t)nv);
+  const size_t oRF = A.reserve(F3), oUF = A.reserve(F3), oPF = A.reserve(F3), oSF = A.reserve(F3);
+  const size_t oWF = A.reserve(F3), oDF = A.reserve(F3);
+  const size_t oPart = A.reserve(sizeof(double) * kPartials * (size_t)ntiles);
   const size_t oPsi = A.reserve(sizeof(double) * nt);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, A.used);
@@ -367,6 +377,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.scenes = carve<SceneParams>(base, oScenes);
   d.solve = carve<SolveState>(base, oSolve);
   d.active = carve<int>(base, oActive);
+  d.bodyRuns = carve<unsigned long long>(base, oBodyRuns);
   d.rest = carve<double>(base, oRest);
   d.x = carve<double>(base, oX);
   d.v = carve<double>(base, oV);
@@ -390,16 +401,17 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.tileV0 = carve<int>(base, oTile0);
   d.tileV1 = carve<int>(base, oTile1);
   d.elemH = carve<double>(base, oEH);
+  d.elemHf = carve<float>(base, oEHf);
   d.elemG = carve<double>(base, oEG);
-  d.lhs = carve<double>(base, oLhs);
-  d.minv = carve<double>(base, oMinv);
   d.rhs = carve<double>(base, oRhs);
   d.y = carve<double>(base, oY);
-  d.r = carve<double>(base, oR);
-  d.z = carve<double>(base, oZ);
-  d.p0 = carve<double>(base, oP0);
-  d.p1 = carve<double>(base, oP1);
-  d.Ap = carve<double>(base, oAp);
+  d.r64 = carve<double>(base, oR64);
+  d.v64 = PcgVecs<double>{carve<double>(base, oLhs), carve<double>(base, oMinv), d.r64,
+                          carve<double>(base, oU), carve<double>(base, oP), carve<double>(base, oS),
+                          carve<double>(base, oW), d.y};
+  d.v32 = PcgVecs<float>{carve<float>(base, oLhsF), carve<float>(base, oMinvF), carve<float>(base, oRF),
+                         carve<float>(base, oUF), carve<float>(base, oPF), carve<float>(base, oSF),
+                         carve<float>(base, oWF), carve<float>(base, oDF)};
   d.partial = carve<double>(base, oPart);
   d.psi = carve<double>(base, oPsi);
 
@@ -434,12 +446,15 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   return HOBAK_OK;
 }
 
+int sweeps_of(const hobak_solver_opts& o);
+
 int upload_solver_opts(hobak_batch_t* B) {
   std::vector<SolveState> st(B->scenes.size());
   for (auto& s : st) {
     std::memset(&s, 0, sizeof(s));
     s.tol = B->opts.tol;
     s.maxit = B->opts.max_iters;
+    s.maxSweeps = sweeps_of(B->opts);
   }
   CUDA_TRY(cudaMemcpy(B->d.solve, st.data(), sizeof(SolveState) * st.size(), cudaMemcpyHostToDevice));
   return HOBAK_OK;
@@ -456,73 +471,171 @@ int check_opts(const hobak_solver_opts* o) {
   return HOBAK_OK;
 }
 
-// Capture kChunk PCG iterations (p ping-pong fixed) as one graph.
-int ensure_chunk_graph(hobak_batch_t* B) {
-  if (B->chunkGraph) return HOBAK_OK;
-  cudaGraph_t g = nullptr;
-  CUDA_TRY(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
-  for (int c = 0; c < kChunk; c += 2) {
-    launch_pcg_iteration(B->d, B->d.p0, B->d.p1, B->stream);
-    launch_pcg_iteration(B->d, B->d.p1, B->d.p0, B->stream);
-  }
-  CUDA_TRY(cudaStreamEndCapture(B->stream, &g));
-  cudaError_t e = cudaGraphInstantiate(&B->chunkGraph, g, 0);
-  cudaGraphDestroy(g);
-  if (e != cudaSuccess) return fail(HOBAK_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+int sweeps_of(const hobak_solver_opts& o) {
+  return o.precision == HOBAK_PRECISION_MIXED ? 1 + o.max_refinements : 1;
+}
+
+// Kernels launched per step outside the PCG loop bodies.
+long long fixed_launches(const hobak_batch_t* B) {
+  const int sweeps = sweeps_of(B->opts);
+  const bool mixed = B->opts.precision == HOBAK_PRECISION_MIXED;
+  return 6 + sweeps * (2 + (mixed ? 2 : 0));
+}
+
+// One PCG chunk: kChunk iterations (2 kernels each).
+template <typename T>
+void enqueue_chunk(const DeviceBatch& d, const PcgVecs<T>& v, cudaStream_t s) {
+  for (int c = 0; c < kChunk; c++) launch_pcg_iteration<T>(d, v, s);
+}
+
+// While-loop node on the capturing stream `s`: body = one chunk followed by
+// k_continue, which keeps the loop going while any scene's inner PCG runs.
+template <typename T>
+int capture_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t capG = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CUDA_TRY(cudaStreamGetCaptureInfo(s, &cs, nullptr, &capG, &deps, nullptr, &nd));
+  if (cs != cudaStreamCaptureStatusActive) return fail(HOBAK_ERR_CUDA, "stream is not capturing");
+  cudaGraphConditionalHandle h;
+  CUDA_TRY(cudaGraphConditionalHandleCreate(&h, capG, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  CUDA_TRY(cudaGraphAddNode(&node, capG, deps, nullptr, nd, &p));
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  CUDA_TRY(cudaStreamBeginCaptureToGraph(B->captureStream, body, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+  enqueue_chunk<T>(B->d, v, B->captureStream);
+  launch_continue(B->d, (unsigned long long)h, B->captureStream);
+  cudaGraph_t out = nullptr;
+  CUDA_TRY(cudaStreamEndCapture(B->captureStream, &out));
   return HOBAK_OK;
 }
 
-int run_step(hobak_batch_t* B) {
-  DeviceBatch& d = B->d;
-  cudaStream_t s = B->stream;
-  const bool T = B->timing;
-  if (T) CUDA_TRY(cudaEventRecord(B->ev[0], s));
-  launch_begin_step(d, s);
-  launch_element(d, s);
-  if (T) CUDA_TRY(cudaEventRecord(B->ev[1], s));
-  launch_assemble(d, s);
-  launch_diag_inverse(d, B->opts.preconditioner, s);
-  if (T) CUDA_TRY(cudaEventRecord(B->ev[2], s));
-  const int n = (int)B->scenes.size();
-  *B->pinnedActive = n;
-  CUDA_TRY(cudaMemcpyAsync(d.active, B->pinnedActive, sizeof(int), cudaMemcpyHostToDevice, s));
-  launch_pcg_init(d, s);
-  if (T) CUDA_TRY(cudaEventRecord(B->ev[3], s));
-  int iters = 0;
-  if (B->opts.use_graph) {
-    int rc = ensure_chunk_graph(B);
-    if (rc) return rc;
-  }
-  while (true) {
-    CUDA_TRY(cudaMemcpyAsync(B->pinnedActive, d.active, sizeof(int), cudaMemcpyDeviceToHost, s));
+// Eager loop: chunks until the device reports no running scene (host polls).
+template <typename T>
+int eager_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
+  for (int iters = 0; iters <= B->opts.max_iters; iters += kChunk) {
+    CUDA_TRY(cudaMemcpyAsync(B->pinnedActive, B->d.active, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
-    if (*B->pinnedActive <= 0 || iters >= B->opts.max_iters) break;
+    if (*B->pinnedActive <= 0) break;
+    enqueue_chunk<T>(B->d, v, s);
+    B->eagerChunks++;
+  }
+  return HOBAK_OK;
+}
+
+// One BACKWARD_EULER_VELOCITY step: element terms, assembly, preconditioner,
+// rhs, then per sweep an inner PCG (and, mixed, the FP64 refinement), update.
+// `capture` builds the device-side loops of a graph; otherwise loops poll.
+template <typename T>
+int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, const PcgVecs<T>& v) {
+  const DeviceBatch& d = B->d;
+  const bool mixed = sizeof(T) == sizeof(float);
+  if (timed) CUDA_TRY(cudaEventRecord(B->ev[0], s));
+  launch_begin_step(d, s);
+  if (mixed) launch_element_mixed(d, s);
+  else launch_element(d, s);
+  if (timed) CUDA_TRY(cudaEventRecord(B->ev[1], s));
+  launch_assemble<T>(d, v, s);
+  launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
+  if (timed) CUDA_TRY(cudaEventRecord(B->ev[2], s));
+  launch_rhs(d, s);
+  if (timed) CUDA_TRY(cudaEventRecord(B->ev[3], s));
+  const int sweeps = sweeps_of(B->opts);
+  for (int k = 0; k < sweeps; k++) {
+    launch_set_active(d, s);
+    launch_inner_init<T>(d, v, s);
+    int rc = capture ? capture_pcg_loop<T>(B, s, v) : eager_pcg_loop<T>(B, s, v);
+    if (rc) return rc;
+    if (mixed) launch_refine(d, s);
+  }
+  if (timed) CUDA_TRY(cudaEventRecord(B->ev[4], s));
+  launch_finish_step(d, s);
+  if (timed) CUDA_TRY(cudaEventRecord(B->ev[5], s));
+  return HOBAK_OK;
+}
+
+int enqueue_step(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed) {
+  if (B->opts.precision == HOBAK_PRECISION_MIXED) return enqueue_step_t<float>(B, s, capture, timed, B->d.v32);
+  return enqueue_step_t<double>(B, s, capture, timed, B->d.v64);
+}
+
+// The whole step as one graph (device-side while loops over PCG chunks), one
+// instance per timing mode, built on first use.
+int ensure_step_graph(hobak_batch_t* B, bool timed) {
+  cudaGraphExec_t& exec = B->stepGraph[timed ? 1 : 0];
+  if (exec) return HOBAK_OK;
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_step(B, B->stream, true, timed);
+  cudaError_t e = cudaStreamEndCapture(B->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(HOBAK_ERR_CUDA, std::string("step graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    exec = nullptr;
+    return fail(HOBAK_ERR_CUDA, std::string("step graph instantiate: ") + cudaGetErrorString(e));
+  }
+  return HOBAK_OK;
+}
+
+void drop_graphs(hobak_batch_t* B) {
+  for (auto& g : B->stepGraph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+// Enqueue nsteps steps; with graphs nothing waits on the host in between.
+int run_steps(hobak_batch_t* B, int nsteps) {
+  cudaStream_t s = B->stream;
+  const bool timed = B->timing;
+  for (int k = 0; k < nsteps; k++) {
     if (B->opts.use_graph) {
-      CUDA_TRY(cudaGraphLaunch(B->chunkGraph, s));
+      int rc = ensure_step_graph(B, timed);
+      if (rc) return rc;
+      CUDA_TRY(cudaGraphLaunch(B->stepGraph[timed ? 1 : 0], s));
     } else {
-      for (int c = 0; c < kChunk; c += 2) {
-        launch_pcg_iteration(d, d.p0, d.p1, s);
-        launch_pcg_iteration(d, d.p1, d.p0, s);
+      int rc = enqueue_step(B, s, false, timed);
+      if (rc) return rc;
+    }
+    B->launches += fixed_launches(B);
+    B->phaseLaunches[0] += 2;
+    B->phaseLaunches[1] += 2;
+    B->phaseLaunches[2] += 1;
+    B->phaseLaunches[3] += fixed_launches(B) - 6;
+    B->phaseLaunches[4] += 1;
+    if (timed) {
+      CUDA_TRY(cudaEventSynchronize(B->ev[5]));
+      for (int i = 0; i < 5; i++) {
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, B->ev[i], B->ev[i + 1]));
+        B->phaseMs[i] += ms;
       }
     }
-    iters += kChunk;
   }
-  if (T) CUDA_TRY(cudaEventRecord(B->ev[4], s));
-  launch_finish_step(d, s);
-  if (T) CUDA_TRY(cudaEventRecord(B->ev[5], s));
   CUDA_TRY(cudaGetLastError());
-  const long long pcgLaunches = 2LL * iters;
-  const long long phase[5] = {2, 2, 1, pcgLaunches, 1};
-  for (int k = 0; k < 5; k++) B->phaseLaunches[k] += phase[k];
-  B->launches += 6 + pcgLaunches;
-  if (T) {
-    CUDA_TRY(cudaEventSynchronize(B->ev[5]));
-    for (int k = 0; k < 5; k++) {
-      float ms = 0;
-      CUDA_TRY(cudaEventElapsedTime(&ms, B->ev[k], B->ev[k + 1]));
-      B->phaseMs[k] += ms;
-    }
-  }
+  return HOBAK_OK;
+}
+
+// Loop-body kernels launched so far (device counter of loop-body runs, or
+// the host count of eager chunks).
+int count_loop_launches(hobak_batch_t* B, long long* out) {
+  unsigned long long runs = 0;
+  CUDA_TRY(cudaMemcpy(&runs, B->d.bodyRuns, sizeof(runs), cudaMemcpyDeviceToHost));
+  *out = (long long)(runs * (2ull * kChunk + 1ull)) + B->eagerChunks * 2LL * kChunk;
   return HOBAK_OK;
 }
 
@@ -575,6 +688,7 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
   else
     hobak_default_solver_opts(&B->opts);
   CUDA_TRY(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaStreamCreateWithFlags(&B->captureStream, cudaStreamNonBlocking));
   CUDA_TRY(cudaMallocHost(&B->pinnedActive, sizeof(int)));
   for (auto& e : B->ev) CUDA_TRY(cudaEventCreate(&e));
   if ((rc = build_batch(B.get(), scenes, nscenes))) {
@@ -591,7 +705,8 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
 
 int hobak_batch_destroy(hobak_batch b) {
   if (!b) return HOBAK_OK;
-  if (b->chunkGraph) cudaGraphExecDestroy(b->chunkGraph);
+  drop_graphs(b);
+  if (b->captureStream) cudaStreamDestroy(b->captureStream);
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
   if (b->pinnedActive) cudaFreeHost(b->pinnedActive);
@@ -610,10 +725,8 @@ int hobak_batch_num_scenes(hobak_batch b, int* n) {
 int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats) {
   if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
   if (nsteps < 0) return fail(HOBAK_ERR_INVALID, "nsteps < 0");
-  for (int k = 0; k < nsteps; k++) {
-    int rc = run_step(b);
-    if (rc) return rc;
-  }
+  int rc = run_steps(b, nsteps);
+  if (rc) return rc;
   const int n = (int)b->scenes.size();
   b->lastSolve.resize(n);
   CUDA_TRY(cudaMemcpyAsync(b->lastSolve.data(), b->d.solve, sizeof(SolveState) * n, cudaMemcpyDeviceToHost,
@@ -625,10 +738,10 @@ int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats) {
     if (st.converged < 0) status = HOBAK_ERR_NAN;
     else if (st.converged == 0 && status == HOBAK_OK) status = HOBAK_WARN_NOT_CONVERGED;
     if (stats) {
-      stats[s].iterations = st.iters;
+      stats[s].iterations = st.totalIters;
       stats[s].converged = st.converged > 0 ? 1 : 0;
-      stats[s].rel_residual = st.rhsNorm2 > 0 ? std::sqrt(st.rr / st.rhsNorm2) : 0.0;
-      stats[s].refinements = st.refinements;
+      stats[s].rel_residual = st.rhsNorm2 > 0 ? std::sqrt(st.rr64 / st.rhsNorm2) : 0.0;
+      stats[s].refinements = st.sweep > 0 ? st.sweep - 1 : 0;
     }
   }
   if (status == HOBAK_ERR_NAN) return fail(status, "non-finite residual in PCG");
@@ -669,6 +782,7 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   int rc = check_opts(opts);
   if (rc) return rc;
   b->opts = *opts;
+  drop_graphs(b);
   return upload_solver_opts(b);
 }
 
@@ -716,7 +830,10 @@ int hobak_batch_phase_times(hobak_batch b, double* ms, long long* launches) {
 
 int hobak_batch_launch_count(hobak_batch b, long long* launches) {
   if (!b || !launches) return fail(HOBAK_ERR_INVALID, "bad arguments");
-  *launches = b->launches;
+  long long loop = 0;
+  int rc = count_loop_launches(b, &loop);
+  if (rc) return rc;
+  *launches = b->launches + loop;
   return HOBAK_OK;
 }
 
@@ -730,20 +847,32 @@ int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
   CUDA_TRY(cudaMemcpy(st.data(), d.solve, sizeof(SolveState) * n, cudaMemcpyDeviceToHost));
   for (auto& x : st) {
     x.done = 0;
-    x.threshold = -1.0;
+    x.outerDone = 0;
+    x.innerThreshold = -1.0;
     x.maxit = 0x7fffffff;
+    x.totalIters = 0;
     if (!(x.alpha == x.alpha)) x.alpha = 0.0;
     if (!(x.beta == x.beta)) x.beta = 0.0;
   }
   CUDA_TRY(cudaMemcpy(d.solve, st.data(), sizeof(SolveState) * n, cudaMemcpyHostToDevice));
   cudaEvent_t e0 = b->ev[0], e1 = b->ev[1];
+  const bool mixed = b->opts.precision == HOBAK_PRECISION_MIXED;
   for (int k = 0; k < 4; k++) {
     CUDA_TRY(cudaEventRecord(e0, s));
     for (int r = 0; r < reps; r++) {
-      if (k == 0) launch_element(d, s);
-      else if (k == 1) launch_assemble(d, s);
-      else if (k == 2) launch_spmv(d, d.p0, d.p1, s);
-      else launch_update(d, d.p1, s);
+      if (k == 0) {
+        if (mixed) launch_element_mixed(d, s);
+        else launch_element(d, s);
+      } else if (k == 1) {
+        if (mixed) launch_assemble<float>(d, d.v32, s);
+        else launch_assemble<double>(d, d.v64, s);
+      } else if (k == 2) {
+        if (mixed) launch_spmv<float>(d, d.v32, s);
+        else launch_spmv<double>(d, d.v64, s);
+      } else {
+        if (mixed) launch_update<float>(d, d.v32, s);
+        else launch_update<double>(d, d.v64, s);
+      }
     }
     CUDA_TRY(cudaEventRecord(e1, s));
     CUDA_TRY(cudaEventSynchronize(e1));
@@ -759,14 +888,15 @@ int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
 int hobak_batch_kernel_bytes(hobak_batch b, double* bytes) {
   if (!b || !bytes) return fail(HOBAK_ERR_INVALID, "bad arguments");
   const double T = b->nt, V = b->nv, B = b->nblocks, C = 16.0 * b->nt;
-  // element: tets 16, 4 x (rest, x, v) 288, DmInv 72, vol 8, scene id 4; writes 90 + 12 doubles
-  bytes[0] = T * (16 + 288 + 72 + 8 + 4 + 8.0 * (kElemHess + 12));
-  // assembly: element Hessians once, contribution map, block ids, LHS write; mask/mass per vertex
-  bytes[1] = T * 8.0 * kElemHess + C * 4 + B * (4 + 4 + 4 + 72) + V * (1 + 8 + 4);
-  // spmv: LHS 72 + col 4 per block; rowptr, z, pOld read and pNew, Ap written per vertex
-  bytes[2] = B * 76 + V * (4 + 24 * 4);
-  // update: y rw, p, r rw, Ap, Minv (72), z write per vertex
-  bytes[3] = V * (48 + 24 + 48 + 24 + 72 + 24);
+  const double w = b->opts.precision == HOBAK_PRECISION_MIXED ? 4.0 : 8.0;  // inner value width
+  // element: tets 16, 4 x (rest, x, v) 288, DmInv 72, vol 8, scene id 4; writes 90 Hessian values + 12 doubles
+  bytes[0] = T * (16 + 288 + 72 + 8 + 4 + w * kElemHess + 96);
+  // assembly: element Hessians once, contribution map, block row/col/ptr, LHS write; mask/mass/scene per vertex
+  bytes[1] = T * w * kElemHess + C * 4 + B * (4 + 4 + 4 + 9 * w) + V * (1 + 8 + 4);
+  // spmv: LHS row block + column per block; rowptr, u read and w written per vertex
+  bytes[2] = B * (9 * w + 4) + V * (4 + 2 * 3 * w);
+  // update: u, p rw, w, s rw, d rw, r rw, Minv (9), u write per vertex
+  bytes[3] = V * w * (3 + 6 + 3 + 6 + 6 + 6 + 9 + 3);
   return HOBAK_OK;
 }
 
@@ -861,10 +991,10 @@ int hobak_batch_assemble(hobak_batch b, int scene, int* nblocks, int* rowptr, in
   DeviceBatch d = b->d;
   launch_begin_step(d, b->stream);
   launch_element(d, b->stream, 1);
-  launch_assemble_raw(d, d.lhs, d.rhs, b->stream);
+  launch_assemble_raw(d, d.v64.lhs, d.rhs, b->stream);
   CUDA_TRY(cudaGetLastError());
   if (K)
-    CUDA_TRY(cudaMemcpyAsync(K, d.lhs + 9 * (size_t)rb0, 9 * sizeof(double) * (rb1 - rb0), cudaMemcpyDeviceToHost,
+    CUDA_TRY(cudaMemcpyAsync(K, d.v64.lhs + 9 * (size_t)rb0, 9 * sizeof(double) * (rb1 - rb0), cudaMemcpyDeviceToHost,
                              b->stream));
   if (R)
     CUDA_TRY(cudaMemcpyAsync(R, d.rhs + 3 * (size_t)H.v0, 3 * sizeof(double) * H.nv, cudaMemcpyDeviceToHost,

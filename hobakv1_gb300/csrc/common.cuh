@@ -22,7 +22,7 @@ enum MaterialKind : int { MAT_SNH = 0, MAT_ARAP = 1, MAT_STVK = 2, MAT_LINEAR = 
 
 constexpr int kTileV = 128;       // vertices per PCG tile (one CTA)
 constexpr int kElemHess = 90;     // 10 upper blocks x 9
-constexpr int kElemStride = 102;  // 90 Hessian + 12 rhs values per tet
+constexpr int kPartials = 4;      // per-tile partial sums slots
 
 // Index of block (a, b), a <= b, in the 10-block upper triangle of a 4x4
 // block matrix: (0,0)(0,1)(0,2)(0,3)(1,1)(1,2)(1,3)(2,2)(2,3)(3,3).
@@ -40,17 +40,25 @@ struct SceneParams {
 };
 
 // Per-scene solver scalars, written by the last CTA of each reduction.
+// The inner PCG is the Chronopoulos-Gear form of preconditioned CG (one
+// reduction phase per kernel); the outer loop is FP64 iterative refinement
+// (mixed precision only).
 struct SolveState {
-  double rhsNorm2, threshold;
-  double rz, pAp, alpha, beta, rr;
+  // outer (FP64) system
+  double rhsNorm2;     // |rhs|^2
+  double threshold;    // max(tol^2 |rhs|^2, DBL_MIN)
+  double rr64;         // |rhs - A y|^2 after the last refinement
   double tol;
-  int iters, maxit;
-  int done;        // 1 when this scene's PCG has finished
-  int converged;
+  int outerDone;       // 1 when the step's linear solve is finished
+  int sweep;           // refinement sweeps done
+  int maxSweeps;       // 1 (FP64) or 1 + max_refinements (mixed)
+  int converged;       // 1 converged, 0 not, -1 non-finite
+  int totalIters;      // inner iterations summed over sweeps
+  int maxit;
+  // inner PCG
+  double gamma, gammaOld, delta, alpha, beta, rr, innerThreshold;
+  int iters, done;
   unsigned ticketA, ticketB;
-  int totalIters;  // summed over refinement sweeps
-  int refinements;
-  int pad;
 };
 
 }  // namespace hobak

@@ -192,7 +192,10 @@ __device__ __forceinline__ void deformation_gradient(const double X[4][3], const
 
 // Batched step kernel: element Hessian blocks and right-hand-side terms
 // g = dt (f + dt He v) for every tet of every scene.
-__global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces) {
+// HT is the Hessian's arithmetic/storage type: double (FP64 path) or float
+// (mixed path: F, SVD, stress and forces stay FP64).
+template <typename HT>
+__global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces, HT* __restrict__ outH) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= b.nt) return;
   const int4 tv = b.tets[t];
@@ -211,8 +214,8 @@ __global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces) {
   material_pk1(m, F, U, V, P);
   element_force(P, Dinv, vol, f);
 
-  double Hr[45];
-  reduced_hessian<double>(m, U, S, V, Dinv, Hr);
+  HT Hr[45];
+  reduced_hessian<HT>(m, U, S, V, Dinv, Hr);
 
   // He v = -vol D^T Hr (D v): D v = relative velocities of vertices 1..3
   const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
@@ -232,7 +235,7 @@ __global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces) {
   for (int r = 0; r < 9; r++) {
     double s = 0;
 #pragma unroll
-    for (int c = 0; c < 9; c++) s += ((r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)]) * dv[c];
+    for (int c = 0; c < 9; c++) s += double((r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)]) * dv[c];
     const double hv = -vol * s;
     h0[r % 3] += hv;
     g[3 + r] = rawForces ? f[3 + r] : dt * (f[3 + r] + dt * hv);
@@ -240,7 +243,7 @@ __global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces) {
 #pragma unroll
   for (int i = 0; i < 3; i++) g[i] = rawForces ? f[i] : dt * (f[i] - dt * h0[i]);
 
-  expand_blocks<double, double>(Hr, vol, b.elemH + kElemHess * (size_t)t);
+  expand_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
 }
 
 // Standalone: clamped 9x9 Hessian, PK1 and psi of n deformation gradients.
@@ -329,7 +332,12 @@ __global__ void k_energy(DeviceBatch b) {
 
 void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces) {
   if (b.nt == 0) return;
-  k_element<<<(b.nt + 127) / 128, 128, 0, s>>>(b, rawForces);
+  k_element<double><<<(b.nt + 127) / 128, 128, 0, s>>>(b, rawForces, b.elemH);
+}
+
+void launch_element_mixed(const DeviceBatch& b, cudaStream_t s) {
+  if (b.nt == 0) return;
+  k_element<float><<<(b.nt + 127) / 128, 128, 0, s>>>(b, 0, b.elemHf);
 }
 
 void launch_energy(const DeviceBatch& b, cudaStream_t s) {

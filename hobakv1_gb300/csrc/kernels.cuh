@@ -1,4 +1,4 @@
-// Kernel argument blocks and launch wrappers shared by kernels.cu and api.cu.
+// Kernel argument blocks and launch wrappers shared by the .cu files.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -6,12 +6,26 @@
 
 namespace hobak {
 
+// Vectors and matrix of one inner PCG solve, in arithmetic type T.
+template <typename T>
+struct PcgVecs {
+  T* lhs;   // [B][9] row major
+  T* minv;  // [V][9] row major
+  T* r;     // residual of the inner solve
+  T* u;     // preconditioned residual
+  T* p;     // search direction
+  T* s;     // A p (updated by recurrence)
+  T* w;     // A u
+  T* d;     // inner solution (the correction)
+};
+
 // Device pointers of one packed batch.  Plain struct passed by value.
 struct DeviceBatch {
   int nscenes, nv, nt, nblocks, ntiles;
   const SceneParams* scenes;
   SolveState* solve;
-  int* active;  // scenes whose PCG is still running
+  int* active;  // scenes whose inner PCG is still running
+  unsigned long long* bodyRuns;  // PCG loop bodies executed (graph mode), for launch accounting
 
   // vertices
   const double* rest;
@@ -44,35 +58,46 @@ struct DeviceBatch {
   const int* tileV1;
 
   // per-tet element outputs
-  double* elemH;  // [T][90]
-  double* elemG;  // [T][12]
+  double* elemH;   // [T][90] FP64 path
+  float* elemHf;   // [T][90] mixed path
+  double* elemG;   // [T][12]
 
-  // system and PCG vectors (FP64 path)
-  double* lhs;    // [B][9] row major
-  double* minv;   // [V][9] row major
+  // outer FP64 system
   double* rhs;
   double* y;
-  double* r;
-  double* z;
-  double* p0;
-  double* p1;
-  double* Ap;
-  double* partial;  // [ntiles][2]
-  double* psi;      // [T] energy density scratch
+  double* r64;
+  // inner solves
+  PcgVecs<double> v64;  // FP64 path (r = r64, d = y)
+  PcgVecs<float> v32;   // mixed path
+  double* partial;      // [ntiles][kPartials]
+  double* psi;          // [T] energy density scratch
 };
 
 void launch_begin_step(const DeviceBatch& b, cudaStream_t s);
 // rawForces = 1 stores the element force f itself in elemG instead of dt (f + dt He v)
 void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces = 0);
+void launch_element_mixed(const DeviceBatch& b, cudaStream_t s);
 // K blocks (column major, un-masked, no mass) and R = sum of element forces, for inspection
 void launch_assemble_raw(const DeviceBatch& b, double* K, double* R, cudaStream_t s);
-void launch_assemble(const DeviceBatch& b, cudaStream_t s);
-void launch_diag_inverse(const DeviceBatch& b, int precond, cudaStream_t s);
-void launch_pcg_init(const DeviceBatch& b, cudaStream_t s);
-void launch_pcg_iteration(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s);
-void launch_spmv(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s);
-void launch_update(const DeviceBatch& b, const double* p, cudaStream_t s);
-void launch_finish_step(const DeviceBatch& b, cudaStream_t s);
+template <typename T>
+void launch_assemble(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
+template <typename T>
+void launch_diag_inverse(const DeviceBatch& b, const PcgVecs<T>& v, int precond, cudaStream_t s);
+void launch_rhs(const DeviceBatch& b, cudaStream_t s);
+void launch_set_active(const DeviceBatch& b, cudaStream_t s);
+template <typename T>
+void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
+template <typename T>
+void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
+template <typename T>
+void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
+template <typename T>
+void launch_pcg_iteration(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
+  launch_spmv<T>(b, v, s);
+  launch_update<T>(b, v, s);
+}
+void launch_refine(const DeviceBatch& b, cudaStream_t s);  // y += d, then r64 = rhs - A y
+void launch_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s);void launch_finish_step(const DeviceBatch& b, cudaStream_t s);
 void launch_energy(const DeviceBatch& b, cudaStream_t s);
 
 // element-level entry points (standalone, no batch)

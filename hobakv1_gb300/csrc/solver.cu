@@ -1,11 +1,27 @@
-// Assembly, right-hand side and block-Jacobi PCG kernels (FP64 path).
+// Assembly, right-hand side, PCG and refinement kernels.
 //
 // System of one BACKWARD_EULER_VELOCITY step (BACKWARD_EULER_VELOCITY.cpp:157-176):
 //   b   = dt (R + dt K v + f_ext)
 //   A   = M - dt^2 K                      (C = 0: TIMESTEPPER.cpp:657)
 //   LHS = S A S + (I - S),  rhs = S b     (S = 0 blocks at pinned vertices)
-// solved by PCG from y = 0 with the stopping rule of Eigen's
-// conjugate_gradient (ConjugateGradient.h:28-90).
+// solved from y = 0 with the stopping rule of Eigen's conjugate_gradient
+// (ConjugateGradient.h:28-90): |r|^2 < max(tol^2 |rhs|^2, DBL_MIN) on the
+// recursive residual.
+//
+// PCG runs in the Chronopoulos-Gear arrangement (same iterates as the
+// textbook loop in exact arithmetic) so that each iteration is exactly two
+// kernels with one reduction each and the SpMV multiplies a vector that is
+// already final:
+//   k_spmv:   w = A u, delta = (w, u)          -> beta, alpha
+//   k_update: p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s,
+//             u = Minv r, gamma = (r, u), |r|^2 -> convergence test
+// On GB300 the FP64 pipe, not HBM, bounds the FP64 SpMV, so the product does
+// only the 9 DFMA per block it must (one thread per scalar row, no lane
+// reductions).
+//
+// Mixed precision: the inner PCG runs on FP32 vectors and an FP32 matrix; the
+// outer loop keeps y and the residual rhs - A y in FP64 (iterative refinement,
+// at most 1 + max_refinements sweeps) and stops on the same FP64 test.
 //
 // No atomics touch values: every matrix block and vertex sums its element
 // contributions in ascending tet order, and every dot product is a fixed tree
@@ -21,8 +37,8 @@ namespace hobak {
 
 namespace {
 
-constexpr int kLanes = 8;        // threads per vertex row in the SpMV
-constexpr int kSpmvThreads = 256;
+constexpr int kVecThreads = kTileV;       // vector kernels: one thread per vertex
+constexpr int kSpmvThreads = 3 * kTileV;  // SpMV: one thread per scalar row
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -30,7 +46,7 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Fixed-order sum over the CTA; result valid in thread 0.  nthreads multiple of 32.
+// Fixed-order sum over the CTA; result valid in thread 0.  NT multiple of 32.
 template <int NT>
 __device__ __forceinline__ double block_sum(double v, double* sh) {
   v = warp_sum(v);
@@ -46,8 +62,8 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return s;
 }
 
-// After a CTA wrote its partial(s): returns true in the CTA that finishes the
-// scene's reduction (ticket == ntiles - 1).  The ticket is reset for reuse.
+// After a CTA wrote its partial(s): true in the CTA that finishes the scene's
+// reduction (ticket == ntiles - 1).  The ticket is reset for reuse.
 __device__ __forceinline__ bool last_tile(unsigned* ticket, int ntiles, int* flag) {
   __threadfence();
   if (threadIdx.x == 0) {
@@ -61,15 +77,15 @@ __device__ __forceinline__ bool last_tile(unsigned* ticket, int ntiles, int* fla
   return last;
 }
 
-// Sum partial[tile0 .. tile0+n) (stride `stride`, component `comp`) in a fixed
-// order with all threads of the CTA; valid in thread 0.
+// Sum partial[(tile0 + i) * kPartials + comp] over i < n in a fixed order.
 template <int NT>
-__device__ __forceinline__ double sum_partials(const double* partial, int tile0, int n, int stride, int comp,
-                                               double* sh) {
+__device__ __forceinline__ double sum_partials(const double* partial, int tile0, int n, int comp, double* sh) {
   double s = 0;
-  for (int i = threadIdx.x; i < n; i += NT) s += __ldcg(&partial[(size_t)(tile0 + i) * stride + comp]);
+  for (int i = threadIdx.x; i < n; i += NT) s += __ldcg(&partial[(size_t)(tile0 + i) * kPartials + comp]);
   return block_sum<NT>(s, sh);
 }
+
+__device__ __forceinline__ bool finite(double x) { return x == x && fabs(x) <= DBL_MAX; }
 
 // x[pinned] = pin target at the start of a step
 // (applyKinematicConstraints, TIMESTEPPER.cpp:105-122).
@@ -80,28 +96,36 @@ __global__ void k_begin_step(DeviceBatch b) {
   for (int i = 0; i < 3; i++) b.x[3 * u + i] = b.pinTarget[3 * u + i];
 }
 
-// One thread per (block, entry): LHS block = S(M - dt^2 K)S + (I - S), with
-// K's block the ascending-tet sum of its element contributions
+// Sum of one block entry over its element contributions, ascending tet
 // (TET_MESH_FASTER.cpp:113-131 gathers the same entries per non-zero).
-__global__ void k_assemble(DeviceBatch b) {
+template <typename HT>
+__device__ __forceinline__ double gather_block_entry(const DeviceBatch& b, const HT* __restrict__ elemH, int blk,
+                                                     int r, int c) {
+  double sum = 0.0;
+  const int k1 = b.blkptr[blk + 1];
+  for (int k = b.blkptr[blk]; k < k1; k++) {
+    const int src = b.blksrc[k];
+    const int t = src >> 4, ea = (src >> 2) & 3, eb = src & 3;
+    const HT* H = elemH + (size_t)kElemHess * t;
+    sum += (double)((ea <= eb) ? H[9 * upper_block(ea, eb) + 3 * r + c] : H[9 * upper_block(eb, ea) + 3 * c + r]);
+  }
+  return sum;
+}
+
+// One thread per (block, entry): LHS block = S(M - dt^2 K)S + (I - S).
+template <typename HT, typename T>
+__global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
   const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= 9L * b.nblocks) return;
   const int blk = (int)(g / 9), e = (int)(g % 9);
   const int r = e / 3, c = e % 3;
-  double sum = 0.0;
-  const int k0 = b.blkptr[blk], k1 = b.blkptr[blk + 1];
-  for (int k = k0; k < k1; k++) {
-    const int src = b.blksrc[k];
-    const int t = src >> 4, ea = (src >> 2) & 3, eb = src & 3;
-    const double* H = b.elemH + (size_t)kElemHess * t;
-    sum += (ea <= eb) ? H[9 * upper_block(ea, eb) + 3 * r + c] : H[9 * upper_block(eb, ea) + 3 * c + r];
-  }
+  const double sum = gather_block_entry(b, elemH, blk, r, c);
   const int u = b.blkRow[blk], w = b.cols[blk];
   const double dt = b.scenes[b.vertexScene[u]].dt;
   const bool fu = b.freeMask[u] != 0, fw = b.freeMask[w] != 0;
   double val = (fu && fw) ? -(dt * dt) * sum : 0.0;
   if (u == w && r == c) val += fu ? b.mass[u] : 1.0;
-  b.lhs[9 * (size_t)blk + e] = val;
+  lhs[9 * (size_t)blk + e] = T(val);
 }
 
 // Raw K blocks (column major) and R: the reference's stiffness and force
@@ -111,14 +135,7 @@ __global__ void k_assemble_raw(DeviceBatch b, double* K, double* R) {
   if (g < 9L * b.nblocks) {
     const int blk = (int)(g / 9), e = (int)(g % 9);
     const int r = e / 3, c = e % 3;
-    double sum = 0.0;
-    for (int k = b.blkptr[blk]; k < b.blkptr[blk + 1]; k++) {
-      const int src = b.blksrc[k];
-      const int t = src >> 4, ea = (src >> 2) & 3, eb = src & 3;
-      const double* H = b.elemH + (size_t)kElemHess * t;
-      sum += (ea <= eb) ? H[9 * upper_block(ea, eb) + 3 * r + c] : H[9 * upper_block(eb, ea) + 3 * c + r];
-    }
-    K[9 * (size_t)blk + r + 3 * c] = sum;
+    K[9 * (size_t)blk + r + 3 * c] = gather_block_entry(b, b.elemH, blk, r, c);
   }
   if (g < 3L * b.nv) {
     const int u = (int)(g / 3), i = (int)(g % 3);
@@ -133,46 +150,49 @@ __global__ void k_assemble_raw(DeviceBatch b, double* K, double* R) {
 
 // Preconditioner from LHS's diagonal blocks: 3x3 inverse (block Jacobi) or
 // 1/diag (Jacobi, BasicPreconditioners.h:67-75; zero diagonal -> 1).
-__global__ void k_diag_inverse(DeviceBatch b, int precond) {
+template <typename T>
+__global__ void k_diag_inverse(DeviceBatch b, const T* __restrict__ lhs, T* __restrict__ minv, int precond) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= b.nv) return;
   int k = b.rowptr[u];
   while (b.cols[k] != u) k++;
-  const double* D = b.lhs + 9 * (size_t)k;
-  double* M = b.minv + 9 * (size_t)u;
+  double D[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) D[i] = (double)lhs[9 * (size_t)k + i];
+  T* M = minv + 9 * (size_t)u;
   if (precond == 1) {
     const double c00 = D[4] * D[8] - D[5] * D[7];
     const double c01 = D[5] * D[6] - D[3] * D[8];
     const double c02 = D[3] * D[7] - D[4] * D[6];
     const double det = D[0] * c00 + D[1] * c01 + D[2] * c02;
     const double id = 1.0 / det;
-    M[0] = c00 * id;
-    M[1] = (D[2] * D[7] - D[1] * D[8]) * id;
-    M[2] = (D[1] * D[5] - D[2] * D[4]) * id;
-    M[3] = c01 * id;
-    M[4] = (D[0] * D[8] - D[2] * D[6]) * id;
-    M[5] = (D[2] * D[3] - D[0] * D[5]) * id;
-    M[6] = c02 * id;
-    M[7] = (D[1] * D[6] - D[0] * D[7]) * id;
-    M[8] = (D[0] * D[4] - D[1] * D[3]) * id;
+    M[0] = T(c00 * id);
+    M[1] = T((D[2] * D[7] - D[1] * D[8]) * id);
+    M[2] = T((D[1] * D[5] - D[2] * D[4]) * id);
+    M[3] = T(c01 * id);
+    M[4] = T((D[0] * D[8] - D[2] * D[6]) * id);
+    M[5] = T((D[2] * D[3] - D[0] * D[5]) * id);
+    M[6] = T(c02 * id);
+    M[7] = T((D[1] * D[6] - D[0] * D[7]) * id);
+    M[8] = T((D[0] * D[4] - D[1] * D[3]) * id);
   } else {
 #pragma unroll
-    for (int i = 0; i < 9; i++) M[i] = 0.0;
+    for (int i = 0; i < 9; i++) M[i] = T(0);
 #pragma unroll
-    for (int i = 0; i < 3; i++) M[4 * i] = D[4 * i] != 0.0 ? 1.0 / D[4 * i] : 1.0;
+    for (int i = 0; i < 3; i++) M[4 * i] = T(D[4 * i] != 0.0 ? 1.0 / D[4 * i] : 1.0);
   }
 }
 
 // rhs = S dt (sum_e g_e + f_ext) per vertex (element g already carries
-// dt (f + dt He v)), then PCG start: y = 0, r = rhs, z = Minv r, p = 0.
-// Per-scene: rhsNorm2, threshold and the early exits of conjugate_gradient.
-__global__ void __launch_bounds__(kTileV) k_pcg_init(DeviceBatch b) {
-  __shared__ double sh[kTileV / 32];
+// dt (f + dt He v)); y = 0; r64 = rhs.  Per scene: |rhs|^2 and the FP64
+// stopping threshold; an all-zero right-hand side finishes the solve (x = 0).
+__global__ void __launch_bounds__(kVecThreads) k_rhs(DeviceBatch b) {
+  __shared__ double sh[kVecThreads / 32];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
   const int u = b.tileV0[tile] + threadIdx.x;
-  double rr = 0, rz = 0;
+  double rr = 0;
   if (u < b.tileV1[tile]) {
     const double dt = b.scenes[s].dt;
     double acc[3] = {0.0, 0.0, 0.0};
@@ -183,170 +203,290 @@ __global__ void __launch_bounds__(kTileV) k_pcg_init(DeviceBatch b) {
       for (int i = 0; i < 3; i++) acc[i] += g[i];
     }
     const bool fu = b.freeMask[u] != 0;
-    double r3[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      r3[i] = fu ? acc[i] + dt * b.fext[3 * u + i] : 0.0;
-      b.rhs[3 * u + i] = r3[i];
-      b.r[3 * u + i] = r3[i];
+      const double ri = fu ? acc[i] + dt * b.fext[3 * u + i] : 0.0;
+      b.rhs[3 * u + i] = ri;
+      b.r64[3 * u + i] = ri;
       b.y[3 * u + i] = 0.0;
-      b.p0[3 * u + i] = 0.0;
-      b.p1[3 * u + i] = 0.0;
-    }
-    const double* M = b.minv + 9 * (size_t)u;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      const double zi = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
-      b.z[3 * u + i] = zi;
-      rr += r3[i] * r3[i];
-      rz += r3[i] * zi;
+      rr += ri * ri;
     }
   }
-  const double trr = block_sum<kTileV>(rr, sh);
-  const double trz = block_sum<kTileV>(rz, sh);
-  if (threadIdx.x == 0) {
-    b.partial[2 * tile] = trr;
-    b.partial[2 * tile + 1] = trz;
-  }
+  const double t = block_sum<kVecThreads>(rr, sh);
+  if (threadIdx.x == 0) b.partial[kPartials * tile] = t;
   SolveState& st = b.solve[s];
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketB, sp.ntiles, &flag)) return;
-  const double srr = sum_partials<kTileV>(b.partial, sp.tile0, sp.ntiles, 2, 0, sh);
-  const double srz = sum_partials<kTileV>(b.partial, sp.tile0, sp.ntiles, 2, 1, sh);
+  const double srr = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 0, sh);
   if (threadIdx.x == 0) {
     st.rhsNorm2 = srr;
     st.threshold = fmax(st.tol * st.tol * srr, DBL_MIN);
+    st.rr64 = srr;
+    st.sweep = 0;
+    st.totalIters = 0;
+    st.converged = 0;
+    st.outerDone = 0;
+    if (srr == 0.0) {  // ConjugateGradient.h:49-55
+      st.outerDone = 1;
+      st.converged = 1;
+    } else if (!finite(srr)) {
+      st.outerDone = 1;
+      st.converged = -1;
+    }
+  }
+}
+
+__global__ void k_set_active(DeviceBatch b) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *b.active = b.nscenes;
+}
+
+// Start of one inner solve on r_T = (T) r64: d = 0, p = s = 0, u = Minv r,
+// gamma = (r, u), |r|^2.  Inner tolerance: the outer one for FP64; for FP32
+// the relative reduction still needed, floored at 1e-5 (FP32 stagnation).
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_inner_init(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[kVecThreads / 32];
+  __shared__ int flag;
+  const int tile = blockIdx.x;
+  const int s = b.tileScene[tile];
+  SolveState& st = b.solve[s];
+  const SceneParams& sp = b.scenes[s];
+  if (st.outerDone) {
+    // this scene's solve is over: mark the inner solve done once
+    if (tile == sp.tile0 && threadIdx.x == 0) {
+      st.done = 1;
+      atomicSub(b.active, 1);
+    }
+    return;
+  }
+  const int u = b.tileV0[tile] + threadIdx.x;
+  double rr = 0, ru = 0;
+  if (u < b.tileV1[tile]) {
+    T r3[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      r3[i] = T(b.r64[3 * u + i]);
+      if (sizeof(T) != sizeof(double)) v.r[3 * u + i] = r3[i];
+      v.d[3 * u + i] = T(0);
+      v.p[3 * u + i] = T(0);
+      v.s[3 * u + i] = T(0);
+      rr += double(r3[i]) * double(r3[i]);
+    }
+    const T* M = v.minv + 9 * (size_t)u;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
+      v.u[3 * u + i] = ui;
+      ru += double(r3[i]) * double(ui);
+    }
+  }
+  const double trr = block_sum<kVecThreads>(rr, sh);
+  const double tru = block_sum<kVecThreads>(ru, sh);
+  if (threadIdx.x == 0) {
+    b.partial[kPartials * tile] = trr;
+    b.partial[kPartials * tile + 1] = tru;
+  }
+  if (!last_tile(&st.ticketB, sp.ntiles, &flag)) return;
+  const double srr = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 0, sh);
+  const double sru = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 1, sh);
+  if (threadIdx.x == 0) {
+    double itol = st.tol;
+    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr, DBL_MIN)), 1e-5);
     st.rr = srr;
-    st.rz = srz;
+    st.gamma = sru;
+    st.gammaOld = 1.0;
+    st.alpha = 1.0;
     st.beta = 0.0;
     st.iters = 0;
-    st.converged = 0;
+    st.innerThreshold = fmax(itol * itol * srr, DBL_MIN);
     st.done = 0;
-    if (srr == 0.0 || srr < st.threshold) {
+    if (srr == 0.0 || srr < st.innerThreshold) {
       st.done = 1;
-      st.converged = 1;
       atomicSub(b.active, 1);
     }
   }
 }
 
-// Ap = LHS p with p = z + beta pOld formed on the fly (own rows written to
-// pNew), and the scene's p.Ap -> alpha = rz / p.Ap.
-__global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, const double* __restrict__ pOld,
-                                                       double* __restrict__ pNew) {
+// w = A u, one thread per scalar row (9 DFMA per block in FP64), and
+// delta = (w, u); the scene's last CTA forms beta and alpha.
+template <typename T>
+__global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T> v) {
   __shared__ double sh[kSpmvThreads / 32];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
   SolveState& st = b.solve[s];
   if (st.done) return;
-  const double beta = st.beta;
-  const int v0 = b.tileV0[tile], v1 = b.tileV1[tile];
-  const int lane = threadIdx.x % kLanes;
-  const double* __restrict__ z = b.z;
-  double pap = 0.0;
-  constexpr int kRowsPerPass = kSpmvThreads / kLanes;
-  const int passes = (v1 - v0 + kRowsPerPass - 1) / kRowsPerPass;  // uniform: shuffles need every lane
-  for (int pass = 0; pass < passes; pass++) {
-    const int u = v0 + pass * kRowsPerPass + threadIdx.x / kLanes;
-    const bool valid = u < v1;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    const int k1 = valid ? b.rowptr[u + 1] : 0;
-    for (int k = valid ? b.rowptr[u] + lane : 0; k < k1; k += kLanes) {
-      const int w = b.cols[k];
-      const double q0 = z[3 * w] + beta * pOld[3 * w];
-      const double q1 = z[3 * w + 1] + beta * pOld[3 * w + 1];
-      const double q2 = z[3 * w + 2] + beta * pOld[3 * w + 2];
-      const double* B = b.lhs + 9 * (size_t)k;
-      a0 += B[0] * q0 + B[1] * q1 + B[2] * q2;
-      a1 += B[3] * q0 + B[4] * q1 + B[5] * q2;
-      a2 += B[6] * q0 + B[7] * q1 + B[8] * q2;
+  const int row = 3 * b.tileV0[tile] + threadIdx.x;
+  double dl = 0.0;
+  if (row < 3 * b.tileV1[tile]) {
+    const int u = row / 3, i = row - 3 * u;
+    const T* __restrict__ uu = v.u;
+    const T* __restrict__ A = v.lhs + 3 * i;
+    T acc = T(0);
+    const int k1 = b.rowptr[u + 1];
+    for (int k = b.rowptr[u]; k < k1; k++) {
+      const int w = __ldg(&b.cols[k]);
+      const T* B = A + 9 * (size_t)k;
+      acc += B[0] * uu[3 * w] + B[1] * uu[3 * w + 1] + B[2] * uu[3 * w + 2];
     }
-#pragma unroll
-    for (int o = kLanes / 2; o > 0; o >>= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-    }
-    if (valid && lane == 0) {
-      const double p0 = z[3 * u] + beta * pOld[3 * u];
-      const double p1 = z[3 * u + 1] + beta * pOld[3 * u + 1];
-      const double p2 = z[3 * u + 2] + beta * pOld[3 * u + 2];
-      pNew[3 * u] = p0;
-      pNew[3 * u + 1] = p1;
-      pNew[3 * u + 2] = p2;
-      b.Ap[3 * u] = a0;
-      b.Ap[3 * u + 1] = a1;
-      b.Ap[3 * u + 2] = a2;
-      pap += p0 * a0 + p1 * a1 + p2 * a2;
-    }
+    v.w[row] = acc;
+    dl = double(acc) * double(uu[row]);
   }
-  const double tp = block_sum<kSpmvThreads>(pap, sh);
-  if (threadIdx.x == 0) b.partial[2 * tile] = tp;
+  const double t = block_sum<kSpmvThreads>(dl, sh);
+  if (threadIdx.x == 0) b.partial[kPartials * tile + 2] = t;
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketA, sp.ntiles, &flag)) return;
-  const double spap = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 2, 0, sh);
-  if (threadIdx.x == 0) st.alpha = st.rz / spap;
+  const double delta = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 2, sh);
+  if (threadIdx.x == 0) {
+    st.delta = delta;
+    if (st.iters == 0) {
+      st.beta = 0.0;
+      st.alpha = st.gamma / delta;
+    } else {
+      const double beta = st.gamma / st.gammaOld;
+      st.beta = beta;
+      st.alpha = st.gamma / (delta - beta * st.gamma / st.alpha);
+    }
+  }
 }
 
-// y += alpha p; r -= alpha Ap; z = Minv r; then the residual test and beta
-// (ConjugateGradient.h:69-86).
-__global__ void __launch_bounds__(kTileV) k_update(DeviceBatch b, const double* __restrict__ p) {
-  __shared__ double sh[kTileV / 32];
+// p = u + beta p; s = w + beta s; d += alpha p; r -= alpha s; u = Minv r;
+// gamma' = (r, u); |r|^2 -> stop when |r|^2 < threshold (ConjugateGradient.h:75-78).
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_update(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[kVecThreads / 32];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
   SolveState& st = b.solve[s];
   if (st.done) return;
-  const double alpha = st.alpha;
+  const T alpha = T(st.alpha), beta = T(st.beta);
   const int u = b.tileV0[tile] + threadIdx.x;
-  double rr = 0, rz = 0;
+  double rr = 0, ru = 0;
+  T* __restrict__ r = (sizeof(T) == sizeof(double)) ? reinterpret_cast<T*>(b.r64) : v.r;
   if (u < b.tileV1[tile]) {
-    double r3[3];
+    T r3[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      b.y[3 * u + i] += alpha * p[3 * u + i];
-      r3[i] = b.r[3 * u + i] - alpha * b.Ap[3 * u + i];
-      b.r[3 * u + i] = r3[i];
-      rr += r3[i] * r3[i];
+      const int k = 3 * u + i;
+      const T p = v.u[k] + beta * v.p[k];
+      const T sv = v.w[k] + beta * v.s[k];
+      v.p[k] = p;
+      v.s[k] = sv;
+      v.d[k] += alpha * p;
+      r3[i] = r[k] - alpha * sv;
+      r[k] = r3[i];
+      rr += double(r3[i]) * double(r3[i]);
     }
-    const double* M = b.minv + 9 * (size_t)u;
+    const T* M = v.minv + 9 * (size_t)u;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const double zi = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
-      b.z[3 * u + i] = zi;
-      rz += r3[i] * zi;
+      const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
+      v.u[3 * u + i] = ui;
+      ru += double(r3[i]) * double(ui);
     }
   }
-  const double trr = block_sum<kTileV>(rr, sh);
-  const double trz = block_sum<kTileV>(rz, sh);
+  const double trr = block_sum<kVecThreads>(rr, sh);
+  const double tru = block_sum<kVecThreads>(ru, sh);
   if (threadIdx.x == 0) {
-    b.partial[2 * tile] = trr;
-    b.partial[2 * tile + 1] = trz;
+    b.partial[kPartials * tile] = trr;
+    b.partial[kPartials * tile + 1] = tru;
   }
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketB, sp.ntiles, &flag)) return;
-  const double srr = sum_partials<kTileV>(b.partial, sp.tile0, sp.ntiles, 2, 0, sh);
-  const double srz = sum_partials<kTileV>(b.partial, sp.tile0, sp.ntiles, 2, 1, sh);
+  const double srr = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 0, sh);
+  const double sru = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 1, sh);
   if (threadIdx.x == 0) {
     st.rr = srr;
-    if (srr < st.threshold) {
-      st.done = 1;
-      st.converged = 1;
-      atomicSub(b.active, 1);
-    } else if (!(srr == srr) || !(srz == srz)) {
-      st.done = 1;  // non-finite: stop, the host reports HOBAK_ERR_NAN
+    st.iters += 1;
+    st.totalIters += 1;
+    bool stop = false;
+    if (srr < st.innerThreshold) {
+      stop = true;
+    } else if (!finite(srr) || !finite(sru) || !finite(st.alpha)) {
+      stop = true;
       st.converged = -1;
-      atomicSub(b.active, 1);
+      st.outerDone = 1;
     } else {
-      st.beta = srz / st.rz;
-      st.rz = srz;
-      st.iters += 1;
-      if (st.iters >= st.maxit) {
-        st.done = 1;
-        atomicSub(b.active, 1);
+      st.gammaOld = st.gamma;
+      st.gamma = sru;
+      if (st.totalIters >= st.maxit) stop = true;
+    }
+    if (stop) {
+      st.done = 1;
+      atomicSub(b.active, 1);
+      if (sizeof(T) == sizeof(double) && st.converged >= 0) {
+        // FP64 path: the recursive residual is the solver's verdict (Eigen)
+        st.rr64 = srr;
+        st.converged = srr < st.threshold ? 1 : 0;
+        st.outerDone = 1;
       }
     }
+  }
+}
+
+// Mixed precision, after an inner solve: y += d (FP64), one vertex per thread.
+__global__ void k_accumulate(DeviceBatch b) {
+  const int tile = blockIdx.x;
+  const int s = b.tileScene[tile];
+  if (b.solve[s].outerDone) return;
+  const int u = b.tileV0[tile] + threadIdx.x;
+  if (u >= b.tileV1[tile]) return;
+#pragma unroll
+  for (int i = 0; i < 3; i++) b.y[3 * u + i] += double(b.v32.d[3 * u + i]);
+}
+
+// Mixed precision: r64 = rhs - A y in FP64 (FP32 matrix entries promoted),
+// |r64|^2, then the outer test: converged, out of sweeps, or refine again.
+__global__ void __launch_bounds__(kSpmvThreads) k_residual(DeviceBatch b) {
+  __shared__ double sh[kSpmvThreads / 32];
+  __shared__ int flag;
+  const int tile = blockIdx.x;
+  const int s = b.tileScene[tile];
+  SolveState& st = b.solve[s];
+  if (st.outerDone) return;
+  const int row = 3 * b.tileV0[tile] + threadIdx.x;
+  double rr = 0.0;
+  if (row < 3 * b.tileV1[tile]) {
+    const int u = row / 3, i = row - 3 * u;
+    const float* A = b.v32.lhs + 3 * i;
+    double acc = 0.0;
+    for (int k = b.rowptr[u]; k < b.rowptr[u + 1]; k++) {
+      const int w = b.cols[k];
+      const float* B = A + 9 * (size_t)k;
+      acc += double(B[0]) * b.y[3 * w] + double(B[1]) * b.y[3 * w + 1] + double(B[2]) * b.y[3 * w + 2];
+    }
+    const double ri = b.rhs[row] - acc;
+    b.r64[row] = ri;
+    rr = ri * ri;
+  }
+  const double t = block_sum<kSpmvThreads>(rr, sh);
+  if (threadIdx.x == 0) b.partial[kPartials * tile + 3] = t;
+  const SceneParams& sp = b.scenes[s];
+  if (!last_tile(&st.ticketA, sp.ntiles, &flag)) return;
+  const double srr = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 3, sh);
+  if (threadIdx.x == 0) {
+    st.rr64 = srr;
+    st.sweep += 1;
+    if (srr < st.threshold) {
+      st.outerDone = 1;
+      st.converged = 1;
+    } else if (!finite(srr)) {
+      st.outerDone = 1;
+      st.converged = -1;
+    } else if (st.sweep >= st.maxSweeps || st.totalIters >= st.maxit) {
+      st.outerDone = 1;
+      st.converged = 0;
+    }
+  }
+}
+
+// Graph loop control: keep iterating while any scene's inner PCG runs.
+__global__ void k_continue(const int* active, unsigned long long* bodyRuns, cudaGraphConditionalHandle h) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    *bodyRuns += 1ull;
+    cudaGraphSetConditional(h, *active > 0 ? 1u : 0u);
   }
 }
 
@@ -370,9 +510,13 @@ void launch_begin_step(const DeviceBatch& b, cudaStream_t s) {
   k_begin_step<<<(b.nv + 255) / 256, 256, 0, s>>>(b);
 }
 
-void launch_assemble(const DeviceBatch& b, cudaStream_t s) {
+template <typename T>
+void launch_assemble(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
   const long n = 9L * b.nblocks;
-  k_assemble<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b);
+  if (sizeof(T) == sizeof(double))
+    k_assemble<double, T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, b.elemH, v.lhs);
+  else
+    k_assemble<float, T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, b.elemHf, v.lhs);
 }
 
 void launch_assemble_raw(const DeviceBatch& b, double* K, double* R, cudaStream_t s) {
@@ -380,27 +524,51 @@ void launch_assemble_raw(const DeviceBatch& b, double* K, double* R, cudaStream_
   k_assemble_raw<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, K, R);
 }
 
-void launch_diag_inverse(const DeviceBatch& b, int precond, cudaStream_t s) {
-  k_diag_inverse<<<(b.nv + 255) / 256, 256, 0, s>>>(b, precond);
+template <typename T>
+void launch_diag_inverse(const DeviceBatch& b, const PcgVecs<T>& v, int precond, cudaStream_t s) {
+  k_diag_inverse<T><<<(b.nv + 255) / 256, 256, 0, s>>>(b, v.lhs, v.minv, precond);
 }
 
-void launch_pcg_init(const DeviceBatch& b, cudaStream_t s) { k_pcg_init<<<b.ntiles, kTileV, 0, s>>>(b); }
+void launch_rhs(const DeviceBatch& b, cudaStream_t s) { k_rhs<<<b.ntiles, kVecThreads, 0, s>>>(b); }
 
-void launch_spmv(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s) {
-  k_spmv<<<b.ntiles, kSpmvThreads, 0, s>>>(b, pOld, pNew);
+void launch_set_active(const DeviceBatch& b, cudaStream_t s) { k_set_active<<<1, 32, 0, s>>>(b); }
+
+template <typename T>
+void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
+  k_inner_init<T><<<b.ntiles, kVecThreads, 0, s>>>(b, v);
 }
 
-void launch_update(const DeviceBatch& b, const double* p, cudaStream_t s) {
-  k_update<<<b.ntiles, kTileV, 0, s>>>(b, p);
+template <typename T>
+void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
+  k_spmv<T><<<b.ntiles, kSpmvThreads, 0, s>>>(b, v);
 }
 
-void launch_pcg_iteration(const DeviceBatch& b, const double* pOld, double* pNew, cudaStream_t s) {
-  launch_spmv(b, pOld, pNew, s);
-  launch_update(b, pNew, s);
+template <typename T>
+void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
+  k_update<T><<<b.ntiles, kVecThreads, 0, s>>>(b, v);
 }
 
+void launch_refine(const DeviceBatch& b, cudaStream_t s) {
+  k_accumulate<<<b.ntiles, kVecThreads, 0, s>>>(b);
+  k_residual<<<b.ntiles, kSpmvThreads, 0, s>>>(b);
+}
+
+void launch_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s) {
+  k_continue<<<1, 32, 0, s>>>(b.active, b.bodyRuns, (cudaGraphConditionalHandle)handle);
+}
 void launch_finish_step(const DeviceBatch& b, cudaStream_t s) {
   k_finish_step<<<(b.nv + 255) / 256, 256, 0, s>>>(b);
 }
+
+template void launch_assemble<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t);
+template void launch_assemble<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t);
+template void launch_diag_inverse<double>(const DeviceBatch&, const PcgVecs<double>&, int, cudaStream_t);
+template void launch_diag_inverse<float>(const DeviceBatch&, const PcgVecs<float>&, int, cudaStream_t);
+template void launch_inner_init<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t);
+template void launch_inner_init<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t);
+template void launch_spmv<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t);
+template void launch_spmv<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t);
+template void launch_update<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t);
+template void launch_update<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t);
 
 }  // namespace hobak
