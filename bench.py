@@ -12,9 +12,13 @@ CPU restatement of the reference algorithm (oracle/) on the host cores for the
 same workload.
 
 Workloads (synthetic, seeded; see hobakv1_gb300/scenes.py):
-  kuhn40_snh_twist   40^3 Kuhn cube, 384,000 tets, SNH E=1e4 nu=0.45, compressed 0.6 + twisted, FP64
-  kuhn40_arap_twist  same with ARAP
-  kuhn10_snh         10^3 Kuhn cube, 6,000 tets, SNH E=1e3 nu=0.45 (the CPU-runnable case)
+  kuhn40_snh_twist        40^3 Kuhn cube, 384,000 tets, SNH E=1e4 nu=0.45, compressed 0.6 + twisted, FP64
+  kuhn40_arap_twist       same with ARAP
+  kuhn40_snh_twist_mixed  the SNH case with FP32 Hessian/SpMV/inner PCG and FP64 refinement
+  kuhn10_snh              10^3 Kuhn cube, 6,000 tets, SNH E=1e3 nu=0.45 (the CPU-runnable case)
+  mix256_mixed            256 scenes, N ~ U{6..24} cells per side, SNH/ARAP, mu log-uniform,
+                          one batched mixed-precision step = every scene advanced once
+  mix256_fp64             the same mix batched in FP64
 """
 from __future__ import annotations
 
@@ -37,7 +41,10 @@ METRIC = "steps/s, p50/p99 step latency: batched mixed-precision vs plain FP64, 
 WORKLOADS = {
     "kuhn40_snh_twist": dict(kind="config2", N=40, material="snh", precision=0),
     "kuhn40_arap_twist": dict(kind="config2", N=40, material="arap", precision=0),
+    "kuhn40_snh_twist_mixed": dict(kind="config2", N=40, material="snh", precision=1),
     "kuhn10_snh": dict(kind="config1", N=10, material="snh", precision=0),
+    "mix256_mixed": dict(kind="mix", count=256, material="snh/arap", precision=1),
+    "mix256_fp64": dict(kind="mix", count=256, material="snh/arap", precision=0),
 }
 DEFAULT_WORKLOAD = "kuhn40_snh_twist"
 
@@ -48,6 +55,8 @@ def make_scenes(spec):
         return [scenes.config2_scene(spec["N"], spec["material"])]
     if spec["kind"] == "config1":
         return [scenes.config1_scene(spec["N"], spec["material"])]
+    if spec["kind"] == "mix":
+        return scenes.config4_scenes(spec["count"])
     raise ValueError(spec)
 
 
@@ -125,23 +134,50 @@ def ncu_traffic(workload):
         return json.load(f).get(workload, {})
 
 
-def cpu_baseline(scene_list, steps, warmup):
+def cpu_baseline(scene_list, steps, warmup, max_scenes=16):
     """The oracle (CPU restatement of the reference algorithm, OpenMP on all
-    host cores) on the same workload; bounded sample."""
+    host cores) on the same workload; bounded sample.  Large mixes time a
+    seeded subset (every k-th scene) and scale by scene count.
+    Returns (steps/s of the whole workload, per-step seconds, cores, sample)."""
     from oracle import oracle
     oracle.build()
-    sims = [oracle.Sim(s, precond=0) for s in scene_list]
-    for sim in sims:
-        sim.step(warmup) if warmup else None
-    t0 = time.perf_counter()
+    stride = max(1, -(-len(scene_list) // max_scenes))
+    subset = scene_list[::stride]
+    scale = len(scene_list) / len(subset)
+    sims = [oracle.Sim(s, precond=0) for s in subset]
+    if warmup:
+        for sim in sims:
+            sim.step(warmup)
     lat = []
     for _ in range(steps):
         ts = time.perf_counter()
         for sim in sims:
             sim.step(1)
-        lat.append(time.perf_counter() - ts)
+        lat.append((time.perf_counter() - ts) * scale)
+    value = steps / sum(lat)
+    sample = (f"{steps} steps of {len(subset)} of {len(scene_list)} scene(s) (every {stride}th), "
+              f"time scaled by {scale:.1f}" if stride > 1 else f"{steps} steps of all {len(scene_list)} scene(s)")
+    return value, lat, oracle.lib().oracle_threads(), sample
+
+
+def plain_fp64_gpu(scene_list, steps):
+    """The plain FP64 GPU path on a mix: every scene as its own batch, one
+    after another (no batching), same tolerance.  Returns mix steps/s."""
+    import torch
+    from hobakv1_gb300 import hobak
+    batches = [hobak.BATCH([s], hobak.solver_opts(precision=hobak.PRECISION_FP64)) for s in scene_list]
+    for b in batches:
+        b.step(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for b in batches:
+            b.step(1)
+    torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    return steps / dt, lat, oracle.lib().oracle_threads()
+    for b in batches:
+        b.close()
+    return steps / dt
 
 
 def run_reference(args, spec, scene_list):
@@ -150,8 +186,7 @@ def run_reference(args, spec, scene_list):
         return
     steps = max(1, min(args.steps, 5))
     warm = 1 if args.warmup > 0 else 0
-    value, lat, cores = cpu_baseline(scene_list, steps, warm)
-    sample = f"{steps} timed steps after {warm} warm-up of {args.workload} ({len(scene_list)} scene(s))"
+    value, lat, cores, sample = cpu_baseline(scene_list, steps, warm)
     lat_ms = [1e3 * x for x in lat]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": warm, "ms_per_step": 1e3 / value,
@@ -166,11 +201,13 @@ def run_reference(args, spec, scene_list):
 
 
 def config_of(spec, scene_list, preconditioner="block_jacobi"):
-    return {"scenes": len(scene_list), "tets": int(sum(s.nt for s in scene_list)),
-            "verts": int(sum(s.nv for s in scene_list)),
+    nt = int(sum(s.nt for s in scene_list))
+    hess_mb = nt * 90 * (8 if spec["precision"] == 0 else 4) / 1e6
+    return {"scenes": len(scene_list), "tets": nt, "verts": int(sum(s.nv for s in scene_list)),
             "material": spec["material"], "precision": "fp64" if spec["precision"] == 0 else "mixed",
             "pcg_tol": 1e-8, "pcg_max_iters": 1000, "preconditioner": preconditioner,
-            "l2": "per-step working set (element Hessians alone 276 MB at 40^3) exceeds the 129 MB L2; no flush"}
+            "l2": f"each step writes {hess_mb:.0f} MB of element Hessians (> 129 MB L2 at 40^3 and the mix); "
+                  "no explicit flush"}
 
 
 def run_ours(args, spec, scene_list):
@@ -271,9 +308,16 @@ def run_ours(args, spec, scene_list):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         steps = 3 if sum(s.nt for s in scene_list) > 100_000 else 20
-        cv, _, cores = cpu_baseline(scene_list, steps, 0)
+        cv, _, cores, sample = cpu_baseline(scene_list, steps, 0)
         cpu = {"value": cv, "unit": "steps/s", "cores": cores, "kind": "port",
-               "sample": f"{steps} steps of {args.workload} on the host cores (OpenMP), from the initial state"}
+               "sample": sample + f" of {args.workload} on the host cores (OpenMP), from the initial state"}
+
+    # the plain FP64 GPU path (one scene at a time) on the same mix
+    plain = None
+    if spec["kind"] == "mix" and not args.no_plain:
+        pv = plain_fp64_gpu(scene_list, 2)
+        plain = {"value": pv, "unit": "steps/s", "speedup_of_value": value / pv,
+                 "how": "each scene its own FP64 batch (CUDA graph per step), scenes stepped one after another"}
 
     if rank == 0:
         lat_sorted = sorted(lat)
@@ -285,7 +329,8 @@ def run_ours(args, spec, scene_list):
                 "config": {"workload": args.workload, **config_of(spec, scene_list)},
                 "pcg_iters_per_step": float(np.mean(iters)),
                 "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(gpu_launches),
+                "roofline": roofline, "cpu_baseline": cpu, "plain_fp64_gpu": plain, "e2e": e2e,
+                "gpu_launches": int(gpu_launches),
                 "clocks": clock}
         print(json.dumps(line), flush=True)
     batch.close()
@@ -301,6 +346,7 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the unbatched FP64 comparison on mixes")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
     scene_list = make_scenes(spec)

@@ -538,16 +538,16 @@ template <typename T>
 int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, const PcgVecs<T>& v) {
   const DeviceBatch& d = B->d;
   const bool mixed = sizeof(T) == sizeof(float);
-  if (timed) CUDA_TRY(cudaEventRecord(B->ev[0], s));
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[0], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   launch_begin_step(d, s);
   if (mixed) launch_element_mixed(d, s);
   else launch_element(d, s);
-  if (timed) CUDA_TRY(cudaEventRecord(B->ev[1], s));
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[1], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   launch_assemble<T>(d, v, s);
   launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
-  if (timed) CUDA_TRY(cudaEventRecord(B->ev[2], s));
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[2], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   launch_rhs(d, s);
-  if (timed) CUDA_TRY(cudaEventRecord(B->ev[3], s));
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[3], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   const int sweeps = sweeps_of(B->opts);
   for (int k = 0; k < sweeps; k++) {
     launch_set_active(d, s);
@@ -556,9 +556,9 @@ int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, c
     if (rc) return rc;
     if (mixed) launch_refine(d, s);
   }
-  if (timed) CUDA_TRY(cudaEventRecord(B->ev[4], s));
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[4], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   launch_finish_step(d, s);
-  if (timed) CUDA_TRY(cudaEventRecord(B->ev[5], s));
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[5], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   return HOBAK_OK;
 }
 

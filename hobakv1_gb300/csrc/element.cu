@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces, H
   load_tet(tv, b.rest, b.x, X);
   double F[9], U[9], S[3], V[9], P[9], f[12];
   deformation_gradient(X, Dinv, F);
-  svd3_rv(F, U, S, V);
+  svd3_rv_fast(F, U, S, V);
   material_pk1(m, F, U, V, P);
   element_force(P, Dinv, vol, f);
 
@@ -253,7 +253,7 @@ __global__ void k_material_eval(MatParams m, int n, const double* Fin, double* p
   double F[9], U[9], S[3], V[9];
 #pragma unroll
   for (int k = 0; k < 9; k++) F[k] = Fin[9 * (size_t)e + k];
-  svd3_rv(F, U, S, V);
+  svd3_rv_fast(F, U, S, V);
   if (psi) psi[e] = material_psi(m, F, S);
   if (Pout) material_pk1(m, F, U, V, Pout + 9 * (size_t)e);
   if (Hout) {
@@ -286,7 +286,7 @@ __global__ void k_element_eval(int nt, const int4* tets, const double* rest, con
   load_tet(tets[t], rest, x, X);
   double F[9], U[9], S[3], V[9], P[9], f[12];
   deformation_gradient(X, Dinv, F);
-  svd3_rv(F, U, S, V);
+  svd3_rv_fast(F, U, S, V);
   if (Fo)
     for (int k = 0; k < 9; k++) Fo[9 * (size_t)t + k] = F[k];
   if (So)
@@ -324,7 +324,7 @@ __global__ void k_energy(DeviceBatch b) {
   load_tet(b.tets[t], b.rest, b.x, X);
   double F[9], U[9], S[3], V[9];
   deformation_gradient(X, Dinv, F);
-  svd3_rv(F, U, S, V);
+  svd3_rv_fast(F, U, S, V);
   b.psi[t] = b.vol[t] * material_psi(m, F, S);
 }
 

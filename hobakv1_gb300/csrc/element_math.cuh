@@ -17,44 +17,9 @@ __device__ __forceinline__ double det3(const double* A) {
          A[6] * (A[1] * A[5] - A[4] * A[2]);
 }
 
-// Rotation-variant SVD F = U diag(S) V^T (the svd_rv convention,
-// util/MATRIX_UTIL.cpp:76-95): S sorted by magnitude, U and V rotations, the
-// sign of det F carried by S[2].  One-sided Jacobi: plane rotations applied
-// on the right orthogonalise F's columns; V accumulates them.  Converges
-// quadratically; the loop stops when no pair needs a rotation.
-__device__ __forceinline__ void svd3_rv(const double* F, double* U, double* S, double* V) {
-  double A[9];
-#pragma unroll
-  for (int k = 0; k < 9; k++) A[k] = F[k];
-#pragma unroll
-  for (int k = 0; k < 9; k++) V[k] = (k % 4 == 0) ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 12; sweep++) {
-    bool rotated = false;
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-      const int p = (r == 2) ? 1 : 0;
-      const int q = (r == 0) ? 1 : 2;
-      const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
-      const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
-      const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
-      if (fabs(gamma) > 1e-17 * sqrt(alpha * beta)) {
-        rotated = true;
-        const double zeta = (beta - alpha) / (2.0 * gamma);
-        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = rsqrt(1.0 + t * t), s = c * t;
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-          const double x = A[3 * p + i], y = A[3 * q + i];
-          A[3 * p + i] = c * x - s * y;
-          A[3 * q + i] = s * x + c * y;
-          const double vx = V[3 * p + i], vy = V[3 * q + i];
-          V[3 * p + i] = c * vx - s * vy;
-          V[3 * q + i] = s * vx + c * vy;
-        }
-      }
-    }
-    if (!rotated) break;
-  }
+// Sort A's (orthogonal) columns by norm, form U = A / sigma (completing
+// vanishing columns), and fold reflections into S[2] (svd_rv convention).
+__device__ __forceinline__ void svd3_finish(double* A, double* U, double* S, double* V) {
   double n[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) n[k] = A[3 * k] * A[3 * k] + A[3 * k + 1] * A[3 * k + 1] + A[3 * k + 2] * A[3 * k + 2];
@@ -117,6 +82,145 @@ __device__ __forceinline__ void svd3_rv(const double* F, double* U, double* S, d
     V[6] = -V[6]; V[7] = -V[7]; V[8] = -V[8];
     S[2] = -S[2];
   }
+}
+
+// Rotation-variant SVD F = U diag(S) V^T (the svd_rv convention,
+// util/MATRIX_UTIL.cpp:76-95): S sorted by magnitude, U and V rotations, the
+// sign of det F carried by S[2].  One-sided Jacobi: plane rotations applied
+// on the right orthogonalise F's columns; V accumulates them.  Converges
+// quadratically; the loop stops when no pair needs a rotation.
+__device__ __forceinline__ void svd3_rv(const double* F, double* U, double* S, double* V) {
+  double A[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) A[k] = F[k];
+#pragma unroll
+  for (int k = 0; k < 9; k++) V[k] = (k % 4 == 0) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 12; sweep++) {
+    bool rotated = false;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const int p = (r == 2) ? 1 : 0;
+      const int q = (r == 0) ? 1 : 2;
+      const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
+      const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
+      const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
+      if (fabs(gamma) > 1e-17 * sqrt(alpha * beta)) {
+        rotated = true;
+        const double zeta = (beta - alpha) / (2.0 * gamma);
+        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = rsqrt(1.0 + t * t), s = c * t;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double x = A[3 * p + i], y = A[3 * q + i];
+          A[3 * p + i] = c * x - s * y;
+          A[3 * q + i] = s * x + c * y;
+          const double vx = V[3 * p + i], vy = V[3 * q + i];
+          V[3 * p + i] = c * vx - s * vy;
+          V[3 * q + i] = s * vx + c * vy;
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  svd3_finish(A, U, S, V);
+}
+
+// The same SVD with most of the Jacobi work moved off the FP64 pipe, which is
+// the scarce resource on GB300 (FP32 issues far faster):
+//   1. one-sided Jacobi sweeps in FP32 give V32 with F V32 orthogonal to ~1e-7;
+//   2. V32 is re-orthonormalised in FP64 (modified Gram-Schmidt), so V stays an
+//      exact rotation to FP64 precision;
+//   3. FP64 one-sided Jacobi on A = F V finishes the job; starting ~1e-7 from
+//      orthogonal it converges in one sweep (quadratic convergence) and a
+//      second sweep only confirms.  Rotation angles are computed in FP32 and
+//      turned into an exactly orthogonal (c, s) pair in FP64.
+// The result has FP64 accuracy (same convergence test as svd3_rv).
+__device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double* S, double* V) {
+  // ---- stage 1: FP32 Jacobi ----
+  float a[9], w[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    a[k] = float(F[k]);
+    w[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+  }
+  for (int sweep = 0; sweep < 10; sweep++) {
+    bool rotated = false;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const int p = (r == 2) ? 1 : 0;
+      const int q = (r == 0) ? 1 : 2;
+      const float al = a[3 * p] * a[3 * p] + a[3 * p + 1] * a[3 * p + 1] + a[3 * p + 2] * a[3 * p + 2];
+      const float be = a[3 * q] * a[3 * q] + a[3 * q + 1] * a[3 * q + 1] + a[3 * q + 2] * a[3 * q + 2];
+      const float ga = a[3 * p] * a[3 * q] + a[3 * p + 1] * a[3 * q + 1] + a[3 * p + 2] * a[3 * q + 2];
+      if (fabsf(ga) > 1e-6f * sqrtf(al * be)) {
+        rotated = true;
+        const float zeta = (be - al) / (2.0f * ga);
+        const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+        const float c = rsqrtf(1.0f + t * t), s = c * t;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const float x = a[3 * p + i], y = a[3 * q + i];
+          a[3 * p + i] = c * x - s * y;
+          a[3 * q + i] = s * x + c * y;
+          const float vx = w[3 * p + i], vy = w[3 * q + i];
+          w[3 * p + i] = c * vx - s * vy;
+          w[3 * q + i] = s * vx + c * vy;
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  // ---- stage 2: FP64 modified Gram-Schmidt on V32's columns ----
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) V[3 * k + i] = double(w[3 * k + i]);
+#pragma unroll
+    for (int j = 0; j < k; j++) {
+      const double d = V[3 * j] * V[3 * k] + V[3 * j + 1] * V[3 * k + 1] + V[3 * j + 2] * V[3 * k + 2];
+#pragma unroll
+      for (int i = 0; i < 3; i++) V[3 * k + i] -= d * V[3 * j + i];
+    }
+    const double n = rsqrt(V[3 * k] * V[3 * k] + V[3 * k + 1] * V[3 * k + 1] + V[3 * k + 2] * V[3 * k + 2]);
+#pragma unroll
+    for (int i = 0; i < 3; i++) V[3 * k + i] *= n;
+  }
+  // ---- stage 3: FP64 Jacobi on A = F V ----
+  double A[9];
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) A[i + 3 * j] = F[i] * V[3 * j] + F[i + 3] * V[3 * j + 1] + F[i + 6] * V[3 * j + 2];
+  for (int sweep = 0; sweep < 8; sweep++) {
+    bool rotated = false;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const int p = (r == 2) ? 1 : 0;
+      const int q = (r == 0) ? 1 : 2;
+      const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
+      const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
+      const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
+      if (fabs(gamma) > 1e-17 * sqrt(alpha * beta)) {
+        rotated = true;
+        // angle in FP32 (only orthogonality of (c, s) must be FP64-exact)
+        const float zf = float((beta - alpha) / (2.0 * gamma));
+        const float tf = copysignf(1.0f, zf) / (fabsf(zf) + sqrtf(1.0f + zf * zf));
+        const double t = double(tf);
+        const double c = rsqrt(1.0 + t * t), s = c * t;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double x = A[3 * p + i], y = A[3 * q + i];
+          A[3 * p + i] = c * x - s * y;
+          A[3 * q + i] = s * x + c * y;
+          const double vx = V[3 * p + i], vy = V[3 * q + i];
+          V[3 * p + i] = c * vx - s * vy;
+          V[3 * q + i] = s * vx + c * vy;
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  svd3_finish(A, U, S, V);
 }
 
 // Symmetric 3x3 eigensystem by cyclic Jacobi: A = Q diag(L) Q^T.
