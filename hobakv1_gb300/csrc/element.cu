@@ -59,18 +59,22 @@ __device__ __forceinline__ void reduced_hessian(const MatParams& m, const double
 #pragma unroll
     for (int k = 0; k < 9; k++) Q3[k] = (k % 4 == 0) ? T(1) : T(0);
   }
-  // B(a, m) = sum_j DmInv(a, j) V(j, m); U in T
-  T U[9], B[9];
+  // B(a, m) = sum_j DmInv(a, j) V(j, m), computed in T; U in T
+  T U[9], B[9], Dt[9], Vt[9];
 #pragma unroll
-  for (int k = 0; k < 9; k++) U[k] = T(Ud[k]);
+  for (int k = 0; k < 9; k++) {
+    U[k] = T(Ud[k]);
+    Dt[k] = T(Dinv[k]);
+    Vt[k] = T(Vd[k]);
+  }
 #pragma unroll
   for (int mm = 0; mm < 3; mm++)
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-      double s = 0;
+      T s = T(0);
 #pragma unroll
-      for (int j = 0; j < 3; j++) s += Dinv[a + 3 * j] * Vd[j + 3 * mm];
-      B[a + 3 * mm] = T(s);
+      for (int j = 0; j < 3; j++) s += Dt[a + 3 * j] * Vt[j + 3 * mm];
+      B[a + 3 * mm] = s;
     }
   const T rs2 = T(kInvSqrt2);
 #pragma unroll
@@ -218,8 +222,9 @@ __global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces, H
   reduced_hessian<HT>(m, U, S, V, Dinv, Hr);
 
   // He v = -vol D^T Hr (D v): D v = relative velocities of vertices 1..3
+  // (in the mixed path He v is formed in FP32 like He itself)
   const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
-  double dv[9];
+  HT dv[9];
   {
     double v0[3];
 #pragma unroll
@@ -227,16 +232,16 @@ __global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces, H
 #pragma unroll
     for (int a = 0; a < 3; a++)
 #pragma unroll
-      for (int i = 0; i < 3; i++) dv[3 * a + i] = b.v[3 * vid[a + 1] + i] - v0[i];
+      for (int i = 0; i < 3; i++) dv[3 * a + i] = HT(b.v[3 * vid[a + 1] + i] - v0[i]);
   }
   double* g = b.elemG + 12 * (size_t)t;
   double h0[3] = {0.0, 0.0, 0.0};
 #pragma unroll
   for (int r = 0; r < 9; r++) {
-    double s = 0;
+    HT s = HT(0);
 #pragma unroll
-    for (int c = 0; c < 9; c++) s += double((r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)]) * dv[c];
-    const double hv = -vol * s;
+    for (int c = 0; c < 9; c++) s += ((r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)]) * dv[c];
+    const double hv = -vol * double(s);
     h0[r % 3] += hv;
     g[3 + r] = rawForces ? f[3 + r] : dt * (f[3 + r] + dt * hv);
   }

@@ -41,19 +41,24 @@ __device__ __forceinline__ void svd3_finish(double* A, double* U, double* S, dou
   if (n[0] < n[1]) swapcols(0, 1);
   if (n[0] < n[2]) swapcols(0, 2);
   if (n[1] < n[2]) swapcols(1, 2);
+  // sigma = sqrt(n) and 1/sigma from one reciprocal square root each
+  double rs[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) S[k] = sqrt(n[k]);
+  for (int k = 0; k < 3; k++) {
+    rs[k] = n[k] > 0.0 ? rsqrt(n[k]) : 0.0;
+    S[k] = n[k] * rs[k];
+  }
   // U columns; complete vanishing columns with cross products
   const double tiny = 1e-300;
   if (S[0] > tiny) {
-    const double r0 = 1.0 / S[0];
+    const double r0 = rs[0];
 #pragma unroll
     for (int i = 0; i < 3; i++) U[i] = A[i] * r0;
   } else {
     U[0] = 1.0; U[1] = 0.0; U[2] = 0.0;
   }
   if (S[1] > tiny) {
-    const double r1 = 1.0 / S[1];
+    const double r1 = rs[1];
 #pragma unroll
     for (int i = 0; i < 3; i++) U[3 + i] = A[3 + i] * r1;
   } else {
@@ -66,7 +71,7 @@ __device__ __forceinline__ void svd3_finish(double* A, double* U, double* S, dou
     U[3] = w0 * rn; U[4] = w1 * rn; U[5] = w2 * rn;
   }
   if (S[2] > tiny && S[1] > tiny) {
-    const double r2 = 1.0 / S[2];
+    const double r2 = rs[2];
 #pragma unroll
     for (int i = 0; i < 3; i++) U[6 + i] = A[6 + i] * r2;
   } else {
@@ -200,10 +205,10 @@ __device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double*
       const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
       const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
       const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
-      if (fabs(gamma) > 1e-17 * sqrt(alpha * beta)) {
+      if (gamma * gamma > 1e-34 * (alpha * beta)) {
         rotated = true;
         // angle in FP32 (only orthogonality of (c, s) must be FP64-exact)
-        const float zf = float((beta - alpha) / (2.0 * gamma));
+        const float zf = float(beta - alpha) / (2.0f * float(gamma));
         const float tf = copysignf(1.0f, zf) / (fabsf(zf) + sqrtf(1.0f + zf * zf));
         const double t = double(tf);
         const double c = rsqrt(1.0 + t * t), s = c * t;

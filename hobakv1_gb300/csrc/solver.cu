@@ -98,16 +98,18 @@ __global__ void k_begin_step(DeviceBatch b) {
 
 // Sum of one block entry over its element contributions, ascending tet
 // (TET_MESH_FASTER.cpp:113-131 gathers the same entries per non-zero).
+// The sum is formed in HT: FP64 for the FP64 path, FP32 for the mixed path
+// (whose matrix is FP32 anyway; converting every term would load the FP64 pipe).
 template <typename HT>
-__device__ __forceinline__ double gather_block_entry(const DeviceBatch& b, const HT* __restrict__ elemH, int blk,
-                                                     int r, int c) {
-  double sum = 0.0;
+__device__ __forceinline__ HT gather_block_entry(const DeviceBatch& b, const HT* __restrict__ elemH, int blk,
+                                                 int r, int c) {
+  HT sum = HT(0);
   const int k1 = b.blkptr[blk + 1];
   for (int k = b.blkptr[blk]; k < k1; k++) {
     const int src = b.blksrc[k];
     const int t = src >> 4, ea = (src >> 2) & 3, eb = src & 3;
     const HT* H = elemH + (size_t)kElemHess * t;
-    sum += (double)((ea <= eb) ? H[9 * upper_block(ea, eb) + 3 * r + c] : H[9 * upper_block(eb, ea) + 3 * c + r]);
+    sum += (ea <= eb) ? H[9 * upper_block(ea, eb) + 3 * r + c] : H[9 * upper_block(eb, ea) + 3 * c + r];
   }
   return sum;
 }
@@ -119,12 +121,12 @@ __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __res
   if (g >= 9L * b.nblocks) return;
   const int blk = (int)(g / 9), e = (int)(g % 9);
   const int r = e / 3, c = e % 3;
-  const double sum = gather_block_entry(b, elemH, blk, r, c);
+  const HT sum = gather_block_entry(b, elemH, blk, r, c);
   const int u = b.blkRow[blk], w = b.cols[blk];
   const double dt = b.scenes[b.vertexScene[u]].dt;
   const bool fu = b.freeMask[u] != 0, fw = b.freeMask[w] != 0;
-  double val = (fu && fw) ? -(dt * dt) * sum : 0.0;
-  if (u == w && r == c) val += fu ? b.mass[u] : 1.0;
+  HT val = (fu && fw) ? HT(-(dt * dt)) * sum : HT(0);
+  if (u == w && r == c) val += fu ? HT(b.mass[u]) : HT(1);
   lhs[9 * (size_t)blk + e] = T(val);
 }
 

@@ -15,7 +15,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <array>
 #include <limits>
+#include <map>
 #include <numeric>
 #include <vector>
 #ifdef _OPENMP
@@ -646,9 +648,266 @@ double dot(const std::vector<double>& a, const std::vector<double>& b) {
   return s;
 }
 
+// ---------------------------------------------------------------------------
+// Vertex-face self collisions (collision tets, VERTEX_FACE_SQRT_COLLISION).
+// ---------------------------------------------------------------------------
+typedef std::array<double, 3> V3;
+inline V3 sub(const V3& a, const V3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
+inline V3 add(const V3& a, const V3& b) { return {a[0] + b[0], a[1] + b[1], a[2] + b[2]}; }
+inline V3 mul(double s, const V3& a) { return {s * a[0], s * a[1], s * a[2]}; }
+inline double dot3(const V3& a, const V3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline V3 cross3(const V3& a, const V3& b) {
+  return {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+}
+inline double norm3(const V3& a) { return std::sqrt(dot3(a, a)); }
+inline V3 normalized(const V3& a) { return mul(1.0 / norm3(a), a); }
+
+struct Collisions {
+  bool on = false;
+  double eps = 0.01, mu = 1.0, beta = 0.001;
+  std::vector<int> tris;         // 3 per surface triangle, reference winding
+  std::vector<int> surfVerts;    // ascending vertex ids
+  std::vector<int> surfId;       // vertex -> index in surfVerts, or -1
+  std::vector<int> nbr;          // 3 neighbouring triangles per triangle
+  std::vector<double> restArea;  // per surface triangle
+  std::vector<double> ringArea;  // per surface vertex
+  // per step
+  std::vector<int> pairs;        // (vertex, triangle) pairs
+  std::vector<int> ctets;        // 4 per pair: vertex, face[2], face[1], face[0]
+  std::vector<double> weight;    // rest face area + rest vertex one-ring area
+  std::vector<double> f12, H12;  // per pair: -w grad (12), -w clamped Hessian (144, column major)
+};
+
+// Surface triangles in tet order with the reference winding
+// (TET_MESH.cpp:294-350), surface vertices (567-590), triangle neighbours
+// across edges (423-490) and rest areas (494-525).
+void buildSurface(const Mesh& M, Collisions& C) {
+  std::map<std::array<int, 3>, int> counts;
+  auto faces = [&](int t, std::array<int, 3> f[4]) {
+    const int* v = &M.tets[4 * (size_t)t];
+    f[0] = {v[0], v[1], v[3]};
+    f[1] = {v[0], v[2], v[1]};
+    f[2] = {v[0], v[3], v[2]};
+    f[3] = {v[1], v[2], v[3]};
+  };
+  for (int t = 0; t < M.nt; t++) {
+    std::array<int, 3> f[4];
+    faces(t, f);
+    for (auto& x : f) {
+      std::array<int, 3> s = x;
+      std::sort(s.begin(), s.end());
+      counts[s]++;
+    }
+  }
+  C.tris.clear();
+  for (int t = 0; t < M.nt; t++) {
+    std::array<int, 3> f[4];
+    faces(t, f);
+    for (auto& x : f) {
+      std::array<int, 3> s = x;
+      std::sort(s.begin(), s.end());
+      if (counts[s] < 2) C.tris.insert(C.tris.end(), x.begin(), x.end());
+    }
+  }
+  const int ntri = (int)C.tris.size() / 3;
+  std::vector<char> on(M.nv, 0);
+  for (int k : C.tris) on[k] = 1;
+  C.surfVerts.clear();
+  C.surfId.assign(M.nv, -1);
+  for (int v = 0; v < M.nv; v++)
+    if (on[v]) {
+      C.surfId[v] = (int)C.surfVerts.size();
+      C.surfVerts.push_back(v);
+    }
+  std::multimap<std::pair<int, int>, int> edges;
+  for (int i = 0; i < ntri; i++)
+    for (int j = 0; j < 3; j++) {
+      int a = C.tris[3 * i + j], b = C.tris[3 * i + (j + 1) % 3];
+      if (a > b) std::swap(a, b);
+      edges.insert({{a, b}, i});
+    }
+  C.nbr.assign(3 * (size_t)ntri, -1);
+  for (int i = 0; i < ntri; i++)
+    for (int j = 0; j < 3; j++) {
+      int a = C.tris[3 * i + j], b = C.tris[3 * i + (j + 1) % 3];
+      if (a > b) std::swap(a, b);
+      auto range = edges.equal_range({a, b});
+      for (auto it = range.first; it != range.second; ++it)
+        if (it->second != i) C.nbr[3 * i + j] = it->second;
+    }
+  auto restV = [&](int v) { return V3{M.rest[3 * v], M.rest[3 * v + 1], M.rest[3 * v + 2]}; };
+  C.restArea.resize(ntri);
+  C.ringArea.assign(C.surfVerts.size(), 0.0);
+  for (int i = 0; i < ntri; i++) {
+    const V3 a = restV(C.tris[3 * i]), b = restV(C.tris[3 * i + 1]), c = restV(C.tris[3 * i + 2]);
+    C.restArea[i] = 0.5 * norm3(cross3(sub(b, a), sub(c, a)));
+    for (int j = 0; j < 3; j++) C.ringArea[C.surfId[C.tris[3 * i + j]]] += (1.0 / 3.0) * C.restArea[i];
+  }
+}
+
+// TET_MESH::pointProjectsInsideTriangle (TET_MESH.cpp:1296-1317) and the
+// barycentric test it shares with pointTriangleDistance.
+bool projectsInside(const V3& v0, const V3& v1, const V3& v2, const V3& v) {
+  const V3 n = cross3(sub(v1, v0), sub(v2, v0));
+  const double nn = dot3(n, n);
+  const double b0 = dot3(n, cross3(sub(v2, v1), sub(v, v1))) / nn;
+  const double b1 = dot3(n, cross3(sub(v0, v2), sub(v, v2))) / nn;
+  const double b2 = dot3(n, cross3(sub(v1, v0), sub(v, v0))) / nn;
+  return std::fabs(b0) + std::fabs(b1) + std::fabs(b2) - 1.0 < 1e-8;
+}
+
+// TET_MESH::pointTriangleDistance (TET_MESH.cpp:1322-1388)
+double pointTriangleDistance(const V3& v0, const V3& v1, const V3& v2, const V3& v) {
+  const V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+  const V3 n = cross3(e1, e2);
+  if (projectsInside(v0, v1, v2, v)) return std::fabs(dot3(mul(1.0 / norm3(n), n), sub(v, v0)));
+  const V3 e3 = sub(v2, v1), ev = sub(v, v0), ev3 = sub(v, v1);
+  const double big = std::numeric_limits<float>::max();
+  double ed[3] = {big, big, big};
+  const double l1 = norm3(e1), l2 = norm3(e2), l3 = norm3(e3);
+  const double d1 = dot3(mul(1.0 / l1, e1), ev);
+  if (d1 > 0.0 && d1 < l1) ed[0] = norm3(sub(v, add(v0, mul(d1, mul(1.0 / l1, e1)))));
+  const double d2 = dot3(mul(1.0 / l2, e2), ev);
+  if (d2 > 0.0 && d2 < l2) ed[1] = norm3(sub(v, add(v0, mul(d2, mul(1.0 / l2, e2)))));
+  const double d3 = dot3(mul(1.0 / l3, e3), ev3);
+  if (d3 > 0.0 && d3 < l3) ed[2] = norm3(sub(v, add(v1, mul(d3, mul(1.0 / l3, e3)))));
+  const double vmin = std::min(norm3(sub(v, v0)), std::min(norm3(sub(v, v1)), norm3(sub(v, v2))));
+  const double emin = std::min(ed[0], std::min(ed[1], ed[2]));
+  return vmin < emin ? vmin : emin;
+}
+
+// VERTEX_FACE_SQRT_COLLISION on a collision tet (v0 = vertex, v1..v3 = face):
+// gradient (VERTEX_FACE_SQRT_COLLISION.cpp:140-181) and the eigenvalue-clamped
+// Hessian (185-219 with clampEigenvalues, MATRIX_UTIL.cpp:116-127), with the
+// inside barycentric coordinates of COLLISION_UTIL.cpp:314-502.
+void vfSqrt(const V3 v[4], double mu, double eps, double* g, double* H);
+
+void jacobiEigen(int n, std::vector<double>& a, std::vector<double>& q);
+
+void vfBarycentric(const V3 v[4], double bary[3]) {
+  const V3 e1 = sub(v[2], v[1]), e2 = sub(v[3], v[1]);
+  const V3 n = cross3(e1, e2);
+  const V3 nh = mul(1.0 / norm3(n), n);
+  const V3 p = sub(v[0], mul(dot3(nh, sub(v[0], v[1])), nh));
+  const double nn = dot3(n, n);
+  bary[0] = dot3(n, cross3(sub(v[3], v[2]), sub(p, v[2]))) / nn;
+  bary[1] = dot3(n, cross3(sub(v[1], v[3]), sub(p, v[3]))) / nn;
+  bary[2] = dot3(n, cross3(sub(v[2], v[1]), sub(p, v[1]))) / nn;
+  if (bary[0] >= 0.0 && bary[1] >= 0.0 && bary[2] >= 0.0) return;
+  auto lineDist = [](const V3& p0, const V3& p1, const V3& p2) {
+    const V3 e0 = sub(p0, p1), e = sub(p2, p1);
+    const double l = norm3(e);
+    const double proj = dot3(e0, mul(1.0 / l, e));
+    if (proj > 0.0 && proj < l) return norm3(sub(e0, mul(proj, mul(1.0 / l, e))));
+    const double a = norm3(sub(p0, p1)), b = norm3(sub(p0, p2));
+    return a < b ? a : b;
+  };
+  auto lerp = [](const V3& p0, const V3& p1, const V3& p2, double out[2]) {
+    const V3 e0 = sub(p0, p1), e = sub(p2, p1);
+    const double l = norm3(e);
+    const double proj = dot3(e0, mul(1.0 / l, e));
+    if (proj < 0.0) { out[0] = 1.0; out[1] = 0.0; return; }
+    if (proj >= l) { out[0] = 0.0; out[1] = 1.0; return; }
+    const double r = proj / l;
+    out[0] = 1.0 - r;
+    out[1] = r;
+  };
+  const double d12 = lineDist(v[0], v[1], v[2]), d23 = lineDist(v[0], v[2], v[3]), d31 = lineDist(v[0], v[3], v[1]);
+  double l[2];
+  if (d12 <= d23 && d12 <= d31) {
+    lerp(v[0], v[1], v[2], l);
+    bary[0] = l[0]; bary[1] = l[1]; bary[2] = 0.0;
+  } else if (d23 <= d12 && d23 <= d31) {
+    lerp(v[0], v[2], v[3], l);
+    bary[0] = 0.0; bary[1] = l[0]; bary[2] = l[1];
+  } else {
+    lerp(v[0], v[3], v[1], l);
+    bary[0] = l[1]; bary[1] = 0.0; bary[2] = l[0];
+  }
+}
+
+void vfSqrt(const V3 v[4], double mu, double eps, double* g, double* H) {
+  double bary[3];
+  vfBarycentric(v, bary);
+  // reverse(): n = e2 x e0 with e0 = v3 - v2, e1 = v0 - v2, e2 = v1 - v2
+  const V3 e0 = sub(v[3], v[2]), e1 = sub(v[0], v[2]), e2 = sub(v[1], v[2]);
+  const V3 n = normalized(cross3(e2, e0));
+  const bool reversal = dot3(n, e1) < 0;
+  const V3 xs = add(add(mul(bary[0], v[1]), mul(bary[1], v[2])), mul(bary[2], v[3]));
+  const V3 t = sub(v[0], xs);
+  const double tt = dot3(t, t), tm = std::sqrt(tt);
+  const double spring = reversal ? tm + eps : tm - eps;
+  std::fill(g, g + 12, 0.0);
+  std::fill(H, H + 144, 0.0);
+  if (std::fabs(tm) <= 1e-8 || std::fabs(tt) < 1e-8) return;
+  const double c[4] = {1.0, -bary[0], -bary[1], -bary[2]};  // tDiffPartial (MCADAMS_COLLISION.cpp:238-248)
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++) g[3 * a + i] = 2.0 * mu * spring * (1.0 / tm) * c[a] * t[i];
+  // hessian = 2 mu ((1/tt - spring/(tt tm)) (D^T t)(D^T t)^T + (spring/tm) D^T D)
+  std::vector<double> A(144);
+  const double k1 = 1.0 / tt - spring / (tt * tm), k2 = spring / tm;
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++)
+      for (int b = 0; b < 4; b++)
+        for (int j = 0; j < 3; j++) {
+          const double pp = (c[a] * t[i]) * (c[b] * t[j]);
+          const double dd = (i == j) ? c[a] * c[b] : 0.0;
+          A[(3 * a + i) + 12 * (3 * b + j)] = 2.0 * mu * (k1 * pp + k2 * dd);
+        }
+  std::vector<double> Q;
+  jacobiEigen(12, A, Q);  // A -> diagonal, Q eigenvectors (columns)
+  for (int r = 0; r < 12; r++)
+    for (int cc = 0; cc < 12; cc++) {
+      double s = 0;
+      for (int k = 0; k < 12; k++) {
+        const double lam = A[k + 12 * k] > 0.0 ? A[k + 12 * k] : 0.0;
+        s += Q[r + 12 * k] * lam * Q[cc + 12 * k];
+      }
+      H[r + 12 * cc] = s;
+    }
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric n x n matrix (column
+// major, overwritten by its eigenvalues on the diagonal); Q = eigenvectors.
+// Stands in for Eigen::SelfAdjointEigenSolver (MATRIX_UTIL.cpp:116-127).
+void jacobiEigen(int n, std::vector<double>& a, std::vector<double>& q) {
+  q.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) q[i + n * i] = 1.0;
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0, diag = 0;
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) (i == j ? diag : off) += std::fabs(a[i + n * j]);
+    if (off == 0.0 || off <= 1e-20 * diag) break;
+    for (int p = 0; p < n; p++)
+      for (int k = p + 1; k < n; k++) {
+        const double apk = a[p + n * k];
+        if (apk == 0.0) continue;
+        const double theta = (a[k + n * k] - a[p + n * p]) / (2.0 * apk);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int m = 0; m < n; m++) {
+          const double amp = a[m + n * p], amk = a[m + n * k];
+          a[m + n * p] = c * amp - s * amk;
+          a[m + n * k] = s * amp + c * amk;
+        }
+        for (int m = 0; m < n; m++) {
+          const double apm = a[p + n * m], akm = a[k + n * m];
+          a[p + n * m] = c * apm - s * akm;
+          a[k + n * m] = s * apm + c * akm;
+        }
+        for (int m = 0; m < n; m++) {
+          const double qmp = q[m + n * p], qmk = q[m + n * k];
+          q[m + n * p] = c * qmp - s * qmk;
+          q[m + n * k] = s * qmp + c * qmk;
+        }
+      }
+  }
+}
+
 struct Sim {
   Mesh M;
   MaterialParams mat;
+  Collisions coll;
   std::vector<int> pinned;
   std::vector<double> pinTarget;  // 3 per pinned vertex
   std::vector<unsigned char> free;  // per vertex: 1 = free, 0 = pinned (S block = I or 0)
@@ -659,9 +918,112 @@ struct Sim {
   int precond = 0;  // 0 = scalar Jacobi (Eigen DiagonalPreconditioner), 1 = 3x3 block Jacobi
   std::vector<double> x, v, fext;
   std::vector<double> K, A, R, He, fe;
+  std::vector<double> collDiag;  // per vertex 3x3: collision part of LHS's diagonal
+  double collScale = 0.0;        // -(dt beta + dt^2): collision Hessian's weight in A
   int lastIters = 0;
   double lastErr = 0;
 };
+
+// Vertex-face detection at the current displacement: inverted vertices
+// (TET_MESH.cpp:2450-2475), then per surface vertex in ascending order the
+// triangles that pass the narrow phase of
+// TET_MESH_FASTER::computeVertexFaceCollisions (TET_MESH_FASTER.cpp:248-334),
+// brute force instead of the AABB broad phase, in ascending triangle order,
+// and the collision tets of buildVertexFaceCollisionTets (TET_MESH.cpp:1785-1826).
+void vfDetect(Sim& s) {
+  const Mesh& M = s.M;
+  Collisions& C = s.coll;
+  auto pos = [&](int v) {
+    return V3{M.rest[3 * v] + s.x[3 * v], M.rest[3 * v + 1] + s.x[3 * v + 1], M.rest[3 * v + 2] + s.x[3 * v + 2]};
+  };
+  std::vector<char> inverted(M.nv, 0);
+  for (int t = 0; t < M.nt; t++) {
+    const int* tv = &M.tets[4 * (size_t)t];
+    const V3 x0 = pos(tv[0]);
+    double Ds[9], F[9];
+    for (int a = 0; a < 3; a++) {
+      const V3 d = sub(pos(tv[a + 1]), x0);
+      for (int i = 0; i < 3; i++) Ds[i + 3 * a] = d[i];
+    }
+    mul3(Ds, &M.DmInv[9 * (size_t)t], F);
+    if (det3(F) > 0.0) continue;
+    for (int a = 0; a < 4; a++) inverted[tv[a]] = 1;
+  }
+  const int ntri = (int)C.tris.size() / 3;
+  std::vector<char> degenerate(ntri), allInverted(ntri);
+  for (int f = 0; f < ntri; f++) {
+    const int* t = &C.tris[3 * f];
+    const double area = 0.5 * norm3(cross3(sub(pos(t[1]), pos(t[0])), sub(pos(t[2]), pos(t[0]))));
+    degenerate[f] = area / C.restArea[f] < 1e-4;  // surfaceTriangleIsDegenerate (TET_MESH.cpp:2421-2445)
+    allInverted[f] = inverted[t[0]] && inverted[t[1]] && inverted[t[2]];
+  }
+  C.pairs.clear();
+  for (int v : C.surfVerts) {
+    if (inverted[v]) continue;
+    const V3 p = pos(v);
+    for (int f = 0; f < ntri; f++) {
+      const int* t = &C.tris[3 * f];
+      if (degenerate[f] || allInverted[f]) continue;
+      if (t[0] == v || t[1] == v || t[2] == v) continue;
+      const V3 a = pos(t[0]), b = pos(t[1]), c = pos(t[2]);
+      if (!(pointTriangleDistance(a, b, c, p) < C.eps)) continue;
+      bool hit = projectsInside(a, b, c, p);
+      if (!hit) {  // insideCollisionCell (TET_MESH.cpp:1396-1437)
+        const V3 vv[3] = {a, b, c};
+        const V3 n = normalized(cross3(sub(b, a), sub(c, a)));
+        hit = true;
+        for (int k = 0; k < 3 && hit; k++) {
+          const int* tn = &C.tris[3 * C.nbr[3 * f + k]];
+          const V3 na = pos(tn[0]), nb = pos(tn[1]), nc = pos(tn[2]);
+          const V3 nn = normalized(cross3(sub(nb, na), sub(nc, na)));
+          const V3 ne = normalized(add(nn, n));
+          const V3 eij = sub(vv[(k + 1) % 3], vv[k]);
+          const V3 neb = normalized(cross3(ne, eij));
+          if (dot3(neb, sub(p, vv[k])) < 0.0) hit = false;
+        }
+      }
+      if (hit) {
+        C.pairs.push_back(v);
+        C.pairs.push_back(f);
+      }
+    }
+  }
+  const int np = (int)C.pairs.size() / 2;
+  C.ctets.resize(4 * (size_t)np);
+  C.weight.resize(np);
+  for (int k = 0; k < np; k++) {
+    const int v = C.pairs[2 * k], f = C.pairs[2 * k + 1];
+    const int* t = &C.tris[3 * f];
+    C.ctets[4 * k] = v;
+    C.ctets[4 * k + 1] = t[2];
+    C.ctets[4 * k + 2] = t[1];
+    C.ctets[4 * k + 3] = t[0];
+    C.weight[k] = C.restArea[f] + C.ringArea[C.surfId[v]];
+  }
+}
+
+// Collision forces and clamped Hessians per collision tet
+// (TET_MESH.cpp:1831-1877, 2045-2088), both scaled by -weight.
+void vfResponse(Sim& s) {
+  const Mesh& M = s.M;
+  Collisions& C = s.coll;
+  const int np = (int)C.weight.size();
+  C.f12.assign(12 * (size_t)np, 0.0);
+  C.H12.assign(144 * (size_t)np, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < np; k++) {
+    V3 v[4];
+    for (int a = 0; a < 4; a++) {
+      const int id = C.ctets[4 * k + a];
+      v[a] = V3{M.rest[3 * id] + s.x[3 * id], M.rest[3 * id + 1] + s.x[3 * id + 1],
+                M.rest[3 * id + 2] + s.x[3 * id + 2]};
+    }
+    double g[12], H[144];
+    vfSqrt(v, C.mu, C.eps, g, H);
+    for (int i = 0; i < 12; i++) C.f12[12 * (size_t)k + i] = -C.weight[k] * g[i];
+    for (int i = 0; i < 144; i++) C.H12[144 * (size_t)k + i] = -C.weight[k] * H[i];
+  }
+}
 
 // K = sum of element Hessians per block, gathered per row in ascending tet
 // order like TET_MESH_FASTER's _hessianGathers (TET_MESH_FASTER.cpp:113-131);
@@ -715,6 +1077,21 @@ void applyLHS(const Sim& s, const std::vector<double>& A, const std::vector<doub
       y[3 * u + i] = acc;
     }
   }
+  // collision tets: y += S (-(dt beta + dt^2) H_coll) S x, in pair order
+  const Collisions& C = s.coll;
+  for (size_t k = 0; k < C.weight.size(); k++) {
+    const double* H = &C.H12[144 * k];
+    for (int a = 0; a < 4; a++) {
+      const int u = C.ctets[4 * k + a];
+      if (!s.free[u]) continue;
+      for (int b = 0; b < 4; b++) {
+        const int w = C.ctets[4 * k + b];
+        if (!s.free[w]) continue;
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) y[3 * u + i] += s.collScale * H[(3 * a + i) + 12 * (3 * b + j)] * x[3 * w + j];
+      }
+    }
+  }
 }
 
 // Preconditioned CG restating Eigen's conjugate_gradient
@@ -733,7 +1110,9 @@ void pcg(Sim& s, const std::vector<double>& A, const std::vector<double>& rhs, s
       B[0] = B[4] = B[8] = 1.0;
       continue;
     }
-    const double* D = &A[9 * (size_t)M.diag[u]];
+    double D[9];
+    for (int k = 0; k < 9; k++)
+      D[k] = A[9 * (size_t)M.diag[u] + k] + (s.collDiag.empty() ? 0.0 : s.collDiag[9 * (size_t)u + k]);
     if (s.precond == 1) {
       inv3(D, B);
     } else {
@@ -801,6 +1180,37 @@ void step(Sim& s) {
     for (int i = 0; i < 3; i++) s.x[3 * s.pinned[k] + i] = s.pinTarget[3 * k + i];
   assemble(s);
   const double dt = s.dt;
+  // computeCollisionDetection + computeCollisionResponse (TIMESTEPPER.cpp:614-720):
+  // R += f_coll, K += H_coll, C = beta H_coll, so A gains -(dt beta + dt^2) H_coll
+  Collisions& C = s.coll;
+  C.weight.clear();
+  s.collDiag.clear();
+  std::vector<double> collKv;
+  if (C.on) {
+    vfDetect(s);
+    vfResponse(s);
+    s.collScale = -(dt * C.beta + dt * dt);
+    std::vector<double> fc(3 * (size_t)nv, 0.0);
+    collKv.assign(3 * (size_t)nv, 0.0);
+    s.collDiag.assign(9 * (size_t)nv, 0.0);
+    for (size_t k = 0; k < C.weight.size(); k++) {
+      const double* H = &C.H12[144 * k];
+      for (int a = 0; a < 4; a++) {
+        const int u = C.ctets[4 * k + a];
+        for (int i = 0; i < 3; i++) fc[3 * u + i] += C.f12[12 * k + 3 * a + i];
+        for (int b = 0; b < 4; b++) {
+          const int w = C.ctets[4 * k + b];
+          for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+              const double h = H[(3 * a + i) + 12 * (3 * b + j)];
+              collKv[3 * u + i] += h * s.v[3 * w + j];
+              if (u == w && s.free[u]) s.collDiag[9 * (size_t)u + i + 3 * j] += s.collScale * h;
+            }
+        }
+      }
+    }
+    for (size_t k = 0; k < fc.size(); k++) s.R[k] = s.R[k] + fc[k];
+  }
   // K v
   std::vector<double> Kv(3 * (size_t)nv);
 #pragma omp parallel for schedule(static)
@@ -819,7 +1229,8 @@ void step(Sim& s) {
   for (int u = 0; u < nv; u++)
     for (int i = 0; i < 3; i++) {
       const size_t k = 3 * (size_t)u + i;
-      const double b = dt * (s.R[k] + dt * Kv[k] + s.fext[k]);
+      const double kv = collKv.empty() ? Kv[k] : Kv[k] + collKv[k];
+      const double b = dt * (s.R[k] + dt * kv + s.fext[k]);
       rhs[k] = s.free[u] ? b : 0.0;
     }
   s.A.resize(s.K.size());
@@ -960,6 +1371,41 @@ int oracle_step(void* h, int nsteps, int* iters, double* errs) {
 }
 
 int oracle_nblocks(void* h) { return static_cast<Sim*>(h)->M.rowptr.back(); }
+
+// Vertex-face self collisions on (eps = collision distance, mu = stiffness,
+// beta = damping), like TIMESTEPPER's flags and setCollisionEps.
+int oracle_set_collisions(void* h, int vf_on, double eps, double mu, double beta) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  s->coll.on = vf_on != 0;
+  s->coll.eps = eps;
+  s->coll.mu = mu;
+  s->coll.beta = beta;
+  if (s->coll.on && s->coll.tris.empty()) buildSurface(s->M, s->coll);
+  return 0;
+}
+
+// Detect at the current state; returns the number of pairs and copies up to
+// cap (vertex, triangle) pairs.  surface triangles: 3 ints each when tris != NULL.
+int oracle_vf_pairs(void* h, int* pairs, int cap, int* tris) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  if (s->coll.tris.empty()) buildSurface(s->M, s->coll);
+  vfDetect(*s);
+  const int np = (int)s->coll.pairs.size() / 2;
+  for (int k = 0; k < std::min(np, cap); k++) {
+    pairs[2 * k] = s->coll.pairs[2 * k];
+    pairs[2 * k + 1] = s->coll.pairs[2 * k + 1];
+  }
+  if (tris) std::copy(s->coll.tris.begin(), s->coll.tris.end(), tris);
+  return np;
+}
+
+int oracle_num_surface_triangles(void* h) {
+  Sim* s = static_cast<Sim*>(h);
+  if (s->coll.tris.empty()) buildSurface(s->M, s->coll);
+  return (int)s->coll.tris.size() / 3;
+}
 
 // BSR pattern (rowptr V+1, cols nblocks) and, at the current displacement,
 // the assembled stiffness K (9 per block, column major) and forces R (3V).
