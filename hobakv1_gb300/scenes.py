@@ -190,3 +190,22 @@ def config4_scenes(count: int = 256, nmin: int = 6, nmax: int = 24,
         out.append(Scene(f"mix{s}_n{N}_{material}", rest, tets, material, mu, lam,
                          top_layer(N), zeros.copy(), zeros.copy(), N=N))
     return out
+
+
+def two_cubes_scene(N: int = 8, gap: float = 5e-4, offset: float = 0.1, material: str = "snh",
+                    E: float = 1e4, nu: float = 0.45, jitter: float = 0.002, seed: int = BASE_SEED + 5) -> Scene:
+    """Two Kuhn cubes in one mesh, the upper one resting `gap` above the lower
+    one and shifted by `offset` in x and z, so their faces start inside the
+    vertex-face collision distance.  The lower cube's bottom face (j = 0) is
+    pinned; contact between the cubes is vertex-face self collision."""
+    rest_a, tets_a = kuhn_cube(N, jitter=jitter, seed=seed)
+    rest_b, tets_b = kuhn_cube(N, jitter=jitter, seed=seed + 1)
+    rest_b = rest_b + np.array([offset, 1.0 + gap, offset])
+    rest = np.concatenate([rest_a, rest_b])
+    tets = np.concatenate([tets_a, tets_b + len(rest_a)]).astype(np.int32)
+    n1 = N + 1
+    k, i = np.meshgrid(np.arange(n1), np.arange(n1), indexing="ij")
+    bottom = (i.reshape(-1) + n1 * (0 + n1 * k.reshape(-1))).astype(np.int32)
+    mu, lam = lame(E, nu)
+    zeros = np.zeros_like(rest)
+    return Scene(f"two_cubes{N}_{material}", rest, tets, material, mu, lam, bottom, zeros.copy(), zeros.copy(), N=N)

@@ -50,6 +50,10 @@ def lib():
         L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp]
         L.oracle_nblocks.argtypes = [ctypes.c_void_p]
         L.oracle_assemble.argtypes = [ctypes.c_void_p, _ip, _ip, _dp, _dp]
+        L.oracle_set_collisions.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double]
+        L.oracle_vf_pairs.argtypes = [ctypes.c_void_p, _ip, ctypes.c_int, _ip]
+        L.oracle_num_surface_triangles.argtypes = [ctypes.c_void_p]
         L.oracle_energy.argtypes = [ctypes.c_void_p]
         L.oracle_energy.restype = ctypes.c_double
         _lib = L
@@ -106,6 +110,20 @@ class Sim:
         pins = np.ascontiguousarray(scene.pinned, dtype=np.int32)
         assert L.oracle_attach_pins(self.h, len(pins), _i(pins)) == 0
         L.oracle_set_solver(self.h, tol, maxit, precond)
+
+    def set_collisions(self, vf=True, eps=0.01, mu=1.0, beta=0.001):
+        """Vertex-face self collisions (TIMESTEPPER.cpp:83-86 defaults: mu 1, beta 0.001)."""
+        assert lib().oracle_set_collisions(self.h, int(vf), eps, mu, beta) == 0
+
+    def vf_pairs(self):
+        """(vertex, surface triangle) pairs at the current state, and the surface triangles."""
+        L = lib()
+        ntri = L.oracle_num_surface_triangles(self.h)
+        tris = np.zeros(3 * ntri, dtype=np.int32)
+        cap = 1 << 20
+        pairs = np.zeros(2 * cap, dtype=np.int32)
+        n = L.oracle_vf_pairs(self.h, _i(pairs), cap, _i(tris))
+        return pairs[:2 * n].reshape(-1, 2), tris.reshape(-1, 3)
 
     def step(self, n=1):
         iters = np.zeros(n, dtype=np.int32)

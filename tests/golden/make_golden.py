@@ -65,8 +65,24 @@ def make_trajectories():
         print("trajectory", s.name, r["iters"].sum())
 
 
+def make_collisions():
+    """Two cubes in contact: vertex-face pairs (reference AABB broad phase +
+    narrow phase) at the start and along a 40-step trajectory with collisions."""
+    s = scenes.two_cubes_scene(6)
+    r = refrun.run(s, 40, stride=10, vf=True, coll_eps=1e-3, coll_mu=1e3, coll_beta=0.001)
+    pairs = {}
+    for k in range(r["x"].shape[0]):
+        c = refrun.collide(s.rest, s.tets, r["x"][k], 1e-3)
+        pairs[f"pairs_{k}"] = c["vf_pairs"]
+    np.savez_compressed(os.path.join(OUT, f"traj_{s.name}_vf.npz"), x=r["x"], v=r["v"], iters=r["iters"],
+                        steps=40, stride=10, surface_triangles=c["surface_triangles"],
+                        surface_vertices=c["surface_vertices"], **pairs)
+    print("collisions", s.name, [len(v) for v in pairs.values()])
+
+
 if __name__ == "__main__":
     if not refrun.available():
         sys.exit("reference build missing: make -C oracle/ref REF=<reference checkout>")
     make_elements()
     make_trajectories()
+    make_collisions()
