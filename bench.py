@@ -220,7 +220,7 @@ def run_ours(args, spec, scene_list):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    opts = hobak.solver_opts(precision=spec["precision"])
+    opts = hobak.solver_opts(precision=spec["precision"], use_graph=not args.eager)
     batch = hobak.BATCH(scene_list, opts)
     stream = torch.cuda.ExternalStream(batch.stream_handle())
 
@@ -347,6 +347,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the unbatched FP64 comparison on mixes")
+    ap.add_argument("--eager", action="store_true",
+                    help="launch kernels one by one instead of the step graph (for per-kernel profilers)")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
     scene_list = make_scenes(spec)

@@ -69,6 +69,10 @@ SIGNATURES = {
     "hobak_batch_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "hobak_batch_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "hobak_batch_kernel_bytes": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "hobak_batch_set_collisions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_double]),
+    "hobak_batch_collision_pairs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, _ip,
+                                                   ctypes.c_int, _ip, _ip]),
     "hobak_element_eval_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.POINTER(HobakMaterial), ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -4,7 +4,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <map>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -82,6 +84,12 @@ struct hobak_batch_t {
   int lastStatus = HOBAK_OK;
   std::vector<SolveState> lastSolve;
   std::vector<int> hostRowptr, hostCols;
+  std::vector<double> restHost;  // rest positions (surface areas for collisions)
+  // vertex-face collisions
+  std::vector<CollisionScene> collScenes;
+  std::vector<int> surfTri, surfTriStart, svHost, svStart;  // global ids; per-scene ranges
+  void* collArena = nullptr;
+  size_t collBytes = 0;
   int* pinnedActive = nullptr;   // pinned host word for the convergence poll
   long long launches = 0;        // kernels launched by this batch
   bool timing = false;
@@ -442,6 +450,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   CUDA_TRY(up(d.tileV0, tileV0.data(), sizeof(int) * ntiles));
   CUDA_TRY(up(d.tileV1, tileV1.data(), sizeof(int) * ntiles));
   B->hostRowptr = rowptr;
+  B->restHost = rest;
   B->hostCols = cols;
   return HOBAK_OK;
 }
@@ -542,8 +551,10 @@ int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, c
   launch_begin_step(d, s);
   if (mixed) launch_element_mixed(d, s);
   else launch_element(d, s);
+  if (d.collOn) launch_collisions(d, d.coll, s);
   if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[1], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   launch_assemble<T>(d, v, s);
+  if (d.collOn) launch_collision_diag<T>(d, d.coll, v.lhs, s);
   launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
   if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[2], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   launch_rhs(d, s);
@@ -596,6 +607,182 @@ void drop_graphs(hobak_batch_t* B) {
       cudaGraphExecDestroy(g);
       g = nullptr;
     }
+}
+
+// Surfaces of every scene (TET_MESH.cpp:294-350 order and winding, surface
+// vertices 567-590, triangle neighbours 423-490, rest areas 494-525) and the
+// device buffers of the per-step collision pipeline.
+int build_collisions(hobak_batch_t* B) {
+  const int n = (int)B->scenes.size();
+  const auto& rest = B->restHost;
+  B->surfTri.clear();
+  B->svHost.clear();
+  B->surfTriStart.assign(1, 0);
+  B->svStart.assign(1, 0);
+  std::vector<int> triScene, triNbr, svScene;
+  std::vector<double> triArea, svArea;
+  auto area = [&](int a, int b2, int c) {
+    double e1[3], e2[3];
+    for (int i = 0; i < 3; i++) {
+      e1[i] = rest[3 * (size_t)b2 + i] - rest[3 * (size_t)a + i];
+      e2[i] = rest[3 * (size_t)c + i] - rest[3 * (size_t)a + i];
+    }
+    const double x = e1[1] * e2[2] - e1[2] * e2[1], y = e1[2] * e2[0] - e1[0] * e2[2], z = e1[0] * e2[1] - e1[1] * e2[0];
+    return 0.5 * std::sqrt(x * x + y * y + z * z);
+  };
+  for (int s = 0; s < n; s++) {
+    const SceneHost& H = B->scenes[s];
+    // faces with their sorted keys; a face is on the surface if its key occurs once
+    std::vector<std::array<int, 5>> keys;  // sorted triple, tet-local face index, position
+    keys.reserve(4 * (size_t)H.nt);
+    std::vector<std::array<int, 3>> faces(4 * (size_t)H.nt);
+    for (int t = 0; t < H.nt; t++) {
+      const int* v = &B->tetsHost[4 * (size_t)(H.t0 + t)];
+      const std::array<int, 3> f[4] = {{v[0], v[1], v[3]}, {v[0], v[2], v[1]}, {v[0], v[3], v[2]}, {v[1], v[2], v[3]}};
+      for (int k = 0; k < 4; k++) {
+        faces[4 * (size_t)t + k] = f[k];
+        std::array<int, 3> sk = f[k];
+        std::sort(sk.begin(), sk.end());
+        keys.push_back({sk[0], sk[1], sk[2], 0, 4 * t + k});
+      }
+    }
+    std::sort(keys.begin(), keys.end());
+    std::vector<char> surface(4 * (size_t)H.nt, 0);
+    for (size_t i = 0; i < keys.size();) {
+      size_t j = i;
+      while (j < keys.size() && keys[j][0] == keys[i][0] && keys[j][1] == keys[i][1] && keys[j][2] == keys[i][2]) j++;
+      if (j - i < 2) surface[keys[i][4]] = 1;
+      i = j;
+    }
+    const int triBase = (int)B->surfTri.size() / 3;
+    for (size_t k = 0; k < surface.size(); k++)
+      if (surface[k]) {
+        B->surfTri.insert(B->surfTri.end(), faces[k].begin(), faces[k].end());
+        triScene.push_back(s);
+      }
+    const int ntri = (int)B->surfTri.size() / 3 - triBase;
+    // surface vertices, ascending
+    std::vector<int> sv;
+    for (int k = 3 * triBase; k < 3 * (triBase + ntri); k++) sv.push_back(B->surfTri[k]);
+    std::sort(sv.begin(), sv.end());
+    sv.erase(std::unique(sv.begin(), sv.end()), sv.end());
+    const int svBase = (int)B->svHost.size();
+    B->svHost.insert(B->svHost.end(), sv.begin(), sv.end());
+    svScene.insert(svScene.end(), sv.size(), s);
+    svArea.resize(B->svHost.size(), 0.0);
+    // neighbours across each edge (the other triangle sharing it)
+    std::map<std::pair<int, int>, std::vector<int>> edges;
+    for (int i = 0; i < ntri; i++)
+      for (int j = 0; j < 3; j++) {
+        int a = B->surfTri[3 * (triBase + i) + j], c = B->surfTri[3 * (triBase + i) + (j + 1) % 3];
+        if (a > c) std::swap(a, c);
+        edges[{a, c}].push_back(triBase + i);
+      }
+    for (int i = 0; i < ntri; i++) {
+      const int f = triBase + i;
+      for (int j = 0; j < 3; j++) {
+        int a = B->surfTri[3 * f + j], c = B->surfTri[3 * f + (j + 1) % 3];
+        if (a > c) std::swap(a, c);
+        int nb = -1;
+        for (int g : edges[{a, c}])
+          if (g != f) nb = g;
+        triNbr.push_back(nb);
+      }
+      const double A = area(B->surfTri[3 * f], B->surfTri[3 * f + 1], B->surfTri[3 * f + 2]);
+      triArea.push_back(A);
+      for (int j = 0; j < 3; j++) {
+        const int v = B->surfTri[3 * f + j];
+        const int id = svBase + int(std::lower_bound(sv.begin(), sv.end(), v) - sv.begin());
+        svArea[id] += (1.0 / 3.0) * A;
+      }
+    }
+    B->surfTriStart.push_back((int)B->surfTri.size() / 3);
+    B->svStart.push_back((int)B->svHost.size());
+  }
+  const int ntri = (int)B->surfTri.size() / 3, nsv = (int)B->svHost.size(), nv = B->nv;
+  int hash = 1024;
+  while (hash < 16 * std::max(ntri, 1)) hash <<= 1;
+  const int cap = std::max(nsv * kMaxPairsPerVertex, 1);
+  const int scanBlocks = (std::max(std::max(hash, nsv), nv) + 1023) / 1024 + 1;
+  Arena A;
+  const size_t oScenes = A.reserve(sizeof(CollisionScene) * n);
+  const size_t oTri = A.reserve(sizeof(int) * 3 * (size_t)ntri), oTriScene = A.reserve(sizeof(int) * ntri);
+  const size_t oTriArea = A.reserve(sizeof(double) * ntri), oTriNbr = A.reserve(sizeof(int) * 3 * (size_t)ntri);
+  const size_t oSv = A.reserve(sizeof(int) * nsv), oSvScene = A.reserve(sizeof(int) * nsv);
+  const size_t oSvArea = A.reserve(sizeof(double) * nsv);
+  const size_t oCell = A.reserve(sizeof(unsigned) * n), oInv = A.reserve(nv), oSkip = A.reserve(ntri);
+  const size_t oBucket = A.reserve(sizeof(int) * (hash + 1)), oCursor = A.reserve(sizeof(int) * hash);
+  const size_t oEntry = A.reserve(sizeof(int) * 8 * (size_t)ntri);
+  const size_t oSvCount = A.reserve(sizeof(int) * (nsv + 1));
+  const size_t oCand = A.reserve(sizeof(int) * (size_t)kMaxPairsPerVertex * nsv);
+  const size_t oOver = A.reserve(sizeof(int)), oNp = A.reserve(sizeof(int));
+  const size_t oPairTet = A.reserve(sizeof(int4) * (size_t)cap), oPairC = A.reserve(sizeof(double) * 4 * (size_t)cap);
+  const size_t oPairG = A.reserve(sizeof(double) * 9 * (size_t)cap);
+  const size_t oPairR = A.reserve(sizeof(double) * 12 * (size_t)cap);
+  const size_t oIncCount = A.reserve(sizeof(int) * (nv + 1)), oIncCursor = A.reserve(sizeof(int) * nv);
+  const size_t oIncList = A.reserve(sizeof(int) * 4 * (size_t)cap);
+  const size_t oScan = A.reserve(sizeof(int) * scanBlocks);
+  void* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, A.used);
+  if (e != cudaSuccess)
+    return fail(e == cudaErrorMemoryAllocation ? HOBAK_ERR_NO_MEMORY : HOBAK_ERR_CUDA,
+                std::string("cudaMalloc of collision buffers: ") + cudaGetErrorString(e));
+  B->collArena = base;
+  B->collBytes = A.used;
+  CUDA_TRY(cudaMemset(base, 0, A.used));
+  DeviceCollisions& c = B->d.coll;
+  c.nscenes = n;
+  c.ntri = ntri;
+  c.nsv = nsv;
+  c.nv = nv;
+  c.hashSize = hash;
+  c.pairCap = cap;
+  c.scenes = carve<CollisionScene>(base, oScenes);
+  c.tri = carve<int>(base, oTri);
+  c.triScene = carve<int>(base, oTriScene);
+  c.triArea = carve<double>(base, oTriArea);
+  c.triNbr = carve<int>(base, oTriNbr);
+  c.sv = carve<int>(base, oSv);
+  c.svScene = carve<int>(base, oSvScene);
+  c.svArea = carve<double>(base, oSvArea);
+  c.cellBits = carve<unsigned>(base, oCell);
+  c.vInverted = carve<unsigned char>(base, oInv);
+  c.triSkip = carve<unsigned char>(base, oSkip);
+  c.bucketCount = carve<int>(base, oBucket);
+  c.bucketCursor = carve<int>(base, oCursor);
+  c.entryTri = carve<int>(base, oEntry);
+  c.svCount = carve<int>(base, oSvCount);
+  c.svCand = carve<int>(base, oCand);
+  c.overflow = carve<int>(base, oOver);
+  c.npairs = carve<int>(base, oNp);
+  c.pairTet = carve<int4>(base, oPairTet);
+  c.pairC = carve<double>(base, oPairC);
+  c.pairG = carve<double>(base, oPairG);
+  c.pairRhs = carve<double>(base, oPairR);
+  c.incCount = carve<int>(base, oIncCount);
+  c.incCursor = carve<int>(base, oIncCursor);
+  c.incList = carve<int>(base, oIncList);
+  c.scanTmp = carve<int>(base, oScan);
+  B->collScenes.assign(n, CollisionScene{0, 0, 0, 0, 0, 0.01, 1.0, 0.001});
+  for (int s = 0; s < n; s++) {
+    B->collScenes[s].tri0 = B->surfTriStart[s];
+    B->collScenes[s].ntri = B->surfTriStart[s + 1] - B->surfTriStart[s];
+    B->collScenes[s].sv0 = B->svStart[s];
+    B->collScenes[s].nsv = B->svStart[s + 1] - B->svStart[s];
+  }
+  auto up = [&](const void* dst, const void* src, size_t bytes) {
+    return bytes ? cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+  };
+  CUDA_TRY(up(c.scenes, B->collScenes.data(), sizeof(CollisionScene) * n));
+  CUDA_TRY(up(c.tri, B->surfTri.data(), sizeof(int) * B->surfTri.size()));
+  CUDA_TRY(up(c.triScene, triScene.data(), sizeof(int) * triScene.size()));
+  CUDA_TRY(up(c.triArea, triArea.data(), sizeof(double) * triArea.size()));
+  CUDA_TRY(up(c.triNbr, triNbr.data(), sizeof(int) * triNbr.size()));
+  CUDA_TRY(up(c.sv, B->svHost.data(), sizeof(int) * B->svHost.size()));
+  CUDA_TRY(up(c.svScene, svScene.data(), sizeof(int) * svScene.size()));
+  CUDA_TRY(up(c.svArea, svArea.data(), sizeof(double) * svArea.size()));
+  B->d.collOn = 1;
+  return HOBAK_OK;
 }
 
 // Enqueue nsteps steps; with graphs nothing waits on the host in between.
@@ -705,6 +892,7 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
 
 int hobak_batch_destroy(hobak_batch b) {
   if (!b) return HOBAK_OK;
+  if (b->collArena) cudaFree(b->collArena);
   drop_graphs(b);
   if (b->captureStream) cudaStreamDestroy(b->captureStream);
   for (auto& e : b->ev)
@@ -745,6 +933,12 @@ int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats) {
     }
   }
   if (status == HOBAK_ERR_NAN) return fail(status, "non-finite residual in PCG");
+  if (b->d.collOn) {
+    int over = 0;
+    CUDA_TRY(cudaMemcpy(&over, b->d.coll.overflow, sizeof(int), cudaMemcpyDeviceToHost));
+    if (over)
+      return fail(HOBAK_ERR_OVERFLOW, "a surface vertex had more than 16 vertex-face candidates; contacts were dropped");
+  }
   return status;
 }
 
@@ -784,6 +978,62 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   b->opts = *opts;
   drop_graphs(b);
   return upload_solver_opts(b);
+}
+
+int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, double stiffness,
+                               double damping_beta) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  if (vf_on && !(eps > 0.0)) return fail(HOBAK_ERR_INVALID, "collision distance must be > 0");
+  if (!b->collArena) {
+    int rc = build_collisions(b);
+    if (rc) return rc;
+  }
+  CollisionScene& cs = b->collScenes[scene];
+  cs.vfOn = vf_on ? 1 : 0;
+  cs.eps = eps;
+  cs.mu = stiffness;
+  cs.beta = damping_beta;
+  CUDA_TRY(cudaMemcpy(const_cast<CollisionScene*>(b->d.coll.scenes), b->collScenes.data(),
+                      sizeof(CollisionScene) * b->collScenes.size(), cudaMemcpyHostToDevice));
+  drop_graphs(b);
+  return HOBAK_OK;
+}
+
+int hobak_batch_collision_pairs(hobak_batch b, int scene, int detect_now, int* npairs, int* pairs, int cap,
+                                int* ntris, int* tris) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  if (!b->collArena) {
+    int rc = build_collisions(b);
+    if (rc) return rc;
+  }
+  const SceneHost& H = b->scenes[scene];
+  const int t0 = b->surfTriStart[scene], t1 = b->surfTriStart[scene + 1];
+  const int s0 = b->svStart[scene], s1 = b->svStart[scene + 1];
+  if (ntris) *ntris = t1 - t0;
+  if (tris)
+    for (int k = 3 * t0; k < 3 * t1; k++) tris[k - 3 * t0] = b->surfTri[k] - H.v0;
+  if (detect_now) {
+    launch_begin_step(b->d, b->stream);
+    launch_collisions(b->d, b->d.coll, b->stream);
+    CUDA_TRY(cudaGetLastError());
+  }
+  std::vector<int> offs(s1 - s0 + 1), cand((size_t)kMaxPairsPerVertex * (s1 - s0));
+  CUDA_TRY(cudaMemcpyAsync(offs.data(), b->d.coll.svCount + s0, sizeof(int) * offs.size(), cudaMemcpyDeviceToHost,
+                           b->stream));
+  CUDA_TRY(cudaMemcpyAsync(cand.data(), b->d.coll.svCand + (size_t)kMaxPairsPerVertex * s0,
+                           sizeof(int) * cand.size(), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  int n = 0;
+  for (int i = 0; i < s1 - s0; i++) {
+    const int c = offs[i + 1] - offs[i];
+    for (int j = 0; j < c; j++, n++)
+      if (pairs && n < cap) {
+        pairs[2 * n] = b->svHost[s0 + i] - H.v0;
+        pairs[2 * n + 1] = cand[(size_t)kMaxPairsPerVertex * i + j] - t0;
+      }
+  }
+  if (npairs) *npairs = n;
+  return HOBAK_OK;
 }
 
 int hobak_batch_device_bytes(hobak_batch b, long long* bytes) {

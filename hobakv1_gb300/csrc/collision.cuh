@@ -1,0 +1,65 @@
+// Vertex-face self-collision data of a batch (device side).
+//
+// Surfaces are extracted once on the host (TET_MESH.cpp:294-350 order and
+// winding); every step the GPU rebuilds a spatial hash of the surface
+// triangles, runs the reference's narrow phase per surface vertex, and turns
+// each (vertex, triangle) pair into a collision tet with a spring force and an
+// eigen-clamped Hessian (VERTEX_FACE_SQRT_COLLISION).  All lists are built in
+// a fixed order (pairs sorted by scene, surface vertex, triangle; per-vertex
+// incidences sorted by pair), so results are deterministic.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace hobak {
+
+constexpr int kMaxPairsPerVertex = 16;  // candidate triangles kept per surface vertex
+
+struct CollisionScene {
+  int vfOn;
+  int tri0, ntri;   // surface triangle range
+  int sv0, nsv;     // surface vertex range
+  double eps, mu, beta;
+};
+
+struct DeviceCollisions {
+  int nscenes, ntri, nsv, nv, hashSize, pairCap;
+  const CollisionScene* scenes;
+  // surface (static)
+  const int* tri;          // [ntri][3] global vertex ids, reference winding
+  const int* triScene;     // [ntri]
+  const double* triArea;   // [ntri] rest area
+  const int* triNbr;       // [ntri][3] neighbouring triangle across edge (j, j+1)
+  const int* sv;           // [nsv] global vertex ids, ascending per scene
+  const int* svScene;      // [nsv]
+  const double* svArea;    // [nsv] rest one-ring area
+  // per step
+  unsigned* cellBits;      // [nscenes] largest triangle extent (float bits) -> cell size
+  unsigned char* vInverted;  // [nv]
+  unsigned char* triSkip;    // [ntri] degenerate or all-inverted
+  int* bucketCount;        // [hashSize + 1] then exclusive scan
+  int* bucketCursor;       // [hashSize]
+  int* entryTri;           // [8 * ntri]
+  int* svCount;            // [nsv + 1] then exclusive scan
+  int* svCand;             // [nsv][kMaxPairsPerVertex]
+  int* overflow;           // [1] set when a vertex had more candidates than fit
+  int* npairs;             // [1]
+  int4* pairTet;           // [pairCap] collision tet (v, f2, f1, f0)
+  double* pairC;           // [pairCap][4] (1, -b0, -b1, -b2)
+  double* pairG;           // [pairCap][9] 3x3 factor of the clamped Hessian, times -w 2 mu
+  double* pairRhs;         // [pairCap][12] dt (f + dt H v)
+  int* incCount;           // [nv + 1] then exclusive scan
+  int* incCursor;          // [nv]
+  int* incList;            // [4 * pairCap] pair * 4 + slot
+  int* scanTmp;            // block sums for the device-wide scans
+};
+
+struct DeviceBatch;
+
+// Enqueue the per-step detection and response (after the element kernel,
+// before assembly uses them).  dtScale: per-scene dt taken from the batch.
+void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStream_t s);
+// Adds the collision part of LHS's diagonal blocks (before the preconditioner).
+template <typename T>
+void launch_collision_diag(const DeviceBatch& b, const DeviceCollisions& c, T* lhs, cudaStream_t s);
+
+}  // namespace hobak

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "collision.cuh"
 #include "common.cuh"
 
 namespace hobak {
@@ -71,6 +72,9 @@ struct DeviceBatch {
   PcgVecs<float> v32;   // mixed path
   double* partial;      // [ntiles][kPartials]
   double* psi;          // [T] energy density scratch
+  // vertex-face collisions (collOn = 0: none in this batch)
+  int collOn;
+  DeviceCollisions coll;
 };
 
 void launch_begin_step(const DeviceBatch& b, cudaStream_t s);

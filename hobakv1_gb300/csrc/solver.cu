@@ -205,6 +205,14 @@ __global__ void __launch_bounds__(kVecThreads) k_rhs(DeviceBatch b) {
       for (int i = 0; i < 3; i++) acc[i] += g[i];
     }
     const bool fu = b.freeMask[u] != 0;
+    if (b.collOn && fu) {  // collision tets: dt (f + dt H v), in pair order
+      for (int k = b.coll.incCount[u]; k < b.coll.incCount[u + 1]; k++) {
+        const int e = b.coll.incList[k];
+        const double* g = b.coll.pairRhs + 12 * (size_t)(e >> 2) + 3 * (e & 3);
+#pragma unroll
+        for (int i = 0; i < 3; i++) acc[i] += g[i];
+      }
+    }
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       const double ri = fu ? acc[i] + dt * b.fext[3 * u + i] : 0.0;
@@ -309,6 +317,33 @@ __global__ void __launch_bounds__(kVecThreads) k_inner_init(DeviceBatch b, PcgVe
   }
 }
 
+// Row i of vertex u of -(dt beta + dt^2) H_coll x, H_coll = sum over the
+// vertex's collision tets of (c c^T) (x) G (free rows only; x vanishes on
+// pinned rows, which keeps the columns masked too).
+template <typename T>
+__device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int i, const T* __restrict__ x) {
+  const DeviceCollisions& c = b.coll;
+  const int k0 = c.incCount[u], k1 = c.incCount[u + 1];
+  if (k0 == k1) return 0.0;
+  const int s = b.vertexScene[u];
+  const double dt = b.scenes[s].dt, scale = -(dt * c.scenes[s].beta + dt * dt);
+  double acc = 0.0;
+  for (int k = k0; k < k1; k++) {
+    const int e = c.incList[k], p = e >> 2, a = e & 3;
+    const int4 ct = c.pairTet[p];
+    const double* C = c.pairC + 4 * (size_t)p;
+    const double* G = c.pairG + 9 * (size_t)p;
+    const int id[4] = {ct.x, ct.y, ct.z, ct.w};
+    double z[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) z[j] += C[q] * double(x[3 * id[q] + j]);
+    acc += C[a] * (G[i] * z[0] + G[i + 3] * z[1] + G[i + 6] * z[2]);
+  }
+  return scale * acc;
+}
+
 // w = A u, one thread per scalar row (9 DFMA per block in FP64), and
 // delta = (w, u); the scene's last CTA forms beta and alpha.
 template <typename T>
@@ -332,6 +367,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T>
       const T* B = A + 9 * (size_t)k;
       acc += B[0] * uu[3 * w] + B[1] * uu[3 * w + 1] + B[2] * uu[3 * w + 2];
     }
+    if (b.collOn && b.freeMask[u]) acc += T(collision_row<T>(b, u, i, uu));
     v.w[row] = acc;
     dl = double(acc) * double(uu[row]);
   }
@@ -459,6 +495,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_residual(DeviceBatch b) {
       const float* B = A + 9 * (size_t)k;
       acc += double(B[0]) * b.y[3 * w] + double(B[1]) * b.y[3 * w + 1] + double(B[2]) * b.y[3 * w + 2];
     }
+    if (b.collOn && b.freeMask[u]) acc += collision_row<double>(b, u, i, b.y);
     const double ri = b.rhs[row] - acc;
     b.r64[row] = ri;
     rr = ri * ri;

@@ -277,6 +277,26 @@ class BATCH:
               "hobak_batch_assemble")
         return rowptr, cols, K.reshape(-1, 9), R
 
+    def set_collisions(self, scene: int, vf: bool = True, eps: float = 0.01, stiffness: float = 1.0,
+                       damping_beta: float = 0.001):
+        """Vertex-face self collisions of one scene (TIMESTEPPER.h:62-69 flags,
+        TET_MESH::setCollisionEps)."""
+        check(_lib.load().hobak_batch_set_collisions(self.h, scene, int(vf), eps, stiffness, damping_beta),
+              "hobak_batch_set_collisions")
+
+    def collision_pairs(self, scene: int, detect_now: bool = False):
+        """(vertex, surface triangle) pairs (scene-local ids, sorted) and the
+        scene's surface triangles."""
+        L = _lib.load()
+        n, nt = ctypes.c_int(), ctypes.c_int()
+        check(L.hobak_batch_collision_pairs(self.h, scene, int(detect_now), ctypes.byref(n), None, 0,
+                                            ctypes.byref(nt), None), "hobak_batch_collision_pairs")
+        pairs = np.zeros(2 * max(n.value, 1), dtype=np.int32)
+        tris = np.zeros(3 * max(nt.value, 1), dtype=np.int32)
+        check(L.hobak_batch_collision_pairs(self.h, scene, 0, ctypes.byref(n), iptr(pairs), n.value,
+                                            ctypes.byref(nt), iptr(tris)), "hobak_batch_collision_pairs")
+        return pairs[:2 * n.value].reshape(-1, 2), tris[:3 * nt.value].reshape(-1, 3)
+
     # ---- measurement ----
     KERNELS = ("element", "assemble", "spmv", "pcg_update")
     PHASES = ("element", "assembly", "pcg_init", "pcg_iterations", "update")

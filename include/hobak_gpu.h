@@ -35,6 +35,7 @@ extern "C" {
 #define HOBAK_ERR_ADMISSION -5       /* serving: job does not fit the memory budget */
 #define HOBAK_ERR_TIMEOUT -6         /* a bounded device wait gave up */
 #define HOBAK_ERR_NO_DEVICE -7       /* no usable sm_103 device */
+#define HOBAK_ERR_OVERFLOW -8        /* a fixed-capacity device list overflowed (collision candidates) */
 
 /* ---- materials: the VOLUME::HYPERELASTIC family (Hyperelastic/Volume/) ---- */
 #define HOBAK_MATERIAL_SNH 0            /* SNH.cpp (Stable Neo-Hookean)        */
@@ -124,6 +125,23 @@ int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v);
 /* Replace the external force vector (3*nv) of one scene; the default is M g. */
 int hobak_batch_set_external_forces(hobak_batch b, int scene, const double* f);
 int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts);
+/* Vertex-face self collisions of one scene (TIMESTEPPER's
+ * vertexFaceSelfCollisionsOn / collisionStiffness / collisionDampingBeta,
+ * TIMESTEPPER.h:62-69, and TET_MESH::setCollisionEps, TET_MESH.cpp:2160-2165).
+ * Off by default (the reference's default is on; edge-edge collisions are not
+ * implemented).  Detection runs on the GPU every step: a spatial hash replaces
+ * the AABB tree, the narrow phase is the reference's
+ * (TET_MESH_FASTER.cpp:248-334).  The first call builds the surfaces of every
+ * scene in the batch. */
+int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, double stiffness,
+                               double damping_beta);
+/* Vertex-face pairs of one scene found by the last step's detection (or by a
+ * fresh detection at the current state when `detect_now` is 1): *npairs is
+ * the count; up to cap (vertex, surface triangle) pairs in scene-local ids,
+ * sorted.  Surface triangles (3 ints each, scene-local vertex ids, reference
+ * order and winding) when tris is not NULL. */
+int hobak_batch_collision_pairs(hobak_batch b, int scene, int detect_now, int* npairs, int* pairs, int cap,
+                                int* ntris, int* tris);
 /* Device memory held by the batch, in bytes. */
 int hobak_batch_device_bytes(hobak_batch b, long long* bytes);
 /* Mesh-wide hyperelastic energy sum(restVolume * psi(F)) of one scene

@@ -1,0 +1,68 @@
+"""GPU vertex-face collisions against the reference's golden pairs and
+trajectory (tests/golden/traj_two_cubes6_snh_vf.npz) and the CPU oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from hobakv1_gb300 import hobak, scenes
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+EPS, MU, BETA = 1e-3, 1e3, 0.001
+
+
+def as_set(p):
+    return sorted(map(tuple, np.asarray(p).tolist()))
+
+
+def test_pairs_and_trajectory_match_reference():
+    g = np.load(os.path.join(GOLDEN, "traj_two_cubes6_snh_vf.npz"))
+    s = scenes.two_cubes_scene(6)
+    b = hobak.BATCH([s])
+    b.set_collisions(0, True, EPS, MU, BETA)
+    pairs, tris = b.collision_pairs(0, detect_now=True)
+    assert np.array_equal(tris, g["surface_triangles"])  # surface extraction bit-exact
+    assert as_set(pairs) == as_set(g["pairs_0"])          # pair set bit-exact
+    stride = int(g["stride"])
+    for k in range(1, g["x"].shape[0]):
+        b.step(stride)
+        x, _ = b.get_state(0)
+        err = np.linalg.norm(x - g["x"][k]) / np.linalg.norm(g["x"][k])
+        assert err < 1e-8, (k, err)
+        pairs, _ = b.collision_pairs(0, detect_now=True)
+        assert as_set(pairs) == as_set(g[f"pairs_{k}"]), k
+
+
+@pytest.mark.parametrize("N", [8, 12])
+def test_collision_pairs_match_oracle_along_a_trajectory(N):
+    s = scenes.two_cubes_scene(N, gap=2e-4)
+    b = hobak.BATCH([s])
+    b.set_collisions(0, True, EPS, MU, BETA)
+    sim = oracle.Sim(s, precond=1)
+    sim.set_collisions(True, EPS, MU, BETA)
+    for k in range(4):
+        gp, _ = b.collision_pairs(0, detect_now=True)
+        op, _ = sim.vf_pairs()
+        assert as_set(gp) == as_set(op), k
+        b.step(5)
+        sim.step(5)
+        x, _ = b.get_state(0)
+        xo, _ = sim.state()
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
+
+
+def test_collision_scene_alone_and_in_a_mix():
+    mix = [scenes.two_cubes_scene(6), scenes.config1_scene(5), scenes.two_cubes_scene(7, gap=3e-4)]
+    batch = hobak.BATCH(mix)
+    for i in (0, 2):
+        batch.set_collisions(i, True, EPS, MU, BETA)
+    batch.step(6)
+    for i in (0, 2):
+        alone = hobak.BATCH([mix[i]])
+        alone.set_collisions(0, True, EPS, MU, BETA)
+        alone.step(6)
+        xa, _ = alone.get_state(0)
+        xm, _ = batch.get_state(i)
+        assert np.array_equal(xa, xm), i
