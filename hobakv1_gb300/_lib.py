@@ -47,6 +47,9 @@ SIGNATURES = {
     "hobak_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "hobak_batch_num_scenes": (ctypes.c_int, [ctypes.c_void_p, _ip]),
     "hobak_batch_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(HobakStepStats)]),
+    "hobak_batch_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "hobak_batch_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakStepStats)]),
+    "hobak_batch_set_active": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "hobak_batch_set_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
     "hobak_batch_get_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
     "hobak_batch_set_external_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
@@ -73,6 +76,7 @@ SIGNATURES = {
                                                   ctypes.c_double, ctypes.c_double]),
     "hobak_batch_collision_pairs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, _ip,
                                                    ctypes.c_int, _ip, _ip]),
+    "hobak_batch_collision_response": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp]),
     "hobak_element_eval_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.POINTER(HobakMaterial), ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -84,6 +84,9 @@ struct hobak_batch_t {
   int lastStatus = HOBAK_OK;
   std::vector<SolveState> lastSolve;
   std::vector<int> hostRowptr, hostCols;
+  std::vector<SceneParams> sceneParams;   // host copy (active flags)
+  SolveState* solvePinned = nullptr;      // pinned landing buffer for per-step stats
+  bool pending = false;                   // steps enqueued, stats not collected yet
   std::vector<double> restHost;  // rest positions (surface areas for collisions)
   // vertex-face collisions
   std::vector<CollisionScene> collScenes;
@@ -325,6 +328,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     p.lambda = mp.lambda;
     p.alpha = mp.alpha;
     p.dt = H.dt;
+    p.active = 1;
     sparams.push_back(p);
   }
   const int ntiles = (int)tileScene.size();
@@ -427,6 +431,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     return cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice);
   };
   CUDA_TRY(up(d.scenes, sparams.data(), sizeof(SceneParams) * n));
+  B->sceneParams = sparams;
   CUDA_TRY(up(d.rest, rest.data(), V3));
   CUDA_TRY(up(d.x, x.data(), V3));
   CUDA_TRY(up(d.v, v.data(), V3));
@@ -719,6 +724,7 @@ int build_collisions(hobak_batch_t* B) {
   const size_t oPairTet = A.reserve(sizeof(int4) * (size_t)cap), oPairC = A.reserve(sizeof(double) * 4 * (size_t)cap);
   const size_t oPairG = A.reserve(sizeof(double) * 9 * (size_t)cap);
   const size_t oPairR = A.reserve(sizeof(double) * 12 * (size_t)cap);
+  const size_t oPairF = A.reserve(sizeof(double) * 12 * (size_t)cap);
   const size_t oIncCount = A.reserve(sizeof(int) * (nv + 1)), oIncCursor = A.reserve(sizeof(int) * nv);
   const size_t oIncList = A.reserve(sizeof(int) * 4 * (size_t)cap);
   const size_t oScan = A.reserve(sizeof(int) * scanBlocks);
@@ -759,6 +765,7 @@ int build_collisions(hobak_batch_t* B) {
   c.pairC = carve<double>(base, oPairC);
   c.pairG = carve<double>(base, oPairG);
   c.pairRhs = carve<double>(base, oPairR);
+  c.pairF = carve<double>(base, oPairF);
   c.incCount = carve<int>(base, oIncCount);
   c.incCursor = carve<int>(base, oIncCursor);
   c.incList = carve<int>(base, oIncList);
@@ -877,6 +884,7 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
   CUDA_TRY(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
   CUDA_TRY(cudaStreamCreateWithFlags(&B->captureStream, cudaStreamNonBlocking));
   CUDA_TRY(cudaMallocHost(&B->pinnedActive, sizeof(int)));
+  CUDA_TRY(cudaMallocHost(&B->solvePinned, sizeof(SolveState) * nscenes));
   for (auto& e : B->ev) CUDA_TRY(cudaEventCreate(&e));
   if ((rc = build_batch(B.get(), scenes, nscenes))) {
     hobak_batch_destroy(B.release());
@@ -898,6 +906,7 @@ int hobak_batch_destroy(hobak_batch b) {
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
   if (b->pinnedActive) cudaFreeHost(b->pinnedActive);
+  if (b->solvePinned) cudaFreeHost(b->solvePinned);
   if (b->arena) cudaFree(b->arena);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -910,16 +919,32 @@ int hobak_batch_num_scenes(hobak_batch b, int* n) {
   return HOBAK_OK;
 }
 
-int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats) {
+int hobak_batch_step_async(hobak_batch b, int nsteps) {
   if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
   if (nsteps < 0) return fail(HOBAK_ERR_INVALID, "nsteps < 0");
   int rc = run_steps(b, nsteps);
   if (rc) return rc;
   const int n = (int)b->scenes.size();
-  b->lastSolve.resize(n);
-  CUDA_TRY(cudaMemcpyAsync(b->lastSolve.data(), b->d.solve, sizeof(SolveState) * n, cudaMemcpyDeviceToHost,
-                           b->stream));
+  CUDA_TRY(cudaMemcpyAsync(b->solvePinned, b->d.solve, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, b->stream));
+  b->pending = true;
+  return HOBAK_OK;
+}
+
+int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats) {
+  int rc = hobak_batch_step_async(b, nsteps);
+  if (rc) return rc;
+  return hobak_batch_wait(b, stats);
+}
+
+int hobak_batch_wait(hobak_batch b, hobak_step_stats* stats) {
+  if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
   CUDA_TRY(cudaStreamSynchronize(b->stream));
+  const int n = (int)b->scenes.size();
+  if (b->pending) {
+    b->lastSolve.assign(b->solvePinned, b->solvePinned + n);
+    b->pending = false;
+  }
+  if ((int)b->lastSolve.size() != n) return HOBAK_OK;  // nothing stepped yet
   int status = HOBAK_OK;
   for (int s = 0; s < n; s++) {
     const SolveState& st = b->lastSolve[s];
@@ -993,8 +1018,11 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
   cs.eps = eps;
   cs.mu = stiffness;
   cs.beta = damping_beta;
-  CUDA_TRY(cudaMemcpy(const_cast<CollisionScene*>(b->d.coll.scenes), b->collScenes.data(),
-                      sizeof(CollisionScene) * b->collScenes.size(), cudaMemcpyHostToDevice));
+  std::vector<CollisionScene> eff = b->collScenes;
+  for (size_t k = 0; k < eff.size(); k++)
+    if (!b->sceneParams[k].active) eff[k].vfOn = 0;
+  CUDA_TRY(cudaMemcpy(const_cast<CollisionScene*>(b->d.coll.scenes), eff.data(), sizeof(CollisionScene) * eff.size(),
+                      cudaMemcpyHostToDevice));
   drop_graphs(b);
   return HOBAK_OK;
 }
@@ -1033,6 +1061,56 @@ int hobak_batch_collision_pairs(hobak_batch b, int scene, int detect_now, int* n
       }
   }
   if (npairs) *npairs = n;
+  return HOBAK_OK;
+}
+
+int hobak_batch_collision_response(hobak_batch b, int scene, int cap, int* tets, double* force, double* hessian) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  if (!b->collArena) return fail(HOBAK_ERR_INVALID, "collisions were never enabled on this batch");
+  const SceneHost& H = b->scenes[scene];
+  const int s0 = b->svStart[scene], s1 = b->svStart[scene + 1];
+  int p0 = 0, p1 = 0;
+  CUDA_TRY(cudaMemcpy(&p0, b->d.coll.svCount + s0, sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(&p1, b->d.coll.svCount + s1, sizeof(int), cudaMemcpyDeviceToHost));
+  const int n = std::min(p1 - p0, cap);
+  if (n <= 0) return HOBAK_OK;
+  std::vector<int4> ct(n);
+  std::vector<double> C(4 * (size_t)n), G(9 * (size_t)n), F(12 * (size_t)n);
+  CUDA_TRY(cudaMemcpy(ct.data(), b->d.coll.pairTet + p0, sizeof(int4) * n, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(C.data(), b->d.coll.pairC + 4 * (size_t)p0, sizeof(double) * C.size(), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(G.data(), b->d.coll.pairG + 9 * (size_t)p0, sizeof(double) * G.size(), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(F.data(), b->d.coll.pairF + 12 * (size_t)p0, sizeof(double) * F.size(), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < n; k++) {
+    if (tets) {
+      tets[4 * k] = ct[k].x - H.v0;
+      tets[4 * k + 1] = ct[k].y - H.v0;
+      tets[4 * k + 2] = ct[k].z - H.v0;
+      tets[4 * k + 3] = ct[k].w - H.v0;
+    }
+    if (force) std::copy(&F[12 * (size_t)k], &F[12 * (size_t)k + 12], force + 12 * (size_t)k);
+    if (hessian)
+      for (int a = 0; a < 4; a++)
+        for (int bb = 0; bb < 4; bb++)
+          for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+              hessian[144 * (size_t)k + (3 * a + i) + 12 * (3 * bb + j)] =
+                  C[4 * (size_t)k + a] * C[4 * (size_t)k + bb] * G[9 * (size_t)k + i + 3 * j];
+  }
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_active(hobak_batch b, int scene, int active) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->sceneParams[scene].active = active ? 1 : 0;
+  CUDA_TRY(cudaMemcpy(const_cast<SceneParams*>(b->d.scenes) + scene, &b->sceneParams[scene], sizeof(SceneParams),
+                      cudaMemcpyHostToDevice));
+  if (b->collArena) {  // a parked scene takes no part in collision detection either
+    CollisionScene cs = b->collScenes[scene];
+    if (!active) cs.vfOn = 0;
+    CUDA_TRY(cudaMemcpy(const_cast<CollisionScene*>(b->d.coll.scenes) + scene, &cs, sizeof(CollisionScene),
+                        cudaMemcpyHostToDevice));
+  }
   return HOBAK_OK;
 }
 

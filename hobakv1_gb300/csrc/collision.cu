@@ -354,9 +354,10 @@ __global__ void k_vf_pairs(DeviceBatch b, DeviceCollisions c) {
     double* G = c.pairG + 9 * (size_t)pidx;
     double* R = c.pairRhs + 12 * (size_t)pidx;
     for (int a = 0; a < 4; a++) C[a] = cvec[a];
+    double* Fo = c.pairF + 12 * (size_t)pidx;
     if (fabs(tm) <= 1e-8 || fabs(tt) < 1e-8) {  // VERTEX_FACE_SQRT_COLLISION.cpp:158,206
       for (int k = 0; k < 9; k++) G[k] = 0.0;
-      for (int k = 0; k < 12; k++) R[k] = 0.0;
+      for (int k = 0; k < 12; k++) R[k] = Fo[k] = 0.0;
       continue;
     }
     // force -w grad = -w 2 mu spring / tm (c (x) t)
@@ -376,7 +377,10 @@ __global__ void k_vf_pairs(DeviceBatch b, DeviceCollisions c) {
     for (int r = 0; r < 3; r++) Gz[r] = G[r] * zv[0] + G[r + 3] * zv[1] + G[r + 6] * zv[2];
     const double tv[3] = {t.x, t.y, t.z};
     for (int a = 0; a < 4; a++)
-      for (int k = 0; k < 3; k++) R[3 * a + k] = dt * (fs * cvec[a] * tv[k] + dt * cvec[a] * Gz[k]);
+      for (int k = 0; k < 3; k++) {
+        Fo[3 * a + k] = fs * cvec[a] * tv[k];
+        R[3 * a + k] = dt * (fs * cvec[a] * tv[k] + dt * cvec[a] * Gz[k]);
+      }
   }
 }
 

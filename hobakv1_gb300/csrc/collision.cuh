@@ -47,6 +47,7 @@ struct DeviceCollisions {
   double* pairC;           // [pairCap][4] (1, -b0, -b1, -b2)
   double* pairG;           // [pairCap][9] 3x3 factor of the clamped Hessian, times -w 2 mu
   double* pairRhs;         // [pairCap][12] dt (f + dt H v)
+  double* pairF;           // [pairCap][12] collision force -w grad psi (for inspection)
   int* incCount;           // [nv + 1] then exclusive scan
   int* incCursor;          // [nv]
   int* incList;            // [4 * pairCap] pair * 4 + slot

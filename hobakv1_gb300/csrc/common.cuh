@@ -35,6 +35,7 @@ struct SceneParams {
   int t0, nt;          // tet range
   int tile0, ntiles;   // PCG tile range
   int kind;            // material
+  int active;          // 0: the scene is parked (serving) and every kernel skips it
   double mu, lambda, alpha;  // reparameterised material constants
   double dt;
 };

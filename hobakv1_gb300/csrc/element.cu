@@ -202,8 +202,9 @@ template <typename HT>
 __global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces, HT* __restrict__ outH) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= b.nt) return;
-  const int4 tv = b.tets[t];
   const SceneParams& sp = b.scenes[b.tetScene[t]];
+  if (!sp.active) return;
+  const int4 tv = b.tets[t];
   const MatParams m{sp.kind, sp.mu, sp.lambda, sp.alpha};
   const double dt = rawForces ? 0.0 : sp.dt;
   double Dinv[9];

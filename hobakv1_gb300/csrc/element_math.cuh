@@ -109,7 +109,7 @@ __device__ __forceinline__ void svd3_rv(const double* F, double* U, double* S, d
       const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
       const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
       const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
-      if (fabs(gamma) > 1e-17 * sqrt(alpha * beta)) {
+      if (gamma * gamma > 1e-30 * (alpha * beta)) {  // off-diagonal above ~1e-15 relative
         rotated = true;
         const double zeta = (beta - alpha) / (2.0 * gamma);
         const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
@@ -205,7 +205,7 @@ __device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double*
       const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
       const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
       const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
-      if (gamma * gamma > 1e-34 * (alpha * beta)) {
+      if (gamma * gamma > 1e-30 * (alpha * beta)) {  // ~1e-15 relative: FP64 rounding floor
         rotated = true;
         // angle in FP32 (only orthogonality of (c, s) must be FP64-exact)
         const float zf = float(beta - alpha) / (2.0f * float(gamma));
@@ -234,7 +234,7 @@ __device__ __forceinline__ void eig3sym(const T* Ain, T* Q, T* L) {
   T a00 = Ain[0], a01 = Ain[3], a02 = Ain[6], a11 = Ain[4], a12 = Ain[7], a22 = Ain[8];
 #pragma unroll
   for (int k = 0; k < 9; k++) Q[k] = (k % 4 == 0) ? T(1) : T(0);
-  const T eps = sizeof(T) == 8 ? T(1e-18) : T(1e-9);
+  const T eps = sizeof(T) == 8 ? T(1e-15) : T(1e-6);  // just above each type's rounding floor
   for (int sweep = 0; sweep < 16; sweep++) {
     const T off = fabs(a01) + fabs(a02) + fabs(a12);
     const T dg = fabs(a00) + fabs(a11) + fabs(a22);

@@ -120,6 +120,7 @@ __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __res
   const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= 9L * b.nblocks) return;
   const int blk = (int)(g / 9), e = (int)(g % 9);
+  if (!b.scenes[b.vertexScene[b.blkRow[blk]]].active) return;
   const int r = e / 3, c = e % 3;
   const HT sum = gather_block_entry(b, elemH, blk, r, c);
   const int u = b.blkRow[blk], w = b.cols[blk];
@@ -155,7 +156,7 @@ __global__ void k_assemble_raw(DeviceBatch b, double* K, double* R) {
 template <typename T>
 __global__ void k_diag_inverse(DeviceBatch b, const T* __restrict__ lhs, T* __restrict__ minv, int precond) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= b.nv) return;
+  if (u >= b.nv || !b.scenes[b.vertexScene[u]].active) return;
   int k = b.rowptr[u];
   while (b.cols[k] != u) k++;
   double D[9];
@@ -193,6 +194,16 @@ __global__ void __launch_bounds__(kVecThreads) k_rhs(DeviceBatch b) {
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
+  if (!b.scenes[s].active) {  // parked scene: nothing to solve this step
+    if (tile == b.scenes[s].tile0 && threadIdx.x == 0) {
+      SolveState& st = b.solve[s];
+      st.outerDone = 1;
+      st.converged = 1;
+      st.totalIters = 0;
+      st.sweep = 0;
+    }
+    return;
+  }
   const int u = b.tileV0[tile] + threadIdx.x;
   double rr = 0;
   if (u < b.tileV1[tile]) {
@@ -362,7 +373,22 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T>
     const T* __restrict__ A = v.lhs + 3 * i;
     T acc = T(0);
     const int k1 = b.rowptr[u + 1];
-    for (int k = b.rowptr[u]; k < k1; k++) {
+    int k = b.rowptr[u];
+    // four blocks per trip so their independent loads are in flight together
+    for (; k + 3 < k1; k += 4) {
+      const int w0 = __ldg(&b.cols[k]), w1 = __ldg(&b.cols[k + 1]);
+      const int w2 = __ldg(&b.cols[k + 2]), w3 = __ldg(&b.cols[k + 3]);
+      const T* B = A + 9 * (size_t)k;
+      const T t0 = B[0] * uu[3 * w0] + B[1] * uu[3 * w0 + 1] + B[2] * uu[3 * w0 + 2];
+      const T t1 = B[9] * uu[3 * w1] + B[10] * uu[3 * w1 + 1] + B[11] * uu[3 * w1 + 2];
+      const T t2 = B[18] * uu[3 * w2] + B[19] * uu[3 * w2 + 1] + B[20] * uu[3 * w2 + 2];
+      const T t3 = B[27] * uu[3 * w3] + B[28] * uu[3 * w3 + 1] + B[29] * uu[3 * w3 + 2];
+      acc += t0;
+      acc += t1;
+      acc += t2;
+      acc += t3;
+    }
+    for (; k < k1; k++) {
       const int w = __ldg(&b.cols[k]);
       const T* B = A + 9 * (size_t)k;
       acc += B[0] * uu[3 * w] + B[1] * uu[3 * w + 1] + B[2] * uu[3 * w + 2];
@@ -532,7 +558,7 @@ __global__ void k_continue(const int* active, unsigned long long* bodyRuns, cuda
 // v += y; x += dt v; v = S v (BACKWARD_EULER_VELOCITY.cpp:191-201).
 __global__ void k_finish_step(DeviceBatch b) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= b.nv) return;
+  if (u >= b.nv || !b.scenes[b.vertexScene[u]].active) return;
   const double dt = b.scenes[b.vertexScene[u]].dt;
   const bool fu = b.freeMask[u] != 0;
 #pragma unroll

@@ -235,6 +235,19 @@ class BATCH:
         self.last_stats = [(s.iterations, s.converged, s.rel_residual, s.refinements) for s in stats]
         return self.last_stats
 
+    def step_async(self, nsteps: int = 1):
+        check(_lib.load().hobak_batch_step_async(self.h, nsteps), "hobak_batch_step_async")
+
+    def wait(self):
+        stats = (HobakStepStats * len(self))()
+        self.last_status = check(_lib.load().hobak_batch_wait(self.h, stats), "hobak_batch_wait")
+        self.last_stats = [(s.iterations, s.converged, s.rel_residual, s.refinements) for s in stats]
+        return self.last_stats
+
+    def set_active(self, scene: int, active: bool = True):
+        """Park (False) or resume one scene; parked scenes keep their state."""
+        check(_lib.load().hobak_batch_set_active(self.h, scene, int(active)), "hobak_batch_set_active")
+
     def get_state(self, scene: int):
         n = 3 * self.nv[scene]
         x, v = np.zeros(n), np.zeros(n)
@@ -296,6 +309,17 @@ class BATCH:
         check(L.hobak_batch_collision_pairs(self.h, scene, 0, ctypes.byref(n), iptr(pairs), n.value,
                                             ctypes.byref(nt), iptr(tris)), "hobak_batch_collision_pairs")
         return pairs[:2 * n.value].reshape(-1, 2), tris[:3 * nt.value].reshape(-1, 3)
+
+    def collision_response(self, scene: int):
+        """Collision tets, forces (-w grad psi) and clamped Hessians of the last detection."""
+        pairs, _ = self.collision_pairs(scene)
+        n = len(pairs)
+        tets = np.zeros(4 * max(n, 1), dtype=np.int32)
+        f = np.zeros(12 * max(n, 1))
+        H = np.zeros(144 * max(n, 1))
+        check(_lib.load().hobak_batch_collision_response(self.h, scene, n, iptr(tets), dptr(f), dptr(H)),
+              "hobak_batch_collision_response")
+        return tets[:4 * n].reshape(-1, 4), f[:12 * n].reshape(-1, 12), H[:144 * n].reshape(-1, 144)
 
     # ---- measurement ----
     KERNELS = ("element", "assemble", "spmv", "pcg_update")

@@ -1,0 +1,169 @@
+"""Continuous-batching server for scene-timestep jobs.
+
+A job is a scene plus a number of BACKWARD_EULER_VELOCITY steps.  The server
+keeps every admitted job's state resident on the GPU until it finishes and
+runs a tick loop:
+
+  1. admission: queued jobs (FIFO) are admitted while their estimated device
+     footprint fits the memory budget; the jobs admitted in one tick are packed
+     into one batch (a "cohort") that joins the running set;
+  2. every cohort with running jobs enqueues one step on its own CUDA stream
+     (hobak_batch_step_async), so the cohorts' work overlaps on the device;
+  3. the server waits for all of them (hobak_batch_wait); each running job
+     records the tick's latency as its step latency; finished jobs are parked
+     (hobak_batch_set_active(scene, 0): state kept, kernels skip them) and
+     their final state is read back; a cohort whose jobs are all done is freed.
+
+Within a cohort every scene keeps its own reduction tiles, so a job's result
+does not depend on which other jobs shared its batch or the device.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+from collections import deque
+from typing import Deque, Dict, List, Optional
+
+import numpy as np
+
+from . import hobak
+
+
+def footprint_bytes(scene, precision: int) -> int:
+    """Conservative device bytes of one scene in a batch (both precisions'
+    buffers are allocated; ~15 blocks per vertex in tet meshes)."""
+    nv, nt = scene.nv, scene.nt
+    nb = 16 * nv
+    per_tet = 16 + 72 + 8 + 4 + 720 + 360 + 96 + 64 + 16 + 8
+    per_block = 4 + 4 + 4 + 4 + 72 + 36
+    per_vertex = 6 * 24 + 8 + 1 + 4 + 3 * 24 + 72 + 36 + 4 * 24 + 6 * 12 + 8
+    return int(nt * per_tet + nb * per_block + nv * per_vertex + (1 << 20))
+
+
+@dataclasses.dataclass
+class Job:
+    id: int
+    scene: object
+    nsteps: int
+    collisions: Optional[tuple] = None  # (eps, stiffness, beta) for vertex-face contact
+    submitted: float = 0.0
+    admitted: float = -1.0
+    finished: float = -1.0
+    done_steps: int = 0
+    step_ms: List[float] = dataclasses.field(default_factory=list)
+    result_x: Optional[np.ndarray] = None
+    result_v: Optional[np.ndarray] = None
+    cohort: Optional["Cohort"] = None
+    slot: int = -1
+
+
+class Cohort:
+    def __init__(self, jobs: List[Job], opts):
+        self.jobs = jobs
+        self.batch = hobak.BATCH([j.scene for j in jobs], opts)
+        for k, j in enumerate(jobs):
+            j.cohort, j.slot = self, k
+            if j.collisions is not None:
+                eps, mu, beta = j.collisions
+                self.batch.set_collisions(k, True, eps, mu, beta)
+        self.bytes = self.batch.device_bytes()
+        self.running = len(jobs)
+
+    def close(self):
+        self.batch.close()
+
+
+class Server:
+    """Tick-driven continuous batching under a device-memory budget."""
+
+    def __init__(self, budget_bytes: int, precision: int = hobak.PRECISION_MIXED,
+                 max_admit_per_tick: int = 64, keep_results: bool = True):
+        self.budget = int(budget_bytes)
+        self.opts = hobak.solver_opts(precision=precision)
+        self.max_admit = max_admit_per_tick
+        self.keep_results = keep_results
+        self.queue: Deque[Job] = deque()
+        self.cohorts: List[Cohort] = []
+        self.finished: Dict[int, Job] = {}
+        self.used = 0
+        self.ticks = 0
+        self.tick_ms: List[float] = []
+        self.rejected = 0
+
+    # ---- client side ----
+    def submit(self, job: Job):
+        job.submitted = time.perf_counter()
+        if footprint_bytes(job.scene, self.opts.precision) > self.budget:
+            self.rejected += 1  # can never fit: refuse instead of blocking the queue
+            raise ValueError(f"job {job.id} needs more than the whole memory budget")
+        self.queue.append(job)
+
+    def idle(self) -> bool:
+        return not self.queue and not self.cohorts
+
+    # ---- server loop ----
+    def _admit(self):
+        take: List[Job] = []
+        est = 0
+        while self.queue and len(take) < self.max_admit:
+            need = footprint_bytes(self.queue[0].scene, self.opts.precision)
+            if self.used + est + need > self.budget:
+                break
+            est += need
+            take.append(self.queue.popleft())
+        if take:
+            c = Cohort(take, self.opts)
+            now = time.perf_counter()
+            for j in take:
+                j.admitted = now
+            self.used += c.bytes
+            self.cohorts.append(c)
+
+    def tick(self) -> int:
+        """One scheduling round; returns the number of job-steps it completed."""
+        self._admit()
+        live = [c for c in self.cohorts if c.running > 0]
+        if not live:
+            return 0
+        t0 = time.perf_counter()
+        for c in live:
+            hobak._lib.check(hobak._lib.load().hobak_batch_step_async(c.batch.h, 1), "hobak_batch_step_async")
+        stats = {}
+        for c in live:
+            st = (hobak._lib.HobakStepStats * len(c.jobs))()
+            hobak._lib.check(hobak._lib.load().hobak_batch_wait(c.batch.h, st), "hobak_batch_wait")
+            stats[id(c)] = st
+        ms = (time.perf_counter() - t0) * 1e3
+        self.tick_ms.append(ms)
+        self.ticks += 1
+        done = 0
+        now = time.perf_counter()
+        for c in live:
+            for j in c.jobs:
+                if j.finished >= 0:
+                    continue
+                j.done_steps += 1
+                j.step_ms.append(ms)
+                done += 1
+                if j.done_steps >= j.nsteps:
+                    j.finished = now
+                    if self.keep_results:
+                        j.result_x, j.result_v = c.batch.get_state(j.slot)
+                    c.batch.set_active(j.slot, False)
+                    c.running -= 1
+                    self.finished[j.id] = j
+        for c in [c for c in self.cohorts if c.running == 0]:
+            self.used -= c.bytes
+            c.close()
+            self.cohorts.remove(c)
+        return done
+
+    def drain(self, max_ticks: int = 1_000_000):
+        while not self.idle() and max_ticks > 0:
+            self.tick()
+            max_ticks -= 1
+
+    def close(self):
+        for c in self.cohorts:
+            c.close()
+        self.cohorts.clear()

@@ -119,6 +119,15 @@ int hobak_batch_num_scenes(hobak_batch b, int* n);
  * (BACKWARD_EULER_VELOCITY.cpp:96-235).  State stays on the device.
  * stats may be NULL or point at nscenes entries (stats of the last step). */
 int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats);
+/* hobak_batch_step split in two (no reference counterpart; for overlapping
+ * several batches on the device): enqueue nsteps steps and return at once,
+ * then wait for them and collect the stats of the last step. */
+int hobak_batch_step_async(hobak_batch b, int nsteps);
+int hobak_batch_wait(hobak_batch b, hobak_step_stats* stats);
+/* Park (active = 0) or resume one scene: a parked scene keeps its state and is
+ * skipped by every kernel, so a serving loop can retire finished jobs without
+ * re-packing the batch (no reference counterpart). */
+int hobak_batch_set_active(hobak_batch b, int scene, int active);
 /* Host <-> device state of one scene (3*nv doubles each; NULL skips). */
 int hobak_batch_set_state(hobak_batch b, int scene, const double* x, const double* v);
 int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v);
@@ -142,6 +151,12 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
  * order and winding) when tris is not NULL. */
 int hobak_batch_collision_pairs(hobak_batch b, int scene, int detect_now, int* npairs, int* pairs, int cap,
                                 int* ntris, int* tris);
+/* Per-pair response of the last detection, in the order of
+ * hobak_batch_collision_pairs: collision tet (4 scene-local vertex ids:
+ * vertex, face[2], face[1], face[0]; TET_MESH.cpp:1785-1826), force
+ * -w grad psi (12) and clamped Hessian -w H+ (144, column major)
+ * (TET_MESH.cpp:1831-1877, 2045-2088).  Any output may be NULL. */
+int hobak_batch_collision_response(hobak_batch b, int scene, int cap, int* tets, double* force, double* hessian);
 /* Device memory held by the batch, in bytes. */
 int hobak_batch_device_bytes(hobak_batch b, long long* bytes);
 /* Mesh-wide hyperelastic energy sum(restVolume * psi(F)) of one scene

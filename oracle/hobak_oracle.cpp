@@ -88,7 +88,7 @@ void svd_rv(const double* F, double* U, double* S, double* V) {
       const double alpha = ap[0] * ap[0] + ap[1] * ap[1] + ap[2] * ap[2];
       const double beta = aq[0] * aq[0] + aq[1] * aq[1] + aq[2] * aq[2];
       const double gamma = ap[0] * aq[0] + ap[1] * aq[1] + ap[2] * aq[2];
-      if (gamma == 0.0 || std::fabs(gamma) <= 1e-17 * std::sqrt(alpha * beta)) continue;
+      if (gamma == 0.0 || std::fabs(gamma) <= 1e-15 * std::sqrt(alpha * beta)) continue;
       rotated = true;
       const double zeta = (beta - alpha) / (2.0 * gamma);
       const double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
@@ -162,7 +162,7 @@ void eig3sym(const double* Ain, double* Q, double* L) {
   for (int sweep = 0; sweep < 50; sweep++) {
     double off = std::fabs(a[0][1]) + std::fabs(a[0][2]) + std::fabs(a[1][2]);
     double diag = std::fabs(a[0][0]) + std::fabs(a[1][1]) + std::fabs(a[2][2]);
-    if (off == 0.0 || off <= 1e-18 * diag) break;
+    if (off == 0.0 || off <= 1e-15 * diag) break;
     for (int r = 0; r < 3; r++) {
       const int p = pq[r][0], k = pq[r][1];
       if (a[p][k] == 0.0) continue;
@@ -877,7 +877,7 @@ void jacobiEigen(int n, std::vector<double>& a, std::vector<double>& q) {
     double off = 0, diag = 0;
     for (int j = 0; j < n; j++)
       for (int i = 0; i < n; i++) (i == j ? diag : off) += std::fabs(a[i + n * j]);
-    if (off == 0.0 || off <= 1e-20 * diag) break;
+    if (off == 0.0 || off <= 1e-15 * diag) break;
     for (int p = 0; p < n; p++)
       for (int k = p + 1; k < n; k++) {
         const double apk = a[p + n * k];
@@ -1399,6 +1399,19 @@ int oracle_vf_pairs(void* h, int* pairs, int cap, int* tris) {
   }
   if (tris) std::copy(s->coll.tris.begin(), s->coll.tris.end(), tris);
   return np;
+}
+
+// Collision tets, forces (12) and clamped Hessians (144, column major) of the
+// pairs found by the last oracle_vf_pairs call.
+int oracle_vf_response(void* h, int* tets, double* f12, double* H12) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  vfResponse(*s);
+  const size_t np = s->coll.weight.size();
+  if (tets) std::copy(s->coll.ctets.begin(), s->coll.ctets.end(), tets);
+  if (f12) std::copy(s->coll.f12.begin(), s->coll.f12.end(), f12);
+  if (H12) std::copy(s->coll.H12.begin(), s->coll.H12.end(), H12);
+  return (int)np;
 }
 
 int oracle_num_surface_triangles(void* h) {

@@ -54,6 +54,7 @@ def lib():
                                             ctypes.c_double]
         L.oracle_vf_pairs.argtypes = [ctypes.c_void_p, _ip, ctypes.c_int, _ip]
         L.oracle_num_surface_triangles.argtypes = [ctypes.c_void_p]
+        L.oracle_vf_response.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
         L.oracle_energy.argtypes = [ctypes.c_void_p]
         L.oracle_energy.restype = ctypes.c_double
         _lib = L
@@ -124,6 +125,16 @@ class Sim:
         pairs = np.zeros(2 * cap, dtype=np.int32)
         n = L.oracle_vf_pairs(self.h, _i(pairs), cap, _i(tris))
         return pairs[:2 * n].reshape(-1, 2), tris.reshape(-1, 3)
+
+    def vf_response(self):
+        """Collision tets, forces and clamped Hessians of the last vf_pairs() detection."""
+        pairs, _ = self.vf_pairs()
+        n = len(pairs)
+        tets = np.zeros(4 * max(n, 1), dtype=np.int32)
+        f = np.zeros(12 * max(n, 1))
+        H = np.zeros(144 * max(n, 1))
+        lib().oracle_vf_response(self.h, _i(tets), _d(f), _d(H))
+        return tets[:4 * n].reshape(-1, 4), f[:12 * n].reshape(-1, 12), H[:144 * n].reshape(-1, 144)
 
     def step(self, n=1):
         iters = np.zeros(n, dtype=np.int32)

@@ -66,3 +66,20 @@ def test_collision_scene_alone_and_in_a_mix():
         xa, _ = alone.get_state(0)
         xm, _ = batch.get_state(i)
         assert np.array_equal(xa, xm), i
+
+
+@pytest.mark.parametrize("N", [6, 10])
+def test_per_pair_force_and_hessian_match_oracle(N):
+    """Collision tets bit-exact; -w grad psi and -w clamped Hessian per pair
+    within 1e-10 of the oracle (whose clamp is a numeric 12x12 eigensolve)."""
+    s = scenes.two_cubes_scene(N, gap=2e-4)
+    b = hobak.BATCH([s])
+    b.set_collisions(0, True, EPS, MU, BETA)
+    b.collision_pairs(0, detect_now=True)
+    gt, gf, gH = b.collision_response(0)
+    sim = oracle.Sim(s)
+    sim.set_collisions(True, EPS, MU, BETA)
+    ot, of, oH = sim.vf_response()
+    assert len(gt) > 0 and np.array_equal(gt, ot)
+    assert np.abs(gf - of).max() <= 1e-10 * np.abs(of).max()
+    assert np.abs(gH - oH).max() <= 1e-10 * np.abs(oH).max()

@@ -1,0 +1,64 @@
+"""Serving loop: jobs arriving while others run are admitted under the memory
+budget, stepped concurrently, and each result is the same as the job run
+alone."""
+import numpy as np
+import pytest
+
+from hobakv1_gb300 import hobak, scenes
+from hobakv1_gb300.serving import Job, Server, footprint_bytes
+
+pytestmark = pytest.mark.gpu
+VF = (1e-3, 1e3, 0.001)
+
+
+def jobs():
+    mix = scenes.config4_scenes(count=4, nmin=5, nmax=8)
+    out = [Job(0, mix[0], 7), Job(1, scenes.two_cubes_scene(6), 9, VF), Job(2, mix[1], 3),
+           Job(3, mix[2], 11), Job(4, scenes.two_cubes_scene(5, gap=3e-4), 5, VF), Job(5, mix[3], 6)]
+    return out
+
+
+def alone(job, precision):
+    b = hobak.BATCH([job.scene], hobak.solver_opts(precision=precision))
+    if job.collisions:
+        b.set_collisions(0, True, *job.collisions)
+    b.step(job.nsteps)
+    return b.get_state(0)
+
+
+@pytest.mark.parametrize("precision", [hobak.PRECISION_FP64, hobak.PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_results_equal_alone_and_in_the_mix(precision):
+    js = jobs()
+    srv = Server(budget_bytes=1 << 34, precision=precision)
+    # staggered arrivals: two jobs, a few ticks, then the rest while those run
+    srv.submit(js[0])
+    srv.submit(js[1])
+    srv.tick()
+    srv.tick()
+    for j in js[2:]:
+        srv.submit(j)
+        srv.tick()
+    srv.drain()
+    assert len(srv.finished) == len(js)
+    for j in js:
+        assert j.done_steps == j.nsteps
+        x, v = alone(j, precision)
+        # per-scene tiles and reductions: bitwise the same alone and in the mix
+        assert np.array_equal(j.result_x, x) and np.array_equal(j.result_v, v), j.id
+
+
+def test_admission_respects_the_memory_budget():
+    js = jobs()
+    budget = max(footprint_bytes(j.scene, 1) for j in js) * 2  # about two jobs at a time
+    srv = Server(budget_bytes=budget, precision=hobak.PRECISION_MIXED)
+    for j in js:
+        srv.submit(j)
+    peak = 0
+    while not srv.idle():
+        srv.tick()
+        assert srv.used <= budget
+        peak = max(peak, len(srv.cohorts))
+    assert len(srv.finished) == len(js)
+    assert all(j.admitted >= j.submitted for j in js)
+    with pytest.raises(ValueError):
+        Server(budget_bytes=1024).submit(js[0])
