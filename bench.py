@@ -19,6 +19,9 @@ Workloads (synthetic, seeded; see hobakv1_gb300/scenes.py):
   mix256_mixed            256 scenes, N ~ U{6..24} cells per side, SNH/ARAP, mu log-uniform,
                           one batched mixed-precision step = every scene advanced once
   mix256_fp64             the same mix batched in FP64
+  serve_poisson           continuous batching: 32 jobs (N ~ U{8..32}, 10-200 steps, half two cubes in
+                          vertex-face contact) arriving as a Poisson stream at 50, 400 and 2000 jobs/s,
+                          mixed precision and plain FP64; job-steps/s, p50/p99 step and job latency
 """
 from __future__ import annotations
 
@@ -45,6 +48,8 @@ WORKLOADS = {
     "kuhn10_snh": dict(kind="config1", N=10, material="snh", precision=0),
     "mix256_mixed": dict(kind="mix", count=256, material="snh/arap", precision=1),
     "mix256_fp64": dict(kind="mix", count=256, material="snh/arap", precision=0),
+    "serve_poisson": dict(kind="serve", count=32, lambdas=[50, 400, 2000], material="snh/arap",
+                          precision=1),
 }
 DEFAULT_WORKLOAD = "kuhn40_snh_twist"
 
@@ -57,6 +62,8 @@ def make_scenes(spec):
         return [scenes.config1_scene(spec["N"], spec["material"])]
     if spec["kind"] == "mix":
         return scenes.config4_scenes(spec["count"])
+    if spec["kind"] == "serve":
+        return scenes.config5_jobs(spec["count"])
     raise ValueError(spec)
 
 
@@ -180,6 +187,83 @@ def plain_fp64_gpu(scene_list, steps):
     return steps / dt
 
 
+def serve_once(job_specs, arrivals, precision, budget_bytes):
+    """Drive the continuous-batching server with jobs arriving at the given
+    times (seconds from start).  Returns (wall seconds, jobs, server)."""
+    from hobakv1_gb300 import serving
+    srv = serving.Server(budget_bytes, precision=precision, async_build=True)
+    jobs = [serving.Job(k, sc, n, contact) for k, (sc, n, contact) in enumerate(job_specs)]
+    t0 = time.perf_counter()
+    i = 0
+    while i < len(jobs) or not srv.idle():
+        now = time.perf_counter() - t0
+        while i < len(jobs) and arrivals[i] <= now:
+            srv.submit(jobs[i])
+            i += 1
+        if srv.idle():
+            if i < len(jobs):
+                time.sleep(max(0.0, arrivals[i] - (time.perf_counter() - t0)))
+            continue
+        srv.tick()
+    wall = time.perf_counter() - t0
+    srv.close()
+    return wall, jobs, srv
+
+
+def run_serving(args, spec, job_specs):
+    """Poisson arrivals at each rate of `lambdas`, mixed precision and plain
+    FP64, the same seeded jobs; p50/p99 of step latency (the tick each job-step
+    ran in) and of job latency (arrival to result on the host); job-steps/s
+    over the wall time; the mixed result's position error against FP64."""
+    import torch
+    torch.cuda.set_device(0)
+    from hobakv1_gb300 import hobak
+    rng = np.random.default_rng(20261203 + 7)
+    gaps = rng.exponential(1.0, len(job_specs))
+    total_steps = sum(n for _, n, _ in job_specs)
+    budget = int(float(spec.get("budget_gb", 64)) * (1 << 30))
+    # warm the library (module load, first graph capture) outside the timing
+    serve_once(job_specs[:2], [0.0, 0.0], hobak.PRECISION_MIXED, budget)
+    runs = {}
+    finals = {}
+    for prec_name, prec in (("mixed", hobak.PRECISION_MIXED), ("fp64", hobak.PRECISION_FP64)):
+        for lam in spec["lambdas"]:
+            arrivals = np.cumsum(gaps) / lam
+            wall, jobs, srv = serve_once(job_specs, arrivals, prec, budget)
+            step_ms = [ms for j in jobs for ms in j.step_ms]
+            job_s = [j.finished - j.submitted for j in jobs]
+            runs[f"{prec_name}@{lam}"] = {
+                "lambda_per_s": lam, "precision": prec_name, "job_steps_per_s": total_steps / wall,
+                "wall_s": wall, "step_p50_ms": float(np.percentile(step_ms, 50)),
+                "step_p99_ms": float(np.percentile(step_ms, 99)),
+                "job_p50_s": float(np.percentile(job_s, 50)), "job_p99_s": float(np.percentile(job_s, 99)),
+                "ticks": srv.ticks}
+            finals[(prec_name, lam)] = [j.result_x + j.scene.rest.reshape(-1) for j in jobs]
+    lam_hi = max(spec["lambdas"])
+    errs = [np.linalg.norm(a - b) / np.linalg.norm(b)
+            for a, b in zip(finals[("mixed", lam_hi)], finals[("fp64", lam_hi)])]
+    hi_m, hi_f = runs[f"mixed@{lam_hi}"], runs[f"fp64@{lam_hi}"]
+    nbytes_in = sum(sc.nv * 3 * 8 * 2 + sc.nt * 16 + sc.nv * 24 for sc, _, _ in job_specs)
+    nbytes_out = sum(sc.nv * 3 * 8 * 2 for sc, _, _ in job_specs)
+    line = {"metric": METRIC, "value": hi_m["job_steps_per_s"], "unit": "job-steps/s", "n_gpus": 1,
+            "steps": total_steps, "warmup": 1, "ms_per_step": 1e3 / hi_m["job_steps_per_s"],
+            "p50_ms": hi_m["step_p50_ms"], "p99_ms": hi_m["step_p99_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": args.workload, "jobs": len(job_specs), "lambdas_per_s": spec["lambdas"],
+                       "cells_per_side": "U{8..32}", "steps_per_job": "U{10..200}",
+                       "contact": "even jobs: two SNH cubes, vertex-face eps 1e-3, stiffness 1e3, beta 1e-3",
+                       "tets_total": int(sum(sc.nt for sc, _, _ in job_specs)), "pcg_tol": 1e-8,
+                       "budget_gb": budget / (1 << 30),
+                       "timing": "wall clock from the first arrival to the last result on the host"},
+            "serving": runs,
+            "mixed_over_fp64_at_max_lambda": hi_m["job_steps_per_s"] / hi_f["job_steps_per_s"],
+            "mixed_vs_fp64_rel_pos_err": {"max": float(max(errs)), "median": float(np.median(errs))},
+            "e2e": {"value": hi_m["job_steps_per_s"], "unit": "job-steps/s", "h2d_bytes_per_step":
+                    nbytes_in / total_steps, "d2h_bytes_per_step": nbytes_out / total_steps,
+                    "api": "serving.Server over hobak_batch_create/step_async/wait/get_state"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, spec, scene_list):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -197,6 +281,36 @@ def run_reference(args, spec, scene_list):
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_serving(args, spec, job_specs, sample_jobs=4, steps=2):
+    """The oracle on the serving mix: a bounded sample (the first jobs, each
+    `steps` steps from its initial state, contact on where the job has it),
+    run one after another on the host cores; job-steps/s."""
+    if dist_info()[0] != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    sims = []
+    for sc, _, contact in job_specs[:sample_jobs]:
+        sim = oracle.Sim(sc, precond=0)
+        if contact is not None:
+            sim.set_collisions(True, *contact)
+        sims.append(sim)
+    t0 = time.perf_counter()
+    for sim in sims:
+        sim.step(steps)
+    value = steps * len(sims) / (time.perf_counter() - t0)
+    sample = (f"{steps} steps of each of the first {len(sims)} of {len(job_specs)} jobs "
+              f"({sum(s.scene.nt for s in sims)} tets), one after another")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "job-steps/s", "n_gpus": args.gpus,
+            "steps": steps * len(sims), "warmup": 0, "ms_per_step": 1e3 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "jobs": len(job_specs)},
+            "cpu_baseline": {"value": value, "unit": "job-steps/s", "cores": oracle.lib().oracle_threads(),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "job-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -352,7 +466,12 @@ def main():
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
     scene_list = make_scenes(spec)
-    if args.impl == "reference":
+    if spec["kind"] == "serve":
+        if args.impl == "reference":
+            run_reference_serving(args, spec, scene_list)
+        elif dist_info()[0] == 0:
+            run_serving(args, spec, scene_list)
+    elif args.impl == "reference":
         run_reference(args, spec, scene_list)
     else:
         run_ours(args, spec, scene_list)

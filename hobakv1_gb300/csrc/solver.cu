@@ -40,18 +40,15 @@ namespace {
 constexpr int kVecThreads = kTileV;       // vector kernels: one thread per vertex
 constexpr int kSpmvThreads = 3 * kTileV;  // SpMV: one thread per scalar row
 
-__device__ __forceinline__ double warp_sum(double v) {
+// Fixed-order sum over the CTA; result valid in thread 0.  NT multiple of 32.
+// The warp tree runs in R (FP32 for the inner solve of the mixed path, which
+// keeps its dot products off the FP64 pipe), the sum over warps in FP64.
+template <int NT, typename R>
+__device__ __forceinline__ double block_sum(R v, double* sh) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Fixed-order sum over the CTA; result valid in thread 0.  NT multiple of 32.
-template <int NT>
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-  v = warp_sum(v);
   const int w = threadIdx.x / 32, l = threadIdx.x % 32;
-  if (l == 0) sh[w] = v;
+  if (l == 0) sh[w] = double(v);
   __syncthreads();
   double s = 0;
   if (threadIdx.x == 0) {
@@ -281,7 +278,7 @@ __global__ void __launch_bounds__(kVecThreads) k_inner_init(DeviceBatch b, PcgVe
     return;
   }
   const int u = b.tileV0[tile] + threadIdx.x;
-  double rr = 0, ru = 0;
+  T rr = T(0), ru = T(0);
   if (u < b.tileV1[tile]) {
     T r3[3];
 #pragma unroll
@@ -291,14 +288,14 @@ __global__ void __launch_bounds__(kVecThreads) k_inner_init(DeviceBatch b, PcgVe
       v.d[3 * u + i] = T(0);
       v.p[3 * u + i] = T(0);
       v.s[3 * u + i] = T(0);
-      rr += double(r3[i]) * double(r3[i]);
+      rr += r3[i] * r3[i];
     }
     const T* M = v.minv + 9 * (size_t)u;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
       v.u[3 * u + i] = ui;
-      ru += double(r3[i]) * double(ui);
+      ru += r3[i] * ui;
     }
   }
   const double trr = block_sum<kVecThreads>(rr, sh);
@@ -328,9 +325,11 @@ __global__ void __launch_bounds__(kVecThreads) k_inner_init(DeviceBatch b, PcgVe
   }
 }
 
-// Row i of vertex u of -(dt beta + dt^2) H_coll x, H_coll = sum over the
-// vertex's collision tets of (c c^T) (x) G (free rows only; x vanishes on
-// pinned rows, which keeps the columns masked too).
+// Row i of vertex u of the off-diagonal part of -(dt beta + dt^2) H_coll x,
+// H_coll = sum over the vertex's collision tets of (c c^T) (x) G (free rows
+// only; x vanishes on pinned rows, which keeps the columns masked too).  The
+// vertex's own 3x3 block was folded into LHS's diagonal by k_coll_diag, so the
+// tet's column for u itself is skipped here.
 template <typename T>
 __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int i, const T* __restrict__ x) {
   const DeviceCollisions& c = b.coll;
@@ -347,9 +346,11 @@ __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int
     const int id[4] = {ct.x, ct.y, ct.z, ct.w};
     double z[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-    for (int q = 0; q < 4; q++)
+    for (int q = 0; q < 4; q++) {
+      if (q == a) continue;
 #pragma unroll
       for (int j = 0; j < 3; j++) z[j] += C[q] * double(x[3 * id[q] + j]);
+    }
     acc += C[a] * (G[i] * z[0] + G[i + 3] * z[1] + G[i + 6] * z[2]);
   }
   return scale * acc;
@@ -366,36 +367,44 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T>
   SolveState& st = b.solve[s];
   if (st.done) return;
   const int row = 3 * b.tileV0[tile] + threadIdx.x;
-  double dl = 0.0;
+  T dl = T(0);
   if (row < 3 * b.tileV1[tile]) {
     const int u = row / 3, i = row - 3 * u;
     const T* __restrict__ uu = v.u;
     const T* __restrict__ A = v.lhs + 3 * i;
-    T acc = T(0);
+    // two FMA chains (3 FMA per block, the FP64 minimum); four blocks per trip
+    // so their independent loads are in flight together
+    T acc0 = T(0), acc1 = T(0);
     const int k1 = b.rowptr[u + 1];
     int k = b.rowptr[u];
-    // four blocks per trip so their independent loads are in flight together
     for (; k + 3 < k1; k += 4) {
       const int w0 = __ldg(&b.cols[k]), w1 = __ldg(&b.cols[k + 1]);
       const int w2 = __ldg(&b.cols[k + 2]), w3 = __ldg(&b.cols[k + 3]);
       const T* B = A + 9 * (size_t)k;
-      const T t0 = B[0] * uu[3 * w0] + B[1] * uu[3 * w0 + 1] + B[2] * uu[3 * w0 + 2];
-      const T t1 = B[9] * uu[3 * w1] + B[10] * uu[3 * w1 + 1] + B[11] * uu[3 * w1 + 2];
-      const T t2 = B[18] * uu[3 * w2] + B[19] * uu[3 * w2 + 1] + B[20] * uu[3 * w2 + 2];
-      const T t3 = B[27] * uu[3 * w3] + B[28] * uu[3 * w3 + 1] + B[29] * uu[3 * w3 + 2];
-      acc += t0;
-      acc += t1;
-      acc += t2;
-      acc += t3;
+      acc0 = fma(B[0], uu[3 * w0], acc0);
+      acc1 = fma(B[9], uu[3 * w1], acc1);
+      acc0 = fma(B[1], uu[3 * w0 + 1], acc0);
+      acc1 = fma(B[10], uu[3 * w1 + 1], acc1);
+      acc0 = fma(B[2], uu[3 * w0 + 2], acc0);
+      acc1 = fma(B[11], uu[3 * w1 + 2], acc1);
+      acc0 = fma(B[18], uu[3 * w2], acc0);
+      acc1 = fma(B[27], uu[3 * w3], acc1);
+      acc0 = fma(B[19], uu[3 * w2 + 1], acc0);
+      acc1 = fma(B[28], uu[3 * w3 + 1], acc1);
+      acc0 = fma(B[20], uu[3 * w2 + 2], acc0);
+      acc1 = fma(B[29], uu[3 * w3 + 2], acc1);
     }
     for (; k < k1; k++) {
       const int w = __ldg(&b.cols[k]);
       const T* B = A + 9 * (size_t)k;
-      acc += B[0] * uu[3 * w] + B[1] * uu[3 * w + 1] + B[2] * uu[3 * w + 2];
+      acc0 = fma(B[0], uu[3 * w], acc0);
+      acc0 = fma(B[1], uu[3 * w + 1], acc0);
+      acc0 = fma(B[2], uu[3 * w + 2], acc0);
     }
+    T acc = acc0 + acc1;
     if (b.collOn && b.freeMask[u]) acc += T(collision_row<T>(b, u, i, uu));
     v.w[row] = acc;
-    dl = double(acc) * double(uu[row]);
+    dl = acc * uu[row];
   }
   const double t = block_sum<kSpmvThreads>(dl, sh);
   if (threadIdx.x == 0) b.partial[kPartials * tile + 2] = t;
@@ -418,49 +427,52 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T>
 // p = u + beta p; s = w + beta s; d += alpha p; r -= alpha s; u = Minv r;
 // gamma' = (r, u); |r|^2 -> stop when |r|^2 < threshold (ConjugateGradient.h:75-78).
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_update(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[kVecThreads / 32];
+// One thread per scalar row (three times the threads of a per-vertex loop,
+// which a 40^3 scene needs to cover the GPU's latency); the 3x3 block of
+// Minv reads its vertex's three new residual rows from shared memory.
+__global__ void __launch_bounds__(kSpmvThreads) k_update(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[kSpmvThreads / 32];
+  __shared__ T rsh[kSpmvThreads];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
   SolveState& st = b.solve[s];
   if (st.done) return;
   const T alpha = T(st.alpha), beta = T(st.beta);
-  const int u = b.tileV0[tile] + threadIdx.x;
-  double rr = 0, ru = 0;
+  const int row = 3 * b.tileV0[tile] + threadIdx.x;
+  const bool valid = row < 3 * b.tileV1[tile];
+  T rr = T(0), ru = T(0);
   T* __restrict__ r = (sizeof(T) == sizeof(double)) ? reinterpret_cast<T*>(b.r64) : v.r;
-  if (u < b.tileV1[tile]) {
-    T r3[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      const int k = 3 * u + i;
-      const T p = v.u[k] + beta * v.p[k];
-      const T sv = v.w[k] + beta * v.s[k];
-      v.p[k] = p;
-      v.s[k] = sv;
-      v.d[k] += alpha * p;
-      r3[i] = r[k] - alpha * sv;
-      r[k] = r3[i];
-      rr += double(r3[i]) * double(r3[i]);
-    }
-    const T* M = v.minv + 9 * (size_t)u;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
-      v.u[3 * u + i] = ui;
-      ru += double(r3[i]) * double(ui);
-    }
+  T rnew = T(0);
+  if (valid) {
+    const T p = v.u[row] + beta * v.p[row];
+    const T sv = v.w[row] + beta * v.s[row];
+    v.p[row] = p;
+    v.s[row] = sv;
+    v.d[row] += alpha * p;
+    rnew = r[row] - alpha * sv;
+    r[row] = rnew;
+    rr = rnew * rnew;
   }
-  const double trr = block_sum<kVecThreads>(rr, sh);
-  const double tru = block_sum<kVecThreads>(ru, sh);
+  rsh[threadIdx.x] = rnew;
+  __syncthreads();
+  if (valid) {
+    const int base = threadIdx.x - threadIdx.x % 3;
+    const T* M = v.minv + 3 * (size_t)row;  // row i of the vertex's block
+    const T ui = M[0] * rsh[base] + M[1] * rsh[base + 1] + M[2] * rsh[base + 2];
+    v.u[row] = ui;
+    ru = rnew * ui;
+  }
+  const double trr = block_sum<kSpmvThreads>(rr, sh);
+  const double tru = block_sum<kSpmvThreads>(ru, sh);
   if (threadIdx.x == 0) {
     b.partial[kPartials * tile] = trr;
     b.partial[kPartials * tile + 1] = tru;
   }
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketB, sp.ntiles, &flag)) return;
-  const double srr = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 0, sh);
-  const double sru = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 1, sh);
+  const double srr = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 0, sh);
+  const double sru = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 1, sh);
   if (threadIdx.x == 0) {
     st.rr = srr;
     st.iters += 1;
@@ -610,7 +622,7 @@ void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
 
 template <typename T>
 void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
-  k_update<T><<<b.ntiles, kVecThreads, 0, s>>>(b, v);
+  k_update<T><<<b.ntiles, kSpmvThreads, 0, s>>>(b, v);
 }
 
 void launch_refine(const DeviceBatch& b, cudaStream_t s) {

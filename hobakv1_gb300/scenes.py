@@ -209,3 +209,32 @@ def two_cubes_scene(N: int = 8, gap: float = 5e-4, offset: float = 0.1, material
     mu, lam = lame(E, nu)
     zeros = np.zeros_like(rest)
     return Scene(f"two_cubes{N}_{material}", rest, tets, material, mu, lam, bottom, zeros.copy(), zeros.copy(), N=N)
+
+
+# vertex-face contact of the serving mix: collision distance, spring stiffness,
+# damping beta (TIMESTEPPER.cpp:86 default)
+SERVE_CONTACT = (1e-3, 1e3, 0.001)
+
+
+def config5_jobs(count: int = 64, nmin: int = 8, nmax: int = 32, smin: int = 10, smax: int = 200,
+                 seed: int = BASE_SEED + 6):
+    """Serving mix: jobs of N ~ U{nmin..nmax} cells per side running
+    U{smin..smax} steps.  Even jobs are two SNH cubes in one mesh (lower bottom
+    face pinned, upper cube 0.1 offset, resting 5e-4 above it, so contact is on
+    from the first step) with vertex-face contact SERVE_CONTACT; odd jobs are
+    single cubes drawn like the batched mix (random rotation, SNH/ARAP,
+    log-uniform mu).  Returns [(scene, nsteps, contact or None)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for j in range(count):
+        N = int(rng.integers(nmin, nmax + 1))
+        steps = int(rng.integers(smin, smax + 1))
+        if j % 2 == 0:
+            sc = two_cubes_scene(N, seed=seed + 1000 + 2 * j)
+            sc.name = f"serve{j}_two_cubes{N}"
+            out.append((sc, steps, SERVE_CONTACT))
+        else:
+            sc = config4_scenes(1, N, N, seed=seed + 1000 + 2 * j)[0]
+            sc.name = f"serve{j}_n{N}_{sc.material}"
+            out.append((sc, steps, None))
+    return out

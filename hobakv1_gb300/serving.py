@@ -16,9 +16,16 @@ runs a tick loop:
 
 Within a cohort every scene keeps its own reduction tiles, so a job's result
 does not depend on which other jobs shared its batch or the device.
+
+With `async_build=True` a builder thread creates the admitted cohorts (mesh
+upload, block pattern, surface extraction; the library calls release the
+GIL), so admission work overlaps the running cohorts' steps instead of
+stalling them; a cohort joins the running set at the first tick after it is
+built.  The memory budget is reserved at admission time.
 """
 from __future__ import annotations
 
+import concurrent.futures
 import dataclasses
 import time
 from collections import deque
@@ -77,7 +84,7 @@ class Server:
     """Tick-driven continuous batching under a device-memory budget."""
 
     def __init__(self, budget_bytes: int, precision: int = hobak.PRECISION_MIXED,
-                 max_admit_per_tick: int = 64, keep_results: bool = True):
+                 max_admit_per_tick: int = 64, keep_results: bool = True, async_build: bool = False):
         self.budget = int(budget_bytes)
         self.opts = hobak.solver_opts(precision=precision)
         self.max_admit = max_admit_per_tick
@@ -89,6 +96,8 @@ class Server:
         self.ticks = 0
         self.tick_ms: List[float] = []
         self.rejected = 0
+        self._pool = concurrent.futures.ThreadPoolExecutor(max_workers=1) if async_build else None
+        self._building: List[tuple] = []  # (future, reserved bytes)
 
     # ---- client side ----
     def submit(self, job: Job):
@@ -99,10 +108,28 @@ class Server:
         self.queue.append(job)
 
     def idle(self) -> bool:
-        return not self.queue and not self.cohorts
+        return not self.queue and not self.cohorts and not self._building
 
     # ---- server loop ----
+    def _join(self, c: Cohort, reserved: int):
+        now = time.perf_counter()
+        for j in c.jobs:
+            j.admitted = now
+        self.used += c.bytes - reserved
+        self.cohorts.append(c)
+
+    def _collect_built(self, block: bool = False):
+        keep = []
+        for fut, reserved in self._building:
+            if fut.done() or block:
+                self._join(fut.result(), reserved)
+            else:
+                keep.append((fut, reserved))
+        self._building = keep
+
     def _admit(self):
+        if self._pool is not None:
+            self._collect_built(block=not self.cohorts)  # nothing running: wait for the build
         take: List[Job] = []
         est = 0
         while self.queue and len(take) < self.max_admit:
@@ -111,13 +138,15 @@ class Server:
                 break
             est += need
             take.append(self.queue.popleft())
-        if take:
-            c = Cohort(take, self.opts)
-            now = time.perf_counter()
-            for j in take:
-                j.admitted = now
-            self.used += c.bytes
-            self.cohorts.append(c)
+        if not take:
+            return
+        self.used += est  # reserved until the cohort reports its real size
+        if self._pool is None:
+            self._join(Cohort(take, self.opts), est)
+        else:
+            self._building.append((self._pool.submit(Cohort, take, self.opts), est))
+            if not self.cohorts:
+                self._collect_built(block=True)
 
     def tick(self) -> int:
         """One scheduling round; returns the number of job-steps it completed."""
@@ -164,6 +193,9 @@ class Server:
             max_ticks -= 1
 
     def close(self):
+        if self._pool is not None:
+            self._collect_built(block=True)
+            self._pool.shutdown()
         for c in self.cohorts:
             c.close()
         self.cohorts.clear()
