@@ -930,6 +930,14 @@ int hobak_batch_step_async(hobak_batch b, int nsteps) {
   return HOBAK_OK;
 }
 
+int hobak_batch_query(hobak_batch b) {
+  if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
+  const cudaError_t e = cudaStreamQuery(b->stream);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return fail(HOBAK_ERR_CUDA, std::string("cudaStreamQuery: ") + cudaGetErrorString(e));
+}
+
 int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats) {
   int rc = hobak_batch_step_async(b, nsteps);
   if (rc) return rc;

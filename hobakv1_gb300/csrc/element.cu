@@ -199,7 +199,10 @@ __device__ __forceinline__ void deformation_gradient(const double X[4][3], const
 // HT is the Hessian's arithmetic/storage type: double (FP64 path) or float
 // (mixed path: F, SVD, stress and forces stay FP64).
 template <typename HT>
-__global__ void __launch_bounds__(128) k_element(DeviceBatch b, int rawForces, HT* __restrict__ outH) {
+// FP32 Hessians fit 128 registers (4 CTAs per SM, a few bytes of spill); the
+// FP64 variant needs ~208 and spills heavily below that.
+__global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
+    k_element(DeviceBatch b, int rawForces, HT* __restrict__ outH) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= b.nt) return;
   const SceneParams& sp = b.scenes[b.tetScene[t]];

@@ -135,11 +135,15 @@ __device__ __forceinline__ void svd3_rv(const double* F, double* U, double* S, d
 //   1. one-sided Jacobi sweeps in FP32 give V32 with F V32 orthogonal to ~1e-7;
 //   2. V32 is re-orthonormalised in FP64 (modified Gram-Schmidt), so V stays an
 //      exact rotation to FP64 precision;
-//   3. FP64 one-sided Jacobi on A = F V finishes the job; starting ~1e-7 from
-//      orthogonal it converges in one sweep (quadratic convergence) and a
-//      second sweep only confirms.  Rotation angles are computed in FP32 and
-//      turned into an exactly orthogonal (c, s) pair in FP64.
-// The result has FP64 accuracy (same convergence test as svd3_rv).
+//   3. FP64 one-sided Jacobi on A = F V finishes the job; starting ~1e-6 from
+//      orthogonal, one sweep brings the columns to ~1e-12 (quadratic
+//      convergence) and the second sweep only checks.  Rotation angles are
+//      computed in FP32 and turned into an exactly orthogonal (c, s) pair in
+//      FP64.
+// V is a rotation to FP64 rounding and F = U S V^T holds to FP64 rounding;
+// U's columns are orthogonal to 1e-13 relative (the stop test), which keeps
+// forces and Hessians within 1e-12 of a fully converged SVD while sparing a
+// second rotating sweep of ~110 FP64 instructions per element.
 __device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double* S, double* V) {
   // ---- stage 1: FP32 Jacobi ----
   float a[9], w[9];
@@ -205,7 +209,7 @@ __device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double*
       const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
       const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
       const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
-      if (gamma * gamma > 1e-30 * (alpha * beta)) {  // ~1e-15 relative: FP64 rounding floor
+      if (gamma * gamma > 1e-26 * (alpha * beta)) {  // columns orthogonal to 1e-13 relative
         rotated = true;
         // angle in FP32 (only orthogonality of (c, s) must be FP64-exact)
         const float zf = float(beta - alpha) / (2.0f * float(gamma));

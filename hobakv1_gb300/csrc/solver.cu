@@ -59,11 +59,40 @@ __device__ __forceinline__ double block_sum(R v, double* sh) {
   return s;
 }
 
-// After a CTA wrote its partial(s): true in the CTA that finishes the scene's
-// reduction (ticket == ntiles - 1).  The ticket is reset for reuse.
-__device__ __forceinline__ bool last_tile(unsigned* ticket, int ntiles, int* flag) {
-  __threadfence();
+// Two sums in one pass (one pair of barriers); results valid in thread 0.
+// `sh` holds 2 * NT / 32 doubles.
+template <int NT, typename R>
+__device__ __forceinline__ void block_sum2(R a, R b, double* sh, double& sa, double& sb) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  if (l == 0) {
+    sh[w] = double(a);
+    sh[NT / 32 + w] = double(b);
+  }
+  __syncthreads();
+  sa = 0.0;
+  sb = 0.0;
   if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NT / 32; i++) {
+      sa += sh[i];
+      sb += sh[NT / 32 + i];
+    }
+  }
+  __syncthreads();
+}
+
+// After thread 0 wrote the CTA's partial(s): true in the CTA that finishes
+// the scene's reduction (ticket == ntiles - 1).  Only thread 0 published
+// anything the last CTA reads, so only it fences before taking its ticket.
+// The ticket is reset for reuse.
+__device__ __forceinline__ bool last_tile(unsigned* ticket, int ntiles, int* flag) {
+  if (threadIdx.x == 0) {
+    __threadfence();
     const unsigned t = atomicAdd(ticket, 1u);
     *flag = (t == (unsigned)(ntiles - 1));
     if (*flag) *ticket = 0u;
@@ -97,16 +126,30 @@ __global__ void k_begin_step(DeviceBatch b) {
 // (TET_MESH_FASTER.cpp:113-131 gathers the same entries per non-zero).
 // The sum is formed in HT: FP64 for the FP64 path, FP32 for the mixed path
 // (whose matrix is FP32 anyway; converting every term would load the FP64 pipe).
+// Contributions are fetched eight at a time (all map entries, then all
+// values, as independent loads) and added in list order, so a diagonal block
+// with ~24 incident tets waits on 6 memory latencies instead of 48.
 template <typename HT>
 __device__ __forceinline__ HT gather_block_entry(const DeviceBatch& b, const HT* __restrict__ elemH, int blk,
                                                  int r, int c) {
   HT sum = HT(0);
   const int k1 = b.blkptr[blk + 1];
-  for (int k = b.blkptr[blk]; k < k1; k++) {
-    const int src = b.blksrc[k];
-    const int t = src >> 4, ea = (src >> 2) & 3, eb = src & 3;
-    const HT* H = elemH + (size_t)kElemHess * t;
-    sum += (ea <= eb) ? H[9 * upper_block(ea, eb) + 3 * r + c] : H[9 * upper_block(eb, ea) + 3 * c + r];
+  for (int k = b.blkptr[blk]; k < k1; k += 8) {
+    int src[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) src[q] = (k + q < k1) ? __ldg(&b.blksrc[k + q]) : 0;
+    HT val[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int t = src[q] >> 4, ea = (src[q] >> 2) & 3, eb = src[q] & 3;
+      const HT* H = elemH + (size_t)kElemHess * t;
+      val[q] = (k + q >= k1) ? HT(0)
+               : (ea <= eb)  ? H[9 * upper_block(ea, eb) + 3 * r + c]
+                             : H[9 * upper_block(eb, ea) + 3 * c + r];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      if (k + q < k1) sum += val[q];
   }
   return sum;
 }
@@ -206,11 +249,23 @@ __global__ void __launch_bounds__(kVecThreads) k_rhs(DeviceBatch b) {
   if (u < b.tileV1[tile]) {
     const double dt = b.scenes[s].dt;
     double acc[3] = {0.0, 0.0, 0.0};
-    for (int k = b.vtxptr[u]; k < b.vtxptr[u + 1]; k++) {
-      const int inc = b.vtxinc[k];
-      const double* g = b.elemG + 12 * (size_t)(inc >> 2) + 3 * (inc & 3);
+    const int k1 = b.vtxptr[u + 1];
+    for (int k = b.vtxptr[u]; k < k1; k += 8) {  // eight incidences in flight, summed in order
+      int inc[8];
 #pragma unroll
-      for (int i = 0; i < 3; i++) acc[i] += g[i];
+      for (int q = 0; q < 8; q++) inc[q] = (k + q < k1) ? __ldg(&b.vtxinc[k + q]) : 0;
+      double gv[8][3];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const double* g = b.elemG + 12 * (size_t)(inc[q] >> 2) + 3 * (inc[q] & 3);
+#pragma unroll
+        for (int i = 0; i < 3; i++) gv[q][i] = (k + q < k1) ? g[i] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (k + q < k1)
+#pragma unroll
+          for (int i = 0; i < 3; i++) acc[i] += gv[q][i];
     }
     const bool fu = b.freeMask[u] != 0;
     if (b.collOn && fu) {  // collision tets: dt (f + dt H v), in pair order
@@ -372,34 +427,32 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T>
     const int u = row / 3, i = row - 3 * u;
     const T* __restrict__ uu = v.u;
     const T* __restrict__ A = v.lhs + 3 * i;
-    // two FMA chains (3 FMA per block, the FP64 minimum); four blocks per trip
-    // so their independent loads are in flight together
+    // Four blocks per trip, all their loads issued together (predicated past
+    // the row's end); the next trip's column indices are fetched one trip
+    // ahead, so each trip waits on one memory latency (the u gather) instead
+    // of two.  Two FMA chains: 3 FMA per block, the FP64 minimum.
     T acc0 = T(0), acc1 = T(0);
-    const int k1 = b.rowptr[u + 1];
-    int k = b.rowptr[u];
-    for (; k + 3 < k1; k += 4) {
-      const int w0 = __ldg(&b.cols[k]), w1 = __ldg(&b.cols[k + 1]);
-      const int w2 = __ldg(&b.cols[k + 2]), w3 = __ldg(&b.cols[k + 3]);
+    const int k0 = b.rowptr[u], k1 = b.rowptr[u + 1];
+    int wn[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) wn[q] = (k0 + q < k1) ? __ldg(&b.cols[k0 + q]) : 0;
+    for (int k = k0; k < k1; k += 4) {
+      int w[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        w[q] = wn[q];
+        wn[q] = (k + 4 + q < k1) ? __ldg(&b.cols[k + 4 + q]) : 0;
+      }
       const T* B = A + 9 * (size_t)k;
-      acc0 = fma(B[0], uu[3 * w0], acc0);
-      acc1 = fma(B[9], uu[3 * w1], acc1);
-      acc0 = fma(B[1], uu[3 * w0 + 1], acc0);
-      acc1 = fma(B[10], uu[3 * w1 + 1], acc1);
-      acc0 = fma(B[2], uu[3 * w0 + 2], acc0);
-      acc1 = fma(B[11], uu[3 * w1 + 2], acc1);
-      acc0 = fma(B[18], uu[3 * w2], acc0);
-      acc1 = fma(B[27], uu[3 * w3], acc1);
-      acc0 = fma(B[19], uu[3 * w2 + 1], acc0);
-      acc1 = fma(B[28], uu[3 * w3 + 1], acc1);
-      acc0 = fma(B[20], uu[3 * w2 + 2], acc0);
-      acc1 = fma(B[29], uu[3 * w3 + 2], acc1);
-    }
-    for (; k < k1; k++) {
-      const int w = __ldg(&b.cols[k]);
-      const T* B = A + 9 * (size_t)k;
-      acc0 = fma(B[0], uu[3 * w], acc0);
-      acc0 = fma(B[1], uu[3 * w + 1], acc0);
-      acc0 = fma(B[2], uu[3 * w + 2], acc0);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (k + q < k1) {
+          T& acc = (q & 1) ? acc1 : acc0;
+          acc = fma(B[9 * q], uu[3 * w[q]], acc);
+          acc = fma(B[9 * q + 1], uu[3 * w[q] + 1], acc);
+          acc = fma(B[9 * q + 2], uu[3 * w[q] + 2], acc);
+        }
+      }
     }
     T acc = acc0 + acc1;
     if (b.collOn && b.freeMask[u]) acc += T(collision_row<T>(b, u, i, uu));
@@ -430,8 +483,8 @@ template <typename T>
 // One thread per scalar row (three times the threads of a per-vertex loop,
 // which a 40^3 scene needs to cover the GPU's latency); the 3x3 block of
 // Minv reads its vertex's three new residual rows from shared memory.
-__global__ void __launch_bounds__(kSpmvThreads) k_update(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[kSpmvThreads / 32];
+__global__ void __launch_bounds__(kSpmvThreads, 5) k_update(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[2 * kSpmvThreads / 32];
   __shared__ T rsh[kSpmvThreads];
   __shared__ int flag;
   const int tile = blockIdx.x;
@@ -443,14 +496,20 @@ __global__ void __launch_bounds__(kSpmvThreads) k_update(DeviceBatch b, PcgVecs<
   const bool valid = row < 3 * b.tileV1[tile];
   T rr = T(0), ru = T(0);
   T* __restrict__ r = (sizeof(T) == sizeof(double)) ? reinterpret_cast<T*>(b.r64) : v.r;
-  T rnew = T(0);
+  T rnew = T(0), M0 = T(0), M1 = T(0), M2 = T(0);
   if (valid) {
-    const T p = v.u[row] + beta * v.p[row];
-    const T sv = v.w[row] + beta * v.s[row];
+    // every load of the thread issued together, Minv's row included
+    const T* M = v.minv + 3 * (size_t)row;  // row i of the vertex's block
+    const T u0 = v.u[row], p0 = v.p[row], w0 = v.w[row], s0 = v.s[row], d0 = v.d[row], r0 = r[row];
+    M0 = M[0];
+    M1 = M[1];
+    M2 = M[2];
+    const T p = u0 + beta * p0;
+    const T sv = w0 + beta * s0;
     v.p[row] = p;
     v.s[row] = sv;
-    v.d[row] += alpha * p;
-    rnew = r[row] - alpha * sv;
+    v.d[row] = d0 + alpha * p;
+    rnew = r0 - alpha * sv;
     r[row] = rnew;
     rr = rnew * rnew;
   }
@@ -458,13 +517,12 @@ __global__ void __launch_bounds__(kSpmvThreads) k_update(DeviceBatch b, PcgVecs<
   __syncthreads();
   if (valid) {
     const int base = threadIdx.x - threadIdx.x % 3;
-    const T* M = v.minv + 3 * (size_t)row;  // row i of the vertex's block
-    const T ui = M[0] * rsh[base] + M[1] * rsh[base + 1] + M[2] * rsh[base + 2];
+    const T ui = M0 * rsh[base] + M1 * rsh[base + 1] + M2 * rsh[base + 2];
     v.u[row] = ui;
     ru = rnew * ui;
   }
-  const double trr = block_sum<kSpmvThreads>(rr, sh);
-  const double tru = block_sum<kSpmvThreads>(ru, sh);
+  double trr, tru;
+  block_sum2<kSpmvThreads>(rr, ru, sh, trr, tru);
   if (threadIdx.x == 0) {
     b.partial[kPartials * tile] = trr;
     b.partial[kPartials * tile + 1] = tru;

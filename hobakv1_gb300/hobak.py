@@ -244,6 +244,10 @@ class BATCH:
         self.last_stats = [(s.iterations, s.converged, s.rel_residual, s.refinements) for s in stats]
         return self.last_stats
 
+    def query(self) -> bool:
+        """True when the batch's enqueued steps have finished (non-blocking)."""
+        return check(_lib.load().hobak_batch_query(self.h), "hobak_batch_query") == 1
+
     def set_active(self, scene: int, active: bool = True):
         """Park (False) or resume one scene; parked scenes keep their state."""
         check(_lib.load().hobak_batch_set_active(self.h, scene, int(active)), "hobak_batch_set_active")

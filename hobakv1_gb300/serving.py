@@ -1,18 +1,22 @@
 """Continuous-batching server for scene-timestep jobs.
 
 A job is a scene plus a number of BACKWARD_EULER_VELOCITY steps.  The server
-keeps every admitted job's state resident on the GPU until it finishes and
-runs a tick loop:
+keeps every admitted job's state resident on the GPU until it finishes:
 
   1. admission: queued jobs (FIFO) are admitted while their estimated device
-     footprint fits the memory budget; the jobs admitted in one tick are packed
+     footprint fits the memory budget; the jobs admitted together are packed
      into one batch (a "cohort") that joins the running set;
-  2. every cohort with running jobs enqueues one step on its own CUDA stream
+  2. every cohort with running jobs steps on its own CUDA stream
      (hobak_batch_step_async), so the cohorts' work overlaps on the device;
-  3. the server waits for all of them (hobak_batch_wait); each running job
-     records the tick's latency as its step latency; finished jobs are parked
+  3. a finished step is booked for the cohort's running jobs (its latency is
+     the job's step latency); finished jobs are parked
      (hobak_batch_set_active(scene, 0): state kept, kernels skip them) and
      their final state is read back; a cohort whose jobs are all done is freed.
+
+`pump()` is the event-driven loop: each cohort is polled
+(hobak_batch_query) and relaunched as soon as its own step is done, so a
+cohort of small fast scenes never waits for a cohort of large ones.
+`tick()` is the lock-step variant (all cohorts step, all are waited for).
 
 Within a cohort every scene keeps its own reduction tiles, so a job's result
 does not depend on which other jobs shared its batch or the device.
@@ -20,8 +24,8 @@ does not depend on which other jobs shared its batch or the device.
 With `async_build=True` a builder thread creates the admitted cohorts (mesh
 upload, block pattern, surface extraction; the library calls release the
 GIL), so admission work overlaps the running cohorts' steps instead of
-stalling them; a cohort joins the running set at the first tick after it is
-built.  The memory budget is reserved at admission time.
+stalling them; a cohort joins the running set at the first scheduling round
+after it is built.  The memory budget is reserved at admission time.
 """
 from __future__ import annotations
 
@@ -75,13 +79,14 @@ class Cohort:
                 self.batch.set_collisions(k, True, eps, mu, beta)
         self.bytes = self.batch.device_bytes()
         self.running = len(jobs)
+        self.t_launch = None  # perf_counter() of the step in flight (pump mode)
 
     def close(self):
         self.batch.close()
 
 
 class Server:
-    """Tick-driven continuous batching under a device-memory budget."""
+    """Continuous batching under a device-memory budget."""
 
     def __init__(self, budget_bytes: int, precision: int = hobak.PRECISION_MIXED,
                  max_admit_per_tick: int = 64, keep_results: bool = True, async_build: bool = False):
@@ -148,43 +153,73 @@ class Server:
             if not self.cohorts:
                 self._collect_built(block=True)
 
+    def _step_done(self, c: Cohort, ms: float, now: float) -> int:
+        """Book one finished step of cohort c (latency ms) for its running jobs."""
+        done = 0
+        for j in c.jobs:
+            if j.finished >= 0:
+                continue
+            j.done_steps += 1
+            j.step_ms.append(ms)
+            done += 1
+            if j.done_steps >= j.nsteps:
+                j.finished = now
+                if self.keep_results:
+                    j.result_x, j.result_v = c.batch.get_state(j.slot)
+                c.batch.set_active(j.slot, False)
+                c.running -= 1
+                self.finished[j.id] = j
+        return done
+
+    def _retire(self):
+        for c in [c for c in self.cohorts if c.running == 0 and c.t_launch is None]:
+            self.used -= c.bytes
+            c.close()
+            self.cohorts.remove(c)
+
     def tick(self) -> int:
-        """One scheduling round; returns the number of job-steps it completed."""
+        """One lock-step scheduling round: every running cohort advances one
+        step, all are waited for; returns the number of job-steps completed."""
         self._admit()
-        live = [c for c in self.cohorts if c.running > 0]
+        live = [c for c in self.cohorts if c.running > 0 and c.t_launch is None]
         if not live:
             return 0
         t0 = time.perf_counter()
         for c in live:
-            hobak._lib.check(hobak._lib.load().hobak_batch_step_async(c.batch.h, 1), "hobak_batch_step_async")
-        stats = {}
+            c.batch.step_async(1)
         for c in live:
-            st = (hobak._lib.HobakStepStats * len(c.jobs))()
-            hobak._lib.check(hobak._lib.load().hobak_batch_wait(c.batch.h, st), "hobak_batch_wait")
-            stats[id(c)] = st
+            c.batch.wait()
         ms = (time.perf_counter() - t0) * 1e3
         self.tick_ms.append(ms)
         self.ticks += 1
-        done = 0
         now = time.perf_counter()
-        for c in live:
-            for j in c.jobs:
-                if j.finished >= 0:
+        done = sum(self._step_done(c, ms, now) for c in live)
+        self._retire()
+        return done
+
+    def pump(self) -> int:
+        """One event-driven scheduling round: admit, start a step on every
+        idle cohort, and book every cohort whose step has finished, starting
+        its next step at once; cohorts never wait for one another.  A job's
+        step latency is its cohort's launch-to-completion time.  Returns the
+        number of job-steps completed (0 when nothing finished yet)."""
+        self._admit()
+        done = 0
+        for c in list(self.cohorts):
+            if c.t_launch is not None:
+                if not c.batch.query():
                     continue
-                j.done_steps += 1
-                j.step_ms.append(ms)
-                done += 1
-                if j.done_steps >= j.nsteps:
-                    j.finished = now
-                    if self.keep_results:
-                        j.result_x, j.result_v = c.batch.get_state(j.slot)
-                    c.batch.set_active(j.slot, False)
-                    c.running -= 1
-                    self.finished[j.id] = j
-        for c in [c for c in self.cohorts if c.running == 0]:
-            self.used -= c.bytes
-            c.close()
-            self.cohorts.remove(c)
+                c.batch.wait()
+                now = time.perf_counter()
+                ms = (now - c.t_launch) * 1e3
+                c.t_launch = None
+                self.tick_ms.append(ms)
+                self.ticks += 1
+                done += self._step_done(c, ms, now)
+            if c.running > 0:
+                c.batch.step_async(1)
+                c.t_launch = time.perf_counter()
+        self._retire()
         return done
 
     def drain(self, max_ticks: int = 1_000_000):

@@ -124,6 +124,10 @@ int hobak_batch_step(hobak_batch b, int nsteps, hobak_step_stats* stats);
  * then wait for them and collect the stats of the last step. */
 int hobak_batch_step_async(hobak_batch b, int nsteps);
 int hobak_batch_wait(hobak_batch b, hobak_step_stats* stats);
+/* Non-blocking: 1 when everything enqueued on the batch has finished (a
+ * following hobak_batch_wait returns without blocking), 0 while work is still
+ * running, negative on error. */
+int hobak_batch_query(hobak_batch b);
 /* Park (active = 0) or resume one scene: a parked scene keeps its state and is
  * skipped by every kernel, so a serving loop can retire finished jobs without
  * re-packing the batch (no reference counterpart). */

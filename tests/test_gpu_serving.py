@@ -62,3 +62,25 @@ def test_admission_respects_the_memory_budget():
     assert all(j.admitted >= j.submitted for j in js)
     with pytest.raises(ValueError):
         Server(budget_bytes=1024).submit(js[0])
+
+
+def test_event_driven_pump_matches_alone():
+    """pump(): cohorts relaunch independently (async builds, small cohorts);
+    results stay bitwise equal to each job run alone."""
+    js = jobs()
+    srv = Server(budget_bytes=1 << 34, precision=hobak.PRECISION_MIXED, async_build=True,
+                 max_admit_per_tick=2)
+    srv.submit(js[0])
+    for _ in range(3):
+        srv.pump()
+    for j in js[1:]:
+        srv.submit(j)
+        srv.pump()
+    while not srv.idle():
+        srv.pump()
+    srv.close()
+    assert len(srv.finished) == len(js)
+    for j in js:
+        assert j.done_steps == j.nsteps and len(j.step_ms) == j.nsteps
+        x, v = alone(j, hobak.PRECISION_MIXED)
+        assert np.array_equal(j.result_x, x) and np.array_equal(j.result_v, v), j.id
