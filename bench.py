@@ -349,6 +349,9 @@ def run_ours(args, spec, scene_list):
     opts = hobak.solver_opts(precision=spec["precision"], use_graph=not args.eager)
     batch = hobak.BATCH(scene_list, opts)
     stream = torch.cuda.ExternalStream(batch.stream_handle())
+    # launch shapes (tile size, CTA sizes, PCG chunk) from the autotuner, on
+    # this batch's data, before the warm-up; the state is left unchanged
+    tuning = batch.get_tuning() if args.no_autotune else batch.autotune(reps=3)
 
     # ---- device-resident timed region ----
     batch.step(args.warmup)
@@ -452,7 +455,8 @@ def run_ours(args, spec, scene_list):
                 "p50_ms": float(np.percentile(lat_sorted, 50)), "p99_ms": float(np.percentile(lat_sorted, 99)),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if spec["precision"] == 0 else "f32+f64", "data": "synthetic",
-                "config": {"workload": args.workload, **config_of(spec, scene_list)},
+                "config": {"workload": args.workload, **config_of(spec, scene_list),
+                           "launch_shapes": {**tuning, "chosen_by": "given" if args.no_autotune else "autotuner"}},
                 "pcg_iters_per_step": float(np.mean(iters)),
                 "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
                 "roofline": roofline, "cpu_baseline": cpu, "plain_fp64_gpu": plain, "e2e": e2e,
@@ -473,6 +477,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the unbatched FP64 comparison on mixes")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--eager", action="store_true",
                     help="launch kernels one by one instead of the step graph (for per-kernel profilers)")
     args = ap.parse_args()

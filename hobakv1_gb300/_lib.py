@@ -31,6 +31,11 @@ class HobakSolverOpts(ctypes.Structure):
                 ("use_graph", ctypes.c_int)]
 
 
+class HobakTuning(ctypes.Structure):
+    _fields_ = [("tile_vertices", ctypes.c_int), ("element_threads", ctypes.c_int),
+                ("assembly_threads", ctypes.c_int), ("pcg_chunk", ctypes.c_int), ("step_ms", ctypes.c_double)]
+
+
 class HobakStepStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int),
                 ("rel_residual", ctypes.c_double), ("refinements", ctypes.c_int)]
@@ -73,6 +78,9 @@ SIGNATURES = {
     "hobak_batch_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "hobak_batch_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "hobak_batch_kernel_bytes": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "hobak_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakTuning)]),
+    "hobak_batch_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakTuning)]),
+    "hobak_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(HobakTuning)]),
     "hobak_batch_set_collisions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                   ctypes.c_double, ctypes.c_double]),
     "hobak_batch_collision_pairs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, _ip,

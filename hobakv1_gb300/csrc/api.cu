@@ -81,6 +81,9 @@ struct hobak_batch_t {
   cudaStream_t captureStream = nullptr;  // fills the bodies of captured while loops
   cudaGraphExec_t stepGraph[2] = {nullptr, nullptr};  // untimed, timed
   long long eagerChunks = 0;
+  long long loopLaunchBase = 0;  // loop-body launches folded in before the last chunk change
+  int chunk = 8;                 // PCG iterations per loop body (graph) or per host poll (eager)
+  int ntilesCap = 0;             // tile tables are sized for the smallest tile size
   int lastStatus = HOBAK_OK;
   std::vector<SolveState> lastSolve;
   std::vector<int> hostRowptr, hostCols;
@@ -103,7 +106,6 @@ struct hobak_batch_t {
 
 namespace {
 
-constexpr int kChunk = 8;  // PCG iterations per loop body (graph) or per host poll (eager)
 
 double tet_volume(const double* x0, const double* x1, const double* x2, const double* x3) {
   const double d1[3] = {x1[0] - x0[0], x1[1] - x0[1], x1[2] - x0[2]};
@@ -304,9 +306,12 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     for (int t = 0; t < nt; t++)
       for (int e = 0; e < 16; e++) blksrc[fill[where[16 * (size_t)t + e]]++] = 16 * t + e;
   }
-  // tiles: kTileV consecutive vertices of one scene
+  // tiles: kTileV consecutive vertices of one scene (apply_tile_size changes
+  // the size later; the tables are sized for kMinTileV)
+  int ntilesCap = 0;
   for (int s = 0; s < n; s++) {
     SceneHost& H = B->scenes[s];
+    ntilesCap += (H.nv + kMinTileV - 1) / kMinTileV;
     H.tile0 = (int)tileScene.size();
     for (int u = 0; u < H.nv; u += kTileV) {
       tileScene.push_back(s);
@@ -333,6 +338,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   }
   const int ntiles = (int)tileScene.size();
   B->ntiles = ntiles;
+  B->ntilesCap = ntilesCap;
 
   // ---- device arena ----
   Arena A;
@@ -353,8 +359,8 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oBlkRow = A.reserve(sizeof(int) * nblocks), oBlkptr = A.reserve(sizeof(int) * (nblocks + 1));
   const size_t oBlksrc = A.reserve(sizeof(int) * 16 * (size_t)nt);
   const size_t oVtxptr = A.reserve(sizeof(int) * (nv + 1)), oVtxinc = A.reserve(sizeof(int) * 4 * (size_t)nt);
-  const size_t oTileS = A.reserve(sizeof(int) * ntiles), oTile0 = A.reserve(sizeof(int) * ntiles);
-  const size_t oTile1 = A.reserve(sizeof(int) * ntiles);
+  const size_t oTileS = A.reserve(sizeof(int) * ntilesCap), oTile0 = A.reserve(sizeof(int) * ntilesCap);
+  const size_t oTile1 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oEH = A.reserve(sizeof(double) * kElemHess * (size_t)nt);
   const size_t oEHf = A.reserve(sizeof(float) * kElemHess * (size_t)nt);
   const size_t oEG = A.reserve(sizeof(double) * 12 * (size_t)nt);
@@ -369,7 +375,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oMinvF = A.reserve(sizeof(float) * 9 * (size_t)nv);
   const size_t oRF = A.reserve(F3), oUF = A.reserve(F3), oPF = A.reserve(F3), oSF = A.reserve(F3);
   const size_t oWF = A.reserve(F3), oDF = A.reserve(F3);
-  const size_t oPart = A.reserve(sizeof(double) * kPartials * (size_t)ntiles);
+  const size_t oPart = A.reserve(sizeof(double) * kPartials * (size_t)ntilesCap);
   const size_t oPsi = A.reserve(sizeof(double) * nt);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, A.used);
@@ -386,6 +392,9 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.nt = nt;
   d.nblocks = nblocks;
   d.ntiles = ntiles;
+  d.tileV = kTileV;
+  d.elemThreads = 128;
+  d.asmThreads = 256;
   d.scenes = carve<SceneParams>(base, oScenes);
   d.solve = carve<SolveState>(base, oSolve);
   d.active = carve<int>(base, oActive);
@@ -496,10 +505,10 @@ long long fixed_launches(const hobak_batch_t* B) {
   return 6 + sweeps * (2 + (mixed ? 2 : 0));
 }
 
-// One PCG chunk: kChunk iterations (2 kernels each).
+// One PCG chunk: `chunk` iterations (2 kernels each).
 template <typename T>
-void enqueue_chunk(const DeviceBatch& d, const PcgVecs<T>& v, cudaStream_t s) {
-  for (int c = 0; c < kChunk; c++) launch_pcg_iteration<T>(d, v, s);
+void enqueue_chunk(const DeviceBatch& d, const PcgVecs<T>& v, cudaStream_t s, int chunk) {
+  for (int c = 0; c < chunk; c++) launch_pcg_iteration<T>(d, v, s);
 }
 
 // While-loop node on the capturing stream `s`: body = one chunk followed by
@@ -525,7 +534,7 @@ int capture_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
   CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
   CUDA_TRY(cudaStreamBeginCaptureToGraph(B->captureStream, body, nullptr, nullptr, 0,
                                          cudaStreamCaptureModeThreadLocal));
-  enqueue_chunk<T>(B->d, v, B->captureStream);
+  enqueue_chunk<T>(B->d, v, B->captureStream, B->chunk);
   launch_continue(B->d, (unsigned long long)h, B->captureStream);
   cudaGraph_t out = nullptr;
   CUDA_TRY(cudaStreamEndCapture(B->captureStream, &out));
@@ -535,11 +544,11 @@ int capture_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
 // Eager loop: chunks until the device reports no running scene (host polls).
 template <typename T>
 int eager_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
-  for (int iters = 0; iters <= B->opts.max_iters; iters += kChunk) {
+  for (int iters = 0; iters <= B->opts.max_iters; iters += B->chunk) {
     CUDA_TRY(cudaMemcpyAsync(B->pinnedActive, B->d.active, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     if (*B->pinnedActive <= 0) break;
-    enqueue_chunk<T>(B->d, v, s);
+    enqueue_chunk<T>(B->d, v, s, B->chunk);
     B->eagerChunks++;
   }
   return HOBAK_OK;
@@ -829,7 +838,53 @@ int run_steps(hobak_batch_t* B, int nsteps) {
 int count_loop_launches(hobak_batch_t* B, long long* out) {
   unsigned long long runs = 0;
   CUDA_TRY(cudaMemcpy(&runs, B->d.bodyRuns, sizeof(runs), cudaMemcpyDeviceToHost));
-  *out = (long long)(runs * (2ull * kChunk + 1ull)) + B->eagerChunks * 2LL * kChunk;
+  *out = B->loopLaunchBase + (long long)(runs * (2ull * B->chunk + 1ull)) + B->eagerChunks * 2LL * B->chunk;
+  return HOBAK_OK;
+}
+
+// Before the chunk size changes: fold the loop launches counted so far into
+// the base and restart the counters.
+int fold_loop_launches(hobak_batch_t* B) {
+  long long n = 0;
+  int rc = count_loop_launches(B, &n);
+  if (rc) return rc;
+  B->loopLaunchBase = n;
+  B->eagerChunks = 0;
+  CUDA_TRY(cudaMemset(B->d.bodyRuns, 0, sizeof(unsigned long long)));
+  return HOBAK_OK;
+}
+
+// Tiles of TV consecutive vertices of one scene (one PCG CTA each): host
+// tables, scene ranges, device upload.  Graphs are dropped (they hold the
+// launch shapes).
+int apply_tile_size(hobak_batch_t* B, int TV) {
+  if (TV != 64 && TV != 128) return fail(HOBAK_ERR_INVALID, "tile size must be 64 or 128 vertices");
+  std::vector<int> tileScene, tileV0, tileV1;
+  for (int s = 0; s < (int)B->scenes.size(); s++) {
+    SceneHost& H = B->scenes[s];
+    H.tile0 = (int)tileScene.size();
+    for (int u = 0; u < H.nv; u += TV) {
+      tileScene.push_back(s);
+      tileV0.push_back(H.v0 + u);
+      tileV1.push_back(H.v0 + std::min(H.nv, u + TV));
+    }
+    H.ntiles = (int)tileScene.size() - H.tile0;
+    B->sceneParams[s].tile0 = H.tile0;
+    B->sceneParams[s].ntiles = H.ntiles;
+  }
+  const int ntiles = (int)tileScene.size();
+  if (ntiles > B->ntilesCap) return fail(HOBAK_ERR_INVALID, "tile tables too small");
+  DeviceBatch& d = B->d;
+  CUDA_TRY(cudaStreamSynchronize(B->stream));
+  CUDA_TRY(cudaMemcpy(const_cast<SceneParams*>(d.scenes), B->sceneParams.data(),
+                      sizeof(SceneParams) * B->sceneParams.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(const_cast<int*>(d.tileScene), tileScene.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(const_cast<int*>(d.tileV0), tileV0.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(const_cast<int*>(d.tileV1), tileV1.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice));
+  d.ntiles = ntiles;
+  d.tileV = TV;
+  B->ntiles = ntiles;
+  drop_graphs(B);
   return HOBAK_OK;
 }
 
@@ -1219,6 +1274,167 @@ int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
   b->launches += 4LL * reps;
   CUDA_TRY(cudaGetLastError());
   return upload_solver_opts(b);
+}
+
+int hobak_batch_get_tuning(hobak_batch b, hobak_tuning* out) {
+  if (!b || !out) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  out->tile_vertices = b->d.tileV;
+  out->element_threads = b->d.elemThreads;
+  out->assembly_threads = b->d.asmThreads;
+  out->pcg_chunk = b->chunk;
+  out->step_ms = 0.0;
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t) {
+  if (!b || !t) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  if (t->element_threads != 64 && t->element_threads != 128)
+    return fail(HOBAK_ERR_INVALID, "element_threads must be 64 or 128");
+  if (t->assembly_threads < 64 || t->assembly_threads > 1024 || t->assembly_threads % 32 != 0)
+    return fail(HOBAK_ERR_INVALID, "assembly_threads must be a multiple of 32 in 64..1024");
+  if (t->pcg_chunk < 1 || t->pcg_chunk > 64) return fail(HOBAK_ERR_INVALID, "pcg_chunk must be in 1..64");
+  if (t->tile_vertices != 64 && t->tile_vertices != 128)
+    return fail(HOBAK_ERR_INVALID, "tile_vertices must be 64 or 128");
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (t->tile_vertices != b->d.tileV) {
+    const int rc = apply_tile_size(b, t->tile_vertices);
+    if (rc) return rc;
+  }
+  if (t->pcg_chunk != b->chunk) {
+    const int rc = fold_loop_launches(b);
+    if (rc) return rc;
+    b->chunk = t->pcg_chunk;
+  }
+  b->d.elemThreads = t->element_threads;
+  b->d.asmThreads = t->assembly_threads;
+  drop_graphs(b);
+  return HOBAK_OK;
+}
+
+namespace {
+struct DeviceScratch {
+  void* p = nullptr;
+  ~DeviceScratch() {
+    if (p) cudaFree(p);
+  }
+};
+struct EventPair {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ~EventPair() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+};
+}  // namespace
+
+int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out) {
+  if (!b || reps <= 0) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  DeviceBatch& d = b->d;
+  cudaStream_t s = b->stream;
+  const bool mixed = b->opts.precision == HOBAK_PRECISION_MIXED;
+  const size_t vbytes = 3 * sizeof(double) * (size_t)b->nv;
+  CUDA_TRY(cudaStreamSynchronize(s));
+  DeviceScratch saved;
+  CUDA_TRY(cudaMalloc(&saved.p, 2 * vbytes));
+  double* x0 = static_cast<double*>(saved.p);
+  double* v0 = x0 + 3 * (size_t)b->nv;
+  CUDA_TRY(cudaMemcpyAsync(x0, d.x, vbytes, cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(v0, d.v, vbytes, cudaMemcpyDeviceToDevice, s));
+  auto restore = [&]() -> int {
+    CUDA_TRY(cudaMemcpyAsync(d.x, x0, vbytes, cudaMemcpyDeviceToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.v, v0, vbytes, cudaMemcpyDeviceToDevice, s));
+    return HOBAK_OK;
+  };
+  EventPair ev;
+  CUDA_TRY(cudaEventCreate(&ev.e0));
+  CUDA_TRY(cudaEventCreate(&ev.e1));
+  auto elapsed = [&](float* ms) -> int {
+    CUDA_TRY(cudaEventSynchronize(ev.e1));
+    CUDA_TRY(cudaEventElapsedTime(ms, ev.e0, ev.e1));
+    return HOBAK_OK;
+  };
+  hobak_tuning best{};
+  hobak_batch_get_tuning(b, &best);
+  // 1. element kernel CTA size (inputs are the saved state; outputs are
+  //    recomputed by every step)
+  {
+    float bestMs = 3.4e38f;
+    for (int et : {64, 128}) {
+      d.elemThreads = et;
+      CUDA_TRY(cudaEventRecord(ev.e0, s));
+      for (int r = 0; r < reps; r++) {
+        if (mixed) launch_element_mixed(d, s);
+        else launch_element(d, s);
+      }
+      CUDA_TRY(cudaEventRecord(ev.e1, s));
+      float ms = 0;
+      int rc = elapsed(&ms);
+      if (rc) return rc;
+      b->launches += reps;
+      if (ms < bestMs) {
+        bestMs = ms;
+        best.element_threads = et;
+      }
+    }
+    d.elemThreads = best.element_threads;
+  }
+  // 2. assembly kernel CTA size
+  {
+    float bestMs = 3.4e38f;
+    for (int at : {128, 256, 512}) {
+      d.asmThreads = at;
+      CUDA_TRY(cudaEventRecord(ev.e0, s));
+      for (int r = 0; r < reps; r++) {
+        if (mixed) launch_assemble<float>(d, d.v32, s);
+        else launch_assemble<double>(d, d.v64, s);
+      }
+      CUDA_TRY(cudaEventRecord(ev.e1, s));
+      float ms = 0;
+      int rc = elapsed(&ms);
+      if (rc) return rc;
+      b->launches += reps;
+      if (ms < bestMs) {
+        bestMs = ms;
+        best.assembly_threads = at;
+      }
+    }
+    d.asmThreads = best.assembly_threads;
+  }
+  // 3. whole steps per (tile size, chunk), each from the saved state
+  double bestStep = 1e300;
+  hobak_tuning trial = best;
+  for (int tv : {64, 128})
+    for (int ch : {4, 8, 16}) {
+      trial.tile_vertices = tv;
+      trial.pcg_chunk = ch;
+      int rc = hobak_batch_set_tuning(b, &trial);
+      if (rc) return rc;
+      if ((rc = restore())) return rc;
+      if ((rc = run_steps(b, 1))) return rc;  // builds this shape's graph
+      double total = 0.0;
+      for (int r = 0; r < reps; r++) {
+        if ((rc = restore())) return rc;
+        CUDA_TRY(cudaEventRecord(ev.e0, s));
+        if ((rc = run_steps(b, 1))) return rc;
+        CUDA_TRY(cudaEventRecord(ev.e1, s));
+        float ms = 0;
+        if ((rc = elapsed(&ms))) return rc;
+        total += ms;
+      }
+      if (total < bestStep) {
+        bestStep = total;
+        best.tile_vertices = tv;
+        best.pcg_chunk = ch;
+      }
+    }
+  best.step_ms = bestStep / reps;
+  int rc = hobak_batch_set_tuning(b, &best);
+  if (rc) return rc;
+  if ((rc = restore())) return rc;
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if ((rc = upload_solver_opts(b))) return rc;
+  if (out) *out = best;
+  return HOBAK_OK;
 }
 
 int hobak_batch_kernel_bytes(hobak_batch b, double* bytes) {

@@ -20,7 +20,9 @@ namespace hobak {
 
 enum MaterialKind : int { MAT_SNH = 0, MAT_ARAP = 1, MAT_STVK = 2, MAT_LINEAR = 3, MAT_NHBW = 4, MAT_SNHB = 5 };
 
-constexpr int kTileV = 128;       // vertices per PCG tile (one CTA)
+constexpr int kTileV = 128;       // default vertices per PCG tile (one CTA)
+constexpr int kMinTileV = 64;     // smallest tile size; tile tables are sized for it
+//       // vertices per PCG tile (one CTA)
 constexpr int kElemHess = 90;     // 10 upper blocks x 9
 constexpr int kPartials = 4;      // per-tile partial sums slots
 

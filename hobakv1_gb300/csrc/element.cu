@@ -339,14 +339,18 @@ __global__ void k_energy(DeviceBatch b) {
 
 }  // namespace
 
+// CTA size: the batch's autotuned elemThreads (64 or 128; the kernels are
+// bounded for 128).
 void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces) {
   if (b.nt == 0) return;
-  k_element<double><<<(b.nt + 127) / 128, 128, 0, s>>>(b, rawForces, b.elemH);
+  const int nt = b.elemThreads;
+  k_element<double><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, rawForces, b.elemH);
 }
 
 void launch_element_mixed(const DeviceBatch& b, cudaStream_t s) {
   if (b.nt == 0) return;
-  k_element<float><<<(b.nt + 127) / 128, 128, 0, s>>>(b, 0, b.elemHf);
+  const int nt = b.elemThreads;
+  k_element<float><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, 0, b.elemHf);
 }
 
 void launch_energy(const DeviceBatch& b, cudaStream_t s) {

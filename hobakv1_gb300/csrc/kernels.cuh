@@ -23,6 +23,9 @@ struct PcgVecs {
 // Device pointers of one packed batch.  Plain struct passed by value.
 struct DeviceBatch {
   int nscenes, nv, nt, nblocks, ntiles;
+  // launch shapes (hobak_batch_autotune): vertices per PCG tile (64 or 128),
+  // element-kernel CTA size (64 or 128), assembly CTA size
+  int tileV, elemThreads, asmThreads;
   const SceneParams* scenes;
   SolveState* solve;
   int* active;  // scenes whose inner PCG is still running

@@ -37,8 +37,10 @@ namespace hobak {
 
 namespace {
 
-constexpr int kVecThreads = kTileV;       // vector kernels: one thread per vertex
-constexpr int kSpmvThreads = 3 * kTileV;  // SpMV: one thread per scalar row
+// Tile kernels are instantiated for every supported tile size TV (vertices
+// per tile): vector kernels run one thread per vertex (TV threads), the SpMV,
+// update and residual one thread per scalar row (3 TV threads).  The batch's
+// tile size is an autotuned launch shape (DeviceBatch::tileV).
 
 // Fixed-order sum over the CTA; result valid in thread 0.  NT multiple of 32.
 // The warp tree runs in R (FP32 for the inner solve of the mixed path, which
@@ -229,8 +231,9 @@ __global__ void k_diag_inverse(DeviceBatch b, const T* __restrict__ lhs, T* __re
 // rhs = S dt (sum_e g_e + f_ext) per vertex (element g already carries
 // dt (f + dt He v)); y = 0; r64 = rhs.  Per scene: |rhs|^2 and the FP64
 // stopping threshold; an all-zero right-hand side finishes the solve (x = 0).
-__global__ void __launch_bounds__(kVecThreads) k_rhs(DeviceBatch b) {
-  __shared__ double sh[kVecThreads / 32];
+template <int TV>
+__global__ void __launch_bounds__(TV) k_rhs(DeviceBatch b) {
+  __shared__ double sh[TV / 32];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
@@ -285,12 +288,12 @@ __global__ void __launch_bounds__(kVecThreads) k_rhs(DeviceBatch b) {
       rr += ri * ri;
     }
   }
-  const double t = block_sum<kVecThreads>(rr, sh);
+  const double t = block_sum<TV>(rr, sh);
   if (threadIdx.x == 0) b.partial[kPartials * tile] = t;
   SolveState& st = b.solve[s];
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketB, sp.ntiles, &flag)) return;
-  const double srr = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 0, sh);
+  const double srr = sum_partials<TV>(b.partial, sp.tile0, sp.ntiles, 0, sh);
   if (threadIdx.x == 0) {
     st.rhsNorm2 = srr;
     st.threshold = fmax(st.tol * st.tol * srr, DBL_MIN);
@@ -316,9 +319,9 @@ __global__ void k_set_active(DeviceBatch b) {
 // Start of one inner solve on r_T = (T) r64: d = 0, p = s = 0, u = Minv r,
 // gamma = (r, u), |r|^2.  Inner tolerance: the outer one for FP64; for FP32
 // the relative reduction still needed, floored at 1e-5 (FP32 stagnation).
-template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_inner_init(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[kVecThreads / 32];
+template <int TV, typename T>
+__global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[TV / 32];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
@@ -353,15 +356,15 @@ __global__ void __launch_bounds__(kVecThreads) k_inner_init(DeviceBatch b, PcgVe
       ru += r3[i] * ui;
     }
   }
-  const double trr = block_sum<kVecThreads>(rr, sh);
-  const double tru = block_sum<kVecThreads>(ru, sh);
+  const double trr = block_sum<TV>(rr, sh);
+  const double tru = block_sum<TV>(ru, sh);
   if (threadIdx.x == 0) {
     b.partial[kPartials * tile] = trr;
     b.partial[kPartials * tile + 1] = tru;
   }
   if (!last_tile(&st.ticketB, sp.ntiles, &flag)) return;
-  const double srr = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 0, sh);
-  const double sru = sum_partials<kVecThreads>(b.partial, sp.tile0, sp.ntiles, 1, sh);
+  const double srr = sum_partials<TV>(b.partial, sp.tile0, sp.ntiles, 0, sh);
+  const double sru = sum_partials<TV>(b.partial, sp.tile0, sp.ntiles, 1, sh);
   if (threadIdx.x == 0) {
     double itol = st.tol;
     if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr, DBL_MIN)), 1e-5);
@@ -413,9 +416,9 @@ __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int
 
 // w = A u, one thread per scalar row (9 DFMA per block in FP64), and
 // delta = (w, u); the scene's last CTA forms beta and alpha.
-template <typename T>
-__global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[kSpmvThreads / 32];
+template <int TV, typename T>
+__global__ void __launch_bounds__(3 * TV) k_spmv(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[3 * TV / 32];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
@@ -459,11 +462,11 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T>
     v.w[row] = acc;
     dl = acc * uu[row];
   }
-  const double t = block_sum<kSpmvThreads>(dl, sh);
+  const double t = block_sum<3 * TV>(dl, sh);
   if (threadIdx.x == 0) b.partial[kPartials * tile + 2] = t;
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketA, sp.ntiles, &flag)) return;
-  const double delta = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 2, sh);
+  const double delta = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 2, sh);
   if (threadIdx.x == 0) {
     st.delta = delta;
     if (st.iters == 0) {
@@ -479,13 +482,13 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(DeviceBatch b, PcgVecs<T>
 
 // p = u + beta p; s = w + beta s; d += alpha p; r -= alpha s; u = Minv r;
 // gamma' = (r, u); |r|^2 -> stop when |r|^2 < threshold (ConjugateGradient.h:75-78).
-template <typename T>
+template <int TV, typename T>
 // One thread per scalar row (three times the threads of a per-vertex loop,
 // which a 40^3 scene needs to cover the GPU's latency); the 3x3 block of
 // Minv reads its vertex's three new residual rows from shared memory.
-__global__ void __launch_bounds__(kSpmvThreads, 5) k_update(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[2 * kSpmvThreads / 32];
-  __shared__ T rsh[kSpmvThreads];
+__global__ void __launch_bounds__(3 * TV, 640 / TV) k_update(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[2 * 3 * TV / 32];
+  __shared__ T rsh[3 * TV];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
@@ -522,15 +525,15 @@ __global__ void __launch_bounds__(kSpmvThreads, 5) k_update(DeviceBatch b, PcgVe
     ru = rnew * ui;
   }
   double trr, tru;
-  block_sum2<kSpmvThreads>(rr, ru, sh, trr, tru);
+  block_sum2<3 * TV>(rr, ru, sh, trr, tru);
   if (threadIdx.x == 0) {
     b.partial[kPartials * tile] = trr;
     b.partial[kPartials * tile + 1] = tru;
   }
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketB, sp.ntiles, &flag)) return;
-  const double srr = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 0, sh);
-  const double sru = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 1, sh);
+  const double srr = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 0, sh);
+  const double sru = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 1, sh);
   if (threadIdx.x == 0) {
     st.rr = srr;
     st.iters += 1;
@@ -573,8 +576,9 @@ __global__ void k_accumulate(DeviceBatch b) {
 
 // Mixed precision: r64 = rhs - A y in FP64 (FP32 matrix entries promoted),
 // |r64|^2, then the outer test: converged, out of sweeps, or refine again.
-__global__ void __launch_bounds__(kSpmvThreads) k_residual(DeviceBatch b) {
-  __shared__ double sh[kSpmvThreads / 32];
+template <int TV>
+__global__ void __launch_bounds__(3 * TV) k_residual(DeviceBatch b) {
+  __shared__ double sh[3 * TV / 32];
   __shared__ int flag;
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
@@ -596,11 +600,11 @@ __global__ void __launch_bounds__(kSpmvThreads) k_residual(DeviceBatch b) {
     b.r64[row] = ri;
     rr = ri * ri;
   }
-  const double t = block_sum<kSpmvThreads>(rr, sh);
+  const double t = block_sum<3 * TV>(rr, sh);
   if (threadIdx.x == 0) b.partial[kPartials * tile + 3] = t;
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketA, sp.ntiles, &flag)) return;
-  const double srr = sum_partials<kSpmvThreads>(b.partial, sp.tile0, sp.ntiles, 3, sh);
+  const double srr = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 3, sh);
   if (threadIdx.x == 0) {
     st.rr64 = srr;
     st.sweep += 1;
@@ -649,9 +653,9 @@ template <typename T>
 void launch_assemble(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
   const long n = 9L * b.nblocks;
   if (sizeof(T) == sizeof(double))
-    k_assemble<double, T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, b.elemH, v.lhs);
+    k_assemble<double, T><<<(unsigned)((n + b.asmThreads - 1) / b.asmThreads), b.asmThreads, 0, s>>>(b, b.elemH, v.lhs);
   else
-    k_assemble<float, T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, b.elemHf, v.lhs);
+    k_assemble<float, T><<<(unsigned)((n + b.asmThreads - 1) / b.asmThreads), b.asmThreads, 0, s>>>(b, b.elemHf, v.lhs);
 }
 
 void launch_assemble_raw(const DeviceBatch& b, double* K, double* R, cudaStream_t s) {
@@ -664,28 +668,38 @@ void launch_diag_inverse(const DeviceBatch& b, const PcgVecs<T>& v, int precond,
   k_diag_inverse<T><<<(b.nv + 255) / 256, 256, 0, s>>>(b, v.lhs, v.minv, precond);
 }
 
-void launch_rhs(const DeviceBatch& b, cudaStream_t s) { k_rhs<<<b.ntiles, kVecThreads, 0, s>>>(b); }
+// Tile-kernel launches dispatch on the batch's tile size.
+#define HOBAK_TILE_LAUNCH(KERNEL, THREADS_PER_V, ...)                                   \
+  do {                                                                                  \
+    if (b.tileV == 64) KERNEL<64><<<b.ntiles, (THREADS_PER_V) * 64, 0, s>>>(__VA_ARGS__);     \
+    else KERNEL<128><<<b.ntiles, (THREADS_PER_V) * 128, 0, s>>>(__VA_ARGS__);                 \
+  } while (0)
+
+void launch_rhs(const DeviceBatch& b, cudaStream_t s) { HOBAK_TILE_LAUNCH(k_rhs, 1, b); }
 
 void launch_set_active(const DeviceBatch& b, cudaStream_t s) { k_set_active<<<1, 32, 0, s>>>(b); }
 
 template <typename T>
 void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
-  k_inner_init<T><<<b.ntiles, kVecThreads, 0, s>>>(b, v);
+  if (b.tileV == 64) k_inner_init<64, T><<<b.ntiles, 64, 0, s>>>(b, v);
+  else k_inner_init<128, T><<<b.ntiles, 128, 0, s>>>(b, v);
 }
 
 template <typename T>
 void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
-  k_spmv<T><<<b.ntiles, kSpmvThreads, 0, s>>>(b, v);
+  if (b.tileV == 64) k_spmv<64, T><<<b.ntiles, 3 * 64, 0, s>>>(b, v);
+  else k_spmv<128, T><<<b.ntiles, 3 * 128, 0, s>>>(b, v);
 }
 
 template <typename T>
 void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
-  k_update<T><<<b.ntiles, kSpmvThreads, 0, s>>>(b, v);
+  if (b.tileV == 64) k_update<64, T><<<b.ntiles, 3 * 64, 0, s>>>(b, v);
+  else k_update<128, T><<<b.ntiles, 3 * 128, 0, s>>>(b, v);
 }
 
 void launch_refine(const DeviceBatch& b, cudaStream_t s) {
-  k_accumulate<<<b.ntiles, kVecThreads, 0, s>>>(b);
-  k_residual<<<b.ntiles, kSpmvThreads, 0, s>>>(b);
+  k_accumulate<<<b.ntiles, b.tileV, 0, s>>>(b);
+  HOBAK_TILE_LAUNCH(k_residual, 3, b);
 }
 
 void launch_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s) {

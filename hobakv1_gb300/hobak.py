@@ -358,6 +358,27 @@ class BATCH:
         check(_lib.load().hobak_batch_kernel_bytes(self.h, dptr(b)), "hobak_batch_kernel_bytes")
         return dict(zip(self.KERNELS, b.tolist()))
 
+    TUNING = ("tile_vertices", "element_threads", "assembly_threads", "pcg_chunk", "step_ms")
+
+    def get_tuning(self) -> dict:
+        """Launch shapes: tile size, element / assembly CTA sizes, PCG chunk."""
+        t = _lib.HobakTuning()
+        check(_lib.load().hobak_batch_get_tuning(self.h, ctypes.byref(t)), "hobak_batch_get_tuning")
+        return {k: getattr(t, k) for k in self.TUNING}
+
+    def set_tuning(self, **kw):
+        cur = self.get_tuning()
+        cur.update(kw)
+        t = _lib.HobakTuning(*[cur[k] for k in self.TUNING])
+        check(_lib.load().hobak_batch_set_tuning(self.h, ctypes.byref(t)), "hobak_batch_set_tuning")
+
+    def autotune(self, reps: int = 3) -> dict:
+        """Time candidate launch shapes on this batch and keep the fastest
+        (state restored afterwards; the trajectory is unchanged)."""
+        t = _lib.HobakTuning()
+        check(_lib.load().hobak_batch_autotune(self.h, reps, ctypes.byref(t)), "hobak_batch_autotune")
+        return {k: getattr(t, k) for k in self.TUNING}
+
     def close(self):
         if getattr(self, "h", None) and self.h.value:
             _lib.load().hobak_batch_destroy(self.h)
