@@ -67,6 +67,10 @@ SIGNATURES = {
     "hobak_gpu_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(HobakStepStats)]),
     "hobak_gpu_set_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     "hobak_gpu_get_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    "hobak_gpu_set_external_forces": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "hobak_gpu_set_collisions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_double]),
+    "hobak_gpu_set_solver": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakSolverOpts)]),
     "hobak_gpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "hobak_material_eval": (ctypes.c_int, [ctypes.POINTER(HobakMaterial), ctypes.c_int, _dp, _dp, _dp, _dp]),
     "hobak_element_eval": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp,

@@ -1458,6 +1458,11 @@ int hobak_gpu_create(const hobak_scene_desc* scene, const hobak_solver_opts* opt
 int hobak_gpu_step(hobak_batch b, int nsteps, hobak_step_stats* stats) { return hobak_batch_step(b, nsteps, stats); }
 int hobak_gpu_set_state(hobak_batch b, const double* x, const double* v) { return hobak_batch_set_state(b, 0, x, v); }
 int hobak_gpu_get_state(hobak_batch b, double* x, double* v) { return hobak_batch_get_state(b, 0, x, v); }
+int hobak_gpu_set_external_forces(hobak_batch b, const double* f) { return hobak_batch_set_external_forces(b, 0, f); }
+int hobak_gpu_set_collisions(hobak_batch b, int vf_on, double eps, double stiffness, double damping_beta) {
+  return hobak_batch_set_collisions(b, 0, vf_on, eps, stiffness, damping_beta);
+}
+int hobak_gpu_set_solver(hobak_batch b, const hobak_solver_opts* opts) { return hobak_batch_set_solver(b, opts); }
 int hobak_gpu_destroy(hobak_batch b) { return hobak_batch_destroy(b); }
 
 int hobak_material_eval(const hobak_material* m, int n, const double* F, double* psi, double* P, double* H) {

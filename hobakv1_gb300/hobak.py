@@ -414,8 +414,46 @@ class BACKWARD_EULER_VELOCITY:
         self._batch: Optional[BATCH] = None
         self._currentTimestep = 0
         self._lastStats = None
+        # contact flags (TIMESTEPPER.cpp:83-86 defaults; edge-edge is not built)
+        self._vertexFaceSelfCollisionsOn = False
+        self._collisionStiffness = 1.0
+        self._collisionDampingBeta = 0.001
+        self._collisionEps = 0.01  # TET_MESH's default collision distance
 
     # ---- reference accessors ----
+    def vertexFaceSelfCollisionsOn(self) -> bool:
+        return self._vertexFaceSelfCollisionsOn
+
+    def setVertexFaceSelfCollisionsOn(self, on: bool):
+        self._vertexFaceSelfCollisionsOn = bool(on)
+        self._push_collisions()
+
+    def collisionStiffness(self) -> float:
+        return self._collisionStiffness
+
+    def setCollisionStiffness(self, mu: float):
+        self._collisionStiffness = float(mu)
+        self._push_collisions()
+
+    def collisionDampingBeta(self) -> float:
+        return self._collisionDampingBeta
+
+    def setCollisionDampingBeta(self, beta: float):
+        self._collisionDampingBeta = float(beta)
+        self._push_collisions()
+
+    def setCollisionEps(self, eps: float):
+        """TET_MESH::setCollisionEps (TET_MESH.cpp:2160-2165)."""
+        self._collisionEps = float(eps)
+        self._push_collisions()
+
+    def _push_collisions(self):
+        if self._batch is None:
+            return
+        check(_lib.load().hobak_gpu_set_collisions(self._batch.h, int(self._vertexFaceSelfCollisionsOn),
+                                                   self._collisionEps, self._collisionStiffness,
+                                                   self._collisionDampingBeta), "hobak_gpu_set_collisions")
+
     def position(self):
         return self._position
 
@@ -471,13 +509,16 @@ class BACKWARD_EULER_VELOCITY:
         s.pinned = np.array(sorted(set(self._pinned)), dtype=np.int32)
         s.x0, s.v0 = self._position, self._velocity
         self._batch = BATCH([s], self._opts)
+        if self._vertexFaceSelfCollisionsOn:
+            self._push_collisions()
 
     def solve(self, verbose: bool = False) -> bool:
         if self._batch is None:
             self._build()
         b = self._batch
         b.set_state(0, self._position, self._velocity)
-        b.set_external_forces(0, self._externalForces)
+        check(_lib.load().hobak_gpu_set_external_forces(b.h, dptr(np.ascontiguousarray(self._externalForces))),
+              "hobak_gpu_set_external_forces")
         stats = b.step(1)
         x, v = b.get_state(0)
         self._position[:] = x

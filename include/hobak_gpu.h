@@ -175,6 +175,14 @@ int hobak_gpu_create(const hobak_scene_desc* scene, const hobak_solver_opts* opt
 int hobak_gpu_step(hobak_batch b, int nsteps, hobak_step_stats* stats);
 int hobak_gpu_set_state(hobak_batch b, const double* x, const double* v);
 int hobak_gpu_get_state(hobak_batch b, double* x, double* v);
+/* TIMESTEPPER::externalForces() (TIMESTEPPER.h:58), 3*nv doubles. */
+int hobak_gpu_set_external_forces(hobak_batch b, const double* f);
+/* vertexFaceSelfCollisionsOn(), TET_MESH::setCollisionEps, collisionStiffness(),
+ * collisionDampingBeta() (TIMESTEPPER.h:62-69; TET_MESH.cpp:2160-2174). */
+int hobak_gpu_set_collisions(hobak_batch b, int vf_on, double eps, double stiffness, double damping_beta);
+/* _cgSolver.setTolerance / setMaxIterations (IterativeSolverBase.h:281-284,
+ * 363) plus precision and preconditioner. */
+int hobak_gpu_set_solver(hobak_batch b, const hobak_solver_opts* opts);
 int hobak_gpu_destroy(hobak_batch b);
 
 /* ---- element-level entry points (the VOLUME::HYPERELASTIC boundary) ----

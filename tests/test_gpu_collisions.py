@@ -83,3 +83,27 @@ def test_per_pair_force_and_hessian_match_oracle(N):
     assert len(gt) > 0 and np.array_equal(gt, ot)
     assert np.abs(gf - of).max() <= 1e-10 * np.abs(of).max()
     assert np.abs(gH - oH).max() <= 1e-10 * np.abs(oH).max()
+
+
+def test_timestepper_mirror_contact_flags_match_oracle():
+    """BACKWARD_EULER_VELOCITY mirror with vertexFaceSelfCollisionsOn, the
+    stiffness, damping beta and collision eps set like the reference's
+    TIMESTEPPER / TET_MESH accessors (hobak_gpu_set_collisions underneath)."""
+    s = scenes.two_cubes_scene(5)
+    mesh = hobak.TET_MESH(s.rest, s.tets)
+    bev = hobak.BACKWARD_EULER_VELOCITY(mesh, hobak.SNH(s.mu, s.lam))
+    bev.scaleMass(s.density)
+    bev.attachKinematicConstraints(s.pinned)
+    bev.setVertexFaceSelfCollisionsOn(True)
+    bev.setCollisionStiffness(MU)
+    bev.setCollisionDampingBeta(BETA)
+    bev.setCollisionEps(EPS)
+    sim = oracle.Sim(s, precond=hobak.PRECOND_BLOCK_JACOBI)
+    sim.set_collisions(True, EPS, MU, BETA)
+    for _ in range(6):
+        bev.externalForces()[:] = 0.0
+        bev.addGravity(np.array(s.gravity) * s.density)
+        bev.solve(False)
+    sim.step(6)
+    x, _ = sim.state()
+    assert np.linalg.norm(bev.position() - x) / np.linalg.norm(x) < 1e-8
