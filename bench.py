@@ -366,9 +366,11 @@ def run_ours(args, spec, scene_list):
     torch.cuda.synchronize()
     clocks.start()
     ev[0].record(stream)
+    scene_iters = []
     for k in range(args.steps):
         st = batch.step(1)
         iters.append(max(s[0] for s in st))
+        scene_iters.extend(s[0] for s in st)
         ev[k + 1].record(stream)
     torch.cuda.synchronize()
     clock = clocks.stop()
@@ -458,6 +460,7 @@ def run_ours(args, spec, scene_list):
                 "config": {"workload": args.workload, **config_of(spec, scene_list),
                            "launch_shapes": {**tuning, "chosen_by": "given" if args.no_autotune else "autotuner"}},
                 "pcg_iters_per_step": float(np.mean(iters)),
+                "pcg_iters_per_scene_pct": {q: float(np.percentile(scene_iters, q)) for q in (10, 50, 90, 100)},
                 "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
                 "roofline": roofline, "cpu_baseline": cpu, "plain_fp64_gpu": plain, "e2e": e2e,
                 "gpu_launches": int(gpu_launches),

@@ -361,6 +361,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oVtxptr = A.reserve(sizeof(int) * (nv + 1)), oVtxinc = A.reserve(sizeof(int) * 4 * (size_t)nt);
   const size_t oTileS = A.reserve(sizeof(int) * ntilesCap), oTile0 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oTile1 = A.reserve(sizeof(int) * ntilesCap);
+  const size_t oLoopTiles = A.reserve(sizeof(int) * ntilesCap), oNLoop = A.reserve(sizeof(int));
   const size_t oEH = A.reserve(sizeof(double) * kElemHess * (size_t)nt);
   const size_t oEHf = A.reserve(sizeof(float) * kElemHess * (size_t)nt);
   const size_t oEG = A.reserve(sizeof(double) * 12 * (size_t)nt);
@@ -421,6 +422,8 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.tileScene = carve<int>(base, oTileS);
   d.tileV0 = carve<int>(base, oTile0);
   d.tileV1 = carve<int>(base, oTile1);
+  d.loopTiles = carve<int>(base, oLoopTiles);
+  d.nLoopTiles = carve<int>(base, oNLoop);
   d.elemH = carve<double>(base, oEH);
   d.elemHf = carve<float>(base, oEHf);
   d.elemG = carve<double>(base, oEG);
@@ -505,9 +508,11 @@ long long fixed_launches(const hobak_batch_t* B) {
   return 6 + sweeps * (2 + (mixed ? 2 : 0));
 }
 
-// One PCG chunk: `chunk` iterations (2 kernels each).
+// One PCG chunk: the list of tiles still iterating, then `chunk` iterations
+// (2 kernels each).
 template <typename T>
 void enqueue_chunk(const DeviceBatch& d, const PcgVecs<T>& v, cudaStream_t s, int chunk) {
+  launch_compact_tiles(d, s);
   for (int c = 0; c < chunk; c++) launch_pcg_iteration<T>(d, v, s);
 }
 
@@ -838,7 +843,9 @@ int run_steps(hobak_batch_t* B, int nsteps) {
 int count_loop_launches(hobak_batch_t* B, long long* out) {
   unsigned long long runs = 0;
   CUDA_TRY(cudaMemcpy(&runs, B->d.bodyRuns, sizeof(runs), cudaMemcpyDeviceToHost));
-  *out = B->loopLaunchBase + (long long)(runs * (2ull * B->chunk + 1ull)) + B->eagerChunks * 2LL * B->chunk;
+  // a loop body = tile compaction + chunk x (SpMV, update) + k_continue; an
+  // eager chunk has no k_continue
+  *out = B->loopLaunchBase + (long long)(runs * (2ull * B->chunk + 2ull)) + B->eagerChunks * (2LL * B->chunk + 1);
   return HOBAK_OK;
 }
 
@@ -1244,10 +1251,14 @@ int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
     x.totalIters = 0;
     if (!(x.alpha == x.alpha)) x.alpha = 0.0;
     if (!(x.beta == x.beta)) x.beta = 0.0;
+    x.alphaF = float(x.alpha);
+    x.betaF = float(x.beta);
   }
   CUDA_TRY(cudaMemcpy(d.solve, st.data(), sizeof(SolveState) * n, cudaMemcpyHostToDevice));
   cudaEvent_t e0 = b->ev[0], e1 = b->ev[1];
   const bool mixed = b->opts.precision == HOBAK_PRECISION_MIXED;
+  launch_compact_tiles(d, s);  // every tile in the PCG loop kernels' list
+  b->launches += 1;
   for (int k = 0; k < 4; k++) {
     CUDA_TRY(cudaEventRecord(e0, s));
     for (int r = 0; r < reps; r++) {

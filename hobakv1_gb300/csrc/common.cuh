@@ -60,6 +60,7 @@ struct SolveState {
   int maxit;
   // inner PCG
   double gamma, gammaOld, delta, alpha, beta, rr, innerThreshold;
+  float alphaF, betaF;  // FP32 copies for the mixed inner solve (no per-thread conversion)
   int iters, done;
   unsigned ticketA, ticketB;
 };

@@ -26,6 +26,10 @@ struct DeviceBatch {
   // launch shapes (hobak_batch_autotune): vertices per PCG tile (64 or 128),
   // element-kernel CTA size (64 or 128), assembly CTA size
   int tileV, elemThreads, asmThreads;
+  // PCG loop kernels: compacted list of tiles still iterating and its length
+  // (k_compact_tiles)
+  int* loopTiles;
+  int* nLoopTiles;
   const SceneParams* scenes;
   SolveState* solve;
   int* active;  // scenes whose inner PCG is still running
@@ -92,6 +96,7 @@ template <typename T>
 void launch_diag_inverse(const DeviceBatch& b, const PcgVecs<T>& v, int precond, cudaStream_t s);
 void launch_rhs(const DeviceBatch& b, cudaStream_t s);
 void launch_set_active(const DeviceBatch& b, cudaStream_t s);
+void launch_compact_tiles(const DeviceBatch& b, cudaStream_t s);
 template <typename T>
 void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
 template <typename T>

@@ -156,12 +156,14 @@ __device__ __forceinline__ HT gather_block_entry(const DeviceBatch& b, const HT*
   return sum;
 }
 
-// One thread per (block, entry): LHS block = S(M - dt^2 K)S + (I - S).
+// FP64 assembly: one thread per (block, entry), so the nine entries of a
+// contribution (72 contiguous bytes) are read by nine neighbouring lanes in one
+// request; at FP64 width this coalescing beats a thread per block.
 template <typename HT, typename T>
-__global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
-  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= 9L * b.nblocks) return;
-  const int blk = (int)(g / 9), e = (int)(g % 9);
+__global__ void k_assemble_entry(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
+  const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= 9u * (unsigned)b.nblocks) return;
+  const int blk = (int)(g / 9u), e = (int)(g % 9u);
   if (!b.scenes[b.vertexScene[b.blkRow[blk]]].active) return;
   const int r = e / 3, c = e % 3;
   const HT sum = gather_block_entry(b, elemH, blk, r, c);
@@ -171,6 +173,77 @@ __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __res
   HT val = (fu && fw) ? HT(-(dt * dt)) * sum : HT(0);
   if (u == w && r == c) val += fu ? HT(b.mass[u]) : HT(1);
   lhs[9 * (size_t)blk + e] = T(val);
+}
+
+// FP32 assembly: one thread per block: its 9 entries summed over the block's
+// element contributions in list order (ascending tet), several contributions' loads
+// in flight at a time (each contribution is 9 contiguous values: a 3x3 block of
+// one element Hessian, transposed for the lower triangle), then
+// LHS block = S(M - dt^2 K)S + (I - S), staged through shared memory so the
+// CTA writes its blocks as one contiguous run.  Dynamic shared memory:
+// blockDim.x * (9 * sizeof(T) + 1).
+template <typename HT, typename T>
+__global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* out = reinterpret_cast<T*>(smem);
+  unsigned char* live = smem + 9 * sizeof(T) * blockDim.x;
+  const int blk0 = blockIdx.x * blockDim.x;
+  const int blk = blk0 + threadIdx.x;
+  bool write = false;
+  if (blk < b.nblocks) {
+    const int u = b.blkRow[blk];
+    const SceneParams& sp = b.scenes[b.vertexScene[u]];
+    if (sp.active) {
+      write = true;
+      HT sum[9];
+#pragma unroll
+      for (int e = 0; e < 9; e++) sum[e] = HT(0);
+      // contributions in flight: 4 in FP32, 2 in FP64 (register budget)
+      constexpr int kQ = sizeof(HT) == sizeof(float) ? 4 : 2;
+      const int k0 = b.blkptr[blk], k1 = b.blkptr[blk + 1];
+      for (int k = k0; k < k1; k += kQ) {
+        int src[kQ];
+#pragma unroll
+        for (int q = 0; q < kQ; q++) src[q] = (k + q < k1) ? __ldg(&b.blksrc[k + q]) : 0;
+        HT val[kQ][9];
+#pragma unroll
+        for (int q = 0; q < kQ; q++) {
+          const int t = src[q] >> 4, ea = (src[q] >> 2) & 3, eb = src[q] & 3;
+          const HT* H = elemH + (size_t)kElemHess * t + 9 * ((ea <= eb) ? upper_block(ea, eb) : upper_block(eb, ea));
+#pragma unroll
+          for (int e = 0; e < 9; e++) val[q][e] = (k + q < k1) ? H[e] : HT(0);
+          if (ea > eb) {  // lower-triangle block: the stored upper block transposed
+            HT tmp;
+            tmp = val[q][1]; val[q][1] = val[q][3]; val[q][3] = tmp;
+            tmp = val[q][2]; val[q][2] = val[q][6]; val[q][6] = tmp;
+            tmp = val[q][5]; val[q][5] = val[q][7]; val[q][7] = tmp;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < kQ; q++)
+          if (k + q < k1)
+#pragma unroll
+            for (int e = 0; e < 9; e++) sum[e] += val[q][e];
+      }
+      const int w = b.cols[blk];
+      const double dt = sp.dt;
+      const bool fu = b.freeMask[u] != 0, fw = b.freeMask[w] != 0;
+      const HT m = fu ? HT(b.mass[u]) : HT(1);
+      const HT ndt2 = HT(-(dt * dt));
+#pragma unroll
+      for (int e = 0; e < 9; e++) {
+        HT val = (fu && fw) ? ndt2 * sum[e] : HT(0);
+        if (u == w && e % 4 == 0) val += m;
+        out[9 * threadIdx.x + e] = T(val);
+      }
+    }
+  }
+  live[threadIdx.x] = write ? 1 : 0;
+  // parked scenes' blocks keep their old values: write back only live blocks
+  __syncthreads();
+  const int nb = min((int)blockDim.x, b.nblocks - blk0);
+  for (int i = threadIdx.x; i < 9 * nb; i += blockDim.x)
+    if (live[i / 9]) lhs[9 * (size_t)blk0 + i] = out[i];
 }
 
 // Raw K blocks (column major) and R: the reference's stiffness and force
@@ -373,6 +446,8 @@ __global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) 
     st.gammaOld = 1.0;
     st.alpha = 1.0;
     st.beta = 0.0;
+    st.alphaF = 1.0f;
+    st.betaF = 0.0f;
     st.iters = 0;
     st.innerThreshold = fmax(itol * itol * srr, DBL_MIN);
     st.done = 0;
@@ -417,10 +492,7 @@ __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int
 // w = A u, one thread per scalar row (9 DFMA per block in FP64), and
 // delta = (w, u); the scene's last CTA forms beta and alpha.
 template <int TV, typename T>
-__global__ void __launch_bounds__(3 * TV) k_spmv(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[3 * TV / 32];
-  __shared__ int flag;
-  const int tile = blockIdx.x;
+__device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh, int* flag) {
   const int s = b.tileScene[tile];
   SolveState& st = b.solve[s];
   if (st.done) return;
@@ -465,7 +537,7 @@ __global__ void __launch_bounds__(3 * TV) k_spmv(DeviceBatch b, PcgVecs<T> v) {
   const double t = block_sum<3 * TV>(dl, sh);
   if (threadIdx.x == 0) b.partial[kPartials * tile + 2] = t;
   const SceneParams& sp = b.scenes[s];
-  if (!last_tile(&st.ticketA, sp.ntiles, &flag)) return;
+  if (!last_tile(&st.ticketA, sp.ntiles, flag)) return;
   const double delta = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 2, sh);
   if (threadIdx.x == 0) {
     st.delta = delta;
@@ -477,7 +549,27 @@ __global__ void __launch_bounds__(3 * TV) k_spmv(DeviceBatch b, PcgVecs<T> v) {
       st.beta = beta;
       st.alpha = st.gamma / (delta - beta * st.gamma / st.alpha);
     }
+    st.alphaF = float(st.alpha);
+    st.betaF = float(st.beta);
   }
+}
+
+// CTA -> tile of the PCG loop kernels (grid = all tiles).  While every scene
+// iterates, CTA i takes tile i; once scenes have finished, the CTAs take the
+// compacted list of tiles still iterating (k_compact_tiles) and the rest exit
+// after a single load instead of walking tile -> scene -> solve state.
+__device__ __forceinline__ int loop_tile(const DeviceBatch& b) {
+  const int n = *b.nLoopTiles;
+  if (n == b.ntiles) return blockIdx.x;
+  return (int)blockIdx.x < n ? b.loopTiles[blockIdx.x] : -1;
+}
+
+template <int TV, typename T>
+__global__ void __launch_bounds__(3 * TV) k_spmv(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[3 * TV / 32];
+  __shared__ int flag;
+  const int tile = loop_tile(b);
+  if (tile >= 0) spmv_tile<TV, T>(b, v, tile, sh, &flag);
 }
 
 // p = u + beta p; s = w + beta s; d += alpha p; r -= alpha s; u = Minv r;
@@ -486,15 +578,21 @@ template <int TV, typename T>
 // One thread per scalar row (three times the threads of a per-vertex loop,
 // which a 40^3 scene needs to cover the GPU's latency); the 3x3 block of
 // Minv reads its vertex's three new residual rows from shared memory.
-__global__ void __launch_bounds__(3 * TV, 640 / TV) k_update(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[2 * 3 * TV / 32];
-  __shared__ T rsh[3 * TV];
-  __shared__ int flag;
-  const int tile = blockIdx.x;
+__device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh, T* rsh,
+                                            int* flag) {
   const int s = b.tileScene[tile];
   SolveState& st = b.solve[s];
   if (st.done) return;
-  const T alpha = T(st.alpha), beta = T(st.beta);
+  // FP32 scalars come pre-converted: a double-to-float conversion per thread
+  // would occupy GB300's narrow FP64 pipe
+  T alpha, beta;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    alpha = st.alphaF;
+    beta = st.betaF;
+  } else {
+    alpha = st.alpha;
+    beta = st.beta;
+  }
   const int row = 3 * b.tileV0[tile] + threadIdx.x;
   const bool valid = row < 3 * b.tileV1[tile];
   T rr = T(0), ru = T(0);
@@ -531,7 +629,7 @@ __global__ void __launch_bounds__(3 * TV, 640 / TV) k_update(DeviceBatch b, PcgV
     b.partial[kPartials * tile + 1] = tru;
   }
   const SceneParams& sp = b.scenes[s];
-  if (!last_tile(&st.ticketB, sp.ntiles, &flag)) return;
+  if (!last_tile(&st.ticketB, sp.ntiles, flag)) return;
   const double srr = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 0, sh);
   const double sru = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 1, sh);
   if (threadIdx.x == 0) {
@@ -561,6 +659,56 @@ __global__ void __launch_bounds__(3 * TV, 640 / TV) k_update(DeviceBatch b, PcgV
       }
     }
   }
+}
+
+template <int TV, typename T>
+__global__ void __launch_bounds__(3 * TV, TV == 64 ? 8 : 5) k_update(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[2 * 3 * TV / 32];
+  __shared__ T rsh[3 * TV];
+  __shared__ int flag;
+  const int tile = loop_tile(b);
+  if (tile >= 0) update_tile<TV, T>(b, v, tile, sh, rsh, &flag);
+}
+
+// Compacted list of the tiles whose scene's inner PCG still runs, rebuilt at
+// the start of every PCG loop body (one CTA; scenes in order, tiles in order).
+__global__ void __launch_bounds__(1024) k_compact_tiles(DeviceBatch b) {
+  __shared__ int warpTot[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+  for (int base = 0; base < b.nscenes; base += 1024) {
+    const int s = base + threadIdx.x;
+    const int cnt = (s < b.nscenes && !b.solve[s].done) ? b.scenes[s].ntiles : 0;
+    int x = cnt;  // inclusive scan in the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warpTot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int t = warpTot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      warpTot[lane] = t;  // inclusive over warps
+    }
+    __syncthreads();
+    const int off = carry + (wid > 0 ? warpTot[wid - 1] : 0) + x - cnt;
+    if (cnt > 0) {
+      const int t0 = b.scenes[s].tile0;
+      for (int j = 0; j < cnt; j++) b.loopTiles[off + j] = t0 + j;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warpTot[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *b.nLoopTiles = carry;
 }
 
 // Mixed precision, after an inner solve: y += d (FP64), one vertex per thread.
@@ -651,11 +799,15 @@ void launch_begin_step(const DeviceBatch& b, cudaStream_t s) {
 
 template <typename T>
 void launch_assemble(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
-  const long n = 9L * b.nblocks;
-  if (sizeof(T) == sizeof(double))
-    k_assemble<double, T><<<(unsigned)((n + b.asmThreads - 1) / b.asmThreads), b.asmThreads, 0, s>>>(b, b.elemH, v.lhs);
-  else
-    k_assemble<float, T><<<(unsigned)((n + b.asmThreads - 1) / b.asmThreads), b.asmThreads, 0, s>>>(b, b.elemHf, v.lhs);
+  if (b.nblocks == 0) return;
+  if (sizeof(T) == sizeof(double)) {
+    const unsigned n = 9u * (unsigned)b.nblocks;
+    k_assemble_entry<double, T><<<(n + b.asmThreads - 1) / b.asmThreads, b.asmThreads, 0, s>>>(b, b.elemH, v.lhs);
+  } else {
+    const unsigned grid = (unsigned)((b.nblocks + b.asmThreads - 1) / b.asmThreads);
+    const size_t smem = (9 * sizeof(T) + 1) * (size_t)b.asmThreads;
+    k_assemble<float, T><<<grid, b.asmThreads, smem, s>>>(b, b.elemHf, v.lhs);
+  }
 }
 
 void launch_assemble_raw(const DeviceBatch& b, double* K, double* R, cudaStream_t s) {
@@ -678,6 +830,8 @@ void launch_diag_inverse(const DeviceBatch& b, const PcgVecs<T>& v, int precond,
 void launch_rhs(const DeviceBatch& b, cudaStream_t s) { HOBAK_TILE_LAUNCH(k_rhs, 1, b); }
 
 void launch_set_active(const DeviceBatch& b, cudaStream_t s) { k_set_active<<<1, 32, 0, s>>>(b); }
+
+void launch_compact_tiles(const DeviceBatch& b, cudaStream_t s) { k_compact_tiles<<<1, 1024, 0, s>>>(b); }
 
 template <typename T>
 void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
