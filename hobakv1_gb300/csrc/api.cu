@@ -573,7 +573,7 @@ int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, c
   if (d.collOn) launch_collisions(d, d.coll, s);
   if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[1], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   launch_assemble<T>(d, v, s);
-  if (d.collOn) launch_collision_diag<T>(d, d.coll, v.lhs, s);
+  if (d.collOn) launch_collision_diag(d, d.coll, s);
   launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
   if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[2], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   launch_rhs(d, s);
@@ -739,6 +739,7 @@ int build_collisions(hobak_batch_t* B) {
   const size_t oPairG = A.reserve(sizeof(double) * 9 * (size_t)cap);
   const size_t oPairR = A.reserve(sizeof(double) * 12 * (size_t)cap);
   const size_t oPairF = A.reserve(sizeof(double) * 12 * (size_t)cap);
+  const size_t oDiag = A.reserve(sizeof(double) * 9 * (size_t)nv);
   const size_t oIncCount = A.reserve(sizeof(int) * (nv + 1)), oIncCursor = A.reserve(sizeof(int) * nv);
   const size_t oIncList = A.reserve(sizeof(int) * 4 * (size_t)cap);
   const size_t oScan = A.reserve(sizeof(int) * scanBlocks);
@@ -780,6 +781,7 @@ int build_collisions(hobak_batch_t* B) {
   c.pairG = carve<double>(base, oPairG);
   c.pairRhs = carve<double>(base, oPairR);
   c.pairF = carve<double>(base, oPairF);
+  c.diag = carve<double>(base, oDiag);
   c.incCount = carve<int>(base, oIncCount);
   c.incCursor = carve<int>(base, oIncCursor);
   c.incList = carve<int>(base, oIncList);

@@ -425,14 +425,21 @@ __global__ void k_copy_total(const int* src, int* dst) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 
-// Collision part of LHS's diagonal: -(dt beta + dt^2) sum c_a^2 G over the
-// vertex's incidences (free rows only).
-template <typename T>
-__global__ void k_coll_diag(DeviceBatch b, DeviceCollisions c, T* lhs) {
+// Collision part of LHS's diagonal, -(dt beta + dt^2) sum c_a^2 G over the
+// vertex's incidences (free rows only; zero elsewhere), kept in FP64 beside
+// the LHS: the preconditioner adds it to the diagonal block, the products
+// (collision_row) apply it in FP64, so the mixed path's FP64 residual sees the
+// stiff contact block unrounded.
+__global__ void k_coll_diag(DeviceBatch b, DeviceCollisions c) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= c.nv || !b.freeMask[u]) return;
+  if (u >= c.nv) return;
+  double* out = c.diag + 9 * (size_t)u;
   const int k0 = c.incCount[u], k1 = c.incCount[u + 1];
-  if (k0 == k1) return;
+  if (k0 == k1 || !b.freeMask[u]) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) out[q] = 0.0;
+    return;
+  }
   const int s = b.vertexScene[u];
   const double dt = b.scenes[s].dt, scale = -(dt * c.scenes[s].beta + dt * dt);
   double D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -441,11 +448,8 @@ __global__ void k_coll_diag(DeviceBatch b, DeviceCollisions c, T* lhs) {
     const double ca = c.pairC[4 * (size_t)p + a];
     for (int q = 0; q < 9; q++) D[q] += scale * ca * ca * c.pairG[9 * (size_t)p + q];
   }
-  int kd = b.rowptr[u];
-  while (b.cols[kd] != u) kd++;
-  T* B = lhs + 9 * (size_t)kd;
   for (int r = 0; r < 3; r++)
-    for (int q = 0; q < 3; q++) B[3 * r + q] = T(double(B[3 * r + q]) + D[r + 3 * q]);
+    for (int q = 0; q < 3; q++) out[3 * r + q] = D[r + 3 * q];  // row major like the LHS blocks
 }
 
 }  // namespace
@@ -473,11 +477,8 @@ void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStre
   k_inc_sort<<<(c.nv + 255) / 256, 256, 0, s>>>(c);
 }
 
-template <typename T>
-void launch_collision_diag(const DeviceBatch& b, const DeviceCollisions& c, T* lhs, cudaStream_t s) {
-  k_coll_diag<T><<<(c.nv + 255) / 256, 256, 0, s>>>(b, c, lhs);
+void launch_collision_diag(const DeviceBatch& b, const DeviceCollisions& c, cudaStream_t s) {
+  k_coll_diag<<<(c.nv + 255) / 256, 256, 0, s>>>(b, c);
 }
-template void launch_collision_diag<double>(const DeviceBatch&, const DeviceCollisions&, double*, cudaStream_t);
-template void launch_collision_diag<float>(const DeviceBatch&, const DeviceCollisions&, float*, cudaStream_t);
 
 }  // namespace hobak

@@ -48,6 +48,7 @@ struct DeviceCollisions {
   double* pairG;           // [pairCap][9] 3x3 factor of the clamped Hessian, times -w 2 mu
   double* pairRhs;         // [pairCap][12] dt (f + dt H v)
   double* pairF;           // [pairCap][12] collision force -w grad psi (for inspection)
+  double* diag;            // [nv][9] vertex's own 3x3 block of -(dt beta + dt^2) H_coll (FP64)
   int* incCount;           // [nv + 1] then exclusive scan
   int* incCursor;          // [nv]
   int* incList;            // [4 * pairCap] pair * 4 + slot
@@ -59,8 +60,8 @@ struct DeviceBatch;
 // Enqueue the per-step detection and response (after the element kernel,
 // before assembly uses them).  dtScale: per-scene dt taken from the batch.
 void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStream_t s);
-// Adds the collision part of LHS's diagonal blocks (before the preconditioner).
-template <typename T>
-void launch_collision_diag(const DeviceBatch& b, const DeviceCollisions& c, T* lhs, cudaStream_t s);
+// The vertices' own collision blocks (DeviceCollisions::diag, FP64), before
+// the preconditioner reads them.
+void launch_collision_diag(const DeviceBatch& b, const DeviceCollisions& c, cudaStream_t s);
 
 }  // namespace hobak

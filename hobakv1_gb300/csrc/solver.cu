@@ -277,6 +277,10 @@ __global__ void k_diag_inverse(DeviceBatch b, const T* __restrict__ lhs, T* __re
   double D[9];
 #pragma unroll
   for (int i = 0; i < 9; i++) D[i] = (double)lhs[9 * (size_t)k + i];
+  if (b.collOn) {  // the vertex's own contact block (FP64, beside the LHS)
+#pragma unroll
+    for (int i = 0; i < 9; i++) D[i] += b.coll.diag[9 * (size_t)u + i];
+  }
   T* M = minv + 9 * (size_t)u;
   if (precond == 1) {
     const double c00 = D[4] * D[8] - D[5] * D[7];
@@ -458,11 +462,10 @@ __global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) 
   }
 }
 
-// Row i of vertex u of the off-diagonal part of -(dt beta + dt^2) H_coll x,
-// H_coll = sum over the vertex's collision tets of (c c^T) (x) G (free rows
-// only; x vanishes on pinned rows, which keeps the columns masked too).  The
-// vertex's own 3x3 block was folded into LHS's diagonal by k_coll_diag, so the
-// tet's column for u itself is skipped here.
+// Row i of vertex u of -(dt beta + dt^2) H_coll x, H_coll = sum over the
+// vertex's collision tets of (c c^T) (x) G (free rows only; x vanishes on
+// pinned rows, which keeps the columns masked too).  FP64 throughout: the
+// contact blocks are not part of the (possibly FP32) assembled LHS.
 template <typename T>
 __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int i, const T* __restrict__ x) {
   const DeviceCollisions& c = b.coll;
@@ -479,11 +482,9 @@ __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int
     const int id[4] = {ct.x, ct.y, ct.z, ct.w};
     double z[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      if (q == a) continue;
+    for (int q = 0; q < 4; q++)
 #pragma unroll
       for (int j = 0; j < 3; j++) z[j] += C[q] * double(x[3 * id[q] + j]);
-    }
     acc += C[a] * (G[i] * z[0] + G[i + 3] * z[1] + G[i + 6] * z[2]);
   }
   return scale * acc;
