@@ -132,18 +132,20 @@ __device__ __forceinline__ void svd3_rv(const double* F, double* U, double* S, d
 
 // The same SVD with most of the Jacobi work moved off the FP64 pipe, which is
 // the scarce resource on GB300 (FP32 issues far faster):
-//   1. one-sided Jacobi sweeps in FP32 give V32 with F V32 orthogonal to ~1e-7;
+//   1. one-sided Jacobi sweeps in FP32 give V32 with F V32 orthogonal to
+//      ~3e-7 (a few FP32 ulps; more FP32 sweeps cost far less than an FP64 one);
 //   2. V32 is re-orthonormalised in FP64 (modified Gram-Schmidt), so V stays an
 //      exact rotation to FP64 precision;
-//   3. FP64 one-sided Jacobi on A = F V finishes the job; starting ~1e-6 from
-//      orthogonal, one sweep brings the columns to ~1e-12 (quadratic
-//      convergence) and the second sweep only checks.  Rotation angles are
-//      computed in FP32 and turned into an exactly orthogonal (c, s) pair in
-//      FP64.
+//   3. FP64 one-sided Jacobi on A = F V finishes the job; starting ~3e-7 from
+//      orthogonal, one sweep brings well-separated columns to ~1e-13
+//      (quadratic convergence) and the second sweep only checks; nearly
+//      equal singular values may take one more rotating sweep.  Rotation
+//      angles are computed in FP32 and turned into an exactly orthogonal
+//      (c, s) pair in FP64.
 // V is a rotation to FP64 rounding and F = U S V^T holds to FP64 rounding;
-// U's columns are orthogonal to 1e-13 relative (the stop test), which keeps
-// forces and Hessians within 1e-12 of a fully converged SVD while sparing a
-// second rotating sweep of ~110 FP64 instructions per element.
+// U's columns are orthogonal to 1e-12 relative (the stop test), which keeps
+// forces and Hessians within ~1e-12 of a fully converged SVD while sparing
+// rotating sweeps of ~110 FP64 instructions per element each.
 __device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double* S, double* V) {
   // ---- stage 1: FP32 Jacobi ----
   float a[9], w[9];
@@ -161,7 +163,7 @@ __device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double*
       const float al = a[3 * p] * a[3 * p] + a[3 * p + 1] * a[3 * p + 1] + a[3 * p + 2] * a[3 * p + 2];
       const float be = a[3 * q] * a[3 * q] + a[3 * q + 1] * a[3 * q + 1] + a[3 * q + 2] * a[3 * q + 2];
       const float ga = a[3 * p] * a[3 * q] + a[3 * p + 1] * a[3 * q + 1] + a[3 * p + 2] * a[3 * q + 2];
-      if (fabsf(ga) > 1e-6f * sqrtf(al * be)) {
+      if (fabsf(ga) > 3e-7f * sqrtf(al * be)) {  // a few FP32 ulps above the rounding noise
         rotated = true;
         const float zeta = (be - al) / (2.0f * ga);
         const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
@@ -209,7 +211,7 @@ __device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double*
       const double alpha = A[3 * p] * A[3 * p] + A[3 * p + 1] * A[3 * p + 1] + A[3 * p + 2] * A[3 * p + 2];
       const double beta = A[3 * q] * A[3 * q] + A[3 * q + 1] * A[3 * q + 1] + A[3 * q + 2] * A[3 * q + 2];
       const double gamma = A[3 * p] * A[3 * q] + A[3 * p + 1] * A[3 * q + 1] + A[3 * p + 2] * A[3 * q + 2];
-      if (gamma * gamma > 1e-26 * (alpha * beta)) {  // columns orthogonal to 1e-13 relative
+      if (gamma * gamma > 1e-24 * (alpha * beta)) {  // columns orthogonal to 1e-12 relative
         rotated = true;
         // angle in FP32 (only orthogonality of (c, s) must be FP64-exact)
         const float zf = float(beta - alpha) / (2.0f * float(gamma));
