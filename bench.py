@@ -401,39 +401,38 @@ def run_ours(args, spec, scene_list):
                                 "launches_per_step": per_step_launches[k]} for k in kms}}
 
     # ---- e2e: public API with pinned host buffers in/out every step ----
+    # whole-batch calls (every scene's state is contiguous on the device): the
+    # inputs x, v, f_ext go up and x, v come back every step
     nvs = [s.nv for s in scene_list]
-    host = [(torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy(),
-             torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy(),
-             torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy()) for n in nvs]
-    for i, (x, v, f) in enumerate(host):
-        xx, vv = batch.get_state(i)
-        x[:], v[:] = xx, vv
-        s = scene_list[i]
+    ntot = 3 * sum(nvs)
+    pinned = lambda: torch.empty(ntot, dtype=torch.float64, pin_memory=True).numpy()
+    hx, hv, hf = pinned(), pinned(), pinned()
+    batch.get_state_all(hx, hv)
+    off = 0
+    for s in scene_list:
         mass = np.zeros(s.nv)
         np.add.at(mass, s.tets.reshape(-1), np.repeat(0.25 * np.abs(
             np.einsum("ij,ij->i", s.rest[s.tets[:, 3]] - s.rest[s.tets[:, 0]],
                       np.cross(s.rest[s.tets[:, 1]] - s.rest[s.tets[:, 0]],
                                s.rest[s.tets[:, 2]] - s.rest[s.tets[:, 0]])) / 6.0), 4))
-        f[:] = (mass[:, None] * (s.density * np.array(s.gravity))[None, :]).reshape(-1)
+        hf[off:off + 3 * s.nv] = (mass[:, None] * (s.density * np.array(s.gravity))[None, :]).reshape(-1)
+        off += 3 * s.nv
     e2e_steps = max(3, min(args.steps, 20))
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(e2e_steps):
-        for i, (x, v, f) in enumerate(host):
-            batch.set_state(i, x, v)
-            batch.set_external_forces(i, f)
+        batch.set_state_all(hx, hv)
+        batch.set_external_forces_all(hf)
         batch.step(1)
-        for i, (x, v, f) in enumerate(host):
-            xx, vv = batch.get_state(i)
-            x[:], v[:] = xx, vv
+        batch.get_state_all(hx, hv)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
-    nbytes = sum(nvs) * 3 * 8
+    nbytes = ntot * 8
     e2e = {"value": world * e2e_steps / (e2e_ms / 1e3), "unit": "steps/s",
-           "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": 2 * nbytes + 32 * len(nvs),
-           "api": "hobak_batch_set_state/set_external_forces/step/get_state"}
+           "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": 2 * nbytes + 136 * len(nvs),
+           "api": "hobak_batch_set_state_all/set_external_forces_all/step/get_state_all"}
 
     # ---- CPU baseline (rank 0, N = 1 only) ----
     cpu = None

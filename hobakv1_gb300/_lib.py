@@ -55,6 +55,9 @@ SIGNATURES = {
     "hobak_batch_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "hobak_batch_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakStepStats)]),
     "hobak_batch_query": (ctypes.c_int, [ctypes.c_void_p]),
+    "hobak_batch_set_state_all": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    "hobak_batch_get_state_all": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    "hobak_batch_set_external_forces_all": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "hobak_batch_set_active": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "hobak_batch_set_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
     "hobak_batch_get_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),

@@ -513,7 +513,7 @@ long long fixed_launches(const hobak_batch_t* B) {
 template <typename T>
 void enqueue_chunk(const DeviceBatch& d, const PcgVecs<T>& v, cudaStream_t s, int chunk) {
   launch_compact_tiles(d, s);
-  for (int c = 0; c < chunk; c++) launch_pcg_iteration<T>(d, v, s);
+  for (int c = 0; c < chunk; c++) launch_pcg_iteration<T>(d, v, s, c == 0);
 }
 
 // While-loop node on the capturing stream `s`: body = one chunk followed by
@@ -1056,6 +1056,32 @@ int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v) {
   if (x) CUDA_TRY(cudaMemcpyAsync(x, b->d.x + 3 * (size_t)H.v0, bytes, cudaMemcpyDeviceToHost, b->stream));
   if (v) CUDA_TRY(cudaMemcpyAsync(v, b->d.v + 3 * (size_t)H.v0, bytes, cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+// Whole-batch state: every scene's 3*nv values back to back in scene order,
+// which is how the batch keeps them on the device, so each is one copy.
+int hobak_batch_set_state_all(hobak_batch b, const double* x, const double* v) {
+  if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
+  const size_t bytes = 3 * sizeof(double) * (size_t)b->nv;
+  if (x) CUDA_TRY(cudaMemcpyAsync(b->d.x, x, bytes, cudaMemcpyHostToDevice, b->stream));
+  if (v) CUDA_TRY(cudaMemcpyAsync(b->d.v, v, bytes, cudaMemcpyHostToDevice, b->stream));
+  return HOBAK_OK;
+}
+
+int hobak_batch_get_state_all(hobak_batch b, double* x, double* v) {
+  if (!b) return fail(HOBAK_ERR_INVALID, "null handle");
+  const size_t bytes = 3 * sizeof(double) * (size_t)b->nv;
+  if (x) CUDA_TRY(cudaMemcpyAsync(x, b->d.x, bytes, cudaMemcpyDeviceToHost, b->stream));
+  if (v) CUDA_TRY(cudaMemcpyAsync(v, b->d.v, bytes, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_external_forces_all(hobak_batch b, const double* f) {
+  if (!b || !f) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  CUDA_TRY(cudaMemcpyAsync(const_cast<double*>(b->d.fext), f, 3 * sizeof(double) * (size_t)b->nv,
+                           cudaMemcpyHostToDevice, b->stream));
   return HOBAK_OK;
 }
 

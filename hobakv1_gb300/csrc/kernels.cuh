@@ -100,13 +100,16 @@ void launch_compact_tiles(const DeviceBatch& b, cudaStream_t s);
 template <typename T>
 void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
 template <typename T>
-void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
+void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl = false);
 template <typename T>
-void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
+void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl = false);
 template <typename T>
-void launch_pcg_iteration(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
-  launch_spmv<T>(b, v, s);
-  launch_update<T>(b, v, s);
+// One PCG iteration.  The update always overlaps the SpMV's drain; the SpMV
+// overlaps the previous update's except right after k_compact_tiles (`first`),
+// whose tile list it reads before its dependency wait.
+void launch_pcg_iteration(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool first = false) {
+  launch_spmv<T>(b, v, s, !first);
+  launch_update<T>(b, v, s, true);
 }
 void launch_refine(const DeviceBatch& b, cudaStream_t s);  // y += d, then r64 = rhs - A y
 void launch_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s);void launch_finish_step(const DeviceBatch& b, cudaStream_t s);

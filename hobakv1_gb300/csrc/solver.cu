@@ -115,6 +115,18 @@ __device__ __forceinline__ double sum_partials(const double* partial, int tile0,
 
 __device__ __forceinline__ bool finite(double x) { return x == x && fabs(x) <= DBL_MAX; }
 
+// Programmatic dependent launch (sm_90 and later).  The PCG loop kernels are
+// launched with programmatic stream serialisation: the next kernel's CTAs may
+// start once every CTA of the running one has called pdl_trigger (or exited),
+// do the loads that do not depend on it (tile tables, matrix rows, column
+// indices, Minv rows: all written before the loop), and pdl_wait before
+// touching anything it writes (vectors, partials, solve state).  Every CTA
+// triggers at its start, so all CTAs of a kernel are resident or finished
+// before any CTA of the next one waits: no CTA can wait on one that cannot
+// run.  Launched without the attribute, pdl_wait returns at once.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // x[pinned] = pin target at the start of a step
 // (applyKinematicConstraints, TIMESTEPPER.cpp:105-122).
 __global__ void k_begin_step(DeviceBatch b) {
@@ -494,13 +506,24 @@ __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int
 // delta = (w, u); the scene's last CTA forms beta and alpha.
 template <int TV, typename T>
 __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh, int* flag) {
+  // before the dependency wait: what the previous kernel does not write
   const int s = b.tileScene[tile];
+  const int row = 3 * b.tileV0[tile] + threadIdx.x;
+  const bool valid = row < 3 * b.tileV1[tile];
+  const int u = row / 3, i = row - 3 * u;
+  int k0 = 0, k1 = 0;
+  int wn[4] = {0, 0, 0, 0};
+  if (valid) {
+    k0 = b.rowptr[u];
+    k1 = b.rowptr[u + 1];
+#pragma unroll
+    for (int q = 0; q < 4; q++) wn[q] = (k0 + q < k1) ? __ldg(&b.cols[k0 + q]) : 0;
+  }
+  pdl_wait();
   SolveState& st = b.solve[s];
   if (st.done) return;
-  const int row = 3 * b.tileV0[tile] + threadIdx.x;
   T dl = T(0);
-  if (row < 3 * b.tileV1[tile]) {
-    const int u = row / 3, i = row - 3 * u;
+  if (valid) {
     const T* __restrict__ uu = v.u;
     const T* __restrict__ A = v.lhs + 3 * i;
     // Four blocks per trip, all their loads issued together (predicated past
@@ -508,10 +531,6 @@ __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>
     // ahead, so each trip waits on one memory latency (the u gather) instead
     // of two.  Two FMA chains: 3 FMA per block, the FP64 minimum.
     T acc0 = T(0), acc1 = T(0);
-    const int k0 = b.rowptr[u], k1 = b.rowptr[u + 1];
-    int wn[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) wn[q] = (k0 + q < k1) ? __ldg(&b.cols[k0 + q]) : 0;
     for (int k = k0; k < k1; k += 4) {
       int w[4];
 #pragma unroll
@@ -569,6 +588,7 @@ template <int TV, typename T>
 __global__ void __launch_bounds__(3 * TV) k_spmv(DeviceBatch b, PcgVecs<T> v) {
   __shared__ double sh[3 * TV / 32];
   __shared__ int flag;
+  pdl_trigger();
   const int tile = loop_tile(b);
   if (tile >= 0) spmv_tile<TV, T>(b, v, tile, sh, &flag);
 }
@@ -581,7 +601,18 @@ template <int TV, typename T>
 // Minv reads its vertex's three new residual rows from shared memory.
 __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh, T* rsh,
                                             int* flag) {
+  // before the dependency wait: what the previous kernel does not write
   const int s = b.tileScene[tile];
+  const int row = 3 * b.tileV0[tile] + threadIdx.x;
+  const bool valid = row < 3 * b.tileV1[tile];
+  T M0 = T(0), M1 = T(0), M2 = T(0);
+  if (valid) {
+    const T* M = v.minv + 3 * (size_t)row;  // row i of the vertex's block
+    M0 = M[0];
+    M1 = M[1];
+    M2 = M[2];
+  }
+  pdl_wait();
   SolveState& st = b.solve[s];
   if (st.done) return;
   // FP32 scalars come pre-converted: a double-to-float conversion per thread
@@ -594,18 +625,11 @@ __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<
     alpha = st.alpha;
     beta = st.beta;
   }
-  const int row = 3 * b.tileV0[tile] + threadIdx.x;
-  const bool valid = row < 3 * b.tileV1[tile];
   T rr = T(0), ru = T(0);
   T* __restrict__ r = (sizeof(T) == sizeof(double)) ? reinterpret_cast<T*>(b.r64) : v.r;
-  T rnew = T(0), M0 = T(0), M1 = T(0), M2 = T(0);
+  T rnew = T(0);
   if (valid) {
-    // every load of the thread issued together, Minv's row included
-    const T* M = v.minv + 3 * (size_t)row;  // row i of the vertex's block
     const T u0 = v.u[row], p0 = v.p[row], w0 = v.w[row], s0 = v.s[row], d0 = v.d[row], r0 = r[row];
-    M0 = M[0];
-    M1 = M[1];
-    M2 = M[2];
     const T p = u0 + beta * p0;
     const T sv = w0 + beta * s0;
     v.p[row] = p;
@@ -667,6 +691,7 @@ __global__ void __launch_bounds__(3 * TV, TV == 64 ? 8 : 5) k_update(DeviceBatch
   __shared__ double sh[2 * 3 * TV / 32];
   __shared__ T rsh[3 * TV];
   __shared__ int flag;
+  pdl_trigger();
   const int tile = loop_tile(b);
   if (tile >= 0) update_tile<TV, T>(b, v, tile, sh, rsh, &flag);
 }
@@ -821,6 +846,24 @@ void launch_diag_inverse(const DeviceBatch& b, const PcgVecs<T>& v, int precond,
   k_diag_inverse<T><<<(b.nv + 255) / 256, 256, 0, s>>>(b, v.lhs, v.minv, precond);
 }
 
+// PCG loop kernel launch; with `pdl` the kernel may start while the previous
+// kernel in the stream drains (programmatic stream serialisation; the kernel
+// itself waits with pdl_wait before reading what that kernel writes).
+template <typename... KArgs, typename... Args>
+void launch_loop_kernel(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s, bool pdl, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Tile-kernel launches dispatch on the batch's tile size.
 #define HOBAK_TILE_LAUNCH(KERNEL, THREADS_PER_V, ...)                                   \
   do {                                                                                  \
@@ -841,15 +884,15 @@ void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s
 }
 
 template <typename T>
-void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
-  if (b.tileV == 64) k_spmv<64, T><<<b.ntiles, 3 * 64, 0, s>>>(b, v);
-  else k_spmv<128, T><<<b.ntiles, 3 * 128, 0, s>>>(b, v);
+void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl) {
+  if (b.tileV == 64) launch_loop_kernel(k_spmv<64, T>, b.ntiles, 3 * 64, s, pdl, b, v);
+  else launch_loop_kernel(k_spmv<128, T>, b.ntiles, 3 * 128, s, pdl, b, v);
 }
 
 template <typename T>
-void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
-  if (b.tileV == 64) k_update<64, T><<<b.ntiles, 3 * 64, 0, s>>>(b, v);
-  else k_update<128, T><<<b.ntiles, 3 * 128, 0, s>>>(b, v);
+void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl) {
+  if (b.tileV == 64) launch_loop_kernel(k_update<64, T>, b.ntiles, 3 * 64, s, pdl, b, v);
+  else launch_loop_kernel(k_update<128, T>, b.ntiles, 3 * 128, s, pdl, b, v);
 }
 
 void launch_refine(const DeviceBatch& b, cudaStream_t s) {
@@ -870,9 +913,9 @@ template void launch_diag_inverse<double>(const DeviceBatch&, const PcgVecs<doub
 template void launch_diag_inverse<float>(const DeviceBatch&, const PcgVecs<float>&, int, cudaStream_t);
 template void launch_inner_init<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t);
 template void launch_inner_init<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t);
-template void launch_spmv<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t);
-template void launch_spmv<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t);
-template void launch_update<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t);
-template void launch_update<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t);
+template void launch_spmv<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t, bool);
+template void launch_spmv<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t, bool);
+template void launch_update<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t, bool);
+template void launch_update<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t, bool);
 
 }  // namespace hobak

@@ -229,6 +229,14 @@ class BATCH:
     def __len__(self):
         return len(self._arrays)
 
+    @property
+    def total_vertices(self) -> int:
+        return int(sum(self.nv))
+
+    def offsets(self):
+        """First index of every scene in the whole-batch (3 * total vertices) vectors."""
+        return np.concatenate([[0], np.cumsum([3 * n for n in self.nv])])
+
     def step(self, nsteps: int = 1):
         stats = (HobakStepStats * len(self))()
         self.last_status = check(_lib.load().hobak_batch_step(self.h, nsteps, stats), "hobak_batch_step")
@@ -243,6 +251,24 @@ class BATCH:
         self.last_status = check(_lib.load().hobak_batch_wait(self.h, stats), "hobak_batch_wait")
         self.last_stats = [(s.iterations, s.converged, s.rel_residual, s.refinements) for s in stats]
         return self.last_stats
+
+    # ---- whole batch at once (scene order, 3 * total vertices) ----
+    def set_state_all(self, x: np.ndarray, v: np.ndarray):
+        """Enqueue the upload of every scene's displacement and velocity; the
+        arrays must stay unchanged until the next step/wait/get returns."""
+        self._pending_in = (x, v)  # keep the buffers alive until then
+        check(_lib.load().hobak_batch_set_state_all(self.h, dptr(x), dptr(v)), "hobak_batch_set_state_all")
+
+    def set_external_forces_all(self, f: np.ndarray):
+        self._pending_f = f
+        check(_lib.load().hobak_batch_set_external_forces_all(self.h, dptr(f)), "hobak_batch_set_external_forces_all")
+
+    def get_state_all(self, x: Optional[np.ndarray] = None, v: Optional[np.ndarray] = None):
+        n = 3 * self.total_vertices
+        x = np.empty(n) if x is None else x
+        v = np.empty(n) if v is None else v
+        check(_lib.load().hobak_batch_get_state_all(self.h, dptr(x), dptr(v)), "hobak_batch_get_state_all")
+        return x, v
 
     def query(self) -> bool:
         """True when the batch's enqueued steps have finished (non-blocking)."""

@@ -135,6 +135,14 @@ int hobak_batch_set_active(hobak_batch b, int scene, int active);
 /* Host <-> device state of one scene (3*nv doubles each; NULL skips). */
 int hobak_batch_set_state(hobak_batch b, int scene, const double* x, const double* v);
 int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v);
+/* Whole batch at once: every scene's 3*nv values back to back in scene
+ * order (total 3 * sum(nv)); one copy each.  The set calls are enqueued on
+ * the batch's stream and return at once: host buffers must stay unchanged
+ * until the next step, wait or get call returns (pageable buffers are copied
+ * before return).  get_state_all returns with the data on the host. */
+int hobak_batch_set_state_all(hobak_batch b, const double* x, const double* v);
+int hobak_batch_get_state_all(hobak_batch b, double* x, double* v);
+int hobak_batch_set_external_forces_all(hobak_batch b, const double* f);
 /* Replace the external force vector (3*nv) of one scene; the default is M g. */
 int hobak_batch_set_external_forces(hobak_batch b, int scene, const double* f);
 int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts);

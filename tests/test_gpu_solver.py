@@ -88,3 +88,26 @@ def test_zero_rhs_scene_stays_at_rest():
     x, v = b.get_state(0)
     assert np.abs(x).max() == 0.0 and np.abs(v).max() == 0.0
     assert st[0][1] == 1 and st[0][0] == 0
+
+
+def test_whole_batch_state_calls_match_per_scene_calls():
+    mix = scenes.config4_scenes(count=5, nmin=4, nmax=7)
+    b = hobak.BATCH(mix, hobak.solver_opts(precision=hobak.PRECISION_MIXED))
+    b.step(2)
+    x, v = b.get_state_all()
+    off = b.offsets()
+    for i in range(len(mix)):
+        xi, vi = b.get_state(i)
+        assert np.array_equal(x[off[i]:off[i + 1]], xi) and np.array_equal(v[off[i]:off[i + 1]], vi)
+    # a round trip through the whole-batch setters changes nothing
+    c = hobak.BATCH(mix, hobak.solver_opts(precision=hobak.PRECISION_MIXED))
+    c.set_state_all(x, v)
+    # f_ext = 0 everywhere through the whole-batch setter, on both batches
+    zero = np.zeros(3 * b.total_vertices)
+    b.set_external_forces_all(zero)
+    c.set_external_forces_all(zero)
+    b.step(3)
+    c.step(3)
+    xb, vb = b.get_state_all()
+    xc, vc = c.get_state_all()
+    assert np.array_equal(xb, xc) and np.array_equal(vb, vc)
