@@ -43,19 +43,23 @@ namespace {
 // tile size is an autotuned launch shape (DeviceBatch::tileV).
 
 // Fixed-order sum over the CTA; result valid in thread 0.  NT multiple of 32.
-// The warp tree runs in R (FP32 for the inner solve of the mixed path, which
-// keeps its dot products off the FP64 pipe), the sum over warps in FP64.
+// The whole tree runs in R (FP32 for the inner solve of the mixed path) and
+// only the CTA's total is widened to FP64: a conversion per warp costs a
+// 16-cycle issue on GB300's 2-lane FP64 pipe even when one lane uses it.
 template <int NT, typename R>
 __device__ __forceinline__ double block_sum(R v, double* sh) {
+  R* shr = reinterpret_cast<R*>(sh);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x / 32, l = threadIdx.x % 32;
-  if (l == 0) sh[w] = double(v);
+  if (l == 0) shr[w] = v;
   __syncthreads();
   double s = 0;
   if (threadIdx.x == 0) {
+    R t = R(0);
 #pragma unroll
-    for (int i = 0; i < NT / 32; i++) s += sh[i];
+    for (int i = 0; i < NT / 32; i++) t += shr[i];
+    s = double(t);
   }
   __syncthreads();
   return s;
@@ -65,6 +69,7 @@ __device__ __forceinline__ double block_sum(R v, double* sh) {
 // `sh` holds 2 * NT / 32 doubles.
 template <int NT, typename R>
 __device__ __forceinline__ void block_sum2(R a, R b, double* sh, double& sa, double& sb) {
+  R* shr = reinterpret_cast<R*>(sh);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -72,18 +77,21 @@ __device__ __forceinline__ void block_sum2(R a, R b, double* sh, double& sa, dou
   }
   const int w = threadIdx.x / 32, l = threadIdx.x % 32;
   if (l == 0) {
-    sh[w] = double(a);
-    sh[NT / 32 + w] = double(b);
+    shr[w] = a;
+    shr[NT / 32 + w] = b;
   }
   __syncthreads();
   sa = 0.0;
   sb = 0.0;
   if (threadIdx.x == 0) {
+    R ta = R(0), tb = R(0);
 #pragma unroll
     for (int i = 0; i < NT / 32; i++) {
-      sa += sh[i];
-      sb += sh[NT / 32 + i];
+      ta += shr[i];
+      tb += shr[NT / 32 + i];
     }
+    sa = double(ta);
+    sb = double(tb);
   }
   __syncthreads();
 }
@@ -126,6 +134,10 @@ __device__ __forceinline__ bool finite(double x) { return x == x && fabs(x) <= D
 // run.  Launched without the attribute, pdl_wait returns at once.
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// The update kernel puts 10 vertices (30 scalar rows) in each warp so that a
+// vertex's three rows share a warp: ceil(TV / 10) warps per tile.
+__host__ __device__ constexpr int update_warps(int TV) { return (TV + 9) / 10; }
 
 // x[pinned] = pin target at the start of a step
 // (applyKinematicConstraints, TIMESTEPPER.cpp:105-122).
@@ -597,14 +609,15 @@ __global__ void __launch_bounds__(3 * TV) k_spmv(DeviceBatch b, PcgVecs<T> v) {
 // gamma' = (r, u); |r|^2 -> stop when |r|^2 < threshold (ConjugateGradient.h:75-78).
 template <int TV, typename T>
 // One thread per scalar row (three times the threads of a per-vertex loop,
-// which a 40^3 scene needs to cover the GPU's latency); the 3x3 block of
-// Minv reads its vertex's three new residual rows from shared memory.
-__device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh, T* rsh,
+// which a 40^3 scene needs to cover the GPU's latency), 30 rows per warp; the
+// 3x3 block of Minv reads its vertex's three new residual rows by shuffles.
+__device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh,
                                             int* flag) {
   // before the dependency wait: what the previous kernel does not write
   const int s = b.tileScene[tile];
-  const int row = 3 * b.tileV0[tile] + threadIdx.x;
-  const bool valid = row < 3 * b.tileV1[tile];
+  const int lane = threadIdx.x % 32;
+  const int row = 3 * b.tileV0[tile] + 30 * (threadIdx.x / 32) + lane;
+  const bool valid = lane < 30 && row < 3 * b.tileV1[tile];
   T M0 = T(0), M1 = T(0), M2 = T(0);
   if (valid) {
     const T* M = v.minv + 3 * (size_t)row;  // row i of the vertex's block
@@ -639,24 +652,28 @@ __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<
     r[row] = rnew;
     rr = rnew * rnew;
   }
-  rsh[threadIdx.x] = rnew;
-  __syncthreads();
+  // the vertex's three new residual rows sit in lanes base..base+2 of this
+  // warp (10 vertices per warp): exchange them by shuffles, no barrier
+  const int base = lane - lane % 3;
+  const T ra = __shfl_sync(0xffffffffu, rnew, base);
+  const T rb = __shfl_sync(0xffffffffu, rnew, base + 1);
+  const T rc = __shfl_sync(0xffffffffu, rnew, base + 2);
   if (valid) {
-    const int base = threadIdx.x - threadIdx.x % 3;
-    const T ui = M0 * rsh[base] + M1 * rsh[base + 1] + M2 * rsh[base + 2];
+    const T ui = M0 * ra + M1 * rb + M2 * rc;
     v.u[row] = ui;
     ru = rnew * ui;
   }
+  constexpr int NT = 32 * update_warps(TV);
   double trr, tru;
-  block_sum2<3 * TV>(rr, ru, sh, trr, tru);
+  block_sum2<NT>(rr, ru, sh, trr, tru);
   if (threadIdx.x == 0) {
     b.partial[kPartials * tile] = trr;
     b.partial[kPartials * tile + 1] = tru;
   }
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketB, sp.ntiles, flag)) return;
-  const double srr = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 0, sh);
-  const double sru = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 1, sh);
+  const double srr = sum_partials<NT>(b.partial, sp.tile0, sp.ntiles, 0, sh);
+  const double sru = sum_partials<NT>(b.partial, sp.tile0, sp.ntiles, 1, sh);
   if (threadIdx.x == 0) {
     st.rr = srr;
     st.iters += 1;
@@ -687,13 +704,12 @@ __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<
 }
 
 template <int TV, typename T>
-__global__ void __launch_bounds__(3 * TV, TV == 64 ? 8 : 5) k_update(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[2 * 3 * TV / 32];
-  __shared__ T rsh[3 * TV];
+__global__ void __launch_bounds__(32 * update_warps(TV), TV == 64 ? 8 : 4) k_update(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[2 * update_warps(TV)];
   __shared__ int flag;
   pdl_trigger();
   const int tile = loop_tile(b);
-  if (tile >= 0) update_tile<TV, T>(b, v, tile, sh, rsh, &flag);
+  if (tile >= 0) update_tile<TV, T>(b, v, tile, sh, &flag);
 }
 
 // Compacted list of the tiles whose scene's inner PCG still runs, rebuilt at
@@ -891,8 +907,8 @@ void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool
 
 template <typename T>
 void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl) {
-  if (b.tileV == 64) launch_loop_kernel(k_update<64, T>, b.ntiles, 3 * 64, s, pdl, b, v);
-  else launch_loop_kernel(k_update<128, T>, b.ntiles, 3 * 128, s, pdl, b, v);
+  if (b.tileV == 64) launch_loop_kernel(k_update<64, T>, b.ntiles, 32 * update_warps(64), s, pdl, b, v);
+  else launch_loop_kernel(k_update<128, T>, b.ntiles, 32 * update_warps(128), s, pdl, b, v);
 }
 
 void launch_refine(const DeviceBatch& b, cudaStream_t s) {
