@@ -191,11 +191,12 @@ def plain_fp64_gpu(scene_list, steps):
     return steps / dt
 
 
-def serve_once(job_specs, arrivals, precision, budget_bytes):
+def serve_once(job_specs, arrivals, precision, budget_bytes, tuning=None):
     """Drive the continuous-batching server with jobs arriving at the given
     times (seconds from start).  Returns (wall seconds, jobs, server)."""
     from hobakv1_gb300 import serving
-    srv = serving.Server(budget_bytes, precision=precision, async_build=True, max_admit_per_tick=8)
+    srv = serving.Server(budget_bytes, precision=precision, async_build=True, max_admit_per_tick=8,
+                         tuning=tuning)
     jobs = [serving.Job(k, sc, n, contact) for k, (sc, n, contact) in enumerate(job_specs)]
     t0 = time.perf_counter()
     i = 0
@@ -226,6 +227,7 @@ def run_serving(args, spec, job_specs):
     gaps = rng.exponential(1.0, len(job_specs))
     total_steps = sum(n for _, n, _ in job_specs)
     budget = int(float(spec.get("budget_gb", 64)) * (1 << 30))
+    serve_tuning = None if args.cluster_pcg is None else {"cluster_pcg": args.cluster_pcg}
     # warm the library (module load, first graph capture) outside the timing
     serve_once(job_specs[:2], [0.0, 0.0], hobak.PRECISION_MIXED, budget)
     runs = {}
@@ -233,7 +235,7 @@ def run_serving(args, spec, job_specs):
     for prec_name, prec in (("mixed", hobak.PRECISION_MIXED), ("fp64", hobak.PRECISION_FP64)):
         for lam in spec["lambdas"]:
             arrivals = np.cumsum(gaps) / lam
-            wall, jobs, srv = serve_once(job_specs, arrivals, prec, budget)
+            wall, jobs, srv = serve_once(job_specs, arrivals, prec, budget, serve_tuning)
             step_ms = [ms for j in jobs for ms in j.step_ms]
             job_s = [j.finished - j.submitted for j in jobs]
             runs[f"{prec_name}@{lam}"] = {
@@ -261,7 +263,9 @@ def run_serving(args, spec, job_specs):
                        "contact": "even jobs: two SNH cubes, vertex-face eps 1e-3, stiffness 1e3, beta 1e-3",
                        "tets_total": int(sum(sc.nt for sc, _, _ in job_specs)), "pcg_tol": 1e-8,
                        "budget_gb": budget / (1 << 30),
-                       "timing": "wall clock from the first arrival to the last result on the host"},
+                       "timing": "wall clock from the first arrival to the last result on the host",
+                       "pcg_path": "cluster-resident for small contact-free scenes" if args.cluster_pcg
+                       else "tile path"},
             "serving": runs,
             "mixed_over_fp64_at_max_lambda": hi_m["job_steps_per_s"] / hi_f["job_steps_per_s"],
             "mixed_vs_fp64_rel_pos_err": {
@@ -351,6 +355,8 @@ def run_ours(args, spec, scene_list):
     stream = torch.cuda.ExternalStream(batch.stream_handle())
     # launch shapes (tile size, CTA sizes, PCG chunk) from the autotuner, on
     # this batch's data, before the warm-up; the state is left unchanged
+    if args.no_autotune and args.cluster_pcg is not None:
+        batch.set_tuning(cluster_pcg=args.cluster_pcg)
     tuning = batch.get_tuning() if args.no_autotune else batch.autotune(reps=3)
 
     # ---- device-resident timed region ----
@@ -480,6 +486,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the unbatched FP64 comparison on mixes")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--cluster-pcg", type=int, choices=[0, 1], default=None,
+                    help="PCG path of the serving cohorts (and of --no-autotune batches): 1 = cluster-resident")
     ap.add_argument("--eager", action="store_true",
                     help="launch kernels one by one instead of the step graph (for per-kernel profilers)")
     args = ap.parse_args()

@@ -84,6 +84,15 @@ struct hobak_batch_t {
   long long loopLaunchBase = 0;  // loop-body launches folded in before the last chunk change
   int chunk = 8;                 // PCG iterations per loop body (graph) or per host poll (eager)
   int ntilesCap = 0;             // tile tables are sized for the smallest tile size
+  // cluster-resident PCG (cluster_pcg.cu): on/off, the classes of the
+  // current precision, and whether any scene is left to the tile path
+  bool clusterPcg = false;
+  bool clusterDirty = true;
+  ClusterClass classes[kClusterClasses] = {};
+  int* clusterList = nullptr;  // device, nscenes ids grouped by class
+  bool anyTileScene = true;
+  cudaStream_t classStream[kClusterClasses] = {};  // classes run beside the tile path (fork/join)
+  cudaEvent_t evFork = nullptr, evJoin[kClusterClasses] = {};
   int lastStatus = HOBAK_OK;
   std::vector<SolveState> lastSolve;
   std::vector<int> hostRowptr, hostCols;
@@ -362,6 +371,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oTileS = A.reserve(sizeof(int) * ntilesCap), oTile0 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oTile1 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oLoopTiles = A.reserve(sizeof(int) * ntilesCap), oNLoop = A.reserve(sizeof(int));
+  const size_t oClusterList = A.reserve(sizeof(int) * n);
   const size_t oEH = A.reserve(sizeof(double) * kElemHess * (size_t)nt);
   const size_t oEHf = A.reserve(sizeof(float) * kElemHess * (size_t)nt);
   const size_t oEG = A.reserve(sizeof(double) * 12 * (size_t)nt);
@@ -423,6 +433,8 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.tileV0 = carve<int>(base, oTile0);
   d.tileV1 = carve<int>(base, oTile1);
   d.loopTiles = carve<int>(base, oLoopTiles);
+  d.nTileScenes = n;
+  B->clusterList = carve<int>(base, oClusterList);
   d.nLoopTiles = carve<int>(base, oNLoop);
   d.elemH = carve<double>(base, oEH);
   d.elemHf = carve<float>(base, oEHf);
@@ -505,7 +517,69 @@ int sweeps_of(const hobak_solver_opts& o) {
 long long fixed_launches(const hobak_batch_t* B) {
   const int sweeps = sweeps_of(B->opts);
   const bool mixed = B->opts.precision == HOBAK_PRECISION_MIXED;
-  return 6 + sweeps * (2 + (mixed ? 2 : 0));
+  int cl = 0;
+  for (const ClusterClass& c : B->classes) cl += c.count > 0 ? 1 : 0;
+  return 6 + sweeps * (1 + (B->anyTileScene ? 1 : 0) + cl + (mixed ? 2 : 0));
+}
+
+void drop_graphs(hobak_batch_t* B);
+
+// Which scenes solve their inner PCG in a thread-block cluster, and in how
+// large a one, for the current precision: scenes without contact, in the
+// smallest cluster (1, 2, 4, 8 or 16 CTAs) that gives each thread at most one
+// vertex; larger scenes (more than 16 x 1024 vertices) keep the tile path,
+// which spreads them wider.  The choice depends only on the scene itself, so
+// a scene takes the same path alone and in any batch.  Runs outside graph
+// capture (it uploads); drops the graphs when the assignment changed.
+int prepare_cluster_classes(hobak_batch_t* B) {
+  if (!B->clusterDirty) return HOBAK_OK;
+  if (const int ce = configure_cluster_pcg())
+    return fail(HOBAK_ERR_CUDA, std::string("cluster PCG set-up: ") + cudaGetErrorString((cudaError_t)ce));
+  const int n = (int)B->scenes.size();
+  const bool mixed = B->opts.precision == HOBAK_PRECISION_MIXED;
+  const int vpcLimit = (int)((kClusterSmemMax - cluster_fixed_bytes()) / cluster_vertex_bytes(mixed));
+  std::vector<int> cl(n, 0);
+  for (int s = 0; s < n; s++) {
+    const bool contact = B->collArena && s < (int)B->collScenes.size() && B->collScenes[s].vfOn;
+    if (!B->clusterPcg || contact) continue;
+    const int nv = B->scenes[s].nv;
+    int c = 1;
+    while (c < 16 && (nv + c - 1) / c > kClusterThreads) c *= 2;
+    const int vpc = (nv + c - 1) / c;
+    if (vpc <= kClusterThreads && vpc <= vpcLimit) cl[s] = c;  // one vertex per thread at most
+  }
+  std::vector<int> list;
+  bool changed = false;
+  int nTile = 0;
+  const int sizes[kClusterClasses] = {1, 2, 4, 8, 16};
+  for (int k = 0; k < kClusterClasses; k++) {
+    ClusterClass& c = B->classes[k];
+    c.count = 0;
+    c.vpcMax = 0;
+    c.scenes = B->clusterList + list.size();
+    for (int s = 0; s < n; s++)
+      if (cl[s] == sizes[k]) {
+        list.push_back(s);
+        c.count++;
+        c.vpcMax = std::max(c.vpcMax, (B->scenes[s].nv + sizes[k] - 1) / sizes[k]);
+      }
+  }
+  for (int s = 0; s < n; s++) {
+    if (B->sceneParams[s].pcgCluster != cl[s]) changed = true;
+    B->sceneParams[s].pcgCluster = cl[s];
+    if (cl[s] == 0) nTile++;
+  }
+  B->anyTileScene = nTile > 0;
+  if (B->d.nTileScenes != nTile) changed = true;
+  B->d.nTileScenes = nTile;
+  CUDA_TRY(cudaStreamSynchronize(B->stream));
+  if (!list.empty())
+    CUDA_TRY(cudaMemcpy(B->clusterList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(const_cast<SceneParams*>(B->d.scenes), B->sceneParams.data(), sizeof(SceneParams) * n,
+                      cudaMemcpyHostToDevice));
+  if (changed) drop_graphs(B);
+  B->clusterDirty = false;
+  return HOBAK_OK;
 }
 
 // One PCG chunk: the list of tiles still iterating, then `chunk` iterations
@@ -581,9 +655,25 @@ int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, c
   const int sweeps = sweeps_of(B->opts);
   for (int k = 0; k < sweeps; k++) {
     launch_set_active(d, s);
-    launch_inner_init<T>(d, v, s);
-    int rc = capture ? capture_pcg_loop<T>(B, s, v) : eager_pcg_loop<T>(B, s, v);
-    if (rc) return rc;
+    // cluster classes on their own streams, beside the tile path on `s`,
+    // joined before the refinement: small scenes solve while large ones
+    // iterate, and a class's long-running scenes do not hold up the others
+    int forked = 0;
+    for (int c = kClusterClasses - 1; c >= 0; c--) {
+      if (B->classes[c].count == 0) continue;
+      if (!forked++) CUDA_TRY(cudaEventRecord(B->evFork, s));
+      CUDA_TRY(cudaStreamWaitEvent(B->classStream[c], B->evFork, 0));
+      const int ce = launch_cluster_pcg<T>(d, v, B->classes, c, B->classStream[c]);
+      if (ce) return fail(HOBAK_ERR_CUDA, std::string("cluster PCG launch: ") + cudaGetErrorString((cudaError_t)ce));
+      CUDA_TRY(cudaEventRecord(B->evJoin[c], B->classStream[c]));
+    }
+    if (B->anyTileScene) {
+      launch_inner_init<T>(d, v, s);
+      int rc = capture ? capture_pcg_loop<T>(B, s, v) : eager_pcg_loop<T>(B, s, v);
+      if (rc) return rc;
+    }
+    for (int c = 0; c < kClusterClasses; c++)
+      if (B->classes[c].count) CUDA_TRY(cudaStreamWaitEvent(s, B->evJoin[c], 0));
     if (mixed) launch_refine(d, s);
   }
   if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[4], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
@@ -812,6 +902,7 @@ int build_collisions(hobak_batch_t* B) {
 int run_steps(hobak_batch_t* B, int nsteps) {
   cudaStream_t s = B->stream;
   const bool timed = B->timing;
+  if (int rc = prepare_cluster_classes(B)) return rc;
   for (int k = 0; k < nsteps; k++) {
     if (B->opts.use_graph) {
       int rc = ensure_step_graph(B, timed);
@@ -947,6 +1038,9 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
     hobak_default_solver_opts(&B->opts);
   CUDA_TRY(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
   CUDA_TRY(cudaStreamCreateWithFlags(&B->captureStream, cudaStreamNonBlocking));
+  for (auto& cs : B->classStream) CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreateWithFlags(&B->evFork, cudaEventDisableTiming));
+  for (auto& e : B->evJoin) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CUDA_TRY(cudaMallocHost(&B->pinnedActive, sizeof(int)));
   CUDA_TRY(cudaMallocHost(&B->solvePinned, sizeof(SolveState) * nscenes));
   for (auto& e : B->ev) CUDA_TRY(cudaEventCreate(&e));
@@ -967,6 +1061,11 @@ int hobak_batch_destroy(hobak_batch b) {
   if (b->collArena) cudaFree(b->collArena);
   drop_graphs(b);
   if (b->captureStream) cudaStreamDestroy(b->captureStream);
+  for (auto& cs : b->classStream)
+    if (cs) cudaStreamDestroy(cs);
+  if (b->evFork) cudaEventDestroy(b->evFork);
+  for (auto& e : b->evJoin)
+    if (e) cudaEventDestroy(e);
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
   if (b->pinnedActive) cudaFreeHost(b->pinnedActive);
@@ -1099,6 +1198,7 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   int rc = check_opts(opts);
   if (rc) return rc;
   b->opts = *opts;
+  b->clusterDirty = true;
   drop_graphs(b);
   return upload_solver_opts(b);
 }
@@ -1121,6 +1221,7 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
     if (!b->sceneParams[k].active) eff[k].vfOn = 0;
   CUDA_TRY(cudaMemcpy(const_cast<CollisionScene*>(b->d.coll.scenes), eff.data(), sizeof(CollisionScene) * eff.size(),
                       cudaMemcpyHostToDevice));
+  b->clusterDirty = true;
   drop_graphs(b);
   return HOBAK_OK;
 }
@@ -1285,8 +1386,10 @@ int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
   CUDA_TRY(cudaMemcpy(d.solve, st.data(), sizeof(SolveState) * n, cudaMemcpyHostToDevice));
   cudaEvent_t e0 = b->ev[0], e1 = b->ev[1];
   const bool mixed = b->opts.precision == HOBAK_PRECISION_MIXED;
-  launch_compact_tiles(d, s);  // every tile in the PCG loop kernels' list
-  b->launches += 1;
+  // every tile of every scene in the PCG loop kernels' mapping (also the
+  // scenes a cluster solves in the step: this times the tile-path kernels
+  // over the whole batch)
+  CUDA_TRY(cudaMemcpyAsync(d.nLoopTiles, &d.ntiles, sizeof(int), cudaMemcpyHostToDevice, s));
   for (int k = 0; k < 4; k++) {
     CUDA_TRY(cudaEventRecord(e0, s));
     for (int r = 0; r < reps; r++) {
@@ -1321,6 +1424,7 @@ int hobak_batch_get_tuning(hobak_batch b, hobak_tuning* out) {
   out->element_threads = b->d.elemThreads;
   out->assembly_threads = b->d.asmThreads;
   out->pcg_chunk = b->chunk;
+  out->cluster_pcg = b->clusterPcg ? 1 : 0;
   out->step_ms = 0.0;
   return HOBAK_OK;
 }
@@ -1334,6 +1438,7 @@ int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t) {
   if (t->pcg_chunk < 1 || t->pcg_chunk > 64) return fail(HOBAK_ERR_INVALID, "pcg_chunk must be in 1..64");
   if (t->tile_vertices != 64 && t->tile_vertices != 128)
     return fail(HOBAK_ERR_INVALID, "tile_vertices must be 64 or 128");
+  if (t->cluster_pcg != 0 && t->cluster_pcg != 1) return fail(HOBAK_ERR_INVALID, "cluster_pcg must be 0 or 1");
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   if (t->tile_vertices != b->d.tileV) {
     const int rc = apply_tile_size(b, t->tile_vertices);
@@ -1346,6 +1451,10 @@ int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t) {
   }
   b->d.elemThreads = t->element_threads;
   b->d.asmThreads = t->assembly_threads;
+  if ((t->cluster_pcg != 0) != b->clusterPcg) {
+    b->clusterPcg = t->cluster_pcg != 0;
+    b->clusterDirty = true;
+  }
   drop_graphs(b);
   return HOBAK_OK;
 }
@@ -1439,11 +1548,14 @@ int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out) {
     }
     d.asmThreads = best.assembly_threads;
   }
-  // 3. whole steps per (tile size, chunk), each from the saved state
+  // 3. whole steps per (cluster-resident PCG on/off, tile size, chunk), each
+  //    from the saved state
   double bestStep = 1e300;
   hobak_tuning trial = best;
+  for (int cp : {0, 1})
   for (int tv : {64, 128})
     for (int ch : {4, 8, 16}) {
+      trial.cluster_pcg = cp;
       trial.tile_vertices = tv;
       trial.pcg_chunk = ch;
       int rc = hobak_batch_set_tuning(b, &trial);
@@ -1462,6 +1574,7 @@ int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out) {
       }
       if (total < bestStep) {
         bestStep = total;
+        best.cluster_pcg = cp;
         best.tile_vertices = tv;
         best.pcg_chunk = ch;
       }

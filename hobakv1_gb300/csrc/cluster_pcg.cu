@@ -1,0 +1,370 @@
+// Cluster-resident PCG for small scenes.
+//
+// One thread-block cluster solves one scene's inner PCG from start to finish
+// in a single launch: the scene's vertices are split into CL contiguous
+// ranges, one per CTA; the Krylov vectors of a range live in that CTA's
+// shared memory, the SpMV gathers the search vector of neighbouring ranges
+// from the other CTAs' shared memory (distributed shared memory), and every
+// dot product is a CTA tree followed by a fixed-order sum of the CL CTA
+// partials read through distributed shared memory.  An iteration is two
+// cluster barriers; the matrix and Minv stay in L2 across iterations.  The
+// tile path (solver.cu: two grid-wide kernels per iteration, each ending in
+// a ticketed reduction) remains for scenes too large for a cluster and for
+// scenes with contact.
+//
+// The iteration is the same Chronopoulos-Gear PCG as the tile path, with the
+// same scalars, stopping rules and iteration accounting (ConjugateGradient.h
+// stopping rule; the FP64 path's verdict from the recursive residual), so the
+// two paths agree to rounding.  Thread 0 of every CTA computes the scalars
+// from the same partials in the same order, hence every CTA takes the same
+// branches and reaches every barrier.
+#include <cooperative_groups.h>
+
+#include <cfloat>
+
+#include "kernels.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace hobak {
+
+namespace {
+
+__device__ __forceinline__ bool finite_d(double x) { return x == x && fabs(x) <= DBL_MAX; }
+
+// Shared memory of one CTA: [slots: 8 doubles][warp partials: 2 * kClusterWarps T]
+// [u, p, s, w, d, r: 3 * vpc T each].
+constexpr int kSlotBytes = 8 * sizeof(double) + 2 * kClusterWarps * sizeof(double);
+
+template <typename T>
+struct ClusterSmem {
+  double* slots;  // [1] |r|^2, [2] (r, u), [3] delta (a barrier separates reuse)
+  T* warp;        // 2 * kClusterWarps
+  T *u, *p, *s, *w, *d, *r;
+};
+
+template <typename T>
+__device__ __forceinline__ ClusterSmem<T> carve_smem(unsigned char* base, int vpc) {
+  ClusterSmem<T> m;
+  m.slots = reinterpret_cast<double*>(base);
+  m.warp = reinterpret_cast<T*>(base + 8 * sizeof(double));
+  T* v = reinterpret_cast<T*>(base + kSlotBytes);
+  const int n = 3 * vpc;
+  m.u = v;
+  m.p = v + n;
+  m.s = v + 2 * n;
+  m.w = v + 3 * n;
+  m.d = v + 4 * n;
+  m.r = v + 5 * n;
+  return m;
+}
+
+// Sum over the CTA in T (fixed tree), written by thread 0 into this CTA's
+// slots as FP64, then a cluster barrier; thread 0 then adds the CL CTAs'
+// slots in rank order (sa, sb are valid in thread 0 only).  The scalar
+// recurrences that follow run in thread 0 alone and reach the other threads
+// through shared memory: 1024 threads redoing FP64 divisions would occupy
+// GB300's 2-lane FP64 pipe for tens of microseconds per iteration.
+template <int CL, typename T>
+__device__ __forceinline__ void cluster_sum2(cg::cluster_group& cluster, const ClusterSmem<T>& m, T a, T b,
+                                             int slot, double& sa, double& sb) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (lane == 0) {
+    m.warp[wid] = a;
+    m.warp[kClusterWarps + wid] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T ta = T(0), tb = T(0);
+#pragma unroll
+    for (int i = 0; i < kClusterWarps; i++) {
+      ta += m.warp[i];
+      tb += m.warp[kClusterWarps + i];
+    }
+    m.slots[slot] = double(ta);
+    m.slots[slot + 1] = double(tb);
+  }
+  cluster.sync();
+  sa = 0.0;
+  sb = 0.0;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int rnk = 0; rnk < CL; rnk++) {
+      const double* rs = cluster.map_shared_rank(m.slots, rnk);
+      sa += rs[slot];
+      sb += rs[slot + 1];
+    }
+  }
+}
+
+// Values thread 0 hands to the CTA after each reduction.
+template <typename T>
+struct Broadcast {
+  T alpha, beta;
+  int stop;
+};
+
+template <int CL, typename T>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
+    k_pcg_cluster(DeviceBatch b, PcgVecs<T> v, const int* __restrict__ sceneList) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int sc = sceneList[blockIdx.x / CL];
+  SolveState& st = b.solve[sc];
+  const SceneParams& sp = b.scenes[sc];
+  const bool t0 = threadIdx.x == 0;
+  const bool lead = rank == 0 && t0;
+  // a finished or parked scene: nothing to solve (same for every CTA)
+  if (st.outerDone) {
+    if (lead) st.done = 1;
+    return;
+  }
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ Broadcast<T> bc;
+  const int v0 = sp.v0, nvS = sp.nv;
+  const int vpc = (nvS + CL - 1) / CL;  // the scene's own split: alone == in any batch
+  const float rvpc = 1.0f / float(vpc);
+  const ClusterSmem<T> m = carve_smem<T>(smem, vpc);
+  const int my0 = min(nvS, rank * vpc), my1 = min(nvS, (rank + 1) * vpc);
+  const int nmine = my1 - my0;
+
+  // ---- init: r = rhs - A y (FP64, converted), u = Minv r, d = p = s = 0 ----
+  T rr = T(0), ru = T(0);
+  for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
+    const int u = v0 + my0 + lv;
+    T r3[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      r3[i] = T(b.r64[3 * u + i]);
+      m.r[3 * lv + i] = r3[i];
+      m.d[3 * lv + i] = T(0);
+      m.p[3 * lv + i] = T(0);
+      m.s[3 * lv + i] = T(0);
+      rr += r3[i] * r3[i];
+    }
+    const T* M = v.minv + 9 * (size_t)u;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
+      m.u[3 * lv + i] = ui;
+      ru += r3[i] * ui;
+    }
+  }
+  double srr, sru;
+  cluster_sum2<CL, T>(cluster, m, rr, ru, 1, srr, sru);
+  // the scene's scalar state, kept by thread 0 of every CTA (identical copies)
+  double innerThr = 0.0, gamma = 0.0, gammaOld = 1.0, alpha = 1.0, beta = 0.0;
+  int maxit = 0, totalIters = 0, iters = 0, converged = 0, outerDone = 0;
+  if (t0) {
+    double itol = st.tol;
+    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr, DBL_MIN)), 1e-5);
+    innerThr = fmax(itol * itol * srr, DBL_MIN);
+    maxit = st.maxit;
+    totalIters = st.totalIters;
+    converged = st.converged;
+    gamma = sru;
+    bc.stop = (srr == 0.0 || srr < innerThr) ? 1 : 0;
+  }
+  __syncthreads();
+  while (!bc.stop) {
+    // ---- w = A u over my vertices; delta = (w, u) ----
+    T dl = T(0);
+    for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
+      const int u = v0 + my0 + lv;
+      T a0 = T(0), a1 = T(0), a2 = T(0);
+      const int k0 = b.rowptr[u], k1 = b.rowptr[u + 1];
+      // four blocks per trip, their column indices fetched one trip ahead;
+      // the owning CTA of a column from a float reciprocal (corrected by one
+      // step) instead of an integer division
+      int wn[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) wn[q] = (k0 + q < k1) ? __ldg(&b.cols[k0 + q]) - v0 : 0;
+      for (int k = k0; k < k1; k += 4) {
+        int wl[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          wl[q] = wn[q];
+          wn[q] = (k + 4 + q < k1) ? __ldg(&b.cols[k + 4 + q]) - v0 : 0;
+        }
+        T x[4][3];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          int owner = min(CL - 1, (int)(float(wl[q]) * rvpc));
+          if (owner * vpc > wl[q]) owner--;
+          else if ((owner + 1) * vpc <= wl[q]) owner++;
+          const T* uw = (owner == rank ? m.u : cluster.map_shared_rank(m.u, owner)) + 3 * (wl[q] - owner * vpc);
+#pragma unroll
+          for (int i = 0; i < 3; i++) x[q][i] = (k + q < k1) ? uw[i] : T(0);
+        }
+        const T* B = v.lhs + 9 * (size_t)k;  // row major 3x3 blocks
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (k + q < k1) {
+            const T* Bq = B + 9 * q;
+            a0 = fma(Bq[0], x[q][0], fma(Bq[1], x[q][1], fma(Bq[2], x[q][2], a0)));
+            a1 = fma(Bq[3], x[q][0], fma(Bq[4], x[q][1], fma(Bq[5], x[q][2], a1)));
+            a2 = fma(Bq[6], x[q][0], fma(Bq[7], x[q][1], fma(Bq[8], x[q][2], a2)));
+          }
+        }
+      }
+      m.w[3 * lv] = a0;
+      m.w[3 * lv + 1] = a1;
+      m.w[3 * lv + 2] = a2;
+      dl += a0 * m.u[3 * lv] + a1 * m.u[3 * lv + 1] + a2 * m.u[3 * lv + 2];
+    }
+    double delta, unused;
+    cluster_sum2<CL, T>(cluster, m, dl, T(0), 3, delta, unused);
+    if (t0) {
+      if (iters == 0) {
+        beta = 0.0;
+        alpha = gamma / delta;
+      } else {
+        beta = gamma / gammaOld;
+        alpha = gamma / (delta - beta * gamma / alpha);
+      }
+      bc.alpha = T(alpha);
+      bc.beta = T(beta);
+    }
+    __syncthreads();
+    const T ta = bc.alpha, tb = bc.beta;
+    // ---- p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s, u = Minv r ----
+    rr = T(0);
+    ru = T(0);
+    for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
+      const int u = v0 + my0 + lv;
+      T r3[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const int j = 3 * lv + i;
+        const T p = m.u[j] + tb * m.p[j];
+        const T sv = m.w[j] + tb * m.s[j];
+        m.p[j] = p;
+        m.s[j] = sv;
+        m.d[j] += ta * p;
+        r3[i] = m.r[j] - ta * sv;
+        m.r[j] = r3[i];
+        rr += r3[i] * r3[i];
+      }
+      const T* M = v.minv + 9 * (size_t)u;
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
+        m.u[3 * lv + i] = ui;
+        ru += r3[i] * ui;
+      }
+    }
+    // the cluster barrier inside also publishes the new u to the other CTAs
+    cluster_sum2<CL, T>(cluster, m, rr, ru, 1, srr, sru);
+    if (t0) {
+      iters += 1;
+      totalIters += 1;
+      int stop = 0;
+      if (srr < innerThr) {
+        stop = 1;
+      } else if (!finite_d(srr) || !finite_d(sru) || !finite_d(alpha)) {
+        stop = 1;
+        converged = -1;
+        outerDone = 1;
+      } else {
+        gammaOld = gamma;
+        gamma = sru;
+        if (totalIters >= maxit) stop = 1;
+      }
+      bc.stop = stop;
+    }
+    __syncthreads();
+  }
+  // ---- results: the correction d (FP64 path: the solution y itself) ----
+  for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
+    const int u = v0 + my0 + lv;
+#pragma unroll
+    for (int i = 0; i < 3; i++) v.d[3 * u + i] = m.d[3 * lv + i];
+  }
+  if (lead) {
+    st.rr = srr;
+    st.iters = iters;
+    st.totalIters = totalIters;
+    st.gamma = gamma;
+    st.gammaOld = gammaOld;
+    st.alpha = alpha;
+    st.beta = beta;
+    st.innerThreshold = innerThr;
+    st.done = 1;
+    if (outerDone) {
+      st.converged = converged;
+      st.outerDone = 1;
+    } else if (sizeof(T) == sizeof(double)) {
+      // FP64 path: the recursive residual is the solver's verdict (Eigen)
+      st.rr64 = srr;
+      st.converged = srr < st.threshold ? 1 : 0;
+      st.outerDone = 1;
+    }
+  }
+  // no CTA leaves while another may still read its shared memory
+  cluster.sync();
+}
+
+template <int CL, typename T>
+int launch_class(const DeviceBatch& b, const PcgVecs<T>& v, const ClusterClass& c, cudaStream_t s) {
+  if (c.count == 0) return 0;
+  const size_t smem = kSlotBytes + (size_t)18 * c.vpcMax * sizeof(T);
+  k_pcg_cluster<CL, T><<<c.count * CL, kClusterThreads, smem, s>>>(b, v, c.scenes);
+  return 0;
+}
+
+template <int CL, typename T>
+cudaError_t allow_smem() {
+  cudaError_t e = cudaFuncSetAttribute(k_pcg_cluster<CL, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kClusterSmemMax);
+  if (e == cudaSuccess && CL > 8)  // 16-CTA clusters are a non-portable size
+    e = cudaFuncSetAttribute(k_pcg_cluster<CL, T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+}  // namespace
+
+// Opt every cluster kernel into kClusterSmemMax bytes of dynamic shared
+// memory (once per process; outside any stream capture).
+int configure_cluster_pcg() {
+  static int done = 0;
+  if (done) return 0;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = allow_smem<1, float>();
+  if (e == cudaSuccess) e = allow_smem<2, float>();
+  if (e == cudaSuccess) e = allow_smem<4, float>();
+  if (e == cudaSuccess) e = allow_smem<8, float>();
+  if (e == cudaSuccess) e = allow_smem<16, float>();
+  if (e == cudaSuccess) e = allow_smem<1, double>();
+  if (e == cudaSuccess) e = allow_smem<2, double>();
+  if (e == cudaSuccess) e = allow_smem<4, double>();
+  if (e == cudaSuccess) e = allow_smem<8, double>();
+  if (e == cudaSuccess) e = allow_smem<16, double>();
+  if (e != cudaSuccess) return (int)e;
+  done = 1;
+  return 0;
+}
+
+size_t cluster_vertex_bytes(bool mixed) { return (size_t)18 * (mixed ? sizeof(float) : sizeof(double)); }
+size_t cluster_fixed_bytes() { return kSlotBytes; }
+
+template <typename T>
+int launch_cluster_pcg(const DeviceBatch& b, const PcgVecs<T>& v, const ClusterClass* classes, int k, cudaStream_t s) {
+  switch (k) {
+    case 0: return launch_class<1, T>(b, v, classes[0], s);
+    case 1: return launch_class<2, T>(b, v, classes[1], s);
+    case 2: return launch_class<4, T>(b, v, classes[2], s);
+    case 3: return launch_class<8, T>(b, v, classes[3], s);
+    default: return launch_class<16, T>(b, v, classes[4], s);
+  }
+}
+template int launch_cluster_pcg<double>(const DeviceBatch&, const PcgVecs<double>&, const ClusterClass*, int,
+                                        cudaStream_t);
+template int launch_cluster_pcg<float>(const DeviceBatch&, const PcgVecs<float>&, const ClusterClass*, int,
+                                       cudaStream_t);
+
+}  // namespace hobak

@@ -38,6 +38,7 @@ struct SceneParams {
   int tile0, ntiles;   // PCG tile range
   int kind;            // material
   int active;          // 0: the scene is parked (serving) and every kernel skips it
+  int pcgCluster;      // > 0: the inner PCG runs in a cluster of this many CTAs (cluster_pcg.cu)
   double mu, lambda, alpha;  // reparameterised material constants
   double dt;
 };

@@ -20,6 +20,18 @@ struct PcgVecs {
   T* d;     // inner solution (the correction)
 };
 
+// Cluster-resident PCG (cluster_pcg.cu): scenes solved by clusters of
+// 1, 2, 4, 8 or 16 CTAs of kClusterThreads threads (one vertex per thread).
+constexpr int kClusterThreads = 1024;
+constexpr int kClusterWarps = kClusterThreads / 32;
+constexpr int kClusterClasses = 5;           // cluster sizes 1, 2, 4, 8, 16
+constexpr int kClusterSmemMax = 200 * 1024;  // dynamic shared memory per CTA, at most
+struct ClusterClass {
+  int count;          // scenes of this cluster size
+  int vpcMax;         // largest vertices per CTA among them (shared-memory sizing)
+  const int* scenes;  // device list of their scene ids
+};
+
 // Device pointers of one packed batch.  Plain struct passed by value.
 struct DeviceBatch {
   int nscenes, nv, nt, nblocks, ntiles;
@@ -30,6 +42,7 @@ struct DeviceBatch {
   // (k_compact_tiles)
   int* loopTiles;
   int* nLoopTiles;
+  int nTileScenes;  // scenes whose inner PCG runs on the tile path (the rest: clusters)
   const SceneParams* scenes;
   SolveState* solve;
   int* active;  // scenes whose inner PCG is still running
@@ -121,5 +134,16 @@ void launch_material_eval(int kind, double mu, double lambda, int n, const doubl
 void launch_element_eval(int nt, const int4* tets, const double* rest, const double* x, const double* DmInv,
                          const double* vol, int kind, double mu, double lambda, double* F, double* sigma,
                          double* force, double* hessian, cudaStream_t s);
+
+// Inner PCG of every scene of cluster class k (classes[0..4]: cluster sizes
+// 1, 2, 4, 8, 16).  Returns a cudaError_t value (0 on success).
+template <typename T>
+int launch_cluster_pcg(const DeviceBatch& b, const PcgVecs<T>& v, const ClusterClass* classes, int k,
+                       cudaStream_t s);
+// Dynamic shared-memory opt-in of the cluster kernels (once, outside capture).
+int configure_cluster_pcg();
+// Shared memory a cluster CTA needs: fixed part + per-vertex part.
+size_t cluster_vertex_bytes(bool mixed);
+size_t cluster_fixed_bytes();
 
 }  // namespace hobak

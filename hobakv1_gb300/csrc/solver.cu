@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(TV) k_rhs(DeviceBatch b) {
 }
 
 __global__ void k_set_active(DeviceBatch b) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *b.active = b.nscenes;
+  if (threadIdx.x == 0 && blockIdx.x == 0) *b.active = b.nTileScenes;  // cluster scenes never count
 }
 
 // Start of one inner solve on r_T = (T) r64: d = 0, p = s = 0, u = Minv r,
@@ -428,6 +428,7 @@ __global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) 
   const int s = b.tileScene[tile];
   SolveState& st = b.solve[s];
   const SceneParams& sp = b.scenes[s];
+  if (sp.pcgCluster) return;  // solved by its cluster, concurrently (cluster_pcg.cu)
   if (st.outerDone) {
     // this scene's solve is over: mark the inner solve done once
     if (tile == sp.tile0 && threadIdx.x == 0) {
@@ -722,7 +723,7 @@ __global__ void __launch_bounds__(1024) k_compact_tiles(DeviceBatch b) {
   const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
   for (int base = 0; base < b.nscenes; base += 1024) {
     const int s = base + threadIdx.x;
-    const int cnt = (s < b.nscenes && !b.solve[s].done) ? b.scenes[s].ntiles : 0;
+    const int cnt = (s < b.nscenes && !b.solve[s].done && !b.scenes[s].pcgCluster) ? b.scenes[s].ntiles : 0;
     int x = cnt;  // inclusive scan in the warp
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {

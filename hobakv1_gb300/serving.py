@@ -69,9 +69,11 @@ class Job:
 
 
 class Cohort:
-    def __init__(self, jobs: List[Job], opts):
+    def __init__(self, jobs: List[Job], opts, tuning: Optional[dict] = None):
         self.jobs = jobs
         self.batch = hobak.BATCH([j.scene for j in jobs], opts)
+        if tuning:
+            self.batch.set_tuning(**tuning)
         for k, j in enumerate(jobs):
             j.cohort, j.slot = self, k
             if j.collisions is not None:
@@ -89,9 +91,11 @@ class Server:
     """Continuous batching under a device-memory budget."""
 
     def __init__(self, budget_bytes: int, precision: int = hobak.PRECISION_MIXED,
-                 max_admit_per_tick: int = 64, keep_results: bool = True, async_build: bool = False):
+                 max_admit_per_tick: int = 64, keep_results: bool = True, async_build: bool = False,
+                 tuning: Optional[dict] = None):
         self.budget = int(budget_bytes)
         self.opts = hobak.solver_opts(precision=precision)
+        self.tuning = tuning  # launch shapes for every cohort (hobak_batch_set_tuning)
         self.max_admit = max_admit_per_tick
         self.keep_results = keep_results
         self.queue: Deque[Job] = deque()
@@ -147,9 +151,9 @@ class Server:
             return
         self.used += est  # reserved until the cohort reports its real size
         if self._pool is None:
-            self._join(Cohort(take, self.opts), est)
+            self._join(Cohort(take, self.opts, self.tuning), est)
         else:
-            self._building.append((self._pool.submit(Cohort, take, self.opts), est))
+            self._building.append((self._pool.submit(Cohort, take, self.opts, self.tuning), est))
             if not self.cohorts:
                 self._collect_built(block=True)
 

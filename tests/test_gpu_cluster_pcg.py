@@ -1,0 +1,75 @@
+"""Cluster-resident PCG (one thread-block cluster per small scene, vectors in
+distributed shared memory, running beside the tile path) against the tile
+path and the oracle."""
+import numpy as np
+import pytest
+
+from hobakv1_gb300 import hobak, scenes
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def run(scene_list, precision, steps, cluster, precond=hobak.PRECOND_BLOCK_JACOBI):
+    b = hobak.BATCH(scene_list, hobak.solver_opts(precision=precision, preconditioner=precond))
+    b.set_tuning(cluster_pcg=int(cluster))
+    st = b.step(steps)
+    out = [b.get_state(i)[0] + s.rest.reshape(-1) for i, s in enumerate(scene_list)]
+    b.close()
+    return out, st
+
+
+@pytest.mark.parametrize("precision", [hobak.PRECISION_FP64, hobak.PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_cluster_path_matches_tile_path(precision):
+    # scene sizes that land in clusters of 1, 2, 4, 8 and 16 CTAs
+    mix = scenes.config4_scenes(count=10, nmin=5, nmax=24)
+    xc, stc = run(mix, precision, 6, True)
+    xt, stt = run(mix, precision, 6, False)
+    bound = 1e-8 if precision == hobak.PRECISION_FP64 else 1e-6
+    for k in range(len(mix)):
+        assert rel(xc[k], xt[k]) < bound, (k, mix[k].nv, rel(xc[k], xt[k]))
+        assert stc[k][1] == 1 and abs(stc[k][0] - stt[k][0]) <= 2, (stc[k], stt[k])
+
+
+def test_cluster_path_matches_oracle_with_jacobi_iterations():
+    s = scenes.config1_scene(10)  # 1,331 vertices: a two-CTA cluster
+    b = hobak.BATCH([s], hobak.solver_opts(preconditioner=hobak.PRECOND_JACOBI))
+    b.set_tuning(cluster_pcg=1)
+    sim = oracle.Sim(s, precond=0)
+    for _ in range(5):
+        st = b.step(1)
+        it, _ = sim.step(1)
+        assert abs(st[0][0] - int(it[0])) <= 1, (st[0], it)
+    x, _ = b.get_state(0)
+    xo, _ = sim.state()
+    assert rel(x + s.rest.reshape(-1), xo + s.rest.reshape(-1)) < 1e-10
+
+
+@pytest.mark.parametrize("precision", [hobak.PRECISION_FP64, hobak.PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_large_and_small_scenes_share_a_batch(precision):
+    """A scene too large for a cluster takes the tile path while the small
+    ones solve in clusters beside it; each result equals the scene alone."""
+    big = scenes.config2_scene(30, "snh")  # 29,791 vertices: more than 16 x 1024
+    small = scenes.config4_scenes(count=3, nmin=6, nmax=12)
+    together, _ = run([big] + small, precision, 4, True)
+    for k, sc in enumerate([big] + small):
+        alone, _ = run([sc], precision, 4, True)
+        assert np.array_equal(together[k], alone[0]), k
+
+
+def test_contact_scene_keeps_the_tile_path_beside_clusters():
+    two = scenes.two_cubes_scene(5)
+    small = scenes.config4_scenes(count=2, nmin=5, nmax=8)
+    b = hobak.BATCH([two] + small, hobak.solver_opts(precision=hobak.PRECISION_MIXED))
+    b.set_tuning(cluster_pcg=1)
+    b.set_collisions(0, True, 1e-3, 1e3, 0.001)
+    b.step(4)
+    a = hobak.BATCH([two], hobak.solver_opts(precision=hobak.PRECISION_MIXED))
+    a.set_tuning(cluster_pcg=1)
+    a.set_collisions(0, True, 1e-3, 1e3, 0.001)
+    a.step(4)
+    assert np.array_equal(b.get_state(0)[0], a.get_state(0)[0])
