@@ -220,7 +220,9 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   deformation_gradient(X, Dinv, F);
   svd3_rv_fast(F, U, S, V);
   material_pk1(m, F, U, V, P);
-  element_force(P, Dinv, vol, f);
+  // dt f directly (the force scaled by dt * vol instead of vol); raw forces
+  // for inspection have dt = 0 and keep the plain vol
+  element_force(P, Dinv, rawForces ? vol : dt * vol, f);
 
   HT Hr[45];
   reduced_hessian<HT>(m, U, S, V, Dinv, Hr);
@@ -238,19 +240,22 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
 #pragma unroll
       for (int i = 0; i < 3; i++) dv[3 * a + i] = HT(b.v[3 * vid[a + 1] + i] - v0[i]);
   }
+  // g = dt f + dt^2 He v: the He v rows carry the factor -vol dt^2 in HT
+  // (one conversion and one add per entry on the FP64 pipe)
   double* g = b.elemG + 12 * (size_t)t;
-  double h0[3] = {0.0, 0.0, 0.0};
+  const HT ch = HT(-vol * dt * dt);
+  HT h0[3] = {HT(0), HT(0), HT(0)};
 #pragma unroll
   for (int r = 0; r < 9; r++) {
     HT s = HT(0);
 #pragma unroll
     for (int c = 0; c < 9; c++) s += ((r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)]) * dv[c];
-    const double hv = -vol * double(s);
-    h0[r % 3] += hv;
-    g[3 + r] = rawForces ? f[3 + r] : dt * (f[3 + r] + dt * hv);
+    s *= ch;
+    h0[r % 3] += s;
+    g[3 + r] = f[3 + r] + double(s);
   }
 #pragma unroll
-  for (int i = 0; i < 3; i++) g[i] = rawForces ? f[i] : dt * (f[i] - dt * h0[i]);
+  for (int i = 0; i < 3; i++) g[i] = f[i] - double(h0[i]);
 
   expand_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
 }
