@@ -292,6 +292,29 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   }
   const int nblocks = rowptr[nv];
   B->nblocks = nblocks;
+  // sliced LHS storage: 32-vertex slices, each as many slot rows as its
+  // longest block row (lhs_slot)
+  const int nslices = (nv + kSlice - 1) / kSlice;
+  std::vector<int> sliceRow(nslices + 1, 0), slotSlice, colS;
+  for (int sl = 0; sl < nslices; sl++) {
+    int len = 0;
+    for (int u = kSlice * sl; u < std::min(nv, kSlice * (sl + 1)); u++) len = std::max(len, rowptr[u + 1] - rowptr[u]);
+    sliceRow[sl + 1] = sliceRow[sl] + len;
+  }
+  const int nslotRows = sliceRow[nslices];
+  slotSlice.resize(nslotRows);
+  for (int sl = 0; sl < nslices; sl++)
+    for (int r = sliceRow[sl]; r < sliceRow[sl + 1]; r++) slotSlice[r] = sl;
+  colS.resize((size_t)nslotRows * kSlice);
+  for (int u = 0; u < nv; u++) {
+    const int r0 = sliceRow[u / kSlice], lane = u % kSlice;
+    for (int r = r0; r < sliceRow[u / kSlice + 1]; r++) {
+      const int j = r - r0;
+      colS[(size_t)r * kSlice + lane] = j < rowptr[u + 1] - rowptr[u] ? cols[rowptr[u] + j] : u;
+    }
+  }
+  for (int u = nv; u < nslices * kSlice; u++)  // lanes past the last vertex
+    for (int r = sliceRow[u / kSlice]; r < sliceRow[u / kSlice + 1]; r++) colS[(size_t)r * kSlice + u % kSlice] = 0;
   blkRow.resize(nblocks);
   for (int u = 0; u < nv; u++)
     for (int k = rowptr[u]; k < rowptr[u + 1]; k++) blkRow[k] = u;
@@ -368,6 +391,11 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oBlkRow = A.reserve(sizeof(int) * nblocks), oBlkptr = A.reserve(sizeof(int) * (nblocks + 1));
   const size_t oBlksrc = A.reserve(sizeof(int) * 16 * (size_t)nt);
   const size_t oVtxptr = A.reserve(sizeof(int) * (nv + 1)), oVtxinc = A.reserve(sizeof(int) * 4 * (size_t)nt);
+  const size_t oSliceRow = A.reserve(sizeof(int) * (nslices + 1)), oSlotSlice = A.reserve(sizeof(int) * nslotRows);
+  const size_t oColS = A.reserve(sizeof(int) * kSlice * (size_t)nslotRows);
+  // sliced LHS values; the FP64 one also serves as CSR scratch for the
+  // inspection call (hobak_batch_assemble)
+  const size_t lhsVals = std::max((size_t)kSlotVals * nslotRows, 9 * (size_t)nblocks);
   const size_t oTileS = A.reserve(sizeof(int) * ntilesCap), oTile0 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oTile1 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oLoopTiles = A.reserve(sizeof(int) * ntilesCap), oNLoop = A.reserve(sizeof(int));
@@ -377,12 +405,12 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oEG = A.reserve(sizeof(double) * 12 * (size_t)nt);
   const size_t oRhs = A.reserve(V3), oY = A.reserve(V3), oR64 = A.reserve(V3);
   // FP64 inner solve (r = r64, d = y)
-  const size_t oLhs = A.reserve(sizeof(double) * 9 * (size_t)nblocks);
+  const size_t oLhs = A.reserve(sizeof(double) * lhsVals);
   const size_t oMinv = A.reserve(sizeof(double) * 9 * (size_t)nv);
   const size_t oU = A.reserve(V3), oP = A.reserve(V3), oS = A.reserve(V3), oW = A.reserve(V3);
   // FP32 inner solve (mixed precision)
   const size_t F3 = 3 * (size_t)nv * sizeof(float);
-  const size_t oLhsF = A.reserve(sizeof(float) * 9 * (size_t)nblocks);
+  const size_t oLhsF = A.reserve(sizeof(float) * kSlotVals * (size_t)nslotRows);
   const size_t oMinvF = A.reserve(sizeof(float) * 9 * (size_t)nv);
   const size_t oRF = A.reserve(F3), oUF = A.reserve(F3), oPF = A.reserve(F3), oSF = A.reserve(F3);
   const size_t oWF = A.reserve(F3), oDF = A.reserve(F3);
@@ -429,6 +457,10 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.blksrc = carve<int>(base, oBlksrc);
   d.vtxptr = carve<int>(base, oVtxptr);
   d.vtxinc = carve<int>(base, oVtxinc);
+  d.sliceRow = carve<int>(base, oSliceRow);
+  d.slotSlice = carve<int>(base, oSlotSlice);
+  d.colS = carve<int>(base, oColS);
+  d.nslotRows = nslotRows;
   d.tileScene = carve<int>(base, oTileS);
   d.tileV0 = carve<int>(base, oTile0);
   d.tileV1 = carve<int>(base, oTile1);
@@ -475,6 +507,9 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   CUDA_TRY(up(d.blksrc, blksrc.data(), sizeof(int) * 16 * (size_t)nt));
   CUDA_TRY(up(d.vtxptr, vtxptr.data(), sizeof(int) * (nv + 1)));
   CUDA_TRY(up(d.vtxinc, vtxinc.data(), sizeof(int) * 4 * (size_t)nt));
+  CUDA_TRY(up(d.sliceRow, sliceRow.data(), sizeof(int) * (nslices + 1)));
+  CUDA_TRY(up(d.slotSlice, slotSlice.data(), sizeof(int) * nslotRows));
+  CUDA_TRY(up(d.colS, colS.data(), sizeof(int) * kSlice * (size_t)nslotRows));
   CUDA_TRY(up(d.tileScene, tileScene.data(), sizeof(int) * ntiles));
   CUDA_TRY(up(d.tileV0, tileV0.data(), sizeof(int) * ntiles));
   CUDA_TRY(up(d.tileV1, tileV1.data(), sizeof(int) * ntiles));

@@ -201,14 +201,14 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
 #pragma unroll
           for (int i = 0; i < 3; i++) x[q][i] = (k + q < k1) ? uw[i] : T(0);
         }
-        const T* B = v.lhs + 9 * (size_t)k;  // row major 3x3 blocks
+        const T* B = v.lhs + lhs_slot(b, u, k - k0);  // sliced 3x3 blocks, entry e at kSlice * e
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           if (k + q < k1) {
-            const T* Bq = B + 9 * q;
-            a0 = fma(Bq[0], x[q][0], fma(Bq[1], x[q][1], fma(Bq[2], x[q][2], a0)));
-            a1 = fma(Bq[3], x[q][0], fma(Bq[4], x[q][1], fma(Bq[5], x[q][2], a1)));
-            a2 = fma(Bq[6], x[q][0], fma(Bq[7], x[q][1], fma(Bq[8], x[q][2], a2)));
+            const T* Bq = B + (size_t)kSlotVals * q;
+            a0 = fma(Bq[0], x[q][0], fma(Bq[kSlice], x[q][1], fma(Bq[2 * kSlice], x[q][2], a0)));
+            a1 = fma(Bq[3 * kSlice], x[q][0], fma(Bq[4 * kSlice], x[q][1], fma(Bq[5 * kSlice], x[q][2], a1)));
+            a2 = fma(Bq[6 * kSlice], x[q][0], fma(Bq[7 * kSlice], x[q][1], fma(Bq[8 * kSlice], x[q][2], a2)));
           }
         }
       }

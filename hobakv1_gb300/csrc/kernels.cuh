@@ -33,6 +33,16 @@ struct ClusterClass {
 };
 
 // Device pointers of one packed batch.  Plain struct passed by value.
+// LHS storage: 32-vertex slices of 3x3 blocks (SELL-32).  The row of vertex
+// u (blocks k = rowptr[u] + j, j < rowptr[u + 1] - rowptr[u]) lives in the
+// slice of vertices [32 (u / 32), 32 (u / 32) + 32), padded to the slice's
+// longest row; entry e (row major) of block j sits at
+//   lhs[(sliceRow[u / 32] + j) * 288 + 32 e + u % 32]
+// and its column at colS[(sliceRow[u / 32] + j) * 32 + u % 32].  A warp over
+// 32 consecutive vertices reads one entry of one slot as one 128-byte line.
+constexpr int kSlice = 32;
+constexpr int kSlotVals = 9 * kSlice;
+
 struct DeviceBatch {
   int nscenes, nv, nt, nblocks, ntiles;
   // launch shapes (hobak_batch_autotune): vertices per PCG tile (64 or 128),
@@ -72,6 +82,13 @@ struct DeviceBatch {
   const int* blksrc;  // tet*16 + a*4 + b
   const int* vtxptr;  // vertex <- incidences
   const int* vtxinc;  // tet*4 + a
+  // sliced LHS storage (lhs_slot): first slot row of each 32-vertex slice
+  // (nslices + 1 entries), the slice of each slot row, and the column of
+  // every slot (padding slots: the vertex itself)
+  const int* sliceRow;
+  const int* slotSlice;
+  const int* colS;
+  int nslotRows;
 
   // tiles
   const int* tileScene;
@@ -96,6 +113,15 @@ struct DeviceBatch {
   int collOn;
   DeviceCollisions coll;
 };
+
+// Offset of entry 0 of block j of vertex u's row in the sliced LHS (entry e
+// at + kSlice * e), and of its column in colS.
+__device__ __forceinline__ size_t lhs_slot(const DeviceBatch& b, int u, int j) {
+  return (size_t)(b.sliceRow[u >> 5] + j) * kSlotVals + (u & (kSlice - 1));
+}
+__device__ __forceinline__ size_t col_slot(const DeviceBatch& b, int u, int j) {
+  return (size_t)(b.sliceRow[u >> 5] + j) * kSlice + (u & (kSlice - 1));
+}
 
 void launch_begin_step(const DeviceBatch& b, cudaStream_t s);
 // rawForces = 1 stores the element force f itself in elemG instead of dt (f + dt He v)

@@ -16,8 +16,9 @@
 //   k_update: p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s,
 //             u = Minv r, gamma = (r, u), |r|^2 -> convergence test
 // On GB300 the FP64 pipe, not HBM, bounds the FP64 SpMV, so the product does
-// only the 9 DFMA per block it must (one thread per scalar row, no lane
-// reductions).
+// only the 9 DFMA per block it must (one thread per vertex, no lane
+// reductions).  The LHS is stored in 32-vertex slices (lhs_slot), so the
+// SpMV's matrix and column loads are whole 128-byte lines per warp.
 //
 // Mixed precision: the inner PCG runs on FP32 vectors and an FP32 matrix; the
 // outer loop keeps y and the residual rhs - A y in FP64 (iterative refinement,
@@ -38,8 +39,8 @@ namespace hobak {
 namespace {
 
 // Tile kernels are instantiated for every supported tile size TV (vertices
-// per tile): vector kernels run one thread per vertex (TV threads), the SpMV,
-// update and residual one thread per scalar row (3 TV threads).  The batch's
+// per tile): vector kernels and the SpMV run one thread per vertex (TV
+// threads), the update and residual one thread per scalar row.  The batch's
 // tile size is an autotuned launch shape (DeviceBatch::tileV).
 
 // Fixed-order sum over the CTA; result valid in thread 0.  NT multiple of 32.
@@ -180,45 +181,58 @@ __device__ __forceinline__ HT gather_block_entry(const DeviceBatch& b, const HT*
   return sum;
 }
 
-// FP64 assembly: one thread per (block, entry), so the nine entries of a
-// contribution (72 contiguous bytes) are read by nine neighbouring lanes in one
-// request; at FP64 width this coalescing beats a thread per block.
+// Slot of the sliced LHS -> CSR block: slot row r, lane -> vertex u, block
+// k = rowptr[u] + j; false for padding slots and lanes past the last vertex.
+__device__ __forceinline__ bool slot_block(const DeviceBatch& b, int r, int lane, int& u, int& k) {
+  const int sl = b.slotSlice[r];
+  u = kSlice * sl + lane;
+  if (u >= b.nv) return false;
+  const int j = r - b.sliceRow[sl];
+  const int k0 = b.rowptr[u];
+  if (j >= b.rowptr[u + 1] - k0) return false;
+  k = k0 + j;
+  return true;
+}
+
+// FP64 assembly: one thread per (slot, entry), entries of a slot on nine
+// neighbouring lanes, so the nine entries of a contribution (72 contiguous
+// bytes) are read in one request; at FP64 width this coalescing beats a
+// thread per block.
 template <typename HT, typename T>
 __global__ void k_assemble_entry(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
-  const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= 9u * (unsigned)b.nblocks) return;
-  const int blk = (int)(g / 9u), e = (int)(g % 9u);
-  if (!b.scenes[b.vertexScene[b.blkRow[blk]]].active) return;
-  const int r = e / 3, c = e % 3;
-  const HT sum = gather_block_entry(b, elemH, blk, r, c);
-  const int u = b.blkRow[blk], w = b.cols[blk];
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (size_t)kSlotVals * b.nslotRows) return;
+  const int r = (int)(g / kSlotVals), rem = (int)(g % kSlotVals);
+  const int lane = rem / 9, e = rem % 9;
+  int u, blk;
+  if (!slot_block(b, r, lane, u, blk)) return;
+  if (!b.scenes[b.vertexScene[u]].active) return;
+  const int rr = e / 3, c = e % 3;
+  const HT sum = gather_block_entry(b, elemH, blk, rr, c);
+  const int w = b.cols[blk];
   const double dt = b.scenes[b.vertexScene[u]].dt;
   const bool fu = b.freeMask[u] != 0, fw = b.freeMask[w] != 0;
   HT val = (fu && fw) ? HT(-(dt * dt)) * sum : HT(0);
-  if (u == w && r == c) val += fu ? HT(b.mass[u]) : HT(1);
-  lhs[9 * (size_t)blk + e] = T(val);
+  if (u == w && rr == c) val += fu ? HT(b.mass[u]) : HT(1);
+  lhs[(size_t)r * kSlotVals + kSlice * e + lane] = T(val);
 }
 
-// FP32 assembly: one thread per block: its 9 entries summed over the block's
-// element contributions in list order (ascending tet), several contributions' loads
-// in flight at a time (each contribution is 9 contiguous values: a 3x3 block of
-// one element Hessian, transposed for the lower triangle), then
-// LHS block = S(M - dt^2 K)S + (I - S), staged through shared memory so the
-// CTA writes its blocks as one contiguous run.  Dynamic shared memory:
-// blockDim.x * (9 * sizeof(T) + 1).
+// FP32 assembly: one thread per slot (a warp per slot row of 32 vertices):
+// the block's 9 entries summed over its element contributions in list order
+// (ascending tet), several contributions' loads in flight at a time (each
+// contribution is 9 contiguous values: a 3x3 block of one element Hessian,
+// transposed for the lower triangle), then LHS block = S(M - dt^2 K)S + (I - S)
+// written entry by entry, each entry of the warp's 32 slots one 128-byte line.
+// Blocks of parked scenes keep their old values.
 template <typename HT, typename T>
 __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  T* out = reinterpret_cast<T*>(smem);
-  unsigned char* live = smem + 9 * sizeof(T) * blockDim.x;
-  const int blk0 = blockIdx.x * blockDim.x;
-  const int blk = blk0 + threadIdx.x;
-  bool write = false;
-  if (blk < b.nblocks) {
-    const int u = b.blkRow[blk];
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (size_t)kSlice * b.nslotRows) return;
+  const int r = (int)(g / kSlice), lane = (int)(g % kSlice);
+  int u, blk;
+  if (slot_block(b, r, lane, u, blk)) {
     const SceneParams& sp = b.scenes[b.vertexScene[u]];
     if (sp.active) {
-      write = true;
       HT sum[9];
 #pragma unroll
       for (int e = 0; e < 9; e++) sum[e] = HT(0);
@@ -254,20 +268,15 @@ __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __res
       const bool fu = b.freeMask[u] != 0, fw = b.freeMask[w] != 0;
       const HT m = fu ? HT(b.mass[u]) : HT(1);
       const HT ndt2 = HT(-(dt * dt));
+      T* out = lhs + (size_t)r * kSlotVals + lane;
 #pragma unroll
       for (int e = 0; e < 9; e++) {
         HT val = (fu && fw) ? ndt2 * sum[e] : HT(0);
         if (u == w && e % 4 == 0) val += m;
-        out[9 * threadIdx.x + e] = T(val);
+        out[kSlice * e] = T(val);
       }
     }
   }
-  live[threadIdx.x] = write ? 1 : 0;
-  // parked scenes' blocks keep their old values: write back only live blocks
-  __syncthreads();
-  const int nb = min((int)blockDim.x, b.nblocks - blk0);
-  for (int i = threadIdx.x; i < 9 * nb; i += blockDim.x)
-    if (live[i / 9]) lhs[9 * (size_t)blk0 + i] = out[i];
 }
 
 // Raw K blocks (column major) and R: the reference's stiffness and force
@@ -298,9 +307,10 @@ __global__ void k_diag_inverse(DeviceBatch b, const T* __restrict__ lhs, T* __re
   if (u >= b.nv || !b.scenes[b.vertexScene[u]].active) return;
   int k = b.rowptr[u];
   while (b.cols[k] != u) k++;
+  const T* Lu = lhs + lhs_slot(b, u, k - b.rowptr[u]);
   double D[9];
 #pragma unroll
-  for (int i = 0; i < 9; i++) D[i] = (double)lhs[9 * (size_t)k + i];
+  for (int i = 0; i < 9; i++) D[i] = (double)Lu[kSlice * i];
   if (b.collOn) {  // the vertex's own contact block (FP64, beside the LHS)
 #pragma unroll
     for (int i = 0; i < 9; i++) D[i] += b.coll.diag[9 * (size_t)u + i];
@@ -515,22 +525,50 @@ __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int
   return scale * acc;
 }
 
-// w = A u, one thread per scalar row (9 DFMA per block in FP64), and
-// delta = (w, u); the scene's last CTA forms beta and alpha.
+// Threads of an SpMV CTA: one per vertex in FP32 (the sliced LHS makes
+// every matrix and column load of a warp one line, and a vertex's three rows
+// share its column loads and u gathers); one per scalar row in FP64, whose
+// SpMV is bound by GB300's narrow FP64 pipe and wants three times the warps
+// to keep it fed.
+template <typename T>
+__host__ __device__ constexpr int spmv_threads(int TV) { return sizeof(T) == sizeof(float) ? TV : 3 * TV; }
+
+// beta, alpha from delta = (w, u) in the scene's last CTA
+__device__ __forceinline__ void spmv_scalars(SolveState& st, double delta) {
+  st.delta = delta;
+  if (st.iters == 0) {
+    st.beta = 0.0;
+    st.alpha = st.gamma / delta;
+  } else {
+    const double beta = st.gamma / st.gammaOld;
+    st.beta = beta;
+    st.alpha = st.gamma / (delta - beta * st.gamma / st.alpha);
+  }
+  st.alphaF = float(st.alpha);
+  st.betaF = float(st.beta);
+}
+
+// FP64: w = A u, one thread per scalar row (9 DFMA per block over the row's
+// three threads), and delta = (w, u).  In the sliced LHS the row's entries
+// of block j sit at kSlice * (3 i + c) past the slot, so a warp's 30 rows
+// (10 vertices) read three lines per load.
 template <int TV, typename T>
-__device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh, int* flag) {
+__device__ __forceinline__ void spmv_tile_rows(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh,
+                                               int* flag) {
   // before the dependency wait: what the previous kernel does not write
   const int s = b.tileScene[tile];
   const int row = 3 * b.tileV0[tile] + threadIdx.x;
   const bool valid = row < 3 * b.tileV1[tile];
   const int u = row / 3, i = row - 3 * u;
-  int k0 = 0, k1 = 0;
+  int len = 0;
+  size_t mb = 0, cb = 0;
   int wn[4] = {0, 0, 0, 0};
   if (valid) {
-    k0 = b.rowptr[u];
-    k1 = b.rowptr[u + 1];
+    len = b.rowptr[u + 1] - b.rowptr[u];
+    mb = lhs_slot(b, u, 0) + kSlice * 3 * i;
+    cb = col_slot(b, u, 0);
 #pragma unroll
-    for (int q = 0; q < 4; q++) wn[q] = (k0 + q < k1) ? __ldg(&b.cols[k0 + q]) : 0;
+    for (int q = 0; q < 4; q++) wn[q] = (q < len) ? __ldg(&b.colS[cb + kSlice * q]) : 0;
   }
   pdl_wait();
   SolveState& st = b.solve[s];
@@ -538,27 +576,25 @@ __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>
   T dl = T(0);
   if (valid) {
     const T* __restrict__ uu = v.u;
-    const T* __restrict__ A = v.lhs + 3 * i;
     // Four blocks per trip, all their loads issued together (predicated past
-    // the row's end); the next trip's column indices are fetched one trip
-    // ahead, so each trip waits on one memory latency (the u gather) instead
-    // of two.  Two FMA chains: 3 FMA per block, the FP64 minimum.
+    // the row's end); the next trip's columns are fetched one trip ahead.
+    // Two FMA chains: 3 FMA per block, the FP64 minimum.
     T acc0 = T(0), acc1 = T(0);
-    for (int k = k0; k < k1; k += 4) {
+    for (int j = 0; j < len; j += 4) {
       int w[4];
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         w[q] = wn[q];
-        wn[q] = (k + 4 + q < k1) ? __ldg(&b.cols[k + 4 + q]) : 0;
+        wn[q] = (j + 4 + q < len) ? __ldg(&b.colS[cb + kSlice * (j + 4 + q)]) : 0;
       }
-      const T* B = A + 9 * (size_t)k;
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        if (k + q < k1) {
+        if (j + q < len) {
+          const T* B = v.lhs + mb + (size_t)kSlotVals * (j + q);
           T& acc = (q & 1) ? acc1 : acc0;
-          acc = fma(B[9 * q], uu[3 * w[q]], acc);
-          acc = fma(B[9 * q + 1], uu[3 * w[q] + 1], acc);
-          acc = fma(B[9 * q + 2], uu[3 * w[q] + 2], acc);
+          acc = fma(__ldg(&B[0]), __ldg(&uu[3 * w[q]]), acc);
+          acc = fma(__ldg(&B[kSlice]), __ldg(&uu[3 * w[q] + 1]), acc);
+          acc = fma(__ldg(&B[2 * kSlice]), __ldg(&uu[3 * w[q] + 2]), acc);
         }
       }
     }
@@ -572,19 +608,85 @@ __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketA, sp.ntiles, flag)) return;
   const double delta = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 2, sh);
-  if (threadIdx.x == 0) {
-    st.delta = delta;
-    if (st.iters == 0) {
-      st.beta = 0.0;
-      st.alpha = st.gamma / delta;
-    } else {
-      const double beta = st.gamma / st.gammaOld;
-      st.beta = beta;
-      st.alpha = st.gamma / (delta - beta * st.gamma / st.alpha);
-    }
-    st.alphaF = float(st.alpha);
-    st.betaF = float(st.beta);
+  if (threadIdx.x == 0) spmv_scalars(st, delta);
+}
+
+// FP32: w = A u, one thread per vertex (its three rows; 9 FMA per block), and
+// delta = (w, u); the scene's last CTA forms beta and alpha.  The warps run
+// over 32 consecutive vertices, so in the sliced LHS every matrix and column
+// load of a warp is one contiguous line.
+template <int TV, typename T>
+__device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh, int* flag) {
+  // before the dependency wait: what the previous kernel does not write
+  const int s = b.tileScene[tile];
+  const int u = b.tileV0[tile] + threadIdx.x;
+  const bool valid = u < b.tileV1[tile];
+  int len = 0;
+  size_t mb = 0, cb = 0;
+  constexpr int Q0 = sizeof(T) == sizeof(float) ? 4 : 2;
+  int wn[Q0];
+#pragma unroll
+  for (int q = 0; q < Q0; q++) wn[q] = 0;
+  if (valid) {
+    len = b.rowptr[u + 1] - b.rowptr[u];
+    mb = lhs_slot(b, u, 0);
+    cb = col_slot(b, u, 0);
+#pragma unroll
+    for (int q = 0; q < Q0; q++) wn[q] = (q < len) ? __ldg(&b.colS[cb + kSlice * q]) : 0;
   }
+  pdl_wait();
+  SolveState& st = b.solve[s];
+  if (st.done) return;
+  T dl = T(0);
+  if (valid) {
+    const T* __restrict__ uu = v.u;
+    // Q blocks per trip (4 in FP32, 2 in FP64: register budget), all their
+    // loads issued together (predicated past the row's end); the next trip's
+    // columns are fetched one trip ahead, so each trip waits on one memory
+    // latency (the u gather) instead of two.
+    constexpr int Q = sizeof(T) == sizeof(float) ? 4 : 2;
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+    for (int j = 0; j < len; j += Q) {
+      int w[Q];
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        w[q] = wn[q];
+        wn[q] = (j + Q + q < len) ? __ldg(&b.colS[cb + kSlice * (j + Q + q)]) : 0;
+      }
+      T x[Q][3], m[Q][9];
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        const T* B = v.lhs + mb + (size_t)kSlotVals * (j + q);
+#pragma unroll
+        for (int e = 0; e < 9; e++) m[q][e] = (j + q < len) ? __ldg(&B[kSlice * e]) : T(0);
+#pragma unroll
+        for (int c = 0; c < 3; c++) x[q][c] = (j + q < len) ? __ldg(&uu[3 * w[q] + c]) : T(0);
+      }
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        if (j + q < len) {
+          a0 = fma(m[q][0], x[q][0], fma(m[q][1], x[q][1], fma(m[q][2], x[q][2], a0)));
+          a1 = fma(m[q][3], x[q][0], fma(m[q][4], x[q][1], fma(m[q][5], x[q][2], a1)));
+          a2 = fma(m[q][6], x[q][0], fma(m[q][7], x[q][1], fma(m[q][8], x[q][2], a2)));
+        }
+      }
+    }
+    if (b.collOn && b.freeMask[u]) {
+      a0 += T(collision_row<T>(b, u, 0, uu));
+      a1 += T(collision_row<T>(b, u, 1, uu));
+      a2 += T(collision_row<T>(b, u, 2, uu));
+    }
+    v.w[3 * u] = a0;
+    v.w[3 * u + 1] = a1;
+    v.w[3 * u + 2] = a2;
+    dl = a0 * uu[3 * u] + a1 * uu[3 * u + 1] + a2 * uu[3 * u + 2];
+  }
+  const double t = block_sum<TV>(dl, sh);
+  if (threadIdx.x == 0) b.partial[kPartials * tile + 2] = t;
+  const SceneParams& sp = b.scenes[s];
+  if (!last_tile(&st.ticketA, sp.ntiles, flag)) return;
+  const double delta = sum_partials<TV>(b.partial, sp.tile0, sp.ntiles, 2, sh);
+  if (threadIdx.x == 0) spmv_scalars(st, delta);
 }
 
 // CTA -> tile of the PCG loop kernels (grid = all tiles).  While every scene
@@ -598,12 +700,14 @@ __device__ __forceinline__ int loop_tile(const DeviceBatch& b) {
 }
 
 template <int TV, typename T>
-__global__ void __launch_bounds__(3 * TV) k_spmv(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[3 * TV / 32];
+__global__ void __launch_bounds__(spmv_threads<T>(TV)) k_spmv(DeviceBatch b, PcgVecs<T> v) {
+  __shared__ double sh[spmv_threads<T>(TV) / 32];
   __shared__ int flag;
   pdl_trigger();
   const int tile = loop_tile(b);
-  if (tile >= 0) spmv_tile<TV, T>(b, v, tile, sh, &flag);
+  if (tile < 0) return;
+  if constexpr (sizeof(T) == sizeof(float)) spmv_tile<TV, T>(b, v, tile, sh, &flag);
+  else spmv_tile_rows<TV, T>(b, v, tile, sh, &flag);
 }
 
 // p = u + beta p; s = w + beta s; d += alpha p; r -= alpha s; u = Minv r;
@@ -779,12 +883,13 @@ __global__ void __launch_bounds__(3 * TV) k_residual(DeviceBatch b) {
   double rr = 0.0;
   if (row < 3 * b.tileV1[tile]) {
     const int u = row / 3, i = row - 3 * u;
-    const float* A = b.v32.lhs + 3 * i;
+    const float* A = b.v32.lhs + lhs_slot(b, u, 0) + kSlice * 3 * i;
     double acc = 0.0;
-    for (int k = b.rowptr[u]; k < b.rowptr[u + 1]; k++) {
+    const int k0 = b.rowptr[u], k1 = b.rowptr[u + 1];
+    for (int k = k0; k < k1; k++) {
       const int w = b.cols[k];
-      const float* B = A + 9 * (size_t)k;
-      acc += double(B[0]) * b.y[3 * w] + double(B[1]) * b.y[3 * w + 1] + double(B[2]) * b.y[3 * w + 2];
+      const float* B = A + (size_t)kSlotVals * (k - k0);
+      acc += double(B[0]) * b.y[3 * w] + double(B[kSlice]) * b.y[3 * w + 1] + double(B[2 * kSlice]) * b.y[3 * w + 2];
     }
     if (b.collOn && b.freeMask[u]) acc += collision_row<double>(b, u, i, b.y);
     const double ri = b.rhs[row] - acc;
@@ -844,12 +949,13 @@ template <typename T>
 void launch_assemble(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
   if (b.nblocks == 0) return;
   if (sizeof(T) == sizeof(double)) {
-    const unsigned n = 9u * (unsigned)b.nblocks;
-    k_assemble_entry<double, T><<<(n + b.asmThreads - 1) / b.asmThreads, b.asmThreads, 0, s>>>(b, b.elemH, v.lhs);
+    const size_t n = (size_t)kSlotVals * b.nslotRows;
+    k_assemble_entry<double, T><<<(unsigned)((n + b.asmThreads - 1) / b.asmThreads), b.asmThreads, 0, s>>>(
+        b, b.elemH, v.lhs);
   } else {
-    const unsigned grid = (unsigned)((b.nblocks + b.asmThreads - 1) / b.asmThreads);
-    const size_t smem = (9 * sizeof(T) + 1) * (size_t)b.asmThreads;
-    k_assemble<float, T><<<grid, b.asmThreads, smem, s>>>(b, b.elemHf, v.lhs);
+    const size_t n = (size_t)kSlice * b.nslotRows;
+    k_assemble<float, T><<<(unsigned)((n + b.asmThreads - 1) / b.asmThreads), b.asmThreads, 0, s>>>(
+        b, b.elemHf, v.lhs);
   }
 }
 
@@ -902,8 +1008,8 @@ void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s
 
 template <typename T>
 void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl) {
-  if (b.tileV == 64) launch_loop_kernel(k_spmv<64, T>, b.ntiles, 3 * 64, s, pdl, b, v);
-  else launch_loop_kernel(k_spmv<128, T>, b.ntiles, 3 * 128, s, pdl, b, v);
+  if (b.tileV == 64) launch_loop_kernel(k_spmv<64, T>, b.ntiles, spmv_threads<T>(64), s, pdl, b, v);
+  else launch_loop_kernel(k_spmv<128, T>, b.ntiles, spmv_threads<T>(128), s, pdl, b, v);
 }
 
 template <typename T>
