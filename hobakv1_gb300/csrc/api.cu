@@ -77,6 +77,9 @@ struct hobak_batch_t {
   DeviceBatch d{};
   void* arena = nullptr;
   size_t arenaBytes = 0;
+  void* precArena = nullptr;  // buffers of the current precision (alloc_precision)
+  size_t precBytes = 0;
+  bool precMixed = false;
   cudaStream_t stream = nullptr;
   cudaStream_t captureStream = nullptr;  // fills the bodies of captured while loops
   cudaGraphExec_t stepGraph[2] = {nullptr, nullptr};  // untimed, timed
@@ -180,6 +183,53 @@ int validate_scene(const hobak_scene_desc& s, int idx) {
 template <typename T>
 T* carve(void* base, size_t off) {
   return reinterpret_cast<T*>(static_cast<char*>(base) + off);
+}
+
+// Buffers of the batch's precision, in their own allocation (replaced when
+// the precision changes): FP64 element Hessians, sliced LHS, block inverse
+// and inner vectors (r = r64, d = y) for the FP64 path, or their FP32
+// counterparts for the mixed path.  The other path's pointers are null.
+int alloc_precision(hobak_batch_t* B) {
+  if (B->precArena) {
+    CUDA_TRY(cudaFree(B->precArena));
+    B->precArena = nullptr;
+    B->precBytes = 0;
+  }
+  DeviceBatch& d = B->d;
+  const size_t nt = (size_t)B->nt, nv = (size_t)B->nv, vals = (size_t)kSlotVals * d.nslotRows;
+  const bool mixed = B->opts.precision == HOBAK_PRECISION_MIXED;
+  const size_t w = mixed ? sizeof(float) : sizeof(double);
+  Arena A;
+  const size_t oEH = A.reserve(w * kElemHess * nt);
+  const size_t oLhs = A.reserve(w * vals);
+  const size_t oMinv = A.reserve(w * 9 * nv);
+  size_t oVec[6];
+  for (int k = 0; k < (mixed ? 6 : 4); k++) oVec[k] = A.reserve(w * 3 * nv);
+  void* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, A.used);
+  if (e != cudaSuccess)
+    return fail(e == cudaErrorMemoryAllocation ? HOBAK_ERR_NO_MEMORY : HOBAK_ERR_CUDA,
+                std::string("cudaMalloc of precision buffers: ") + cudaGetErrorString(e));
+  B->precArena = base;
+  B->precBytes = A.used;
+  CUDA_TRY(cudaMemset(base, 0, A.used));
+  if (mixed) {
+    d.elemH = nullptr;
+    d.elemHf = carve<float>(base, oEH);
+    d.v64 = PcgVecs<double>{};
+    d.v32 = PcgVecs<float>{carve<float>(base, oLhs), carve<float>(base, oMinv), carve<float>(base, oVec[0]),
+                           carve<float>(base, oVec[1]), carve<float>(base, oVec[2]), carve<float>(base, oVec[3]),
+                           carve<float>(base, oVec[4]), carve<float>(base, oVec[5])};
+  } else {
+    d.elemHf = nullptr;
+    d.elemH = carve<double>(base, oEH);
+    d.v32 = PcgVecs<float>{};
+    d.v64 = PcgVecs<double>{carve<double>(base, oLhs), carve<double>(base, oMinv), d.r64,
+                            carve<double>(base, oVec[0]), carve<double>(base, oVec[1]), carve<double>(base, oVec[2]),
+                            carve<double>(base, oVec[3]), d.y};
+  }
+  B->precMixed = mixed;
+  return HOBAK_OK;
 }
 
 int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
@@ -393,27 +443,13 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oVtxptr = A.reserve(sizeof(int) * (nv + 1)), oVtxinc = A.reserve(sizeof(int) * 4 * (size_t)nt);
   const size_t oSliceRow = A.reserve(sizeof(int) * (nslices + 1)), oSlotSlice = A.reserve(sizeof(int) * nslotRows);
   const size_t oColS = A.reserve(sizeof(int) * kSlice * (size_t)nslotRows);
-  // sliced LHS values; the FP64 one also serves as CSR scratch for the
-  // inspection call (hobak_batch_assemble)
-  const size_t lhsVals = std::max((size_t)kSlotVals * nslotRows, 9 * (size_t)nblocks);
+
   const size_t oTileS = A.reserve(sizeof(int) * ntilesCap), oTile0 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oTile1 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oLoopTiles = A.reserve(sizeof(int) * ntilesCap), oNLoop = A.reserve(sizeof(int));
   const size_t oClusterList = A.reserve(sizeof(int) * n);
-  const size_t oEH = A.reserve(sizeof(double) * kElemHess * (size_t)nt);
-  const size_t oEHf = A.reserve(sizeof(float) * kElemHess * (size_t)nt);
   const size_t oEG = A.reserve(sizeof(double) * 12 * (size_t)nt);
   const size_t oRhs = A.reserve(V3), oY = A.reserve(V3), oR64 = A.reserve(V3);
-  // FP64 inner solve (r = r64, d = y)
-  const size_t oLhs = A.reserve(sizeof(double) * lhsVals);
-  const size_t oMinv = A.reserve(sizeof(double) * 9 * (size_t)nv);
-  const size_t oU = A.reserve(V3), oP = A.reserve(V3), oS = A.reserve(V3), oW = A.reserve(V3);
-  // FP32 inner solve (mixed precision)
-  const size_t F3 = 3 * (size_t)nv * sizeof(float);
-  const size_t oLhsF = A.reserve(sizeof(float) * kSlotVals * (size_t)nslotRows);
-  const size_t oMinvF = A.reserve(sizeof(float) * 9 * (size_t)nv);
-  const size_t oRF = A.reserve(F3), oUF = A.reserve(F3), oPF = A.reserve(F3), oSF = A.reserve(F3);
-  const size_t oWF = A.reserve(F3), oDF = A.reserve(F3);
   const size_t oPart = A.reserve(sizeof(double) * kPartials * (size_t)ntilesCap);
   const size_t oPsi = A.reserve(sizeof(double) * nt);
   void* base = nullptr;
@@ -468,18 +504,10 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.nTileScenes = n;
   B->clusterList = carve<int>(base, oClusterList);
   d.nLoopTiles = carve<int>(base, oNLoop);
-  d.elemH = carve<double>(base, oEH);
-  d.elemHf = carve<float>(base, oEHf);
   d.elemG = carve<double>(base, oEG);
   d.rhs = carve<double>(base, oRhs);
   d.y = carve<double>(base, oY);
   d.r64 = carve<double>(base, oR64);
-  d.v64 = PcgVecs<double>{carve<double>(base, oLhs), carve<double>(base, oMinv), d.r64,
-                          carve<double>(base, oU), carve<double>(base, oP), carve<double>(base, oS),
-                          carve<double>(base, oW), d.y};
-  d.v32 = PcgVecs<float>{carve<float>(base, oLhsF), carve<float>(base, oMinvF), carve<float>(base, oRF),
-                         carve<float>(base, oUF), carve<float>(base, oPF), carve<float>(base, oSF),
-                         carve<float>(base, oWF), carve<float>(base, oDF)};
   d.partial = carve<double>(base, oPart);
   d.psi = carve<double>(base, oPsi);
 
@@ -516,7 +544,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   B->hostRowptr = rowptr;
   B->restHost = rest;
   B->hostCols = cols;
-  return HOBAK_OK;
+  return alloc_precision(B);
 }
 
 int sweeps_of(const hobak_solver_opts& o);
@@ -1106,6 +1134,7 @@ int hobak_batch_destroy(hobak_batch b) {
   if (b->pinnedActive) cudaFreeHost(b->pinnedActive);
   if (b->solvePinned) cudaFreeHost(b->solvePinned);
   if (b->arena) cudaFree(b->arena);
+  if (b->precArena) cudaFree(b->precArena);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return HOBAK_OK;
@@ -1235,6 +1264,10 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   b->opts = *opts;
   b->clusterDirty = true;
   drop_graphs(b);
+  if ((opts->precision == HOBAK_PRECISION_MIXED) != b->precMixed) {
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    if ((rc = alloc_precision(b))) return rc;
+  }
   return upload_solver_opts(b);
 }
 
@@ -1350,7 +1383,7 @@ int hobak_batch_set_active(hobak_batch b, int scene, int active) {
 
 int hobak_batch_device_bytes(hobak_batch b, long long* bytes) {
   if (!b || !bytes) return fail(HOBAK_ERR_INVALID, "bad arguments");
-  *bytes = (long long)b->arenaBytes;
+  *bytes = (long long)(b->arenaBytes + b->precBytes);
   return HOBAK_OK;
 }
 
@@ -1730,15 +1763,21 @@ int hobak_batch_assemble(hobak_batch b, int scene, int* nblocks, int* rowptr, in
   if (cols)
     for (int k = rb0; k < rb1; k++) cols[k - rb0] = b->hostCols[k] - H.v0;
   if (!K && !R) return HOBAK_OK;
-  // element terms at the current state with raw forces, then the device
-  // gathers K and R into the (per-step scratch) LHS and rhs buffers
+  // element terms at the current state with raw forces (FP64 element
+  // Hessians in scratch of this call), then the device gathers K (CSR
+  // order, scratch) and R (into the per-step rhs buffer)
+  DeviceScratch scratch;
+  const size_t ehBytes = sizeof(double) * kElemHess * (size_t)b->nt;
+  CUDA_TRY(cudaMalloc(&scratch.p, ehBytes + sizeof(double) * 9 * (size_t)std::max(b->nblocks, 1)));
   DeviceBatch d = b->d;
+  d.elemH = static_cast<double*>(scratch.p);
+  double* Kd = reinterpret_cast<double*>(static_cast<char*>(scratch.p) + ehBytes);
   launch_begin_step(d, b->stream);
   launch_element(d, b->stream, 1);
-  launch_assemble_raw(d, d.v64.lhs, d.rhs, b->stream);
+  launch_assemble_raw(d, Kd, d.rhs, b->stream);
   CUDA_TRY(cudaGetLastError());
   if (K)
-    CUDA_TRY(cudaMemcpyAsync(K, d.v64.lhs + 9 * (size_t)rb0, 9 * sizeof(double) * (rb1 - rb0), cudaMemcpyDeviceToHost,
+    CUDA_TRY(cudaMemcpyAsync(K, Kd + 9 * (size_t)rb0, 9 * sizeof(double) * (rb1 - rb0), cudaMemcpyDeviceToHost,
                              b->stream));
   if (R)
     CUDA_TRY(cudaMemcpyAsync(R, d.rhs + 3 * (size_t)H.v0, 3 * sizeof(double) * H.nv, cudaMemcpyDeviceToHost,

@@ -636,7 +636,9 @@ __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>
   }
   pdl_wait();
   SolveState& st = b.solve[s];
-  if (st.done) return;
+  // the done test waits for its load only after the first trip's loads are
+  // in flight
+  const int done = st.done;
   T dl = T(0);
   if (valid) {
     const T* __restrict__ uu = v.u;
@@ -662,6 +664,7 @@ __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>
 #pragma unroll
         for (int c = 0; c < 3; c++) x[q][c] = (j + q < len) ? __ldg(&uu[3 * w[q] + c]) : T(0);
       }
+      if (done) return;
 #pragma unroll
       for (int q = 0; q < Q; q++) {
         if (j + q < len) {
@@ -681,6 +684,7 @@ __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>
     v.w[3 * u + 2] = a2;
     dl = a0 * uu[3 * u] + a1 * uu[3 * u + 1] + a2 * uu[3 * u + 2];
   }
+  if (done) return;  // threads without rows (the CTA returns as one)
   const double t = block_sum<TV>(dl, sh);
   if (threadIdx.x == 0) b.partial[kPartials * tile + 2] = t;
   const SceneParams& sp = b.scenes[s];
@@ -731,8 +735,11 @@ __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<
     M2 = M[2];
   }
   pdl_wait();
+  // the solve state and the row's six vectors in one round of loads; the
+  // done test comes after them instead of in front (a finished scene's tiles
+  // leave the compacted list at the next loop body)
   SolveState& st = b.solve[s];
-  if (st.done) return;
+  const int done = st.done;
   // FP32 scalars come pre-converted: a double-to-float conversion per thread
   // would occupy GB300's narrow FP64 pipe
   T alpha, beta;
@@ -743,11 +750,20 @@ __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<
     alpha = st.alpha;
     beta = st.beta;
   }
-  T rr = T(0), ru = T(0);
   T* __restrict__ r = (sizeof(T) == sizeof(double)) ? reinterpret_cast<T*>(b.r64) : v.r;
+  T u0 = T(0), p0 = T(0), w0 = T(0), s0 = T(0), d0 = T(0), r0 = T(0);
+  if (valid) {
+    u0 = v.u[row];
+    p0 = v.p[row];
+    w0 = v.w[row];
+    s0 = v.s[row];
+    d0 = v.d[row];
+    r0 = r[row];
+  }
+  if (done) return;
+  T rr = T(0), ru = T(0);
   T rnew = T(0);
   if (valid) {
-    const T u0 = v.u[row], p0 = v.p[row], w0 = v.w[row], s0 = v.s[row], d0 = v.d[row], r0 = r[row];
     const T p = u0 + beta * p0;
     const T sv = w0 + beta * s0;
     v.p[row] = p;

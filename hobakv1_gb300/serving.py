@@ -41,13 +41,19 @@ from . import hobak
 
 
 def footprint_bytes(scene, precision: int) -> int:
-    """Conservative device bytes of one scene in a batch (both precisions'
-    buffers are allocated; ~15 blocks per vertex in tet meshes)."""
+    """Conservative device bytes of one scene in a batch: the common buffers
+    plus those of its precision (the library allocates only the batch's
+    precision); at most 16 blocks per vertex row, padded in 32-vertex slices."""
     nv, nt = scene.nv, scene.nt
     nb = 16 * nv
-    per_tet = 16 + 72 + 8 + 4 + 720 + 360 + 96 + 64 + 16 + 8
-    per_block = 4 + 4 + 4 + 4 + 72 + 36
-    per_vertex = 6 * 24 + 8 + 1 + 4 + 3 * 24 + 72 + 36 + 4 * 24 + 6 * 12 + 8
+    w = 4 if precision == hobak.PRECISION_MIXED else 8
+    # tets, DmInv, vol, scene id, element g, contribution map, incidences, psi; element Hessians
+    per_tet = 16 + 72 + 8 + 4 + 96 + 64 + 16 + 8 + 90 * w
+    # cols, block row, contribution ranges, sliced column; sliced LHS values
+    per_block = 4 + 4 + 4 + 4 + 9 * w
+    # rest, x, v, f_ext, pin target, mass, mask, scene id, rowptr, incidences,
+    # rhs, y, r64; block inverse and inner vectors
+    per_vertex = 5 * 24 + 8 + 1 + 4 + 4 + 4 + 3 * 24 + 9 * w + (6 if w == 4 else 4) * 3 * w
     return int(nt * per_tet + nb * per_block + nv * per_vertex + (1 << 20))
 
 

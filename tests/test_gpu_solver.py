@@ -111,3 +111,35 @@ def test_whole_batch_state_calls_match_per_scene_calls():
     xb, vb = b.get_state_all()
     xc, vc = c.get_state_all()
     assert np.array_equal(xb, xc) and np.array_equal(vb, vc)
+
+
+def test_precision_switch_reallocates_and_matches_a_new_batch():
+    """Only the batch's precision has buffers; switching precision between
+    steps replaces them, and the steps after the switch equal those of a
+    batch created with that precision from the same state."""
+    mix = scenes.config4_scenes(count=3, nmin=4, nmax=7)
+    b = hobak.BATCH(mix, hobak.solver_opts(precision=hobak.PRECISION_FP64))
+    fp64_bytes = b.device_bytes()
+    b.step(2)
+    x, v = b.get_state_all()
+    b.set_solver(hobak.solver_opts(precision=hobak.PRECISION_MIXED))
+    assert b.device_bytes() < fp64_bytes
+    b.step(3)
+    c = hobak.BATCH(mix, hobak.solver_opts(precision=hobak.PRECISION_MIXED))
+    c.set_state_all(x, v)
+    c.step(3)
+    xb, vb = b.get_state_all()
+    xc, vc = c.get_state_all()
+    assert np.array_equal(xb, xc) and np.array_equal(vb, vc)
+    b.set_solver(hobak.solver_opts(precision=hobak.PRECISION_FP64))
+    assert b.device_bytes() == fp64_bytes
+    b.step(1)
+
+
+@pytest.mark.parametrize("precision", [hobak.PRECISION_FP64, hobak.PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_serving_footprint_estimate_covers_the_allocation(precision):
+    from hobakv1_gb300.serving import footprint_bytes
+    for s in (scenes.config2_scene(6, "snh"), scenes.config4_scenes(count=1, nmin=14, nmax=14)[0]):
+        b = hobak.BATCH([s], hobak.solver_opts(precision=precision))
+        assert footprint_bytes(s, precision) >= b.device_bytes()
+        b.close()
