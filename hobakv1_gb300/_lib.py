@@ -34,7 +34,7 @@ class HobakSolverOpts(ctypes.Structure):
 class HobakTuning(ctypes.Structure):
     _fields_ = [("tile_vertices", ctypes.c_int), ("element_threads", ctypes.c_int),
                 ("assembly_threads", ctypes.c_int), ("pcg_chunk", ctypes.c_int), ("cluster_pcg", ctypes.c_int),
-                ("step_ms", ctypes.c_double)]
+                ("cluster_max", ctypes.c_int), ("step_ms", ctypes.c_double)]
 
 
 class HobakStepStats(ctypes.Structure):

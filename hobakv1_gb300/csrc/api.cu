@@ -81,7 +81,8 @@ struct hobak_batch_t {
   size_t precBytes = 0;
   bool precMixed = false;
   cudaStream_t stream = nullptr;
-  cudaStream_t captureStream = nullptr;  // fills the bodies of captured while loops
+  cudaStream_t captureStream = nullptr;   // fills the bodies of captured while loops
+  cudaStream_t captureStream2 = nullptr;  // fills the bodies of the switch nodes inside them
   cudaGraphExec_t stepGraph[2] = {nullptr, nullptr};  // untimed, timed
   long long eagerChunks = 0;
   long long loopLaunchBase = 0;  // loop-body launches folded in before the last chunk change
@@ -90,6 +91,7 @@ struct hobak_batch_t {
   // cluster-resident PCG (cluster_pcg.cu): on/off, the classes of the
   // current precision, and whether any scene is left to the tile path
   bool clusterPcg = false;
+  int clusterMax = 16;  // largest cluster (CTAs) a scene may use; larger scenes keep the tile path
   bool clusterDirty = true;
   ClusterClass classes[kClusterClasses] = {};
   int* clusterList = nullptr;  // device, nscenes ids grouped by class
@@ -590,8 +592,10 @@ void drop_graphs(hobak_batch_t* B);
 // Which scenes solve their inner PCG in a thread-block cluster, and in how
 // large a one, for the current precision: scenes without contact, in the
 // smallest cluster (1, 2, 4, 8 or 16 CTAs) that gives each thread at most one
-// vertex; larger scenes (more than 16 x 1024 vertices) keep the tile path,
-// which spreads them wider.  The choice depends only on the scene itself, so
+// vertex, or, with the cluster size capped below 16 (clusterMax), in a capped
+// cluster whose threads take several vertices while its vectors fit in shared
+// memory (fewer SMs per scene, more scenes at once); larger scenes keep the
+// tile path, which spreads them wider.  The choice depends only on the scene itself, so
 // a scene takes the same path alone and in any batch.  Runs outside graph
 // capture (it uploads); drops the graphs when the assignment changed.
 int prepare_cluster_classes(hobak_batch_t* B) {
@@ -606,10 +610,13 @@ int prepare_cluster_classes(hobak_batch_t* B) {
     const bool contact = B->collArena && s < (int)B->collScenes.size() && B->collScenes[s].vfOn;
     if (!B->clusterPcg || contact) continue;
     const int nv = B->scenes[s].nv;
+    // the smallest cluster that gives each thread one vertex at most; under
+    // a cap below 16 CTAs, threads of a capped cluster take several vertices
+    // as long as the CTA's vectors fit in its shared memory
     int c = 1;
-    while (c < 16 && (nv + c - 1) / c > kClusterThreads) c *= 2;
+    while (c < B->clusterMax && (nv + c - 1) / c > kClusterThreads) c *= 2;
     const int vpc = (nv + c - 1) / c;
-    if (vpc <= kClusterThreads && vpc <= vpcLimit) cl[s] = c;  // one vertex per thread at most
+    if (vpc <= kClusterThreads || (B->clusterMax < 16 && vpc <= vpcLimit)) cl[s] = c;
   }
   std::vector<int> list;
   bool changed = false;
@@ -645,52 +652,101 @@ int prepare_cluster_classes(hobak_batch_t* B) {
   return HOBAK_OK;
 }
 
-// One PCG chunk: the list of tiles still iterating, then `chunk` iterations
-// (2 kernels each).
+// `chunk` PCG iterations (2 kernels each) on `grid` CTAs.
 template <typename T>
-void enqueue_chunk(const DeviceBatch& d, const PcgVecs<T>& v, cudaStream_t s, int chunk) {
-  launch_compact_tiles(d, s);
-  for (int c = 0; c < chunk; c++) launch_pcg_iteration<T>(d, v, s, c == 0);
+void enqueue_chunk(const DeviceBatch& d, const PcgVecs<T>& v, cudaStream_t s, int chunk, int grid) {
+  for (int c = 0; c < chunk; c++) launch_pcg_iteration<T>(d, v, s, c == 0, grid);
 }
 
-// While-loop node on the capturing stream `s`: body = one chunk followed by
-// k_continue, which keeps the loop going while any scene's inner PCG runs.
-template <typename T>
-int capture_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
+// Adds a conditional node of `type` with `size` bodies after the current
+// capture dependencies of `s` (which then depend on the node); returns the
+// handle and the body graphs.
+int add_conditional(cudaStream_t s, cudaGraphConditionalNodeType type, unsigned size, unsigned defaultValue,
+                    unsigned flags, cudaGraphConditionalHandle* h, cudaGraph_t* bodies) {
   cudaStreamCaptureStatus cs;
   cudaGraph_t capG = nullptr;
   const cudaGraphNode_t* deps = nullptr;
   size_t nd = 0;
   CUDA_TRY(cudaStreamGetCaptureInfo(s, &cs, nullptr, &capG, &deps, nullptr, &nd));
   if (cs != cudaStreamCaptureStatusActive) return fail(HOBAK_ERR_CUDA, "stream is not capturing");
-  cudaGraphConditionalHandle h;
-  CUDA_TRY(cudaGraphConditionalHandleCreate(&h, capG, 1, cudaGraphCondAssignDefault));
+  CUDA_TRY(cudaGraphConditionalHandleCreate(h, capG, defaultValue, flags));
   cudaGraphNodeParams p = {};
   p.type = cudaGraphNodeTypeConditional;
-  p.conditional.handle = h;
-  p.conditional.type = cudaGraphCondTypeWhile;
-  p.conditional.size = 1;
+  p.conditional.handle = *h;
+  p.conditional.type = type;
+  p.conditional.size = size;
   cudaGraphNode_t node;
   CUDA_TRY(cudaGraphAddNode(&node, capG, deps, nullptr, nd, &p));
-  cudaGraph_t body = p.conditional.phGraph_out[0];
+  for (unsigned k = 0; k < size; k++) bodies[k] = p.conditional.phGraph_out[k];
   CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-  CUDA_TRY(cudaStreamBeginCaptureToGraph(B->captureStream, body, nullptr, nullptr, 0,
-                                         cudaStreamCaptureModeThreadLocal));
-  enqueue_chunk<T>(B->d, v, B->captureStream, B->chunk);
-  launch_continue(B->d, (unsigned long long)h, B->captureStream);
-  cudaGraph_t out = nullptr;
-  CUDA_TRY(cudaStreamEndCapture(B->captureStream, &out));
   return HOBAK_OK;
 }
 
-// Eager loop: chunks until the device reports no running scene (host polls).
+// While-loop node on the capturing stream `s`.  Body: tile compaction, which
+// also selects a grid class; a switch node whose bodies are the chunk of
+// PCG iterations at each class's grid; k_continue, which keeps the loop
+// going while any scene's inner PCG runs.
+template <typename T>
+int capture_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
+  cudaGraphConditionalHandle hw, hs;
+  cudaGraph_t body, cls[kGridClasses];
+  if (int rc = add_conditional(s, cudaGraphCondTypeWhile, 1, 1, cudaGraphCondAssignDefault, &hw, &body)) return rc;
+  CUDA_TRY(cudaStreamBeginCaptureToGraph(B->captureStream, body, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+  const GridClasses gc = grid_classes(B->d.ntiles);
+  int rc = HOBAK_OK;
+  {
+    // the switch handle belongs to the body graph, which is being captured
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t capG = nullptr;
+    CUDA_TRY(cudaStreamGetCaptureInfo(B->captureStream, &cs, nullptr, &capG, nullptr, nullptr, nullptr));
+    CUDA_TRY(cudaGraphConditionalHandleCreate(&hs, capG, 0, 0));
+  }
+  launch_compact_tiles(B->d, B->captureStream, (unsigned long long)hs, &gc);
+  {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t capG = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CUDA_TRY(cudaStreamGetCaptureInfo(B->captureStream, &cs, nullptr, &capG, &deps, nullptr, &nd));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = hs;
+    p.conditional.type = cudaGraphCondTypeSwitch;
+    p.conditional.size = (unsigned)gc.n;
+    cudaGraphNode_t node;
+    CUDA_TRY(cudaGraphAddNode(&node, capG, deps, nullptr, nd, &p));
+    for (int k = 0; k < gc.n; k++) cls[k] = p.conditional.phGraph_out[k];
+    CUDA_TRY(cudaStreamUpdateCaptureDependencies(B->captureStream, &node, nullptr, 1,
+                                                 cudaStreamSetCaptureDependencies));
+  }
+  for (int k = 0; k < gc.n && !rc; k++) {
+    CUDA_TRY(cudaStreamBeginCaptureToGraph(B->captureStream2, cls[k], nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal));
+    enqueue_chunk<T>(B->d, v, B->captureStream2, B->chunk, gc.grid[k]);
+    cudaGraph_t out = nullptr;
+    CUDA_TRY(cudaStreamEndCapture(B->captureStream2, &out));
+  }
+  launch_continue(B->d, (unsigned long long)hw, B->captureStream);
+  cudaGraph_t out = nullptr;
+  CUDA_TRY(cudaStreamEndCapture(B->captureStream, &out));
+  return rc;
+}
+
+// Eager loop: compaction, then (host polls) the chunk at the grid class that
+// covers the tiles left, until the device reports no running scene.
 template <typename T>
 int eager_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
+  const GridClasses gc = grid_classes(B->d.ntiles);
   for (int iters = 0; iters <= B->opts.max_iters; iters += B->chunk) {
+    launch_compact_tiles(B->d, s);
     CUDA_TRY(cudaMemcpyAsync(B->pinnedActive, B->d.active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(B->pinnedActive + 1, B->d.nLoopTiles, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
-    if (*B->pinnedActive <= 0) break;
-    enqueue_chunk<T>(B->d, v, s, B->chunk);
+    if (B->pinnedActive[0] <= 0) break;
+    int k = 0;
+    while (k + 1 < gc.n && gc.grid[k + 1] >= B->pinnedActive[1]) k++;
+    enqueue_chunk<T>(B->d, v, s, B->chunk, gc.grid[k]);
     B->eagerChunks++;
   }
   return HOBAK_OK;
@@ -1101,10 +1157,11 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
     hobak_default_solver_opts(&B->opts);
   CUDA_TRY(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
   CUDA_TRY(cudaStreamCreateWithFlags(&B->captureStream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaStreamCreateWithFlags(&B->captureStream2, cudaStreamNonBlocking));
   for (auto& cs : B->classStream) CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreateWithFlags(&B->evFork, cudaEventDisableTiming));
   for (auto& e : B->evJoin) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  CUDA_TRY(cudaMallocHost(&B->pinnedActive, sizeof(int)));
+  CUDA_TRY(cudaMallocHost(&B->pinnedActive, 2 * sizeof(int)));
   CUDA_TRY(cudaMallocHost(&B->solvePinned, sizeof(SolveState) * nscenes));
   for (auto& e : B->ev) CUDA_TRY(cudaEventCreate(&e));
   if ((rc = build_batch(B.get(), scenes, nscenes))) {
@@ -1124,6 +1181,7 @@ int hobak_batch_destroy(hobak_batch b) {
   if (b->collArena) cudaFree(b->collArena);
   drop_graphs(b);
   if (b->captureStream) cudaStreamDestroy(b->captureStream);
+  if (b->captureStream2) cudaStreamDestroy(b->captureStream2);
   for (auto& cs : b->classStream)
     if (cs) cudaStreamDestroy(cs);
   if (b->evFork) cudaEventDestroy(b->evFork);
@@ -1493,6 +1551,7 @@ int hobak_batch_get_tuning(hobak_batch b, hobak_tuning* out) {
   out->assembly_threads = b->d.asmThreads;
   out->pcg_chunk = b->chunk;
   out->cluster_pcg = b->clusterPcg ? 1 : 0;
+  out->cluster_max = b->clusterMax;
   out->step_ms = 0.0;
   return HOBAK_OK;
 }
@@ -1507,6 +1566,8 @@ int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t) {
   if (t->tile_vertices != 64 && t->tile_vertices != 128)
     return fail(HOBAK_ERR_INVALID, "tile_vertices must be 64 or 128");
   if (t->cluster_pcg != 0 && t->cluster_pcg != 1) return fail(HOBAK_ERR_INVALID, "cluster_pcg must be 0 or 1");
+  if (t->cluster_max != 1 && t->cluster_max != 2 && t->cluster_max != 4 && t->cluster_max != 8 && t->cluster_max != 16)
+    return fail(HOBAK_ERR_INVALID, "cluster_max must be 1, 2, 4, 8 or 16");
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   if (t->tile_vertices != b->d.tileV) {
     const int rc = apply_tile_size(b, t->tile_vertices);
@@ -1519,8 +1580,9 @@ int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t) {
   }
   b->d.elemThreads = t->element_threads;
   b->d.asmThreads = t->assembly_threads;
-  if ((t->cluster_pcg != 0) != b->clusterPcg) {
+  if ((t->cluster_pcg != 0) != b->clusterPcg || t->cluster_max != b->clusterMax) {
     b->clusterPcg = t->cluster_pcg != 0;
+    b->clusterMax = t->cluster_max;
     b->clusterDirty = true;
   }
   drop_graphs(b);
@@ -1616,14 +1678,17 @@ int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out) {
     }
     d.asmThreads = best.assembly_threads;
   }
-  // 3. whole steps per (cluster-resident PCG on/off, tile size, chunk), each
-  //    from the saved state
+  // 3. whole steps per (PCG path: tile path only, or clusters of at most 4,
+  //    8 or 16 CTAs for the scenes that fit; tile size; chunk), each from the
+  //    saved state
   double bestStep = 1e300;
   hobak_tuning trial = best;
-  for (int cp : {0, 1})
+  const int paths[4][2] = {{0, 16}, {1, 4}, {1, 8}, {1, 16}};
+  for (const auto& path : paths)
   for (int tv : {64, 128})
     for (int ch : {4, 8, 16}) {
-      trial.cluster_pcg = cp;
+      trial.cluster_pcg = path[0];
+      trial.cluster_max = path[1];
       trial.tile_vertices = tv;
       trial.pcg_chunk = ch;
       int rc = hobak_batch_set_tuning(b, &trial);
@@ -1642,7 +1707,8 @@ int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out) {
       }
       if (total < bestStep) {
         bestStep = total;
-        best.cluster_pcg = cp;
+        best.cluster_pcg = path[0];
+        best.cluster_max = path[1];
         best.tile_vertices = tv;
         best.pcg_chunk = ch;
       }

@@ -7,7 +7,9 @@
 // from the other CTAs' shared memory (distributed shared memory), and every
 // dot product is a CTA tree followed by a fixed-order sum of the CL CTA
 // partials read through distributed shared memory.  An iteration is two
-// cluster barriers; the matrix and Minv stay in L2 across iterations.  The
+// cluster barriers (the fused reduction after the SpMV, and the publication
+// of the new u after the update); the matrix and Minv stay in L2 across
+// iterations.  The
 // tile path (solver.cu: two grid-wide kernels per iteration, each ending in
 // a ticketed reduction) remains for scenes too large for a cluster and for
 // scenes with contact.
@@ -32,14 +34,14 @@ namespace {
 
 __device__ __forceinline__ bool finite_d(double x) { return x == x && fabs(x) <= DBL_MAX; }
 
-// Shared memory of one CTA: [slots: 8 doubles][warp partials: 2 * kClusterWarps T]
+// Shared memory of one CTA: [slots: 8 doubles][warp partials: 3 * kClusterWarps T]
 // [u, p, s, w, d, r: 3 * vpc T each].
-constexpr int kSlotBytes = 8 * sizeof(double) + 2 * kClusterWarps * sizeof(double);
+constexpr int kSlotBytes = 8 * sizeof(double) + 3 * kClusterWarps * sizeof(double);
 
 template <typename T>
 struct ClusterSmem {
   double* slots;  // [1] |r|^2, [2] (r, u), [3] delta (a barrier separates reuse)
-  T* warp;        // 2 * kClusterWarps
+  T* warp;        // 3 * kClusterWarps
   T *u, *p, *s, *w, *d, *r;
 };
 
@@ -98,6 +100,48 @@ __device__ __forceinline__ void cluster_sum2(cg::cluster_group& cluster, const C
       const double* rs = cluster.map_shared_rank(m.slots, rnk);
       sa += rs[slot];
       sb += rs[slot + 1];
+    }
+  }
+}
+
+// Three sums as cluster_sum2 (slots slot .. slot + 2).
+template <int CL, typename T>
+__device__ __forceinline__ void cluster_sum3(cg::cluster_group& cluster, const ClusterSmem<T>& m, T a, T b, T c,
+                                             int slot, double (&out)[3]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (lane == 0) {
+    m.warp[wid] = a;
+    m.warp[kClusterWarps + wid] = b;
+    m.warp[2 * kClusterWarps + wid] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T ta = T(0), tb = T(0), tc = T(0);
+#pragma unroll
+    for (int i = 0; i < kClusterWarps; i++) {
+      ta += m.warp[i];
+      tb += m.warp[kClusterWarps + i];
+      tc += m.warp[2 * kClusterWarps + i];
+    }
+    m.slots[slot] = double(ta);
+    m.slots[slot + 1] = double(tb);
+    m.slots[slot + 2] = double(tc);
+  }
+  cluster.sync();
+  out[0] = out[1] = out[2] = 0.0;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int rnk = 0; rnk < CL; rnk++) {
+      const double* rs = cluster.map_shared_rank(m.slots, rnk);
+      out[0] += rs[slot];
+      out[1] += rs[slot + 1];
+      out[2] += rs[slot + 2];
     }
   }
 }
@@ -172,8 +216,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
   }
   __syncthreads();
   while (!bc.stop) {
-    // ---- w = A u over my vertices; delta = (w, u) ----
-    T dl = T(0);
+    // ---- w = A u over my vertices; delta = (w, u), gamma = (r, u), |r|^2 ----
+    T dl = T(0), gl = T(0), rl = T(0);
     for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
       const int u = v0 + my0 + lv;
       T a0 = T(0), a1 = T(0), a2 = T(0);
@@ -215,26 +259,52 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
       m.w[3 * lv] = a0;
       m.w[3 * lv + 1] = a1;
       m.w[3 * lv + 2] = a2;
-      dl += a0 * m.u[3 * lv] + a1 * m.u[3 * lv + 1] + a2 * m.u[3 * lv + 2];
+      const T u0 = m.u[3 * lv], u1 = m.u[3 * lv + 1], u2 = m.u[3 * lv + 2];
+      const T r0 = m.r[3 * lv], r1 = m.r[3 * lv + 1], r2 = m.r[3 * lv + 2];
+      dl += a0 * u0 + a1 * u1 + a2 * u2;
+      gl += r0 * u0 + r1 * u1 + r2 * u2;
+      rl += r0 * r0 + r1 * r1 + r2 * r2;
     }
-    double delta, unused;
-    cluster_sum2<CL, T>(cluster, m, dl, T(0), 3, delta, unused);
+    double sums[3];
+    cluster_sum3<CL, T>(cluster, m, rl, gl, dl, 1, sums);
     if (t0) {
-      if (iters == 0) {
-        beta = 0.0;
-        alpha = gamma / delta;
-      } else {
-        beta = gamma / gammaOld;
-        alpha = gamma / (delta - beta * gamma / alpha);
+      // after an update: the convergence test on its residual, then the
+      // scalars of this iteration's update (tile path: spmv_decide)
+      int stop = 0;
+      if (iters > 0) {
+        srr = sums[0];
+        if (srr < innerThr) {
+          stop = 1;
+        } else if (!finite_d(srr) || !finite_d(sums[1]) || !finite_d(alpha)) {
+          stop = 1;
+          converged = -1;
+          outerDone = 1;
+        } else if (totalIters >= maxit) {
+          stop = 1;
+        }
+      }
+      if (!stop) {
+        const double g = sums[1], delta = sums[2];
+        if (iters == 0) {
+          beta = 0.0;
+          alpha = g / delta;
+        } else {
+          beta = g / gamma;
+          alpha = g / (delta - beta * g / alpha);
+        }
+        gammaOld = gamma;
+        gamma = g;
+        iters += 1;
+        totalIters += 1;
       }
       bc.alpha = T(alpha);
       bc.beta = T(beta);
+      bc.stop = stop;
     }
     __syncthreads();
+    if (bc.stop) break;
     const T ta = bc.alpha, tb = bc.beta;
     // ---- p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s, u = Minv r ----
-    rr = T(0);
-    ru = T(0);
     for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
       const int u = v0 + my0 + lv;
       T r3[3];
@@ -248,36 +318,13 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
         m.d[j] += ta * p;
         r3[i] = m.r[j] - ta * sv;
         m.r[j] = r3[i];
-        rr += r3[i] * r3[i];
       }
       const T* M = v.minv + 9 * (size_t)u;
 #pragma unroll
-      for (int i = 0; i < 3; i++) {
-        const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
-        m.u[3 * lv + i] = ui;
-        ru += r3[i] * ui;
-      }
+      for (int i = 0; i < 3; i++) m.u[3 * lv + i] = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
     }
-    // the cluster barrier inside also publishes the new u to the other CTAs
-    cluster_sum2<CL, T>(cluster, m, rr, ru, 1, srr, sru);
-    if (t0) {
-      iters += 1;
-      totalIters += 1;
-      int stop = 0;
-      if (srr < innerThr) {
-        stop = 1;
-      } else if (!finite_d(srr) || !finite_d(sru) || !finite_d(alpha)) {
-        stop = 1;
-        converged = -1;
-        outerDone = 1;
-      } else {
-        gammaOld = gamma;
-        gamma = sru;
-        if (totalIters >= maxit) stop = 1;
-      }
-      bc.stop = stop;
-    }
-    __syncthreads();
+    // the new u reaches the other CTAs' SpMV
+    cluster.sync();
   }
   // ---- results: the correction d (FP64 path: the solution y itself) ----
   for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {

@@ -135,20 +135,32 @@ template <typename T>
 void launch_diag_inverse(const DeviceBatch& b, const PcgVecs<T>& v, int precond, cudaStream_t s);
 void launch_rhs(const DeviceBatch& b, cudaStream_t s);
 void launch_set_active(const DeviceBatch& b, cudaStream_t s);
-void launch_compact_tiles(const DeviceBatch& b, cudaStream_t s);
+// Grid sizes of the PCG loop kernels: class 0 launches a CTA per tile of
+// the batch, the smaller classes a CTA per tile still iterating at most.
+constexpr int kGridClasses = 5;
+struct GridClasses {
+  int n;                   // classes in use (1..kGridClasses)
+  int grid[kGridClasses];  // decreasing; grid[0] = ntiles
+};
+GridClasses grid_classes(int ntiles);
+// Compaction of the tiles still iterating; with a switch handle (graph mode)
+// it also selects the smallest grid class that covers them.
+void launch_compact_tiles(const DeviceBatch& b, cudaStream_t s, unsigned long long switchHandle = 0,
+                          const GridClasses* classes = nullptr);
 template <typename T>
 void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s);
 template <typename T>
-void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl = false);
+void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl = false, int grid = 0);
 template <typename T>
-void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl = false);
+void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl = false, int grid = 0);
 template <typename T>
 // One PCG iteration.  The update always overlaps the SpMV's drain; the SpMV
 // overlaps the previous update's except right after k_compact_tiles (`first`),
 // whose tile list it reads before its dependency wait.
-void launch_pcg_iteration(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool first = false) {
-  launch_spmv<T>(b, v, s, !first);
-  launch_update<T>(b, v, s, true);
+void launch_pcg_iteration(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool first = false,
+                          int grid = 0) {
+  launch_spmv<T>(b, v, s, !first, grid);
+  launch_update<T>(b, v, s, true, grid);
 }
 void launch_refine(const DeviceBatch& b, cudaStream_t s);  // y += d, then r64 = rhs - A y
 void launch_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s);void launch_finish_step(const DeviceBatch& b, cudaStream_t s);

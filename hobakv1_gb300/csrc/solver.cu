@@ -9,12 +9,17 @@
 // recursive residual.
 //
 // PCG runs in the Chronopoulos-Gear arrangement (same iterates as the
-// textbook loop in exact arithmetic) so that each iteration is exactly two
-// kernels with one reduction each and the SpMV multiplies a vector that is
-// already final:
-//   k_spmv:   w = A u, delta = (w, u)          -> beta, alpha
+// textbook loop in exact arithmetic) with its three dot products fused into
+// one reduction, so each iteration is two kernels and a single scene-wide
+// reduction, and the SpMV multiplies a vector that is already final:
+//   k_spmv:   w = A u; delta = (w, u), gamma = (r, u), |r|^2
+//             -> convergence test on |r|^2 (the residual of the last
+//                update), then beta, alpha
 //   k_update: p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s,
-//             u = Minv r, gamma = (r, u), |r|^2 -> convergence test
+//             u = Minv r  (no reduction)
+// The test on |r_k|^2 thus runs at the start of iteration k rather than at
+// the end of k - 1: same decision, same iterates and iteration count; a
+// stopping scene computes one SpMV it does not use.
 // On GB300 the FP64 pipe, not HBM, bounds the FP64 SpMV, so the product does
 // only the 9 DFMA per block it must (one thread per vertex, no lane
 // reductions).  The LHS is stored in 32-vertex slices (lhs_slot), so the
@@ -97,6 +102,40 @@ __device__ __forceinline__ void block_sum2(R a, R b, double* sh, double& sa, dou
   __syncthreads();
 }
 
+// Three sums in one pass (one pair of barriers), each in the order of
+// block_sum; results valid in thread 0.  `sh` holds 3 * NT / 32 doubles.
+template <int NT, typename R>
+__device__ __forceinline__ void block_sum3(R a, R b, R c, double* sh, double (&out)[3]) {
+  R* shr = reinterpret_cast<R*>(sh);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  if (l == 0) {
+    shr[w] = a;
+    shr[NT / 32 + w] = b;
+    shr[2 * (NT / 32) + w] = c;
+  }
+  __syncthreads();
+  out[0] = out[1] = out[2] = 0.0;
+  if (threadIdx.x == 0) {
+    R ta = R(0), tb = R(0), tc = R(0);
+#pragma unroll
+    for (int i = 0; i < NT / 32; i++) {
+      ta += shr[i];
+      tb += shr[NT / 32 + i];
+      tc += shr[2 * (NT / 32) + i];
+    }
+    out[0] = double(ta);
+    out[1] = double(tb);
+    out[2] = double(tc);
+  }
+  __syncthreads();
+}
+
 // After thread 0 wrote the CTA's partial(s): true in the CTA that finishes
 // the scene's reduction (ticket == ntiles - 1).  Only thread 0 published
 // anything the last CTA reads, so only it fences before taking its ticket.
@@ -120,6 +159,19 @@ __device__ __forceinline__ double sum_partials(const double* partial, int tile0,
   double s = 0;
   for (int i = threadIdx.x; i < n; i += NT) s += __ldcg(&partial[(size_t)(tile0 + i) * kPartials + comp]);
   return block_sum<NT>(s, sh);
+}
+
+// Partials 0..2 of a scene's tiles, each summed in tile order (one pass).
+template <int NT>
+__device__ __forceinline__ void sum_partials3(const double* partial, int tile0, int n, double* sh, double (&out)[3]) {
+  double a = 0, b = 0, c = 0;
+  for (int i = threadIdx.x; i < n; i += NT) {
+    const double* q = partial + (size_t)(tile0 + i) * kPartials;
+    a += __ldcg(q);
+    b += __ldcg(q + 1);
+    c += __ldcg(q + 2);
+  }
+  block_sum3<NT>(a, b, c, sh, out);
 }
 
 __device__ __forceinline__ bool finite(double x) { return x == x && fabs(x) <= DBL_MAX; }
@@ -533,19 +585,53 @@ __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int
 template <typename T>
 __host__ __device__ constexpr int spmv_threads(int TV) { return sizeof(T) == sizeof(float) ? TV : 3 * TV; }
 
-// beta, alpha from delta = (w, u) in the scene's last CTA
-__device__ __forceinline__ void spmv_scalars(SolveState& st, double delta) {
+// The scene's iteration step in its last SpMV CTA (thread 0), from
+// rho = |r|^2, gamma = (r, u) and delta = (w, u): after an update, stop when
+// |r|^2 < threshold (ConjugateGradient.h:75-78), on a non-finite value, or at
+// the iteration limit; otherwise beta and alpha for this iteration's update,
+// which the iteration count then includes.
+template <typename T>
+__device__ __forceinline__ void spmv_decide(const DeviceBatch& b, SolveState& st, double rho, double gamma,
+                                            double delta) {
+  if (st.iters > 0) {
+    st.rr = rho;
+    bool stop = false;
+    if (rho < st.innerThreshold) {
+      stop = true;
+    } else if (!finite(rho) || !finite(gamma) || !finite(st.alpha)) {
+      stop = true;
+      st.converged = -1;
+      st.outerDone = 1;
+    } else if (st.totalIters >= st.maxit) {
+      stop = true;
+    }
+    if (stop) {
+      st.done = 1;
+      atomicSub(b.active, 1);
+      if (sizeof(T) == sizeof(double) && st.converged >= 0) {
+        // FP64 path: the recursive residual is the solver's verdict (Eigen)
+        st.rr64 = rho;
+        st.converged = rho < st.threshold ? 1 : 0;
+        st.outerDone = 1;
+      }
+      return;
+    }
+  }
   st.delta = delta;
   if (st.iters == 0) {
     st.beta = 0.0;
-    st.alpha = st.gamma / delta;
+    st.alpha = gamma / delta;
   } else {
-    const double beta = st.gamma / st.gammaOld;
+    const double beta = gamma / st.gamma;  // st.gamma: the previous iteration's (r, u)
     st.beta = beta;
-    st.alpha = st.gamma / (delta - beta * st.gamma / st.alpha);
+    st.alpha = gamma / (delta - beta * gamma / st.alpha);
   }
+  st.gammaOld = st.gamma;
+  st.gamma = gamma;
   st.alphaF = float(st.alpha);
   st.betaF = float(st.beta);
+  st.iters += 1;
+  st.totalIters += 1;
 }
 
 // FP64: w = A u, one thread per scalar row (9 DFMA per block over the row's
@@ -573,7 +659,8 @@ __device__ __forceinline__ void spmv_tile_rows(const DeviceBatch& b, const PcgVe
   pdl_wait();
   SolveState& st = b.solve[s];
   if (st.done) return;
-  T dl = T(0);
+  const T* __restrict__ r = (sizeof(T) == sizeof(double)) ? reinterpret_cast<const T*>(b.r64) : v.r;
+  T dl = T(0), gl = T(0), rl = T(0);
   if (valid) {
     const T* __restrict__ uu = v.u;
     // Four blocks per trip, all their loads issued together (predicated past
@@ -601,14 +688,23 @@ __device__ __forceinline__ void spmv_tile_rows(const DeviceBatch& b, const PcgVe
     T acc = acc0 + acc1;
     if (b.collOn && b.freeMask[u]) acc += T(collision_row<T>(b, u, i, uu));
     v.w[row] = acc;
-    dl = acc * uu[row];
+    const T ui = uu[row], ri = r[row];
+    dl = acc * ui;
+    gl = ri * ui;
+    rl = ri * ri;
   }
-  const double t = block_sum<3 * TV>(dl, sh);
-  if (threadIdx.x == 0) b.partial[kPartials * tile + 2] = t;
+  double t[3];
+  block_sum3<3 * TV>(rl, gl, dl, sh, t);
+  if (threadIdx.x == 0) {
+    b.partial[kPartials * tile] = t[0];
+    b.partial[kPartials * tile + 1] = t[1];
+    b.partial[kPartials * tile + 2] = t[2];
+  }
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketA, sp.ntiles, flag)) return;
-  const double delta = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 2, sh);
-  if (threadIdx.x == 0) spmv_scalars(st, delta);
+  double tot[3];
+  sum_partials3<3 * TV>(b.partial, sp.tile0, sp.ntiles, sh, tot);
+  if (threadIdx.x == 0) spmv_decide<T>(b, st, tot[0], tot[1], tot[2]);
 }
 
 // FP32: w = A u, one thread per vertex (its three rows; 9 FMA per block), and
@@ -639,7 +735,7 @@ __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>
   // the done test waits for its load only after the first trip's loads are
   // in flight
   const int done = st.done;
-  T dl = T(0);
+  T dl = T(0), gl = T(0), rl = T(0);
   if (valid) {
     const T* __restrict__ uu = v.u;
     // Q blocks per trip (4 in FP32, 2 in FP64: register budget), all their
@@ -682,15 +778,25 @@ __device__ __forceinline__ void spmv_tile(const DeviceBatch& b, const PcgVecs<T>
     v.w[3 * u] = a0;
     v.w[3 * u + 1] = a1;
     v.w[3 * u + 2] = a2;
-    dl = a0 * uu[3 * u] + a1 * uu[3 * u + 1] + a2 * uu[3 * u + 2];
+    const T u0 = uu[3 * u], u1 = uu[3 * u + 1], u2 = uu[3 * u + 2];
+    const T r0 = v.r[3 * u], r1 = v.r[3 * u + 1], r2 = v.r[3 * u + 2];
+    dl = a0 * u0 + a1 * u1 + a2 * u2;
+    gl = r0 * u0 + r1 * u1 + r2 * u2;
+    rl = r0 * r0 + r1 * r1 + r2 * r2;
   }
   if (done) return;  // threads without rows (the CTA returns as one)
-  const double t = block_sum<TV>(dl, sh);
-  if (threadIdx.x == 0) b.partial[kPartials * tile + 2] = t;
+  double t[3];
+  block_sum3<TV>(rl, gl, dl, sh, t);
+  if (threadIdx.x == 0) {
+    b.partial[kPartials * tile] = t[0];
+    b.partial[kPartials * tile + 1] = t[1];
+    b.partial[kPartials * tile + 2] = t[2];
+  }
   const SceneParams& sp = b.scenes[s];
   if (!last_tile(&st.ticketA, sp.ntiles, flag)) return;
-  const double delta = sum_partials<TV>(b.partial, sp.tile0, sp.ntiles, 2, sh);
-  if (threadIdx.x == 0) spmv_scalars(st, delta);
+  double tot[3];
+  sum_partials3<TV>(b.partial, sp.tile0, sp.ntiles, sh, tot);
+  if (threadIdx.x == 0) spmv_decide<T>(b, st, tot[0], tot[1], tot[2]);
 }
 
 // CTA -> tile of the PCG loop kernels (grid = all tiles).  While every scene
@@ -705,7 +811,7 @@ __device__ __forceinline__ int loop_tile(const DeviceBatch& b) {
 
 template <int TV, typename T>
 __global__ void __launch_bounds__(spmv_threads<T>(TV)) k_spmv(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[spmv_threads<T>(TV) / 32];
+  __shared__ double sh[3 * spmv_threads<T>(TV) / 32];
   __shared__ int flag;
   pdl_trigger();
   const int tile = loop_tile(b);
@@ -714,14 +820,13 @@ __global__ void __launch_bounds__(spmv_threads<T>(TV)) k_spmv(DeviceBatch b, Pcg
   else spmv_tile_rows<TV, T>(b, v, tile, sh, &flag);
 }
 
-// p = u + beta p; s = w + beta s; d += alpha p; r -= alpha s; u = Minv r;
-// gamma' = (r, u); |r|^2 -> stop when |r|^2 < threshold (ConjugateGradient.h:75-78).
+// p = u + beta p; s = w + beta s; d += alpha p; r -= alpha s; u = Minv r
+// (the dot products of the new r and u are the next SpMV's).
 template <int TV, typename T>
 // One thread per scalar row (three times the threads of a per-vertex loop,
 // which a 40^3 scene needs to cover the GPU's latency), 30 rows per warp; the
 // 3x3 block of Minv reads its vertex's three new residual rows by shuffles.
-__device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile, double* sh,
-                                            int* flag) {
+__device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<T>& v, int tile) {
   // before the dependency wait: what the previous kernel does not write
   const int s = b.tileScene[tile];
   const int lane = threadIdx.x % 32;
@@ -761,7 +866,6 @@ __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<
     r0 = r[row];
   }
   if (done) return;
-  T rr = T(0), ru = T(0);
   T rnew = T(0);
   if (valid) {
     const T p = u0 + beta * p0;
@@ -771,7 +875,6 @@ __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<
     v.d[row] = d0 + alpha * p;
     rnew = r0 - alpha * sv;
     r[row] = rnew;
-    rr = rnew * rnew;
   }
   // the vertex's three new residual rows sit in lanes base..base+2 of this
   // warp (10 vertices per warp): exchange them by shuffles, no barrier
@@ -779,63 +882,23 @@ __device__ __forceinline__ void update_tile(const DeviceBatch& b, const PcgVecs<
   const T ra = __shfl_sync(0xffffffffu, rnew, base);
   const T rb = __shfl_sync(0xffffffffu, rnew, base + 1);
   const T rc = __shfl_sync(0xffffffffu, rnew, base + 2);
-  if (valid) {
-    const T ui = M0 * ra + M1 * rb + M2 * rc;
-    v.u[row] = ui;
-    ru = rnew * ui;
-  }
-  constexpr int NT = 32 * update_warps(TV);
-  double trr, tru;
-  block_sum2<NT>(rr, ru, sh, trr, tru);
-  if (threadIdx.x == 0) {
-    b.partial[kPartials * tile] = trr;
-    b.partial[kPartials * tile + 1] = tru;
-  }
-  const SceneParams& sp = b.scenes[s];
-  if (!last_tile(&st.ticketB, sp.ntiles, flag)) return;
-  const double srr = sum_partials<NT>(b.partial, sp.tile0, sp.ntiles, 0, sh);
-  const double sru = sum_partials<NT>(b.partial, sp.tile0, sp.ntiles, 1, sh);
-  if (threadIdx.x == 0) {
-    st.rr = srr;
-    st.iters += 1;
-    st.totalIters += 1;
-    bool stop = false;
-    if (srr < st.innerThreshold) {
-      stop = true;
-    } else if (!finite(srr) || !finite(sru) || !finite(st.alpha)) {
-      stop = true;
-      st.converged = -1;
-      st.outerDone = 1;
-    } else {
-      st.gammaOld = st.gamma;
-      st.gamma = sru;
-      if (st.totalIters >= st.maxit) stop = true;
-    }
-    if (stop) {
-      st.done = 1;
-      atomicSub(b.active, 1);
-      if (sizeof(T) == sizeof(double) && st.converged >= 0) {
-        // FP64 path: the recursive residual is the solver's verdict (Eigen)
-        st.rr64 = srr;
-        st.converged = srr < st.threshold ? 1 : 0;
-        st.outerDone = 1;
-      }
-    }
-  }
+  if (valid) v.u[row] = M0 * ra + M1 * rb + M2 * rc;
 }
 
 template <int TV, typename T>
 __global__ void __launch_bounds__(32 * update_warps(TV), TV == 64 ? 8 : 4) k_update(DeviceBatch b, PcgVecs<T> v) {
-  __shared__ double sh[2 * update_warps(TV)];
-  __shared__ int flag;
   pdl_trigger();
   const int tile = loop_tile(b);
-  if (tile >= 0) update_tile<TV, T>(b, v, tile, sh, &flag);
+  if (tile >= 0) update_tile<TV, T>(b, v, tile);
 }
 
 // Compacted list of the tiles whose scene's inner PCG still runs, rebuilt at
 // the start of every PCG loop body (one CTA; scenes in order, tiles in order).
-__global__ void __launch_bounds__(1024) k_compact_tiles(DeviceBatch b) {
+// In graph mode it also picks the loop body's grid class: the smallest grid
+// that covers the tiles left, so that late iterations with few scenes still
+// running do not launch a CTA per tile of the batch.
+__global__ void __launch_bounds__(1024) k_compact_tiles(DeviceBatch b, unsigned long long switchHandle,
+                                                        GridClasses classes) {
   __shared__ int warpTot[32];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
@@ -871,7 +934,14 @@ __global__ void __launch_bounds__(1024) k_compact_tiles(DeviceBatch b) {
     if (threadIdx.x == 0) carry += warpTot[31];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *b.nLoopTiles = carry;
+  if (threadIdx.x == 0) {
+    *b.nLoopTiles = carry;
+    if (switchHandle) {
+      int k = 0;
+      while (k + 1 < classes.n && classes.grid[k + 1] >= carry) k++;
+      cudaGraphSetConditional((cudaGraphConditionalHandle)switchHandle, (unsigned)k);
+    }
+  }
 }
 
 // Mixed precision, after an inner solve: y += d (FP64), one vertex per thread.
@@ -1014,7 +1084,20 @@ void launch_rhs(const DeviceBatch& b, cudaStream_t s) { HOBAK_TILE_LAUNCH(k_rhs,
 
 void launch_set_active(const DeviceBatch& b, cudaStream_t s) { k_set_active<<<1, 32, 0, s>>>(b); }
 
-void launch_compact_tiles(const DeviceBatch& b, cudaStream_t s) { k_compact_tiles<<<1, 1024, 0, s>>>(b); }
+GridClasses grid_classes(int ntiles) {
+  GridClasses c{};
+  c.n = 1;
+  c.grid[0] = ntiles;
+  for (int g : {4096, 1024, 256, 64})
+    if (g < c.grid[c.n - 1] && c.n < kGridClasses) c.grid[c.n++] = g;
+  return c;
+}
+
+void launch_compact_tiles(const DeviceBatch& b, cudaStream_t s, unsigned long long switchHandle,
+                          const GridClasses* classes) {
+  const GridClasses c = classes ? *classes : grid_classes(b.ntiles);
+  k_compact_tiles<<<1, 1024, 0, s>>>(b, switchHandle, c);
+}
 
 template <typename T>
 void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s) {
@@ -1023,15 +1106,17 @@ void launch_inner_init(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s
 }
 
 template <typename T>
-void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl) {
-  if (b.tileV == 64) launch_loop_kernel(k_spmv<64, T>, b.ntiles, spmv_threads<T>(64), s, pdl, b, v);
-  else launch_loop_kernel(k_spmv<128, T>, b.ntiles, spmv_threads<T>(128), s, pdl, b, v);
+void launch_spmv(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl, int grid) {
+  if (grid <= 0) grid = b.ntiles;
+  if (b.tileV == 64) launch_loop_kernel(k_spmv<64, T>, grid, spmv_threads<T>(64), s, pdl, b, v);
+  else launch_loop_kernel(k_spmv<128, T>, grid, spmv_threads<T>(128), s, pdl, b, v);
 }
 
 template <typename T>
-void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl) {
-  if (b.tileV == 64) launch_loop_kernel(k_update<64, T>, b.ntiles, 32 * update_warps(64), s, pdl, b, v);
-  else launch_loop_kernel(k_update<128, T>, b.ntiles, 32 * update_warps(128), s, pdl, b, v);
+void launch_update(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_t s, bool pdl, int grid) {
+  if (grid <= 0) grid = b.ntiles;
+  if (b.tileV == 64) launch_loop_kernel(k_update<64, T>, grid, 32 * update_warps(64), s, pdl, b, v);
+  else launch_loop_kernel(k_update<128, T>, grid, 32 * update_warps(128), s, pdl, b, v);
 }
 
 void launch_refine(const DeviceBatch& b, cudaStream_t s) {
@@ -1052,9 +1137,9 @@ template void launch_diag_inverse<double>(const DeviceBatch&, const PcgVecs<doub
 template void launch_diag_inverse<float>(const DeviceBatch&, const PcgVecs<float>&, int, cudaStream_t);
 template void launch_inner_init<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t);
 template void launch_inner_init<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t);
-template void launch_spmv<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t, bool);
-template void launch_spmv<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t, bool);
-template void launch_update<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t, bool);
-template void launch_update<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t, bool);
+template void launch_spmv<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t, bool, int);
+template void launch_spmv<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t, bool, int);
+template void launch_update<double>(const DeviceBatch&, const PcgVecs<double>&, cudaStream_t, bool, int);
+template void launch_update<float>(const DeviceBatch&, const PcgVecs<float>&, cudaStream_t, bool, int);
 
 }  // namespace hobak

@@ -384,7 +384,8 @@ class BATCH:
         check(_lib.load().hobak_batch_kernel_bytes(self.h, dptr(b)), "hobak_batch_kernel_bytes")
         return dict(zip(self.KERNELS, b.tolist()))
 
-    TUNING = ("tile_vertices", "element_threads", "assembly_threads", "pcg_chunk", "cluster_pcg", "step_ms")
+    TUNING = ("tile_vertices", "element_threads", "assembly_threads", "pcg_chunk", "cluster_pcg", "cluster_max",
+              "step_ms")
 
     def get_tuning(self) -> dict:
         """Launch shapes: tile size, element / assembly CTA sizes, PCG chunk."""

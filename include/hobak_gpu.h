@@ -259,8 +259,10 @@ int hobak_batch_kernel_bytes(hobak_batch b, double* bytes);
  * 32), PCG iterations per graph loop body / host poll (1..64), and whether
  * scenes of at most 16 x 1024 vertices without contact solve their inner PCG
  * inside one thread-block cluster (1; beside the tile path for the others) or
- * on the batch-wide tile path (0, the default).  step_ms is the measured step
- * time of the chosen shape (autotune only; 0 otherwise).  The tile size and
+ * on the batch-wide tile path (0, the default), and the largest cluster such
+ * a scene may use (cluster_max: 1, 2, 4, 8 or 16 CTAs; larger scenes keep the
+ * tile path, which spreads them over the whole GPU).  step_ms is the measured
+ * step time of the chosen shape (autotune only; 0 otherwise).  The tile size and
  * the PCG path change results, and only by FP rounding (they change the shape
  * of the dot-product reduction trees). */
 typedef struct hobak_tuning {
@@ -269,13 +271,14 @@ typedef struct hobak_tuning {
   int assembly_threads;
   int pcg_chunk;
   int cluster_pcg;
+  int cluster_max;
   double step_ms;
 } hobak_tuning;
 int hobak_batch_get_tuning(hobak_batch b, hobak_tuning* out);
 int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t);
 /* Autotuner: times the element kernel per CTA size and the assembly kernel
  * per CTA size (reps launches each, CUDA events), then whole steps for every
- * (PCG path, tile size, chunk) from the batch's current state (restored before
+ * (PCG path and cluster cap, tile size, chunk) from the batch's current state (restored before
  * every trial and at the end, so the batch's trajectory is unchanged), and
  * applies the fastest shape.  out may be NULL. */
 int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out);

@@ -32,7 +32,7 @@ def test_cta_sizes_and_chunk_do_not_change_results(precision):
     sc = mix()
     ref = run(sc, precision)
     for shape in (dict(element_threads=64), dict(assembly_threads=128), dict(assembly_threads=512),
-                  dict(pcg_chunk=4), dict(pcg_chunk=16)):
+                  dict(pcg_chunk=4), dict(pcg_chunk=16), dict(cluster_max=4)):
         got = run(sc, precision, **shape)
         for (x, v), (xr, vr) in zip(got, ref):
             assert np.array_equal(x, xr) and np.array_equal(v, vr), shape
@@ -56,6 +56,7 @@ def test_autotune_keeps_state_and_trajectory():
     t = b.autotune(reps=2)
     assert t["tile_vertices"] in (64, 128) and t["element_threads"] in (64, 128)
     assert t["assembly_threads"] in (128, 256, 512) and t["pcg_chunk"] in (4, 8, 16)
+    assert t["cluster_pcg"] in (0, 1) and t["cluster_max"] in (4, 8, 16)
     assert t["step_ms"] > 0
     assert b.get_tuning()["tile_vertices"] == t["tile_vertices"]
     after = [b.get_state(i) for i in range(len(sc))]
@@ -77,6 +78,6 @@ def test_autotune_keeps_state_and_trajectory():
 def test_bad_shapes_are_refused():
     b = hobak.BATCH(mix()[:1], hobak.solver_opts())
     for bad in (dict(tile_vertices=96), dict(element_threads=256), dict(assembly_threads=100),
-                dict(pcg_chunk=0)):
+                dict(pcg_chunk=0), dict(cluster_max=3), dict(cluster_max=32)):
         with pytest.raises(_lib.HobakError):
             b.set_tuning(**bad)

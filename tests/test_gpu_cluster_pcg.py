@@ -73,3 +73,31 @@ def test_contact_scene_keeps_the_tile_path_beside_clusters():
     a.set_collisions(0, True, 1e-3, 1e3, 0.001)
     a.step(4)
     assert np.array_equal(b.get_state(0)[0], a.get_state(0)[0])
+
+
+@pytest.mark.parametrize("precision", [hobak.PRECISION_FP64, hobak.PRECISION_MIXED], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("cap", [2, 4])
+def test_capped_clusters_match_the_tile_path_and_the_scene_alone(precision, cap):
+    """Clusters of at most `cap` CTAs: a scene of more than cap x 1024
+    vertices solves in a capped cluster with several vertices per thread
+    (mixed precision: its FP32 vectors fit in shared memory) or on the tile
+    path (FP64 at cap 2: they do not); either way it agrees with the tile path
+    to rounding and equals itself alone bitwise, beside clustered small ones."""
+    big = scenes.config4_scenes(count=1, nmin=18, nmax=18)[0]  # 5,832 vertices: an 8-CTA cluster uncapped
+    small = scenes.config4_scenes(count=2, nmin=6, nmax=9)
+    mix = [big] + small
+    b = hobak.BATCH(mix, hobak.solver_opts(precision=precision))
+    b.set_tuning(cluster_pcg=1, cluster_max=cap)
+    b.step(4)
+    alone = hobak.BATCH([big], hobak.solver_opts(precision=precision))
+    alone.set_tuning(cluster_pcg=1, cluster_max=cap)
+    alone.step(4)
+    assert np.array_equal(b.get_state(0)[0], alone.get_state(0)[0])
+    tile, _ = run([big], precision, 4, False)
+    bound = 1e-8 if precision == hobak.PRECISION_FP64 else 1e-6
+    assert rel(b.get_state(0)[0] + big.rest.reshape(-1), tile[0]) < bound
+    for k, sc in enumerate(small, start=1):
+        c = hobak.BATCH([sc], hobak.solver_opts(precision=precision))
+        c.set_tuning(cluster_pcg=1)
+        c.step(4)
+        assert np.array_equal(b.get_state(k)[0], c.get_state(0)[0]), k
