@@ -360,9 +360,15 @@ def run_ours(args, spec, scene_list):
     tuning = batch.get_tuning() if args.no_autotune else batch.autotune(reps=3)
 
     # ---- device-resident timed region ----
+    # (phase timers off: their events split the step graph; the per-phase
+    # breakdown is taken after the timed region)
     batch.step(args.warmup)
-    batch.enable_timing(True)
-    batch.phase_times()  # reset
+    # the state the timed steps start from: the e2e loop replays the same steps
+    nvs = [s.nv for s in scene_list]
+    ntot = 3 * sum(nvs)
+    pinned = lambda: torch.empty(ntot, dtype=torch.float64, pin_memory=True).numpy()
+    hx, hv, hf = pinned(), pinned(), pinned()
+    batch.get_state_all(hx, hv)
     launches0 = batch.launch_count()
     iters = []
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
@@ -381,7 +387,13 @@ def run_ours(args, spec, scene_list):
     torch.cuda.synchronize()
     clock = clocks.stop()
     gpu_launches = batch.launch_count() - launches0
+    # per-phase CUDA-event times of a few more steps (outside the timed region)
+    phase_steps = min(args.steps, 5)
+    batch.enable_timing(True)
+    batch.phase_times()  # reset
+    batch.step(phase_steps)
     phases = batch.phase_times()
+    batch.enable_timing(False)
     lat = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[args.steps])
     if world > 1:
@@ -408,12 +420,8 @@ def run_ours(args, spec, scene_list):
 
     # ---- e2e: public API with pinned host buffers in/out every step ----
     # whole-batch calls (every scene's state is contiguous on the device): the
-    # inputs x, v, f_ext go up and x, v come back every step
-    nvs = [s.nv for s in scene_list]
-    ntot = 3 * sum(nvs)
-    pinned = lambda: torch.empty(ntot, dtype=torch.float64, pin_memory=True).numpy()
-    hx, hv, hf = pinned(), pinned(), pinned()
-    batch.get_state_all(hx, hv)
+    # inputs x, v, f_ext go up and x, v come back every step; the same steps
+    # as the timed region, from the same state (hx, hv saved before it)
     off = 0
     for s in scene_list:
         mass = np.zeros(s.nv)
@@ -423,7 +431,7 @@ def run_ours(args, spec, scene_list):
                                s.rest[s.tets[:, 2]] - s.rest[s.tets[:, 0]])) / 6.0), 4))
         hf[off:off + 3 * s.nv] = (mass[:, None] * (s.density * np.array(s.gravity))[None, :]).reshape(-1)
         off += 3 * s.nv
-    e2e_steps = max(3, min(args.steps, 20))
+    e2e_steps = args.steps
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -466,7 +474,7 @@ def run_ours(args, spec, scene_list):
                            "launch_shapes": {**tuning, "chosen_by": "given" if args.no_autotune else "autotuner"}},
                 "pcg_iters_per_step": float(np.mean(iters)),
                 "pcg_iters_per_scene_pct": {q: float(np.percentile(scene_iters, q)) for q in (10, 50, 90, 100)},
-                "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
+                "phases_ms_per_step": {k: v[0] / phase_steps for k, v in phases.items()},
                 "roofline": roofline, "cpu_baseline": cpu, "plain_fp64_gpu": plain, "e2e": e2e,
                 "gpu_launches": int(gpu_launches),
                 "clocks": clock}
