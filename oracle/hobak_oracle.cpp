@@ -922,6 +922,11 @@ struct Sim {
   double collScale = 0.0;        // -(dt beta + dt^2): collision Hessian's weight in A
   int lastIters = 0;
   double lastErr = 0;
+  // integrator: 0 BACKWARD_EULER_VELOCITY, 1 BACKWARD_EULER_POSITION (Rayleigh
+  // damped, C = alpha M + beta K0 with K0 the clamped Hessian at rest)
+  int integrator = 0;
+  double rayAlpha = 0.01, rayBeta = 0.01;  // BACKWARD_EULER_POSITION.cpp:53-54
+  std::vector<double> K0;
 };
 
 // Vertex-face detection at the current displacement: inverted vertices
@@ -1254,6 +1259,63 @@ void step(Sim& s) {
     }
 }
 
+// One BACKWARD_EULER_POSITION::solveRayleighDamped step with collisions off
+// and no plane constraints, so z = 0 (BACKWARD_EULER_POSITION.cpp:138-330):
+//   C   = alpha M + beta K0, K0 = clamped Hessian at zero displacement
+//         (buildRayleighDampingMatrix, TIMESTEPPER.cpp:213-236)
+//   b   = (M/dt - C) v + R + f_ext                              (BEP.cpp:196)
+//   A   = M/dt^2 - C/dt - K                                     (BEP.cpp:207)
+//   LHS = S A S + (I - S), rhs = S b; x += y; v = (x - x_old)/dt; v = S v
+void stepPosition(Sim& s) {
+  const Mesh& M = s.M;
+  const int nv = M.nv;
+  const double dt = s.dt, invDt = 1.0 / dt;
+  const std::vector<double> xOld = s.x;  // _positionOld, before the pins move
+  for (size_t k = 0; k < s.pinned.size(); k++)
+    for (int i = 0; i < 3; i++) s.x[3 * s.pinned[k] + i] = s.pinTarget[3 * k + i];
+  if (s.K0.empty()) {
+    const std::vector<double> keep = s.x;
+    std::fill(s.x.begin(), s.x.end(), 0.0);
+    assemble(s);
+    s.K0 = s.K;
+    s.x = keep;
+  }
+  assemble(s);
+  std::vector<double> rhs(3 * (size_t)nv);
+#pragma omp parallel for schedule(static)
+  for (int u = 0; u < nv; u++) {
+    const double m = s.density * M.oneRing[u];
+    for (int i = 0; i < 3; i++) {
+      double k0v = 0;
+      for (int k = M.rowptr[u]; k < M.rowptr[u + 1]; k++) {
+        const double* blk = &s.K0[9 * (size_t)k];
+        const int w = M.cols[k];
+        for (int c = 0; c < 3; c++) k0v += blk[i + 3 * c] * s.v[3 * w + c];
+      }
+      const size_t q = 3 * (size_t)u + i;
+      const double b = (invDt - s.rayAlpha) * m * s.v[q] - s.rayBeta * k0v + s.R[q] + s.fext[q];
+      rhs[q] = s.free[u] ? b : 0.0;
+    }
+  }
+  s.A.resize(s.K.size());
+  const double cK0 = s.rayBeta * invDt;
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < (long)s.K.size(); k++) s.A[k] = -cK0 * s.K0[k] - s.K[k];
+  for (int u = 0; u < nv; u++) {
+    double* D = &s.A[9 * (size_t)M.diag[u]];
+    const double m = s.density * M.oneRing[u];
+    for (int i = 0; i < 3; i++) D[4 * i] = m * (invDt * invDt - s.rayAlpha * invDt) + D[4 * i];
+  }
+  std::vector<double> y;
+  pcg(s, s.A, rhs, y);
+  for (int u = 0; u < nv; u++)
+    for (int i = 0; i < 3; i++) {
+      const size_t k = 3 * (size_t)u + i;
+      s.x[k] = s.x[k] + y[k];
+      s.v[k] = s.free[u] ? invDt * (s.x[k] - xOld[k]) : 0.0;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1363,7 +1425,8 @@ int oracle_step(void* h, int nsteps, int* iters, double* errs) {
   Sim* s = static_cast<Sim*>(h);
   if (!s) return -1;
   for (int k = 0; k < nsteps; k++) {
-    step(*s);
+    if (s->integrator == 1) stepPosition(*s);
+    else step(*s);
     if (iters) iters[k] = s->lastIters;
     if (errs) errs[k] = s->lastErr;
   }
@@ -1371,6 +1434,19 @@ int oracle_step(void* h, int nsteps, int* iters, double* errs) {
 }
 
 int oracle_nblocks(void* h) { return static_cast<Sim*>(h)->M.rowptr.back(); }
+
+// Integrator: 0 BACKWARD_EULER_VELOCITY, 1 BACKWARD_EULER_POSITION with
+// Rayleigh coefficients alpha, beta (collisions off for the latter).
+int oracle_set_integrator(void* h, int integrator, double alpha, double beta) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s || integrator < 0 || integrator > 1) return -1;
+  if (integrator == 1 && s->coll.on) return -2;
+  s->integrator = integrator;
+  s->rayAlpha = alpha;
+  s->rayBeta = beta;
+  s->K0.clear();
+  return 0;
+}
 
 // Vertex-face self collisions on (eps = collision distance, mu = stiffness,
 // beta = damping), like TIMESTEPPER's flags and setCollisionEps.

@@ -55,6 +55,7 @@ def lib():
         L.oracle_vf_pairs.argtypes = [ctypes.c_void_p, _ip, ctypes.c_int, _ip]
         L.oracle_num_surface_triangles.argtypes = [ctypes.c_void_p]
         L.oracle_vf_response.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
+        L.oracle_set_integrator.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.oracle_energy.argtypes = [ctypes.c_void_p]
         L.oracle_energy.restype = ctypes.c_double
         _lib = L
@@ -93,9 +94,12 @@ def svd(F):
 
 
 class Sim:
-    """CPU oracle BACKWARD_EULER_VELOCITY on one scene (collisions off)."""
+    """CPU oracle timestepper on one scene: BACKWARD_EULER_VELOCITY
+    (integrator "velocity", optional vertex-face collisions) or
+    BACKWARD_EULER_POSITION (integrator "position", Rayleigh damped with
+    alpha, beta = rayleigh)."""
 
-    def __init__(self, scene, tol=1e-8, maxit=1000, precond=0):
+    def __init__(self, scene, tol=1e-8, maxit=1000, precond=0, integrator="velocity", rayleigh=(0.01, 0.01)):
         L = lib()
         self.scene = scene
         self._rest = np.ascontiguousarray(scene.rest, dtype=np.float64)
@@ -111,6 +115,8 @@ class Sim:
         pins = np.ascontiguousarray(scene.pinned, dtype=np.int32)
         assert L.oracle_attach_pins(self.h, len(pins), _i(pins)) == 0
         L.oracle_set_solver(self.h, tol, maxit, precond)
+        if integrator != "velocity":
+            assert L.oracle_set_integrator(self.h, 1, rayleigh[0], rayleigh[1]) == 0
 
     def set_collisions(self, vf=True, eps=0.01, mu=1.0, beta=0.001):
         """Vertex-face self collisions (TIMESTEPPER.cpp:83-86 defaults: mu 1, beta 0.001)."""

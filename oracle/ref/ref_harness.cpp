@@ -9,11 +9,12 @@
 //       12x12 Hessians, plus the assembled R and CSC K
 //       (TET_MESH.cpp:643-770, TET_MESH_FASTER.cpp:89-133).
 //   run <in> <out> <material> <mu> <lambda> <steps> <stride>
-//       BACKWARD_EULER_VELOCITY::solve for `steps` steps
-//       (Timestepper/BACKWARD_EULER_VELOCITY.cpp:96-235), recording the
-//       displacement and velocity every `stride` steps.
-//       Options come from <in>/params.npy:
-//         [density, gx, gy, gz, dt, tol, maxit, vf_on, ee_on, coll_eps, coll_mu, coll_beta]
+//       BACKWARD_EULER_VELOCITY::solve (Timestepper/BACKWARD_EULER_VELOCITY.cpp:96-235)
+//       or BACKWARD_EULER_POSITION::solve (Timestepper/BACKWARD_EULER_POSITION.cpp:129-330)
+//       for `steps` steps, recording the displacement and velocity every
+//       `stride` steps.  Options come from <in>/params.npy:
+//         [density, gx, gy, gz, dt, tol, maxit, vf_on, ee_on, coll_eps, coll_mu, coll_beta
+//          (, integrator: 0 velocity / 1 position, rayleigh_alpha, rayleigh_beta)]
 //   collide <in> <out> <coll_eps>
 //       vertex-face detection at the displacement in <in>/x.npy
 //       (TET_MESH_FASTER.cpp:248-334, TET_MESH.cpp:1785-1826).
@@ -23,6 +24,7 @@
 #include <iostream>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "SETTINGS.h"
@@ -34,6 +36,7 @@
 #include "Hyperelastic/Volume/SNH.h"
 #include "Hyperelastic/Volume/SNH_WITH_BARRIER.h"
 #include "Hyperelastic/Volume/STVK.h"
+#include "Timestepper/BACKWARD_EULER_POSITION.h"
 #include "Timestepper/BACKWARD_EULER_VELOCITY.h"
 #include "util/MATRIX_UTIL.h"
 #include "npy.h"
@@ -67,6 +70,29 @@ class HarnessBEV : public TIMESTEPPER::BACKWARD_EULER_VELOCITY {
   int lastIterations() const { return (int)_cgSolver.iterations(); }
   double lastError() const { return (double)_cgSolver.error(); }
   // pin a vertex at its current world position through an identity-transform shape
+  void pin(const KINEMATIC_SHAPE* shape, int vertexID, const VECTOR3& world) {
+    KINEMATIC_CONSTRAINT c;
+    c.shape = shape;
+    c.vertexID = vertexID;
+    c.localPosition = shape->worldVertexToLocal(world);
+    _kinematicConstraints.push_back(c);
+  }
+};
+
+// the same for the position-based stepper, with its Rayleigh coefficients
+class HarnessBEP : public TIMESTEPPER::BACKWARD_EULER_POSITION {
+ public:
+  HarnessBEP(TET_MESH& m, VOLUME::HYPERELASTIC& h) : BACKWARD_EULER_POSITION(m, h) {}
+  void setRayleigh(double alpha, double beta) {
+    _rayleighAlpha = alpha;
+    _rayleighBeta = beta;
+  }
+  void setSolver(double tol, int maxit) {
+    _cgSolver.setTolerance(tol);
+    _cgSolver.setMaxIterations(maxit);
+  }
+  int lastIterations() const { return (int)_cgSolver.iterations(); }
+  double lastError() const { return (double)_cgSolver.error(); }
   void pin(const KINEMATIC_SHAPE* shape, int vertexID, const VECTOR3& world) {
     KINEMATIC_CONSTRAINT c;
     c.shape = shape;
@@ -171,7 +197,8 @@ int modeElements(const std::string& in, const std::string& out, const std::strin
   return 0;
 }
 
-int modeRun(const std::string& in, const std::string& out, const std::string& mat, double mu, double lambda,
+template <class Stepper>
+int runWith(const std::string& in, const std::string& out, const std::string& mat, double mu, double lambda,
             int steps, int stride) {
   std::vector<VECTOR3> rest;
   std::vector<VECTOR4I> tets;
@@ -179,6 +206,7 @@ int modeRun(const std::string& in, const std::string& out, const std::string& ma
   const long nv = rest.size();
   npy::Array prm = npy::load(in + "/params.npy");
   const double* p = prm.f8();
+  const long nprm = prm.size();
   const double density = p[0];
   const VECTOR3 gravity(p[1], p[2], p[3]);
   const double dt = p[4], tol = p[5];
@@ -193,7 +221,10 @@ int modeRun(const std::string& in, const std::string& out, const std::string& ma
   const VECTOR v0 = loadVector(in + "/v0.npy", 3 * nv);
   npy::Array pins = npy::load(in + "/pinned.npy");
 
-  HarnessBEV solver(mesh, *material);
+  Stepper solver(mesh, *material);
+  if constexpr (std::is_same_v<Stepper, HarnessBEP>) {
+    if (nprm >= 15) solver.setRayleigh(p[13], p[14]);
+  }
   solver.setDt(dt);
   solver.setSolver(tol, maxit);
   solver.vertexFaceSelfCollisionsOn() = vf;
@@ -242,6 +273,14 @@ int modeRun(const std::string& in, const std::string& out, const std::string& ma
   double energy = mesh.computeHyperelasticEnergy(*material);
   npy::save(out + "/energy.npy", &energy, "<f8", {1});
   return 0;
+}
+
+int modeRun(const std::string& in, const std::string& out, const std::string& mat, double mu, double lambda,
+            int steps, int stride) {
+  npy::Array prm = npy::load(in + "/params.npy");
+  const bool position = prm.size() >= 13 && prm.f8()[12] == 1.0;
+  if (position) return runWith<HarnessBEP>(in, out, mat, mu, lambda, steps, stride);
+  return runWith<HarnessBEV>(in, out, mat, mu, lambda, steps, stride);
 }
 
 int modeCollide(const std::string& in, const std::string& out, double eps) {

@@ -6,7 +6,7 @@ so this only runs where they are).  Inputs come from hobakv1_gb300.scenes, so
 they are regenerated bit-identically anywhere.  Usage:
 
     make -C oracle/ref REF=<reference checkout> -j8
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [elements] [trajectories] [position] [collisions]
 """
 from __future__ import annotations
 
@@ -65,6 +65,20 @@ def make_trajectories():
         print("trajectory", s.name, r["iters"].sum())
 
 
+def make_position_trajectories():
+    """BACKWARD_EULER_POSITION (Rayleigh damped, alpha = beta = 0.01, the
+    reference's defaults) on the same pinned, compressed and twisted cubes."""
+    cases = [(scenes.config2_scene(6, "snh"), 100, 25),
+             (scenes.config2_scene(6, "arap"), 100, 25),
+             (scenes.config1_scene(8), 60, 20)]
+    for s, steps, stride in cases:
+        r = refrun.run(s, steps, stride=stride, integrator="position", rayleigh=(0.01, 0.01))
+        np.savez_compressed(os.path.join(OUT, f"traj_{s.name}_position.npz"), x=r["x"], v=r["v"],
+                            iters=r["iters"], cg_error=r["cg_error"], energy=r["energy"],
+                            steps=steps, stride=stride, rayleigh=np.array([0.01, 0.01]))
+        print("position trajectory", s.name, r["iters"].sum())
+
+
 def make_collisions():
     """Two cubes in contact: vertex-face pairs (reference AABB broad phase +
     narrow phase) at the start and along a 40-step trajectory with collisions."""
@@ -83,6 +97,12 @@ def make_collisions():
 if __name__ == "__main__":
     if not refrun.available():
         sys.exit("reference build missing: make -C oracle/ref REF=<reference checkout>")
-    make_elements()
-    make_trajectories()
-    make_collisions()
+    which = set(sys.argv[1:]) or {"elements", "trajectories", "position", "collisions"}
+    if "elements" in which:
+        make_elements()
+    if "trajectories" in which:
+        make_trajectories()
+    if "position" in which:
+        make_position_trajectories()
+    if "collisions" in which:
+        make_collisions()

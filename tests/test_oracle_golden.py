@@ -86,6 +86,30 @@ def test_oracle_trajectory_matches_reference(name, scene_fn):
         assert err < 1e-8, (k, err)
 
 
+@pytest.mark.parametrize("name,scene_fn", [
+    ("kuhn6_snh_twist", lambda: scenes.config2_scene(6, "snh")),
+    ("kuhn6_arap_twist", lambda: scenes.config2_scene(6, "arap")),
+    ("kuhn8_snh", lambda: scenes.config1_scene(8)),
+])
+def test_oracle_position_integrator_matches_reference(name, scene_fn):
+    """BACKWARD_EULER_POSITION (Rayleigh damped, alpha = beta = 0.01): the
+    restatement against the reference's own trajectory, positions and
+    velocities, and the iteration count of every step."""
+    g = np.load(os.path.join(GOLDEN, f"traj_{name}_position.npz"))
+    s = scene_fn()
+    a, b = (float(c) for c in g["rayleigh"])
+    sim = oracle.Sim(s, integrator="position", rayleigh=(a, b))
+    stride = int(g["stride"])
+    iters = []
+    for k in range(1, g["x"].shape[0]):
+        it, _ = sim.step(stride)
+        iters.extend(it.tolist())
+        x, v = sim.state()
+        assert np.linalg.norm(x - g["x"][k]) / np.linalg.norm(g["x"][k]) < 1e-10, k
+        assert np.linalg.norm(v - g["v"][k]) / np.linalg.norm(g["v"][k]) < 1e-9, k
+    assert np.abs(np.array(iters) - g["iters"]).max() <= 1
+
+
 def test_oracle_vertex_face_collisions_match_reference():
     """Surface triangles bit-exact; vertex-face pair sets bit-exact at every
     recorded state; the 40-step trajectory with collisions within 1e-8."""
