@@ -28,7 +28,8 @@ class HobakSceneDesc(ctypes.Structure):
 class HobakSolverOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iters", ctypes.c_int), ("precision", ctypes.c_int),
                 ("preconditioner", ctypes.c_int), ("max_refinements", ctypes.c_int),
-                ("use_graph", ctypes.c_int)]
+                ("use_graph", ctypes.c_int), ("integrator", ctypes.c_int),
+                ("rayleigh_alpha", ctypes.c_double), ("rayleigh_beta", ctypes.c_double)]
 
 
 class HobakTuning(ctypes.Structure):

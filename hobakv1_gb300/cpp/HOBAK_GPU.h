@@ -201,7 +201,7 @@ class BACKWARD_EULER_VELOCITY {
   const std::string& lastError() const { return _error; }
   int currentTimestep() const { return _currentTimestep; }
 
- private:
+ protected:
   bool build() {
     const auto& rest = _tetMesh.restVertices();
     const auto& tets = _tetMesh.tets();
@@ -248,6 +248,28 @@ class BACKWARD_EULER_VELOCITY {
   hobak_step_stats _stats{};
   hobak_batch _handle = nullptr;
   std::string _error;
+};
+
+// GPU drop-in for BACKWARD_EULER_POSITION (Rayleigh damped,
+// BACKWARD_EULER_POSITION.cpp:138-330): the same host-state semantics; the
+// unknown of the solve is the position update, and C = alpha M + beta K at
+// rest.  Vertex-face contact is not available with this integrator.
+class BACKWARD_EULER_POSITION : public BACKWARD_EULER_VELOCITY {
+ public:
+  BACKWARD_EULER_POSITION(TET_MESH& tetMesh, VOLUME::HYPERELASTIC& hyperelastic)
+      : BACKWARD_EULER_VELOCITY(tetMesh, hyperelastic) {
+    _opts.integrator = HOBAK_INTEGRATOR_POSITION;
+    _opts.rayleigh_alpha = 0.01;  // BACKWARD_EULER_POSITION.cpp:53-54
+    _opts.rayleigh_beta = 0.01;
+    _name = "BACKWARD_EULER_POSITION";
+  }
+  REAL rayleighAlpha() const { return _opts.rayleigh_alpha; }
+  REAL rayleighBeta() const { return _opts.rayleigh_beta; }
+  // frozen at the first solve(), like the other settings
+  void setRayleigh(const REAL alpha, const REAL beta) {
+    _opts.rayleigh_alpha = alpha;
+    _opts.rayleigh_beta = beta;
+  }
 };
 
 }  // namespace TIMESTEPPER

@@ -78,6 +78,7 @@ struct hobak_batch_t {
   void* arena = nullptr;
   size_t arenaBytes = 0;
   void* precArena = nullptr;  // buffers of the current precision (alloc_precision)
+  double* K0 = nullptr;       // rest-state clamped Hessian (position integrator; rest_hessian)
   size_t precBytes = 0;
   bool precMixed = false;
   cudaStream_t stream = nullptr;
@@ -185,6 +186,48 @@ int validate_scene(const hobak_scene_desc& s, int idx) {
 template <typename T>
 T* carve(void* base, size_t off) {
   return reinterpret_cast<T*>(static_cast<char*>(base) + off);
+}
+
+void drop_graphs(hobak_batch_t* B);
+
+// Clamped Hessian of every scene at zero displacement (the position
+// integrator's Rayleigh damping C = alpha M + beta K0 builds it at rest every
+// step, TIMESTEPPER.cpp:213-236; it never changes, so once per batch), FP64,
+// CSR block order: element Hessians at x = 0 into scratch, gathered like the
+// inspection call's K.  Every scene counts, parked or not.
+int rest_hessian(hobak_batch_t* B) {
+  if (B->K0) return HOBAK_OK;
+  const size_t kBytes = sizeof(double) * 9 * (size_t)std::max(B->nblocks, 1);
+  CUDA_TRY(cudaMalloc(&B->K0, kBytes));
+  const size_t ehBytes = sizeof(double) * kElemHess * (size_t)B->nt, xBytes = sizeof(double) * 3 * (size_t)B->nv;
+  void* scratch = nullptr;
+  CUDA_TRY(cudaMalloc(&scratch, ehBytes + 2 * xBytes));
+  cudaStream_t s = B->stream;
+  DeviceBatch d = B->d;
+  d.elemH = static_cast<double*>(scratch);
+  double* zero = reinterpret_cast<double*>(static_cast<char*>(scratch) + ehBytes);
+  double* R = zero + 3 * (size_t)B->nv;
+  d.x = zero;
+  std::vector<SceneParams> sp = B->sceneParams;
+  for (auto& p : sp) p.active = 1;
+  cudaError_t e = cudaMemsetAsync(zero, 0, xBytes, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(const_cast<SceneParams*>(d.scenes), sp.data(), sizeof(SceneParams) * sp.size(),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    launch_element(d, s, 1);
+    launch_assemble_raw(d, B->K0, R, s);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(const_cast<SceneParams*>(d.scenes), B->sceneParams.data(),
+                        sizeof(SceneParams) * sp.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(scratch);
+  if (e != cudaSuccess) return fail(HOBAK_ERR_CUDA, std::string("rest Hessian: ") + cudaGetErrorString(e));
+  B->d.K0 = B->K0;
+  drop_graphs(B);
+  return HOBAK_OK;
 }
 
 // Buffers of the batch's precision, in their own allocation (replaced when
@@ -417,6 +460,9 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     p.lambda = mp.lambda;
     p.alpha = mp.alpha;
     p.dt = H.dt;
+    p.integrator = B->opts.integrator;
+    p.rayAlpha = B->opts.rayleigh_alpha;
+    p.rayBeta = B->opts.rayleigh_beta;
     p.active = 1;
     sparams.push_back(p);
   }
@@ -571,6 +617,11 @@ int check_opts(const hobak_solver_opts* o) {
   if (o->preconditioner != HOBAK_PRECOND_JACOBI && o->preconditioner != HOBAK_PRECOND_BLOCK_JACOBI)
     return fail(HOBAK_ERR_INVALID, "unknown preconditioner");
   if (o->max_refinements < 0 || o->max_refinements > 3) return fail(HOBAK_ERR_INVALID, "max_refinements in 0..3");
+  if (o->integrator != HOBAK_INTEGRATOR_VELOCITY && o->integrator != HOBAK_INTEGRATOR_POSITION)
+    return fail(HOBAK_ERR_INVALID, "unknown integrator");
+  if (!(o->rayleigh_alpha >= 0.0) || !(o->rayleigh_beta >= 0.0) || !std::isfinite(o->rayleigh_alpha) ||
+      !std::isfinite(o->rayleigh_beta))
+    return fail(HOBAK_ERR_INVALID, "Rayleigh coefficients must be finite and >= 0");
   return HOBAK_OK;
 }
 
@@ -1138,6 +1189,9 @@ void hobak_default_solver_opts(hobak_solver_opts* o) {
   o->preconditioner = HOBAK_PRECOND_BLOCK_JACOBI;
   o->max_refinements = 3;
   o->use_graph = 1;
+  o->integrator = HOBAK_INTEGRATOR_VELOCITY;
+  o->rayleigh_alpha = 0.01;
+  o->rayleigh_beta = 0.01;
 }
 
 int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_solver_opts* opts,
@@ -1168,6 +1222,10 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
     hobak_batch_destroy(B.release());
     return rc;
   }
+  if (B->opts.integrator == HOBAK_INTEGRATOR_POSITION && (rc = rest_hessian(B.get()))) {
+    hobak_batch_destroy(B.release());
+    return rc;
+  }
   if ((rc = upload_solver_opts(B.get()))) {
     hobak_batch_destroy(B.release());
     return rc;
@@ -1193,6 +1251,7 @@ int hobak_batch_destroy(hobak_batch b) {
   if (b->solvePinned) cudaFreeHost(b->solvePinned);
   if (b->arena) cudaFree(b->arena);
   if (b->precArena) cudaFree(b->precArena);
+  if (b->K0) cudaFree(b->K0);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return HOBAK_OK;
@@ -1319,13 +1378,24 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   if (!b || !opts) return fail(HOBAK_ERR_INVALID, "bad arguments");
   int rc = check_opts(opts);
   if (rc) return rc;
+  if (opts->integrator != HOBAK_INTEGRATOR_VELOCITY)
+    for (const CollisionScene& cs : b->collScenes)
+      if (cs.vfOn) return fail(HOBAK_ERR_INVALID, "vertex-face contact needs the velocity integrator");
   b->opts = *opts;
   b->clusterDirty = true;
   drop_graphs(b);
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
   if ((opts->precision == HOBAK_PRECISION_MIXED) != b->precMixed) {
-    CUDA_TRY(cudaStreamSynchronize(b->stream));
     if ((rc = alloc_precision(b))) return rc;
   }
+  for (SceneParams& p : b->sceneParams) {
+    p.integrator = opts->integrator;
+    p.rayAlpha = opts->rayleigh_alpha;
+    p.rayBeta = opts->rayleigh_beta;
+  }
+  CUDA_TRY(cudaMemcpy(const_cast<SceneParams*>(b->d.scenes), b->sceneParams.data(),
+                      sizeof(SceneParams) * b->sceneParams.size(), cudaMemcpyHostToDevice));
+  if (opts->integrator == HOBAK_INTEGRATOR_POSITION && (rc = rest_hessian(b))) return rc;
   return upload_solver_opts(b);
 }
 
@@ -1333,6 +1403,8 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
                                double damping_beta) {
   if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
   if (vf_on && !(eps > 0.0)) return fail(HOBAK_ERR_INVALID, "collision distance must be > 0");
+  if (vf_on && b->opts.integrator != HOBAK_INTEGRATOR_VELOCITY)
+    return fail(HOBAK_ERR_INVALID, "vertex-face contact needs the velocity integrator");
   if (!b->collArena) {
     int rc = build_collisions(b);
     if (rc) return rc;
@@ -1441,7 +1513,7 @@ int hobak_batch_set_active(hobak_batch b, int scene, int active) {
 
 int hobak_batch_device_bytes(hobak_batch b, long long* bytes) {
   if (!b || !bytes) return fail(HOBAK_ERR_INVALID, "bad arguments");
-  *bytes = (long long)(b->arenaBytes + b->precBytes);
+  *bytes = (long long)(b->arenaBytes + b->precBytes + (b->K0 ? sizeof(double) * 9 * (size_t)b->nblocks : 0));
   return HOBAK_OK;
 }
 

@@ -25,6 +25,11 @@ constexpr int kMinTileV = 64;     // smallest tile size; tile tables are sized f
 //       // vertices per PCG tile (one CTA)
 constexpr int kElemHess = 90;     // 10 upper blocks x 9
 constexpr int kPartials = 4;      // per-tile partial sums slots
+// Timesteppers: BACKWARD_EULER_VELOCITY::solve (unknown: the velocity update)
+// and BACKWARD_EULER_POSITION::solveRayleighDamped (unknown: the position
+// update), sharing every kernel but the coefficients of rhs, LHS and update.
+constexpr int kIntegratorVelocity = 0;
+constexpr int kIntegratorPosition = 1;
 
 // Index of block (a, b), a <= b, in the 10-block upper triangle of a 4x4
 // block matrix: (0,0)(0,1)(0,2)(0,3)(1,1)(1,2)(1,3)(2,2)(2,3)(3,3).
@@ -39,8 +44,10 @@ struct SceneParams {
   int kind;            // material
   int active;          // 0: the scene is parked (serving) and every kernel skips it
   int pcgCluster;      // > 0: the inner PCG runs in a cluster of this many CTAs (cluster_pcg.cu)
+  int integrator;      // kIntegratorVelocity or kIntegratorPosition
   double mu, lambda, alpha;  // reparameterised material constants
   double dt;
+  double rayAlpha, rayBeta;  // Rayleigh damping C = rayAlpha M + rayBeta K0 (position integrator)
 };
 
 // Per-scene solver scalars, written by the last CTA of each reduction.

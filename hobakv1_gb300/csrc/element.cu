@@ -209,7 +209,11 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   if (!sp.active) return;
   const int4 tv = b.tets[t];
   const MatParams m{sp.kind, sp.mu, sp.lambda, sp.alpha};
-  const double dt = rawForces ? 0.0 : sp.dt;
+  // rhs term: dt (f + dt He v) for BACKWARD_EULER_VELOCITY; the force itself
+  // for BACKWARD_EULER_POSITION (its rhs has no K v term: the Rayleigh part
+  // uses the rest-state Hessian, k_rhs) and for raw forces (inspection)
+  const bool velocityTerm = !rawForces && sp.integrator == kIntegratorVelocity;
+  const double dt = velocityTerm ? sp.dt : 0.0;
   double Dinv[9];
 #pragma unroll
   for (int k = 0; k < 9; k++) Dinv[k] = b.DmInv[9 * (size_t)t + k];
@@ -220,13 +224,19 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   deformation_gradient(X, Dinv, F);
   svd3_rv_fast(F, U, S, V);
   material_pk1(m, F, U, V, P);
-  // dt f directly (the force scaled by dt * vol instead of vol); raw forces
-  // for inspection have dt = 0 and keep the plain vol
-  element_force(P, Dinv, rawForces ? vol : dt * vol, f);
+  // dt f directly (the force scaled by dt * vol instead of vol)
+  element_force(P, Dinv, velocityTerm ? dt * vol : vol, f);
 
   HT Hr[45];
   reduced_hessian<HT>(m, U, S, V, Dinv, Hr);
 
+  double* g = b.elemG + 12 * (size_t)t;
+  if (!velocityTerm) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) g[k] = f[k];
+    expand_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
+    return;
+  }
   // He v = -vol D^T Hr (D v): D v = relative velocities of vertices 1..3
   // (in the mixed path He v is formed in FP32 like He itself)
   const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
@@ -242,7 +252,6 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   }
   // g = dt f + dt^2 He v: the He v rows carry the factor -vol dt^2 in HT
   // (one conversion and one add per entry on the FP64 pipe)
-  double* g = b.elemG + 12 * (size_t)t;
   const HT ch = HT(-vol * dt * dt);
   HT h0[3] = {HT(0), HT(0), HT(0)};
 #pragma unroll

@@ -89,6 +89,9 @@ struct DeviceBatch {
   const int* slotSlice;
   const int* colS;
   int nslotRows;
+  // clamped Hessian at zero displacement, CSR block order, 3x3 column major
+  // (the position integrator's Rayleigh damping; null when unused)
+  const double* K0;
 
   // tiles
   const int* tileScene;

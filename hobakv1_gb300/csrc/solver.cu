@@ -262,10 +262,19 @@ __global__ void k_assemble_entry(DeviceBatch b, const HT* __restrict__ elemH, T*
   const int rr = e / 3, c = e % 3;
   const HT sum = gather_block_entry(b, elemH, blk, rr, c);
   const int w = b.cols[blk];
-  const double dt = b.scenes[b.vertexScene[u]].dt;
+  const SceneParams& sp = b.scenes[b.vertexScene[u]];
+  const double dt = sp.dt;
   const bool fu = b.freeMask[u] != 0, fw = b.freeMask[w] != 0;
-  HT val = (fu && fw) ? HT(-(dt * dt)) * sum : HT(0);
-  if (u == w && rr == c) val += fu ? HT(b.mass[u]) : HT(1);
+  HT val;
+  if (sp.integrator == kIntegratorPosition) {
+    // A = M (1/dt^2 - alpha/dt) - (beta/dt) K0 - K (BACKWARD_EULER_POSITION.cpp:207)
+    const double invDt = 1.0 / dt;
+    val = (fu && fw) ? HT(-(sp.rayBeta * invDt)) * HT(b.K0[9 * (size_t)blk + rr + 3 * c]) - sum : HT(0);
+    if (u == w && rr == c) val += fu ? HT(b.mass[u] * (invDt * invDt - sp.rayAlpha * invDt)) : HT(1);
+  } else {
+    val = (fu && fw) ? HT(-(dt * dt)) * sum : HT(0);
+    if (u == w && rr == c) val += fu ? HT(b.mass[u]) : HT(1);
+  }
   lhs[(size_t)r * kSlotVals + kSlice * e + lane] = T(val);
 }
 
@@ -318,14 +327,28 @@ __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __res
       const int w = b.cols[blk];
       const double dt = sp.dt;
       const bool fu = b.freeMask[u] != 0, fw = b.freeMask[w] != 0;
-      const HT m = fu ? HT(b.mass[u]) : HT(1);
-      const HT ndt2 = HT(-(dt * dt));
       T* out = lhs + (size_t)r * kSlotVals + lane;
+      if (sp.integrator == kIntegratorPosition) {
+        // A = M (1/dt^2 - alpha/dt) - (beta/dt) K0 - K (BACKWARD_EULER_POSITION.cpp:207)
+        const double invDt = 1.0 / dt;
+        const HT m = fu ? HT(b.mass[u] * (invDt * invDt - sp.rayAlpha * invDt)) : HT(1);
+        const HT cK0 = HT(-(sp.rayBeta * invDt));
+        const double* K0 = b.K0 + 9 * (size_t)blk;
 #pragma unroll
-      for (int e = 0; e < 9; e++) {
-        HT val = (fu && fw) ? ndt2 * sum[e] : HT(0);
-        if (u == w && e % 4 == 0) val += m;
-        out[kSlice * e] = T(val);
+        for (int e = 0; e < 9; e++) {
+          HT val = (fu && fw) ? cK0 * HT(K0[(e / 3) + 3 * (e % 3)]) - sum[e] : HT(0);
+          if (u == w && e % 4 == 0) val += m;
+          out[kSlice * e] = T(val);
+        }
+      } else {
+        const HT m = fu ? HT(b.mass[u]) : HT(1);
+        const HT ndt2 = HT(-(dt * dt));
+#pragma unroll
+        for (int e = 0; e < 9; e++) {
+          HT val = (fu && fw) ? ndt2 * sum[e] : HT(0);
+          if (u == w && e % 4 == 0) val += m;
+          out[kSlice * e] = T(val);
+        }
       }
     }
   }
@@ -442,9 +465,33 @@ __global__ void __launch_bounds__(TV) k_rhs(DeviceBatch b) {
         for (int i = 0; i < 3; i++) acc[i] += g[i];
       }
     }
+    double bi[3];
+    if (b.scenes[s].integrator == kIntegratorPosition) {
+      // b = (M/dt - C) v + R + f_ext with C = alpha M + beta K0
+      // (BACKWARD_EULER_POSITION.cpp:196; K0 at zero displacement,
+      // TIMESTEPPER.cpp:213-236)
+      const SceneParams& sp = b.scenes[s];
+      const double invDt = 1.0 / dt, m = b.mass[u];
+      double k0v[3] = {0.0, 0.0, 0.0};
+      for (int k = b.rowptr[u]; k < b.rowptr[u + 1]; k++) {
+        const double* blk = b.K0 + 9 * (size_t)k;
+        const int w = b.cols[k];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int c = 0; c < 3; c++) k0v[i] += blk[i + 3 * c] * b.v[3 * w + c];
+      }
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        bi[i] = (invDt - sp.rayAlpha) * m * b.v[3 * u + i] - sp.rayBeta * k0v[i] + acc[i] + b.fext[3 * u + i];
+    } else {
+      // b = dt (R + dt K v + f_ext); acc holds dt (R + dt K v)
+#pragma unroll
+      for (int i = 0; i < 3; i++) bi[i] = acc[i] + dt * b.fext[3 * u + i];
+    }
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const double ri = fu ? acc[i] + dt * b.fext[3 * u + i] : 0.0;
+      const double ri = fu ? bi[i] : 0.0;
       b.rhs[3 * u + i] = ri;
       b.r64[3 * u + i] = ri;
       b.y[3 * u + i] = 0.0;
@@ -1014,12 +1061,25 @@ __global__ void k_continue(const int* active, unsigned long long* bodyRuns, cuda
   }
 }
 
-// v += y; x += dt v; v = S v (BACKWARD_EULER_VELOCITY.cpp:191-201).
+// Velocity integrator: v += y; x += dt v; v = S v
+// (BACKWARD_EULER_VELOCITY.cpp:191-201).  Position integrator: x += y;
+// v = (x - x_old) / dt; v = S v (BACKWARD_EULER_POSITION.cpp:241-301).
 __global__ void k_finish_step(DeviceBatch b) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= b.nv || !b.scenes[b.vertexScene[u]].active) return;
-  const double dt = b.scenes[b.vertexScene[u]].dt;
+  const SceneParams& sp = b.scenes[b.vertexScene[u]];
+  const double dt = sp.dt;
   const bool fu = b.freeMask[u] != 0;
+  if (sp.integrator == kIntegratorPosition) {
+    const double invDt = 1.0 / dt;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const double xo = b.x[3 * u + i], xn = xo + b.y[3 * u + i];
+      b.x[3 * u + i] = xn;
+      b.v[3 * u + i] = fu ? invDt * (xn - xo) : 0.0;
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     const double vn = b.v[3 * u + i] + b.y[3 * u + i];

@@ -29,6 +29,8 @@ PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 PRECOND_JACOBI = 0
 PRECOND_BLOCK_JACOBI = 1
+INTEGRATOR_VELOCITY = 0   # BACKWARD_EULER_VELOCITY::solve
+INTEGRATOR_POSITION = 1   # BACKWARD_EULER_POSITION::solveRayleighDamped
 
 
 def _colmajor(F: np.ndarray) -> np.ndarray:
@@ -180,10 +182,16 @@ class TET_MESH:
 
 
 def solver_opts(tol=1e-8, max_iters=1000, precision=PRECISION_FP64, preconditioner=PRECOND_BLOCK_JACOBI,
-                max_refinements=3, use_graph=True) -> HobakSolverOpts:
+                max_refinements=3, use_graph=True, integrator=INTEGRATOR_VELOCITY,
+                rayleigh=(0.01, 0.01)) -> HobakSolverOpts:
+    """Solver options; integrator INTEGRATOR_VELOCITY (BACKWARD_EULER_VELOCITY)
+    or INTEGRATOR_POSITION (BACKWARD_EULER_POSITION, Rayleigh damped with
+    alpha, beta = rayleigh)."""
     o = HobakSolverOpts()
     o.tol, o.max_iters, o.precision = tol, max_iters, precision
     o.preconditioner, o.max_refinements, o.use_graph = preconditioner, max_refinements, int(use_graph)
+    o.integrator = integrator
+    o.rayleigh_alpha, o.rayleigh_beta = rayleigh
     return o
 
 
@@ -558,3 +566,32 @@ class BACKWARD_EULER_VELOCITY:
 
     def lastSolveStats(self):
         return self._lastStats
+
+
+class BACKWARD_EULER_POSITION(BACKWARD_EULER_VELOCITY):
+    """GPU drop-in for TIMESTEPPER::BACKWARD_EULER_POSITION with Rayleigh
+    damping (BACKWARD_EULER_POSITION.cpp:138-330): the same host-state
+    semantics; the solve's unknown is the position update and
+    C = alpha M + beta K(rest).  Vertex-face contact is not available with
+    this integrator."""
+
+    def __init__(self, tetMesh: TET_MESH, hyperelastic: HYPERELASTIC, opts: Optional[HobakSolverOpts] = None):
+        super().__init__(tetMesh, hyperelastic, None if opts is None else HobakSolverOpts.from_buffer_copy(opts))
+        self._opts.integrator = INTEGRATOR_POSITION
+        if opts is None:
+            self._opts.rayleigh_alpha, self._opts.rayleigh_beta = 0.01, 0.01  # BACKWARD_EULER_POSITION.cpp:53-54
+
+    def rayleighAlpha(self) -> float:
+        return self._opts.rayleigh_alpha
+
+    def rayleighBeta(self) -> float:
+        return self._opts.rayleigh_beta
+
+    def setRayleigh(self, alpha: float, beta: float):
+        self._require_unbuilt("setRayleigh")
+        self._opts.rayleigh_alpha, self._opts.rayleigh_beta = float(alpha), float(beta)
+
+    def setVertexFaceSelfCollisionsOn(self, on: bool):
+        if on:
+            raise ValueError("vertex-face contact needs BACKWARD_EULER_VELOCITY")
+        super().setVertexFaceSelfCollisionsOn(False)

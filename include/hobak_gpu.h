@@ -50,6 +50,9 @@ extern "C" {
 #define HOBAK_PRECISION_MIXED 1  /* FP32 Hessian/SpMV/inner PCG, FP64 SVD, residual and refinement */
 
 /* ---- preconditioners ---- */
+#define HOBAK_INTEGRATOR_VELOCITY 0   /* BACKWARD_EULER_VELOCITY::solve (BACKWARD_EULER_VELOCITY.cpp:96-235) */
+#define HOBAK_INTEGRATOR_POSITION 1   /* BACKWARD_EULER_POSITION::solveRayleighDamped (BACKWARD_EULER_POSITION.cpp:138-330) */
+
 #define HOBAK_PRECOND_JACOBI 0        /* scalar 1/diag, Eigen DiagonalPreconditioner */
 #define HOBAK_PRECOND_BLOCK_JACOBI 1  /* inverse of each 3x3 diagonal block */
 
@@ -87,6 +90,9 @@ typedef struct hobak_solver_opts {
   int preconditioner;      /* HOBAK_PRECOND_* */
   int max_refinements;     /* MIXED only: FP64 iterative-refinement sweeps (<= 3) */
   int use_graph;           /* capture each step as a CUDA graph (1) or launch eagerly (0) */
+  int integrator;          /* HOBAK_INTEGRATOR_* (default VELOCITY) */
+  double rayleigh_alpha;   /* POSITION: C = alpha M + beta K(rest) (defaults 0.01, 0.01: */
+  double rayleigh_beta;    /*   BACKWARD_EULER_POSITION.cpp:53-54); vertex-face contact needs VELOCITY */
 } hobak_solver_opts;
 
 /* Per-scene statistics of the last step. */
