@@ -20,6 +20,8 @@ Workloads (synthetic, seeded; see hobakv1_gb300/scenes.py):
                           one batched mixed-precision step = every scene advanced once
   mix256_fp64             the same mix batched in FP64
   mix64_mixed             the first 64 scenes of the mix, mixed (a profiling-sized case)
+  kuhn40_snh_twist_position[_mixed], mix256_position_mixed
+                          the same inputs stepped by BACKWARD_EULER_POSITION (Rayleigh damped)
   serve_poisson           continuous batching: 32 jobs (N ~ U{8..32}, 10-200 steps, half two cubes in
                           vertex-face contact) arriving as a Poisson stream at 50, 400 and 2000 jobs/s,
                           mixed precision and plain FP64; job-steps/s, p50/p99 step and job latency
@@ -50,6 +52,11 @@ WORKLOADS = {
     "mix256_mixed": dict(kind="mix", count=256, material="snh/arap", precision=1),
     "mix256_fp64": dict(kind="mix", count=256, material="snh/arap", precision=0),
     "mix64_mixed": dict(kind="mix", count=64, material="snh/arap", precision=1),
+    # BACKWARD_EULER_POSITION (Rayleigh damped, alpha = beta = 0.01) on the same inputs
+    "kuhn40_snh_twist_position": dict(kind="config2", N=40, material="snh", precision=0, integrator="position"),
+    "kuhn40_snh_twist_position_mixed": dict(kind="config2", N=40, material="snh", precision=1,
+                                            integrator="position"),
+    "mix256_position_mixed": dict(kind="mix", count=256, material="snh/arap", precision=1, integrator="position"),
     "serve_poisson": dict(kind="serve", count=32, lambdas=[50, 400, 2000], material="snh/arap",
                           precision=1),
 }
@@ -145,7 +152,7 @@ def ncu_traffic(workload):
         return json.load(f).get(workload, {})
 
 
-def cpu_baseline(scene_list, steps, warmup, max_scenes=16):
+def cpu_baseline(scene_list, steps, warmup, max_scenes=16, integrator="velocity"):
     """The oracle (CPU restatement of the reference algorithm, OpenMP on all
     host cores) on the same workload; bounded sample.  Large mixes time a
     seeded subset (every k-th scene) and scale by scene count.
@@ -155,7 +162,7 @@ def cpu_baseline(scene_list, steps, warmup, max_scenes=16):
     stride = max(1, -(-len(scene_list) // max_scenes))
     subset = scene_list[::stride]
     scale = len(scene_list) / len(subset)
-    sims = [oracle.Sim(s, precond=0) for s in subset]
+    sims = [oracle.Sim(s, precond=0, integrator=integrator) for s in subset]
     if warmup:
         for sim in sims:
             sim.step(warmup)
@@ -286,7 +293,7 @@ def run_reference(args, spec, scene_list):
         return
     steps = max(1, min(args.steps, 5))
     warm = 1 if args.warmup > 0 else 0
-    value, lat, cores, sample = cpu_baseline(scene_list, steps, warm)
+    value, lat, cores, sample = cpu_baseline(scene_list, steps, warm, integrator=spec.get("integrator", "velocity"))
     lat_ms = [1e3 * x for x in lat]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": warm, "ms_per_step": 1e3 / value,
@@ -335,6 +342,8 @@ def config_of(spec, scene_list, preconditioner="block_jacobi"):
     hess_mb = nt * 90 * (8 if spec["precision"] == 0 else 4) / 1e6
     return {"scenes": len(scene_list), "tets": nt, "verts": int(sum(s.nv for s in scene_list)),
             "material": spec["material"], "precision": "fp64" if spec["precision"] == 0 else "mixed",
+            "integrator": ("BACKWARD_EULER_POSITION (Rayleigh alpha = beta = 0.01)"
+                           if spec.get("integrator") == "position" else "BACKWARD_EULER_VELOCITY"),
             "pcg_tol": 1e-8, "pcg_max_iters": 1000, "preconditioner": preconditioner,
             "l2": f"each step writes {hess_mb:.0f} MB of element Hessians (> 129 MB L2 at 40^3 and the mix); "
                   "no explicit flush"}
@@ -350,7 +359,9 @@ def run_ours(args, spec, scene_list):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    opts = hobak.solver_opts(precision=spec["precision"], use_graph=not args.eager)
+    opts = hobak.solver_opts(precision=spec["precision"], use_graph=not args.eager,
+                             integrator=hobak.INTEGRATOR_POSITION if spec.get("integrator") == "position"
+                             else hobak.INTEGRATOR_VELOCITY)
     batch = hobak.BATCH(scene_list, opts)
     stream = torch.cuda.ExternalStream(batch.stream_handle())
     # launch shapes (tile size, CTA sizes, PCG chunk) from the autotuner, on
@@ -452,7 +463,7 @@ def run_ours(args, spec, scene_list):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         steps = 3 if sum(s.nt for s in scene_list) > 100_000 else 20
-        cv, _, cores, sample = cpu_baseline(scene_list, steps, 0)
+        cv, _, cores, sample = cpu_baseline(scene_list, steps, 0, integrator=spec.get("integrator", "velocity"))
         cpu = {"value": cv, "unit": "steps/s", "cores": cores, "kind": "port",
                "sample": sample + f" of {args.workload} on the host cores (OpenMP), from the initial state"}
 
