@@ -4,20 +4,48 @@
 // solve, read position().  Reads a mesh and state from raw binary files and
 // writes the final displacement, so a test can compare it with the oracle.
 //
-//   bev_gpu_example <in.bin> <out.bin> <steps>
+//   bev_gpu_example <in.bin> <out.bin> <steps> [position]
+// ("position" drives BACKWARD_EULER_POSITION the same way)
 // in.bin: int nv, int nt, int npinned, int material, double mu, lambda,
 //         density, dt, rest[3nv], tets[4nt] (int), pinned[npinned] (int), x0[3nv]
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "../../hobakv1_gb300/cpp/HOBAK_GPU.h"
 
 using namespace HOBAK_GPU;
 
+template <class STEPPER>
+int run(TET_MESH& mesh, VOLUME::HYPERELASTIC& material, const double* prm, const std::vector<double>& x0,
+        const std::vector<int>& pinned, int steps, const char* out) {
+  STEPPER solver(mesh, material);
+  solver.setDt(prm[3]);
+  solver.scaleMass(prm[2]);
+  solver.position() = x0;
+  solver.attachKinematicConstraints(pinned);
+  const VECTOR3 gravity = {0.0, -9.8 * prm[2], 0.0};
+  for (int s = 0; s < steps; s++) {
+    std::fill(solver.externalForces().begin(), solver.externalForces().end(), 0.0);
+    solver.addGravity(gravity);
+    if (!solver.solve(false)) {
+      std::fprintf(stderr, "solve failed: %s\n", solver.lastError().c_str());
+      return 1;
+    }
+  }
+  FILE* o = std::fopen(out, "wb");
+  std::fwrite(solver.position().data(), 8, solver.position().size(), o);
+  std::fwrite(solver.velocity().data(), 8, solver.velocity().size(), o);
+  std::fclose(o);
+  std::printf("%s: steps %d last PCG iterations %d\n", solver.name().c_str(), solver.currentTimestep(),
+              solver.lastSolveStats().iterations);
+  return 0;
+}
+
 int main(int argc, char** argv) {
-  if (argc != 4) {
-    std::fprintf(stderr, "usage: %s in.bin out.bin steps\n", argv[0]);
+  if (argc != 4 && argc != 5) {
+    std::fprintf(stderr, "usage: %s in.bin out.bin steps [position]\n", argv[0]);
     return 2;
   }
   FILE* f = std::fopen(argv[1], "rb");
@@ -42,23 +70,8 @@ int main(int argc, char** argv) {
   VOLUME::ARAP arap(prm[0], prm[1]);
   VOLUME::HYPERELASTIC& material = (kind == HOBAK_MATERIAL_ARAP) ? (VOLUME::HYPERELASTIC&)arap : snh;
 
-  TIMESTEPPER::BACKWARD_EULER_VELOCITY solver(mesh, material);
-  solver.setDt(prm[3]);
-  solver.scaleMass(prm[2]);
-  solver.position() = x0;
-  solver.attachKinematicConstraints(pinned);
-  const VECTOR3 gravity = {0.0, -9.8 * prm[2], 0.0};
-  for (int s = 0; s < std::atoi(argv[3]); s++) {
-    std::fill(solver.externalForces().begin(), solver.externalForces().end(), 0.0);
-    solver.addGravity(gravity);
-    if (!solver.solve(false)) {
-      std::fprintf(stderr, "solve failed: %s\n", solver.lastError().c_str());
-      return 1;
-    }
-  }
-  FILE* o = std::fopen(argv[2], "wb");
-  std::fwrite(solver.position().data(), 8, solver.position().size(), o);
-  std::fclose(o);
-  std::printf("steps %d last PCG iterations %d\n", solver.currentTimestep(), solver.lastSolveStats().iterations);
-  return 0;
+  const int steps = std::atoi(argv[3]);
+  if (argc == 5 && std::string(argv[4]) == "position")
+    return run<TIMESTEPPER::BACKWARD_EULER_POSITION>(mesh, material, prm, x0, pinned, steps, argv[2]);
+  return run<TIMESTEPPER::BACKWARD_EULER_VELOCITY>(mesh, material, prm, x0, pinned, steps, argv[2]);
 }

@@ -39,9 +39,13 @@ def test_cpp_mirror_solve_matches_oracle(tmp_path):
         s.tets.astype(np.int32).tofile(f)
         s.pinned.astype(np.int32).tofile(f)
         s.x0.astype(np.float64).tofile(f)
-    subprocess.run([exe, str(inp), str(out), "10"], check=True)
-    x = np.fromfile(out, dtype=np.float64)
-    sim = oracle.Sim(s, precond=1)
-    sim.step(10)
-    xo, _ = sim.state()
-    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-9
+    for integrator in ("velocity", "position"):
+        subprocess.run([exe, str(inp), str(out), "10"] + ([integrator] if integrator == "position" else []),
+                       check=True)
+        xv = np.fromfile(out, dtype=np.float64)
+        x, v = xv[:3 * s.nv], xv[3 * s.nv:]
+        sim = oracle.Sim(s, precond=1, integrator=integrator)
+        sim.step(10)
+        xo, vo = sim.state()
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-9, integrator
+        assert np.linalg.norm(v - vo) / np.linalg.norm(vo) < 1e-8, integrator
