@@ -927,6 +927,12 @@ struct Sim {
   int integrator = 0;
   double rayAlpha = 0.01, rayBeta = 0.01;  // BACKWARD_EULER_POSITION.cpp:53-54
   std::vector<double> K0;
+  // NEWMARK (integrator 2): acceleration state and the Newton loop's limits
+  // (NEWMARK.cpp:38-43)
+  std::vector<double> acc;
+  int maxNewton = 10;
+  double newtonEps = 1e-7;
+  int lastNewton = 0;
 };
 
 // Vertex-face detection at the current displacement: inverted vertices
@@ -1316,6 +1322,69 @@ void stepPosition(Sim& s) {
     }
 }
 
+// One NEWMARK::solveRayleighDamped step (NEWMARK.cpp:183-340), collisions
+// off, no plane constraints (z = 0).  computeCollisionResponse receives the
+// Rayleigh C as its damping output and zeroes it (TIMESTEPPER.cpp:657) before
+// C is used, so C = 0 here.  beta = 1/4, gamma = 1/2 (NEWMARK.cpp:67-76).
+// Newton: while step < maxNewton and |rhs|^2 > eps (NEWMARK.cpp:212-318):
+//   b = M (a0 (x - x_old) - a2 a_old - a1 v_old) - R - f_ext
+//   A = a0 M - K;  LHS = S A S + (I - S), rhs = S b;  x -= y
+// then v = a3 (x - x_old) + a4 v_old + a5 a_old,
+//      a = a0 (x - x_old) - a1 v_old - a2 a_old, both filtered by S.
+void stepNewmark(Sim& s) {
+  const Mesh& M = s.M;
+  const int nv = M.nv;
+  const double dt = s.dt, beta = 0.25, gamma = 0.5;
+  const double al[6] = {1.0 / (beta * dt * dt),
+                        1.0 / (beta * dt),
+                        (1.0 - 2.0 * beta) / (2.0 * beta),
+                        gamma / (beta * dt),
+                        1.0 - gamma / beta,
+                        (1.0 - gamma / (2.0 * beta)) * dt};
+  if (s.acc.size() != s.x.size()) s.acc.assign(s.x.size(), 0.0);
+  const std::vector<double> xOld = s.x, vOld = s.v, aOld = s.acc;
+  for (size_t k = 0; k < s.pinned.size(); k++)
+    for (int i = 0; i < 3; i++) s.x[3 * s.pinned[k] + i] = s.pinTarget[3 * k + i];
+  double maxR = s.newtonEps * 10;
+  int step = 0;
+  std::vector<double> rhs(3 * (size_t)nv), y;
+  while (step < s.maxNewton && maxR > s.newtonEps) {
+    assemble(s);
+    maxR = 0.0;
+    for (int u = 0; u < nv; u++) {
+      const double m = s.density * M.oneRing[u];
+      for (int i = 0; i < 3; i++) {
+        const size_t q = 3 * (size_t)u + i;
+        const double t = m * (al[0] * (s.x[q] - xOld[q]) - al[2] * aOld[q] - al[1] * vOld[q]);
+        const double b = t - s.R[q] - s.fext[q];
+        rhs[q] = s.free[u] ? b : 0.0;
+        maxR += rhs[q] * rhs[q];
+      }
+    }
+    s.A.resize(s.K.size());
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < (long)s.K.size(); k++) s.A[k] = -s.K[k];
+    for (int u = 0; u < nv; u++) {
+      double* D = &s.A[9 * (size_t)M.diag[u]];
+      const double m = s.density * M.oneRing[u];
+      for (int i = 0; i < 3; i++) D[4 * i] = al[0] * m + D[4 * i];
+    }
+    pcg(s, s.A, rhs, y);
+    for (size_t k = 0; k < s.x.size(); k++) s.x[k] -= y[k];
+    step++;
+  }
+  s.lastNewton = step;
+  for (int u = 0; u < nv; u++)
+    for (int i = 0; i < 3; i++) {
+      const size_t q = 3 * (size_t)u + i;
+      const double dx = s.x[q] - xOld[q];
+      const double vn = al[3] * dx + al[4] * vOld[q] + al[5] * aOld[q];
+      const double an = al[0] * dx - al[1] * vOld[q] - al[2] * aOld[q];
+      s.v[q] = s.free[u] ? vn : 0.0;
+      s.acc[q] = s.free[u] ? an : 0.0;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1426,6 +1495,7 @@ int oracle_step(void* h, int nsteps, int* iters, double* errs) {
   if (!s) return -1;
   for (int k = 0; k < nsteps; k++) {
     if (s->integrator == 1) stepPosition(*s);
+    else if (s->integrator == 2) stepNewmark(*s);
     else step(*s);
     if (iters) iters[k] = s->lastIters;
     if (errs) errs[k] = s->lastErr;
@@ -1436,11 +1506,11 @@ int oracle_step(void* h, int nsteps, int* iters, double* errs) {
 int oracle_nblocks(void* h) { return static_cast<Sim*>(h)->M.rowptr.back(); }
 
 // Integrator: 0 BACKWARD_EULER_VELOCITY, 1 BACKWARD_EULER_POSITION with
-// Rayleigh coefficients alpha, beta (collisions off for the latter).
+// Rayleigh coefficients alpha, beta, 2 NEWMARK (collisions off for 1 and 2).
 int oracle_set_integrator(void* h, int integrator, double alpha, double beta) {
   Sim* s = static_cast<Sim*>(h);
-  if (!s || integrator < 0 || integrator > 1) return -1;
-  if (integrator == 1 && s->coll.on) return -2;
+  if (!s || integrator < 0 || integrator > 2) return -1;
+  if (integrator != 0 && s->coll.on) return -2;
   s->integrator = integrator;
   s->rayAlpha = alpha;
   s->rayBeta = beta;
@@ -1510,6 +1580,8 @@ int oracle_assemble(void* h, int* rowptr, int* cols, double* K, double* R) {
   }
   return 0;
 }
+
+int oracle_newton_iterations(void* h) { return static_cast<Sim*>(h)->lastNewton; }
 
 double oracle_energy(void* h) {
   Sim* s = static_cast<Sim*>(h);

@@ -56,6 +56,7 @@ def lib():
         L.oracle_num_surface_triangles.argtypes = [ctypes.c_void_p]
         L.oracle_vf_response.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
         L.oracle_set_integrator.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.oracle_newton_iterations.argtypes = [ctypes.c_void_p]
         L.oracle_energy.argtypes = [ctypes.c_void_p]
         L.oracle_energy.restype = ctypes.c_double
         _lib = L
@@ -97,7 +98,7 @@ class Sim:
     """CPU oracle timestepper on one scene: BACKWARD_EULER_VELOCITY
     (integrator "velocity", optional vertex-face collisions) or
     BACKWARD_EULER_POSITION (integrator "position", Rayleigh damped with
-    alpha, beta = rayleigh)."""
+    alpha, beta = rayleigh) or NEWMARK (integrator "newmark")."""
 
     def __init__(self, scene, tol=1e-8, maxit=1000, precond=0, integrator="velocity", rayleigh=(0.01, 0.01)):
         L = lib()
@@ -116,7 +117,8 @@ class Sim:
         assert L.oracle_attach_pins(self.h, len(pins), _i(pins)) == 0
         L.oracle_set_solver(self.h, tol, maxit, precond)
         if integrator != "velocity":
-            assert L.oracle_set_integrator(self.h, 1, rayleigh[0], rayleigh[1]) == 0
+            code = {"position": 1, "newmark": 2}[integrator]
+            assert L.oracle_set_integrator(self.h, code, rayleigh[0], rayleigh[1]) == 0
 
     def set_collisions(self, vf=True, eps=0.01, mu=1.0, beta=0.001):
         """Vertex-face self collisions (TIMESTEPPER.cpp:83-86 defaults: mu 1, beta 0.001)."""

@@ -14,7 +14,8 @@
 //       for `steps` steps, recording the displacement and velocity every
 //       `stride` steps.  Options come from <in>/params.npy:
 //         [density, gx, gy, gz, dt, tol, maxit, vf_on, ee_on, coll_eps, coll_mu, coll_beta
-//          (, integrator: 0 velocity / 1 position, rayleigh_alpha, rayleigh_beta)]
+//          (, integrator: 0 velocity / 1 position / 2 Newmark, rayleigh_alpha, rayleigh_beta)]
+//       NEWMARK::solve (Timestepper/NEWMARK.cpp:183-340) is integrator 2.
 //   collide <in> <out> <coll_eps>
 //       vertex-face detection at the displacement in <in>/x.npy
 //       (TET_MESH_FASTER.cpp:248-334, TET_MESH.cpp:1785-1826).
@@ -38,6 +39,7 @@
 #include "Hyperelastic/Volume/STVK.h"
 #include "Timestepper/BACKWARD_EULER_POSITION.h"
 #include "Timestepper/BACKWARD_EULER_VELOCITY.h"
+#include "Timestepper/NEWMARK.h"
 #include "util/MATRIX_UTIL.h"
 #include "npy.h"
 
@@ -87,6 +89,25 @@ class HarnessBEP : public TIMESTEPPER::BACKWARD_EULER_POSITION {
     _rayleighAlpha = alpha;
     _rayleighBeta = beta;
   }
+  void setSolver(double tol, int maxit) {
+    _cgSolver.setTolerance(tol);
+    _cgSolver.setMaxIterations(maxit);
+  }
+  int lastIterations() const { return (int)_cgSolver.iterations(); }
+  double lastError() const { return (double)_cgSolver.error(); }
+  void pin(const KINEMATIC_SHAPE* shape, int vertexID, const VECTOR3& world) {
+    KINEMATIC_CONSTRAINT c;
+    c.shape = shape;
+    c.vertexID = vertexID;
+    c.localPosition = shape->worldVertexToLocal(world);
+    _kinematicConstraints.push_back(c);
+  }
+};
+
+// and for NEWMARK
+class HarnessNewmark : public TIMESTEPPER::NEWMARK {
+ public:
+  HarnessNewmark(TET_MESH& m, VOLUME::HYPERELASTIC& h) : NEWMARK(m, h) {}
   void setSolver(double tol, int maxit) {
     _cgSolver.setTolerance(tol);
     _cgSolver.setMaxIterations(maxit);
@@ -278,8 +299,9 @@ int runWith(const std::string& in, const std::string& out, const std::string& ma
 int modeRun(const std::string& in, const std::string& out, const std::string& mat, double mu, double lambda,
             int steps, int stride) {
   npy::Array prm = npy::load(in + "/params.npy");
-  const bool position = prm.size() >= 13 && prm.f8()[12] == 1.0;
-  if (position) return runWith<HarnessBEP>(in, out, mat, mu, lambda, steps, stride);
+  const double integrator = prm.size() >= 13 ? prm.f8()[12] : 0.0;
+  if (integrator == 1.0) return runWith<HarnessBEP>(in, out, mat, mu, lambda, steps, stride);
+  if (integrator == 2.0) return runWith<HarnessNewmark>(in, out, mat, mu, lambda, steps, stride);
   return runWith<HarnessBEV>(in, out, mat, mu, lambda, steps, stride);
 }
 

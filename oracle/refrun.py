@@ -43,9 +43,10 @@ def elements(rest, tets, x, material, mu, lam):
 def run(scene, steps, stride=1, tol=1e-8, maxit=1000, vf=False, ee=False,
         coll_eps=0.01, coll_mu=1.0, coll_beta=0.001, threads=None, integrator="velocity",
         rayleigh=(0.01, 0.01)):
-    """BACKWARD_EULER_VELOCITY::solve (integrator "velocity") or
+    """BACKWARD_EULER_VELOCITY::solve (integrator "velocity"),
     BACKWARD_EULER_POSITION::solve (integrator "position", Rayleigh damped
-    with alpha, beta = rayleigh) for `steps` steps on `scene`."""
+    with alpha, beta = rayleigh) or NEWMARK::solve (integrator "newmark")
+    for `steps` steps on `scene`."""
     with tempfile.TemporaryDirectory() as tin, tempfile.TemporaryDirectory() as tout:
         _write_mesh(tin, scene.rest, scene.tets)
         np.save(os.path.join(tin, "x0.npy"), scene.x0.reshape(-1).astype(np.float64))
@@ -54,7 +55,7 @@ def run(scene, steps, stride=1, tol=1e-8, maxit=1000, vf=False, ee=False,
         g = scene.gravity
         params = np.array([scene.density, g[0], g[1], g[2], scene.dt, tol, maxit,
                            float(vf), float(ee), coll_eps, coll_mu, coll_beta,
-                           1.0 if integrator == "position" else 0.0, rayleigh[0], rayleigh[1]],
+                           {"velocity": 0.0, "position": 1.0, "newmark": 2.0}[integrator], rayleigh[0], rayleigh[1]],
                           dtype=np.float64)
         np.save(os.path.join(tin, "params.npy"), params)
         env = dict(os.environ)

@@ -6,7 +6,7 @@ so this only runs where they are).  Inputs come from hobakv1_gb300.scenes, so
 they are regenerated bit-identically anywhere.  Usage:
 
     make -C oracle/ref REF=<reference checkout> -j8
-    python tests/golden/make_golden.py [elements] [trajectories] [position] [collisions]
+    python tests/golden/make_golden.py [elements] [trajectories] [position] [newmark] [collisions]
 """
 from __future__ import annotations
 
@@ -79,6 +79,19 @@ def make_position_trajectories():
         print("position trajectory", s.name, r["iters"].sum())
 
 
+def make_newmark_trajectories():
+    """NEWMARK (beta 1/4, gamma 1/2, Newton to |rhs|^2 <= 1e-7, at most 10
+    iterations) on the pinned, compressed and twisted cubes."""
+    cases = [(scenes.config2_scene(6, "snh"), 40, 10),
+             (scenes.config2_scene(6, "arap"), 40, 10)]
+    for s, steps, stride in cases:
+        r = refrun.run(s, steps, stride=stride, integrator="newmark")
+        np.savez_compressed(os.path.join(OUT, f"traj_{s.name}_newmark.npz"), x=r["x"], v=r["v"],
+                            iters=r["iters"], cg_error=r["cg_error"], energy=r["energy"],
+                            steps=steps, stride=stride)
+        print("newmark trajectory", s.name, r["iters"].sum())
+
+
 def make_collisions():
     """Two cubes in contact: vertex-face pairs (reference AABB broad phase +
     narrow phase) at the start and along a 40-step trajectory with collisions."""
@@ -97,12 +110,14 @@ def make_collisions():
 if __name__ == "__main__":
     if not refrun.available():
         sys.exit("reference build missing: make -C oracle/ref REF=<reference checkout>")
-    which = set(sys.argv[1:]) or {"elements", "trajectories", "position", "collisions"}
+    which = set(sys.argv[1:]) or {"elements", "trajectories", "position", "newmark", "collisions"}
     if "elements" in which:
         make_elements()
     if "trajectories" in which:
         make_trajectories()
     if "position" in which:
         make_position_trajectories()
+    if "newmark" in which:
+        make_newmark_trajectories()
     if "collisions" in which:
         make_collisions()

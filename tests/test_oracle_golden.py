@@ -110,6 +110,27 @@ def test_oracle_position_integrator_matches_reference(name, scene_fn):
     assert np.abs(np.array(iters) - g["iters"]).max() <= 1
 
 
+@pytest.mark.parametrize("name,scene_fn", [
+    ("kuhn6_snh_twist", lambda: scenes.config2_scene(6, "snh")),
+    ("kuhn6_arap_twist", lambda: scenes.config2_scene(6, "arap")),
+])
+def test_oracle_newmark_matches_reference(name, scene_fn):
+    """NEWMARK (Newton loop of Rayleigh-damped solves whose C the reference
+    zeroes): the restatement against the reference's own trajectory, and the
+    last Newton iteration's CG count of every step."""
+    g = np.load(os.path.join(GOLDEN, f"traj_{name}_newmark.npz"))
+    sim = oracle.Sim(scene_fn(), integrator="newmark")
+    stride = int(g["stride"])
+    iters = []
+    for k in range(1, g["x"].shape[0]):
+        it, _ = sim.step(stride)
+        iters.extend(it.tolist())
+        x, v = sim.state()
+        assert np.linalg.norm(x - g["x"][k]) / np.linalg.norm(g["x"][k]) < 1e-10, k
+        assert np.linalg.norm(v - g["v"][k]) / np.linalg.norm(g["v"][k]) < 1e-9, k
+    assert np.abs(np.array(iters) - g["iters"]).max() <= 1
+
+
 def test_oracle_vertex_face_collisions_match_reference():
     """Surface triangles bit-exact; vertex-face pair sets bit-exact at every
     recorded state; the 40-step trajectory with collisions within 1e-8."""
