@@ -22,6 +22,8 @@ Workloads (synthetic, seeded; see hobakv1_gb300/scenes.py):
   mix64_mixed             the first 64 scenes of the mix, mixed (a profiling-sized case)
   kuhn40_snh_twist_position[_mixed], mix256_position_mixed
                           the same inputs stepped by BACKWARD_EULER_POSITION (Rayleigh damped)
+  kuhn40_snh_twist_newmark_mixed, mix256_newmark_mixed
+                          ... and by NEWMARK (a Newton loop of solves per step)
   serve_poisson           continuous batching: 32 jobs (N ~ U{8..32}, 10-200 steps, half two cubes in
                           vertex-face contact) arriving as a Poisson stream at 50, 400 and 2000 jobs/s,
                           mixed precision and plain FP64; job-steps/s, p50/p99 step and job latency
@@ -57,6 +59,9 @@ WORKLOADS = {
     "kuhn40_snh_twist_position_mixed": dict(kind="config2", N=40, material="snh", precision=1,
                                             integrator="position"),
     "mix256_position_mixed": dict(kind="mix", count=256, material="snh/arap", precision=1, integrator="position"),
+    # NEWMARK (a Newton loop of linear solves per step)
+    "kuhn40_snh_twist_newmark_mixed": dict(kind="config2", N=40, material="snh", precision=1, integrator="newmark"),
+    "mix256_newmark_mixed": dict(kind="mix", count=256, material="snh/arap", precision=1, integrator="newmark"),
     "serve_poisson": dict(kind="serve", count=32, lambdas=[50, 400, 2000], material="snh/arap",
                           precision=1),
 }
@@ -342,8 +347,9 @@ def config_of(spec, scene_list, preconditioner="block_jacobi"):
     hess_mb = nt * 90 * (8 if spec["precision"] == 0 else 4) / 1e6
     return {"scenes": len(scene_list), "tets": nt, "verts": int(sum(s.nv for s in scene_list)),
             "material": spec["material"], "precision": "fp64" if spec["precision"] == 0 else "mixed",
-            "integrator": ("BACKWARD_EULER_POSITION (Rayleigh alpha = beta = 0.01)"
-                           if spec.get("integrator") == "position" else "BACKWARD_EULER_VELOCITY"),
+            "integrator": {"position": "BACKWARD_EULER_POSITION (Rayleigh alpha = beta = 0.01)",
+                           "newmark": "NEWMARK (beta 1/4, gamma 1/2, Newton to |rhs|^2 <= 1e-7, at most 10)"}
+                          .get(spec.get("integrator"), "BACKWARD_EULER_VELOCITY"),
             "pcg_tol": 1e-8, "pcg_max_iters": 1000, "preconditioner": preconditioner,
             "l2": f"each step writes {hess_mb:.0f} MB of element Hessians (> 129 MB L2 at 40^3 and the mix); "
                   "no explicit flush"}
@@ -360,8 +366,8 @@ def run_ours(args, spec, scene_list):
         dist.init_process_group("nccl")
 
     opts = hobak.solver_opts(precision=spec["precision"], use_graph=not args.eager,
-                             integrator=hobak.INTEGRATOR_POSITION if spec.get("integrator") == "position"
-                             else hobak.INTEGRATOR_VELOCITY)
+                             integrator={"position": hobak.INTEGRATOR_POSITION, "newmark": hobak.INTEGRATOR_NEWMARK}
+                             .get(spec.get("integrator"), hobak.INTEGRATOR_VELOCITY))
     batch = hobak.BATCH(scene_list, opts)
     stream = torch.cuda.ExternalStream(batch.stream_handle())
     # launch shapes (tile size, CTA sizes, PCG chunk) from the autotuner, on

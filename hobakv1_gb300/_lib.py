@@ -29,7 +29,8 @@ class HobakSolverOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iters", ctypes.c_int), ("precision", ctypes.c_int),
                 ("preconditioner", ctypes.c_int), ("max_refinements", ctypes.c_int),
                 ("use_graph", ctypes.c_int), ("integrator", ctypes.c_int),
-                ("rayleigh_alpha", ctypes.c_double), ("rayleigh_beta", ctypes.c_double)]
+                ("rayleigh_alpha", ctypes.c_double), ("rayleigh_beta", ctypes.c_double),
+                ("max_newton", ctypes.c_int), ("newton_tolerance", ctypes.c_double)]
 
 
 class HobakTuning(ctypes.Structure):
@@ -88,6 +89,8 @@ SIGNATURES = {
     "hobak_batch_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "hobak_batch_kernel_bytes": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "hobak_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakTuning)]),
+    "hobak_batch_get_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "hobak_batch_set_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "hobak_batch_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakTuning)]),
     "hobak_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(HobakTuning)]),
     "hobak_batch_set_collisions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,

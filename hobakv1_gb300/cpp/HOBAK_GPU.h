@@ -272,5 +272,30 @@ class BACKWARD_EULER_POSITION : public BACKWARD_EULER_VELOCITY {
   }
 };
 
+// GPU drop-in for NEWMARK (Rayleigh-damped solve, NEWMARK.cpp:183-340): a
+// Newton loop of at most maxNewtonIterations() solves on the device;
+// acceleration() is host state like position() and velocity().  Vertex-face
+// contact is not available with this integrator.
+class NEWMARK : public BACKWARD_EULER_VELOCITY {
+ public:
+  NEWMARK(TET_MESH& tetMesh, VOLUME::HYPERELASTIC& hyperelastic) : BACKWARD_EULER_VELOCITY(tetMesh, hyperelastic) {
+    _opts.integrator = HOBAK_INTEGRATOR_NEWMARK;
+    _name = "NEWMARK";
+    _acceleration.assign(tetMesh.DOFs(), 0.0);
+  }
+  VECTOR& acceleration() { return _acceleration; }
+  int& maxNewtonIterations() { return _opts.max_newton; }
+  bool solve(const bool verbose) {
+    if (!_handle && !build()) return false;
+    if (hobak_batch_set_acceleration(_handle, 0, _acceleration.data()) != HOBAK_OK) return fail();
+    if (!BACKWARD_EULER_VELOCITY::solve(verbose)) return false;
+    if (hobak_batch_get_acceleration(_handle, 0, _acceleration.data()) != HOBAK_OK) return fail();
+    return true;
+  }
+
+ private:
+  VECTOR _acceleration;
+};
+
 }  // namespace TIMESTEPPER
 }  // namespace HOBAK_GPU

@@ -84,6 +84,8 @@ struct hobak_batch_t {
   cudaStream_t stream = nullptr;
   cudaStream_t captureStream = nullptr;   // fills the bodies of captured while loops
   cudaStream_t captureStream2 = nullptr;  // fills the bodies of the switch nodes inside them
+  cudaStream_t captureStreamN = nullptr;  // fills the body of a Newmark step's Newton loop
+  long long eagerNewton = 0;              // Newton bodies enqueued eagerly
   cudaGraphExec_t stepGraph[2] = {nullptr, nullptr};  // untimed, timed
   long long eagerChunks = 0;
   long long loopLaunchBase = 0;  // loop-body launches folded in before the last chunk change
@@ -189,6 +191,24 @@ T* carve(void* base, size_t off) {
 }
 
 void drop_graphs(hobak_batch_t* B);
+
+// A scene's integrator constants: Rayleigh coefficients (position) and the
+// Newmark coefficients for beta = 1/4, gamma = 1/2 from its dt
+// (NEWMARK.cpp:67-76, recomputed by setDt at NEWMARK.cpp:107-116).
+void set_integrator(SceneParams& p, const hobak_solver_opts& o) {
+  p.integrator = o.integrator;
+  p.rayAlpha = o.rayleigh_alpha;
+  p.rayBeta = o.rayleigh_beta;
+  const double dt = p.dt, beta = 0.25, gamma = 0.5;
+  p.nm[0] = 1.0 / (beta * dt * dt);
+  p.nm[1] = 1.0 / (beta * dt);
+  p.nm[2] = (1.0 - 2.0 * beta) / (2.0 * beta);
+  p.nm[3] = gamma / (beta * dt);
+  p.nm[4] = 1.0 - gamma / beta;
+  p.nm[5] = (1.0 - gamma / (2.0 * beta)) * dt;
+  p.newtonEps = o.newton_tolerance;
+  p.maxNewton = o.max_newton;
+}
 
 // Clamped Hessian of every scene at zero displacement (the position
 // integrator's Rayleigh damping C = alpha M + beta K0 builds it at rest every
@@ -460,9 +480,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     p.lambda = mp.lambda;
     p.alpha = mp.alpha;
     p.dt = H.dt;
-    p.integrator = B->opts.integrator;
-    p.rayAlpha = B->opts.rayleigh_alpha;
-    p.rayBeta = B->opts.rayleigh_beta;
+    set_integrator(p, B->opts);
     p.active = 1;
     sparams.push_back(p);
   }
@@ -498,6 +516,9 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oClusterList = A.reserve(sizeof(int) * n);
   const size_t oEG = A.reserve(sizeof(double) * 12 * (size_t)nt);
   const size_t oRhs = A.reserve(V3), oY = A.reserve(V3), oR64 = A.reserve(V3);
+  // Newmark: acceleration and the step's starting x, v, a
+  const size_t oAcc = A.reserve(V3), oXo = A.reserve(V3), oVo = A.reserve(V3), oAo = A.reserve(V3);
+  const size_t oNewton = A.reserve(sizeof(int)), oNewtonRuns = A.reserve(sizeof(unsigned long long));
   const size_t oPart = A.reserve(sizeof(double) * kPartials * (size_t)ntilesCap);
   const size_t oPsi = A.reserve(sizeof(double) * nt);
   void* base = nullptr;
@@ -522,6 +543,12 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.solve = carve<SolveState>(base, oSolve);
   d.active = carve<int>(base, oActive);
   d.bodyRuns = carve<unsigned long long>(base, oBodyRuns);
+  d.acc = carve<double>(base, oAcc);
+  d.xOld = carve<double>(base, oXo);
+  d.vOld = carve<double>(base, oVo);
+  d.aOld = carve<double>(base, oAo);
+  d.newtonActive = carve<int>(base, oNewton);
+  d.newtonRuns = carve<unsigned long long>(base, oNewtonRuns);
   d.rest = carve<double>(base, oRest);
   d.x = carve<double>(base, oX);
   d.v = carve<double>(base, oV);
@@ -617,8 +644,11 @@ int check_opts(const hobak_solver_opts* o) {
   if (o->preconditioner != HOBAK_PRECOND_JACOBI && o->preconditioner != HOBAK_PRECOND_BLOCK_JACOBI)
     return fail(HOBAK_ERR_INVALID, "unknown preconditioner");
   if (o->max_refinements < 0 || o->max_refinements > 3) return fail(HOBAK_ERR_INVALID, "max_refinements in 0..3");
-  if (o->integrator != HOBAK_INTEGRATOR_VELOCITY && o->integrator != HOBAK_INTEGRATOR_POSITION)
+  if (o->integrator != HOBAK_INTEGRATOR_VELOCITY && o->integrator != HOBAK_INTEGRATOR_POSITION &&
+      o->integrator != HOBAK_INTEGRATOR_NEWMARK)
     return fail(HOBAK_ERR_INVALID, "unknown integrator");
+  if (o->max_newton < 1 || o->max_newton > 100 || !(o->newton_tolerance >= 0.0))
+    return fail(HOBAK_ERR_INVALID, "max_newton in 1..100 and newton_tolerance >= 0");
   if (!(o->rayleigh_alpha >= 0.0) || !(o->rayleigh_beta >= 0.0) || !std::isfinite(o->rayleigh_alpha) ||
       !std::isfinite(o->rayleigh_beta))
     return fail(HOBAK_ERR_INVALID, "Rayleigh coefficients must be finite and >= 0");
@@ -630,12 +660,27 @@ int sweeps_of(const hobak_solver_opts& o) {
 }
 
 // Kernels launched per step outside the PCG loop bodies.
-long long fixed_launches(const hobak_batch_t* B) {
+// Kernels of one linear solve outside the PCG loop bodies.
+long long solve_launches(const hobak_batch_t* B) {
   const int sweeps = sweeps_of(B->opts);
   const bool mixed = B->opts.precision == HOBAK_PRECISION_MIXED;
   int cl = 0;
   for (const ClusterClass& c : B->classes) cl += c.count > 0 ? 1 : 0;
-  return 6 + sweeps * (1 + (B->anyTileScene ? 1 : 0) + cl + (mixed ? 2 : 0));
+  // per sweep: k_set_active, inner init (+ the loop's arming kernel in a
+  // graph), the cluster classes, the refinement
+  const int tile = B->anyTileScene ? (B->opts.use_graph ? 2 : 1) : 0;
+  return sweeps * (1 + tile + cl + (mixed ? 2 : 0));
+}
+
+// Kernels of one Newton loop body (Newmark) outside the PCG loop bodies and
+// k_newton_continue: element, assembly, preconditioner, rhs, the solve, and
+// the update + test.
+long long newton_body_launches(const hobak_batch_t* B) { return 4 + solve_launches(B) + 2; }
+
+long long fixed_launches(const hobak_batch_t* B) {
+  // begin, Newton begin, finish (+ the Newton loop's arming kernel in a graph)
+  if (B->opts.integrator == HOBAK_INTEGRATOR_NEWMARK) return 3 + (B->opts.use_graph ? 1 : 0);
+  return 6 + solve_launches(B);
 }
 
 void drop_graphs(hobak_batch_t* B);
@@ -721,6 +766,14 @@ int add_conditional(cudaStream_t s, cudaGraphConditionalNodeType type, unsigned 
   CUDA_TRY(cudaStreamGetCaptureInfo(s, &cs, nullptr, &capG, &deps, nullptr, &nd));
   if (cs != cudaStreamCaptureStatusActive) return fail(HOBAK_ERR_CUDA, "stream is not capturing");
   CUDA_TRY(cudaGraphConditionalHandleCreate(h, capG, defaultValue, flags));
+  if (type == cudaGraphCondTypeWhile) {
+    // a kernel in front of the node sets the condition every time the
+    // enclosing graph reaches it: a loop inside another loop's body (the
+    // PCG loop inside Newmark's Newton loop) would otherwise start from the
+    // value that ended its previous run
+    launch_set_condition((unsigned long long)*h, defaultValue, s);
+    CUDA_TRY(cudaStreamGetCaptureInfo(s, &cs, nullptr, &capG, &deps, nullptr, &nd));
+  }
   cudaGraphNodeParams p = {};
   p.type = cudaGraphNodeTypeConditional;
   p.conditional.handle = *h;
@@ -803,31 +856,17 @@ int eager_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
   return HOBAK_OK;
 }
 
-// One BACKWARD_EULER_VELOCITY step: element terms, assembly, preconditioner,
-// rhs, then per sweep an inner PCG (and, mixed, the FP64 refinement), update.
-// `capture` builds the device-side loops of a graph; otherwise loops poll.
+// The linear solve of a step: per sweep an inner PCG (cluster classes on
+// their own streams beside the tile path, joined before the refinement: small
+// scenes solve while large ones iterate, and a class's long-running scenes do
+// not hold up the others) and, mixed, the FP64 refinement.
 template <typename T>
-int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, const PcgVecs<T>& v) {
+int enqueue_solve_t(hobak_batch_t* B, cudaStream_t s, bool capture, const PcgVecs<T>& v) {
   const DeviceBatch& d = B->d;
   const bool mixed = sizeof(T) == sizeof(float);
-  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[0], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
-  launch_begin_step(d, s);
-  if (mixed) launch_element_mixed(d, s);
-  else launch_element(d, s);
-  if (d.collOn) launch_collisions(d, d.coll, s);
-  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[1], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
-  launch_assemble<T>(d, v, s);
-  if (d.collOn) launch_collision_diag(d, d.coll, s);
-  launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
-  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[2], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
-  launch_rhs(d, s);
-  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[3], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
   const int sweeps = sweeps_of(B->opts);
   for (int k = 0; k < sweeps; k++) {
     launch_set_active(d, s);
-    // cluster classes on their own streams, beside the tile path on `s`,
-    // joined before the refinement: small scenes solve while large ones
-    // iterate, and a class's long-running scenes do not hold up the others
     int forked = 0;
     for (int c = kClusterClasses - 1; c >= 0; c--) {
       if (B->classes[c].count == 0) continue;
@@ -846,9 +885,85 @@ int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, c
       if (B->classes[c].count) CUDA_TRY(cudaStreamWaitEvent(s, B->evJoin[c], 0));
     if (mixed) launch_refine(d, s);
   }
-  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[4], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
+  return HOBAK_OK;
+}
+
+// One Newton iteration of NEWMARK::solveRayleighDamped (NEWMARK.cpp:216-318):
+// element terms at the current x, assembly, preconditioner, rhs and its
+// |rhs|^2, the linear solve, x -= y and the per-scene Newton test.
+template <typename T>
+int enqueue_newton_body(hobak_batch_t* B, cudaStream_t s, bool capture, const PcgVecs<T>& v) {
+  const DeviceBatch& d = B->d;
+  if (sizeof(T) == sizeof(float)) launch_element_mixed(d, s);
+  else launch_element(d, s);
+  launch_assemble<T>(d, v, s);
+  launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
+  launch_rhs(d, s);
+  if (int rc = enqueue_solve_t<T>(B, s, capture, v)) return rc;
+  launch_newton_update(d, s);
+  return HOBAK_OK;
+}
+
+// The Newton loop: a conditional WHILE node (graph) whose body ends in
+// k_newton_continue, or a host loop over the same body (eager).
+template <typename T>
+int enqueue_newton_loop(hobak_batch_t* B, cudaStream_t s, bool capture, const PcgVecs<T>& v) {
+  if (!capture) {
+    for (int it = 0; it < B->opts.max_newton; it++) {
+      if (int rc = enqueue_newton_body<T>(B, s, false, v)) return rc;
+      B->eagerNewton++;
+      CUDA_TRY(cudaMemcpyAsync(B->pinnedActive, B->d.newtonActive, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaStreamSynchronize(s));
+      if (B->pinnedActive[0] <= 0) break;
+    }
+    return HOBAK_OK;
+  }
+  cudaGraphConditionalHandle h;
+  cudaGraph_t body;
+  if (int rc = add_conditional(s, cudaGraphCondTypeWhile, 1, 1, cudaGraphCondAssignDefault, &h, &body)) return rc;
+  CUDA_TRY(cudaStreamBeginCaptureToGraph(B->captureStreamN, body, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_newton_body<T>(B, B->captureStreamN, true, v);
+  launch_newton_continue(B->d, (unsigned long long)h, B->captureStreamN);
+  cudaGraph_t out = nullptr;
+  CUDA_TRY(cudaStreamEndCapture(B->captureStreamN, &out));
+  return rc;
+}
+
+// One step: BACKWARD_EULER_VELOCITY or BACKWARD_EULER_POSITION (element
+// terms, assembly, preconditioner, rhs, the linear solve, update), or NEWMARK
+// (the same inside a Newton loop).  `capture` builds the device-side loops of
+// a graph; otherwise loops poll.  With `timed`, events bracket the phases
+// (for Newmark the whole Newton loop is the solve phase: events cannot sit
+// inside a conditional body).
+template <typename T>
+int enqueue_step_t(hobak_batch_t* B, cudaStream_t s, bool capture, bool timed, const PcgVecs<T>& v) {
+  const DeviceBatch& d = B->d;
+  const bool mixed = sizeof(T) == sizeof(float);
+  const unsigned evFlags = capture ? cudaEventRecordExternal : cudaEventRecordDefault;
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[0], s, evFlags));
+  launch_begin_step(d, s);
+  if (B->opts.integrator == HOBAK_INTEGRATOR_NEWMARK) {
+    launch_newton_begin(d, s);
+    if (timed)
+      for (int i = 1; i <= 3; i++) CUDA_TRY(cudaEventRecordWithFlags(B->ev[i], s, evFlags));
+    if (int rc = enqueue_newton_loop<T>(B, s, capture, v)) return rc;
+  } else {
+    if (mixed) launch_element_mixed(d, s);
+    else launch_element(d, s);
+    if (d.collOn) launch_collisions(d, d.coll, s);
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[1], s, evFlags));
+    launch_assemble<T>(d, v, s);
+    if (d.collOn) launch_collision_diag(d, d.coll, s);
+    launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[2], s, evFlags));
+    launch_rhs(d, s);
+    if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[3], s, evFlags));
+    if (int rc = enqueue_solve_t<T>(B, s, capture, v)) return rc;
+  }
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[4], s, evFlags));
   launch_finish_step(d, s);
-  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[5], s, capture ? cudaEventRecordExternal : cudaEventRecordDefault));
+  if (timed) CUDA_TRY(cudaEventRecordWithFlags(B->ev[5], s, evFlags));
   return HOBAK_OK;
 }
 
@@ -1109,6 +1224,10 @@ int count_loop_launches(hobak_batch_t* B, long long* out) {
   // a loop body = tile compaction + chunk x (SpMV, update) + k_continue; an
   // eager chunk has no k_continue
   *out = B->loopLaunchBase + (long long)(runs * (2ull * B->chunk + 2ull)) + B->eagerChunks * (2LL * B->chunk + 1);
+  // Newmark's Newton loop bodies (graph: with k_newton_continue)
+  unsigned long long nruns = 0;
+  CUDA_TRY(cudaMemcpy(&nruns, B->d.newtonRuns, sizeof(nruns), cudaMemcpyDeviceToHost));
+  *out += (long long)nruns * (newton_body_launches(B) + 1) + B->eagerNewton * newton_body_launches(B);
   return HOBAK_OK;
 }
 
@@ -1121,6 +1240,8 @@ int fold_loop_launches(hobak_batch_t* B) {
   B->loopLaunchBase = n;
   B->eagerChunks = 0;
   CUDA_TRY(cudaMemset(B->d.bodyRuns, 0, sizeof(unsigned long long)));
+  CUDA_TRY(cudaMemset(B->d.newtonRuns, 0, sizeof(unsigned long long)));
+  B->eagerNewton = 0;
   return HOBAK_OK;
 }
 
@@ -1192,6 +1313,8 @@ void hobak_default_solver_opts(hobak_solver_opts* o) {
   o->integrator = HOBAK_INTEGRATOR_VELOCITY;
   o->rayleigh_alpha = 0.01;
   o->rayleigh_beta = 0.01;
+  o->max_newton = 10;           // NEWMARK.cpp:41
+  o->newton_tolerance = 1e-7;   // NEWMARK.cpp:43
 }
 
 int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_solver_opts* opts,
@@ -1212,6 +1335,7 @@ int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_
   CUDA_TRY(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
   CUDA_TRY(cudaStreamCreateWithFlags(&B->captureStream, cudaStreamNonBlocking));
   CUDA_TRY(cudaStreamCreateWithFlags(&B->captureStream2, cudaStreamNonBlocking));
+  CUDA_TRY(cudaStreamCreateWithFlags(&B->captureStreamN, cudaStreamNonBlocking));
   for (auto& cs : B->classStream) CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreateWithFlags(&B->evFork, cudaEventDisableTiming));
   for (auto& e : B->evJoin) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1240,6 +1364,7 @@ int hobak_batch_destroy(hobak_batch b) {
   drop_graphs(b);
   if (b->captureStream) cudaStreamDestroy(b->captureStream);
   if (b->captureStream2) cudaStreamDestroy(b->captureStream2);
+  if (b->captureStreamN) cudaStreamDestroy(b->captureStreamN);
   for (auto& cs : b->classStream)
     if (cs) cudaStreamDestroy(cs);
   if (b->evFork) cudaEventDestroy(b->evFork);
@@ -1339,6 +1464,24 @@ int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v) {
   return HOBAK_OK;
 }
 
+int hobak_batch_get_acceleration(hobak_batch b, int scene, double* a) {
+  if (!b || !a || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  const SceneHost& H = b->scenes[scene];
+  CUDA_TRY(cudaMemcpyAsync(a, b->d.acc + 3 * (size_t)H.v0, 3 * sizeof(double) * H.nv, cudaMemcpyDeviceToHost,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_acceleration(hobak_batch b, int scene, const double* a) {
+  if (!b || !a || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  const SceneHost& H = b->scenes[scene];
+  CUDA_TRY(cudaMemcpyAsync(b->d.acc + 3 * (size_t)H.v0, a, 3 * sizeof(double) * H.nv, cudaMemcpyHostToDevice,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
 // Whole-batch state: every scene's 3*nv values back to back in scene order,
 // which is how the batch keeps them on the device, so each is one copy.
 int hobak_batch_set_state_all(hobak_batch b, const double* x, const double* v) {
@@ -1388,11 +1531,7 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   if ((opts->precision == HOBAK_PRECISION_MIXED) != b->precMixed) {
     if ((rc = alloc_precision(b))) return rc;
   }
-  for (SceneParams& p : b->sceneParams) {
-    p.integrator = opts->integrator;
-    p.rayAlpha = opts->rayleigh_alpha;
-    p.rayBeta = opts->rayleigh_beta;
-  }
+  for (SceneParams& p : b->sceneParams) set_integrator(p, *opts);
   CUDA_TRY(cudaMemcpy(const_cast<SceneParams*>(b->d.scenes), b->sceneParams.data(),
                       sizeof(SceneParams) * b->sceneParams.size(), cudaMemcpyHostToDevice));
   if (opts->integrator == HOBAK_INTEGRATOR_POSITION && (rc = rest_hessian(b))) return rc;

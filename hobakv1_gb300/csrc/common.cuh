@@ -30,6 +30,7 @@ constexpr int kPartials = 4;      // per-tile partial sums slots
 // update), sharing every kernel but the coefficients of rhs, LHS and update.
 constexpr int kIntegratorVelocity = 0;
 constexpr int kIntegratorPosition = 1;
+constexpr int kIntegratorNewmark = 2;  // NEWMARK::solveRayleighDamped: a Newton loop of such solves
 
 // Index of block (a, b), a <= b, in the 10-block upper triangle of a 4x4
 // block matrix: (0,0)(0,1)(0,2)(0,3)(1,1)(1,2)(1,3)(2,2)(2,3)(3,3).
@@ -48,6 +49,9 @@ struct SceneParams {
   double mu, lambda, alpha;  // reparameterised material constants
   double dt;
   double rayAlpha, rayBeta;  // Rayleigh damping C = rayAlpha M + rayBeta K0 (position integrator)
+  double nm[6];              // Newmark coefficients alpha_0..5 (NEWMARK.cpp:71-76) from dt
+  double newtonEps;          // Newmark: Newton stops once |rhs|^2 <= newtonEps ...
+  int maxNewton;             // ... or after maxNewton iterations
 };
 
 // Per-scene solver scalars, written by the last CTA of each reduction.
@@ -71,6 +75,9 @@ struct SolveState {
   float alphaF, betaF;  // FP32 copies for the mixed inner solve (no per-thread conversion)
   int iters, done;
   unsigned ticketA, ticketB;
+  // Newmark's Newton loop: iterations done, finished flag, |rhs|^2 of the last one
+  int newtonStep, newtonDone;
+  double newtonR;
 };
 
 }  // namespace hobak

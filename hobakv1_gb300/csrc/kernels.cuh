@@ -92,6 +92,14 @@ struct DeviceBatch {
   // clamped Hessian at zero displacement, CSR block order, 3x3 column major
   // (the position integrator's Rayleigh damping; null when unused)
   const double* K0;
+  // Newmark: acceleration, the step's starting x, v, a, and the count of
+  // scenes whose Newton loop still runs
+  double* acc;
+  double* xOld;
+  double* vOld;
+  double* aOld;
+  int* newtonActive;
+  unsigned long long* newtonRuns;  // Newton loop bodies executed (graph mode), for launch accounting
 
   // tiles
   const int* tileScene;
@@ -167,6 +175,13 @@ void launch_pcg_iteration(const DeviceBatch& b, const PcgVecs<T>& v, cudaStream_
 }
 void launch_refine(const DeviceBatch& b, cudaStream_t s);  // y += d, then r64 = rhs - A y
 void launch_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s);void launch_finish_step(const DeviceBatch& b, cudaStream_t s);
+// Newmark: save x, v, a and start the Newton loop; after each solve
+// x -= y and the per-scene Newton test; the graph loop's condition.
+void launch_newton_begin(const DeviceBatch& b, cudaStream_t s);
+void launch_newton_update(const DeviceBatch& b, cudaStream_t s);
+void launch_newton_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s);
+// Sets a graph conditional handle (a loop's condition before its node).
+void launch_set_condition(unsigned long long handle, unsigned value, cudaStream_t s);
 void launch_energy(const DeviceBatch& b, cudaStream_t s);
 
 // element-level entry points (standalone, no batch)

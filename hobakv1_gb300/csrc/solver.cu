@@ -194,11 +194,74 @@ __host__ __device__ constexpr int update_warps(int TV) { return (TV + 9) / 10; }
 
 // x[pinned] = pin target at the start of a step
 // (applyKinematicConstraints, TIMESTEPPER.cpp:105-122).
+// Newmark also keeps the step's starting x, v, a (before the pins move x).
 __global__ void k_begin_step(DeviceBatch b) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= b.nv || b.freeMask[u]) return;
+  if (u >= b.nv) return;
+  if (b.scenes[b.vertexScene[u]].integrator == kIntegratorNewmark)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const size_t q = 3 * (size_t)u + i;
+      b.xOld[q] = b.x[q];
+      b.vOld[q] = b.v[q];
+      b.aOld[q] = b.acc[q];
+    }
+  if (b.freeMask[u]) return;
 #pragma unroll
   for (int i = 0; i < 3; i++) b.x[3 * u + i] = b.pinTarget[3 * u + i];
+}
+
+// Newmark: every active scene starts its Newton loop (one CTA over scenes);
+// other integrators and parked scenes count as finished.
+__global__ void __launch_bounds__(256) k_newton_begin(DeviceBatch b) {
+  __shared__ int total;
+  if (threadIdx.x == 0) total = 0;
+  __syncthreads();
+  int n = 0;
+  for (int s = threadIdx.x; s < b.nscenes; s += blockDim.x) {
+    SolveState& st = b.solve[s];
+    const bool run = b.scenes[s].active && b.scenes[s].integrator == kIntegratorNewmark;
+    st.newtonStep = 0;
+    st.newtonDone = run ? 0 : 1;
+    n += run ? 1 : 0;
+  }
+  atomicAdd(&total, n);
+  __syncthreads();
+  if (threadIdx.x == 0) *b.newtonActive = total;
+}
+
+// Newmark, after a solve: x -= y for the scenes still iterating.
+__global__ void k_newton_step(DeviceBatch b) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= b.nv || b.solve[b.vertexScene[u]].newtonDone) return;
+#pragma unroll
+  for (int i = 0; i < 3; i++) b.x[3 * u + i] -= b.y[3 * u + i];
+}
+
+// ... then each scene's Newton test: stop once the iteration just done
+// started from |rhs|^2 <= eps, or after maxNewton iterations
+// (NEWMARK.cpp:216: while step < max && maxR > eps).
+__global__ void __launch_bounds__(256) k_newton_test(DeviceBatch b) {
+  int finished = 0;
+  for (int s = threadIdx.x; s < b.nscenes; s += blockDim.x) {
+    SolveState& st = b.solve[s];
+    if (st.newtonDone) continue;
+    st.newtonStep += 1;
+    const SceneParams& sp = b.scenes[s];
+    if (!(st.newtonR > sp.newtonEps) || st.newtonStep >= sp.maxNewton) {
+      st.newtonDone = 1;
+      finished++;
+    }
+  }
+  if (finished) atomicSub(b.newtonActive, finished);
+}
+
+// Graph loop control of the Newton loop.
+__global__ void k_newton_continue(const int* newtonActive, unsigned long long* runs, cudaGraphConditionalHandle h) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    *runs += 1ull;
+    cudaGraphSetConditional(h, *newtonActive > 0 ? 1u : 0u);
+  }
 }
 
 // Sum of one block entry over its element contributions, ascending tet
@@ -271,6 +334,10 @@ __global__ void k_assemble_entry(DeviceBatch b, const HT* __restrict__ elemH, T*
     const double invDt = 1.0 / dt;
     val = (fu && fw) ? HT(-(sp.rayBeta * invDt)) * HT(b.K0[9 * (size_t)blk + rr + 3 * c]) - sum : HT(0);
     if (u == w && rr == c) val += fu ? HT(b.mass[u] * (invDt * invDt - sp.rayAlpha * invDt)) : HT(1);
+  } else if (sp.integrator == kIntegratorNewmark) {
+    // A = alpha_0 M - K (NEWMARK.cpp:262; its C is zeroed before use)
+    val = (fu && fw) ? -sum : HT(0);
+    if (u == w && rr == c) val += fu ? HT(sp.nm[0] * b.mass[u]) : HT(1);
   } else {
     val = (fu && fw) ? HT(-(dt * dt)) * sum : HT(0);
     if (u == w && rr == c) val += fu ? HT(b.mass[u]) : HT(1);
@@ -337,6 +404,15 @@ __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __res
 #pragma unroll
         for (int e = 0; e < 9; e++) {
           HT val = (fu && fw) ? cK0 * HT(K0[(e / 3) + 3 * (e % 3)]) - sum[e] : HT(0);
+          if (u == w && e % 4 == 0) val += m;
+          out[kSlice * e] = T(val);
+        }
+      } else if (sp.integrator == kIntegratorNewmark) {
+        // A = alpha_0 M - K (NEWMARK.cpp:262; its C is zeroed before use)
+        const HT m = fu ? HT(sp.nm[0] * b.mass[u]) : HT(1);
+#pragma unroll
+        for (int e = 0; e < 9; e++) {
+          HT val = (fu && fw) ? -sum[e] : HT(0);
           if (u == w && e % 4 == 0) val += m;
           out[kSlice * e] = T(val);
         }
@@ -433,6 +509,14 @@ __global__ void __launch_bounds__(TV) k_rhs(DeviceBatch b) {
     }
     return;
   }
+  if (b.solve[s].newtonDone) {  // Newmark: this scene's Newton loop is over
+    const int u = b.tileV0[tile] + threadIdx.x;
+    if (u < b.tileV1[tile])
+#pragma unroll
+      for (int i = 0; i < 3; i++) b.y[3 * u + i] = 0.0;
+    if (tile == b.scenes[s].tile0 && threadIdx.x == 0) b.solve[s].outerDone = 1;
+    return;
+  }
   const int u = b.tileV0[tile] + threadIdx.x;
   double rr = 0;
   if (u < b.tileV1[tile]) {
@@ -484,6 +568,16 @@ __global__ void __launch_bounds__(TV) k_rhs(DeviceBatch b) {
 #pragma unroll
       for (int i = 0; i < 3; i++)
         bi[i] = (invDt - sp.rayAlpha) * m * b.v[3 * u + i] - sp.rayBeta * k0v[i] + acc[i] + b.fext[3 * u + i];
+    } else if (b.scenes[s].integrator == kIntegratorNewmark) {
+      // b = M (a0 (x - x_old) - a2 a_old - a1 v_old) - R - f_ext (NEWMARK.cpp:244-255; C = 0)
+      const double* nm = b.scenes[s].nm;
+      const double m = b.mass[u];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const size_t q = 3 * (size_t)u + i;
+        const double t = m * (nm[0] * (b.x[q] - b.xOld[q]) - nm[2] * b.aOld[q] - nm[1] * b.vOld[q]);
+        bi[i] = t - acc[i] - b.fext[q];
+      }
     } else {
       // b = dt (R + dt K v + f_ext); acc holds dt (R + dt K v)
 #pragma unroll
@@ -506,6 +600,7 @@ __global__ void __launch_bounds__(TV) k_rhs(DeviceBatch b) {
   const double srr = sum_partials<TV>(b.partial, sp.tile0, sp.ntiles, 0, sh);
   if (threadIdx.x == 0) {
     st.rhsNorm2 = srr;
+    st.newtonR = srr;  // Newmark's maxR = |rhs|^2 (NEWMARK.cpp:275)
     st.threshold = fmax(st.tol * st.tol * srr, DBL_MIN);
     st.rr64 = srr;
     st.sweep = 0;
@@ -1080,6 +1175,21 @@ __global__ void k_finish_step(DeviceBatch b) {
     }
     return;
   }
+  if (sp.integrator == kIntegratorNewmark) {
+    // v = a3 dx + a4 v_old + a5 a_old, a = a0 dx - a1 v_old - a2 a_old, S
+    // (NEWMARK.cpp:321-333); x itself was updated by the Newton loop
+    const double* nm = sp.nm;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const size_t q = 3 * (size_t)u + i;
+      const double dx = b.x[q] - b.xOld[q];
+      const double vn = nm[3] * dx + nm[4] * b.vOld[q] + nm[5] * b.aOld[q];
+      const double an = nm[0] * dx - nm[1] * b.vOld[q] - nm[2] * b.aOld[q];
+      b.v[q] = fu ? vn : 0.0;
+      b.acc[q] = fu ? an : 0.0;
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     const double vn = b.v[3 * u + i] + b.y[3 * u + i];
@@ -1190,6 +1300,25 @@ void launch_refine(const DeviceBatch& b, cudaStream_t s) {
 void launch_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s) {
   k_continue<<<1, 32, 0, s>>>(b.active, b.bodyRuns, (cudaGraphConditionalHandle)handle);
 }
+void launch_newton_begin(const DeviceBatch& b, cudaStream_t s) { k_newton_begin<<<1, 256, 0, s>>>(b); }
+
+void launch_newton_update(const DeviceBatch& b, cudaStream_t s) {
+  k_newton_step<<<(b.nv + 255) / 256, 256, 0, s>>>(b);
+  k_newton_test<<<1, 256, 0, s>>>(b);
+}
+
+__global__ void k_set_condition(cudaGraphConditionalHandle h, unsigned value) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, value);
+}
+
+void launch_set_condition(unsigned long long handle, unsigned value, cudaStream_t s) {
+  k_set_condition<<<1, 32, 0, s>>>((cudaGraphConditionalHandle)handle, value);
+}
+
+void launch_newton_continue(const DeviceBatch& b, unsigned long long handle, cudaStream_t s) {
+  k_newton_continue<<<1, 32, 0, s>>>(b.newtonActive, b.newtonRuns, (cudaGraphConditionalHandle)handle);
+}
+
 void launch_finish_step(const DeviceBatch& b, cudaStream_t s) {
   k_finish_step<<<(b.nv + 255) / 256, 256, 0, s>>>(b);
 }

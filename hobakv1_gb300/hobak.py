@@ -31,6 +31,7 @@ PRECOND_JACOBI = 0
 PRECOND_BLOCK_JACOBI = 1
 INTEGRATOR_VELOCITY = 0   # BACKWARD_EULER_VELOCITY::solve
 INTEGRATOR_POSITION = 1   # BACKWARD_EULER_POSITION::solveRayleighDamped
+INTEGRATOR_NEWMARK = 2    # NEWMARK::solveRayleighDamped (Newton loop)
 
 
 def _colmajor(F: np.ndarray) -> np.ndarray:
@@ -183,15 +184,17 @@ class TET_MESH:
 
 def solver_opts(tol=1e-8, max_iters=1000, precision=PRECISION_FP64, preconditioner=PRECOND_BLOCK_JACOBI,
                 max_refinements=3, use_graph=True, integrator=INTEGRATOR_VELOCITY,
-                rayleigh=(0.01, 0.01)) -> HobakSolverOpts:
-    """Solver options; integrator INTEGRATOR_VELOCITY (BACKWARD_EULER_VELOCITY)
-    or INTEGRATOR_POSITION (BACKWARD_EULER_POSITION, Rayleigh damped with
-    alpha, beta = rayleigh)."""
+                rayleigh=(0.01, 0.01), max_newton=10, newton_tolerance=1e-7) -> HobakSolverOpts:
+    """Solver options; integrator INTEGRATOR_VELOCITY (BACKWARD_EULER_VELOCITY),
+    INTEGRATOR_POSITION (BACKWARD_EULER_POSITION, Rayleigh damped with
+    alpha, beta = rayleigh) or INTEGRATOR_NEWMARK (NEWMARK, at most
+    max_newton Newton iterations until |rhs|^2 <= newton_tolerance)."""
     o = HobakSolverOpts()
     o.tol, o.max_iters, o.precision = tol, max_iters, precision
     o.preconditioner, o.max_refinements, o.use_graph = preconditioner, max_refinements, int(use_graph)
     o.integrator = integrator
     o.rayleigh_alpha, o.rayleigh_beta = rayleigh
+    o.max_newton, o.newton_tolerance = max_newton, newton_tolerance
     return o
 
 
@@ -277,6 +280,16 @@ class BATCH:
         v = np.empty(n) if v is None else v
         check(_lib.load().hobak_batch_get_state_all(self.h, dptr(x), dptr(v)), "hobak_batch_get_state_all")
         return x, v
+
+    def get_acceleration(self, scene: int) -> np.ndarray:
+        """NEWMARK's acceleration state of one scene (3*nv)."""
+        a = np.empty(3 * self.nv[scene])
+        check(_lib.load().hobak_batch_get_acceleration(self.h, scene, dptr(a)), "hobak_batch_get_acceleration")
+        return a
+
+    def set_acceleration(self, scene: int, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        check(_lib.load().hobak_batch_set_acceleration(self.h, scene, dptr(a)), "hobak_batch_set_acceleration")
 
     def query(self) -> bool:
         """True when the batch's enqueued steps have finished (non-blocking)."""
@@ -595,3 +608,39 @@ class BACKWARD_EULER_POSITION(BACKWARD_EULER_VELOCITY):
         if on:
             raise ValueError("vertex-face contact needs BACKWARD_EULER_VELOCITY")
         super().setVertexFaceSelfCollisionsOn(False)
+
+
+class NEWMARK(BACKWARD_EULER_VELOCITY):
+    """GPU drop-in for TIMESTEPPER::NEWMARK (Rayleigh-damped solve,
+    NEWMARK.cpp:183-340: a Newton loop of at most maxNewtonIterations() solves,
+    beta = 1/4, gamma = 1/2).  position(), velocity() and acceleration() are
+    host state that solve() uploads and downloads.  Vertex-face contact is not
+    available with this integrator."""
+
+    def __init__(self, tetMesh: TET_MESH, hyperelastic: HYPERELASTIC, opts: Optional[HobakSolverOpts] = None):
+        super().__init__(tetMesh, hyperelastic, None if opts is None else HobakSolverOpts.from_buffer_copy(opts))
+        self._opts.integrator = INTEGRATOR_NEWMARK
+        self._acceleration = np.zeros(tetMesh.DOFs())
+
+    def acceleration(self):
+        return self._acceleration
+
+    def maxNewtonIterations(self) -> int:
+        return self._opts.max_newton
+
+    def setMaxNewtonIterations(self, n: int):
+        self._require_unbuilt("setMaxNewtonIterations")
+        self._opts.max_newton = int(n)
+
+    def setVertexFaceSelfCollisionsOn(self, on: bool):
+        if on:
+            raise ValueError("vertex-face contact needs BACKWARD_EULER_VELOCITY")
+        super().setVertexFaceSelfCollisionsOn(False)
+
+    def solve(self, verbose: bool = False) -> bool:
+        if self._batch is None:
+            self._build()
+        self._batch.set_acceleration(0, self._acceleration)
+        ok = super().solve(verbose)
+        self._acceleration[:] = self._batch.get_acceleration(0)
+        return ok

@@ -52,6 +52,7 @@ extern "C" {
 /* ---- preconditioners ---- */
 #define HOBAK_INTEGRATOR_VELOCITY 0   /* BACKWARD_EULER_VELOCITY::solve (BACKWARD_EULER_VELOCITY.cpp:96-235) */
 #define HOBAK_INTEGRATOR_POSITION 1   /* BACKWARD_EULER_POSITION::solveRayleighDamped (BACKWARD_EULER_POSITION.cpp:138-330) */
+#define HOBAK_INTEGRATOR_NEWMARK 2    /* NEWMARK::solveRayleighDamped (NEWMARK.cpp:183-340): a Newton loop */
 
 #define HOBAK_PRECOND_JACOBI 0        /* scalar 1/diag, Eigen DiagonalPreconditioner */
 #define HOBAK_PRECOND_BLOCK_JACOBI 1  /* inverse of each 3x3 diagonal block */
@@ -93,6 +94,8 @@ typedef struct hobak_solver_opts {
   int integrator;          /* HOBAK_INTEGRATOR_* (default VELOCITY) */
   double rayleigh_alpha;   /* POSITION: C = alpha M + beta K(rest) (defaults 0.01, 0.01: */
   double rayleigh_beta;    /*   BACKWARD_EULER_POSITION.cpp:53-54); vertex-face contact needs VELOCITY */
+  int max_newton;          /* NEWMARK: Newton iterations per step at most (default 10) */
+  double newton_tolerance; /* NEWMARK: stop once |rhs|^2 <= this (default 1e-7, NEWMARK.cpp:43) */
 } hobak_solver_opts;
 
 /* Per-scene statistics of the last step. */
@@ -141,6 +144,10 @@ int hobak_batch_set_active(hobak_batch b, int scene, int active);
 /* Host <-> device state of one scene (3*nv doubles each; NULL skips). */
 int hobak_batch_set_state(hobak_batch b, int scene, const double* x, const double* v);
 int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v);
+/* NEWMARK's acceleration state of one scene (3*nv, zero at creation; the
+ * other integrators leave it untouched). */
+int hobak_batch_get_acceleration(hobak_batch b, int scene, double* a);
+int hobak_batch_set_acceleration(hobak_batch b, int scene, const double* a);
 /* Whole batch at once: every scene's 3*nv values back to back in scene
  * order (total 3 * sum(nv)); one copy each.  The set calls are enqueued on
  * the batch's stream and return at once: host buffers must stay unchanged

@@ -1583,6 +1583,14 @@ int oracle_assemble(void* h, int* rowptr, int* cols, double* K, double* R) {
 
 int oracle_newton_iterations(void* h) { return static_cast<Sim*>(h)->lastNewton; }
 
+// NEWMARK's acceleration state (zero before the first NEWMARK step).
+int oracle_get_acceleration(void* h, double* a) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s || !a) return -1;
+  for (size_t k = 0; k < s->x.size(); k++) a[k] = s->acc.size() == s->x.size() ? s->acc[k] : 0.0;
+  return 0;
+}
+
 double oracle_energy(void* h) {
   Sim* s = static_cast<Sim*>(h);
   double e = 0;

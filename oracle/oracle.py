@@ -57,6 +57,7 @@ def lib():
         L.oracle_vf_response.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
         L.oracle_set_integrator.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.oracle_newton_iterations.argtypes = [ctypes.c_void_p]
+        L.oracle_get_acceleration.argtypes = [ctypes.c_void_p, _dp]
         L.oracle_energy.argtypes = [ctypes.c_void_p]
         L.oracle_energy.restype = ctypes.c_double
         _lib = L
@@ -149,6 +150,15 @@ class Sim:
         errs = np.zeros(n)
         assert lib().oracle_step(self.h, n, _i(iters), _d(errs)) == 0
         return iters, errs
+
+    def acceleration(self):
+        a = np.zeros(3 * self.scene.nv)
+        lib().oracle_get_acceleration(self.h, _d(a))
+        return a
+
+    def newton_iterations(self) -> int:
+        """Newton iterations of the last NEWMARK step."""
+        return lib().oracle_newton_iterations(self.h)
 
     def state(self):
         x = np.zeros(3 * self.scene.nv)

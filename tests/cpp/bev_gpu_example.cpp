@@ -4,8 +4,8 @@
 // solve, read position().  Reads a mesh and state from raw binary files and
 // writes the final displacement, so a test can compare it with the oracle.
 //
-//   bev_gpu_example <in.bin> <out.bin> <steps> [position]
-// ("position" drives BACKWARD_EULER_POSITION the same way)
+//   bev_gpu_example <in.bin> <out.bin> <steps> [position|newmark]
+// ("position" / "newmark" drive BACKWARD_EULER_POSITION / NEWMARK the same way)
 // in.bin: int nv, int nt, int npinned, int material, double mu, lambda,
 //         density, dt, rest[3nv], tets[4nt] (int), pinned[npinned] (int), x0[3nv]
 #include <cstdio>
@@ -73,5 +73,7 @@ int main(int argc, char** argv) {
   const int steps = std::atoi(argv[3]);
   if (argc == 5 && std::string(argv[4]) == "position")
     return run<TIMESTEPPER::BACKWARD_EULER_POSITION>(mesh, material, prm, x0, pinned, steps, argv[2]);
+  if (argc == 5 && std::string(argv[4]) == "newmark")
+    return run<TIMESTEPPER::NEWMARK>(mesh, material, prm, x0, pinned, steps, argv[2]);
   return run<TIMESTEPPER::BACKWARD_EULER_VELOCITY>(mesh, material, prm, x0, pinned, steps, argv[2]);
 }

@@ -39,8 +39,8 @@ def test_cpp_mirror_solve_matches_oracle(tmp_path):
         s.tets.astype(np.int32).tofile(f)
         s.pinned.astype(np.int32).tofile(f)
         s.x0.astype(np.float64).tofile(f)
-    for integrator in ("velocity", "position"):
-        subprocess.run([exe, str(inp), str(out), "10"] + ([integrator] if integrator == "position" else []),
+    for integrator in ("velocity", "position", "newmark"):
+        subprocess.run([exe, str(inp), str(out), "10"] + ([integrator] if integrator != "velocity" else []),
                        check=True)
         xv = np.fromfile(out, dtype=np.float64)
         x, v = xv[:3 * s.nv], xv[3 * s.nv:]
