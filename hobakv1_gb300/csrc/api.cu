@@ -1720,6 +1720,7 @@ int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
     for (auto& x : st) {
       x.done = 0;
       x.outerDone = 0;
+      x.newtonDone = 0;
       x.innerThreshold = -1.0;
       x.maxit = 0x7fffffff;
       x.totalIters = 0;
@@ -1727,6 +1728,7 @@ int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
     CUDA_TRY(cudaMemcpy(d.solve, st.data(), sizeof(SolveState) * n, cudaMemcpyHostToDevice));
     return HOBAK_OK;
   };
+  if (int rc = keep_running()) return rc;  // (Newmark: no scene counts as finished)
   for (int k = 0; k < 4; k++) {
     if (k == 2) {
       std::vector<SceneParams> sp = b->sceneParams;
@@ -1838,14 +1840,17 @@ int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out) {
   const size_t vbytes = 3 * sizeof(double) * (size_t)b->nv;
   CUDA_TRY(cudaStreamSynchronize(s));
   DeviceScratch saved;
-  CUDA_TRY(cudaMalloc(&saved.p, 2 * vbytes));
+  CUDA_TRY(cudaMalloc(&saved.p, 3 * vbytes));
   double* x0 = static_cast<double*>(saved.p);
   double* v0 = x0 + 3 * (size_t)b->nv;
+  double* a0 = v0 + 3 * (size_t)b->nv;  // Newmark's acceleration
   CUDA_TRY(cudaMemcpyAsync(x0, d.x, vbytes, cudaMemcpyDeviceToDevice, s));
   CUDA_TRY(cudaMemcpyAsync(v0, d.v, vbytes, cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(a0, d.acc, vbytes, cudaMemcpyDeviceToDevice, s));
   auto restore = [&]() -> int {
     CUDA_TRY(cudaMemcpyAsync(d.x, x0, vbytes, cudaMemcpyDeviceToDevice, s));
     CUDA_TRY(cudaMemcpyAsync(d.v, v0, vbytes, cudaMemcpyDeviceToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.acc, a0, vbytes, cudaMemcpyDeviceToDevice, s));
     return HOBAK_OK;
   };
   EventPair ev;

@@ -207,6 +207,8 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   if (t >= b.nt) return;
   const SceneParams& sp = b.scenes[b.tetScene[t]];
   if (!sp.active) return;
+  // Newmark: a scene whose Newton loop is over needs no further element terms
+  if (!rawForces && sp.integrator == kIntegratorNewmark && b.solve[b.tetScene[t]].newtonDone) return;
   const int4 tv = b.tets[t];
   const MatParams m{sp.kind, sp.mu, sp.lambda, sp.alpha};
   // rhs term: dt (f + dt He v) for BACKWARD_EULER_VELOCITY; the force itself

@@ -321,7 +321,7 @@ __global__ void k_assemble_entry(DeviceBatch b, const HT* __restrict__ elemH, T*
   const int lane = rem / 9, e = rem % 9;
   int u, blk;
   if (!slot_block(b, r, lane, u, blk)) return;
-  if (!b.scenes[b.vertexScene[u]].active) return;
+  if (!b.scenes[b.vertexScene[u]].active || b.solve[b.vertexScene[u]].newtonDone) return;
   const int rr = e / 3, c = e % 3;
   const HT sum = gather_block_entry(b, elemH, blk, rr, c);
   const int w = b.cols[blk];
@@ -360,7 +360,7 @@ __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __res
   int u, blk;
   if (slot_block(b, r, lane, u, blk)) {
     const SceneParams& sp = b.scenes[b.vertexScene[u]];
-    if (sp.active) {
+    if (sp.active && !b.solve[b.vertexScene[u]].newtonDone) {
       HT sum[9];
 #pragma unroll
       for (int e = 0; e < 9; e++) sum[e] = HT(0);
@@ -455,7 +455,7 @@ __global__ void k_assemble_raw(DeviceBatch b, double* K, double* R) {
 template <typename T>
 __global__ void k_diag_inverse(DeviceBatch b, const T* __restrict__ lhs, T* __restrict__ minv, int precond) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= b.nv || !b.scenes[b.vertexScene[u]].active) return;
+  if (u >= b.nv || !b.scenes[b.vertexScene[u]].active || b.solve[b.vertexScene[u]].newtonDone) return;
   int k = b.rowptr[u];
   while (b.cols[k] != u) k++;
   const T* Lu = lhs + lhs_slot(b, u, k - b.rowptr[u]);
