@@ -91,6 +91,10 @@ SIGNATURES = {
     "hobak_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakTuning)]),
     "hobak_batch_get_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "hobak_batch_set_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "hobak_batch_set_pin_targets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "hobak_batch_snapshot_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
+    "hobak_batch_snapshot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "hobak_batch_restore": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "hobak_batch_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakTuning)]),
     "hobak_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(HobakTuning)]),
     "hobak_batch_set_collisions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,

@@ -15,8 +15,11 @@
 // lastError() says why.
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cmath>
+#include <functional>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -111,6 +114,24 @@ class TET_MESH {
   const std::vector<REAL>& restOneRingVolumes() const { return _oneRing; }
   int totalVertices() const { return (int)_rest.size(); }
   int DOFs() const { return 3 * (int)_rest.size(); }
+  // vertices of the faces that belong to one tet only, ascending
+  // (TET_MESH::computeSurfaceVertices, TET_MESH.cpp:567-590)
+  std::vector<int> surfaceVertices() const {
+    std::map<std::array<int, 3>, int> faces;
+    static const int kFace[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+    for (const auto& t : _tets)
+      for (const auto& f : kFace) {
+        std::array<int, 3> k = {t[f[0]], t[f[1]], t[f[2]]};
+        std::sort(k.begin(), k.end());
+        faces[k]++;
+      }
+    std::vector<int> out;
+    for (const auto& kv : faces)
+      if (kv.second == 1) out.insert(out.end(), kv.first.begin(), kv.first.end());
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+    return out;
+  }
   void setDisplacement(const VECTOR& delta) { _displacement = delta; }
   VECTOR getDisplacement() const { return _displacement; }
 
@@ -169,14 +190,19 @@ class BACKWARD_EULER_VELOCITY {
   }
   // Pin vertices at their current positions (TIMESTEPPER.cpp:380-403); any
   // shape type with bool inside(const VECTOR3&) works, as does a list of ids.
+  // A shape that also has VECTOR3 worldVertexToLocal(const VECTOR3&) and
+  // localVertexToWorld(const VECTOR3&) (KINEMATIC_SHAPE.h:55-69) carries its
+  // pins along when it moves between solves.
   template <typename SHAPE>
   void attachKinematicConstraints(const SHAPE* shape) {
-    const auto& rest = _tetMesh.restVertices();
-    for (size_t x = 0; x < rest.size(); x++) {
-      const VECTOR3 p = {rest[x][0] + _position[3 * x], rest[x][1] + _position[3 * x + 1],
-                         rest[x][2] + _position[3 * x + 2]};
-      if (shape->inside(p)) _pinned.push_back((int)x);
-    }
+    std::vector<int> all(_tetMesh.totalVertices());
+    for (size_t x = 0; x < all.size(); x++) all[x] = (int)x;
+    attachShape(shape, all, 0);
+  }
+  // The surface vertices inside the shape (TIMESTEPPER.cpp:350-375).
+  template <typename SHAPE>
+  void attachKinematicSurfaceConstraints(const SHAPE* shape) {
+    attachShape(shape, _tetMesh.surfaceVertices(), 0);
   }
   void attachKinematicConstraints(const std::vector<int>& vertexIDs) {
     _pinned.insert(_pinned.end(), vertexIDs.begin(), vertexIDs.end());
@@ -186,7 +212,7 @@ class BACKWARD_EULER_VELOCITY {
   bool solve(const bool verbose) {
     if (!_handle && !build()) return false;
     if (hobak_gpu_set_state(_handle, _position.data(), _velocity.data()) != HOBAK_OK ||
-        hobak_batch_set_external_forces(_handle, 0, _externalForces.data()) != HOBAK_OK)
+        hobak_batch_set_external_forces(_handle, 0, _externalForces.data()) != HOBAK_OK || !pushPinTargets())
       return fail();
     const int rc = hobak_gpu_step(_handle, 1, &_stats);
     if (rc < 0) return fail();
@@ -202,6 +228,43 @@ class BACKWARD_EULER_VELOCITY {
   int currentTimestep() const { return _currentTimestep; }
 
  protected:
+  template <typename SHAPE>
+  auto attachShape(const SHAPE* shape, const std::vector<int>& candidates, int)
+      -> decltype(shape->worldVertexToLocal(VECTOR3{}), shape->localVertexToWorld(VECTOR3{}), void()) {
+    const auto& rest = _tetMesh.restVertices();
+    for (int x : candidates) {
+      const VECTOR3 p = {rest[x][0] + _position[3 * x], rest[x][1] + _position[3 * x + 1],
+                         rest[x][2] + _position[3 * x + 2]};
+      if (!shape->inside(p)) continue;
+      _pinned.push_back(x);
+      const VECTOR3 local = shape->worldVertexToLocal(p);
+      // later constraints on a vertex override earlier ones (TIMESTEPPER.cpp:105-122)
+      _shapePins[x] = [shape, local]() { return shape->localVertexToWorld(local); };
+    }
+  }
+  template <typename SHAPE>
+  void attachShape(const SHAPE* shape, const std::vector<int>& candidates, long) {
+    const auto& rest = _tetMesh.restVertices();
+    for (int x : candidates) {
+      const VECTOR3 p = {rest[x][0] + _position[3 * x], rest[x][1] + _position[3 * x + 1],
+                         rest[x][2] + _position[3 * x + 2]};
+      if (shape->inside(p)) _pinned.push_back(x);
+    }
+  }
+  // applyKinematicConstraints (TIMESTEPPER.cpp:105-122): each shape-held
+  // pin's target displacement from the shape's current transform
+  bool pushPinTargets() {
+    if (_shapePins.empty()) return true;
+    const auto& rest = _tetMesh.restVertices();
+    std::vector<REAL> t(3 * _pinned.size());
+    for (size_t k = 0; k < _pinned.size(); k++) {
+      const int u = _pinned[k];
+      auto it = _shapePins.find(u);
+      for (int i = 0; i < 3; i++)
+        t[3 * k + i] = it != _shapePins.end() ? it->second()[i] - rest[u][i] : _pinnedAt[3 * k + i];
+    }
+    return hobak_batch_set_pin_targets(_handle, 0, t.data()) == HOBAK_OK;
+  }
   bool build() {
     const auto& rest = _tetMesh.restVertices();
     const auto& tets = _tetMesh.tets();
@@ -222,6 +285,9 @@ class BACKWARD_EULER_VELOCITY {
     d.dt = _dt;
     d.npinned = (int)_pinned.size();
     d.pinned = _pinned.empty() ? nullptr : _pinned.data();
+    _pinnedAt.resize(3 * _pinned.size());
+    for (size_t k = 0; k < _pinned.size(); k++)
+      for (int i = 0; i < 3; i++) _pinnedAt[3 * k + i] = _position[3 * (size_t)_pinned[k] + i];
     d.x0 = _position.data();
     d.v0 = _velocity.data();
     if (hobak_gpu_create(&d, &_opts, &_handle) != HOBAK_OK) {
@@ -239,6 +305,8 @@ class BACKWARD_EULER_VELOCITY {
   VOLUME::HYPERELASTIC& _hyperelastic;
   VECTOR _position, _velocity, _externalForces;
   std::vector<int> _pinned;
+  std::map<int, std::function<VECTOR3()>> _shapePins;  // pins that follow a shape
+  std::vector<REAL> _pinnedAt;                         // pin displacements when built
   REAL _dt = 1.0 / 60.0;  // BACKWARD_EULER_VELOCITY.cpp:37
   REAL _massScale = 1.0;
   REAL _time = 0.0;

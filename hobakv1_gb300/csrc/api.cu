@@ -63,6 +63,7 @@ struct SceneHost {
   hobak_material mat;
   double density, dt;
   double gravity[3];
+  std::vector<int> pinned;  // global vertex ids, in the order the scene gave them
 };
 
 }  // namespace
@@ -108,6 +109,7 @@ struct hobak_batch_t {
   SolveState* solvePinned = nullptr;      // pinned landing buffer for per-step stats
   bool pending = false;                   // steps enqueued, stats not collected yet
   std::vector<double> restHost;  // rest positions (surface areas for collisions)
+  std::vector<double> pinTargetHost;  // host copy of the pin targets (3 per vertex)
   // vertex-face collisions
   std::vector<CollisionScene> collScenes;
   std::vector<int> surfTri, surfTriStart, svHost, svStart;  // global ids; per-scene ranges
@@ -374,6 +376,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     // pins keep the displacement they have when attached: (rest + x) - rest
     for (int k = 0; k < D.npinned; k++) {
       const int u = v0 + D.pinned[k];
+      B->scenes[s].pinned.push_back(u);
       B->freeMask[u] = 0;
       for (int i = 0; i < 3; i++) {
         const double world = rest[3 * (size_t)u + i] + x[3 * (size_t)u + i];
@@ -598,6 +601,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   CUDA_TRY(up(d.mass, mass.data(), sizeof(double) * nv));
   CUDA_TRY(up(d.freeMask, B->freeMask.data(), nv));
   CUDA_TRY(up(d.pinTarget, pinTarget.data(), V3));
+  B->pinTargetHost = pinTarget;
   CUDA_TRY(up(d.vertexScene, vertexScene.data(), sizeof(int) * nv));
   CUDA_TRY(up(d.tets, B->tetsHost.data(), sizeof(int4) * nt));
   CUDA_TRY(up(d.DmInv, DmInv.data(), sizeof(double) * 9 * (size_t)nt));
@@ -1479,6 +1483,108 @@ int hobak_batch_set_acceleration(hobak_batch b, int scene, const double* a) {
   CUDA_TRY(cudaMemcpyAsync(b->d.acc + 3 * (size_t)H.v0, a, 3 * sizeof(double) * H.nv, cudaMemcpyHostToDevice,
                            b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_pin_targets(hobak_batch b, int scene, const double* targets) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  const SceneHost& H = b->scenes[scene];
+  if (H.pinned.empty()) return HOBAK_OK;
+  if (!targets) return fail(HOBAK_ERR_INVALID, "null targets");
+  for (size_t k = 0; k < H.pinned.size(); k++)
+    for (int i = 0; i < 3; i++) {
+      const double t = targets[3 * k + i];
+      if (!std::isfinite(t)) return fail(HOBAK_ERR_INVALID, "non-finite pin target");
+      b->pinTargetHost[3 * (size_t)H.pinned[k] + i] = t;
+    }
+  // the scene's range in one copy; the step graph reads the targets from HBM
+  const size_t q0 = 3 * (size_t)H.v0;
+  CUDA_TRY(cudaMemcpyAsync(const_cast<double*>(b->d.pinTarget) + q0, b->pinTargetHost.data() + q0,
+                           3 * sizeof(double) * H.nv, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+// Snapshot layout: a 64-byte header, then x, v, acceleration, external
+// forces and pin targets (3 * total vertices doubles each, scenes back to
+// back) and one active byte per scene.
+namespace {
+constexpr unsigned kSnapshotMagic = 0x534b4248u;  // "HBKS"
+constexpr int kSnapshotVersion = 1;
+constexpr int kSnapshotArrays = 5;
+struct SnapshotHeader {
+  unsigned magic;
+  int version, nscenes, nv;
+  unsigned long long vertexHash;  // FNV-1a over the per-scene vertex counts
+  unsigned char pad[40];
+};
+static_assert(sizeof(SnapshotHeader) == 64, "snapshot header is 64 bytes");
+
+unsigned long long scene_shape_hash(const hobak_batch_t* b) {
+  unsigned long long h = 1469598103934665603ull;
+  for (const SceneHost& H : b->scenes) {
+    h ^= (unsigned long long)(unsigned)H.nv;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+size_t snapshot_bytes(const hobak_batch_t* b) {
+  return sizeof(SnapshotHeader) + kSnapshotArrays * 3 * sizeof(double) * (size_t)b->nv + b->scenes.size();
+}
+}  // namespace
+
+int hobak_batch_snapshot_bytes(hobak_batch b, size_t* bytes) {
+  if (!b || !bytes) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  *bytes = snapshot_bytes(b);
+  return HOBAK_OK;
+}
+
+int hobak_batch_snapshot(hobak_batch b, void* dst, size_t bytes) {
+  if (!b || !dst) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  if (bytes < snapshot_bytes(b)) return fail(HOBAK_ERR_INVALID, "snapshot buffer too small");
+  SnapshotHeader h{};
+  h.magic = kSnapshotMagic;
+  h.version = kSnapshotVersion;
+  h.nscenes = (int)b->scenes.size();
+  h.nv = b->nv;
+  h.vertexHash = scene_shape_hash(b);
+  std::vector<unsigned char> active(b->scenes.size());
+  for (size_t i = 0; i < active.size(); i++) active[i] = b->sceneParams[i].active ? 1 : 0;
+  const size_t V3 = 3 * sizeof(double) * (size_t)b->nv;
+  unsigned char* p = static_cast<unsigned char*>(dst);
+  // cudaMemcpyDefault: dst may be host (pageable or pinned) or device memory
+  CUDA_TRY(cudaMemcpyAsync(p, &h, sizeof(h), cudaMemcpyDefault, b->stream));
+  p += sizeof(h);
+  const double* src[kSnapshotArrays] = {b->d.x, b->d.v, b->d.acc, b->d.fext, b->d.pinTarget};
+  for (int k = 0; k < kSnapshotArrays; k++, p += V3)
+    CUDA_TRY(cudaMemcpyAsync(p, src[k], V3, cudaMemcpyDefault, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(p, active.data(), active.size(), cudaMemcpyDefault, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return HOBAK_OK;
+}
+
+int hobak_batch_restore(hobak_batch b, const void* src, size_t bytes) {
+  if (!b || !src) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  if (bytes < snapshot_bytes(b)) return fail(HOBAK_ERR_INVALID, "snapshot too small for this batch");
+  SnapshotHeader h{};
+  CUDA_TRY(cudaMemcpy(&h, src, sizeof(h), cudaMemcpyDefault));
+  if (h.magic != kSnapshotMagic || h.version != kSnapshotVersion) return fail(HOBAK_ERR_INVALID, "not a snapshot");
+  if (h.nscenes != (int)b->scenes.size() || h.nv != b->nv || h.vertexHash != scene_shape_hash(b))
+    return fail(HOBAK_ERR_INVALID, "snapshot of a batch with other scenes");
+  const size_t V3 = 3 * sizeof(double) * (size_t)b->nv;
+  const unsigned char* p = static_cast<const unsigned char*>(src) + sizeof(h);
+  double* dstArr[kSnapshotArrays] = {b->d.x, b->d.v, b->d.acc, const_cast<double*>(b->d.fext),
+                                     const_cast<double*>(b->d.pinTarget)};
+  for (int k = 0; k < kSnapshotArrays; k++, p += V3)
+    CUDA_TRY(cudaMemcpyAsync(dstArr[k], p, V3, cudaMemcpyDefault, b->stream));
+  std::vector<unsigned char> active(b->scenes.size());
+  CUDA_TRY(cudaMemcpyAsync(active.data(), p, active.size(), cudaMemcpyDefault, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(b->pinTargetHost.data(), b->d.pinTarget, V3, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (size_t i = 0; i < active.size(); i++)
+    if ((b->sceneParams[i].active != 0) != (active[i] != 0))
+      if (int rc = hobak_batch_set_active(b, (int)i, active[i])) return rc;
   return HOBAK_OK;
 }
 

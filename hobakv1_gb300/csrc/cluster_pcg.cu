@@ -178,13 +178,15 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
   const int nmine = my1 - my0;
 
   // ---- init: r = rhs - A y (FP64, converted), u = Minv r, d = p = s = 0 ----
+  const double rsc = (sizeof(T) != sizeof(double) && st.rScale > 0.0) ? st.rScale : 1.0;
+  const double inv = 1.0 / rsc;  // exact: rsc is a power of two
   T rr = T(0), ru = T(0);
   for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
     const int u = v0 + my0 + lv;
     T r3[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      r3[i] = T(b.r64[3 * u + i]);
+      r3[i] = T(b.r64[3 * u + i] * inv);
       m.r[3 * lv + i] = r3[i];
       m.d[3 * lv + i] = T(0);
       m.p[3 * lv + i] = T(0);
@@ -206,7 +208,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
   int maxit = 0, totalIters = 0, iters = 0, converged = 0, outerDone = 0;
   if (t0) {
     double itol = st.tol;
-    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr, DBL_MIN)), 1e-5);
+    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr * rsc * rsc, DBL_MIN)), 1e-5);
     innerThr = fmax(itol * itol * srr, DBL_MIN);
     maxit = st.maxit;
     totalIters = st.totalIters;

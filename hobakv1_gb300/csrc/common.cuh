@@ -63,6 +63,7 @@ struct SolveState {
   double rhsNorm2;     // |rhs|^2
   double threshold;    // max(tol^2 |rhs|^2, DBL_MIN)
   double rr64;         // |rhs - A y|^2 after the last refinement
+  double rScale;       // mixed: the FP32 inner solve runs on r64 / rScale (a power of two near |r64|)
   double tol;
   int outerDone;       // 1 when the step's linear solve is finished
   int sweep;           // refinement sweeps done

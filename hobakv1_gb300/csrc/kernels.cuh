@@ -43,6 +43,17 @@ struct ClusterClass {
 constexpr int kSlice = 32;
 constexpr int kSlotVals = 9 * kSlice;
 
+// A power of two within a factor of two of sqrt(rr) (1 for 0 or non-finite):
+// the mixed-precision inner solve runs on r64 / scale, so its FP32 vectors and
+// dot products stay in range for any residual size, and an exact power-of-two
+// scale leaves every FP32 rounding as it would be unscaled.
+__device__ __forceinline__ double pow2_near_norm(double rr) {
+  if (!(rr > 0.0) || !isfinite(rr)) return 1.0;
+  int e;
+  frexp(rr, &e);
+  return ldexp(1.0, e / 2);
+}
+
 struct DeviceBatch {
   int nscenes, nv, nt, nblocks, ntiles;
   // launch shapes (hobak_batch_autotune): vertices per PCG tile (64 or 128),

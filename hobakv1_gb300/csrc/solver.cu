@@ -603,6 +603,7 @@ __global__ void __launch_bounds__(TV) k_rhs(DeviceBatch b) {
     st.newtonR = srr;  // Newmark's maxR = |rhs|^2 (NEWMARK.cpp:275)
     st.threshold = fmax(st.tol * st.tol * srr, DBL_MIN);
     st.rr64 = srr;
+    st.rScale = pow2_near_norm(srr);
     st.sweep = 0;
     st.totalIters = 0;
     st.converged = 0;
@@ -642,12 +643,14 @@ __global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) 
     return;
   }
   const int u = b.tileV0[tile] + threadIdx.x;
+  const double sc = (sizeof(T) != sizeof(double) && st.rScale > 0.0) ? st.rScale : 1.0;
+  const double inv = 1.0 / sc;  // exact: sc is a power of two
   T rr = T(0), ru = T(0);
   if (u < b.tileV1[tile]) {
     T r3[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      r3[i] = T(b.r64[3 * u + i]);
+      r3[i] = T(b.r64[3 * u + i] * inv);
       if (sizeof(T) != sizeof(double)) v.r[3 * u + i] = r3[i];
       v.d[3 * u + i] = T(0);
       v.p[3 * u + i] = T(0);
@@ -673,7 +676,7 @@ __global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) 
   const double sru = sum_partials<TV>(b.partial, sp.tile0, sp.ntiles, 1, sh);
   if (threadIdx.x == 0) {
     double itol = st.tol;
-    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr, DBL_MIN)), 1e-5);
+    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr * sc * sc, DBL_MIN)), 1e-5);
     st.rr = srr;
     st.gamma = sru;
     st.gammaOld = 1.0;
@@ -1096,8 +1099,9 @@ __global__ void k_accumulate(DeviceBatch b) {
   if (b.solve[s].outerDone) return;
   const int u = b.tileV0[tile] + threadIdx.x;
   if (u >= b.tileV1[tile]) return;
+  const double sc = b.solve[s].rScale > 0.0 ? b.solve[s].rScale : 1.0;
 #pragma unroll
-  for (int i = 0; i < 3; i++) b.y[3 * u + i] += double(b.v32.d[3 * u + i]);
+  for (int i = 0; i < 3; i++) b.y[3 * u + i] += sc * double(b.v32.d[3 * u + i]);
 }
 
 // Mixed precision: r64 = rhs - A y in FP64 (FP32 matrix entries promoted),
@@ -1134,6 +1138,7 @@ __global__ void __launch_bounds__(3 * TV) k_residual(DeviceBatch b) {
   const double srr = sum_partials<3 * TV>(b.partial, sp.tile0, sp.ntiles, 3, sh);
   if (threadIdx.x == 0) {
     st.rr64 = srr;
+    st.rScale = pow2_near_norm(srr);
     st.sweep += 1;
     if (srr < st.threshold) {
       st.outerDone = 1;

@@ -156,6 +156,15 @@ class TET_MESH:
     def totalVertices(self) -> int:
         return len(self._rest)
 
+    def surfaceVertices(self):
+        """Vertices of the boundary triangles (tet faces that belong to one
+        tet only), ascending like TET_MESH::computeSurfaceVertices
+        (TET_MESH.cpp:567-590)."""
+        t = self._tets
+        faces = np.concatenate([t[:, [0, 1, 2]], t[:, [0, 1, 3]], t[:, [0, 2, 3]], t[:, [1, 2, 3]]])
+        uniq, count = np.unique(np.sort(faces, axis=1), axis=0, return_counts=True)
+        return np.unique(uniq[count == 1]).astype(np.int64)
+
     def DOFs(self) -> int:
         return 3 * len(self._rest)
 
@@ -290,6 +299,39 @@ class BATCH:
     def set_acceleration(self, scene: int, a: np.ndarray):
         a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
         check(_lib.load().hobak_batch_set_acceleration(self.h, scene, dptr(a)), "hobak_batch_set_acceleration")
+
+    def set_pin_targets(self, scene: int, targets):
+        """Target displacements (world - rest) of one scene's pinned vertices,
+        3 per pin in the scene's pinned order, from the next step on."""
+        t = np.ascontiguousarray(targets, dtype=np.float64).reshape(-1)
+        check(_lib.load().hobak_batch_set_pin_targets(self.h, scene, dptr(t)), "hobak_batch_set_pin_targets")
+
+    def snapshot_bytes(self) -> int:
+        n = ctypes.c_size_t(0)
+        check(_lib.load().hobak_batch_snapshot_bytes(self.h, ctypes.byref(n)), "hobak_batch_snapshot_bytes")
+        return int(n.value)
+
+    def snapshot(self, dst_ptr: Optional[int] = None) -> Optional[np.ndarray]:
+        """The batch's dynamic state as bytes on the host, or written to the
+        device (or host) address dst_ptr of snapshot_bytes() bytes."""
+        n = self.snapshot_bytes()
+        if dst_ptr is not None:
+            check(_lib.load().hobak_batch_snapshot(self.h, ctypes.c_void_p(dst_ptr), n), "hobak_batch_snapshot")
+            return None
+        buf = np.empty(n, dtype=np.uint8)
+        check(_lib.load().hobak_batch_snapshot(self.h, buf.ctypes.data_as(ctypes.c_void_p), n),
+              "hobak_batch_snapshot")
+        return buf
+
+    def restore(self, snap=None, src_ptr: Optional[int] = None, nbytes: Optional[int] = None):
+        """Restore from snapshot() bytes, or from a host/device address."""
+        if src_ptr is not None:
+            n = nbytes if nbytes is not None else self.snapshot_bytes()
+            check(_lib.load().hobak_batch_restore(self.h, ctypes.c_void_p(src_ptr), n), "hobak_batch_restore")
+            return
+        buf = np.ascontiguousarray(snap, dtype=np.uint8)
+        check(_lib.load().hobak_batch_restore(self.h, buf.ctypes.data_as(ctypes.c_void_p), buf.size),
+              "hobak_batch_restore")
 
     def query(self) -> bool:
         """True when the batch's enqueued steps have finished (non-blocking)."""
@@ -459,6 +501,8 @@ class BACKWARD_EULER_VELOCITY:
         self._dt = 1.0 / 60.0  # BACKWARD_EULER_VELOCITY.cpp:37
         self._massScale = 1.0
         self._pinned: list = []
+        self._shapePins: dict = {}  # vertex -> (shape, local position) for pins that follow a shape
+        self._pinnedAt = None       # displacement of each pin when the GPU state was built
         self._batch: Optional[BATCH] = None
         self._currentTimestep = 0
         self._lastStats = None
@@ -530,17 +574,51 @@ class BACKWARD_EULER_VELOCITY:
 
     def attachKinematicConstraints(self, vertices: Iterable[int]):
         """Pin vertices at their current positions (TIMESTEPPER.cpp:380-403).
-        Takes vertex ids, or any object with inside(point) like KINEMATIC_SHAPE."""
+        Takes vertex ids, or a kinematic shape (inside(point); with
+        worldVertexToLocal/localVertexToWorld, like KINEMATIC_SHAPE, the pins
+        follow the shape when it moves between solves)."""
         self._require_unbuilt("attachKinematicConstraints")
         if hasattr(vertices, "inside"):
-            verts = self._mesh.restVertices() + self._position.reshape(-1, 3)
-            ids = [i for i, p in enumerate(verts) if vertices.inside(p)]
+            self._attach_shape(vertices, range(self._mesh.totalVertices()))
         else:
             ids = [int(i) for i in vertices]
-        self._pinned.extend(ids)
+            self._pinned.extend(ids)
+
+    def attachKinematicSurfaceConstraints(self, shape):
+        """Pin the surface vertices inside a kinematic shape to it
+        (TIMESTEPPER.cpp:350-375)."""
+        self._require_unbuilt("attachKinematicSurfaceConstraints")
+        self._attach_shape(shape, self._mesh.surfaceVertices())
+
+    def _attach_shape(self, shape, candidates):
+        verts = self._mesh.restVertices() + self._position.reshape(-1, 3)
+        movable = hasattr(shape, "worldVertexToLocal") and hasattr(shape, "localVertexToWorld")
+        for i in candidates:
+            p = verts[int(i)]
+            if not shape.inside(p):
+                continue
+            self._pinned.append(int(i))
+            if movable:  # later constraints on a vertex override earlier ones (TIMESTEPPER.cpp:105-122)
+                self._shapePins[int(i)] = (shape, np.asarray(shape.worldVertexToLocal(p), dtype=np.float64))
 
     def constrainedNodes(self):
         return sorted(set(self._pinned))
+
+    def _push_pin_targets(self):
+        """applyKinematicConstraints: each shape-held pin's target is
+        localVertexToWorld(local) - rest for the shape's current transform."""
+        if not self._shapePins:
+            return
+        pins = self.constrainedNodes()
+        rest = self._mesh.restVertices()
+        t = np.empty((len(pins), 3))
+        for k, u in enumerate(pins):
+            if u in self._shapePins:
+                shape, local = self._shapePins[u]
+                t[k] = np.asarray(shape.localVertexToWorld(local), dtype=np.float64) - rest[u]
+            else:
+                t[k] = self._pinnedAt[k]
+        self._batch.set_pin_targets(0, t)
 
     def _require_unbuilt(self, what):
         if self._batch is not None:
@@ -556,6 +634,7 @@ class BACKWARD_EULER_VELOCITY:
         s.density, s.gravity, s.dt = self._massScale, (0.0, 0.0, 0.0), self._dt
         s.pinned = np.array(sorted(set(self._pinned)), dtype=np.int32)
         s.x0, s.v0 = self._position, self._velocity
+        self._pinnedAt = self._position.reshape(-1, 3)[s.pinned].copy()
         self._batch = BATCH([s], self._opts)
         if self._vertexFaceSelfCollisionsOn:
             self._push_collisions()
@@ -565,6 +644,7 @@ class BACKWARD_EULER_VELOCITY:
             self._build()
         b = self._batch
         b.set_state(0, self._position, self._velocity)
+        self._push_pin_targets()
         check(_lib.load().hobak_gpu_set_external_forces(b.h, dptr(np.ascontiguousarray(self._externalForces))),
               "hobak_gpu_set_external_forces")
         stats = b.step(1)

@@ -21,6 +21,8 @@
 #ifndef HOBAK_GPU_H
 #define HOBAK_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -148,6 +150,21 @@ int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v);
  * other integrators leave it untouched). */
 int hobak_batch_get_acceleration(hobak_batch b, int scene, double* a);
 int hobak_batch_set_acceleration(hobak_batch b, int scene, const double* a);
+/* Move one scene's pins: 3 target displacements (world - rest) per pinned
+ * vertex, in the order hobak_scene_desc.pinned listed them.  Replaces
+ * applyKinematicConstraints recomputing the targets from moved kinematic
+ * shapes at the start of each solve (TIMESTEPPER.cpp:105-122; scenes such as
+ * NEWMARK_STRETCH.h move a shape between frames).  Applies from the next step. */
+int hobak_batch_set_pin_targets(hobak_batch b, int scene, const double* targets);
+/* Snapshot of the batch's dynamic state (x, v, acceleration, external forces,
+ * pin targets, active flags) into host or device memory, and back.  The
+ * reference's counterpart is the per-frame JSON record of position, velocity
+ * and external forces (FILE_IO.cpp:427-445); a snapshot restores a batch with
+ * the same scenes bitwise.  snapshot_bytes gives the size; dst/src may be any
+ * host or device pointer; restore refuses a snapshot of other scenes. */
+int hobak_batch_snapshot_bytes(hobak_batch b, size_t* bytes);
+int hobak_batch_snapshot(hobak_batch b, void* dst, size_t bytes);
+int hobak_batch_restore(hobak_batch b, const void* src, size_t bytes);
 /* Whole batch at once: every scene's 3*nv values back to back in scene
  * order (total 3 * sum(nv)); one copy each.  The set calls are enqueued on
  * the batch's stream and return at once: host buffers must stay unchanged

@@ -1474,6 +1474,16 @@ int oracle_attach_pins(void* h, int n, const int* ids) {
   return 0;
 }
 
+// Move the pins: new target displacements (world - rest) for the pinned
+// vertices in attach order, as applyKinematicConstraints recomputes them from
+// a moved kinematic shape at the start of each solve (TIMESTEPPER.cpp:105-122).
+int oracle_set_pin_targets(void* h, int n, const double* targets) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s || n != (int)s->pinned.size()) return -1;
+  std::copy(targets, targets + 3 * (size_t)n, s->pinTarget.begin());
+  return 0;
+}
+
 int oracle_set_solver(void* h, double tol, int maxit, int precond) {
   Sim* s = static_cast<Sim*>(h);
   if (!s) return -1;

@@ -45,6 +45,7 @@ def lib():
         L.oracle_set_state.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.oracle_get_state.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.oracle_attach_pins.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip]
+        L.oracle_set_pin_targets.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
         L.oracle_set_solver.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.oracle_set_external_forces.argtypes = [ctypes.c_void_p, _dp]
         L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp]
@@ -120,6 +121,11 @@ class Sim:
         if integrator != "velocity":
             code = {"position": 1, "newmark": 2}[integrator]
             assert L.oracle_set_integrator(self.h, code, rayleigh[0], rayleigh[1]) == 0
+
+    def set_pin_targets(self, targets):
+        """Target displacements of the pinned vertices (scene.pinned order)."""
+        t = np.ascontiguousarray(targets, dtype=np.float64).reshape(-1)
+        assert lib().oracle_set_pin_targets(self.h, len(t) // 3, _d(t)) == 0
 
     def set_collisions(self, vf=True, eps=0.01, mu=1.0, beta=0.001):
         """Vertex-face self collisions (TIMESTEPPER.cpp:83-86 defaults: mu 1, beta 0.001)."""

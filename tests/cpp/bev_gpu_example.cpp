@@ -4,8 +4,11 @@
 // solve, read position().  Reads a mesh and state from raw binary files and
 // writes the final displacement, so a test can compare it with the oracle.
 //
-//   bev_gpu_example <in.bin> <out.bin> <steps> [position|newmark]
-// ("position" / "newmark" drive BACKWARD_EULER_POSITION / NEWMARK the same way)
+//   bev_gpu_example <in.bin> <out.bin> <steps> [position|newmark|stretch]
+// ("position" / "newmark" drive BACKWARD_EULER_POSITION / NEWMARK the same way;
+// "stretch" runs NEWMARK_STRETCH.h's script: NEWMARK, the surface vertices
+// inside two unit cubes pinned to them, the first cube moved 0.01 along -z on
+// frames 2..24, no gravity; pinned[] is unused there)
 // in.bin: int nv, int nt, int npinned, int material, double mu, lambda,
 //         density, dt, rest[3nv], tets[4nt] (int), pinned[npinned] (int), x0[3nv]
 #include <cstdio>
@@ -43,6 +46,46 @@ int run(TET_MESH& mesh, VOLUME::HYPERELASTIC& material, const double* prm, const
   return 0;
 }
 
+// A unit cube kinematic shape (CUBE.cpp:27-55 with KINEMATIC_SHAPE.h:55-69,
+// identity rotation and uniform scale).
+struct CUBE {
+  VECTOR3 translation;
+  REAL scale;
+  VECTOR3 worldVertexToLocal(const VECTOR3& w) const {
+    return {(w[0] - translation[0]) / scale, (w[1] - translation[1]) / scale, (w[2] - translation[2]) / scale};
+  }
+  VECTOR3 localVertexToWorld(const VECTOR3& l) const {
+    return {scale * l[0] + translation[0], scale * l[1] + translation[1], scale * l[2] + translation[2]};
+  }
+  bool inside(const VECTOR3& p) const {
+    const VECTOR3 l = worldVertexToLocal(p);
+    for (int i = 0; i < 3; i++)
+      if (l[i] > 0.5 || l[i] < -0.5) return false;
+    return true;
+  }
+};
+
+int run_stretch(TET_MESH& mesh, VOLUME::HYPERELASTIC& material, const double* prm, int steps, const char* out) {
+  TIMESTEPPER::NEWMARK solver(mesh, material);
+  solver.setDt(prm[3]);
+  CUBE c0{{0.56, 0.48, -0.24}, 1.0}, c1{{0.56, 0.48, 1.23}, 1.0};
+  solver.attachKinematicSurfaceConstraints(&c0);
+  solver.attachKinematicSurfaceConstraints(&c1);
+  for (int frame = 0; frame < steps; frame++) {
+    if (frame > 1 && frame < 25) c0.translation[2] -= 0.01;
+    std::fill(solver.externalForces().begin(), solver.externalForces().end(), 0.0);
+    if (!solver.solve(false)) {
+      std::fprintf(stderr, "solve failed: %s\n", solver.lastError().c_str());
+      return 1;
+    }
+  }
+  FILE* o = std::fopen(out, "wb");
+  std::fwrite(solver.position().data(), 8, solver.position().size(), o);
+  std::fwrite(solver.velocity().data(), 8, solver.velocity().size(), o);
+  std::fclose(o);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc != 4 && argc != 5) {
     std::fprintf(stderr, "usage: %s in.bin out.bin steps [position]\n", argv[0]);
@@ -71,6 +114,7 @@ int main(int argc, char** argv) {
   VOLUME::HYPERELASTIC& material = (kind == HOBAK_MATERIAL_ARAP) ? (VOLUME::HYPERELASTIC&)arap : snh;
 
   const int steps = std::atoi(argv[3]);
+  if (argc == 5 && std::string(argv[4]) == "stretch") return run_stretch(mesh, material, prm, steps, argv[2]);
   if (argc == 5 && std::string(argv[4]) == "position")
     return run<TIMESTEPPER::BACKWARD_EULER_POSITION>(mesh, material, prm, x0, pinned, steps, argv[2]);
   if (argc == 5 && std::string(argv[4]) == "newmark")

@@ -49,3 +49,27 @@ def test_cpp_mirror_solve_matches_oracle(tmp_path):
         xo, vo = sim.state()
         assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-9, integrator
         assert np.linalg.norm(v - vo) / np.linalg.norm(vo) < 1e-8, integrator
+
+
+@pytest.mark.gpu
+def test_cpp_mirror_moving_pins_match_the_reference_regression_record(tmp_path):
+    """NEWMARK_STRETCH through the C++ mirror (pins attached to two cube
+    shapes with attachKinematicSurfaceConstraints, one cube moved between
+    solves) against the reference's recorded last frame, at its 1e-8."""
+    exe = compile_example(tmp_path)
+    g = np.load(os.path.join(ROOT, "tests", "golden", "regression_newmark_stretch.npz"))
+    rest, tets = g["rest"], g["tets"]
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(inp, "wb") as f:
+        np.array([len(rest), len(tets), 0, 0], dtype=np.int32).tofile(f)
+        np.array([1.0, 10.0, 1.0, float(g["dt"])], dtype=np.float64).tofile(f)
+        rest.astype(np.float64).tofile(f)
+        tets.astype(np.int32).tofile(f)
+        np.zeros(3 * len(rest)).tofile(f)
+    n = int(g["total_frames"])
+    subprocess.run([exe, str(inp), str(out), str(n), "stretch"], check=True)
+    xv = np.fromfile(out, dtype=np.float64)
+    x, v = xv[:3 * len(rest)], xv[3 * len(rest):]
+    assert int(g["frames"][-1]) == n - 1
+    assert np.linalg.norm(x - g["position"][-1]) / np.linalg.norm(g["position"][-1]) < 1e-8
+    assert np.linalg.norm(v - g["velocity"][-1]) / np.linalg.norm(g["velocity"][-1]) < 1e-6

@@ -143,3 +143,22 @@ def test_serving_footprint_estimate_covers_the_allocation(precision):
         b = hobak.BATCH([s], hobak.solver_opts(precision=precision))
         assert footprint_bytes(s, precision) >= b.device_bytes()
         b.close()
+
+
+@pytest.mark.parametrize("integrator", [hobak.INTEGRATOR_VELOCITY, hobak.INTEGRATOR_NEWMARK], ids=["bev", "newmark"])
+def test_mixed_precision_handles_a_tiny_right_hand_side(integrator):
+    """An unloaded mesh at rest: the right-hand side is only the rounding
+    residue of the rest-state forces (~1e-16).  The FP32 inner solve runs on
+    the residual scaled by a power of two, so its dot products do not
+    underflow to 0/0; the result stays at the FP64 solve's noise level."""
+    import dataclasses
+    s = dataclasses.replace(scenes.config1_scene(6), gravity=(0.0, 0.0, 0.0))
+    out = {}
+    for prec in (hobak.PRECISION_FP64, hobak.PRECISION_MIXED):
+        b = hobak.BATCH([s], hobak.solver_opts(precision=prec, integrator=integrator))
+        b.step(3)
+        out[prec] = b.get_state(0)[0]
+        b.close()
+    x64, x32 = out[hobak.PRECISION_FP64], out[hobak.PRECISION_MIXED]
+    assert np.isfinite(x32).all() and np.linalg.norm(x64) < 1e-12
+    assert np.linalg.norm(x32 - x64) < 1e-12
