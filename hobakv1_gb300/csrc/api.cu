@@ -1627,9 +1627,9 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   if (!b || !opts) return fail(HOBAK_ERR_INVALID, "bad arguments");
   int rc = check_opts(opts);
   if (rc) return rc;
-  if (opts->integrator != HOBAK_INTEGRATOR_VELOCITY)
+  if (opts->integrator == HOBAK_INTEGRATOR_NEWMARK)
     for (const CollisionScene& cs : b->collScenes)
-      if (cs.vfOn) return fail(HOBAK_ERR_INVALID, "vertex-face contact needs the velocity integrator");
+      if (cs.vfOn) return fail(HOBAK_ERR_INVALID, "vertex-face contact is not available with NEWMARK");
   b->opts = *opts;
   b->clusterDirty = true;
   drop_graphs(b);
@@ -1648,8 +1648,8 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
                                double damping_beta) {
   if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
   if (vf_on && !(eps > 0.0)) return fail(HOBAK_ERR_INVALID, "collision distance must be > 0");
-  if (vf_on && b->opts.integrator != HOBAK_INTEGRATOR_VELOCITY)
-    return fail(HOBAK_ERR_INVALID, "vertex-face contact needs the velocity integrator");
+  if (vf_on && b->opts.integrator == HOBAK_INTEGRATOR_NEWMARK)
+    return fail(HOBAK_ERR_INVALID, "vertex-face contact is not available with NEWMARK");
   if (!b->collArena) {
     int rc = build_collisions(b);
     if (rc) return rc;

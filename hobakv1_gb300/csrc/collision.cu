@@ -376,10 +376,14 @@ __global__ void k_vf_pairs(DeviceBatch b, DeviceCollisions c) {
     double Gz[3];
     for (int r = 0; r < 3; r++) Gz[r] = G[r] * zv[0] + G[r + 3] * zv[1] + G[r + 6] * zv[2];
     const double tv[3] = {t.x, t.y, t.z};
+    // right-hand side: dt (f + dt H v) for the velocity integrator; the
+    // position integrator's b takes the force alone (collisionC and K stay
+    // out of it, BACKWARD_EULER_POSITION.cpp:196-203)
+    const bool position = b.scenes[s].integrator == kIntegratorPosition;
     for (int a = 0; a < 4; a++)
       for (int k = 0; k < 3; k++) {
         Fo[3 * a + k] = fs * cvec[a] * tv[k];
-        R[3 * a + k] = dt * (fs * cvec[a] * tv[k] + dt * cvec[a] * Gz[k]);
+        R[3 * a + k] = position ? fs * cvec[a] * tv[k] : dt * (fs * cvec[a] * tv[k] + dt * cvec[a] * Gz[k]);
       }
   }
 }
@@ -425,7 +429,7 @@ __global__ void k_copy_total(const int* src, int* dst) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 
-// Collision part of LHS's diagonal, -(dt beta + dt^2) sum c_a^2 G over the
+// Collision part of LHS's diagonal, w sum c_a^2 G (w = collision_lhs_scale) over the
 // vertex's incidences (free rows only; zero elsewhere), kept in FP64 beside
 // the LHS: the preconditioner adds it to the diagonal block, the products
 // (collision_row) apply it in FP64, so the mixed path's FP64 residual sees the
@@ -440,8 +444,7 @@ __global__ void k_coll_diag(DeviceBatch b, DeviceCollisions c) {
     for (int q = 0; q < 9; q++) out[q] = 0.0;
     return;
   }
-  const int s = b.vertexScene[u];
-  const double dt = b.scenes[s].dt, scale = -(dt * c.scenes[s].beta + dt * dt);
+  const double scale = collision_lhs_scale(b, b.vertexScene[u]);
   double D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int k = k0; k < k1; k++) {
     const int e = c.incList[k], p = e >> 2, a = e & 3;

@@ -145,6 +145,16 @@ __device__ __forceinline__ size_t col_slot(const DeviceBatch& b, int u, int j) {
   return (size_t)(b.sliceRow[u >> 5] + j) * kSlice + (u & (kSlice - 1));
 }
 
+// Weight of the collision Hessian H_coll in the step's matrix A, with
+// K += H_coll and collision damping beta H_coll (TIMESTEPPER.cpp:645-720):
+// velocity integrator A = M - dt C - dt^2 K gives -(dt beta + dt^2);
+// position integrator A = M/dt^2 - (C + collisionC)/dt - K gives
+// -(beta/dt + 1) (BACKWARD_EULER_POSITION.cpp:187-208).
+__device__ __forceinline__ double collision_lhs_scale(const DeviceBatch& b, int s) {
+  const double dt = b.scenes[s].dt, beta = b.coll.scenes[s].beta;
+  return b.scenes[s].integrator == kIntegratorPosition ? -(beta / dt + 1.0) : -(dt * beta + dt * dt);
+}
+
 void launch_begin_step(const DeviceBatch& b, cudaStream_t s);
 // rawForces = 1 stores the element force f itself in elemG instead of dt (f + dt He v)
 void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces = 0);

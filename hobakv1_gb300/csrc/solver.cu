@@ -694,7 +694,7 @@ __global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) 
   }
 }
 
-// Row i of vertex u of -(dt beta + dt^2) H_coll x, H_coll = sum over the
+// Row i of vertex u of w H_coll x (w = collision_lhs_scale), H_coll = sum over the
 // vertex's collision tets of (c c^T) (x) G (free rows only; x vanishes on
 // pinned rows, which keeps the columns masked too).  FP64 throughout: the
 // contact blocks are not part of the (possibly FP32) assembled LHS.
@@ -703,8 +703,7 @@ __device__ __forceinline__ double collision_row(const DeviceBatch& b, int u, int
   const DeviceCollisions& c = b.coll;
   const int k0 = c.incCount[u], k1 = c.incCount[u + 1];
   if (k0 == k1) return 0.0;
-  const int s = b.vertexScene[u];
-  const double dt = b.scenes[s].dt, scale = -(dt * c.scenes[s].beta + dt * dt);
+  const double scale = collision_lhs_scale(b, b.vertexScene[u]);
   double acc = 0.0;
   for (int k = k0; k < k1; k++) {
     const int e = c.incList[k], p = e >> 2, a = e & 3;

@@ -665,8 +665,8 @@ class BACKWARD_EULER_POSITION(BACKWARD_EULER_VELOCITY):
     """GPU drop-in for TIMESTEPPER::BACKWARD_EULER_POSITION with Rayleigh
     damping (BACKWARD_EULER_POSITION.cpp:138-330): the same host-state
     semantics; the solve's unknown is the position update and
-    C = alpha M + beta K(rest).  Vertex-face contact is not available with
-    this integrator."""
+    C = alpha M + beta K(rest).  Vertex-face contact works as for
+    BACKWARD_EULER_VELOCITY (forces in b, beta H_coll / dt + H_coll in A)."""
 
     def __init__(self, tetMesh: TET_MESH, hyperelastic: HYPERELASTIC, opts: Optional[HobakSolverOpts] = None):
         super().__init__(tetMesh, hyperelastic, None if opts is None else HobakSolverOpts.from_buffer_copy(opts))
@@ -684,10 +684,6 @@ class BACKWARD_EULER_POSITION(BACKWARD_EULER_VELOCITY):
         self._require_unbuilt("setRayleigh")
         self._opts.rayleigh_alpha, self._opts.rayleigh_beta = float(alpha), float(beta)
 
-    def setVertexFaceSelfCollisionsOn(self, on: bool):
-        if on:
-            raise ValueError("vertex-face contact needs BACKWARD_EULER_VELOCITY")
-        super().setVertexFaceSelfCollisionsOn(False)
 
 
 class NEWMARK(BACKWARD_EULER_VELOCITY):

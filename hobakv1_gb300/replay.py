@@ -289,6 +289,107 @@ class NEWMARK_STRETCH(SIMULATION_SCENE):
         self.frameNumber += 1
 
 
+def compute_mu(E: float, nu: float) -> float:
+    """HYPERELASTIC::computeMu (HYPERELASTIC.cpp:111-114)."""
+    return E / (2.0 * (1.0 + nu))
+
+
+def compute_lambda(E: float, nu: float) -> float:
+    """HYPERELASTIC::computeLambda (HYPERELASTIC.cpp:119-122)."""
+    return (E * nu) / ((1.0 + nu) * (1.0 - 2.0 * nu))
+
+
+class _TWO_TET_VF(SIMULATION_SCENE):
+    """The two-tet vertex-face contact scenes: BACKWARD_EULER_POSITION at
+    dt = 1/30, the surface vertices inside the kinematic cubes pinned, vertex-
+    face self collisions on, edge-edge off.  The reference also registers the
+    lower cube as a collision object (addKinematicCollisionObject, plane
+    constraints); in these scenes no free vertex ever enters it, so that part
+    never acts and is not built."""
+
+    mesh_file = ""
+    material = None        # hobak material class
+    E = nu = 0.0
+    gravity_y = 0.0
+    shapes = ()            # ((center), scale) of each pinning cube
+    collision_eps = 0.01   # TET_MESH default (TET_MESH.cpp:70)
+    rayleigh = None        # (alpha, beta), None: the integrator's default
+    pause = 0
+
+    def __init__(self, rest: np.ndarray, tets: np.ndarray, opts: Optional[hobak.HobakSolverOpts] = None):
+        super().__init__(opts)
+        self._rest, self._tets = rest, tets
+
+    def collision_mu(self, mu: float) -> float:
+        raise NotImplementedError
+
+    def buildScene(self) -> bool:
+        self.tetMeshFilename = self.mesh_file
+        self.gravity = np.array([0.0, self.gravity_y, 0.0])
+        mu, lam = compute_mu(self.E, self.nu), compute_lambda(self.E, self.nu)
+        self.tetMesh = hobak.TET_MESH(self._rest, self._tets)
+        self.materialName = self.material.NAME
+        solver = hobak.BACKWARD_EULER_POSITION(self.tetMesh, self.material(mu, lam), self.opts)
+        self._solver = solver
+        solver.setDt(1.0 / 30.0)
+        solver.setCollisionEps(self.collision_eps)
+        self.kinematicShapes = [CUBE(c, sc) for c, sc in self.shapes]
+        for shape in self.kinematicShapes:
+            solver.attachKinematicSurfaceConstraints(shape)
+        if self.rayleigh is not None:
+            solver.setRayleigh(*self.rayleigh)
+        solver.setCollisionStiffness(self.collision_mu(mu))
+        solver.setCollisionDampingBeta(0.01)
+        solver.setVertexFaceSelfCollisionsOn(True)
+        self.edgeEdgeSelfCollisionsOn = False
+        self.eye = np.array([-2.13557, 0.947023, 2.39579])
+        self.lookAt = np.array([-1.35707, 0.964614, 1.76839])
+        self.up = np.array([-0.00368317, 0.999718, 0.0234604])
+        self.pauseFrame = self.pause
+        return True
+
+    def vertexFaceCollisions(self):
+        b = self._solver._batch
+        return [] if b is None else [tuple(p) for p in b.collision_pairs(0)[0]]
+
+
+class TWO_TET_DROP_VF(_TWO_TET_VF):
+    """TWO_TET_DROP_VF.h: a tet dropped (gravity 0.3) onto a pinned one,
+    SNH(E = 3, nu = 0.45), collision stiffness 10."""
+    mesh_file = "../data/two_tets_vertex_face.tobj"
+    material = hobak.SNH
+    E, nu, gravity_y = 3.0, 0.45, -0.3
+    shapes = (((0.0, -4.90, 0.0), 10.0),)
+    pause = 200
+
+    def collision_mu(self, mu):
+        return 10.0
+
+    def buildScene(self) -> bool:
+        self.sceneName = "two_tet_drop_vf"
+        return super().buildScene()
+
+
+class TWO_TET_KISS_VF(_TWO_TET_VF):
+    """TWO_TET_KISS_VF.h: two pinned tets barely touching at a vertex and a
+    face, ARAP(E = 10, nu = 0.45), collision distance 0.03, stiffness 10 mu,
+    no Rayleigh damping."""
+    mesh_file = "../data/two_tets_vertex_face_kiss.tobj"
+    material = hobak.ARAP
+    E, nu, gravity_y = 10.0, 0.45, 0.0
+    shapes = (((0.0, -4.90, 0.0), 10.0), ((0.0, 6.9, 0.0), 10.0))
+    collision_eps = 0.03
+    rayleigh = (0.0, 0.0)
+    pause = 100
+
+    def collision_mu(self, mu):
+        return mu * 10.0
+
+    def buildScene(self) -> bool:
+        self.sceneName = "two_tet_kiss_vf"
+        return super().buildScene()
+
+
 # --------------------------------------------------------------- regression
 
 def scene_regression(scene: SIMULATION_SCENE, truth: SceneRecord, tol: float = 1e-8,

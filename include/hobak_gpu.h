@@ -95,7 +95,7 @@ typedef struct hobak_solver_opts {
   int use_graph;           /* capture each step as a CUDA graph (1) or launch eagerly (0) */
   int integrator;          /* HOBAK_INTEGRATOR_* (default VELOCITY) */
   double rayleigh_alpha;   /* POSITION: C = alpha M + beta K(rest) (defaults 0.01, 0.01: */
-  double rayleigh_beta;    /*   BACKWARD_EULER_POSITION.cpp:53-54); vertex-face contact needs VELOCITY */
+  double rayleigh_beta;    /*   BACKWARD_EULER_POSITION.cpp:53-54); NEWMARK has no vertex-face contact */
   int max_newton;          /* NEWMARK: Newton iterations per step at most (default 10) */
   double newton_tolerance; /* NEWMARK: stop once |rhs|^2 <= this (default 1e-7, NEWMARK.cpp:43) */
 } hobak_solver_opts;

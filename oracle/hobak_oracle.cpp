@@ -1179,6 +1179,41 @@ void pcg(Sim& s, const std::vector<double>& A, const std::vector<double>& rhs, s
   s.lastIters = i;
 }
 
+// computeCollisionDetection + computeCollisionResponse (TIMESTEPPER.cpp:614-720)
+// for a step whose A weighs the collision Hessian H_coll by collScale:
+// R += f_coll; the PCG adds collScale H_coll (in pair order) and its
+// diagonal blocks to the preconditioner; with collKv, also H_coll v.
+void collisionTerms(Sim& s, double collScale, std::vector<double>* collKv) {
+  const int nv = s.M.nv;
+  Collisions& C = s.coll;
+  C.weight.clear();
+  s.collDiag.clear();
+  if (!C.on) return;
+  vfDetect(s);
+  vfResponse(s);
+  s.collScale = collScale;
+  std::vector<double> fc(3 * (size_t)nv, 0.0);
+  if (collKv) collKv->assign(3 * (size_t)nv, 0.0);
+  s.collDiag.assign(9 * (size_t)nv, 0.0);
+  for (size_t k = 0; k < C.weight.size(); k++) {
+    const double* H = &C.H12[144 * k];
+    for (int a = 0; a < 4; a++) {
+      const int u = C.ctets[4 * k + a];
+      for (int i = 0; i < 3; i++) fc[3 * u + i] += C.f12[12 * k + 3 * a + i];
+      for (int b = 0; b < 4; b++) {
+        const int w = C.ctets[4 * k + b];
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) {
+            const double h = H[(3 * a + i) + 12 * (3 * b + j)];
+            if (collKv) (*collKv)[3 * u + i] += h * s.v[3 * w + j];
+            if (u == w && s.free[u]) s.collDiag[9 * (size_t)u + i + 3 * j] += s.collScale * h;
+          }
+      }
+    }
+  }
+  for (size_t k = 0; k < fc.size(); k++) s.R[k] = s.R[k] + fc[k];
+}
+
 // One BACKWARD_EULER_VELOCITY::solveRayleighDamped step with collisions off
 // (BACKWARD_EULER_VELOCITY.cpp:107-235).  The Rayleigh C built at line 118 is
 // zeroed by computeCollisionResponse (TIMESTEPPER.cpp:657) before use, so it
@@ -1191,37 +1226,9 @@ void step(Sim& s) {
     for (int i = 0; i < 3; i++) s.x[3 * s.pinned[k] + i] = s.pinTarget[3 * k + i];
   assemble(s);
   const double dt = s.dt;
-  // computeCollisionDetection + computeCollisionResponse (TIMESTEPPER.cpp:614-720):
   // R += f_coll, K += H_coll, C = beta H_coll, so A gains -(dt beta + dt^2) H_coll
-  Collisions& C = s.coll;
-  C.weight.clear();
-  s.collDiag.clear();
   std::vector<double> collKv;
-  if (C.on) {
-    vfDetect(s);
-    vfResponse(s);
-    s.collScale = -(dt * C.beta + dt * dt);
-    std::vector<double> fc(3 * (size_t)nv, 0.0);
-    collKv.assign(3 * (size_t)nv, 0.0);
-    s.collDiag.assign(9 * (size_t)nv, 0.0);
-    for (size_t k = 0; k < C.weight.size(); k++) {
-      const double* H = &C.H12[144 * k];
-      for (int a = 0; a < 4; a++) {
-        const int u = C.ctets[4 * k + a];
-        for (int i = 0; i < 3; i++) fc[3 * u + i] += C.f12[12 * k + 3 * a + i];
-        for (int b = 0; b < 4; b++) {
-          const int w = C.ctets[4 * k + b];
-          for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) {
-              const double h = H[(3 * a + i) + 12 * (3 * b + j)];
-              collKv[3 * u + i] += h * s.v[3 * w + j];
-              if (u == w && s.free[u]) s.collDiag[9 * (size_t)u + i + 3 * j] += s.collScale * h;
-            }
-        }
-      }
-    }
-    for (size_t k = 0; k < fc.size(); k++) s.R[k] = s.R[k] + fc[k];
-  }
+  collisionTerms(s, -(dt * s.coll.beta + dt * dt), &collKv);
   // K v
   std::vector<double> Kv(3 * (size_t)nv);
 #pragma omp parallel for schedule(static)
@@ -1265,8 +1272,10 @@ void step(Sim& s) {
     }
 }
 
-// One BACKWARD_EULER_POSITION::solveRayleighDamped step with collisions off
-// and no plane constraints, so z = 0 (BACKWARD_EULER_POSITION.cpp:138-330):
+// One BACKWARD_EULER_POSITION::solveRayleighDamped step without plane
+// constraints, so z = 0 (BACKWARD_EULER_POSITION.cpp:138-330), with optional
+// vertex-face contact (R += f_coll; collisionC = beta H_coll enters A only,
+// BEP.cpp:187-208, so A gains -(beta/dt + 1) H_coll):
 //   C   = alpha M + beta K0, K0 = clamped Hessian at zero displacement
 //         (buildRayleighDampingMatrix, TIMESTEPPER.cpp:213-236)
 //   b   = (M/dt - C) v + R + f_ext                              (BEP.cpp:196)
@@ -1287,6 +1296,7 @@ void stepPosition(Sim& s) {
     s.x = keep;
   }
   assemble(s);
+  collisionTerms(s, -(s.coll.beta * invDt + 1.0), nullptr);
   std::vector<double> rhs(3 * (size_t)nv);
 #pragma omp parallel for schedule(static)
   for (int u = 0; u < nv; u++) {
@@ -1520,7 +1530,7 @@ int oracle_nblocks(void* h) { return static_cast<Sim*>(h)->M.rowptr.back(); }
 int oracle_set_integrator(void* h, int integrator, double alpha, double beta) {
   Sim* s = static_cast<Sim*>(h);
   if (!s || integrator < 0 || integrator > 2) return -1;
-  if (integrator != 0 && s->coll.on) return -2;
+  if (integrator == 2 && s->coll.on) return -2;  // NEWMARK: no contact
   s->integrator = integrator;
   s->rayAlpha = alpha;
   s->rayBeta = beta;
@@ -1533,6 +1543,7 @@ int oracle_set_integrator(void* h, int integrator, double alpha, double beta) {
 int oracle_set_collisions(void* h, int vf_on, double eps, double mu, double beta) {
   Sim* s = static_cast<Sim*>(h);
   if (!s) return -1;
+  if (vf_on && s->integrator == 2) return -2;  // NEWMARK: no contact
   s->coll.on = vf_on != 0;
   s->coll.eps = eps;
   s->coll.mu = mu;

@@ -119,15 +119,34 @@ def test_switching_integrator_matches_a_new_batch():
     assert np.array_equal(xb, xc) and np.array_equal(vb, vc)
 
 
-def test_contact_needs_the_velocity_integrator():
+def test_contact_is_refused_for_newmark_only():
     two = scenes.two_cubes_scene(4)
-    b = hobak.BATCH([two], hobak.solver_opts(integrator=POS))
+    b = hobak.BATCH([two], hobak.solver_opts(integrator=hobak.INTEGRATOR_NEWMARK))
     with pytest.raises(_lib.HobakError):
         b.set_collisions(0, True, 1e-3, 1e3, 0.001)
-    c = hobak.BATCH([two], hobak.solver_opts())
+    c = hobak.BATCH([two], hobak.solver_opts(integrator=POS))
     c.set_collisions(0, True, 1e-3, 1e3, 0.001)
     with pytest.raises(_lib.HobakError):
-        c.set_solver(hobak.solver_opts(integrator=POS))
+        c.set_solver(hobak.solver_opts(integrator=hobak.INTEGRATOR_NEWMARK))
+
+
+@pytest.mark.parametrize("precision,bound", [(hobak.PRECISION_FP64, 1e-8), (hobak.PRECISION_MIXED, 1e-6)],
+                         ids=["fp64", "mixed"])
+def test_position_integrator_with_contact_matches_oracle(precision, bound):
+    """Two cubes pressed together (vertex-face pairs every step): forces in
+    b, -(beta/dt + 1) H_coll in A (BACKWARD_EULER_POSITION.cpp:187-208)."""
+    two = scenes.two_cubes_scene(5)
+    b = hobak.BATCH([two], hobak.solver_opts(integrator=POS, precision=precision))
+    b.set_collisions(0, True, 1e-3, 1e3, 0.001)
+    sim = oracle.Sim(two, precond=1, integrator="position")
+    sim.set_collisions(True, 1e-3, 1e3, 0.001)
+    for _ in range(4):
+        b.step(2)
+        sim.step(2)
+        assert len(b.collision_pairs(0)[0]) > 0
+        x, _ = b.get_state(0)
+        xo, _ = sim.state()
+        assert rel(x + two.rest.reshape(-1), xo + two.rest.reshape(-1)) < bound
 
 
 def test_python_mirror_position_solve_matches_oracle():

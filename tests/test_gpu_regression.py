@@ -109,3 +109,27 @@ def test_pin_targets_move_the_pins():
     assert np.allclose(x.reshape(-1, 3)[s.pinned], t)
     with pytest.raises(_lib.HobakError):
         b.set_pin_targets(0, np.full_like(t, np.nan))
+
+
+@pytest.mark.parametrize("precision,bound", [(hobak.PRECISION_FP64, 1e-8), (hobak.PRECISION_MIXED, 1e-5)],
+                         ids=["fp64", "mixed"])  # mixed: 1e-8 per solve, grown over 200 frames of contact
+@pytest.mark.parametrize("name", ["two_tet_drop_vf", "two_tet_kiss_vf"])
+def test_two_tet_contact_scenes_match_the_reference(name, precision, bound):
+    """The reference's two-tet vertex-face regression scenes through the
+    BACKWARD_EULER_POSITION drop-in with contact, frame by frame: against
+    the reference built here (fixture) at `bound`, against the recorded file
+    at 2e-7 (FP64; the reference itself is 2.5e-8 / 8.9e-8 from it here),
+    and the vertex-face pair count of every frame equal to the record's."""
+    g = np.load(os.path.join(GOLDEN, f"regression_{name}.npz"))
+    cls = {"two_tet_drop_vf": replay.TWO_TET_DROP_VF, "two_tet_kiss_vf": replay.TWO_TET_KISS_VF}[name]
+    sc = cls(g["rest"], g["tets"], hobak.solver_opts(precision=precision, preconditioner=hobak.PRECOND_JACOBI,
+                                                     integrator=hobak.INTEGRATOR_POSITION))
+    sc.buildScene()
+    for k in range(int(g["total_frames"])):
+        sc.stepSimulation()
+        x = sc.solver().position()
+        xr = g["ref_position"][k]
+        assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < bound, k
+        if precision == hobak.PRECISION_FP64:
+            assert np.linalg.norm(x - g["position"][k]) / np.linalg.norm(g["position"][k]) < 2e-7, k
+        assert len(sc.vertexFaceCollisions()) == int(g["vf_pairs"][k]), k

@@ -124,3 +124,35 @@ def test_oracle_newmark_stretch_matches_the_reference_regression_record():
         else:
             assert np.linalg.norm(x - g) / np.linalg.norm(g) < 1e-10, frame
             assert np.linalg.norm(v - rec.velocity[r]) / np.linalg.norm(rec.velocity[r]) < 1e-8, frame
+
+
+def two_tet_record(name):
+    g = np.load(os.path.join(GOLDEN, f"regression_{name}.npz"))
+    return g
+
+
+@pytest.mark.parametrize("name", ["two_tet_drop_vf", "two_tet_kiss_vf"])
+def test_oracle_two_tet_contact_scenes_match_the_reference(name):
+    """BACKWARD_EULER_POSITION with vertex-face contact on the reference's
+    two-tet regression scenes: against the reference built here at 1e-9 for
+    every frame, and against the recorded file at 2e-7 (the reference itself
+    is 2.5e-8 / 8.9e-8 from that record on this machine)."""
+    g = two_tet_record(name)
+    cls = {"two_tet_drop_vf": replay.TWO_TET_DROP_VF, "two_tet_kiss_vf": replay.TWO_TET_KISS_VF}[name]
+    rest, tets = g["rest"], g["tets"]
+    sc = cls(rest, tets)
+    mu, lam = replay.compute_mu(cls.E, cls.nu), replay.compute_lambda(cls.E, cls.nu)
+    shapes = [replay.CUBE(c, s) for c, s in cls.shapes]
+    pins = np.array([v for v in range(len(rest)) if any(s.inside(rest[v]) for s in shapes)], dtype=np.int32)
+    z = np.zeros_like(rest)
+    s = scenes.Scene(name, rest, tets, cls.material.NAME.lower(), mu, lam, pins, z, z.copy(), density=1.0,
+                     gravity=(0.0, cls.gravity_y, 0.0), dt=float(g["dt"]))
+    sim = oracle.Sim(s, precond=0, integrator="position",
+                     rayleigh=cls.rayleigh if cls.rayleigh is not None else (0.01, 0.01))
+    sim.set_collisions(True, cls.collision_eps, sc.collision_mu(mu), 0.01)
+    assert (g["vf_pairs"] > 0).any()
+    for k in range(int(g["total_frames"])):
+        sim.step(1)
+        x, _ = sim.state()
+        assert np.linalg.norm(x - g["ref_position"][k]) / np.linalg.norm(g["ref_position"][k]) < 1e-9, k
+        assert np.linalg.norm(x - g["position"][k]) / np.linalg.norm(g["position"][k]) < 2e-7, k
