@@ -12,6 +12,7 @@
 // (util/MATRIX_UTIL.cpp:33-43); 9x9 and 12x12 matrices are column major.
 // Sparse matrices are 3x3-block CSR (BSR) with blocks stored column major.
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -664,6 +665,11 @@ inline V3 normalized(const V3& a) { return mul(1.0 / norm3(a), a); }
 
 struct Collisions {
   bool on = false;
+  bool ee = false;               // edge-edge self collisions
+  std::vector<int> edges;        // 2 per surface edge, (lo, hi), ascending like a std::map
+  std::vector<double> edgeArea;  // per surface edge: 1/3 of each adjacent triangle's rest area
+  std::vector<int> edgeTri;      // 2 per surface edge: first two adjacent triangles (-1: none)
+  std::vector<int> eePairs;      // per step: (edge, edge) pairs, surface edge indices
   double eps = 0.01, mu = 1.0, beta = 0.001;
   std::vector<int> tris;         // 3 per surface triangle, reference winding
   std::vector<int> surfVerts;    // ascending vertex ids
@@ -1036,6 +1042,244 @@ void vfResponse(Sim& s) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Edge-edge self collisions (EDGE_SQRT_COLLISION on surface edge pairs).
+// ---------------------------------------------------------------------------
+// Surface edges in std::map order of (lo, hi) (TET_MESH::computeSurfaceEdges,
+// TET_MESH.cpp:595-630), each edge's rest area (a third of each adjacent
+// surface triangle's rest area, TET_MESH.cpp:530-562) and its first two
+// adjacent triangles in triangle order (computeSurfaceEdgeTriangleNeighbors,
+// TET_MESH.cpp:356-412).
+void buildEdges(Collisions& C) {
+  const int ntri = (int)C.tris.size() / 3;
+  std::vector<std::pair<int, int>> e;
+  for (int t = 0; t < ntri; t++)
+    for (int j = 0; j < 3; j++) {
+      const int a = C.tris[3 * t + j], b = C.tris[3 * t + (j + 1) % 3];
+      e.push_back({std::min(a, b), std::max(a, b)});
+    }
+  std::sort(e.begin(), e.end());
+  e.erase(std::unique(e.begin(), e.end()), e.end());
+  const int ne = (int)e.size();
+  C.edges.resize(2 * ne);
+  for (int k = 0; k < ne; k++) {
+    C.edges[2 * k] = e[k].first;
+    C.edges[2 * k + 1] = e[k].second;
+  }
+  C.edgeArea.assign(ne, 0.0);
+  C.edgeTri.assign(2 * ne, -1);
+  for (int t = 0; t < ntri; t++)
+    for (int j = 0; j < 3; j++) {
+      const int a = C.tris[3 * t + j], b = C.tris[3 * t + (j + 1) % 3];
+      const int k = (int)(std::lower_bound(e.begin(), e.end(), std::make_pair(std::min(a, b), std::max(a, b))) -
+                          e.begin());
+      C.edgeArea[k] += C.restArea[t] / 3.0;
+      if (C.edgeTri[2 * k] < 0) C.edgeTri[2 * k] = t;
+      else if (C.edgeTri[2 * k + 1] < 0) C.edgeTri[2 * k + 1] = t;
+    }
+}
+
+// Closest points of two segments, restating the published routine the
+// reference uses (Rhodes, "Fast, Robust Intersection of 3D Line Segments",
+// Game Programming Gems II; LINE_INTERSECT.cpp), with its tolerances: the
+// call passes 1e-8 both as the parallel/degenerate tolerance and where the
+// helpers take a squared tolerance.
+namespace segseg {
+const double kTol = 1e-8;
+inline bool outside01(double a) { return a < 0.0 || a > 1.0; }
+inline double clamp01(double a) { return std::max(0.0, std::min(1.0, a)); }
+// nearest point to q on the line/segment p + s L
+void nearestOnSegment(const V3& p, const V3& L, const V3& q, bool infinite, V3& out, double& param) {
+  const double D = dot3(L, L);
+  if (D < kTol) {
+    out = p;
+    return;
+  }
+  param = dot3(L, sub(q, p)) / D;
+  if (!infinite) param = clamp01(param);
+  out = add(p, mul(param, L));
+}
+void parallel(const V3& a1, const V3& a2, const V3& La, const V3& b1, const V3& b2, const V3& Lb, V3& pa, V3& pb) {
+  double s0 = 0.0, s1 = 0.0, tmp = 0.0;
+  nearestOnSegment(a1, La, b1, true, pa, s0);
+  V3 scratch;
+  nearestOnSegment(a1, La, b2, true, scratch, s1);
+  if (s0 < 0.0 && s1 < 0.0) {
+    pa = a1;
+    pb = s0 < s1 ? b2 : b1;
+  } else if (s0 > 1.0 && s1 > 1.0) {
+    pa = a2;
+    pb = s0 < s1 ? b1 : b2;
+  } else {
+    tmp = 0.5 * (clamp01(s0) + clamp01(s1));
+    pa = add(a1, mul(tmp, La));
+    nearestOnSegment(b1, Lb, pa, true, pb, tmp);
+  }
+}
+void adjust(const V3& a1, const V3& La, const V3& b1, const V3& Lb, double s, double t, V3& pa, V3& pb) {
+  if (outside01(s) && outside01(t)) {
+    s = clamp01(s);
+    pa = add(a1, mul(s, La));
+    nearestOnSegment(b1, Lb, pa, true, pb, t);
+    if (outside01(t)) {
+      t = clamp01(t);
+      pb = add(b1, mul(t, Lb));
+      nearestOnSegment(a1, La, pb, false, pa, s);
+      nearestOnSegment(b1, Lb, pa, false, pb, t);
+    }
+  } else if (outside01(s)) {
+    s = clamp01(s);
+    pa = add(a1, mul(s, La));
+    nearestOnSegment(b1, Lb, pa, false, pb, t);
+  } else if (outside01(t)) {
+    t = clamp01(t);
+    pb = add(b1, mul(t, Lb));
+    nearestOnSegment(a1, La, pb, false, pa, s);
+  }
+}
+void closest(const V3& a1, const V3& a2, const V3& b1, const V3& b2, V3& pa, V3& pb) {
+  const V3 La = sub(a2, a1), Lb = sub(b2, b1);
+  const double L11 = dot3(La, La), L22 = dot3(Lb, Lb), tol2 = kTol * kTol;
+  double tmp = 0.0;
+  if (L11 < tol2) {
+    pa = a1;
+    nearestOnSegment(b1, Lb, a1, false, pb, tmp);
+  } else if (L22 < tol2) {
+    pb = b1;
+    nearestOnSegment(a1, La, b1, false, pa, tmp);
+  } else {
+    const V3 AB = sub(b1, a1);
+    const double L12 = -dot3(La, Lb);
+    const double det = L11 * L22 - L12 * L12;
+    if (std::fabs(det) < kTol) {
+      parallel(a1, a2, La, b1, b2, Lb, pa, pb);
+    } else {
+      const double ra = dot3(La, AB);
+      const double rb = -dot3(Lb, AB);
+      const double t = (L11 * rb - ra * L12) / det;
+      const double s = (ra - L12 * t) / L11;
+      pa = add(a1, mul(s, La));
+      pb = add(b1, mul(t, Lb));
+      if (outside01(s) || outside01(t)) adjust(a1, La, b1, Lb, s, t, pa, pb);
+    }
+  }
+}
+}  // namespace segseg
+
+// faceEdgeIntersection (COLLISION_UTIL.cpp:577-613): does the ray from e0
+// along e1 - e0 cross triangle (a, b, c) before reaching e1?
+bool faceEdgeCross(const V3& a, const V3& b, const V3& c, const V3& e0, const V3& e1) {
+  const V3 ed = sub(e1, e0);
+  const V3 dir = normalized(ed);
+  const V3 n = normalized(cross3(sub(b, a), sub(c, a)));
+  const double denom = dot3(dir, n);
+  if (std::fabs(denom) <= 0.0) return false;
+  const double t = dot3(sub(a, e0), n) / denom;
+  if (t < 0) return false;
+  const V3 h = add(e0, mul(t, dir));
+  if (dot3(n, cross3(sub(b, a), sub(h, a))) < 0) return false;
+  if (dot3(n, cross3(sub(c, b), sub(h, b))) < 0) return false;
+  if (dot3(n, cross3(sub(a, c), sub(h, c))) < 0) return false;
+  return t < norm3(ed);
+}
+
+// TET_MESH_FASTER::computeEdgeEdgeCollisions (TET_MESH_FASTER.cpp:340-500):
+// for every surface edge x the closest non-adjacent surface edge y >= x whose
+// closest points lie inside both edges (parameters in [1e-4, 1 - 1e-4]),
+// ties to the later one; kept when no endpoint pair is a surface edge (the
+// one-ring test, TET_MESH.cpp:2145-2155) and the distance is below eps.  Then
+// EDGE_SQRT_COLLISION (EDGE_SQRT_COLLISION.cpp:40-231) on the pair, negated
+// when the edge crosses a triangle next to the other edge:
+//   diff = (b0 v2 + b1 v3) - (a0 v0 + a1 v1), r = |diff|, n = diff / r,
+//   c = (-a0, -a1, b0, b1), spring = r - eps (negated: r + eps),
+//   grad = 2 mu spring (c (x) n), clamped Hessian = (c c^T) (x) G with
+//   G = 2 mu (n n^T + max(spring / r, 0) (I - n n^T)) -- the 12x12
+//   eigenvalue clamp of (c c^T) (x) G3 clamps G3 alone;
+//   zero when r < 1e-7.  Forces -w grad, Hessians -w H, w = the two edges'
+//   rest areas summed.
+void eeCollisions(Sim& s) {
+  const Mesh& M = s.M;
+  Collisions& C = s.coll;
+  if (C.edges.empty()) buildEdges(C);
+  const int ne = (int)C.edges.size() / 2;
+  auto pos = [&](int id) {
+    return V3{M.rest[3 * id] + s.x[3 * id], M.rest[3 * id + 1] + s.x[3 * id + 1], M.rest[3 * id + 2] + s.x[3 * id + 2]};
+  };
+  std::vector<std::pair<int, int>> adj;
+  for (int k = 0; k < ne; k++) {
+    adj.push_back({C.edges[2 * k], C.edges[2 * k + 1]});
+    adj.push_back({C.edges[2 * k + 1], C.edges[2 * k]});
+  }
+  std::sort(adj.begin(), adj.end());
+  auto adjacent = [&](int a, int b) { return std::binary_search(adj.begin(), adj.end(), std::make_pair(a, b)); };
+  const double farAway = (double)FLT_MAX;
+  for (int x = 0; x < ne; x++) {
+    const int o0 = C.edges[2 * x], o1 = C.edges[2 * x + 1];
+    const V3 v0 = pos(o0), v1 = pos(o1);
+    int best = -1;
+    double bestD = farAway, ba[2] = {-1, -1}, bb[2] = {-1, -1};
+    for (int y = x; y < ne; y++) {
+      const int i0 = C.edges[2 * y], i1 = C.edges[2 * y + 1];
+      if (o0 == i0 || o0 == i1 || o1 == i0 || o1 == i1) continue;
+      const V3 v2 = pos(i0), v3 = pos(i1);
+      V3 po, pi;
+      segseg::closest(v0, v1, v2, v3, po, pi);
+      const double d = norm3(sub(pi, po));
+      if (d > bestD) continue;
+      double a[2], b[2];
+      a[1] = norm3(sub(po, v0)) / norm3(sub(v1, v0));
+      a[0] = 1.0 - a[1];
+      b[1] = norm3(sub(pi, v2)) / norm3(sub(v3, v2));
+      b[0] = 1.0 - b[1];
+      const double skip = 1e-4;
+      if (a[0] < skip || a[0] > 1.0 - skip || a[1] < skip || a[1] > 1.0 - skip) continue;
+      if (b[0] < skip || b[0] > 1.0 - skip || b[1] < skip || b[1] > 1.0 - skip) continue;
+      bestD = d;
+      best = y;
+      ba[0] = a[0], ba[1] = a[1], bb[0] = b[0], bb[1] = b[1];
+    }
+    if (best < 0) continue;
+    const int i0 = C.edges[2 * best], i1 = C.edges[2 * best + 1];
+    if (adjacent(o0, i0) || adjacent(o0, i1) || adjacent(o1, i0) || adjacent(o1, i1)) continue;
+    if (!(bestD < C.eps)) continue;
+    // penetration: the outer edge through a triangle next to the inner edge
+    bool crossing = false;
+    for (int q = 0; q < 2; q++) {
+      const int t = C.edgeTri[2 * best + q];
+      if (t < 0) continue;
+      const bool hit = faceEdgeCross(pos(C.tris[3 * t]), pos(C.tris[3 * t + 1]), pos(C.tris[3 * t + 2]), v0, v1);
+      crossing = crossing || hit;
+    }
+    const double w = C.edgeArea[x] + C.edgeArea[best];
+    const int ids[4] = {o0, o1, i0, i1};
+    const double cv[4] = {-ba[0], -ba[1], bb[0], bb[1]};
+    V3 diff = {0, 0, 0};
+    for (int a = 0; a < 4; a++) diff = add(diff, mul(cv[a], pos(ids[a])));
+    const double r = norm3(diff);
+    const size_t k = C.weight.size();
+    C.eePairs.push_back(x);
+    C.eePairs.push_back(best);
+    for (int a = 0; a < 4; a++) C.ctets.push_back(ids[a]);
+    C.weight.push_back(w);
+    C.f12.resize(12 * (k + 1), 0.0);
+    C.H12.resize(144 * (k + 1), 0.0);
+    if (r < 1e-7) continue;
+    const V3 n = mul(1.0 / r, diff);
+    const double spring = crossing ? r + C.eps : r - C.eps;
+    const double k2 = std::max(spring / r, 0.0);
+    double G[9];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) G[i + 3 * j] = 2.0 * C.mu * ((1.0 - k2) * n[i] * n[j] + (i == j ? k2 : 0.0));
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++) C.f12[12 * k + 3 * a + i] = -w * (2.0 * C.mu * spring * cv[a] * n[i]);
+    for (int a = 0; a < 4; a++)
+      for (int b = 0; b < 4; b++)
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++)
+            C.H12[144 * k + (3 * a + i) + 12 * (3 * b + j)] = -w * cv[a] * cv[b] * G[i + 3 * j];
+  }
+}
+
 // K = sum of element Hessians per block, gathered per row in ascending tet
 // order like TET_MESH_FASTER's _hessianGathers (TET_MESH_FASTER.cpp:113-131);
 // R = sum of element forces per vertex in ascending tet order
@@ -1188,9 +1432,18 @@ void collisionTerms(Sim& s, double collScale, std::vector<double>* collKv) {
   Collisions& C = s.coll;
   C.weight.clear();
   s.collDiag.clear();
-  if (!C.on) return;
-  vfDetect(s);
-  vfResponse(s);
+  if (!C.on && !C.ee) return;
+  if (C.on) {
+    vfDetect(s);
+    vfResponse(s);
+  } else {
+    C.pairs.clear();
+    C.ctets.clear();
+    C.f12.clear();
+    C.H12.clear();
+  }
+  C.eePairs.clear();
+  if (C.ee) eeCollisions(s);  // appended after the vertex-face pairs (TIMESTEPPER.cpp:665-690)
   s.collScale = collScale;
   std::vector<double> fc(3 * (size_t)nv, 0.0);
   if (collKv) collKv->assign(3 * (size_t)nv, 0.0);
@@ -1527,6 +1780,21 @@ int oracle_nblocks(void* h) { return static_cast<Sim*>(h)->M.rowptr.back(); }
 
 // Integrator: 0 BACKWARD_EULER_VELOCITY, 1 BACKWARD_EULER_POSITION with
 // Rayleigh coefficients alpha, beta, 2 NEWMARK (collisions off for 1 and 2).
+// Edge-edge pairs of the last step, as surface edge indices, and the surface
+// edges themselves (2 ids each).  Returns the pair count (or the edge count
+// with pairs == NULL), -1 on a bad handle.
+int oracle_ee_pairs(void* h, int* pairs, int* edges) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s) return -1;
+  const Collisions& C = s->coll;
+  if (!pairs) {
+    if (edges) std::copy(C.edges.begin(), C.edges.end(), edges);
+    return (int)C.edges.size() / 2;
+  }
+  std::copy(C.eePairs.begin(), C.eePairs.end(), pairs);
+  return (int)C.eePairs.size() / 2;
+}
+
 int oracle_set_integrator(void* h, int integrator, double alpha, double beta) {
   Sim* s = static_cast<Sim*>(h);
   if (!s || integrator < 0 || integrator > 2) return -1;
@@ -1544,11 +1812,12 @@ int oracle_set_collisions(void* h, int vf_on, double eps, double mu, double beta
   Sim* s = static_cast<Sim*>(h);
   if (!s) return -1;
   if (vf_on && s->integrator == 2) return -2;  // NEWMARK: no contact
-  s->coll.on = vf_on != 0;
+  s->coll.on = (vf_on & 1) != 0;
+  s->coll.ee = (vf_on & 2) != 0;  // bit 1: edge-edge collisions
   s->coll.eps = eps;
   s->coll.mu = mu;
   s->coll.beta = beta;
-  if (s->coll.on && s->coll.tris.empty()) buildSurface(s->M, s->coll);
+  if ((s->coll.on || s->coll.ee) && s->coll.tris.empty()) buildSurface(s->M, s->coll);
   return 0;
 }
 

@@ -46,6 +46,7 @@ def lib():
         L.oracle_get_state.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.oracle_attach_pins.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip]
         L.oracle_set_pin_targets.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
+        L.oracle_ee_pairs.argtypes = [ctypes.c_void_p, _ip, _ip]
         L.oracle_set_solver.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.oracle_set_external_forces.argtypes = [ctypes.c_void_p, _dp]
         L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp]
@@ -127,9 +128,23 @@ class Sim:
         t = np.ascontiguousarray(targets, dtype=np.float64).reshape(-1)
         assert lib().oracle_set_pin_targets(self.h, len(t) // 3, _d(t)) == 0
 
-    def set_collisions(self, vf=True, eps=0.01, mu=1.0, beta=0.001):
-        """Vertex-face self collisions (TIMESTEPPER.cpp:83-86 defaults: mu 1, beta 0.001)."""
-        assert lib().oracle_set_collisions(self.h, int(vf), eps, mu, beta) == 0
+    def ee_pairs(self):
+        """Edge-edge pairs of the last step as vertex quadruples
+        (edge0[0], edge0[1], edge1[0], edge1[1])."""
+        L = lib()
+        ne = L.oracle_ee_pairs(self.h, None, None)
+        edges = np.zeros(2 * max(ne, 1), dtype=np.int32)
+        L.oracle_ee_pairs(self.h, None, _i(edges))
+        pairs = np.zeros(2 * max(ne, 1), dtype=np.int32)
+        n = L.oracle_ee_pairs(self.h, _i(pairs), None)
+        e = edges[:2 * ne].reshape(-1, 2)
+        p = pairs[:2 * n].reshape(-1, 2)
+        return np.concatenate([e[p[:, 0]], e[p[:, 1]]], axis=1) if n else np.zeros((0, 4), np.int32)
+
+    def set_collisions(self, vf=True, eps=0.01, mu=1.0, beta=0.001, ee=False):
+        """Vertex-face (and with ee, edge-edge) self collisions
+        (TIMESTEPPER.cpp:83-86 defaults: mu 1, beta 0.001)."""
+        assert lib().oracle_set_collisions(self.h, int(bool(vf)) | (2 if ee else 0), eps, mu, beta) == 0
 
     def vf_pairs(self):
         """(vertex, surface triangle) pairs at the current state, and the surface triangles."""
