@@ -92,6 +92,8 @@ SIGNATURES = {
     "hobak_batch_get_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "hobak_batch_set_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "hobak_batch_set_pin_targets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "hobak_batch_set_edge_collisions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "hobak_batch_edge_pairs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip, ctypes.c_int]),
     "hobak_batch_snapshot_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
     "hobak_batch_snapshot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "hobak_batch_restore": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),

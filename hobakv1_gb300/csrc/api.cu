@@ -113,6 +113,7 @@ struct hobak_batch_t {
   // vertex-face collisions
   std::vector<CollisionScene> collScenes;
   std::vector<int> surfTri, surfTriStart, svHost, svStart;  // global ids; per-scene ranges
+  std::vector<int> edgeHost, edgeStart;                     // surface edges (lo, hi), global ids; per-scene ranges
   void* collArena = nullptr;
   size_t collBytes = 0;
   int* pinnedActive = nullptr;   // pinned host word for the convergence poll
@@ -707,7 +708,8 @@ int prepare_cluster_classes(hobak_batch_t* B) {
   const int vpcLimit = (int)((kClusterSmemMax - cluster_fixed_bytes()) / cluster_vertex_bytes(mixed));
   std::vector<int> cl(n, 0);
   for (int s = 0; s < n; s++) {
-    const bool contact = B->collArena && s < (int)B->collScenes.size() && B->collScenes[s].vfOn;
+    const bool contact =
+        B->collArena && s < (int)B->collScenes.size() && (B->collScenes[s].vfOn || B->collScenes[s].eeOn);
     if (!B->clusterPcg || contact) continue;
     const int nv = B->scenes[s].nv;
     // the smallest cluster that gives each thread one vertex at most; under
@@ -1015,10 +1017,12 @@ int build_collisions(hobak_batch_t* B) {
   const auto& rest = B->restHost;
   B->surfTri.clear();
   B->svHost.clear();
+  B->edgeHost.clear();
   B->surfTriStart.assign(1, 0);
   B->svStart.assign(1, 0);
-  std::vector<int> triScene, triNbr, svScene;
-  std::vector<double> triArea, svArea;
+  B->edgeStart.assign(1, 0);
+  std::vector<int> triScene, triNbr, svScene, edgeScene, edgeTri;
+  std::vector<double> triArea, svArea, edgeArea;
   auto area = [&](int a, int b2, int c) {
     double e1[3], e2[3];
     for (int i = 0; i < 3; i++) {
@@ -1094,14 +1098,42 @@ int build_collisions(hobak_batch_t* B) {
         svArea[id] += (1.0 / 3.0) * A;
       }
     }
+    // surface edges (lo, hi) ascending (TET_MESH::computeSurfaceEdges,
+    // TET_MESH.cpp:595-630), rest area = a third of each adjacent triangle's
+    // in triangle order (TET_MESH.cpp:530-562), first two adjacent triangles
+    // (computeSurfaceEdgeTriangleNeighbors, TET_MESH.cpp:356-412)
+    {
+      std::vector<std::array<int, 3>> ek;  // lo, hi, triangle
+      for (int i = 0; i < ntri; i++)
+        for (int j = 0; j < 3; j++) {
+          int a = B->surfTri[3 * (triBase + i) + j], c = B->surfTri[3 * (triBase + i) + (j + 1) % 3];
+          if (a > c) std::swap(a, c);
+          ek.push_back({a, c, triBase + i});
+        }
+      std::sort(ek.begin(), ek.end());
+      for (size_t i = 0; i < ek.size();) {
+        size_t j = i;
+        double A = 0.0;
+        while (j < ek.size() && ek[j][0] == ek[i][0] && ek[j][1] == ek[i][1]) A += triArea[ek[j++][2]] / 3.0;
+        B->edgeHost.push_back(ek[i][0]);
+        B->edgeHost.push_back(ek[i][1]);
+        edgeScene.push_back(s);
+        edgeArea.push_back(A);
+        edgeTri.push_back(ek[i][2]);
+        edgeTri.push_back(j - i > 1 ? ek[i + 1][2] : -1);
+        i = j;
+      }
+    }
     B->surfTriStart.push_back((int)B->surfTri.size() / 3);
     B->svStart.push_back((int)B->svHost.size());
+    B->edgeStart.push_back((int)B->edgeHost.size() / 2);
   }
+  const int nedge = (int)B->edgeHost.size() / 2;
   const int ntri = (int)B->surfTri.size() / 3, nsv = (int)B->svHost.size(), nv = B->nv;
   int hash = 1024;
   while (hash < 16 * std::max(ntri, 1)) hash <<= 1;
-  const int cap = std::max(nsv * kMaxPairsPerVertex, 1);
-  const int scanBlocks = (std::max(std::max(hash, nsv), nv) + 1023) / 1024 + 1;
+  const int cap = std::max(nsv * kMaxPairsPerVertex + nedge, 1);
+  const int scanBlocks = (std::max(std::max(std::max(hash, nsv), nv), nedge) + 1023) / 1024 + 1;
   Arena A;
   const size_t oScenes = A.reserve(sizeof(CollisionScene) * n);
   const size_t oTri = A.reserve(sizeof(int) * 3 * (size_t)ntri), oTriScene = A.reserve(sizeof(int) * ntri);
@@ -1122,6 +1154,10 @@ int build_collisions(hobak_batch_t* B) {
   const size_t oIncCount = A.reserve(sizeof(int) * (nv + 1)), oIncCursor = A.reserve(sizeof(int) * nv);
   const size_t oIncList = A.reserve(sizeof(int) * 4 * (size_t)cap);
   const size_t oScan = A.reserve(sizeof(int) * scanBlocks);
+  const size_t oEdge = A.reserve(sizeof(int2) * (size_t)nedge), oEdgeScene = A.reserve(sizeof(int) * nedge);
+  const size_t oEdgeArea = A.reserve(sizeof(double) * nedge), oEdgeTri = A.reserve(sizeof(int2) * (size_t)nedge);
+  const size_t oEeSel = A.reserve(sizeof(int) * nedge), oEeKeep = A.reserve(nedge), oEeCross = A.reserve(nedge);
+  const size_t oEeAB = A.reserve(sizeof(double4) * (size_t)nedge), oEeCount = A.reserve(sizeof(int) * (nedge + 1));
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, A.used);
   if (e != cudaSuccess)
@@ -1165,12 +1201,24 @@ int build_collisions(hobak_batch_t* B) {
   c.incCursor = carve<int>(base, oIncCursor);
   c.incList = carve<int>(base, oIncList);
   c.scanTmp = carve<int>(base, oScan);
+  c.nedge = nedge;
+  c.edge = carve<int2>(base, oEdge);
+  c.edgeScene = carve<int>(base, oEdgeScene);
+  c.edgeArea = carve<double>(base, oEdgeArea);
+  c.edgeTri = carve<int2>(base, oEdgeTri);
+  c.eeSel = carve<int>(base, oEeSel);
+  c.eeKeep = carve<unsigned char>(base, oEeKeep);
+  c.eeCross = carve<unsigned char>(base, oEeCross);
+  c.eeAB = carve<double4>(base, oEeAB);
+  c.eeCount = carve<int>(base, oEeCount);
   B->collScenes.assign(n, CollisionScene{0, 0, 0, 0, 0, 0.01, 1.0, 0.001});
   for (int s = 0; s < n; s++) {
     B->collScenes[s].tri0 = B->surfTriStart[s];
     B->collScenes[s].ntri = B->surfTriStart[s + 1] - B->surfTriStart[s];
     B->collScenes[s].sv0 = B->svStart[s];
     B->collScenes[s].nsv = B->svStart[s + 1] - B->svStart[s];
+    B->collScenes[s].e0 = B->edgeStart[s];
+    B->collScenes[s].ne = B->edgeStart[s + 1] - B->edgeStart[s];
   }
   auto up = [&](const void* dst, const void* src, size_t bytes) {
     return bytes ? cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
@@ -1183,6 +1231,12 @@ int build_collisions(hobak_batch_t* B) {
   CUDA_TRY(up(c.sv, B->svHost.data(), sizeof(int) * B->svHost.size()));
   CUDA_TRY(up(c.svScene, svScene.data(), sizeof(int) * svScene.size()));
   CUDA_TRY(up(c.svArea, svArea.data(), sizeof(double) * svArea.size()));
+  if (nedge > 0) {
+    CUDA_TRY(up(c.edge, B->edgeHost.data(), sizeof(int2) * (size_t)nedge));
+    CUDA_TRY(up(c.edgeScene, edgeScene.data(), sizeof(int) * nedge));
+    CUDA_TRY(up(c.edgeArea, edgeArea.data(), sizeof(double) * nedge));
+    CUDA_TRY(up(c.edgeTri, edgeTri.data(), sizeof(int2) * (size_t)nedge));
+  }
   B->d.collOn = 1;
   return HOBAK_OK;
 }
@@ -1629,7 +1683,7 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   if (rc) return rc;
   if (opts->integrator == HOBAK_INTEGRATOR_NEWMARK)
     for (const CollisionScene& cs : b->collScenes)
-      if (cs.vfOn) return fail(HOBAK_ERR_INVALID, "vertex-face contact is not available with NEWMARK");
+      if (cs.vfOn || cs.eeOn) return fail(HOBAK_ERR_INVALID, "self collisions are not available with NEWMARK");
   b->opts = *opts;
   b->clusterDirty = true;
   drop_graphs(b);
@@ -1661,11 +1715,59 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
   cs.beta = damping_beta;
   std::vector<CollisionScene> eff = b->collScenes;
   for (size_t k = 0; k < eff.size(); k++)
-    if (!b->sceneParams[k].active) eff[k].vfOn = 0;
+    if (!b->sceneParams[k].active) eff[k].vfOn = eff[k].eeOn = 0;
   CUDA_TRY(cudaMemcpy(const_cast<CollisionScene*>(b->d.coll.scenes), eff.data(), sizeof(CollisionScene) * eff.size(),
                       cudaMemcpyHostToDevice));
   b->clusterDirty = true;
   drop_graphs(b);
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_edge_collisions(hobak_batch b, int scene, int ee_on) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  if (ee_on && b->opts.integrator == HOBAK_INTEGRATOR_NEWMARK)
+    return fail(HOBAK_ERR_INVALID, "self collisions are not available with NEWMARK");
+  if (!b->collArena) {
+    int rc = build_collisions(b);
+    if (rc) return rc;
+  }
+  CollisionScene& cs = b->collScenes[scene];
+  if (ee_on && !(cs.eps > 0.0)) return fail(HOBAK_ERR_INVALID, "collision distance must be > 0");
+  cs.eeOn = ee_on ? 1 : 0;
+  CollisionScene eff = cs;
+  if (!b->sceneParams[scene].active) eff.vfOn = eff.eeOn = 0;
+  CUDA_TRY(cudaMemcpy(const_cast<CollisionScene*>(b->d.coll.scenes) + scene, &eff, sizeof(CollisionScene),
+                      cudaMemcpyHostToDevice));
+  b->clusterDirty = true;
+  drop_graphs(b);
+  return HOBAK_OK;
+}
+
+int hobak_batch_edge_pairs(hobak_batch b, int scene, int* npairs, int* quads, int cap) {
+  if (!b || !npairs || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  *npairs = 0;
+  if (!b->collArena) return HOBAK_OK;
+  const int e0 = b->edgeStart[scene], e1 = b->edgeStart[scene + 1], ne = e1 - e0;
+  if (ne == 0) return HOBAK_OK;
+  std::vector<int> sel(ne);
+  std::vector<unsigned char> keep(ne);
+  CUDA_TRY(cudaMemcpyAsync(sel.data(), b->d.coll.eeSel + e0, sizeof(int) * ne, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(keep.data(), b->d.coll.eeKeep + e0, ne, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  const int v0 = b->scenes[scene].v0;
+  int n = 0;
+  for (int x = 0; x < ne; x++) {
+    if (!keep[x]) continue;
+    if (quads && n < cap) {
+      const int y = sel[x];
+      quads[4 * n] = b->edgeHost[2 * (e0 + x)] - v0;
+      quads[4 * n + 1] = b->edgeHost[2 * (e0 + x) + 1] - v0;
+      quads[4 * n + 2] = b->edgeHost[2 * y] - v0;
+      quads[4 * n + 3] = b->edgeHost[2 * y + 1] - v0;
+    }
+    n++;
+  }
+  *npairs = n;
   return HOBAK_OK;
 }
 
@@ -1749,7 +1851,7 @@ int hobak_batch_set_active(hobak_batch b, int scene, int active) {
                       cudaMemcpyHostToDevice));
   if (b->collArena) {  // a parked scene takes no part in collision detection either
     CollisionScene cs = b->collScenes[scene];
-    if (!active) cs.vfOn = 0;
+    if (!active) cs.vfOn = cs.eeOn = 0;
     CUDA_TRY(cudaMemcpy(const_cast<CollisionScene*>(b->d.coll.scenes) + scene, &cs, sizeof(CollisionScene),
                         cudaMemcpyHostToDevice));
   }

@@ -455,6 +455,238 @@ __global__ void k_coll_diag(DeviceBatch b, DeviceCollisions c) {
     for (int q = 0; q < 3; q++) out[3 * r + q] = D[r + 3 * q];  // row major like the LHS blocks
 }
 
+// ---- 6. edge-edge (TET_MESH_FASTER.cpp:340-500, EDGE_SQRT_COLLISION.cpp) ----
+// Closest points of two segments, restating the published routine the
+// reference uses (Rhodes, "Fast, Robust Intersection of 3D Line Segments",
+// Game Programming Gems II; LINE_INTERSECT.cpp) with its tolerances: 1e-8
+// for parallel/degenerate lines, also where its helpers take a squared one.
+namespace seg {
+constexpr double kTol = 1e-8;
+__device__ __forceinline__ bool outside01(double a) { return a < 0.0 || a > 1.0; }
+__device__ __forceinline__ double clamp01(double a) { return fmax(0.0, fmin(1.0, a)); }
+__device__ void nearest(D3 p, D3 L, D3 q, bool infinite, D3& out, double& param) {
+  const double D = dot(L, L);
+  if (D < kTol) {
+    out = p;
+    return;
+  }
+  param = dot(L, q - p) / D;
+  if (!infinite) param = clamp01(param);
+  out = p + param * L;
+}
+__device__ void closest(D3 a1, D3 a2, D3 b1, D3 b2, D3& pa, D3& pb) {
+  const D3 La = a2 - a1, Lb = b2 - b1;
+  const double L11 = dot(La, La), L22 = dot(Lb, Lb);
+  double tmp = 0.0;
+  if (L11 < kTol * kTol) {
+    pa = a1;
+    nearest(b1, Lb, a1, false, pb, tmp);
+    return;
+  }
+  if (L22 < kTol * kTol) {
+    pb = b1;
+    nearest(a1, La, b1, false, pa, tmp);
+    return;
+  }
+  const D3 AB = b1 - a1;
+  const double L12 = -dot(La, Lb);
+  const double det = L11 * L22 - L12 * L12;
+  if (fabs(det) < kTol) {  // parallel
+    double s0 = 0.0, s1 = 0.0;
+    D3 scratch;
+    nearest(a1, La, b1, true, pa, s0);
+    nearest(a1, La, b2, true, scratch, s1);
+    if (s0 < 0.0 && s1 < 0.0) {
+      pa = a1;
+      pb = s0 < s1 ? b2 : b1;
+    } else if (s0 > 1.0 && s1 > 1.0) {
+      pa = a2;
+      pb = s0 < s1 ? b1 : b2;
+    } else {
+      tmp = 0.5 * (clamp01(s0) + clamp01(s1));
+      pa = a1 + tmp * La;
+      nearest(b1, Lb, pa, true, pb, tmp);
+    }
+    return;
+  }
+  const double ra = dot(La, AB), rb = -dot(Lb, AB);
+  double t = (L11 * rb - ra * L12) / det;
+  double s = (ra - L12 * t) / L11;
+  pa = a1 + s * La;
+  pb = b1 + t * Lb;
+  if (!(outside01(s) || outside01(t))) return;
+  if (outside01(s) && outside01(t)) {
+    s = clamp01(s);
+    pa = a1 + s * La;
+    nearest(b1, Lb, pa, true, pb, t);
+    if (outside01(t)) {
+      t = clamp01(t);
+      pb = b1 + t * Lb;
+      nearest(a1, La, pb, false, pa, s);
+      nearest(b1, Lb, pa, false, pb, t);
+    }
+  } else if (outside01(s)) {
+    s = clamp01(s);
+    pa = a1 + s * La;
+    nearest(b1, Lb, pa, false, pb, t);
+  } else {
+    t = clamp01(t);
+    pb = b1 + t * Lb;
+    nearest(a1, La, pb, false, pa, s);
+  }
+}
+}  // namespace seg
+
+// faceEdgeIntersection (COLLISION_UTIL.cpp:577-613)
+__device__ bool face_edge_cross(D3 a, D3 b, D3 c, D3 e0, D3 e1) {
+  const D3 ed = e1 - e0, dir = unit(ed);
+  const D3 n = unit(cross(b - a, c - a));
+  const double denom = dot(dir, n);
+  if (fabs(denom) <= 0.0) return false;
+  const double t = dot(a - e0, n) / denom;
+  if (t < 0) return false;
+  const D3 h = e0 + t * dir;
+  if (dot(n, cross(b - a, h - a)) < 0) return false;
+  if (dot(n, cross(c - b, h - b)) < 0) return false;
+  if (dot(n, cross(a - c, h - c)) < 0) return false;
+  return t < norm(ed);
+}
+
+// is (u, w) a surface edge of the scene (the one-ring test of
+// TET_MESH::computeSurfaceVertexOneRings, TET_MESH.cpp:2145-2155)
+__device__ bool surface_edge(const DeviceCollisions& c, const CollisionScene& cs, int u, int w) {
+  const int lo = min(u, w), hi = max(u, w);
+  int l = cs.e0, r = cs.e0 + cs.ne;
+  while (l < r) {
+    const int m = (l + r) >> 1;
+    const int2 e = c.edge[m];
+    if (e.x < lo || (e.x == lo && e.y < hi)) l = m + 1;
+    else r = m;
+  }
+  return l < cs.e0 + cs.ne && c.edge[l].x == lo && c.edge[l].y == hi;
+}
+
+// One thread per surface edge x: the closest non-adjacent edge y >= x of the
+// scene whose closest points lie inside both edges (parameters within
+// [1e-4, 1 - 1e-4]; equal distances go to the later edge), kept when no
+// endpoint pair is a surface edge and the distance is below eps.  All edges
+// of the scene are candidates (the reference's AABB query only removes edges
+// farther than eps, which cannot be kept).
+__global__ void k_ee_detect(DeviceBatch b, DeviceCollisions c) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= c.nedge) return;
+  c.eeSel[x] = -1;
+  c.eeKeep[x] = 0;
+  c.eeCount[x] = 0;
+  const int s = c.edgeScene[x];
+  const CollisionScene& cs = c.scenes[s];
+  if (!cs.eeOn) return;
+  const int2 o = c.edge[x];
+  const D3 v0 = pos(b, o.x), v1 = pos(b, o.y);
+  const double len0 = norm(v1 - v0);
+  int best = -1;
+  double bestD = (double)3.402823466e+38f, ab[4] = {-1, -1, -1, -1};
+  for (int y = x; y < cs.e0 + cs.ne; y++) {
+    const int2 in = c.edge[y];
+    if (o.x == in.x || o.x == in.y || o.y == in.x || o.y == in.y) continue;
+    const D3 v2 = pos(b, in.x), v3 = pos(b, in.y);
+    D3 po, pi;
+    seg::closest(v0, v1, v2, v3, po, pi);
+    const double d = norm(pi - po);
+    if (d > bestD) continue;
+    const double a1 = norm(po - v0) / len0, a0 = 1.0 - a1;
+    const double b1 = norm(pi - v2) / norm(v3 - v2), b0 = 1.0 - b1;
+    const double skip = 1e-4;
+    if (a0 < skip || a0 > 1.0 - skip || a1 < skip || a1 > 1.0 - skip) continue;
+    if (b0 < skip || b0 > 1.0 - skip || b1 < skip || b1 > 1.0 - skip) continue;
+    bestD = d;
+    best = y;
+    ab[0] = a0, ab[1] = a1, ab[2] = b0, ab[3] = b1;
+  }
+  if (best < 0) return;
+  const int2 in = c.edge[best];
+  if (surface_edge(c, cs, o.x, in.x) || surface_edge(c, cs, o.x, in.y) || surface_edge(c, cs, o.y, in.x) ||
+      surface_edge(c, cs, o.y, in.y))
+    return;
+  if (!(bestD < cs.eps)) return;
+  bool crossing = false;
+  const int2 tt = c.edgeTri[best];
+  const int tq[2] = {tt.x, tt.y};
+  for (int q = 0; q < 2; q++) {
+    if (tq[q] < 0) continue;
+    const int* tv = c.tri + 3 * (size_t)tq[q];
+    const bool hit = face_edge_cross(pos(b, tv[0]), pos(b, tv[1]), pos(b, tv[2]), v0, v1);
+    crossing = crossing || hit;
+  }
+  c.eeSel[x] = best;
+  c.eeKeep[x] = 1;
+  c.eeCount[x] = 1;
+  c.eeCross[x] = crossing ? 1 : 0;
+  c.eeAB[x] = make_double4(ab[0], ab[1], ab[2], ab[3]);
+}
+
+// The kept edge pairs after the vertex-face pairs, in edge order:
+// EDGE_SQRT_COLLISION with c = (-a0, -a1, b0, b1), diff = sum c_a x_a,
+// r = |diff|, n = diff / r, spring = r - eps (r + eps when crossing),
+// force -w 2 mu spring c (x) n, clamped Hessian -w (c c^T) (x)
+// 2 mu (n n^T + max(spring / r, 0) (I - n n^T)) (the 12x12 eigenvalue clamp
+// of (c c^T) (x) G3 clamps G3 alone), zero when r < 1e-7.
+__global__ void k_ee_pairs(DeviceBatch b, DeviceCollisions c) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= c.nedge || !c.eeKeep[x]) return;
+  const int pidx = *c.npairs + c.eeCount[x];
+  if (pidx >= c.pairCap) {
+    atomicExch(c.overflow, 1);
+    return;
+  }
+  const int s = c.edgeScene[x];
+  const CollisionScene& cs = c.scenes[s];
+  const int y = c.eeSel[x];
+  const int2 o = c.edge[x], in = c.edge[y];
+  const int id[4] = {o.x, o.y, in.x, in.y};
+  c.pairTet[pidx] = make_int4(o.x, o.y, in.x, in.y);
+  const double4 ab = c.eeAB[x];
+  const double cvec[4] = {-ab.x, -ab.y, ab.z, ab.w};
+  double* C = c.pairC + 4 * (size_t)pidx;
+  double* G = c.pairG + 9 * (size_t)pidx;
+  double* R = c.pairRhs + 12 * (size_t)pidx;
+  double* Fo = c.pairF + 12 * (size_t)pidx;
+  for (int a = 0; a < 4; a++) C[a] = cvec[a];
+  D3 diff = {0.0, 0.0, 0.0};
+  for (int a = 0; a < 4; a++) diff = diff + cvec[a] * pos(b, id[a]);
+  const double r = norm(diff);
+  if (r < 1e-7) {  // EDGE_SQRT_COLLISION.cpp:_tooSmall
+    for (int k = 0; k < 9; k++) G[k] = 0.0;
+    for (int k = 0; k < 12; k++) R[k] = Fo[k] = 0.0;
+    return;
+  }
+  const double w = c.edgeArea[x] + c.edgeArea[y];
+  const D3 n = (1.0 / r) * diff;
+  const double spring = c.eeCross[x] ? r + cs.eps : r - cs.eps;
+  const double k2 = fmax(spring / r, 0.0);
+  const double n3[3] = {n.x, n.y, n.z};
+  const double gs = -w * 2.0 * cs.mu;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) G[i + 3 * j] = gs * ((1.0 - k2) * n3[i] * n3[j] + (i == j ? k2 : 0.0));
+  double zv[3] = {0, 0, 0};
+  for (int q = 0; q < 4; q++)
+    for (int k = 0; k < 3; k++) zv[k] += cvec[q] * b.v[3 * id[q] + k];
+  double Gz[3];
+  for (int i = 0; i < 3; i++) Gz[i] = G[i] * zv[0] + G[i + 3] * zv[1] + G[i + 6] * zv[2];
+  const double dt = b.scenes[s].dt;
+  const bool position = b.scenes[s].integrator == kIntegratorPosition;
+  const double fs = gs * spring;
+  for (int a = 0; a < 4; a++)
+    for (int k = 0; k < 3; k++) {
+      Fo[3 * a + k] = fs * cvec[a] * n3[k];
+      R[3 * a + k] = position ? Fo[3 * a + k] : dt * (Fo[3 * a + k] + dt * cvec[a] * Gz[k]);
+    }
+}
+
+__global__ void k_add_total(const int* src, int* dst) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *dst += *src;
+}
+
 }  // namespace
 
 void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStream_t s) {
@@ -474,6 +706,12 @@ void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStre
   scan_counts(c.svCount, c.nsv, c.scanTmp, s);
   k_copy_total<<<1, 32, 0, s>>>(c.svCount + c.nsv, c.npairs);
   k_vf_pairs<<<(c.nsv + 127) / 128, 128, 0, s>>>(b, c);
+  if (c.nedge > 0) {  // edge-edge pairs follow the vertex-face ones (TIMESTEPPER.cpp:665-690)
+    k_ee_detect<<<(c.nedge + 127) / 128, 128, 0, s>>>(b, c);
+    scan_counts(c.eeCount, c.nedge, c.scanTmp, s);
+    k_ee_pairs<<<(c.nedge + 127) / 128, 128, 0, s>>>(b, c);
+    k_add_total<<<1, 32, 0, s>>>(c.eeCount + c.nedge, c.npairs);
+  }
   k_inc_count<<<(4 * c.pairCap + 255) / 256, 256, 0, s>>>(c);
   scan_counts(c.incCount, c.nv, c.scanTmp, s);
   k_inc_fill<<<(4 * c.pairCap + 255) / 256, 256, 0, s>>>(c);

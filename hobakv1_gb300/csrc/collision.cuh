@@ -19,6 +19,8 @@ struct CollisionScene {
   int tri0, ntri;   // surface triangle range
   int sv0, nsv;     // surface vertex range
   double eps, mu, beta;
+  int eeOn;         // edge-edge self collisions (same eps, mu, beta)
+  int e0, ne;       // surface edge range
 };
 
 struct DeviceCollisions {
@@ -32,6 +34,11 @@ struct DeviceCollisions {
   const int* sv;           // [nsv] global vertex ids, ascending per scene
   const int* svScene;      // [nsv]
   const double* svArea;    // [nsv] rest one-ring area
+  int nedge;
+  const int2* edge;        // [nedge] surface edges (lo, hi), global ids, ascending per scene
+  const int* edgeScene;    // [nedge]
+  const double* edgeArea;  // [nedge] a third of each adjacent triangle's rest area
+  const int2* edgeTri;     // [nedge] first two adjacent surface triangles (-1: none)
   // per step
   unsigned* cellBits;      // [nscenes] largest triangle extent (float bits) -> cell size
   unsigned char* vInverted;  // [nv]
@@ -53,6 +60,12 @@ struct DeviceCollisions {
   int* incCursor;          // [nv]
   int* incList;            // [4 * pairCap] pair * 4 + slot
   int* scanTmp;            // block sums for the device-wide scans
+  // edge-edge, per step: each surface edge's closest admissible partner
+  int* eeSel;              // [nedge] partner edge or -1
+  unsigned char* eeKeep;   // [nedge] 1: the pair is a collision
+  unsigned char* eeCross;  // [nedge] 1: the edge crosses a triangle next to its partner
+  double4* eeAB;           // [nedge] (a0, a1, b0, b1)
+  int* eeCount;            // [nedge + 1] keep flags, then exclusive scan
 };
 
 struct DeviceBatch;

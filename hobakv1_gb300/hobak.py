@@ -403,6 +403,20 @@ class BATCH:
                                             ctypes.byref(nt), iptr(tris)), "hobak_batch_collision_pairs")
         return pairs[:2 * n.value].reshape(-1, 2), tris[:3 * nt.value].reshape(-1, 3)
 
+    def set_edge_collisions(self, scene: int, on: bool = True):
+        """Edge-edge self collisions (edgeEdgeSelfCollisionsOn) with the
+        scene's collision distance, stiffness and damping."""
+        check(_lib.load().hobak_batch_set_edge_collisions(self.h, scene, int(on)), "hobak_batch_set_edge_collisions")
+
+    def edge_pairs(self, scene: int) -> np.ndarray:
+        """Edge-edge pairs of the last detection, [n, 4] scene-local vertex ids."""
+        L = _lib.load()
+        n = ctypes.c_int(0)
+        check(L.hobak_batch_edge_pairs(self.h, scene, ctypes.byref(n), None, 0), "hobak_batch_edge_pairs")
+        q = np.zeros(4 * max(n.value, 1), dtype=np.int32)
+        check(L.hobak_batch_edge_pairs(self.h, scene, ctypes.byref(n), iptr(q), n.value), "hobak_batch_edge_pairs")
+        return q[:4 * n.value].reshape(-1, 4)
+
     def collision_response(self, scene: int):
         """Collision tets, forces (-w grad psi) and clamped Hessians of the last detection."""
         pairs, _ = self.collision_pairs(scene)
@@ -506,8 +520,9 @@ class BACKWARD_EULER_VELOCITY:
         self._batch: Optional[BATCH] = None
         self._currentTimestep = 0
         self._lastStats = None
-        # contact flags (TIMESTEPPER.cpp:83-86 defaults; edge-edge is not built)
+        # contact flags (TIMESTEPPER.cpp:83-86 defaults)
         self._vertexFaceSelfCollisionsOn = False
+        self._edgeEdgeSelfCollisionsOn = False
         self._collisionStiffness = 1.0
         self._collisionDampingBeta = 0.001
         self._collisionEps = 0.01  # TET_MESH's default collision distance
@@ -518,6 +533,13 @@ class BACKWARD_EULER_VELOCITY:
 
     def setVertexFaceSelfCollisionsOn(self, on: bool):
         self._vertexFaceSelfCollisionsOn = bool(on)
+        self._push_collisions()
+
+    def edgeEdgeSelfCollisionsOn(self) -> bool:
+        return self._edgeEdgeSelfCollisionsOn
+
+    def setEdgeEdgeSelfCollisionsOn(self, on: bool):
+        self._edgeEdgeSelfCollisionsOn = bool(on)
         self._push_collisions()
 
     def collisionStiffness(self) -> float:
@@ -545,6 +567,7 @@ class BACKWARD_EULER_VELOCITY:
         check(_lib.load().hobak_gpu_set_collisions(self._batch.h, int(self._vertexFaceSelfCollisionsOn),
                                                    self._collisionEps, self._collisionStiffness,
                                                    self._collisionDampingBeta), "hobak_gpu_set_collisions")
+        self._batch.set_edge_collisions(0, self._edgeEdgeSelfCollisionsOn)
 
     def position(self):
         return self._position
@@ -636,7 +659,7 @@ class BACKWARD_EULER_VELOCITY:
         s.x0, s.v0 = self._position, self._velocity
         self._pinnedAt = self._position.reshape(-1, 3)[s.pinned].copy()
         self._batch = BATCH([s], self._opts)
-        if self._vertexFaceSelfCollisionsOn:
+        if self._vertexFaceSelfCollisionsOn or self._edgeEdgeSelfCollisionsOn:
             self._push_collisions()
 
     def solve(self, verbose: bool = False) -> bool:
@@ -710,8 +733,13 @@ class NEWMARK(BACKWARD_EULER_VELOCITY):
 
     def setVertexFaceSelfCollisionsOn(self, on: bool):
         if on:
-            raise ValueError("vertex-face contact needs BACKWARD_EULER_VELOCITY")
+            raise ValueError("self collisions are not available with NEWMARK")
         super().setVertexFaceSelfCollisionsOn(False)
+
+    def setEdgeEdgeSelfCollisionsOn(self, on: bool):
+        if on:
+            raise ValueError("self collisions are not available with NEWMARK")
+        super().setEdgeEdgeSelfCollisionsOn(False)
 
     def solve(self, verbose: bool = False) -> bool:
         if self._batch is None:

@@ -300,9 +300,9 @@ def compute_lambda(E: float, nu: float) -> float:
 
 
 class _TWO_TET_VF(SIMULATION_SCENE):
-    """The two-tet vertex-face contact scenes: BACKWARD_EULER_POSITION at
-    dt = 1/30, the surface vertices inside the kinematic cubes pinned, vertex-
-    face self collisions on, edge-edge off.  The reference also registers the
+    """The two-tet contact scenes: BACKWARD_EULER_POSITION at dt = 1/30, the
+    surface vertices inside the kinematic cubes pinned, vertex-face or
+    edge-edge self collisions on.  The reference also registers the
     lower cube as a collision object (addKinematicCollisionObject, plane
     constraints); in these scenes no free vertex ever enters it, so that part
     never acts and is not built."""
@@ -315,6 +315,7 @@ class _TWO_TET_VF(SIMULATION_SCENE):
     collision_eps = 0.01   # TET_MESH default (TET_MESH.cpp:70)
     rayleigh = None        # (alpha, beta), None: the integrator's default
     pause = 0
+    vf, ee = True, False   # which self collisions
 
     def __init__(self, rest: np.ndarray, tets: np.ndarray, opts: Optional[hobak.HobakSolverOpts] = None):
         super().__init__(opts)
@@ -340,8 +341,9 @@ class _TWO_TET_VF(SIMULATION_SCENE):
             solver.setRayleigh(*self.rayleigh)
         solver.setCollisionStiffness(self.collision_mu(mu))
         solver.setCollisionDampingBeta(0.01)
-        solver.setVertexFaceSelfCollisionsOn(True)
-        self.edgeEdgeSelfCollisionsOn = False
+        solver.setVertexFaceSelfCollisionsOn(self.vf)
+        solver.setEdgeEdgeSelfCollisionsOn(self.ee)
+        self.edgeEdgeSelfCollisionsOn = self.ee
         self.eye = np.array([-2.13557, 0.947023, 2.39579])
         self.lookAt = np.array([-1.35707, 0.964614, 1.76839])
         self.up = np.array([-0.00368317, 0.999718, 0.0234604])
@@ -350,7 +352,12 @@ class _TWO_TET_VF(SIMULATION_SCENE):
 
     def vertexFaceCollisions(self):
         b = self._solver._batch
-        return [] if b is None else [tuple(p) for p in b.collision_pairs(0)[0]]
+        return [] if b is None or not self.vf else [tuple(p) for p in b.collision_pairs(0)[0]]
+
+    def edgeEdgeQuads(self):
+        """The last step's edge-edge pairs as vertex quadruples."""
+        b = self._solver._batch
+        return np.zeros((0, 4), np.int32) if b is None or not self.ee else b.edge_pairs(0)
 
 
 class TWO_TET_DROP_VF(_TWO_TET_VF):
@@ -387,6 +394,45 @@ class TWO_TET_KISS_VF(_TWO_TET_VF):
 
     def buildScene(self) -> bool:
         self.sceneName = "two_tet_kiss_vf"
+        return super().buildScene()
+
+
+class TWO_TET_DROP_EE(_TWO_TET_VF):
+    """TWO_TET_DROP_EE.h: a tet dropped edge-first (gravity 0.3) onto a
+    pinned one, SNH(E = 1, nu = 0.45), edge-edge collisions, stiffness 10."""
+    mesh_file = "../data/two_tets_edge_edge.tobj"
+    material = hobak.SNH
+    E, nu, gravity_y = 1.0, 0.45, -0.3
+    shapes = (((0.0, -4.90, 0.0), 10.0),)
+    pause = 200
+    vf, ee = False, True
+
+    def collision_mu(self, mu):
+        return 10.0
+
+    def buildScene(self) -> bool:
+        self.sceneName = "two_tet_drop_ee"
+        return super().buildScene()
+
+
+class TWO_TET_KISS_EE(_TWO_TET_VF):
+    """TWO_TET_KISS_EE.h: two pinned tets whose edges barely touch,
+    ARAP(E = 1, nu = 0.45), collision distance 0.03, stiffness 1000, no
+    Rayleigh damping."""
+    mesh_file = "../data/two_tets_edge_edge_kiss.tobj"
+    material = hobak.ARAP
+    E, nu, gravity_y = 1.0, 0.45, 0.0
+    shapes = (((0.0, -4.90, 0.0), 10.0), ((0.0, 6.9, 0.0), 10.0))
+    collision_eps = 0.03
+    rayleigh = (0.0, 0.0)
+    pause = 30
+    vf, ee = False, True
+
+    def collision_mu(self, mu):
+        return 1000.0
+
+    def buildScene(self) -> bool:
+        self.sceneName = "two_tet_kiss_ee"
         return super().buildScene()
 
 

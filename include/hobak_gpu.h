@@ -186,6 +186,18 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts);
  * scene in the batch. */
 int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, double stiffness,
                                double damping_beta);
+/* Edge-edge self collisions of one scene on or off (TIMESTEPPER's
+ * edgeEdgeSelfCollisionsOn, TIMESTEPPER.h:62-69): surface edge pairs
+ * (TET_MESH_FASTER::computeEdgeEdgeCollisions, TET_MESH_FASTER.cpp:340-500)
+ * with EDGE_SQRT_COLLISION forces and clamped Hessians, using the collision
+ * distance, stiffness and damping set with hobak_batch_set_collisions (the
+ * reference's defaults 0.01, 1, 0.001 when never set).  Velocity and
+ * position integrators; off by default. */
+int hobak_batch_set_edge_collisions(hobak_batch b, int scene, int ee_on);
+/* The edge-edge pairs of the last detection as scene-local vertex quadruples
+ * (edge0[0], edge0[1], edge1[0], edge1[1]), in surface edge order; *npairs
+ * gets the count, at most cap quadruples are written (quads may be NULL). */
+int hobak_batch_edge_pairs(hobak_batch b, int scene, int* npairs, int* quads, int cap);
 /* Vertex-face pairs of one scene found by the last step's detection (or by a
  * fresh detection at the current state when `detect_now` is 1): *npairs is
  * the count; up to cap (vertex, surface triangle) pairs in scene-local ids,

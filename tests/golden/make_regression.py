@@ -25,7 +25,9 @@ from hobakv1_gb300.replay import read_tobj  # noqa: E402
 REF = "/root/reference"
 SCENES = {"newmark_stretch": ("data/regression/newmark_stretch.json.gz", "data/cube_10.tobj", 3),
           "two_tet_drop_vf": ("data/regression/two_tet_drop_vf.json", "data/two_tets_vertex_face.tobj", 1),
-          "two_tet_kiss_vf": ("data/regression/two_tet_kiss_vf.json", "data/two_tets_vertex_face_kiss.tobj", 1)}
+          "two_tet_kiss_vf": ("data/regression/two_tet_kiss_vf.json", "data/two_tets_vertex_face_kiss.tobj", 1),
+          "two_tet_drop_ee": ("data/regression/two_tet_drop_ee.json", "data/two_tets_edge_edge.tobj", 1),
+          "two_tet_kiss_ee": ("data/regression/two_tet_kiss_ee.json", "data/two_tets_edge_edge_kiss.tobj", 1)}
 
 
 def reference_run(name, rest, tets, frames):
@@ -36,7 +38,8 @@ def reference_run(name, rest, tets, frames):
     to the record at a looser bound."""
     from hobakv1_gb300 import replay, scenes
     from oracle import refrun
-    cls = {"two_tet_drop_vf": replay.TWO_TET_DROP_VF, "two_tet_kiss_vf": replay.TWO_TET_KISS_VF}[name]
+    cls = {"two_tet_drop_vf": replay.TWO_TET_DROP_VF, "two_tet_kiss_vf": replay.TWO_TET_KISS_VF,
+           "two_tet_drop_ee": replay.TWO_TET_DROP_EE, "two_tet_kiss_ee": replay.TWO_TET_KISS_EE}[name]
     sc = cls(rest, tets)
     mu, lam = replay.compute_mu(cls.E, cls.nu), replay.compute_lambda(cls.E, cls.nu)
     shapes = [replay.CUBE(c, s) for c, s in cls.shapes]
@@ -44,7 +47,8 @@ def reference_run(name, rest, tets, frames):
     z = np.zeros_like(rest)
     s = scenes.Scene(name, rest, tets, cls.material.NAME.lower(), mu, lam, pins, z, z.copy(), density=1.0,
                      gravity=(0.0, cls.gravity_y, 0.0), dt=1.0 / 30.0)
-    r = refrun.run(s, frames, vf=True, coll_eps=cls.collision_eps, coll_mu=sc.collision_mu(mu), coll_beta=0.01,
+    r = refrun.run(s, frames, vf=cls.vf, ee=cls.ee, coll_eps=cls.collision_eps, coll_mu=sc.collision_mu(mu),
+                   coll_beta=0.01,
                    integrator="position", rayleigh=cls.rayleigh if cls.rayleigh is not None else (0.01, 0.01))
     return r["x"][1:], r["v"][1:]
 
@@ -62,7 +66,8 @@ def main():
         if name != "newmark_stretch":
             xr, vr = reference_run(name, rest, tets, n)
             extra = dict(ref_position=xr[keep], ref_velocity=vr[keep],
-                         vf_pairs=np.array([len(frames[k]["vertexFaceCollisions"]) // 2 for k in keep]))
+                         vf_pairs=np.array([len(frames[k]["vertexFaceCollisions"]) // 2 for k in keep]),
+                         ee_pairs=np.array([len(frames[k]["edgeEdgeCollisions"]) // 2 for k in keep]))
         np.savez_compressed(
             os.path.join(HERE, f"regression_{name}.npz"), rest=rest, tets=tets, dt=doc["scene"]["dt"],
             total_frames=n, frames=np.array(keep),

@@ -113,7 +113,7 @@ def test_pin_targets_move_the_pins():
 
 @pytest.mark.parametrize("precision,bound", [(hobak.PRECISION_FP64, 1e-8), (hobak.PRECISION_MIXED, 1e-5)],
                          ids=["fp64", "mixed"])  # mixed: 1e-8 per solve, grown over 200 frames of contact
-@pytest.mark.parametrize("name", ["two_tet_drop_vf", "two_tet_kiss_vf"])
+@pytest.mark.parametrize("name", ["two_tet_drop_vf", "two_tet_kiss_vf", "two_tet_drop_ee", "two_tet_kiss_ee"])
 def test_two_tet_contact_scenes_match_the_reference(name, precision, bound):
     """The reference's two-tet vertex-face regression scenes through the
     BACKWARD_EULER_POSITION drop-in with contact, frame by frame: against
@@ -121,7 +121,8 @@ def test_two_tet_contact_scenes_match_the_reference(name, precision, bound):
     at 2e-7 (FP64; the reference itself is 2.5e-8 / 8.9e-8 from it here),
     and the vertex-face pair count of every frame equal to the record's."""
     g = np.load(os.path.join(GOLDEN, f"regression_{name}.npz"))
-    cls = {"two_tet_drop_vf": replay.TWO_TET_DROP_VF, "two_tet_kiss_vf": replay.TWO_TET_KISS_VF}[name]
+    cls = {"two_tet_drop_vf": replay.TWO_TET_DROP_VF, "two_tet_kiss_vf": replay.TWO_TET_KISS_VF,
+           "two_tet_drop_ee": replay.TWO_TET_DROP_EE, "two_tet_kiss_ee": replay.TWO_TET_KISS_EE}[name]
     sc = cls(g["rest"], g["tets"], hobak.solver_opts(precision=precision, preconditioner=hobak.PRECOND_JACOBI,
                                                      integrator=hobak.INTEGRATOR_POSITION))
     sc.buildScene()
@@ -133,3 +134,28 @@ def test_two_tet_contact_scenes_match_the_reference(name, precision, bound):
         if precision == hobak.PRECISION_FP64:
             assert np.linalg.norm(x - g["position"][k]) / np.linalg.norm(g["position"][k]) < 2e-7, k
         assert len(sc.vertexFaceCollisions()) == int(g["vf_pairs"][k]), k
+        assert len(sc.edgeEdgeQuads()) == int(g["ee_pairs"][k]), k
+
+
+def test_edge_edge_pairs_match_oracle_on_two_cubes():
+    """Edge-edge pairs (vertex quadruples) and trajectory of two cubes pressed
+    together with both vertex-face and edge-edge contact, against the oracle."""
+    from oracle import oracle
+    two = scenes.two_cubes_scene(4)
+    b = hobak.BATCH([two], hobak.solver_opts(integrator=hobak.INTEGRATOR_POSITION))
+    b.set_collisions(0, True, 2e-2, 1e3, 0.001)
+    b.set_edge_collisions(0, True)
+    sim = oracle.Sim(two, precond=1, integrator="position")
+    sim.set_collisions(True, 2e-2, 1e3, 0.001, ee=True)
+    seen = 0
+    for _ in range(5):
+        b.step(1)
+        sim.step(1)
+        q, qo = b.edge_pairs(0), sim.ee_pairs()
+        assert np.array_equal(q, qo)
+        seen += len(q)
+        x, _ = b.get_state(0)
+        xo, _ = sim.state()
+        r = two.rest.reshape(-1)
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo + r) < 1e-9
+    assert seen > 0

@@ -131,14 +131,20 @@ def two_tet_record(name):
     return g
 
 
-@pytest.mark.parametrize("name", ["two_tet_drop_vf", "two_tet_kiss_vf"])
+TWO_TET = {"two_tet_drop_vf": replay.TWO_TET_DROP_VF, "two_tet_kiss_vf": replay.TWO_TET_KISS_VF,
+           "two_tet_drop_ee": replay.TWO_TET_DROP_EE, "two_tet_kiss_ee": replay.TWO_TET_KISS_EE}
+
+
+@pytest.mark.parametrize("name", list(TWO_TET))
 def test_oracle_two_tet_contact_scenes_match_the_reference(name):
-    """BACKWARD_EULER_POSITION with vertex-face contact on the reference's
-    two-tet regression scenes: against the reference built here at 1e-9 for
-    every frame, and against the recorded file at 2e-7 (the reference itself
-    is 2.5e-8 / 8.9e-8 from that record on this machine)."""
+    """BACKWARD_EULER_POSITION with vertex-face or edge-edge contact on the
+    reference's two-tet regression scenes: against the reference built here
+    at 1e-9 for every frame, against the recorded file at 2e-7 (the
+    reference itself is up to 8.9e-8 from the vertex-face records on this
+    machine; the edge-edge ones it matches to 4e-10), and the edge-edge pair
+    count of every frame equal to the record's."""
     g = two_tet_record(name)
-    cls = {"two_tet_drop_vf": replay.TWO_TET_DROP_VF, "two_tet_kiss_vf": replay.TWO_TET_KISS_VF}[name]
+    cls = TWO_TET[name]
     rest, tets = g["rest"], g["tets"]
     sc = cls(rest, tets)
     mu, lam = replay.compute_mu(cls.E, cls.nu), replay.compute_lambda(cls.E, cls.nu)
@@ -149,10 +155,12 @@ def test_oracle_two_tet_contact_scenes_match_the_reference(name):
                      gravity=(0.0, cls.gravity_y, 0.0), dt=float(g["dt"]))
     sim = oracle.Sim(s, precond=0, integrator="position",
                      rayleigh=cls.rayleigh if cls.rayleigh is not None else (0.01, 0.01))
-    sim.set_collisions(True, cls.collision_eps, sc.collision_mu(mu), 0.01)
-    assert (g["vf_pairs"] > 0).any()
+    sim.set_collisions(cls.vf, cls.collision_eps, sc.collision_mu(mu), 0.01, ee=cls.ee)
+    assert (g["ee_pairs" if cls.ee else "vf_pairs"] > 0).any()
     for k in range(int(g["total_frames"])):
         sim.step(1)
         x, _ = sim.state()
+        if cls.ee:
+            assert len(sim.ee_pairs()) == int(g["ee_pairs"][k]), k
         assert np.linalg.norm(x - g["ref_position"][k]) / np.linalg.norm(g["ref_position"][k]) < 1e-9, k
         assert np.linalg.norm(x - g["position"][k]) / np.linalg.norm(g["position"][k]) < 2e-7, k
