@@ -1133,7 +1133,9 @@ int build_collisions(hobak_batch_t* B) {
   int hash = 1024;
   while (hash < 16 * std::max(ntri, 1)) hash <<= 1;
   const int cap = std::max(nsv * kMaxPairsPerVertex + nedge, 1);
-  const int scanBlocks = (std::max(std::max(std::max(hash, nsv), nv), nedge) + 1023) / 1024 + 1;
+  int eeHash = 1024;
+  while (eeHash < 16 * std::max(nedge, 1)) eeHash <<= 1;
+  const int scanBlocks = (std::max(std::max(std::max(hash, nsv), nv), std::max(nedge, eeHash)) + 1023) / 1024 + 1;
   Arena A;
   const size_t oScenes = A.reserve(sizeof(CollisionScene) * n);
   const size_t oTri = A.reserve(sizeof(int) * 3 * (size_t)ntri), oTriScene = A.reserve(sizeof(int) * ntri);
@@ -1158,6 +1160,8 @@ int build_collisions(hobak_batch_t* B) {
   const size_t oEdgeArea = A.reserve(sizeof(double) * nedge), oEdgeTri = A.reserve(sizeof(int2) * (size_t)nedge);
   const size_t oEeSel = A.reserve(sizeof(int) * nedge), oEeKeep = A.reserve(nedge), oEeCross = A.reserve(nedge);
   const size_t oEeAB = A.reserve(sizeof(double4) * (size_t)nedge), oEeCount = A.reserve(sizeof(int) * (nedge + 1));
+  const size_t oEeCell = A.reserve(sizeof(unsigned) * n), oEeBucket = A.reserve(sizeof(int) * (eeHash + 1));
+  const size_t oEeCursor = A.reserve(sizeof(int) * eeHash), oEeEntry = A.reserve(sizeof(int) * 8 * (size_t)nedge);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, A.used);
   if (e != cudaSuccess)
@@ -1211,6 +1215,11 @@ int build_collisions(hobak_batch_t* B) {
   c.eeCross = carve<unsigned char>(base, oEeCross);
   c.eeAB = carve<double4>(base, oEeAB);
   c.eeCount = carve<int>(base, oEeCount);
+  c.eeHashSize = eeHash;
+  c.eeCellBits = carve<unsigned>(base, oEeCell);
+  c.eeBucketCount = carve<int>(base, oEeBucket);
+  c.eeBucketCursor = carve<int>(base, oEeCursor);
+  c.eeEntry = carve<int>(base, oEeEntry);
   B->collScenes.assign(n, CollisionScene{0, 0, 0, 0, 0, 0.01, 1.0, 0.001});
   for (int s = 0; s < n; s++) {
     B->collScenes[s].tri0 = B->surfTriStart[s];

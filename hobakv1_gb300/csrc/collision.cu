@@ -566,12 +566,59 @@ __device__ bool surface_edge(const DeviceCollisions& c, const CollisionScene& cs
   return l < cs.e0 + cs.ne && c.edge[l].x == lo && c.edge[l].y == hi;
 }
 
+__device__ __forceinline__ double ee_cell_size(const DeviceCollisions& c, int scene) {
+  return fmax((double)__uint_as_float(c.eeCellBits[scene]), 1e-12) * (1.0 + 1e-6);
+}
+
+// the scene's largest eps-inflated edge extent sets its cell size
+__global__ void k_edge_prepare(DeviceBatch b, DeviceCollisions c) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= c.nedge) return;
+  const int s = c.edgeScene[x];
+  const CollisionScene& cs = c.scenes[s];
+  if (!cs.eeOn) return;
+  const int2 e = c.edge[x];
+  const D3 p = pos(b, e.x), q = pos(b, e.y);
+  const double ext = fmax(fmax(fabs(p.x - q.x), fabs(p.y - q.y)), fabs(p.z - q.z)) + 2.0 * cs.eps;
+  atomicMax(&c.eeCellBits[s], __float_as_uint(__double2float_ru(ext)));
+}
+
+// every edge into the cells its eps-inflated box overlaps (<= 2 per axis)
+template <bool FILL>
+__global__ void k_edge_bucket(DeviceBatch b, DeviceCollisions c) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= c.nedge) return;
+  const int s = c.edgeScene[x];
+  const CollisionScene& cs = c.scenes[s];
+  if (!cs.eeOn) return;
+  const int2 e = c.edge[x];
+  const D3 p = pos(b, e.x), q = pos(b, e.y);
+  const double h = ee_cell_size(c, s), ep = cs.eps;
+  const int x0 = (int)floor((fmin(p.x, q.x) - ep) / h), x1 = (int)floor((fmax(p.x, q.x) + ep) / h);
+  const int y0 = (int)floor((fmin(p.y, q.y) - ep) / h), y1 = (int)floor((fmax(p.y, q.y) + ep) / h);
+  const int z0 = (int)floor((fmin(p.z, q.z) - ep) / h), z1 = (int)floor((fmax(p.z, q.z) + ep) / h);
+  const int mask = c.eeHashSize - 1;
+  for (int ix = x0; ix <= x1 && ix <= x0 + 1; ix++)
+    for (int iy = y0; iy <= y1 && iy <= y0 + 1; iy++)
+      for (int iz = z0; iz <= z1 && iz <= z0 + 1; iz++) {
+        const unsigned bk = hash_cell(s, ix, iy, iz, mask);
+        if (!FILL) {
+          atomicAdd(&c.eeBucketCount[bk], 1);
+        } else {
+          const int pp = c.eeBucketCount[bk] + atomicAdd(&c.eeBucketCursor[bk], 1);
+          c.eeEntry[pp] = x;
+        }
+      }
+}
+
 // One thread per surface edge x: the closest non-adjacent edge y >= x of the
 // scene whose closest points lie inside both edges (parameters within
-// [1e-4, 1 - 1e-4]; equal distances go to the later edge), kept when no
-// endpoint pair is a surface edge and the distance is below eps.  All edges
-// of the scene are candidates (the reference's AABB query only removes edges
-// farther than eps, which cannot be kept).
+// [1e-4, 1 - 1e-4]; equal distances go to the later edge, as the reference's
+// ascending scan keeps the last), kept when no endpoint pair is a surface
+// edge and the distance is below eps.  Candidates come from the cells x's own
+// box overlaps: any edge within eps of x has a point of its inflated box in
+// one of them; farther edges cannot be kept, so the pairs are those of a scan
+// over all edges.
 __global__ void k_ee_detect(DeviceBatch b, DeviceCollisions c) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= c.nedge) return;
@@ -586,14 +633,25 @@ __global__ void k_ee_detect(DeviceBatch b, DeviceCollisions c) {
   const double len0 = norm(v1 - v0);
   int best = -1;
   double bestD = (double)3.402823466e+38f, ab[4] = {-1, -1, -1, -1};
-  for (int y = x; y < cs.e0 + cs.ne; y++) {
+  const double h = ee_cell_size(c, s);
+  const int cx0 = (int)floor(fmin(v0.x, v1.x) / h), cx1 = (int)floor(fmax(v0.x, v1.x) / h);
+  const int cy0 = (int)floor(fmin(v0.y, v1.y) / h), cy1 = (int)floor(fmax(v0.y, v1.y) / h);
+  const int cz0 = (int)floor(fmin(v0.z, v1.z) / h), cz1 = (int)floor(fmax(v0.z, v1.z) / h);
+  const int mask = c.eeHashSize - 1;
+  for (int ix = cx0; ix <= cx1 && ix <= cx0 + 1; ix++)
+  for (int iy = cy0; iy <= cy1 && iy <= cy0 + 1; iy++)
+  for (int iz = cz0; iz <= cz1 && iz <= cz0 + 1; iz++) {
+  const unsigned bk = hash_cell(s, ix, iy, iz, mask);
+  for (int k = c.eeBucketCount[bk]; k < c.eeBucketCount[bk + 1]; k++) {
+    const int y = c.eeEntry[k];
+    if (y < x || c.edgeScene[y] != s) continue;
     const int2 in = c.edge[y];
     if (o.x == in.x || o.x == in.y || o.y == in.x || o.y == in.y) continue;
     const D3 v2 = pos(b, in.x), v3 = pos(b, in.y);
     D3 po, pi;
     seg::closest(v0, v1, v2, v3, po, pi);
     const double d = norm(pi - po);
-    if (d > bestD) continue;
+    if (d > bestD || (d == bestD && y <= best)) continue;
     const double a1 = norm(po - v0) / len0, a0 = 1.0 - a1;
     const double b1 = norm(pi - v2) / norm(v3 - v2), b0 = 1.0 - b1;
     const double skip = 1e-4;
@@ -602,6 +660,7 @@ __global__ void k_ee_detect(DeviceBatch b, DeviceCollisions c) {
     bestD = d;
     best = y;
     ab[0] = a0, ab[1] = a1, ab[2] = b0, ab[3] = b1;
+  }
   }
   if (best < 0) return;
   const int2 in = c.edge[best];
@@ -707,6 +766,13 @@ void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStre
   k_copy_total<<<1, 32, 0, s>>>(c.svCount + c.nsv, c.npairs);
   k_vf_pairs<<<(c.nsv + 127) / 128, 128, 0, s>>>(b, c);
   if (c.nedge > 0) {  // edge-edge pairs follow the vertex-face ones (TIMESTEPPER.cpp:665-690)
+    cudaMemsetAsync(c.eeCellBits, 0, sizeof(unsigned) * c.nscenes, s);
+    cudaMemsetAsync(c.eeBucketCount, 0, sizeof(int) * (c.eeHashSize + 1), s);
+    cudaMemsetAsync(c.eeBucketCursor, 0, sizeof(int) * c.eeHashSize, s);
+    k_edge_prepare<<<(c.nedge + 255) / 256, 256, 0, s>>>(b, c);
+    k_edge_bucket<false><<<(c.nedge + 255) / 256, 256, 0, s>>>(b, c);
+    scan_counts(c.eeBucketCount, c.eeHashSize, c.scanTmp, s);
+    k_edge_bucket<true><<<(c.nedge + 255) / 256, 256, 0, s>>>(b, c);
     k_ee_detect<<<(c.nedge + 127) / 128, 128, 0, s>>>(b, c);
     scan_counts(c.eeCount, c.nedge, c.scanTmp, s);
     k_ee_pairs<<<(c.nedge + 127) / 128, 128, 0, s>>>(b, c);

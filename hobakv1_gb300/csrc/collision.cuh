@@ -66,6 +66,13 @@ struct DeviceCollisions {
   unsigned char* eeCross;  // [nedge] 1: the edge crosses a triangle next to its partner
   double4* eeAB;           // [nedge] (a0, a1, b0, b1)
   int* eeCount;            // [nedge + 1] keep flags, then exclusive scan
+  // edge-edge broad phase: each edge's eps-inflated box hashed into cells no
+  // smaller than the scene's largest inflated edge extent (<= 8 cells each)
+  int eeHashSize;
+  unsigned* eeCellBits;    // [nscenes] largest inflated edge extent (float bits)
+  int* eeBucketCount;      // [eeHashSize + 1] then exclusive scan
+  int* eeBucketCursor;     // [eeHashSize]
+  int* eeEntry;            // [8 * nedge]
 };
 
 struct DeviceBatch;

@@ -137,11 +137,13 @@ def test_two_tet_contact_scenes_match_the_reference(name, precision, bound):
         assert len(sc.edgeEdgeQuads()) == int(g["ee_pairs"][k]), k
 
 
-def test_edge_edge_pairs_match_oracle_on_two_cubes():
-    """Edge-edge pairs (vertex quadruples) and trajectory of two cubes pressed
-    together with both vertex-face and edge-edge contact, against the oracle."""
+@pytest.mark.parametrize("N", [4, 8])
+def test_edge_edge_pairs_match_oracle_on_two_cubes(N):
+    """Edge-edge pairs (vertex quadruples; the GPU's hashed broad phase
+    against the oracle's scan over all edge pairs) and trajectory of two
+    cubes pressed together with vertex-face and edge-edge contact."""
     from oracle import oracle
-    two = scenes.two_cubes_scene(4)
+    two = scenes.two_cubes_scene(N)
     b = hobak.BATCH([two], hobak.solver_opts(integrator=hobak.INTEGRATOR_POSITION))
     b.set_collisions(0, True, 2e-2, 1e3, 0.001)
     b.set_edge_collisions(0, True)
