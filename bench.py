@@ -28,6 +28,9 @@ Workloads (synthetic, seeded; see hobakv1_gb300/scenes.py):
   serve_poisson           continuous batching: 32 jobs (N ~ U{8..32}, 10-200 steps, half two cubes in
                           vertex-face contact) arriving as a Poisson stream at 50, 400 and 2000 jobs/s,
                           mixed precision and plain FP64; job-steps/s, p50/p99 step and job latency
+  two_cubes24_contact_position[_mixed]
+                          two 24^3 cubes in self contact (vertex-face and edge-edge, distance 1e-2),
+                          BACKWARD_EULER_POSITION
 """
 from __future__ import annotations
 
@@ -69,6 +72,13 @@ WORKLOADS = {
     "mix256_newmark_mixed": dict(kind="mix", count=256, material="snh/arap", precision=1, integrator="newmark"),
     "serve_poisson": dict(kind="serve", count=32, lambdas=[50, 400, 2000], material="snh/arap",
                           precision=1),
+    # self contact: two 24^3 cubes resting on each other (62,500 vertices),
+    # vertex-face and edge-edge collisions at distance 1e-2, position integrator
+    "two_cubes24_contact_position_mixed": dict(kind="contact", N=24, material="snh", precision=1,
+                                               integrator="position",
+                                               contact=dict(vf=True, ee=True, eps=1e-2, mu=1e3, beta=1e-3)),
+    "two_cubes24_contact_position": dict(kind="contact", N=24, material="snh", precision=0, integrator="position",
+                                         contact=dict(vf=True, ee=True, eps=1e-2, mu=1e3, beta=1e-3)),
 }
 # the metric's headline: batched mixed precision on the 256-scene mix, with the
 # plain (unbatched) FP64 GPU path measured beside it
@@ -85,6 +95,8 @@ def make_scenes(spec):
         return scenes.config4_scenes(spec["count"])
     if spec["kind"] == "serve":
         return scenes.config5_jobs(spec["count"])
+    if spec["kind"] == "contact":
+        return [scenes.two_cubes_scene(spec["N"])]
     raise ValueError(spec)
 
 
@@ -162,7 +174,7 @@ def ncu_traffic(workload):
         return json.load(f).get(workload, {})
 
 
-def cpu_baseline(scene_list, steps, warmup, max_scenes=16, integrator="velocity"):
+def cpu_baseline(scene_list, steps, warmup, max_scenes=16, integrator="velocity", contact=None):
     """The oracle (CPU restatement of the reference algorithm, OpenMP on all
     host cores) on the same workload; bounded sample.  Large mixes time a
     seeded subset (every k-th scene) and scale by scene count.
@@ -173,6 +185,9 @@ def cpu_baseline(scene_list, steps, warmup, max_scenes=16, integrator="velocity"
     subset = scene_list[::stride]
     scale = len(scene_list) / len(subset)
     sims = [oracle.Sim(s, precond=0, integrator=integrator) for s in subset]
+    if contact:
+        for sim in sims:
+            sim.set_collisions(contact["vf"], contact["eps"], contact["mu"], contact["beta"], ee=contact["ee"])
     if warmup:
         for sim in sims:
             sim.step(warmup)
@@ -304,7 +319,8 @@ def run_reference(args, spec, scene_list):
         return
     steps = max(1, min(args.steps, 5))
     warm = 1 if args.warmup > 0 else 0
-    value, lat, cores, sample = cpu_baseline(scene_list, steps, warm, integrator=spec.get("integrator", "velocity"))
+    value, lat, cores, sample = cpu_baseline(scene_list, steps, warm, integrator=spec.get("integrator", "velocity"),
+                                             contact=spec.get("contact"))
     lat_ms = [1e3 * x for x in lat]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": warm, "ms_per_step": 1e3 / value,
@@ -356,6 +372,9 @@ def config_of(spec, scene_list, preconditioner="block_jacobi"):
             "integrator": {"position": "BACKWARD_EULER_POSITION (Rayleigh alpha = beta = 0.01)",
                            "newmark": "NEWMARK (beta 1/4, gamma 1/2, Newton to |rhs|^2 <= 1e-7, at most 10)"}
                           .get(spec.get("integrator"), "BACKWARD_EULER_VELOCITY"),
+            **({"contact": {"vertex_face": spec["contact"]["vf"], "edge_edge": spec["contact"]["ee"],
+                            "eps": spec["contact"]["eps"], "stiffness": spec["contact"]["mu"],
+                            "damping_beta": spec["contact"]["beta"]}} if spec.get("contact") else {}),
             "pcg_tol": 1e-8, "pcg_max_iters": 1000, "preconditioner": preconditioner,
             "l2": f"each step writes {hess_mb:.0f} MB of element Hessians (> 129 MB L2 at 40^3 and the mix); "
                   "no explicit flush"}
@@ -375,6 +394,11 @@ def run_ours(args, spec, scene_list):
         spec.get("integrator"), hobak.INTEGRATOR_VELOCITY)
     opts = hobak.solver_opts(precision=spec["precision"], use_graph=not args.eager, integrator=solver_integrator)
     batch = hobak.BATCH(scene_list, opts)
+    if spec.get("contact"):
+        ct = spec["contact"]
+        for i in range(len(scene_list)):
+            batch.set_collisions(i, ct["vf"], ct["eps"], ct["mu"], ct["beta"])
+            batch.set_edge_collisions(i, ct["ee"])
     stream = torch.cuda.ExternalStream(batch.stream_handle())
     # launch shapes (tile size, CTA sizes, PCG chunk) from the autotuner, on
     # this batch's data, before the warm-up; the state is left unchanged
@@ -475,7 +499,8 @@ def run_ours(args, spec, scene_list):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         steps = 3 if sum(s.nt for s in scene_list) > 100_000 else 20
-        cv, _, cores, sample = cpu_baseline(scene_list, steps, 0, integrator=spec.get("integrator", "velocity"))
+        cv, _, cores, sample = cpu_baseline(scene_list, steps, 0, integrator=spec.get("integrator", "velocity"),
+                                        contact=spec.get("contact"))
         cpu = {"value": cv, "unit": "steps/s", "cores": cores, "kind": "port",
                "sample": sample + f" of {args.workload} on the host cores (OpenMP), from the initial state"}
 

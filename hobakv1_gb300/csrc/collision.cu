@@ -634,6 +634,8 @@ __global__ void k_ee_detect(DeviceBatch b, DeviceCollisions c) {
   int best = -1;
   double bestD = (double)3.402823466e+38f, ab[4] = {-1, -1, -1, -1};
   const double h = ee_cell_size(c, s);
+  const D3 bmin = {fmin(v0.x, v1.x), fmin(v0.y, v1.y), fmin(v0.z, v1.z)};
+  const D3 bmax = {fmax(v0.x, v1.x), fmax(v0.y, v1.y), fmax(v0.z, v1.z)};
   const int cx0 = (int)floor(fmin(v0.x, v1.x) / h), cx1 = (int)floor(fmax(v0.x, v1.x) / h);
   const int cy0 = (int)floor(fmin(v0.y, v1.y) / h), cy1 = (int)floor(fmax(v0.y, v1.y) / h);
   const int cz0 = (int)floor(fmin(v0.z, v1.z) / h), cz1 = (int)floor(fmax(v0.z, v1.z) / h);
@@ -648,6 +650,12 @@ __global__ void k_ee_detect(DeviceBatch b, DeviceCollisions c) {
     const int2 in = c.edge[y];
     if (o.x == in.x || o.x == in.y || o.y == in.x || o.y == in.y) continue;
     const D3 v2 = pos(b, in.x), v3 = pos(b, in.y);
+    // boxes farther apart than eps: farther than eps, never kept (skipping
+    // such a candidate cannot change which partner a kept pair has)
+    if (fmin(v2.x, v3.x) - cs.eps > bmax.x || fmax(v2.x, v3.x) + cs.eps < bmin.x ||
+        fmin(v2.y, v3.y) - cs.eps > bmax.y || fmax(v2.y, v3.y) + cs.eps < bmin.y ||
+        fmin(v2.z, v3.z) - cs.eps > bmax.z || fmax(v2.z, v3.z) + cs.eps < bmin.z)
+      continue;
     D3 po, pi;
     seg::closest(v0, v1, v2, v3, po, pi);
     const double d = norm(pi - po);

@@ -1213,6 +1213,23 @@ void eeCollisions(Sim& s) {
   std::sort(adj.begin(), adj.end());
   auto adjacent = [&](int a, int b) { return std::binary_search(adj.begin(), adj.end(), std::make_pair(a, b)); };
   const double farAway = (double)FLT_MAX;
+  // boxes for a cheap prefilter: an edge whose eps-inflated box misses x's
+  // box is farther than eps and can neither be kept nor be x's partner in a
+  // kept pair, so skipping it leaves the pairs unchanged
+  std::vector<double> box(6 * (size_t)ne);
+  for (int k = 0; k < ne; k++) {
+    const V3 p = pos(C.edges[2 * k]), q = pos(C.edges[2 * k + 1]);
+    for (int i = 0; i < 3; i++) {
+      box[6 * k + i] = std::min(p[i], q[i]);
+      box[6 * k + 3 + i] = std::max(p[i], q[i]);
+    }
+  }
+  struct Hit {
+    int best;
+    double d, a[2], b[2];
+  };
+  std::vector<Hit> hits(ne);
+#pragma omp parallel for schedule(dynamic, 64)
   for (int x = 0; x < ne; x++) {
     const int o0 = C.edges[2 * x], o1 = C.edges[2 * x + 1];
     const V3 v0 = pos(o0), v1 = pos(o1);
@@ -1221,6 +1238,10 @@ void eeCollisions(Sim& s) {
     for (int y = x; y < ne; y++) {
       const int i0 = C.edges[2 * y], i1 = C.edges[2 * y + 1];
       if (o0 == i0 || o0 == i1 || o1 == i0 || o1 == i1) continue;
+      bool apart = false;
+      for (int i = 0; i < 3; i++)
+        apart = apart || box[6 * y + i] - C.eps > box[6 * x + 3 + i] || box[6 * y + 3 + i] + C.eps < box[6 * x + i];
+      if (apart) continue;
       const V3 v2 = pos(i0), v3 = pos(i1);
       V3 po, pi;
       segseg::closest(v0, v1, v2, v3, po, pi);
@@ -1238,6 +1259,13 @@ void eeCollisions(Sim& s) {
       best = y;
       ba[0] = a[0], ba[1] = a[1], bb[0] = b[0], bb[1] = b[1];
     }
+    hits[x] = Hit{best, bestD, {ba[0], ba[1]}, {bb[0], bb[1]}};
+  }
+  for (int x = 0; x < ne; x++) {
+    const int o0 = C.edges[2 * x], o1 = C.edges[2 * x + 1];
+    const V3 v0 = pos(o0), v1 = pos(o1);
+    const int best = hits[x].best;
+    const double bestD = hits[x].d, ba[2] = {hits[x].a[0], hits[x].a[1]}, bb[2] = {hits[x].b[0], hits[x].b[1]};
     if (best < 0) continue;
     const int i0 = C.edges[2 * best], i1 = C.edges[2 * best + 1];
     if (adjacent(o0, i0) || adjacent(o0, i1) || adjacent(o1, i0) || adjacent(o1, i1)) continue;
