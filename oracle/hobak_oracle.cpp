@@ -938,6 +938,7 @@ struct Sim {
   std::vector<double> acc;
   int maxNewton = 10;
   double newtonEps = 1e-7;
+  double greenMu = 0.0;  // NEWMARK with GREEN_DAMPING(mu): the energy-damped solve
   int lastNewton = 0;
 };
 
@@ -1641,6 +1642,69 @@ void stepNewmark(Sim& s) {
   std::vector<double> rhs(3 * (size_t)nv), y;
   while (step < s.maxNewton && maxR > s.newtonEps) {
     assemble(s);
+    if (s.greenMu > 0.0) {
+      // NEWMARK::solveEnergyDamped (NEWMARK.cpp:344-480): the iterate's
+      // velocity S (a3 (x - x_old) + a4 v_old + a5 a_old), Fdot = V DmInv
+      // (TET_MESH::computeFdots, TET_MESH.cpp:660-684), and R gains the
+      // GREEN_DAMPING force -vol dF/dx^T mu F (F^T Fdot + Fdot^T F)
+      // (GREEN_DAMPING.cpp PK1; TET_MESH.cpp:816-860); its Hessian is passed to
+      // computeCollisionResponse, which zeroes it, so A is unchanged
+      std::vector<double> vi(3 * (size_t)nv);
+      for (int u = 0; u < nv; u++)
+        for (int i = 0; i < 3; i++) {
+          const size_t q = 3 * (size_t)u + i;
+          vi[q] = s.free[u] ? al[3] * (s.x[q] - xOld[q]) + al[4] * vOld[q] + al[5] * aOld[q] : 0.0;
+        }
+      std::vector<double> fd(12 * (size_t)M.nt);
+#pragma omp parallel for schedule(static)
+      for (int t = 0; t < M.nt; t++) {
+        const int* tv = &M.tets[4 * (size_t)t];
+        const double* Dinv = &M.DmInv[9 * (size_t)t];
+        double Ds[9], Vs[9], F[9], Fd[9];
+        for (int a = 0; a < 3; a++)
+          for (int i = 0; i < 3; i++) {
+            Ds[i + 3 * a] = (M.rest[3 * tv[a + 1] + i] + s.x[3 * tv[a + 1] + i]) - (M.rest[3 * tv[0] + i] + s.x[3 * tv[0] + i]);
+            Vs[i + 3 * a] = vi[3 * tv[a + 1] + i] - vi[3 * tv[0] + i];
+          }
+        for (int j = 0; j < 3; j++)
+          for (int i = 0; i < 3; i++) {
+            F[i + 3 * j] = Ds[i] * Dinv[3 * j] + Ds[i + 3] * Dinv[1 + 3 * j] + Ds[i + 6] * Dinv[2 + 3 * j];
+            Fd[i + 3 * j] = Vs[i] * Dinv[3 * j] + Vs[i + 3] * Dinv[1 + 3 * j] + Vs[i + 6] * Dinv[2 + 3 * j];
+          }
+        double G[9], P[9];  // G = F^T Fdot + Fdot^T F, P = mu F G
+        for (int j = 0; j < 3; j++)
+          for (int i = 0; i < 3; i++) {
+            double a = 0.0, b = 0.0;
+            for (int k = 0; k < 3; k++) {
+              a += F[k + 3 * i] * Fd[k + 3 * j];
+              b += Fd[k + 3 * i] * F[k + 3 * j];
+            }
+            G[i + 3 * j] = a + b;
+          }
+        for (int j = 0; j < 3; j++)
+          for (int i = 0; i < 3; i++) {
+            double a = 0.0;
+            for (int k = 0; k < 3; k++) a += F[i + 3 * k] * G[k + 3 * j];
+            P[i + 3 * j] = s.greenMu * a;
+          }
+        // force on vertex a+1 = -vol P DmInv^T row a; vertex 0 = minus their sum
+        const double vol = M.vol[t];
+        double f0[3] = {0.0, 0.0, 0.0};
+        for (int a = 0; a < 3; a++)
+          for (int i = 0; i < 3; i++) {
+            double acc = 0.0;
+            for (int j = 0; j < 3; j++) acc += P[i + 3 * j] * Dinv[a + 3 * j];
+            fd[12 * (size_t)t + 3 * (a + 1) + i] = -vol * acc;
+            f0[i] += vol * acc;
+          }
+        for (int i = 0; i < 3; i++) fd[12 * (size_t)t + i] = f0[i];
+      }
+      for (int u = 0; u < nv; u++)
+        for (int k = M.vtxptr[u]; k < M.vtxptr[u + 1]; k++) {
+          const int t = M.vtxinc[k] / 4, a = M.vtxinc[k] % 4;
+          for (int i = 0; i < 3; i++) s.R[3 * u + i] += fd[12 * (size_t)t + 3 * a + i];
+        }
+    }
     maxR = 0.0;
     for (int u = 0; u < nv; u++) {
       const double m = s.density * M.oneRing[u];
@@ -1821,6 +1885,14 @@ int oracle_ee_pairs(void* h, int* pairs, int* edges) {
   }
   std::copy(C.eePairs.begin(), C.eePairs.end(), pairs);
   return (int)C.eePairs.size() / 2;
+}
+
+// NEWMARK's energy-damped solve with GREEN_DAMPING(mu) (mu = 0: Rayleigh).
+int oracle_set_green_damping(void* h, double mu) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s || !(mu >= 0.0)) return -1;
+  s->greenMu = mu;
+  return 0;
 }
 
 int oracle_set_integrator(void* h, int integrator, double alpha, double beta) {

@@ -47,6 +47,7 @@ def lib():
         L.oracle_attach_pins.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip]
         L.oracle_set_pin_targets.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
         L.oracle_ee_pairs.argtypes = [ctypes.c_void_p, _ip, _ip]
+        L.oracle_set_green_damping.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.oracle_set_solver.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.oracle_set_external_forces.argtypes = [ctypes.c_void_p, _dp]
         L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp]
@@ -122,6 +123,10 @@ class Sim:
         if integrator != "velocity":
             code = {"position": 1, "newmark": 2}[integrator]
             assert L.oracle_set_integrator(self.h, code, rayleigh[0], rayleigh[1]) == 0
+
+    def set_green_damping(self, mu):
+        """NEWMARK's energy-damped solve with GREEN_DAMPING(mu)."""
+        assert lib().oracle_set_green_damping(self.h, float(mu)) == 0
 
     def set_pin_targets(self, targets):
         """Target displacements of the pinned vertices (scene.pinned order)."""

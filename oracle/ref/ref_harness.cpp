@@ -30,6 +30,7 @@
 
 #include "SETTINGS.h"
 #include "Geometry/CUBE.h"
+#include "Damping/Volume/GREEN_DAMPING.h"
 #include "Geometry/TET_MESH_FASTER.h"
 #include "Hyperelastic/Volume/ARAP.h"
 #include "Hyperelastic/Volume/LINEAR.h"
@@ -108,6 +109,14 @@ class HarnessBEP : public TIMESTEPPER::BACKWARD_EULER_POSITION {
 class HarnessNewmark : public TIMESTEPPER::NEWMARK {
  public:
   HarnessNewmark(TET_MESH& m, VOLUME::HYPERELASTIC& h) : NEWMARK(m, h) {}
+  ~HarnessNewmark() { delete _green; }
+  // the energy-damped solve (NEWMARK::solve takes it when _damping is set)
+  void setGreenDamping(double mu) {
+    delete _green;
+    _green = new VOLUME::GREEN_DAMPING(mu);
+    _damping = _green;
+  }
+  VOLUME::GREEN_DAMPING* _green = nullptr;
   void setSolver(double tol, int maxit) {
     _cgSolver.setTolerance(tol);
     _cgSolver.setMaxIterations(maxit);
@@ -245,6 +254,9 @@ int runWith(const std::string& in, const std::string& out, const std::string& ma
   Stepper solver(mesh, *material);
   if constexpr (std::is_same_v<Stepper, HarnessBEP>) {
     if (nprm >= 15) solver.setRayleigh(p[13], p[14]);
+  }
+  if constexpr (std::is_same_v<Stepper, HarnessNewmark>) {
+    if (nprm >= 16 && p[15] > 0.0) solver.setGreenDamping(p[15]);
   }
   solver.setDt(dt);
   solver.setSolver(tol, maxit);

@@ -42,7 +42,7 @@ def elements(rest, tets, x, material, mu, lam):
 
 def run(scene, steps, stride=1, tol=1e-8, maxit=1000, vf=False, ee=False,
         coll_eps=0.01, coll_mu=1.0, coll_beta=0.001, threads=None, integrator="velocity",
-        rayleigh=(0.01, 0.01)):
+        rayleigh=(0.01, 0.01), green_damping=0.0):
     """BACKWARD_EULER_VELOCITY::solve (integrator "velocity"),
     BACKWARD_EULER_POSITION::solve (integrator "position", Rayleigh damped
     with alpha, beta = rayleigh) or NEWMARK::solve (integrator "newmark")
@@ -55,7 +55,8 @@ def run(scene, steps, stride=1, tol=1e-8, maxit=1000, vf=False, ee=False,
         g = scene.gravity
         params = np.array([scene.density, g[0], g[1], g[2], scene.dt, tol, maxit,
                            float(vf), float(ee), coll_eps, coll_mu, coll_beta,
-                           {"velocity": 0.0, "position": 1.0, "newmark": 2.0}[integrator], rayleigh[0], rayleigh[1]],
+                           {"velocity": 0.0, "position": 1.0, "newmark": 2.0}[integrator], rayleigh[0], rayleigh[1],
+                           green_damping],
                           dtype=np.float64)
         np.save(os.path.join(tin, "params.npy"), params)
         env = dict(os.environ)

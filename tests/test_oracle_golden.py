@@ -149,3 +149,21 @@ def test_oracle_vertex_face_collisions_match_reference():
         pairs, _ = sim.vf_pairs()
         ref = g[f"pairs_{k}"]
         assert sorted(map(tuple, pairs.tolist())) == sorted(map(tuple, ref.tolist())), k
+
+
+def test_oracle_green_damped_newmark_matches_the_reference_when_built():
+    """NEWMARK's energy-damped solve with GREEN_DAMPING(mu) (NEWMARK.cpp:
+    344-480): the restatement against the reference built here (oracle/ref),
+    when that build exists in this checkout."""
+    from oracle import refrun
+    if not os.path.exists(refrun.REF_BIN):
+        pytest.skip("reference build not present")
+    s = scenes.config1_scene(5)
+    for mu in (0.05, 1.0):
+        r = refrun.run(s, 4, integrator="newmark", green_damping=mu)
+        sim = oracle.Sim(s, precond=0, integrator="newmark")
+        sim.set_green_damping(mu)
+        for k in range(4):
+            sim.step(1)
+            x, _ = sim.state()
+            assert np.linalg.norm(x - r["x"][k + 1]) / np.linalg.norm(r["x"][k + 1]) < 1e-12, (mu, k)
