@@ -224,6 +224,54 @@ def plain_fp64_gpu(scene_list, steps, integrator=0):
     return steps / dt
 
 
+def batched_fp64_gpu(scene_list, steps, warmup, integrator, no_autotune):
+    """The same mix as one FP64 batch: steps/s and ms per step (CUDA events)."""
+    import torch
+    from hobakv1_gb300 import hobak
+    b = hobak.BATCH(scene_list, hobak.solver_opts(precision=hobak.PRECISION_FP64, integrator=integrator))
+    tune = b.get_tuning() if no_autotune else b.autotune(reps=1)
+    b.step(max(warmup, 1))
+    stream = torch.cuda.ExternalStream(b.stream_handle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        b.step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    b.close()
+    return 1e3 / ms, ms, tune
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (/proc/cpuinfo), or the machine type."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    return line.split(":", 1)[1].strip()
+        import platform
+        return platform.machine() + " (no model name in /proc/cpuinfo)"
+    except OSError:
+        import platform
+        return platform.machine()
+
+
+def port_vs_reference():
+    """Speed of the oracle port against the reference built from its sources,
+    measured side by side on the x86 build host (oracle/port_vs_reference.py),
+    where the reference compiles; the reference's x86 build cannot run here."""
+    path = os.path.join(ROOT, "oracle", "port_vs_reference.json")
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        m = json.load(f)
+    return {"port_speed_vs_reference": m.get("port_speed_vs_reference"),
+            "port_vs_reference_how": m.get("how")}
+
+
 def serve_once(job_specs, arrivals, precision, budget_bytes, tuning=None):
     """Drive the continuous-batching server with jobs arriving at the given
     times (seconds from start).  Returns (wall seconds, jobs, server)."""
@@ -314,22 +362,62 @@ def run_serving(args, spec, job_specs):
 
 
 def run_reference(args, spec, scene_list):
+    """The reference algorithm on the host cores: the oracle port (the x86
+    reference build cannot run on this host) on every scene of the workload,
+    W warm-up steps then exactly K timed steps, each a full step of the whole
+    workload (no subset, no extrapolation); plus a 1-thread figure on a
+    sample of the scenes."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    steps = max(1, min(args.steps, 5))
-    warm = 1 if args.warmup > 0 else 0
-    value, lat, cores, sample = cpu_baseline(scene_list, steps, warm, integrator=spec.get("integrator", "velocity"),
-                                             contact=spec.get("contact"))
+    from oracle import oracle
+    oracle.build()
+    integrator = spec.get("integrator", "velocity")
+    contact = spec.get("contact")
+    sims = [oracle.Sim(s, precond=0, integrator=integrator) for s in scene_list]
+    if contact:
+        for sim in sims:
+            sim.set_collisions(contact["vf"], contact["eps"], contact["mu"], contact["beta"], ee=contact["ee"])
+    cores = oracle.set_threads(0)
+    for _ in range(args.warmup):
+        for sim in sims:
+            sim.step(1)
+    lat = []
+    for _ in range(args.steps):
+        ts = time.perf_counter()
+        for sim in sims:
+            sim.step(1)
+        lat.append(time.perf_counter() - ts)
+    value = args.steps / sum(lat)
+    # 1 thread against all threads on the same sample (every k-th scene, one step)
+    stride = max(1, len(sims) // 16)
+    sample = sims[::stride]
+    t_all = time.perf_counter()
+    for sim in sample:
+        sim.step(1)
+    t_all = time.perf_counter() - t_all
+    oracle.set_threads(1)
+    t_one = time.perf_counter()
+    for sim in sample:
+        sim.step(1)
+    t_one = time.perf_counter() - t_one
+    oracle.set_threads(0)
     lat_ms = [1e3 * x for x in lat]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
-            "steps": steps, "warmup": warm, "ms_per_step": 1e3 / value,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
             "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": args.workload,
-                                              **config_of(spec, scene_list, "jacobi (Eigen DiagonalPreconditioner)")},
+            "data": "synthetic", "config": {"workload": args.workload, **config_of(spec, scene_list)},
+            "preconditioner": "jacobi (Eigen DiagonalPreconditioner, the reference's)",
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": f"every step of all {len(sims)} scene(s): {args.warmup} warm-up steps, "
+                                       f"then {args.steps} timed steps from the workload's initial state",
+                             "cpu_model": cpu_model(),
+                             "one_thread": {"sample": f"one step of {len(sample)} of the {len(sims)} scene(s) "
+                                                      f"(every {stride}th), after the timed steps",
+                                            "ms_1_thread": 1e3 * t_one, f"ms_{cores}_threads": 1e3 * t_all,
+                                            "thread_speedup": t_one / t_all if t_all > 0 else None},
+                             **port_vs_reference()},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -364,7 +452,7 @@ def run_reference_serving(args, spec, job_specs, sample_jobs=4, steps=2):
     print(json.dumps(line), flush=True)
 
 
-def config_of(spec, scene_list, preconditioner="block_jacobi"):
+def config_of(spec, scene_list):
     nt = int(sum(s.nt for s in scene_list))
     hess_mb = nt * 90 * (8 if spec["precision"] == 0 else 4) / 1e6
     return {"scenes": len(scene_list), "tets": nt, "verts": int(sum(s.nv for s in scene_list)),
@@ -375,9 +463,96 @@ def config_of(spec, scene_list, preconditioner="block_jacobi"):
             **({"contact": {"vertex_face": spec["contact"]["vf"], "edge_edge": spec["contact"]["ee"],
                             "eps": spec["contact"]["eps"], "stiffness": spec["contact"]["mu"],
                             "damping_beta": spec["contact"]["beta"]}} if spec.get("contact") else {}),
-            "pcg_tol": 1e-8, "pcg_max_iters": 1000, "preconditioner": preconditioner,
+            "pcg_tol": 1e-8, "pcg_max_iters": 1000,
             "l2": f"each step writes {hess_mb:.0f} MB of element Hessians (> 129 MB L2 at 40^3 and the mix); "
                   "no explicit flush"}
+
+
+# GB300 issues FP64 at 2 thread-instructions per SM per clock (ncu:
+# sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained = 304 over
+# 152 SMs), 1/64 of the FP32 rate.
+FP64_PER_SM_CLK = 2
+NUM_SMS = 152
+
+
+def step_rooflines(batch, spec, scene_list, phases, phase_steps, iters_by_scene, workload, sm_mhz):
+    """Rooflines of the kernels the timed step launches.
+
+    element, assembly: k_element / k_assemble, one launch each per step
+      (velocity and position integrators): algorithmic bytes per launch
+      (hobak_batch_kernel_bytes) over the CUDA-event launch time
+      (hobak_batch_time_kernels), against the measured HBM copy bandwidth;
+      the element kernel also against the FP64 pipe, from the ncu count of
+      its FP64 thread-instructions on this workload (profiles/traffic.json).
+    pcg: the step's inner solves, every refinement sweep, on whichever path
+      each scene takes (thread-block clusters, or the tile path's SpMV and
+      update kernels): per scene, PCG iterations x the bytes one iteration
+      streams (the tile path's SpMV + update bytes of that scene), summed over
+      scenes, over the phase's CUDA-event time per step.
+    spmv, pcg_update: the tile-path kernels timed over the whole batch; the
+      step launches them only for scenes on the tile path."""
+    kms = batch.time_kernels(reps=10)
+    kbytes = batch.kernel_bytes()
+    peak, peak_kind = measured_peaks()
+    traffic = ncu_traffic(workload)
+    w = 4.0 if spec["precision"] == 1 else 8.0
+    paths = batch.pcg_path()
+    n_tile = int((paths == 0).sum())
+    phase_ms = {k: v[0] / phase_steps for k, v in phases.items()}
+    newmark = spec.get("integrator") == "newmark"
+    gbs = lambda nbytes, ms: nbytes / (ms * 1e-3) / 1e9
+    ent = {}
+    for k, name in (("element", "k_element<float>" if w == 4 else "k_element<double>"),
+                    ("assemble", "k_assemble<float>" if w == 4 else "k_assemble<double>")):
+        a = gbs(kbytes[k], kms[k])
+        ent[k] = {"kernel": name, "launch_ms": kms[k], "algorithmic_bytes": kbytes[k], "GB/s": a,
+                  "frac_hbm": a / peak, "traffic": traffic.get(k),
+                  "step_ms": phase_ms["element" if k == "element" else "assembly"],
+                  "launches_per_step": None if newmark else 1}
+    fp64_inst = traffic.get("fp64_inst_element")
+    if fp64_inst and sm_mhz:
+        rate = fp64_inst / (kms["element"] * 1e-3)
+        fpeak = FP64_PER_SM_CLK * NUM_SMS * sm_mhz * 1e6
+        ent["element"]["fp64"] = {"inst_per_launch": fp64_inst, "inst_per_s": rate, "peak_inst_per_s": fpeak,
+                                  "frac": rate / fpeak, "clock_mhz": sm_mhz,
+                                  "how": "ncu FP64 thread-instructions (dadd + dmul + dfma) of one launch on this "
+                                         "workload, over the live launch time; peak 2 per SM per clock"}
+    # per-scene bytes one PCG iteration streams: the tile path's SpMV (blocks
+    # + columns, rowptr, u gathered, w written) and update (42 values per vertex)
+    per_iter = np.array([batch.blocks(i) * (9 * w + 4) + s.nv * (4 + 6 * w) + s.nv * w * 42
+                         for i, s in enumerate(scene_list)])
+    pcg_bytes = float((iters_by_scene * per_iter).sum())
+    pcg_ms = phase_ms["pcg_iterations"]
+    slow = float(iters_by_scene.max())
+    ent["pcg"] = {"kernel": ("k_pcg_cluster<1..16>" + (" + tile path" if n_tile else "")) if n_tile < len(paths)
+                  else "k_spmv + k_update (tile path)",
+                  "step_ms": pcg_ms, "algorithmic_bytes_per_step": pcg_bytes, "GB/s": gbs(pcg_bytes, pcg_ms),
+                  "frac_hbm": gbs(pcg_bytes, pcg_ms) / peak, "traffic": traffic.get("pcg"),
+                  "scenes_cluster_path": int(len(paths) - n_tile), "scenes_tile_path": n_tile,
+                  "iterations_slowest_scene": slow,
+                  "us_per_iteration_slowest_scene": 1e3 * pcg_ms / slow if slow else None,
+                  "how": "sum over scenes of PCG iterations x (SpMV + update bytes of the scene), over the "
+                         "phase's CUDA-event time per step (all refinement sweeps)"}
+    for k in ("spmv", "pcg_update"):
+        a = gbs(kbytes[k], kms[k])
+        ent[k] = {"kernel": "k_spmv" if k == "spmv" else "k_update", "launch_ms": kms[k],
+                  "algorithmic_bytes": kbytes[k], "GB/s": a, "frac_hbm": a / peak, "traffic": traffic.get(k),
+                  "note": (f"tile path, timed over every scene of the batch; the step runs it for the {n_tile} "
+                           "scene(s) on the tile path only") if n_tile < len(paths) else "tile path (every scene)"}
+    if newmark:
+        dom = "pcg"
+    else:
+        dom = max(("element", "assemble", "pcg"), key=lambda k: ent[k]["step_ms"])
+    e = ent[dom]
+    achieved = e["GB/s"]
+    binding = {"element": "FP64 pipe (2 FP64 lanes per SM per clock on GB300): see kernels.element.fp64",
+               "assemble": "latency of the gather chains",
+               "pcg": "latency: the slowest scene's iterations run one after another (barriers per iteration); "
+                      "see kernels.pcg.us_per_iteration_slowest_scene"}[dom]
+    return {"kernel": e["kernel"], "phase": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": e.get("traffic"),
+            "algorithmic_bytes": e.get("algorithmic_bytes", e.get("algorithmic_bytes_per_step")),
+            "time_ms": e.get("launch_ms", e.get("step_ms")), "binding": binding, "kernels": ent}
 
 
 def run_ours(args, spec, scene_list):
@@ -426,10 +601,12 @@ def run_ours(args, spec, scene_list):
     clocks.start()
     ev[0].record(stream)
     scene_iters = []
+    iters_by_scene = np.zeros(len(scene_list))
     for k in range(args.steps):
         st = batch.step(1)
         iters.append(max(s[0] for s in st))
         scene_iters.extend(s[0] for s in st)
+        iters_by_scene += [s[0] for s in st]
         ev[k + 1].record(stream)
     torch.cuda.synchronize()
     clock = clocks.stop()
@@ -441,6 +618,7 @@ def run_ours(args, spec, scene_list):
     batch.step(phase_steps)
     phases = batch.phase_times()
     batch.enable_timing(False)
+    iters_by_scene /= max(args.steps, 1)
     lat = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[args.steps])
     if world > 1:
@@ -449,21 +627,9 @@ def run_ours(args, spec, scene_list):
         total_ms = float(t.item())
     value = world * args.steps / (total_ms / 1e3)
 
-    # ---- kernel rooflines: per-launch CUDA-event time of the hot kernels ----
-    kms = batch.time_kernels(reps=10)
-    kbytes = batch.kernel_bytes()
-    per_step_launches = {"element": 1, "assemble": 1, "spmv": float(np.mean(iters)) + 1,
-                         "pcg_update": float(np.mean(iters)) + 1}
-    share = {k: kms[k] * per_step_launches[k] for k in kms}
-    dominant = max(share, key=share.get)
-    peak, peak_kind = measured_peaks()
-    achieved = kbytes[dominant] / (kms[dominant] * 1e-3) / 1e9
-    traffic = ncu_traffic(args.workload).get(dominant)
-    roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                "algorithmic_bytes": kbytes[dominant], "launch_ms": kms[dominant],
-                "kernels": {k: {"launch_ms": kms[k], "GB/s": kbytes[k] / (kms[k] * 1e-3) / 1e9,
-                                "launches_per_step": per_step_launches[k]} for k in kms}}
+    # ---- rooflines of the kernels the timed step runs ----
+    roofline = step_rooflines(batch, spec, scene_list, phases, phase_steps, iters_by_scene, args.workload,
+                              clock.get("sm_mhz"))
 
     # ---- e2e: public API with pinned host buffers in/out every step ----
     # whole-batch calls (every scene's state is contiguous on the device): the
@@ -502,14 +668,22 @@ def run_ours(args, spec, scene_list):
         cv, _, cores, sample = cpu_baseline(scene_list, steps, 0, integrator=spec.get("integrator", "velocity"),
                                         contact=spec.get("contact"))
         cpu = {"value": cv, "unit": "steps/s", "cores": cores, "kind": "port",
-               "sample": sample + f" of {args.workload} on the host cores (OpenMP), from the initial state"}
+               "sample": sample + f" of {args.workload} on the host cores (OpenMP), from the initial state",
+               "cpu_model": cpu_model(), **port_vs_reference()}
 
-    # the plain FP64 GPU path (one scene at a time) on the same mix
-    plain = None
-    if spec["kind"] == "mix" and not args.no_plain:
+    # the plain FP64 GPU path (one scene at a time) on the same mix, and the
+    # same mix batched in FP64 (the precision-only comparison)
+    plain = batched64 = None
+    if spec["kind"] == "mix" and not args.no_plain and spec["precision"] == 1:
         pv = plain_fp64_gpu(scene_list, 2, integrator=solver_integrator)
         plain = {"value": pv, "unit": "steps/s", "speedup_of_value": value / pv,
                  "how": "each scene its own FP64 batch (CUDA graph per step), scenes stepped one after another"}
+        bv, bms, btune = batched_fp64_gpu(scene_list, min(args.steps, 10), args.warmup, solver_integrator,
+                                          args.no_autotune)
+        batched64 = {"value": bv, "unit": "steps/s", "ms_per_step": bms, "speedup_of_value": value / bv,
+                     "launch_shapes": btune,
+                     "how": "the same mix as one FP64 batch (CUDA graph per step, autotuned launch shapes), "
+                            f"{min(args.steps, 10)} steps after {args.warmup} warm-up steps"}
 
     if rank == 0:
         lat_sorted = sorted(lat)
@@ -518,15 +692,17 @@ def run_ours(args, spec, scene_list):
                 "p50_ms": float(np.percentile(lat_sorted, 50)), "p99_ms": float(np.percentile(lat_sorted, 99)),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if spec["precision"] == 0 else "f32+f64", "data": "synthetic",
-                "config": {"workload": args.workload, **config_of(spec, scene_list),
-                           "launch_shapes": {**tuning, "chosen_by": "given" if args.no_autotune else "autotuner"}},
+                "config": {"workload": args.workload, **config_of(spec, scene_list)},
+                "preconditioner": "block_jacobi",
+                "launch_shapes": {**tuning, "chosen_by": "given" if args.no_autotune else "autotuner"},
                 "pcg_iters_per_step": float(np.mean(iters)),
                 "pcg_iters_per_scene_pct": {q: float(np.percentile(scene_iters, q)) for q in (10, 50, 90, 100)},
                 "phases_ms_per_step": {k: v[0] / phase_steps for k, v in phases.items()},
                 **({"phases_note": "the Newton loop is one graph node: its element, assembly, rhs and PCG "
                                    "time of every Newton iteration is counted under pcg_iterations"}
                    if spec.get("integrator") == "newmark" else {}),
-                "roofline": roofline, "cpu_baseline": cpu, "plain_fp64_gpu": plain, "e2e": e2e,
+                "roofline": roofline, "cpu_baseline": cpu, "plain_fp64_gpu": plain, "batched_fp64_gpu": batched64,
+                "e2e": e2e,
                 "gpu_launches": int(gpu_launches),
                 "clocks": clock}
         print(json.dumps(line), flush=True)

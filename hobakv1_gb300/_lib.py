@@ -76,6 +76,7 @@ SIGNATURES = {
     "hobak_gpu_set_external_forces": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "hobak_gpu_set_collisions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                                 ctypes.c_double]),
+    "hobak_gpu_set_edge_collisions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "hobak_gpu_set_solver": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakSolverOpts)]),
     "hobak_gpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "hobak_material_eval": (ctypes.c_int, [ctypes.POINTER(HobakMaterial), ctypes.c_int, _dp, _dp, _dp, _dp]),
@@ -89,6 +90,7 @@ SIGNATURES = {
     "hobak_batch_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "hobak_batch_kernel_bytes": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "hobak_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakTuning)]),
+    "hobak_batch_pcg_path": (ctypes.c_int, [ctypes.c_void_p, _ip]),
     "hobak_batch_get_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "hobak_batch_set_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "hobak_batch_set_pin_targets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),

@@ -2000,6 +2000,13 @@ int hobak_batch_get_tuning(hobak_batch b, hobak_tuning* out) {
   return HOBAK_OK;
 }
 
+int hobak_batch_pcg_path(hobak_batch b, int* cluster_ctas) {
+  if (!b || !cluster_ctas) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  if (int rc = prepare_cluster_classes(b)) return rc;
+  for (size_t s = 0; s < b->scenes.size(); s++) cluster_ctas[s] = b->sceneParams[s].pcgCluster;
+  return HOBAK_OK;
+}
+
 int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t) {
   if (!b || !t) return fail(HOBAK_ERR_INVALID, "bad arguments");
   if (t->element_threads != 64 && t->element_threads != 128)
@@ -2195,6 +2202,7 @@ int hobak_gpu_set_external_forces(hobak_batch b, const double* f) { return hobak
 int hobak_gpu_set_collisions(hobak_batch b, int vf_on, double eps, double stiffness, double damping_beta) {
   return hobak_batch_set_collisions(b, 0, vf_on, eps, stiffness, damping_beta);
 }
+int hobak_gpu_set_edge_collisions(hobak_batch b, int ee_on) { return hobak_batch_set_edge_collisions(b, 0, ee_on); }
 int hobak_gpu_set_solver(hobak_batch b, const hobak_solver_opts* opts) { return hobak_batch_set_solver(b, opts); }
 int hobak_gpu_destroy(hobak_batch b) { return hobak_batch_destroy(b); }
 

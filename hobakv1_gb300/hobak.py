@@ -470,6 +470,19 @@ class BATCH:
         check(_lib.load().hobak_batch_get_tuning(self.h, ctypes.byref(t)), "hobak_batch_get_tuning")
         return {k: getattr(t, k) for k in self.TUNING}
 
+    def pcg_path(self) -> np.ndarray:
+        """Per scene: CTAs of the cluster that solves its inner PCG (0: the tile path)."""
+        out = np.zeros(len(self), dtype=np.int32)
+        check(_lib.load().hobak_batch_pcg_path(self.h, iptr(out)), "hobak_batch_pcg_path")
+        return out
+
+    def blocks(self, scene: int) -> int:
+        """3x3 blocks of one scene's system matrix (its BSR pattern)."""
+        n = ctypes.c_int()
+        check(_lib.load().hobak_batch_assemble(self.h, scene, ctypes.byref(n), None, None, None, None),
+              "hobak_batch_assemble")
+        return n.value
+
     def set_tuning(self, **kw):
         cur = self.get_tuning()
         cur.update(kw)
@@ -567,7 +580,8 @@ class BACKWARD_EULER_VELOCITY:
         check(_lib.load().hobak_gpu_set_collisions(self._batch.h, int(self._vertexFaceSelfCollisionsOn),
                                                    self._collisionEps, self._collisionStiffness,
                                                    self._collisionDampingBeta), "hobak_gpu_set_collisions")
-        self._batch.set_edge_collisions(0, self._edgeEdgeSelfCollisionsOn)
+        check(_lib.load().hobak_gpu_set_edge_collisions(self._batch.h, int(self._edgeEdgeSelfCollisionsOn)),
+              "hobak_gpu_set_edge_collisions")
 
     def position(self):
         return self._position

@@ -179,8 +179,10 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts);
 /* Vertex-face self collisions of one scene (TIMESTEPPER's
  * vertexFaceSelfCollisionsOn / collisionStiffness / collisionDampingBeta,
  * TIMESTEPPER.h:62-69, and TET_MESH::setCollisionEps, TET_MESH.cpp:2160-2165).
- * Off by default (the reference's default is on; edge-edge collisions are not
- * implemented).  Detection runs on the GPU every step: a spatial hash replaces
+ * Off by default here; the reference turns vertex-face and edge-edge self
+ * collisions on by default (TIMESTEPPER.cpp:83-84), so a binding that mirrors
+ * a stock HOBAK timestepper also calls hobak_batch_set_edge_collisions
+ * (hobak_gpu_set_edge_collisions).  Detection runs on the GPU every step: a spatial hash replaces
  * the AABB tree, the narrow phase is the reference's
  * (TET_MESH_FASTER.cpp:248-334).  The first call builds the surfaces of every
  * scene in the batch. */
@@ -230,6 +232,10 @@ int hobak_gpu_set_external_forces(hobak_batch b, const double* f);
 /* vertexFaceSelfCollisionsOn(), TET_MESH::setCollisionEps, collisionStiffness(),
  * collisionDampingBeta() (TIMESTEPPER.h:62-69; TET_MESH.cpp:2160-2174). */
 int hobak_gpu_set_collisions(hobak_batch b, int vf_on, double eps, double stiffness, double damping_beta);
+/* edgeEdgeSelfCollisionsOn() (TIMESTEPPER.h:62-69; on by default in the
+ * reference, TIMESTEPPER.cpp:84): the single-scene form of
+ * hobak_batch_set_edge_collisions. */
+int hobak_gpu_set_edge_collisions(hobak_batch b, int ee_on);
 /* _cgSolver.setTolerance / setMaxIterations (IterativeSolverBase.h:281-284,
  * 363) plus precision and preconditioner. */
 int hobak_gpu_set_solver(hobak_batch b, const hobak_solver_opts* opts);
@@ -317,6 +323,10 @@ typedef struct hobak_tuning {
   double step_ms;
 } hobak_tuning;
 int hobak_batch_get_tuning(hobak_batch b, hobak_tuning* out);
+/* Which inner-PCG path each scene takes under the current tuning (no
+ * reference counterpart): cluster_ctas[s] = the CTAs of scene s's
+ * thread-block cluster, or 0 for the batch-wide tile path. */
+int hobak_batch_pcg_path(hobak_batch b, int* cluster_ctas);
 int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t);
 /* Autotuner: times the element kernel per CTA size and the assembly kernel
  * per CTA size (reps launches each, CUDA events), then whole steps for every

@@ -1888,9 +1888,12 @@ int oracle_ee_pairs(void* h, int* pairs, int* edges) {
 }
 
 // NEWMARK's energy-damped solve with GREEN_DAMPING(mu) (mu = 0: Rayleigh).
+// Only NEWMARK reads the damping: set the integrator first; other integrators
+// refuse it (the reference's energy-damped BACKWARD_EULER_VELOCITY solve reads
+// a never-computed Fdot).
 int oracle_set_green_damping(void* h, double mu) {
   Sim* s = static_cast<Sim*>(h);
-  if (!s || !(mu >= 0.0)) return -1;
+  if (!s || !(mu >= 0.0) || s->integrator != 2) return -1;
   s->greenMu = mu;
   return 0;
 }
@@ -1996,6 +1999,17 @@ int oracle_threads() {
 #ifdef _OPENMP
   return omp_get_max_threads();
 #else
+  return 1;
+#endif
+}
+
+// Threads of the OpenMP regions that follow (n <= 0: every host core).
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
+  return omp_get_max_threads();
+#else
+  (void)n;
   return 1;
 #endif
 }

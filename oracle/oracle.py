@@ -63,8 +63,14 @@ def lib():
         L.oracle_get_acceleration.argtypes = [ctypes.c_void_p, _dp]
         L.oracle_energy.argtypes = [ctypes.c_void_p]
         L.oracle_energy.restype = ctypes.c_double
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
+
+
+def set_threads(n: int) -> int:
+    """OpenMP threads of the oracle's next calls (n <= 0: every host core)."""
+    return lib().oracle_set_threads(int(n))
 
 
 def _d(a):

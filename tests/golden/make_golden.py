@@ -6,7 +6,7 @@ so this only runs where they are).  Inputs come from hobakv1_gb300.scenes, so
 they are regenerated bit-identically anywhere.  Usage:
 
     make -C oracle/ref REF=<reference checkout> -j8
-    python tests/golden/make_golden.py [elements] [trajectories] [position] [newmark] [collisions]
+    python tests/golden/make_golden.py [elements] [trajectories] [position] [newmark] [green] [collisions]
 """
 from __future__ import annotations
 
@@ -92,6 +92,23 @@ def make_newmark_trajectories():
         print("newmark trajectory", s.name, r["iters"].sum())
 
 
+def make_green_damping():
+    """NEWMARK's energy-damped solve with GREEN_DAMPING(mu) (NEWMARK.cpp:
+    344-420) on the 5^3 cube hanging under gravity, mu = 0.05 and 1.0, six
+    steps each (every step recorded)."""
+    s = scenes.config1_scene(5)
+    out = {}
+    for mu in (0.05, 1.0):
+        r = refrun.run(s, 6, integrator="newmark", green_damping=mu)
+        tag = f"mu{mu:g}".replace(".", "p")
+        out[f"x_{tag}"] = r["x"]
+        out[f"v_{tag}"] = r["v"]
+        out[f"iters_{tag}"] = r["iters"]
+    np.savez_compressed(os.path.join(OUT, f"traj_{s.name}_newmark_green.npz"), steps=6, mus=np.array([0.05, 1.0]),
+                        **out)
+    print("green damping", s.name)
+
+
 def make_collisions():
     """Two cubes in contact: vertex-face pairs (reference AABB broad phase +
     narrow phase) at the start and along a 40-step trajectory with collisions."""
@@ -110,7 +127,7 @@ def make_collisions():
 if __name__ == "__main__":
     if not refrun.available():
         sys.exit("reference build missing: make -C oracle/ref REF=<reference checkout>")
-    which = set(sys.argv[1:]) or {"elements", "trajectories", "position", "newmark", "collisions"}
+    which = set(sys.argv[1:]) or {"elements", "trajectories", "position", "newmark", "green", "collisions"}
     if "elements" in which:
         make_elements()
     if "trajectories" in which:
@@ -119,5 +136,7 @@ if __name__ == "__main__":
         make_position_trajectories()
     if "newmark" in which:
         make_newmark_trajectories()
+    if "green" in which:
+        make_green_damping()
     if "collisions" in which:
         make_collisions()

@@ -10,7 +10,7 @@ frame (plus the first three and the last) -- for the two-tet contact scenes
 also the same frames from the reference built here (oracle/ref) and the
 recorded vertex-face pair counts -- and newmark_stretch_head.json.gz: that
 file's scene object and first three frames unchanged, for the JSON reader.
-Reads the reference checkout at /root/reference (this container only)."""
+Reads the reference checkout named by HOBAK_REF (where it exists)."""
 import gzip
 import json
 import os
@@ -22,7 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from hobakv1_gb300.replay import read_tobj  # noqa: E402
 
-REF = "/root/reference"
+REF = os.environ.get("HOBAK_REF", "")
+if not os.path.isdir(os.path.join(REF, "data")):
+    sys.exit("set HOBAK_REF to the reference checkout")
 SCENES = {"newmark_stretch": ("data/regression/newmark_stretch.json.gz", "data/cube_10.tobj", 3),
           "two_tet_drop_vf": ("data/regression/two_tet_drop_vf.json", "data/two_tets_vertex_face.tobj", 1),
           "two_tet_kiss_vf": ("data/regression/two_tet_kiss_vf.json", "data/two_tets_vertex_face_kiss.tobj", 1),

@@ -151,19 +151,49 @@ def test_oracle_vertex_face_collisions_match_reference():
         assert sorted(map(tuple, pairs.tolist())) == sorted(map(tuple, ref.tolist())), k
 
 
-def test_oracle_green_damped_newmark_matches_the_reference_when_built():
+def test_oracle_green_damped_newmark_matches_the_reference_fixture():
     """NEWMARK's energy-damped solve with GREEN_DAMPING(mu) (NEWMARK.cpp:
-    344-480): the restatement against the reference built here (oracle/ref),
-    when that build exists in this checkout."""
+    344-420, GREEN_DAMPING.cpp:46-74): the restatement against the committed
+    trajectories of the reference built from its sources
+    (traj_kuhn5_snh_newmark_green.npz, tests/golden/make_golden.py green),
+    six steps at mu = 0.05 and 1.0."""
+    g = np.load(os.path.join(GOLDEN, "traj_kuhn5_snh_newmark_green.npz"))
+    s = scenes.config1_scene(5)
+    undamped = oracle.Sim(s, precond=0, integrator="newmark")
+    undamped.step(int(g["steps"]))
+    xu, _ = undamped.state()
+    for mu in g["mus"]:
+        tag = f"mu{mu:g}".replace(".", "p")
+        xr = g[f"x_{tag}"]
+        sim = oracle.Sim(s, precond=0, integrator="newmark")
+        sim.set_green_damping(mu)
+        for k in range(int(g["steps"])):
+            sim.step(1)
+            x, _ = sim.state()
+            assert np.linalg.norm(x - xr[k + 1]) / np.linalg.norm(xr[k + 1]) < 1e-12, (mu, k)
+        # the damping term matters at this size: far above the bound
+        assert np.linalg.norm(xu - xr[-1]) / np.linalg.norm(xr[-1]) > 1e-7, mu
+
+
+def test_oracle_green_damping_refused_outside_newmark():
+    """Only NEWMARK's energy-damped solve is defined (the reference's damped
+    BACKWARD_EULER_VELOCITY reads a never-computed Fdot)."""
+    sim = oracle.Sim(scenes.config1_scene(3), precond=0)
+    assert oracle.lib().oracle_set_green_damping(sim.h, 0.1) == -1
+
+
+def test_oracle_green_damped_newmark_matches_the_reference_when_built():
+    """The same against a live run of the reference build, when that build
+    exists in this checkout."""
     from oracle import refrun
     if not os.path.exists(refrun.REF_BIN):
         pytest.skip("reference build not present")
     s = scenes.config1_scene(5)
     for mu in (0.05, 1.0):
-        r = refrun.run(s, 4, integrator="newmark", green_damping=mu)
+        r = refrun.run(s, 6, integrator="newmark", green_damping=mu)
         sim = oracle.Sim(s, precond=0, integrator="newmark")
         sim.set_green_damping(mu)
-        for k in range(4):
+        for k in range(6):
             sim.step(1)
             x, _ = sim.state()
             assert np.linalg.norm(x - r["x"][k + 1]) / np.linalg.norm(r["x"][k + 1]) < 1e-12, (mu, k)
