@@ -28,7 +28,11 @@ import numpy as np
 BASE_SEED = 20261203
 
 # material kinds; the integer codes are the C ABI's HOBAK_MATERIAL_* values
-MATERIALS = {"snh": 0, "arap": 1, "stvk": 2, "linear": 3, "neo_hookean_bw": 4, "snh_barrier": 5}
+MATERIALS = {"snh": 0, "arap": 1, "stvk": 2, "linear": 3, "neo_hookean_bw": 4, "snh_barrier": 5,
+             "aniso_arap": 6, "aniso_stvk": 7, "aniso_fung": 8, "aniso_dirichlet": 9}
+ANISOTROPIC = ("aniso_arap", "aniso_stvk", "aniso_fung", "aniso_dirichlet")
+# fibre direction of the anisotropic test scenes (normalised by the material)
+FIBER = (0.3, 0.8, -0.52)
 
 
 def lame(E: float, nu: float):
@@ -142,6 +146,7 @@ class Scene:
     gravity: tuple = (0.0, -9.8, 0.0)
     dt: float = 1.0 / 60.0
     N: int = 0
+    fiber: Optional[tuple] = None  # anisotropic energies: fibre direction a
 
     @property
     def nv(self) -> int:
@@ -169,6 +174,19 @@ def config2_scene(N: int = 40, material: str = "snh") -> Scene:
     x = compress_and_twist(rest, N)
     return Scene(f"kuhn{N}_{material}_twist", rest, tets, material, mu, lam, top_layer(N),
                  x - rest, np.zeros_like(rest), N=N)
+
+
+def aniso_scene(N: int = 6, material: str = "aniso_arap", fiber=FIBER) -> Scene:
+    """An anisotropic energy (ANISOTROPIC_ARAP / STVK / FUNG / DIRICHLET, with
+    mu from E = 1e4, nu = 0.45 and fibre direction `fiber`) on the compressed
+    and twisted Kuhn cube of config2_scene, top layer pinned, no gravity: the
+    cube springs back along the fibre."""
+    s = config2_scene(N, "snh")
+    s.name = f"kuhn{N}_{material}_twist"
+    s.material = material
+    s.fiber = tuple(float(c) for c in fiber)
+    s.gravity = (0.0, 0.0, 0.0)
+    return s
 
 
 def config4_scenes(count: int = 256, nmin: int = 6, nmax: int = 24,

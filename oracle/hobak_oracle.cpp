@@ -27,7 +27,12 @@
 
 namespace {
 
-enum Material { SNH = 0, ARAP = 1, STVK = 2, LINEAR = 3, NHBW = 4, SNHB = 5 };
+enum Material {
+  SNH = 0, ARAP = 1, STVK = 2, LINEAR = 3, NHBW = 4, SNHB = 5,
+  // anisotropic energies along a fibre direction a (Hyperelastic/Volume/ANISOTROPIC_*.cpp)
+  AARAP = 6, ASTVK = 7, AFUNG = 8, ADIR = 9
+};
+inline bool anisotropic(int kind) { return kind >= AARAP && kind <= ADIR; }
 
 inline double det3(const double* A) {
   return A[0] * (A[4] * A[8] - A[7] * A[5]) - A[3] * (A[1] * A[8] - A[7] * A[2]) +
@@ -197,10 +202,15 @@ void eig3sym(const double* Ain, double* Q, double* L) {
 struct MaterialParams {
   int kind;
   double mu, lambda, alpha;
+  double a[3];  // anisotropic energies: unit fibre direction (the constructor normalises it)
 };
 
-MaterialParams makeMaterial(int kind, double mu, double lambda) {
-  MaterialParams m{kind, mu, lambda, 0.0};
+MaterialParams makeMaterial(int kind, double mu, double lambda, const double* fiber = nullptr) {
+  MaterialParams m{kind, mu, lambda, 0.0, {1.0, 0.0, 0.0}};
+  if (fiber) {  // ANISOTROPIC_ARAP.cpp:26-29 (_a.normalize(), _A = a a^T)
+    const double n = std::sqrt(fiber[0] * fiber[0] + fiber[1] * fiber[1] + fiber[2] * fiber[2]);
+    for (int i = 0; i < 3; i++) m.a[i] = n > 0.0 ? fiber[i] / n : fiber[i];
+  }
   if (kind == SNH) {  // SNH.cpp:23-32
     m.lambda = lambda + mu;
     m.alpha = 1.0 + m.mu / m.lambda;
@@ -236,10 +246,128 @@ inline double sqnorm9(const double* A) {
   return s;
 }
 
+// Anisotropic energies (ANISOTROPIC_ARAP/STVK/FUNG/DIRICHLET.cpp): with the
+// unit fibre direction a, g = F a, F A = g a^T (A = a a^T) and
+// I5 = |F a|^2 (invariant5, MATRIX_UTIL.cpp:553-556).  Every stress is a
+// scalar times F A, every Hessian alpha H5 + beta fa fa^T with
+// H5 = kronIdentity(A) (MATRIX_UTIL.cpp:512-524) and fa = vec(F A).
+void fiberTerms(const MaterialParams& m, const double* F, double* g, double* FA, double& I5) {
+  for (int i = 0; i < 3; i++) g[i] = F[i] * m.a[0] + F[i + 3] * m.a[1] + F[i + 6] * m.a[2];
+  I5 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) {
+      double s = 0;
+      for (int k = 0; k < 3; k++) s += F[i + 3 * k] * (m.a[k] * m.a[j]);
+      FA[i + 3 * j] = s;
+    }
+}
+
+// I4 = a^T (V Sigma V^T) a with svd_rv (invariant4, MATRIX_UTIL.cpp:545-552);
+// only its sign and magnitude near 0 are used
+double invariant4(const MaterialParams& m, const double* F) {
+  double U[9], S[3], V[9];
+  svd_rv(F, U, S, V);
+  double I4 = 0;
+  for (int k = 0; k < 3; k++) {
+    const double va = V[3 * k] * m.a[0] + V[3 * k + 1] * m.a[1] + V[3 * k + 2] * m.a[2];
+    I4 += S[k] * va * va;
+  }
+  return I4;
+}
+
+double psiAniso(const MaterialParams& m, const double* F) {
+  double g[3], FA[9], I5;
+  fiberTerms(m, F, g, FA, I5);
+  switch (m.kind) {
+    case AARAP: {  // ANISOTROPIC_ARAP.cpp:40-47
+      const double SI4 = invariant4(m, F) > 0.0 ? 1.0 : -1.0;
+      const double diff = std::sqrt(I5) - SI4;
+      return 0.5 * m.mu * diff * diff;
+    }
+    case ASTVK: return 0.5 * m.mu * (I5 - 1.0) * (I5 - 1.0);   // ANISOTROPIC_STVK.cpp:42-46
+    case AFUNG: return m.mu * (std::exp(I5 - 1.0) - I5);       // ANISOTROPIC_FUNG.cpp:40-44
+    default: return m.mu * I5;                                 // ANISOTROPIC_DIRICHLET.cpp:36-39
+  }
+}
+
+// P = s(F) F A: ANISOTROPIC_ARAP.cpp:52-65 (with its |I4| < 1e-8 branch),
+// ANISOTROPIC_STVK.cpp:51-55, ANISOTROPIC_FUNG.cpp:50-54, ANISOTROPIC_DIRICHLET.cpp:44-47
+void PK1Aniso(const MaterialParams& m, const double* F, double* P) {
+  double g[3], FA[9], I5, sc;
+  fiberTerms(m, F, g, FA, I5);
+  switch (m.kind) {
+    case AARAP: {
+      const double I4 = invariant4(m, F);
+      const double SI4 = I4 > 0.0 ? 1.0 : -1.0;
+      sc = std::fabs(I4) >= 1e-8 ? m.mu * (1.0 - SI4 / std::sqrt(I5)) : -1.0 * m.mu * (1.0 - 1.0 / 2.0);
+      break;
+    }
+    case ASTVK: sc = 2.0 * m.mu * (I5 - 1.0); break;
+    case AFUNG: sc = 2.0 * m.mu * (std::exp(I5 - 1.0) - 1.0); break;
+    default: sc = 2.0 * m.mu; break;
+  }
+  for (int k = 0; k < 9; k++) P[k] = sc * FA[k];
+}
+
+// (alpha, beta) of the Hessian alpha H5 + beta fa fa^T, clamped or not:
+// ANISOTROPIC_ARAP.cpp:70-110, ANISOTROPIC_STVK.cpp:60-100,
+// ANISOTROPIC_FUNG.cpp:60-105, ANISOTROPIC_DIRICHLET.cpp:52-77.
+void hessianAnisoCoeffs(const MaterialParams& m, const double* F, bool clamp, double& al, double& be) {
+  double g[3], FA[9], I5;
+  fiberTerms(m, F, g, FA, I5);
+  const double fa2 = sqnorm9(FA);
+  switch (m.kind) {
+    case AARAP: {
+      const double SI4 = invariant4(m, F) > 0.0 ? 1.0 : -1.0;
+      if (!clamp || I5 >= SI4) {
+        const double si = 1.0 / std::sqrt(I5);
+        al = m.mu * (1.0 - SI4 * si);
+        be = m.mu * (SI4 * si * si * si);
+      } else {
+        al = 0.0;
+        be = m.mu * (1.0 / I5);
+      }
+      return;
+    }
+    case ASTVK:
+    case AFUNG: {
+      const double e = m.kind == AFUNG ? std::exp(I5 - 1.0) : 1.0;
+      const double l1 = m.kind == AFUNG ? 2.0 * m.mu * (e - 1.0) : 2.0 * m.mu * (I5 - 1.0);
+      const double l0 = m.kind == AFUNG ? l1 + 4.0 * m.mu * I5 * e : l1 + 4.0 * m.mu * I5;
+      if (!clamp || (l0 > 0.0 && l1 > 0.0)) {
+        al = l1;
+        be = 4.0 * m.mu * e;
+      } else if (l0 < 0.0) {
+        al = be = 0.0;
+      } else {  // lambda0 along fa / |fa| (Eigen's normalized(): fa itself when |fa| = 0)
+        al = 0.0;
+        be = fa2 > 0.0 ? l0 / fa2 : l0;
+      }
+      return;
+    }
+    default:
+      al = 2.0 * m.mu;
+      be = 0.0;
+      return;
+  }
+}
+
+void hessianAniso(const MaterialParams& m, const double* F, bool clamp, double* H9) {
+  double g[3], FA[9], I5, al, be;
+  fiberTerms(m, F, g, FA, I5);
+  hessianAnisoCoeffs(m, F, clamp, al, be);
+  for (int c = 0; c < 9; c++)
+    for (int r = 0; r < 9; r++) {
+      const double h5 = (r % 3 == c % 3) ? m.a[r / 3] * m.a[c / 3] : 0.0;
+      H9[r + 9 * c] = al * h5 + be * FA[r] * FA[c];
+    }
+}
+
 // Strain energy density psi(F): SNH.cpp:34-43, ARAP.cpp:39-43 (through
 // HYPERELASTIC.cpp:41-47), STVK.cpp psi, LINEAR.cpp psi, NEO_HOOKEAN_BW.cpp psi,
 // SNH_WITH_BARRIER.cpp psi.
 double psi(const MaterialParams& m, const double* F) {
+  if (anisotropic(m.kind)) return psiAniso(m, F);
   switch (m.kind) {
     case SNH: {
       const double Ic = sqnorm9(F), Jm = det3(F) - m.alpha;
@@ -288,6 +416,7 @@ double psi(const MaterialParams& m, const double* F) {
 // HYPERELASTIC.cpp:61-67), STVK.cpp PK1, LINEAR.cpp PK1, NEO_HOOKEAN_BW.cpp PK1,
 // SNH_WITH_BARRIER.cpp PK1.
 void PK1(const MaterialParams& m, const double* F, double* P) {
+  if (anisotropic(m.kind)) return PK1Aniso(m, F, P);
   switch (m.kind) {
     case SNH: {
       double G[9];
@@ -378,10 +507,10 @@ void scaling(const double* U, const double* Q3, const double* V, double* Q9) {
       }
 }
 
-// H9 = Q diag(max(L, 0)) Q^T
-void assembleClamped(const double* Q9, double* L, double* H9) {
+// H9 = Q diag(max(L, 0)) Q^T (clamp) or Q diag(L) Q^T
+void assembleClamped(const double* Q9, double* L, double* H9, bool clamp = true) {
   for (int k = 0; k < 9; k++)
-    if (L[k] < 0.0) L[k] = 0.0;
+    if (clamp && L[k] < 0.0) L[k] = 0.0;
   for (int c = 0; c < 9; c++)
     for (int r = 0; r < 9; r++) {
       double s = 0;
@@ -394,7 +523,20 @@ void assembleClamped(const double* Q9, double* L, double* H9) {
 // (U, Sigma, V): SNH.cpp:94-144, ARAP.cpp:113-135, STVK.cpp buildEigensystem
 // (Appendix F.1 eigensystem), LINEAR.cpp hessian (no clamp),
 // NEO_HOOKEAN_BW.cpp clampedHessian, SNH_WITH_BARRIER.cpp clampedHessian.
-void clampedHessian(const MaterialParams& m, const double* U, const double* S, const double* V, double* H9) {
+// With clamp = false the same eigensystem gives the unclamped Hessian
+// (SNH.cpp, STVK.cpp, LINEAR.cpp, NEO_HOOKEAN_BW.cpp, SNH_WITH_BARRIER.cpp
+// hessian(F); ARAP.cpp hessian(U, Sigma, V)).  Anisotropic energies take the
+// F-form through F = U diag(Sigma) V^T, as HYPERELASTIC.cpp:99-103 does.
+void eigenHessian(const MaterialParams& m, const double* U, const double* S, const double* V, double* H9,
+                  bool clamp) {
+  if (anisotropic(m.kind)) {
+    double US[9], F[9];
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < 3; i++) US[i + 3 * j] = U[i + 3 * j] * S[j];
+    mul3t(US, V, F);
+    hessianAniso(m, F, clamp, H9);
+    return;
+  }
   double Q9[81], L[9];
   const double s0 = S[0], s1 = S[1], s2 = S[2];
   if (m.kind == LINEAR) {
@@ -419,7 +561,7 @@ void clampedHessian(const MaterialParams& m, const double* U, const double* S, c
     L[2] = m.mu * (2.0 - 4.0 / (s0 + s1));
     const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     scaling(U, I3, V, Q9);
-    assembleClamped(Q9, L, H9);
+    assembleClamped(Q9, L, H9, clamp);
     return;
   }
   double A[9];
@@ -490,7 +632,11 @@ void clampedHessian(const MaterialParams& m, const double* U, const double* S, c
   eig3sym(A, Q3, L3);
   for (int k = 0; k < 3; k++) L[6 + k] = L3[k];
   scaling(U, Q3, V, Q9);
-  assembleClamped(Q9, L, H9);
+  assembleClamped(Q9, L, H9, clamp);
+}
+
+void clampedHessian(const MaterialParams& m, const double* U, const double* S, const double* V, double* H9) {
+  eigenHessian(m, U, S, V, H9, true);
 }
 
 // pFpx (9x12) from DmInv (TET_MESH.cpp:197-252): column 3*a+i, row i+3*j.
@@ -1745,13 +1891,15 @@ void stepNewmark(Sim& s) {
 extern "C" {
 
 // Per-tet quantities at displacement `disp`; any output pointer may be null.
+// fiber: the anisotropic energies' direction (may be null otherwise); H9u:
+// the unclamped 9x9 Hessian (HYPERELASTIC.h:44).
 int oracle_elements(int nv, int nt, const double* rest, const int* tets, const double* disp, int material, double mu,
-                    double lambda, double* F, double* Sigma, double* psiOut, double* P, double* H9, double* fe,
-                    double* He) {
+                    double lambda, const double* fiber, double* F, double* Sigma, double* psiOut, double* P,
+                    double* H9, double* fe, double* He, double* H9u) {
   if (nv <= 0 || nt <= 0 || !rest || !tets || !disp) return -1;
   Mesh M;
   buildMesh(M, nv, nt, rest, tets);
-  const MaterialParams mat = makeMaterial(material, mu, lambda);
+  const MaterialParams mat = makeMaterial(material, mu, lambda, fiber);
 #pragma omp parallel for schedule(static)
   for (int t = 0; t < nt; t++) {
     double f[9], U[9], S[3], V[9], fl[12], H[144];
@@ -1761,6 +1909,7 @@ int oracle_elements(int nv, int nt, const double* rest, const int* tets, const d
     if (psiOut) psiOut[t] = psi(mat, f);
     if (P) PK1(mat, f, P + 9 * (size_t)t);
     if (H9) clampedHessian(mat, U, S, V, H9 + 81 * (size_t)t);
+    if (H9u) eigenHessian(mat, U, S, V, H9u + 81 * (size_t)t, false);
     if (fe) std::memcpy(fe + 12 * (size_t)t, fl, sizeof(fl));
     if (He) std::memcpy(He + 144 * (size_t)t, H, sizeof(H));
   }
@@ -1793,6 +1942,15 @@ void* oracle_create(int nv, int nt, const double* rest, const int* tets, int mat
 }
 
 void oracle_destroy(void* h) { delete static_cast<Sim*>(h); }
+
+// Fibre direction of an anisotropic material (normalised here, as the
+// reference constructors do, ANISOTROPIC_ARAP.cpp:26-29).
+int oracle_set_fiber(void* h, const double* a) {
+  Sim* s = static_cast<Sim*>(h);
+  if (!s || !a || !anisotropic(s->mat.kind)) return -1;
+  s->mat = makeMaterial(s->mat.kind, s->mat.mu, s->mat.lambda, a);
+  return 0;
+}
 
 int oracle_set_state(void* h, const double* x, const double* v) {
   Sim* s = static_cast<Sim*>(h);

@@ -19,7 +19,8 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
 _lib = None
 
-MATERIALS = {"snh": 0, "arap": 1, "stvk": 2, "linear": 3, "neo_hookean_bw": 4, "snh_barrier": 5}
+MATERIALS = {"snh": 0, "arap": 1, "stvk": 2, "linear": 3, "neo_hookean_bw": 4, "snh_barrier": 5,
+             "aniso_arap": 6, "aniso_stvk": 7, "aniso_fung": 8, "aniso_dirichlet": 9}
 
 
 def build(quiet: bool = True) -> str:
@@ -36,7 +37,8 @@ def lib():
             build()
         L = ctypes.CDLL(LIB_PATH)
         L.oracle_elements.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp, ctypes.c_int, ctypes.c_double,
-                                      ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+                                      ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oracle_set_fiber.argtypes = [ctypes.c_void_p, _dp]
         L.oracle_svd.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp]
         L.oracle_create.restype = ctypes.c_void_p
         L.oracle_create.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _ip, ctypes.c_int, ctypes.c_double,
@@ -81,17 +83,20 @@ def _i(a):
     return a.ctypes.data_as(_ip) if a is not None else None
 
 
-def elements(rest, tets, x, material, mu, lam):
+def elements(rest, tets, x, material, mu, lam, fiber=None):
+    """Per-tet F, svd_rv sigma, psi, PK1, clamped and unclamped 9x9 Hessians
+    (H9, H9u), element forces and 12x12 element Hessians."""
     rest = np.ascontiguousarray(rest, dtype=np.float64)
     tets = np.ascontiguousarray(tets, dtype=np.int32)
     x = np.ascontiguousarray(x, dtype=np.float64)
+    a = np.ascontiguousarray(fiber, dtype=np.float64) if fiber is not None else None
     nv, nt = rest.shape[0], tets.shape[0]
     out = {k: np.zeros((nt, n)) for k, n in
-           [("F", 9), ("Sigma", 3), ("P", 9), ("H9", 81), ("fe", 12), ("He", 144)]}
+           [("F", 9), ("Sigma", 3), ("P", 9), ("H9", 81), ("fe", 12), ("He", 144), ("H9u", 81)]}
     out["psi"] = np.zeros(nt)
-    rc = lib().oracle_elements(nv, nt, _d(rest), _i(tets), _d(x), MATERIALS[material], mu, lam,
+    rc = lib().oracle_elements(nv, nt, _d(rest), _i(tets), _d(x), MATERIALS[material], mu, lam, _d(a),
                                _d(out["F"]), _d(out["Sigma"]), _d(out["psi"]), _d(out["P"]),
-                               _d(out["H9"]), _d(out["fe"]), _d(out["He"]))
+                               _d(out["H9"]), _d(out["fe"]), _d(out["He"]), _d(out["H9u"]))
     assert rc == 0
     return out
 
@@ -122,6 +127,9 @@ class Sim:
         assert self.h
         x0 = np.ascontiguousarray(scene.x0.reshape(-1), dtype=np.float64)
         v0 = np.ascontiguousarray(scene.v0.reshape(-1), dtype=np.float64)
+        if getattr(scene, "fiber", None) is not None:
+            a = np.ascontiguousarray(scene.fiber, dtype=np.float64)
+            assert L.oracle_set_fiber(self.h, _d(a)) == 0
         L.oracle_set_state(self.h, _d(x0), _d(v0))
         pins = np.ascontiguousarray(scene.pinned, dtype=np.int32)
         assert L.oracle_attach_pins(self.h, len(pins), _i(pins)) == 0

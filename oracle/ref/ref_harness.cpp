@@ -5,9 +5,11 @@
 //
 // Modes (all inputs/outputs are .npy files in a directory):
 //   elements <in> <out> <material> <mu> <lambda>
-//       per-tet F, svd_rv(F), psi, PK1, clampedHessian, element forces and
+//       per-tet F, svd_rv(F), psi, PK1, clampedHessian, hessian, element forces and
 //       12x12 Hessians, plus the assembled R and CSC K
-//       (TET_MESH.cpp:643-770, TET_MESH_FASTER.cpp:89-133).
+//       (TET_MESH.cpp:643-770, TET_MESH_FASTER.cpp:89-133).  Anisotropic
+//       materials (aniso_arap, aniso_stvk, aniso_fung, aniso_dirichlet) take
+//       their fibre direction from <in>/fiber.npy (run mode too).
 //   run <in> <out> <material> <mu> <lambda> <steps> <stride>
 //       BACKWARD_EULER_VELOCITY::solve (Timestepper/BACKWARD_EULER_VELOCITY.cpp:96-235)
 //       or BACKWARD_EULER_POSITION::solve (Timestepper/BACKWARD_EULER_POSITION.cpp:129-330)
@@ -32,6 +34,10 @@
 #include "Geometry/CUBE.h"
 #include "Damping/Volume/GREEN_DAMPING.h"
 #include "Geometry/TET_MESH_FASTER.h"
+#include "Hyperelastic/Volume/ANISOTROPIC_ARAP.h"
+#include "Hyperelastic/Volume/ANISOTROPIC_DIRICHLET.h"
+#include "Hyperelastic/Volume/ANISOTROPIC_FUNG.h"
+#include "Hyperelastic/Volume/ANISOTROPIC_STVK.h"
 #include "Hyperelastic/Volume/ARAP.h"
 #include "Hyperelastic/Volume/LINEAR.h"
 #include "Hyperelastic/Volume/NEO_HOOKEAN_BW.h"
@@ -132,7 +138,21 @@ class HarnessNewmark : public TIMESTEPPER::NEWMARK {
   }
 };
 
-std::unique_ptr<VOLUME::HYPERELASTIC> makeMaterial(const std::string& name, double mu, double lambda) {
+// fibre direction of the anisotropic energies: <in>/fiber.npy (3 doubles), else x
+VECTOR3 loadFiber(const std::string& dir) {
+  FILE* f = std::fopen((dir + "/fiber.npy").c_str(), "rb");
+  if (!f) return VECTOR3(1, 0, 0);
+  std::fclose(f);
+  npy::Array a = npy::load(dir + "/fiber.npy");
+  return VECTOR3(a.f8()[0], a.f8()[1], a.f8()[2]);
+}
+
+std::unique_ptr<VOLUME::HYPERELASTIC> makeMaterial(const std::string& name, double mu, double lambda,
+                                                   const VECTOR3& fiber = VECTOR3(1, 0, 0)) {
+  if (name == "aniso_arap") return std::make_unique<VOLUME::ANISOTROPIC_ARAP>(mu, fiber);
+  if (name == "aniso_stvk") return std::make_unique<VOLUME::ANISOTROPIC_STVK>(mu, fiber);
+  if (name == "aniso_fung") return std::make_unique<VOLUME::ANISOTROPIC_FUNG>(mu, fiber);
+  if (name == "aniso_dirichlet") return std::make_unique<VOLUME::ANISOTROPIC_DIRICHLET>(mu, fiber);
   if (name == "snh") return std::make_unique<VOLUME::SNH>(mu, lambda);
   if (name == "arap") return std::make_unique<VOLUME::ARAP>(mu, lambda);
   if (name == "stvk") return std::make_unique<VOLUME::STVK>(mu, lambda);
@@ -174,7 +194,7 @@ int modeElements(const std::string& in, const std::string& out, const std::strin
   loadMesh(in, rest, tets);
   const long nv = rest.size(), nt = tets.size();
   HarnessMesh mesh(rest, tets);
-  auto material = makeMaterial(mat, mu, lambda);
+  auto material = makeMaterial(mat, mu, lambda, loadFiber(in));
   mesh.setDisplacement(loadVector(in + "/x.npy", 3 * nv));
   mesh.computeFs();
   mesh.computeSVDs();
@@ -183,7 +203,8 @@ int modeElements(const std::string& in, const std::string& out, const std::strin
   save3(out + "/U.npy", mesh.Us());
   save3(out + "/V.npy", mesh.Vs());
   save3(out + "/DmInv.npy", mesh.DmInvs());
-  std::vector<double> sig(3 * nt), psi(nt), P(9 * nt), H9(81 * nt), fe(12 * nt), H12(144 * nt), vol(nt);
+  std::vector<double> sig(3 * nt), psi(nt), P(9 * nt), H9(81 * nt), H9u(81 * nt), fe(12 * nt), H12(144 * nt),
+      vol(nt);
   for (long i = 0; i < nt; i++) {
     const MATRIX3& F = mesh.Fs()[i];
     for (int k = 0; k < 3; k++) sig[3 * i + k] = mesh.Sigmas()[i][k];
@@ -195,6 +216,9 @@ int modeElements(const std::string& in, const std::string& out, const std::strin
     const MATRIX9 H = material->clampedHessian(mesh.Us()[i], mesh.Sigmas()[i], mesh.Vs()[i]);
     for (int c = 0; c < 9; c++)
       for (int r = 0; r < 9; r++) H9[81 * i + 9 * c + r] = H(r, c);  // column-major
+    const MATRIX9 Hu = material->hessian(F);  // unclamped (HYPERELASTIC.h:44)
+    for (int c = 0; c < 9; c++)
+      for (int r = 0; r < 9; r++) H9u[81 * i + 9 * c + r] = Hu(r, c);
     const MATRIX9x12& pFpx = mesh.pFpxs()[i];
     const VECTOR12 f = -vol[i] * (pFpx.transpose() * pf);
     for (int k = 0; k < 12; k++) fe[12 * i + k] = f[k];
@@ -206,6 +230,7 @@ int modeElements(const std::string& in, const std::string& out, const std::strin
   npy::save(out + "/psi.npy", psi.data(), "<f8", {nt});
   npy::save(out + "/P.npy", P.data(), "<f8", {nt, 9});
   npy::save(out + "/H9.npy", H9.data(), "<f8", {nt, 81});
+  npy::save(out + "/H9u.npy", H9u.data(), "<f8", {nt, 81});
   npy::save(out + "/fe.npy", fe.data(), "<f8", {nt, 12});
   npy::save(out + "/He.npy", H12.data(), "<f8", {nt, 144});
   npy::save(out + "/restVolume.npy", vol.data(), "<f8", {nt});
@@ -246,7 +271,7 @@ int runWith(const std::string& in, const std::string& out, const std::string& ma
 
   HarnessMesh mesh(rest, tets);
   if (vf || ee) mesh.setCollisionEps(collEps);
-  auto material = makeMaterial(mat, mu, lambda);
+  auto material = makeMaterial(mat, mu, lambda, loadFiber(in));
   const VECTOR x0 = loadVector(in + "/x0.npy", 3 * nv);
   const VECTOR v0 = loadVector(in + "/v0.npy", 3 * nv);
   npy::Array pins = npy::load(in + "/pinned.npy");

@@ -30,10 +30,13 @@ def _read_dir(d):
     return {f[:-4]: np.load(os.path.join(d, f)) for f in os.listdir(d) if f.endswith(".npy")}
 
 
-def elements(rest, tets, x, material, mu, lam):
-    """Per-tet F, svd_rv, psi, PK1, clamped Hessian, element force/Hessian, R and CSC K."""
+def elements(rest, tets, x, material, mu, lam, fiber=None):
+    """Per-tet F, svd_rv, psi, PK1, clamped and unclamped Hessians, element
+    force/Hessian, R and CSC K (fiber: the anisotropic energies' direction)."""
     with tempfile.TemporaryDirectory() as tin, tempfile.TemporaryDirectory() as tout:
         _write_mesh(tin, rest, tets)
+        if fiber is not None:
+            np.save(os.path.join(tin, "fiber.npy"), np.asarray(fiber, dtype=np.float64))
         np.save(os.path.join(tin, "x.npy"), np.ascontiguousarray(x, dtype=np.float64).reshape(-1))
         subprocess.run([REF_BIN, "elements", tin, tout, material, repr(float(mu)), repr(float(lam))],
                        check=True, stdout=subprocess.DEVNULL)
@@ -49,6 +52,8 @@ def run(scene, steps, stride=1, tol=1e-8, maxit=1000, vf=False, ee=False,
     for `steps` steps on `scene`."""
     with tempfile.TemporaryDirectory() as tin, tempfile.TemporaryDirectory() as tout:
         _write_mesh(tin, scene.rest, scene.tets)
+        if getattr(scene, "fiber", None) is not None:
+            np.save(os.path.join(tin, "fiber.npy"), np.asarray(scene.fiber, dtype=np.float64))
         np.save(os.path.join(tin, "x0.npy"), scene.x0.reshape(-1).astype(np.float64))
         np.save(os.path.join(tin, "v0.npy"), scene.v0.reshape(-1).astype(np.float64))
         np.save(os.path.join(tin, "pinned.npy"), scene.pinned.astype(np.int32))

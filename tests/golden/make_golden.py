@@ -6,7 +6,7 @@ so this only runs where they are).  Inputs come from hobakv1_gb300.scenes, so
 they are regenerated bit-identically anywhere.  Usage:
 
     make -C oracle/ref REF=<reference checkout> -j8
-    python tests/golden/make_golden.py [elements] [trajectories] [position] [newmark] [green] [collisions]
+    python tests/golden/make_golden.py [elements] [trajectories] [aniso] [position] [newmark] [green] [collisions]
 """
 from __future__ import annotations
 
@@ -37,20 +37,36 @@ def element_states(N):
 
 
 def make_elements():
+    """Per-element terms of every material at three states; the anisotropic
+    energies with the fibre direction scenes.FIBER (stored as `fiber`)."""
     for mat in scenes.MATERIALS:
         N = 3 if mat in ("snh", "arap") else 2
         rest, tets, states = element_states(N)
         mu, lam = scenes.lame(1e4, 0.45)
+        fiber = np.array(scenes.FIBER) if mat in scenes.ANISOTROPIC else None
         for name, x in states.items():
             if mat == "neo_hookean_bw" and name == "wild":
                 continue  # log(J) of inverted tets is undefined for this energy
-            r = refrun.elements(rest, tets, x, mat, mu, lam)
+            r = refrun.elements(rest, tets, x, mat, mu, lam, fiber=fiber)
+            extra = {"fiber": fiber} if fiber is not None else {}
             np.savez_compressed(os.path.join(OUT, f"elements_{mat}_{name}.npz"),
-                                rest=rest, tets=tets, x=x, mu=mu, lam=lam,
-                                **{k: r[k] for k in ["F", "Sigma", "psi", "P", "H9", "fe", "He", "R",
+                                rest=rest, tets=tets, x=x, mu=mu, lam=lam, **extra,
+                                **{k: r[k] for k in ["F", "Sigma", "psi", "P", "H9", "H9u", "fe", "He", "R",
                                                      "K_colptr", "K_rowidx", "K_values", "energy",
                                                      "restVolume", "oneRingVolume"]})
             print("elements", mat, name, len(tets))
+
+
+def make_aniso_trajectories():
+    """BACKWARD_EULER_VELOCITY on the 6^3 compressed and twisted cube with
+    each anisotropic energy (fibre scenes.FIBER, no gravity), 40 steps."""
+    for mat in scenes.ANISOTROPIC:
+        s = scenes.aniso_scene(6, mat)
+        r = refrun.run(s, 40, stride=10)
+        np.savez_compressed(os.path.join(OUT, f"traj_{s.name}.npz"), x=r["x"], v=r["v"],
+                            iters=r["iters"], cg_error=r["cg_error"], energy=r["energy"],
+                            steps=40, stride=10, fiber=np.array(s.fiber))
+        print("aniso trajectory", s.name, r["iters"].sum())
 
 
 def make_trajectories():
@@ -127,11 +143,13 @@ def make_collisions():
 if __name__ == "__main__":
     if not refrun.available():
         sys.exit("reference build missing: make -C oracle/ref REF=<reference checkout>")
-    which = set(sys.argv[1:]) or {"elements", "trajectories", "position", "newmark", "green", "collisions"}
+    which = set(sys.argv[1:]) or {"elements", "trajectories", "aniso", "position", "newmark", "green", "collisions"}
     if "elements" in which:
         make_elements()
     if "trajectories" in which:
         make_trajectories()
+    if "aniso" in which:
+        make_aniso_trajectories()
     if "position" in which:
         make_position_trajectories()
     if "newmark" in which:

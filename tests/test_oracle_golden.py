@@ -33,22 +33,28 @@ ELEMENT_FILES = sorted(glob.glob(os.path.join(GOLDEN, "elements_*.npz")))
 def test_oracle_elements_match_reference(path):
     g = np.load(path)
     mat = os.path.basename(path)[len("elements_"):].rsplit("_", 1)[0]
-    o = oracle.elements(g["rest"], g["tets"], g["x"], mat, float(g["mu"]), float(g["lam"]))
-    # per-element forces and Hessians within 1e-10 relative (FP64)
+    fiber = g["fiber"] if "fiber" in g.files else None
+    o = oracle.elements(g["rest"], g["tets"], g["x"], mat, float(g["mu"]), float(g["lam"]), fiber=fiber)
+    # per-element forces and Hessians within 1e-10 relative (FP64); H9u is
+    # the unclamped hessian(F) (HYPERELASTIC.h:44)
     floors = natural_floors(g)
-    for k in ["F", "psi", "P", "H9", "fe", "He"]:
+    for k in ["F", "psi", "P", "H9", "H9u", "fe", "He"]:
         err = relmax(o[k], g[k], floors.get(k, 1e-300))
         assert err < 1e-10, (k, err)
     # singular values with the svd_rv sign convention
     assert relmax(o["Sigma"], g["Sigma"]) < 1e-10
 
 
-@pytest.mark.parametrize("path", ELEMENT_FILES[:3], ids=lambda p: os.path.basename(p))
+ASSEMBLY_FILES = [p for p in ELEMENT_FILES if os.path.basename(p).startswith(("elements_arap", "elements_aniso_arap"))]
+
+
+@pytest.mark.parametrize("path", ASSEMBLY_FILES, ids=lambda p: os.path.basename(p))
 def test_oracle_assembly_matches_reference_csc(path):
     g = np.load(path)
     mat = os.path.basename(path)[len("elements_"):].rsplit("_", 1)[0]
     s = scenes.Scene("g", g["rest"], g["tets"], mat, float(g["mu"]), float(g["lam"]),
-                     np.zeros(0, np.int32), g["x"].reshape(-1, 3), np.zeros_like(g["x"]).reshape(-1, 3))
+                     np.zeros(0, np.int32), g["x"].reshape(-1, 3), np.zeros_like(g["x"]).reshape(-1, 3),
+                     fiber=tuple(g["fiber"]) if "fiber" in g.files else None)
     sim = oracle.Sim(s)
     rowptr, cols, K, R = sim.assemble()
     nv = s.nv
@@ -73,7 +79,7 @@ def test_oracle_assembly_matches_reference_csc(path):
     ("kuhn10_snh", lambda: scenes.config1_scene(10)),
     ("kuhn6_snh_twist", lambda: scenes.config2_scene(6, "snh")),
     ("kuhn6_arap_twist", lambda: scenes.config2_scene(6, "arap")),
-])
+] + [(f"kuhn6_{m}_twist", (lambda m=m: scenes.aniso_scene(6, m))) for m in scenes.ANISOTROPIC])
 def test_oracle_trajectory_matches_reference(name, scene_fn):
     g = np.load(os.path.join(GOLDEN, f"traj_{name}.npz"))
     s = scene_fn()
