@@ -15,7 +15,8 @@ _ip = ctypes.POINTER(ctypes.c_int)
 
 
 class HobakMaterial(ctypes.Structure):
-    _fields_ = [("kind", ctypes.c_int), ("mu", ctypes.c_double), ("lambda_", ctypes.c_double)]
+    _fields_ = [("kind", ctypes.c_int), ("mu", ctypes.c_double), ("lambda_", ctypes.c_double),
+                ("fiber", ctypes.c_double * 3)]
 
 
 class HobakSceneDesc(ctypes.Structure):
@@ -80,6 +81,10 @@ SIGNATURES = {
     "hobak_gpu_set_solver": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakSolverOpts)]),
     "hobak_gpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "hobak_material_eval": (ctypes.c_int, [ctypes.POINTER(HobakMaterial), ctypes.c_int, _dp, _dp, _dp, _dp]),
+    "hobak_material_hessian": (ctypes.c_int, [ctypes.POINTER(HobakMaterial), ctypes.c_int, _dp, _dp]),
+    "hobak_material_eval_svd": (ctypes.c_int, [ctypes.POINTER(HobakMaterial), ctypes.c_int, _dp, _dp, _dp,
+                                               _dp, _dp, _dp, _dp]),
+    "hobak_material_needs_svd": (ctypes.c_int, [ctypes.c_int, _ip, _ip]),
     "hobak_element_eval": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp,
                                           ctypes.POINTER(HobakMaterial), _dp, _dp, _dp, _dp]),
     "hobak_batch_assemble": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _ip, _dp, _dp]),

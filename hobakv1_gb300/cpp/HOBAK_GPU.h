@@ -36,9 +36,28 @@ namespace VOLUME {
 
 class HYPERELASTIC {
  public:
-  HYPERELASTIC(int kind, REAL mu, REAL lambda) : _material{kind, mu, lambda} {}
+  HYPERELASTIC(int kind, REAL mu, REAL lambda) : _material{kind, mu, lambda, {0.0, 0.0, 0.0}} {}
   virtual ~HYPERELASTIC() = default;
   virtual std::string name() const = 0;
+
+  // energyNeedsSVD() / PK1NeedsSVD() (HYPERELASTIC.h:56-59)
+  bool energyNeedsSVD() const {
+    int e = 0, p = 0;
+    hobak_material_needs_svd(_material.kind, &e, &p);
+    return e != 0;
+  }
+  bool PK1NeedsSVD() const {
+    int e = 0, p = 0;
+    hobak_material_needs_svd(_material.kind, &e, &p);
+    return p != 0;
+  }
+  // hessian(F) (HYPERELASTIC.h:44): unclamped, 81 doubles column major
+  bool hessian(const REAL* F, REAL* H) const { return hobak_material_hessian(&_material, 1, F, H) == HOBAK_OK; }
+  // The (U, Sigma, V) overloads (HYPERELASTIC.h:37-49); NULL outputs skip
+  bool evaluate(const REAL* U, const REAL* Sigma, const REAL* V, REAL* psi, REAL* P, REAL* H,
+                REAL* clampedH) const {
+    return hobak_material_eval_svd(&_material, 1, U, Sigma, V, psi, P, H, clampedH) == HOBAK_OK;
+  }
 
   // Single-F forms (HYPERELASTIC.h:36-48); F, P column major (flatten order).
   REAL psi(const REAL* F) const {
@@ -93,6 +112,36 @@ class SNH_WITH_BARRIER : public HYPERELASTIC {
  public:
   SNH_WITH_BARRIER(const REAL& mu, const REAL& lambda) : HYPERELASTIC(HOBAK_MATERIAL_SNH_BARRIER, mu, lambda) {}
   std::string name() const override { return "SNH_WITH_BARRIER"; }
+};
+
+// The anisotropic energies take (mu, a) like ANISOTROPIC_ARAP(mu, a)
+// (ANISOTROPIC_ARAP.h:28); the library normalises a.
+class ANISOTROPIC : public HYPERELASTIC {
+ public:
+  ANISOTROPIC(int kind, const REAL& mu, const VECTOR3& a) : HYPERELASTIC(kind, mu, 0.0) {
+    for (int i = 0; i < 3; i++) _material.fiber[i] = a[i];
+  }
+};
+class ANISOTROPIC_ARAP : public ANISOTROPIC {
+ public:
+  ANISOTROPIC_ARAP(const REAL& mu, const VECTOR3& a) : ANISOTROPIC(HOBAK_MATERIAL_ANISOTROPIC_ARAP, mu, a) {}
+  std::string name() const override { return "ANISOTROPIC_ARAP"; }
+};
+class ANISOTROPIC_STVK : public ANISOTROPIC {
+ public:
+  ANISOTROPIC_STVK(const REAL& mu, const VECTOR3& a) : ANISOTROPIC(HOBAK_MATERIAL_ANISOTROPIC_STVK, mu, a) {}
+  std::string name() const override { return "ANISOTROPIC_STVK"; }
+};
+class ANISOTROPIC_FUNG : public ANISOTROPIC {
+ public:
+  ANISOTROPIC_FUNG(const REAL& mu, const VECTOR3& a) : ANISOTROPIC(HOBAK_MATERIAL_ANISOTROPIC_FUNG, mu, a) {}
+  std::string name() const override { return "ANISOTROPIC_FUNG"; }
+};
+class ANISOTROPIC_DIRICHLET : public ANISOTROPIC {
+ public:
+  ANISOTROPIC_DIRICHLET(const REAL& mu, const VECTOR3& a)
+      : ANISOTROPIC(HOBAK_MATERIAL_ANISOTROPIC_DIRICHLET, mu, a) {}
+  std::string name() const override { return "ANISOTROPIC_DIRICHLET"; }
 };
 
 }  // namespace VOLUME

@@ -157,16 +157,30 @@ void dm_inverse(const double* x0, const double* x1, const double* x2, const doub
   Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
 }
 
+// A known kind; the anisotropic energies need a non-zero, finite fibre.
+int validate_material(const hobak_material& m, int idx) {
+  char buf[160];
+  if (m.kind < HOBAK_MATERIAL_SNH || m.kind > HOBAK_MATERIAL_ANISOTROPIC_DIRICHLET) {
+    std::snprintf(buf, sizeof(buf), "scene %d: unknown material kind %d", idx, m.kind);
+    return fail(HOBAK_ERR_INVALID, buf);
+  }
+  if (is_anisotropic(m.kind)) {
+    const double n2 = m.fiber[0] * m.fiber[0] + m.fiber[1] * m.fiber[1] + m.fiber[2] * m.fiber[2];
+    if (!(n2 > 0.0) || !std::isfinite(n2)) {
+      std::snprintf(buf, sizeof(buf), "scene %d: anisotropic material needs a non-zero fibre direction", idx);
+      return fail(HOBAK_ERR_INVALID, buf);
+    }
+  }
+  return HOBAK_OK;
+}
+
 int validate_scene(const hobak_scene_desc& s, int idx) {
   char buf[160];
   if (s.nv <= 0 || s.nt <= 0 || !s.rest || !s.tets) {
     std::snprintf(buf, sizeof(buf), "scene %d: empty mesh or null rest/tets", idx);
     return fail(HOBAK_ERR_INVALID, buf);
   }
-  if (s.material.kind < 0 || s.material.kind > 5) {
-    std::snprintf(buf, sizeof(buf), "scene %d: unknown material kind %d", idx, s.material.kind);
-    return fail(HOBAK_ERR_INVALID, buf);
-  }
+  if (int rc = validate_material(s.material, idx)) return rc;
   if (!(s.dt > 0.0) || !(s.density > 0.0)) {
     std::snprintf(buf, sizeof(buf), "scene %d: dt and density must be positive", idx);
     return fail(HOBAK_ERR_INVALID, buf);
@@ -460,6 +474,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   // tiles: kTileV consecutive vertices of one scene (apply_tile_size changes
   // the size later; the tables are sized for kMinTileV)
   int ntilesCap = 0;
+  int anyAniso = 0;
   for (int s = 0; s < n; s++) {
     SceneHost& H = B->scenes[s];
     ntilesCap += (H.nv + kMinTileV - 1) / kMinTileV;
@@ -471,7 +486,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     }
     H.ntiles = (int)tileScene.size() - H.tile0;
     H.b0 = rowptr[H.v0];
-    const MatParams mp = make_material(H.mat.kind, H.mat.mu, H.mat.lambda);
+    const MatParams mp = make_material(H.mat.kind, H.mat.mu, H.mat.lambda, H.mat.fiber);
     SceneParams p{};
     p.v0 = H.v0;
     p.nv = H.nv;
@@ -483,6 +498,8 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     p.mu = mp.mu;
     p.lambda = mp.lambda;
     p.alpha = mp.alpha;
+    for (int i = 0; i < 3; i++) p.fiber[i] = mp.a[i];
+    if (is_anisotropic(mp.kind)) anyAniso = 1;
     p.dt = H.dt;
     set_integrator(p, B->opts);
     p.active = 1;
@@ -589,6 +606,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.r64 = carve<double>(base, oR64);
   d.partial = carve<double>(base, oPart);
   d.psi = carve<double>(base, oPsi);
+  d.anyAniso = anyAniso;
 
   auto up = [&](const void* dst, const void* src, size_t bytes) {
     return cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice);
@@ -2206,34 +2224,86 @@ int hobak_gpu_set_edge_collisions(hobak_batch b, int ee_on) { return hobak_batch
 int hobak_gpu_set_solver(hobak_batch b, const hobak_solver_opts* opts) { return hobak_batch_set_solver(b, opts); }
 int hobak_gpu_destroy(hobak_batch b) { return hobak_batch_destroy(b); }
 
-int hobak_material_eval(const hobak_material* m, int n, const double* F, double* psi, double* P, double* H) {
-  if (!m || n <= 0 || !F) return fail(HOBAK_ERR_INVALID, "bad arguments");
-  if (m->kind < 0 || m->kind > 5) return fail(HOBAK_ERR_INVALID, "unknown material");
+namespace {
+// psi / PK1 / clampedHessian / hessian of n elements given F, or (U, Sigma, V)
+// when U is not null; one device allocation for inputs and outputs.
+int material_eval(const hobak_material* m, int n, const double* F, const double* U, const double* S,
+                  const double* V, double* psi, double* P, double* H, double* Hu) {
+  if (!m || n <= 0 || (!F && !(U && S && V))) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  if (int rc = validate_material(*m, 0)) return rc;
   int rc = hobak_device_check(nullptr, nullptr, nullptr);
   if (rc) return rc;
-  double *dF = nullptr, *dPsi = nullptr, *dP = nullptr, *dH = nullptr;
   const size_t N = (size_t)n;
-  CUDA_TRY(cudaMalloc(&dF, 9 * N * sizeof(double)));
-  if (psi) CUDA_TRY(cudaMalloc(&dPsi, N * sizeof(double)));
-  if (P) CUDA_TRY(cudaMalloc(&dP, 9 * N * sizeof(double)));
-  if (H) CUDA_TRY(cudaMalloc(&dH, 81 * N * sizeof(double)));
-  CUDA_TRY(cudaMemcpy(dF, F, 9 * N * sizeof(double), cudaMemcpyHostToDevice));
-  launch_material_eval(m->kind, m->mu, m->lambda, n, dF, dPsi, dP, dH, 0);
+  // inputs (F: 9, or U, Sigma, V: 21) then outputs psi 1, P 9, H 81, Hu 81 per element
+  const size_t nin = U ? 21 : 9;
+  const size_t nout = (psi ? 1 : 0) + (P ? 9 : 0) + (H ? 81 : 0) + (Hu ? 81 : 0);
+  DeviceScratch scratch;
+  CUDA_TRY(cudaMalloc(&scratch.p, (nin + nout) * N * sizeof(double)));
+  double* cur = static_cast<double*>(scratch.p);
+  auto take = [&](size_t per) {
+    double* p = cur;
+    cur += per * N;
+    return p;
+  };
+  double *dF = nullptr, *dU = nullptr, *dS = nullptr, *dV = nullptr;
+  if (U) {
+    dU = take(9);
+    dS = take(3);
+    dV = take(9);
+    CUDA_TRY(cudaMemcpy(dU, U, 9 * N * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dS, S, 3 * N * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dV, V, 9 * N * sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    dF = take(9);
+    CUDA_TRY(cudaMemcpy(dF, F, 9 * N * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  double* dPsi = psi ? take(1) : nullptr;
+  double* dP = P ? take(9) : nullptr;
+  double* dH = H ? take(81) : nullptr;
+  double* dHu = Hu ? take(81) : nullptr;
+  launch_material_eval(m->kind, m->mu, m->lambda, m->fiber, n, dF, dU, dS, dV, dPsi, dP, dH, dHu, 0);
   CUDA_TRY(cudaGetLastError());
   if (psi) CUDA_TRY(cudaMemcpy(psi, dPsi, N * sizeof(double), cudaMemcpyDeviceToHost));
   if (P) CUDA_TRY(cudaMemcpy(P, dP, 9 * N * sizeof(double), cudaMemcpyDeviceToHost));
   if (H) CUDA_TRY(cudaMemcpy(H, dH, 81 * N * sizeof(double), cudaMemcpyDeviceToHost));
-  cudaFree(dF);
-  cudaFree(dPsi);
-  cudaFree(dP);
-  cudaFree(dH);
+  if (Hu) CUDA_TRY(cudaMemcpy(Hu, dHu, 81 * N * sizeof(double), cudaMemcpyDeviceToHost));
+  return HOBAK_OK;
+}
+}  // namespace
+
+int hobak_material_eval(const hobak_material* m, int n, const double* F, double* psi, double* P, double* H) {
+  if (!F) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  return material_eval(m, n, F, nullptr, nullptr, nullptr, psi, P, H, nullptr);
+}
+
+int hobak_material_hessian(const hobak_material* m, int n, const double* F, double* H) {
+  if (!F || !H) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  return material_eval(m, n, F, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, H);
+}
+
+int hobak_material_eval_svd(const hobak_material* m, int n, const double* U, const double* sigma, const double* V,
+                            double* psi, double* P, double* H, double* clampedH) {
+  if (!U || !sigma || !V) return fail(HOBAK_ERR_INVALID, "bad arguments");
+  return material_eval(m, n, nullptr, U, sigma, V, psi, P, clampedH, H);
+}
+
+int hobak_material_needs_svd(int kind, int* energy, int* pk1) {
+  if (kind < HOBAK_MATERIAL_SNH || kind > HOBAK_MATERIAL_ANISOTROPIC_DIRICHLET)
+    return fail(HOBAK_ERR_INVALID, "unknown material");
+  // energyNeedsSVD / PK1NeedsSVD as each material class answers them
+  // (SNH.cpp, ARAP.cpp, STVK.cpp, LINEAR.cpp, NEO_HOOKEAN_BW.cpp,
+  // SNH_WITH_BARRIER.cpp, ANISOTROPIC_*.cpp)
+  static const int e[10] = {0, 1, 0, 0, 0, 0, 1, 1, 1, 0};
+  static const int p[10] = {0, 1, 0, 0, 0, 0, 1, 1, 1, 0};
+  if (energy) *energy = e[kind];
+  if (pk1) *pk1 = p[kind];
   return HOBAK_OK;
 }
 
 int hobak_element_eval(int nv, int nt, const double* rest, const int* tets, const double* x, const hobak_material* m,
                        double* F, double* sigma, double* force, double* hessian) {
   if (nv <= 0 || nt <= 0 || !rest || !tets || !x || !m) return fail(HOBAK_ERR_INVALID, "bad arguments");
-  if (m->kind < 0 || m->kind > 5) return fail(HOBAK_ERR_INVALID, "unknown material");
+  if (int rc = validate_material(*m, 0)) return rc;
   for (long k = 0; k < 4L * nt; k++)
     if (tets[k] < 0 || tets[k] >= nv) return fail(HOBAK_ERR_INVALID, "tet vertex id out of range");
   int rc = hobak_device_check(nullptr, nullptr, nullptr);
@@ -2262,7 +2332,7 @@ int hobak_element_eval(int nv, int nt, const double* rest, const int* tets, cons
   CUDA_TRY(cudaMemcpy(dDm, Dm.data(), 9 * T * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(dVol, vol.data(), T * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(dTets, tets, T * sizeof(int4), cudaMemcpyHostToDevice));
-  launch_element_eval(nt, dTets, dRest, dX, dDm, dVol, m->kind, m->mu, m->lambda, dF, dS, dFo, dH, 0);
+  launch_element_eval(nt, dTets, dRest, dX, dDm, dVol, m->kind, m->mu, m->lambda, m->fiber, dF, dS, dFo, dH, 0);
   CUDA_TRY(cudaGetLastError());
   if (F) CUDA_TRY(cudaMemcpy(F, dF, 9 * T * sizeof(double), cudaMemcpyDeviceToHost));
   if (sigma) CUDA_TRY(cudaMemcpy(sigma, dS, 3 * T * sizeof(double), cudaMemcpyDeviceToHost));

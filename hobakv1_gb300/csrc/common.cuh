@@ -18,7 +18,12 @@
 
 namespace hobak {
 
-enum MaterialKind : int { MAT_SNH = 0, MAT_ARAP = 1, MAT_STVK = 2, MAT_LINEAR = 3, MAT_NHBW = 4, MAT_SNHB = 5 };
+enum MaterialKind : int {
+  MAT_SNH = 0, MAT_ARAP = 1, MAT_STVK = 2, MAT_LINEAR = 3, MAT_NHBW = 4, MAT_SNHB = 5,
+  // anisotropic energies along a fibre direction (Hyperelastic/Volume/ANISOTROPIC_*.cpp)
+  MAT_AARAP = 6, MAT_ASTVK = 7, MAT_AFUNG = 8, MAT_ADIR = 9
+};
+__host__ __device__ __forceinline__ bool is_anisotropic(int kind) { return kind >= MAT_AARAP && kind <= MAT_ADIR; }
 
 constexpr int kTileV = 128;       // default vertices per PCG tile (one CTA)
 constexpr int kMinTileV = 64;     // smallest tile size; tile tables are sized for it
@@ -52,6 +57,8 @@ struct SceneParams {
   double nm[6];              // Newmark coefficients alpha_0..5 (NEWMARK.cpp:71-76) from dt
   double newtonEps;          // Newmark: Newton stops once |rhs|^2 <= newtonEps ...
   int maxNewton;             // ... or after maxNewton iterations
+  double fiber[3];           // anisotropic energies: unit fibre direction
+  double greenMu;            // Newmark: GREEN_DAMPING mu of the energy-damped solve (0: none)
 };
 
 // Per-scene solver scalars, written by the last CTA of each reduction.

@@ -24,9 +24,11 @@ __host__ __device__ __forceinline__ constexpr int sym9(int r, int c) { return r 
 
 // Hr = sum_k L_k w_k w_k^T over the 9 eigenmodes (reduced 9x9, vertices 1..3).
 // Returns in Hr[45].  U, B are the SVD's U and B = DmInv V.
+// clamp = false keeps negative eigenvalues: the unclamped hessian()
+// (HYPERELASTIC.h:44) from the same eigensystem.
 template <typename T>
 __device__ __forceinline__ void reduced_hessian(const MatParams& m, const double* Ud, const double* Sd,
-                                                const double* Vd, const double* Dinv, T* Hr) {
+                                                const double* Vd, const double* Dinv, T* Hr, bool clamp = true) {
 #pragma unroll
   for (int k = 0; k < 45; k++) Hr[k] = T(0);
   if (m.kind == MAT_LINEAR) {
@@ -79,7 +81,7 @@ __device__ __forceinline__ void reduced_hessian(const MatParams& m, const double
   const T rs2 = T(kInvSqrt2);
 #pragma unroll
   for (int k = 0; k < 9; k++) {
-    const T lam = L[k] > T(0) ? L[k] : T(0);  // clamp (SNH.cpp:138-141)
+    const T lam = (!clamp || L[k] > T(0)) ? L[k] : T(0);  // clamp (SNH.cpp:138-141)
     if (lam == T(0)) continue;
     T w[9];  // w[(a, comp)] = (U M_k B^T)(comp, a)
     if (k < 6) {
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= b.nt) return;
   const SceneParams& sp = b.scenes[b.tetScene[t]];
-  if (!sp.active) return;
+  if (!sp.active || is_anisotropic(sp.kind)) return;  // anisotropic energies: k_element_aniso
   // Newmark: a scene whose Newton loop is over needs no further element terms
   if (!rawForces && sp.integrator == kIntegratorNewmark && b.solve[b.tetScene[t]].newtonDone) return;
   const int4 tv = b.tets[t];
@@ -271,30 +273,159 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   expand_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
 }
 
-// Standalone: clamped 9x9 Hessian, PK1 and psi of n deformation gradients.
-__global__ void k_material_eval(MatParams m, int n, const double* Fin, double* psi, double* Pout, double* Hout) {
+// Element terms of the anisotropic energies (ANISOTROPIC_ARAP, STVK, FUNG,
+// DIRICHLET): P = s F A gives the element force f_{a+1} = -vol s g d_a,
+// f_0 = vol s g (d_1 + d_2 + d_3) with g = F a and d = DmInv a, and the
+// clamped Hessian alpha H5 + beta fa fa^T gives the element Hessian
+// -vol (c c^T) (x) G with c = (-(d_1 + d_2 + d_3), d_1, d_2, d_3) and
+// G = alpha I + beta g g^T: one 3x3 matrix per tet instead of a 9x9
+// eigen-reconstruction.  Only ANISOTROPIC_ARAP needs the SVD (the sign of
+// I4).  Same outputs, layout and precision split as k_element; launched
+// beside it when the batch holds anisotropic scenes, so the isotropic
+// kernel's code and registers are unchanged.
+template <typename HT>
+__global__ void __launch_bounds__(128) k_element_aniso(DeviceBatch b, int rawForces, HT* __restrict__ outH) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.nt) return;
+  const int sc = b.tetScene[t];
+  const SceneParams& sp = b.scenes[sc];
+  if (!sp.active || !is_anisotropic(sp.kind)) return;
+  if (!rawForces && sp.integrator == kIntegratorNewmark && b.solve[sc].newtonDone) return;
+  const int4 tv = b.tets[t];
+  const MatParams m = make_material(sp.kind, sp.mu, sp.lambda, sp.fiber);
+  const bool velocityTerm = !rawForces && sp.integrator == kIntegratorVelocity;
+  const double dt = velocityTerm ? sp.dt : 0.0;
+  double Dinv[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) Dinv[k] = b.DmInv[9 * (size_t)t + k];
+  const double vol = b.vol[t];
+  double X[4][3], F[9], g[3];
+  load_tet(tv, b.rest, b.x, X);
+  deformation_gradient(X, Dinv, F);
+  const double I5 = aniso_stretch(m, F, g);
+  double I4 = 1.0;
+  if (m.kind == MAT_AARAP) {
+    double U[9], S[3], V[9];
+    svd3_rv_fast(F, U, S, V);
+    I4 = aniso_invariant4(m, S, V);
+  }
+  // d = DmInv a, c = (-(d1 + d2 + d3), d1, d2, d3)
+  double c[4];
+#pragma unroll
+  for (int a = 0; a < 3; a++) c[a + 1] = Dinv[a] * m.a[0] + Dinv[a + 3] * m.a[1] + Dinv[a + 6] * m.a[2];
+  c[0] = -(c[1] + c[2] + c[3]);
+  const double fs = -(velocityTerm ? dt * vol : vol) * aniso_pk1_scale(m, I5, I4);
+  double f[12];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[3 * a + i] = fs * c[a] * g[i];
+  double al, be;
+  const double a2 = m.a[0] * m.a[0] + m.a[1] * m.a[1] + m.a[2] * m.a[2];
+  aniso_hessian_coeffs(m, I5, I4, I5 * a2, true, al, be);
+  HT G[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) G[3 * i + k] = HT((i == k ? al : 0.0) + be * g[i] * g[k]);
+  HT* out = outH + kElemHess * (size_t)t;
+  const HT nv = HT(-vol);
+#pragma unroll
+  for (int A = 0; A < 4; A++)
+#pragma unroll
+    for (int B = A; B < 4; B++) {
+      const HT cc = nv * HT(c[A]) * HT(c[B]);
+#pragma unroll
+      for (int e = 0; e < 9; e++) out[9 * upper_block(A, B) + e] = cc * G[e];
+    }
+  double* gout = b.elemG + 12 * (size_t)t;
+  if (!velocityTerm) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) gout[k] = f[k];
+    return;
+  }
+  // He v = -vol c_A G (sum_B c_B v_B), sum_B c_B v_B = sum_a d_a (v_a - v_0)
+  const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
+  HT w[3] = {HT(0), HT(0), HT(0)};
+#pragma unroll
+  for (int a = 1; a < 4; a++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) w[i] += HT(c[a]) * HT(b.v[3 * vid[a] + i] - b.v[3 * vid[0] + i]);
+  const HT ch = HT(-vol * dt * dt);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const HT gw = ch * (G[3 * i] * w[0] + G[3 * i + 1] * w[1] + G[3 * i + 2] * w[2]);
+#pragma unroll
+    for (int a = 0; a < 4; a++) gout[3 * a + i] = f[3 * a + i] + double(HT(c[a]) * gw);
+  }
+}
+
+// 9x9 (column major, flatten order) of the reduced Hessian with DmInv = I:
+// then Hr[(a,i),(b,k)] = H9[i + 3a, k + 3b].
+__device__ __forceinline__ void reduced_to_h9(const double* Hr, double* H) {
+#pragma unroll
+  for (int r = 0; r < 9; r++)
+#pragma unroll
+    for (int c = 0; c < 9; c++) H[r + 9 * c] = (r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)];
+}
+
+// Standalone material terms of n elements (the VOLUME::HYPERELASTIC
+// interface): psi, PK1, clampedHessian and the unclamped hessian, from F
+// (svd_rv computed here) or, when Uin is given, from (U, Sigma, V) as the
+// reference's overloads take them (HYPERELASTIC.h:37-49: F = U diag(Sigma)
+// V^T for the F-form energies; ARAP and the eigensystems use the factors
+// themselves).  Any output may be null.
+__global__ void k_material_eval(MatParams m, int n, const double* Fin, const double* Uin, const double* Sin,
+                                const double* Vin, double* psi, double* Pout, double* Hout, double* Huout) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   double F[9], U[9], S[3], V[9];
+  if (Uin) {
 #pragma unroll
-  for (int k = 0; k < 9; k++) F[k] = Fin[9 * (size_t)e + k];
-  svd3_rv_fast(F, U, S, V);
+    for (int k = 0; k < 9; k++) {
+      U[k] = Uin[9 * (size_t)e + k];
+      V[k] = Vin[9 * (size_t)e + k];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) S[k] = Sin[3 * (size_t)e + k];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        F[i + 3 * j] = U[i] * S[0] * V[j] + U[i + 3] * S[1] * V[j + 3] + U[i + 6] * S[2] * V[j + 6];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) F[k] = Fin[9 * (size_t)e + k];
+    svd3_rv_fast(F, U, S, V);
+  }
+  if (is_anisotropic(m.kind)) {
+    double g[3];
+    const double I5 = aniso_stretch(m, F, g);
+    const double I4 = aniso_invariant4(m, S, V);
+    if (psi) psi[e] = aniso_psi(m, I5, I4);
+    if (Pout) {
+      const double sc = aniso_pk1_scale(m, I5, I4);
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) Pout[9 * (size_t)e + i + 3 * j] = sc * (g[i] * m.a[j]);
+    }
+    if (Hout) aniso_hessian9(m, F, I4, true, Hout + 81 * (size_t)e);
+    if (Huout) aniso_hessian9(m, F, I4, false, Huout + 81 * (size_t)e);
+    return;
+  }
   if (psi) psi[e] = material_psi(m, F, S);
   if (Pout) material_pk1(m, F, U, V, Pout + 9 * (size_t)e);
+  const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   if (Hout) {
-    // H9 through the same reduced path with DmInv = I (pFpx then selects F itself)
-    const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     double Hr[45];
     reduced_hessian<double>(m, U, S, V, I3, Hr);
-    // with DmInv = I, Hr[(a,i),(b,k)] = H9[(i + 3a), (k + 3b)] in flatten order
-    double* H = Hout + 81 * (size_t)e;
-#pragma unroll
-    for (int r = 0; r < 9; r++)
-#pragma unroll
-      for (int c = 0; c < 9; c++) {
-        const int rr = 3 * (r / 3) + r % 3, cc = 3 * (c / 3) + c % 3;
-        H[r + 9 * c] = (rr <= cc) ? Hr[sym9(rr, cc)] : Hr[sym9(cc, rr)];
-      }
+    reduced_to_h9(Hr, Hout + 81 * (size_t)e);
+  }
+  if (Huout) {
+    double Hr[45];
+    reduced_hessian<double>(m, U, S, V, I3, Hr, false);
+    reduced_to_h9(Hr, Huout + 81 * (size_t)e);
   }
 }
 
@@ -316,15 +447,41 @@ __global__ void k_element_eval(int nt, const int4* tets, const double* rest, con
     for (int k = 0; k < 9; k++) Fo[9 * (size_t)t + k] = F[k];
   if (So)
     for (int k = 0; k < 3; k++) So[3 * (size_t)t + k] = S[k];
+  const bool aniso = is_anisotropic(m.kind);
+  double g[3], c[4], I5 = 0.0, I4 = 0.0;
+  if (aniso) {
+    I5 = aniso_stretch(m, F, g);
+    I4 = aniso_invariant4(m, S, V);
+    for (int a = 0; a < 3; a++) c[a + 1] = Dinv[a] * m.a[0] + Dinv[a + 3] * m.a[1] + Dinv[a + 6] * m.a[2];
+    c[0] = -(c[1] + c[2] + c[3]);
+  }
   if (fo) {
-    material_pk1(m, F, U, V, P);
-    element_force(P, Dinv, vol, f);
+    if (aniso) {
+      const double sc = aniso_pk1_scale(m, I5, I4);
+      for (int a = 0; a < 4; a++)
+        for (int i = 0; i < 3; i++) f[3 * a + i] = -vol * sc * c[a] * g[i];
+    } else {
+      material_pk1(m, F, U, V, P);
+      element_force(P, Dinv, vol, f);
+    }
     for (int k = 0; k < 12; k++) fo[12 * (size_t)t + k] = f[k];
   }
   if (Ho) {
-    double Hr[45], blk[kElemHess];
-    reduced_hessian<double>(m, U, S, V, Dinv, Hr);
-    expand_blocks<double, double>(Hr, vol, blk);
+    double blk[kElemHess];
+    if (aniso) {
+      double al, be;
+      const double a2 = m.a[0] * m.a[0] + m.a[1] * m.a[1] + m.a[2] * m.a[2];
+      aniso_hessian_coeffs(m, I5, I4, I5 * a2, true, al, be);
+      for (int A = 0; A < 4; A++)
+        for (int B = A; B < 4; B++)
+          for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++)
+              blk[9 * upper_block(A, B) + 3 * i + k] = -vol * c[A] * c[B] * ((i == k ? al : 0.0) + be * g[i] * g[k]);
+    } else {
+      double Hr[45];
+      reduced_hessian<double>(m, U, S, V, Dinv, Hr);
+      expand_blocks<double, double>(Hr, vol, blk);
+    }
     double* H = Ho + 144 * (size_t)t;
     for (int a = 0; a < 4; a++)
       for (int bb = 0; bb < 4; bb++)
@@ -342,7 +499,7 @@ __global__ void k_energy(DeviceBatch b) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= b.nt) return;
   const SceneParams& sp = b.scenes[b.tetScene[t]];
-  const MatParams m{sp.kind, sp.mu, sp.lambda, sp.alpha};
+  const MatParams m = make_material(sp.kind, sp.mu, sp.lambda, sp.fiber);
   double Dinv[9];
   for (int k = 0; k < 9; k++) Dinv[k] = b.DmInv[9 * (size_t)t + k];
   double X[4][3];
@@ -350,7 +507,17 @@ __global__ void k_energy(DeviceBatch b) {
   double F[9], U[9], S[3], V[9];
   deformation_gradient(X, Dinv, F);
   svd3_rv_fast(F, U, S, V);
-  b.psi[t] = b.vol[t] * material_psi(m, F, S);
+  double psi;
+  if (is_anisotropic(m.kind)) {
+    double g[3];
+    const double I5 = aniso_stretch(m, F, g);
+    psi = aniso_psi(m, I5, aniso_invariant4(m, S, V));
+  } else {
+    // isotropic energies keep the reparameterised constants of the scene
+    const MatParams mi{sp.kind, sp.mu, sp.lambda, sp.alpha};
+    psi = material_psi(mi, F, S);
+  }
+  b.psi[t] = b.vol[t] * psi;
 }
 
 }  // namespace
@@ -361,12 +528,14 @@ void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces) {
   if (b.nt == 0) return;
   const int nt = b.elemThreads;
   k_element<double><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, rawForces, b.elemH);
+  if (b.anyAniso) k_element_aniso<double><<<(b.nt + 127) / 128, 128, 0, s>>>(b, rawForces, b.elemH);
 }
 
 void launch_element_mixed(const DeviceBatch& b, cudaStream_t s) {
   if (b.nt == 0) return;
   const int nt = b.elemThreads;
   k_element<float><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, 0, b.elemHf);
+  if (b.anyAniso) k_element_aniso<float><<<(b.nt + 127) / 128, 128, 0, s>>>(b, 0, b.elemHf);
 }
 
 void launch_energy(const DeviceBatch& b, cudaStream_t s) {
@@ -374,18 +543,20 @@ void launch_energy(const DeviceBatch& b, cudaStream_t s) {
   k_energy<<<(b.nt + 127) / 128, 128, 0, s>>>(b);
 }
 
-void launch_material_eval(int kind, double mu, double lambda, int n, const double* F, double* psi, double* P,
-                          double* H, cudaStream_t s) {
+void launch_material_eval(int kind, double mu, double lambda, const double* fiber, int n, const double* F,
+                          const double* U, const double* S, const double* V, double* psi, double* P, double* H,
+                          double* Hu, cudaStream_t s) {
   if (n <= 0) return;
-  k_material_eval<<<(n + 127) / 128, 128, 0, s>>>(make_material(kind, mu, lambda), n, F, psi, P, H);
+  k_material_eval<<<(n + 127) / 128, 128, 0, s>>>(make_material(kind, mu, lambda, fiber), n, F, U, S, V, psi, P,
+                                                   H, Hu);
 }
 
 void launch_element_eval(int nt, const int4* tets, const double* rest, const double* x, const double* DmInv,
-                         const double* vol, int kind, double mu, double lambda, double* F, double* sigma,
-                         double* force, double* hessian, cudaStream_t s) {
+                         const double* vol, int kind, double mu, double lambda, const double* fiber, double* F,
+                         double* sigma, double* force, double* hessian, cudaStream_t s) {
   if (nt <= 0) return;
-  k_element_eval<<<(nt + 127) / 128, 128, 0, s>>>(nt, tets, rest, x, DmInv, vol, make_material(kind, mu, lambda), F,
-                                                   sigma, force, hessian);
+  k_element_eval<<<(nt + 127) / 128, 128, 0, s>>>(nt, tets, rest, x, DmInv, vol,
+                                                   make_material(kind, mu, lambda, fiber), F, sigma, force, hessian);
 }
 
 }  // namespace hobak

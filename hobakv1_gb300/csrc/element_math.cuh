@@ -285,10 +285,18 @@ __device__ __forceinline__ void eig3sym(const T* Ain, T* Q, T* L) {
 struct MatParams {
   int kind;
   double mu, lambda, alpha;
+  double a[3];  // anisotropic energies: unit fibre direction
 };
 
-__host__ __device__ inline MatParams make_material(int kind, double mu, double lambda) {
-  MatParams m{kind, mu, lambda, 0.0};
+// fiber: the anisotropic energies' direction, normalised here as their
+// constructors do (ANISOTROPIC_ARAP.cpp:26-29); ignored by the isotropic ones.
+__host__ __device__ inline MatParams make_material(int kind, double mu, double lambda,
+                                                   const double* fiber = nullptr) {
+  MatParams m{kind, mu, lambda, 0.0, {1.0, 0.0, 0.0}};
+  if (fiber) {
+    const double n = sqrt(fiber[0] * fiber[0] + fiber[1] * fiber[1] + fiber[2] * fiber[2]);
+    for (int i = 0; i < 3; i++) m.a[i] = n > 0.0 ? fiber[i] / n : fiber[i];
+  }
   if (kind == MAT_SNH) {  // SNH.cpp:23-32
     m.lambda = lambda + mu;
     m.alpha = 1.0 + m.mu / m.lambda;
@@ -537,6 +545,112 @@ __device__ inline bool material_eigensystem(const MatParams& mp, const double* S
       return true;
     }
   }
+}
+
+// ---- anisotropic energies (Hyperelastic/Volume/ANISOTROPIC_*.cpp) ----
+// With the unit fibre direction a, g = F a, F A = g a^T (A = a a^T) and
+// I5 = |g|^2 (invariant5, MATRIX_UTIL.cpp:553-556), every stress is a scalar
+// times F A and every Hessian is alpha H5 + beta vec(FA) vec(FA)^T with
+// H5 = kronIdentity(A) (MATRIX_UTIL.cpp:512-524).  Pushed through pFpx, that
+// Hessian is the Kronecker product (c c^T) (x) (alpha I + beta g g^T) with
+// c = (-sum d, d) and d = DmInv a: a 3x3 block per vertex pair, no 9x9 form.
+
+// I4 = a^T (V Sigma V^T) a from the svd_rv factors (invariant4,
+// MATRIX_UTIL.cpp:545-552); ANISOTROPIC_ARAP reads its sign and |I4| < 1e-8.
+__device__ __forceinline__ double aniso_invariant4(const MatParams& m, const double* S, const double* V) {
+  double I4 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double va = V[3 * k] * m.a[0] + V[3 * k + 1] * m.a[1] + V[3 * k + 2] * m.a[2];
+    I4 += S[k] * va * va;
+  }
+  return I4;
+}
+
+// g = F a and I5 = |g|^2
+__device__ __forceinline__ double aniso_stretch(const MatParams& m, const double* F, double* g) {
+#pragma unroll
+  for (int i = 0; i < 3; i++) g[i] = F[i] * m.a[0] + F[i + 3] * m.a[1] + F[i + 6] * m.a[2];
+  return g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+}
+
+// psi: ANISOTROPIC_ARAP.cpp:40-47, ANISOTROPIC_STVK.cpp:42-46,
+// ANISOTROPIC_FUNG.cpp:40-44, ANISOTROPIC_DIRICHLET.cpp:36-39
+__device__ inline double aniso_psi(const MatParams& m, double I5, double I4) {
+  switch (m.kind) {
+    case MAT_AARAP: {
+      const double d = sqrt(I5) - (I4 > 0.0 ? 1.0 : -1.0);
+      return 0.5 * m.mu * d * d;
+    }
+    case MAT_ASTVK: return 0.5 * m.mu * (I5 - 1.0) * (I5 - 1.0);
+    case MAT_AFUNG: return m.mu * (exp(I5 - 1.0) - I5);
+    default: return m.mu * I5;
+  }
+}
+
+// s with P = s F A: ANISOTROPIC_ARAP.cpp:52-65 (near I4 = 0 the reference's
+// fixed value), ANISOTROPIC_STVK.cpp:51-55, ANISOTROPIC_FUNG.cpp:50-54,
+// ANISOTROPIC_DIRICHLET.cpp:44-47
+__device__ inline double aniso_pk1_scale(const MatParams& m, double I5, double I4) {
+  switch (m.kind) {
+    case MAT_AARAP:
+      return fabs(I4) >= 1e-8 ? m.mu * (1.0 - (I4 > 0.0 ? 1.0 : -1.0) / sqrt(I5)) : -0.5 * m.mu;
+    case MAT_ASTVK: return 2.0 * m.mu * (I5 - 1.0);
+    case MAT_AFUNG: return 2.0 * m.mu * (exp(I5 - 1.0) - 1.0);
+    default: return 2.0 * m.mu;
+  }
+}
+
+// (alpha, beta) of the Hessian alpha H5 + beta fa fa^T, unclamped (hessian)
+// or clamped (clampedHessian): ANISOTROPIC_ARAP.cpp:70-110,
+// ANISOTROPIC_STVK.cpp:60-100, ANISOTROPIC_FUNG.cpp:60-105,
+// ANISOTROPIC_DIRICHLET.cpp:52-77.  fa2 = |vec(F A)|^2 (= I5 for a unit a).
+__device__ inline void aniso_hessian_coeffs(const MatParams& m, double I5, double I4, double fa2, bool clamp,
+                                            double& al, double& be) {
+  if (m.kind == MAT_AARAP) {
+    const double SI4 = I4 > 0.0 ? 1.0 : -1.0;
+    if (!clamp || I5 >= SI4) {
+      const double si = 1.0 / sqrt(I5);
+      al = m.mu * (1.0 - SI4 * si);
+      be = m.mu * (SI4 * si * si * si);
+    } else {
+      al = 0.0;
+      be = m.mu * (1.0 / I5);
+    }
+    return;
+  }
+  if (m.kind == MAT_ADIR) {
+    al = 2.0 * m.mu;
+    be = 0.0;
+    return;
+  }
+  const bool fung = m.kind == MAT_AFUNG;
+  const double e = fung ? exp(I5 - 1.0) : 1.0;
+  const double l1 = fung ? 2.0 * m.mu * (e - 1.0) : 2.0 * m.mu * (I5 - 1.0);
+  const double l0 = fung ? l1 + 4.0 * m.mu * I5 * e : l1 + 4.0 * m.mu * I5;
+  if (!clamp || (l0 > 0.0 && l1 > 0.0)) {
+    al = l1;
+    be = 4.0 * m.mu * e;
+  } else if (l0 < 0.0) {
+    al = be = 0.0;
+  } else {  // the rank-one part along fa / |fa| only (fa itself when |fa| = 0)
+    al = 0.0;
+    be = fa2 > 0.0 ? l0 / fa2 : l0;
+  }
+}
+
+// 9x9 (column major, flatten order) alpha H5 + beta fa fa^T of F
+__device__ inline void aniso_hessian9(const MatParams& m, const double* F, double I4, bool clamp, double* H) {
+  double g[3];
+  const double I5 = aniso_stretch(m, F, g);
+  const double a2 = m.a[0] * m.a[0] + m.a[1] * m.a[1] + m.a[2] * m.a[2];
+  double al, be;
+  aniso_hessian_coeffs(m, I5, I4, I5 * a2, clamp, al, be);
+  for (int c = 0; c < 9; c++)
+    for (int r = 0; r < 9; r++) {
+      const double h5 = (r % 3 == c % 3) ? m.a[r / 3] * m.a[c / 3] : 0.0;
+      H[r + 9 * c] = al * h5 + be * (g[r % 3] * m.a[r / 3]) * (g[c % 3] * m.a[c / 3]);
+    }
 }
 
 }  // namespace hobak

@@ -131,6 +131,7 @@ struct DeviceBatch {
   PcgVecs<float> v32;   // mixed path
   double* partial;      // [ntiles][kPartials]
   double* psi;          // [T] energy density scratch
+  int anyAniso;          // some scene has an anisotropic energy (k_element_aniso)
   // vertex-face collisions (collOn = 0: none in this batch)
   int collOn;
   DeviceCollisions coll;
@@ -206,11 +207,13 @@ void launch_set_condition(unsigned long long handle, unsigned value, cudaStream_
 void launch_energy(const DeviceBatch& b, cudaStream_t s);
 
 // element-level entry points (standalone, no batch)
-void launch_material_eval(int kind, double mu, double lambda, int n, const double* F, double* psi, double* P,
-                          double* H, cudaStream_t s);
+// (F or, when U is given, U/S/V input; fiber: anisotropic energies' direction or null)
+void launch_material_eval(int kind, double mu, double lambda, const double* fiber, int n, const double* F,
+                          const double* U, const double* S, const double* V, double* psi, double* P, double* H,
+                          double* Hu, cudaStream_t s);
 void launch_element_eval(int nt, const int4* tets, const double* rest, const double* x, const double* DmInv,
-                         const double* vol, int kind, double mu, double lambda, double* F, double* sigma,
-                         double* force, double* hessian, cudaStream_t s);
+                         const double* vol, int kind, double mu, double lambda, const double* fiber, double* F,
+                         double* sigma, double* force, double* hessian, cudaStream_t s);
 
 // Inner PCG of every scene of cluster class k (classes[0..4]: cluster sizes
 // 1, 2, 4, 8, 16).  Returns a cudaError_t value (0 on success).

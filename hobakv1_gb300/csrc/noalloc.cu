@@ -116,7 +116,11 @@ extern "C" int hobak_element_eval_noalloc(int nv, int nt, const double* rest, co
   if (nt > kMaxTets)
     return fail(HOBAK_ERR_INVALID, "hobak_element_eval_noalloc: " + std::to_string(nt) + " tets exceed the " +
                                        std::to_string(kMaxTets) + "-tet scratch limit (HOBAK_NOALLOC_MAX_TETS)");
-  if (m->kind < 0 || m->kind > 5) return fail(HOBAK_ERR_INVALID, "unknown material");
+  if (m->kind < HOBAK_MATERIAL_SNH || m->kind > HOBAK_MATERIAL_ANISOTROPIC_DIRICHLET)
+    return fail(HOBAK_ERR_INVALID, "unknown material");
+  if (hobak::is_anisotropic(m->kind) &&
+      !(m->fiber[0] * m->fiber[0] + m->fiber[1] * m->fiber[1] + m->fiber[2] * m->fiber[2] > 0.0))
+    return fail(HOBAK_ERR_INVALID, "anisotropic material needs a non-zero fibre direction");
   if (reinterpret_cast<uintptr_t>(tets) % 16 != 0) return fail(HOBAK_ERR_INVALID, "tets must be 16-byte aligned");
   double* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
@@ -133,7 +137,7 @@ extern "C" int hobak_element_eval_noalloc(int nv, int nt, const double* rest, co
   if (e != cudaSuccess) return fail(HOBAK_ERR_CUDA, std::string("rest shape: ") + cudaGetErrorString(e));
   if (bad) return fail(HOBAK_ERR_INVALID, "tet " + std::to_string(bad - 1) + " has a vertex id outside [0, nv)");
   hobak::launch_element_eval(nt, reinterpret_cast<const int4*>(tets), rest, x, scratch, scratch + 9 * (size_t)kMaxTets,
-                             m->kind, m->mu, m->lambda, F, sigma, force, hessian, s);
+                             m->kind, m->mu, m->lambda, m->fiber, F, sigma, force, hessian, s);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail(HOBAK_ERR_CUDA, std::string("element kernel: ") + cudaGetErrorString(e));

@@ -4,8 +4,11 @@ Class and method names follow the reference so code written against it reads
 the same:
 
   * VOLUME::HYPERELASTIC and its energies (Hyperelastic/Volume/HYPERELASTIC.h:31-64):
-    SNH, ARAP, STVK, LINEAR, NEO_HOOKEAN_BW, SNH_WITH_BARRIER with
-    psi / PK1 / clampedHessian, evaluated on the GPU in batches.
+    SNH, ARAP, STVK, LINEAR, NEO_HOOKEAN_BW, SNH_WITH_BARRIER and the
+    anisotropic ANISOTROPIC_ARAP, ANISOTROPIC_STVK, ANISOTROPIC_FUNG,
+    ANISOTROPIC_DIRICHLET with psi / PK1 / hessian / clampedHessian (from F or
+    from (U, Sigma, V)), energyNeedsSVD / PK1NeedsSVD, evaluated on the GPU
+    in batches.
   * TET_MESH (Geometry/TET_MESH.h): rest vertices, tets, displacement.
   * TIMESTEPPER::BACKWARD_EULER_VELOCITY (Timestepper/BACKWARD_EULER_VELOCITY.h:35-58):
     position() / velocity() / externalForces() host state, setDt, addGravity,
@@ -42,10 +45,11 @@ def _colmajor(F: np.ndarray) -> np.ndarray:
 
 
 class HYPERELASTIC:
-    """Base of the isotropic volume energies; (mu, lambda) are the reference
-    constructor arguments (the SNH reparameterisation happens in the library)."""
+    """Base of the volume energies; (mu, lambda) are the reference constructor
+    arguments (the SNH reparameterisation happens in the library)."""
     KIND = -1
     NAME = "HYPERELASTIC"
+    fiber = None
 
     def __init__(self, mu: float, lam: float):
         self.mu = float(mu)
@@ -55,7 +59,22 @@ class HYPERELASTIC:
         return self.NAME
 
     def _c(self) -> HobakMaterial:
-        return HobakMaterial(self.KIND, self.mu, self.lam)
+        a = self.fiber if self.fiber is not None else (0.0, 0.0, 0.0)
+        return HobakMaterial(self.KIND, self.mu, self.lam, (ctypes.c_double * 3)(*a))
+
+    def energyNeedsSVD(self) -> bool:
+        """HYPERELASTIC::energyNeedsSVD (HYPERELASTIC.h:56)."""
+        e, p = ctypes.c_int(), ctypes.c_int()
+        check(_lib.load().hobak_material_needs_svd(self.KIND, ctypes.byref(e), ctypes.byref(p)),
+              "hobak_material_needs_svd")
+        return bool(e.value)
+
+    def PK1NeedsSVD(self) -> bool:
+        """HYPERELASTIC::PK1NeedsSVD (HYPERELASTIC.h:59)."""
+        e, p = ctypes.c_int(), ctypes.c_int()
+        check(_lib.load().hobak_material_needs_svd(self.KIND, ctypes.byref(e), ctypes.byref(p)),
+              "hobak_material_needs_svd")
+        return bool(p.value)
 
     @staticmethod
     def computeMu(E: float, nu: float) -> float:
@@ -89,11 +108,52 @@ class HYPERELASTIC:
         P = P.reshape(-1, 3, 3).transpose(0, 2, 1)
         return P[0] if single else P
 
-    def clampedHessian(self, F):
-        """d2psi/dF2 projected to PSD, 9x9 in flatten() order, [..., 9, 9]."""
+    def clampedHessian(self, F, Sigma=None, V=None):
+        """d2psi/dF2 projected to PSD, 9x9 in flatten() order, [..., 9, 9];
+        clampedHessian(U, Sigma, V) with three arguments."""
+        if Sigma is not None:
+            return self._eval_svd(F, Sigma, V)[3]
         _, _, H, single = self._eval(F, want_H=True)
         H = H.reshape(-1, 9, 9).transpose(0, 2, 1)
         return H[0] if single else H
+
+    def hessian(self, F, Sigma=None, V=None):
+        """The unclamped d2psi/dF2 (HYPERELASTIC.h:44-45), 9x9 in flatten()
+        order; hessian(U, Sigma, V) with three arguments."""
+        if Sigma is not None:
+            return self._eval_svd(F, Sigma, V)[2]
+        Fc, single = _colmajor(F)
+        n = Fc.shape[0]
+        H = np.zeros((n, 81))
+        mat = self._c()
+        check(_lib.load().hobak_material_hessian(ctypes.byref(mat), n, dptr(Fc), dptr(H)), "hobak_material_hessian")
+        H = H.reshape(-1, 9, 9).transpose(0, 2, 1)
+        return H[0] if single else H
+
+    def _eval_svd(self, U, Sigma, V):
+        """psi, PK1, hessian, clampedHessian of the (U, Sigma, V) overloads."""
+        Uc, single = _colmajor(U)
+        Vc, _ = _colmajor(V)
+        S = np.ascontiguousarray(np.asarray(Sigma, dtype=np.float64).reshape(-1, 3))
+        n = Uc.shape[0]
+        psi, P, H, Hc = np.zeros(n), np.zeros((n, 9)), np.zeros((n, 81)), np.zeros((n, 81))
+        mat = self._c()
+        check(_lib.load().hobak_material_eval_svd(ctypes.byref(mat), n, dptr(Uc), dptr(S), dptr(Vc), dptr(psi),
+                                                  dptr(P), dptr(H), dptr(Hc)), "hobak_material_eval_svd")
+        P = P.reshape(-1, 3, 3).transpose(0, 2, 1)
+        H = H.reshape(-1, 9, 9).transpose(0, 2, 1)
+        Hc = Hc.reshape(-1, 9, 9).transpose(0, 2, 1)
+        if single:
+            return float(psi[0]), P[0], H[0], Hc[0]
+        return psi, P, H, Hc
+
+    def psi_svd(self, U, Sigma, V):
+        """psi(U, Sigma, V) (HYPERELASTIC.h:37)."""
+        return self._eval_svd(U, Sigma, V)[0]
+
+    def PK1_svd(self, U, Sigma, V):
+        """PK1(U, Sigma, V) (HYPERELASTIC.h:41)."""
+        return self._eval_svd(U, Sigma, V)[1]
 
 
 class SNH(HYPERELASTIC):
@@ -120,12 +180,44 @@ class SNH_WITH_BARRIER(HYPERELASTIC):
     KIND, NAME = 5, "SNH_WITH_BARRIER"
 
 
+class ANISOTROPIC(HYPERELASTIC):
+    """Base of the anisotropic energies: constructed as (mu, a) like
+    ANISOTROPIC_ARAP(mu, a) (ANISOTROPIC_ARAP.h:28); the library normalises a."""
+
+    def __init__(self, mu: float, a):
+        super().__init__(mu, 0.0)
+        self.fiber = tuple(float(c) for c in np.asarray(a, dtype=np.float64).reshape(3))
+
+
+class ANISOTROPIC_ARAP(ANISOTROPIC):
+    KIND, NAME = 6, "ANISOTROPIC_ARAP"
+
+
+class ANISOTROPIC_STVK(ANISOTROPIC):
+    KIND, NAME = 7, "ANISOTROPIC_STVK"
+
+
+class ANISOTROPIC_FUNG(ANISOTROPIC):
+    KIND, NAME = 8, "ANISOTROPIC_FUNG"
+
+
+class ANISOTROPIC_DIRICHLET(ANISOTROPIC):
+    KIND, NAME = 9, "ANISOTROPIC_DIRICHLET"
+
+
 MATERIAL_CLASSES = {"snh": SNH, "arap": ARAP, "stvk": STVK, "linear": LINEAR,
-                    "neo_hookean_bw": NEO_HOOKEAN_BW, "snh_barrier": SNH_WITH_BARRIER}
+                    "neo_hookean_bw": NEO_HOOKEAN_BW, "snh_barrier": SNH_WITH_BARRIER,
+                    "aniso_arap": ANISOTROPIC_ARAP, "aniso_stvk": ANISOTROPIC_STVK,
+                    "aniso_fung": ANISOTROPIC_FUNG, "aniso_dirichlet": ANISOTROPIC_DIRICHLET}
 
 
-def make_material(name: str, mu: float, lam: float) -> HYPERELASTIC:
-    return MATERIAL_CLASSES[name](mu, lam)
+def make_material(name: str, mu: float, lam: float, fiber=None) -> HYPERELASTIC:
+    """The material class of a scene: (mu, lambda) for the isotropic energies,
+    (mu, fiber) for the anisotropic ones."""
+    cls = MATERIAL_CLASSES[name]
+    if issubclass(cls, ANISOTROPIC):
+        return cls(mu, fiber if fiber is not None else (1.0, 0.0, 0.0))
+    return cls(mu, lam)
 
 
 class TET_MESH:
@@ -234,7 +326,8 @@ class BATCH:
 
     def __init__(self, scenes: Sequence, opts: Optional[HobakSolverOpts] = None):
         L = _lib.load()
-        self._arrays = [_SceneArrays(s.rest, s.tets, make_material(s.material, s.mu, s.lam), s.density,
+        self._arrays = [_SceneArrays(s.rest, s.tets,
+                                     make_material(s.material, s.mu, s.lam, getattr(s, "fiber", None)), s.density,
                                      s.gravity, s.dt, s.pinned, s.x0, s.v0) for s in scenes]
         descs = (HobakSceneDesc * len(self._arrays))(*[a.desc for a in self._arrays])
         self.nv = [len(a.rest) // 3 for a in self._arrays]
@@ -668,6 +761,7 @@ class BACKWARD_EULER_VELOCITY:
         s.rest, s.tets = self._mesh.restVertices(), self._mesh.tets()
         s.material = [k for k, c in MATERIAL_CLASSES.items() if c is type(self._material)][0]
         s.mu, s.lam = self._material.mu, self._material.lam
+        s.fiber = self._material.fiber
         s.density, s.gravity, s.dt = self._massScale, (0.0, 0.0, 0.0), self._dt
         s.pinned = np.array(sorted(set(self._pinned)), dtype=np.int32)
         s.x0, s.v0 = self._position, self._velocity

@@ -46,6 +46,11 @@ extern "C" {
 #define HOBAK_MATERIAL_LINEAR 3         /* LINEAR.cpp                          */
 #define HOBAK_MATERIAL_NEO_HOOKEAN_BW 4 /* NEO_HOOKEAN_BW.cpp                  */
 #define HOBAK_MATERIAL_SNH_BARRIER 5    /* SNH_WITH_BARRIER.cpp                */
+/* anisotropic energies along a fibre direction (hobak_material.fiber) */
+#define HOBAK_MATERIAL_ANISOTROPIC_ARAP 6      /* ANISOTROPIC_ARAP.cpp      */
+#define HOBAK_MATERIAL_ANISOTROPIC_STVK 7      /* ANISOTROPIC_STVK.cpp      */
+#define HOBAK_MATERIAL_ANISOTROPIC_FUNG 8      /* ANISOTROPIC_FUNG.cpp      */
+#define HOBAK_MATERIAL_ANISOTROPIC_DIRICHLET 9 /* ANISOTROPIC_DIRICHLET.cpp */
 
 /* ---- precision modes ---- */
 #define HOBAK_PRECISION_FP64 0   /* every kernel in FP64 */
@@ -61,11 +66,15 @@ extern "C" {
 
 /* Lame parameters as the reference materials take them: the constructor
  * arguments (mu, lambda) of SNH(mu, lambda), ARAP(mu, lambda), ...  The SNH
- * reparameterisation lambda' = lambda + mu (SNH.cpp:23-32) happens inside. */
+ * reparameterisation lambda' = lambda + mu (SNH.cpp:23-32) happens inside.
+ * The anisotropic energies take (mu, a): ANISOTROPIC_ARAP(mu, a) and its
+ * siblings (ANISOTROPIC_ARAP.h:28); lambda is unused there and `fiber` is a,
+ * normalised inside as their constructors do (ANISOTROPIC_ARAP.cpp:26-29). */
 typedef struct hobak_material {
   int kind;      /* HOBAK_MATERIAL_* */
   double mu;
   double lambda;
+  double fiber[3];  /* anisotropic energies only: the fibre direction a */
 } hobak_material;
 
 /* One scene (one tet mesh with its material and pins). */
@@ -253,6 +262,19 @@ int hobak_gpu_destroy(hobak_batch b);
  *     pFpx^T (-V clampedHessian) pFpx (TET_MESH_FASTER.cpp:95-103), 144 per
  *     tet, column major. */
 int hobak_material_eval(const hobak_material* m, int n, const double* F, double* psi, double* P, double* H);
+/* hessian(F) (HYPERELASTIC.h:44): the unclamped 9x9 d2psi/dF2 of n
+ * gradients, 81 per F, column major. */
+int hobak_material_hessian(const hobak_material* m, int n, const double* F, double* H);
+/* The (U, Sigma, V) overloads psi, PK1, hessian and clampedHessian
+ * (HYPERELASTIC.h:37, 41, 45, 49) for n factorisations (U and V 9 doubles,
+ * column major; sigma 3 doubles each, svd_rv convention).  As in the
+ * reference, ARAP and the eigensystem-based Hessians use the factors
+ * themselves and the F-form energies F = U diag(sigma) V^T.  Any output
+ * may be NULL. */
+int hobak_material_eval_svd(const hobak_material* m, int n, const double* U, const double* sigma, const double* V,
+                            double* psi, double* P, double* H, double* clampedH);
+/* energyNeedsSVD() / PK1NeedsSVD() (HYPERELASTIC.h:56-59) of a material kind. */
+int hobak_material_needs_svd(int kind, int* energy, int* pk1);
 int hobak_element_eval(int nv, int nt, const double* rest, const int* tets, const double* x,
                        const hobak_material* m, double* F, double* sigma, double* force, double* hessian);
 /* Assembled stiffness of one scene at its current state: BSR pattern

@@ -51,7 +51,7 @@ def make_elements():
             extra = {"fiber": fiber} if fiber is not None else {}
             np.savez_compressed(os.path.join(OUT, f"elements_{mat}_{name}.npz"),
                                 rest=rest, tets=tets, x=x, mu=mu, lam=lam, **extra,
-                                **{k: r[k] for k in ["F", "Sigma", "psi", "P", "H9", "H9u", "fe", "He", "R",
+                                **{k: r[k] for k in ["F", "U", "Sigma", "V", "psi", "P", "H9", "H9u", "fe", "He", "R",
                                                      "K_colptr", "K_rowidx", "K_values", "energy",
                                                      "restVolume", "oneRingVolume"]})
             print("elements", mat, name, len(tets))

@@ -28,13 +28,19 @@ def _mat(path):
     return os.path.basename(path)[len("elements_"):].rsplit("_", 1)[0]
 
 
+def _material(path, g):
+    """The golden file's material (anisotropic ones with their fibre)."""
+    return hobak.make_material(_mat(path), float(g["mu"]), float(g["lam"]),
+                               g["fiber"] if "fiber" in g.files else None)
+
+
 @pytest.mark.parametrize("path", ELEMENT_FILES, ids=[os.path.basename(p)[9:-4] for p in ELEMENT_FILES])
 def test_element_terms_match_reference(path):
     """Per-element F, sigma, force and 12x12 Hessian within 1e-10 (FP64)."""
     g = np.load(path)
     mesh = hobak.TET_MESH(g["rest"], g["tets"])
     mesh.setDisplacement(g["x"])
-    mat = hobak.make_material(_mat(path), float(g["mu"]), float(g["lam"]))
+    mat = _material(path, g)
     e = mesh.computeElements(mat)
     fl = floors(g)
     assert relmax(e["F"], g["F"]) < 1e-10
@@ -45,16 +51,34 @@ def test_element_terms_match_reference(path):
 
 @pytest.mark.parametrize("path", ELEMENT_FILES, ids=[os.path.basename(p)[9:-4] for p in ELEMENT_FILES])
 def test_material_interface_matches_reference(path):
-    """psi / PK1 / clampedHessian of the HYPERELASTIC boundary within 1e-10."""
+    """psi / PK1 / clampedHessian / hessian of the HYPERELASTIC boundary
+    within 1e-10, from F (HYPERELASTIC.h:36-48) and from the reference's own
+    (U, Sigma, V) (HYPERELASTIC.h:37-49)."""
     g = np.load(path)
-    mat = hobak.make_material(_mat(path), float(g["mu"]), float(g["lam"]))
-    F = g["F"].reshape(-1, 3, 3).transpose(0, 2, 1)  # column-major flatten -> [i, j]
+    mat = _material(path, g)
+    sq = lambda a: a.reshape(-1, 3, 3).transpose(0, 2, 1)  # column-major flatten -> [i, j]
+    flat = lambda a, n: a.transpose(0, 2, 1).reshape(-1, n)
+    F = sq(g["F"])
     fl = floors(g)
     assert relmax(mat.psi(F), g["psi"], fl["psi"]) < 1e-10
-    P = mat.PK1(F).transpose(0, 2, 1).reshape(-1, 9)
-    assert relmax(P, g["P"], fl["P"]) < 1e-10
-    H = mat.clampedHessian(F).transpose(0, 2, 1).reshape(-1, 81)
-    assert relmax(H, g["H9"]) < 1e-10
+    assert relmax(flat(mat.PK1(F), 9), g["P"], fl["P"]) < 1e-10
+    assert relmax(flat(mat.clampedHessian(F), 81), g["H9"]) < 1e-10
+    assert relmax(flat(mat.hessian(F), 81), g["H9u"], fl["P"]) < 1e-10
+    psi, P, H, Hc = mat._eval_svd(sq(g["U"]), g["Sigma"], sq(g["V"]))
+    assert relmax(psi, g["psi"], fl["psi"]) < 1e-10
+    assert relmax(flat(P, 9), g["P"], fl["P"]) < 1e-10
+    assert relmax(flat(Hc, 81), g["H9"]) < 1e-10
+    assert relmax(flat(H, 81), g["H9u"], fl["P"]) < 1e-10
+
+
+def test_material_needs_svd_flags():
+    """energyNeedsSVD / PK1NeedsSVD as each reference class answers them."""
+    expect = {"snh": False, "arap": True, "stvk": False, "linear": False, "neo_hookean_bw": False,
+              "snh_barrier": False, "aniso_arap": True, "aniso_stvk": True, "aniso_fung": True,
+              "aniso_dirichlet": False}
+    for name, flag in expect.items():
+        m = hobak.make_material(name, 1.0, 1.0)
+        assert m.energyNeedsSVD() == flag and m.PK1NeedsSVD() == flag, name
 
 
 @pytest.mark.parametrize("path", [p for p in ELEMENT_FILES if "_snh_" in p or "_arap_" in p],
@@ -63,7 +87,8 @@ def test_assembled_stiffness_matches_reference_csc(path):
     """Block pattern bit-exact against the reference CSC; K and R within 1e-10."""
     g = np.load(path)
     s = scenes.Scene("g", g["rest"], g["tets"], _mat(path), float(g["mu"]), float(g["lam"]),
-                     np.zeros(0, np.int32), g["x"].reshape(-1, 3), np.zeros_like(g["x"]).reshape(-1, 3))
+                     np.zeros(0, np.int32), g["x"].reshape(-1, 3), np.zeros_like(g["x"]).reshape(-1, 3),
+                     fiber=tuple(g["fiber"]) if "fiber" in g.files else None)
     b = hobak.BATCH([s])
     rowptr, cols, K, R = b.assemble(0)
     nv = s.nv
@@ -84,7 +109,8 @@ def test_assembled_stiffness_matches_reference_csc(path):
 
 TRAJ = [("kuhn10_snh", lambda: scenes.config1_scene(10)),
         ("kuhn6_snh_twist", lambda: scenes.config2_scene(6, "snh")),
-        ("kuhn6_arap_twist", lambda: scenes.config2_scene(6, "arap"))]
+        ("kuhn6_arap_twist", lambda: scenes.config2_scene(6, "arap"))] + \
+       [(f"kuhn6_{m}_twist", (lambda m=m: scenes.aniso_scene(6, m))) for m in scenes.ANISOTROPIC]
 
 
 @pytest.mark.parametrize("precond", [hobak.PRECOND_JACOBI, hobak.PRECOND_BLOCK_JACOBI], ids=["jacobi", "block"])
@@ -135,3 +161,23 @@ def test_larger_mesh_matches_oracle_few_steps():
     x, _ = b.get_state(0)
     xo, _ = sim.state()
     assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
+
+
+@pytest.mark.parametrize("precision,bound", [(hobak.PRECISION_FP64, 1e-8), (hobak.PRECISION_MIXED, 1e-6)],
+                         ids=["fp64", "mixed"])
+def test_anisotropic_and_isotropic_scenes_batched(precision, bound):
+    """Anisotropic energies (k_element_aniso) beside isotropic ones
+    (k_element) in one batch: each scene against the oracle, and the
+    anisotropic scene's result the same alone and in the batch."""
+    mix = [scenes.aniso_scene(6, "aniso_arap"), scenes.config2_scene(5, "snh"), scenes.aniso_scene(5, "aniso_fung")]
+    b = hobak.BATCH(mix, hobak.solver_opts(precision=precision))
+    b.step(10)
+    for i, s in enumerate(mix):
+        sim = oracle.Sim(s, precond=hobak.PRECOND_BLOCK_JACOBI)
+        sim.step(10)
+        x, _ = b.get_state(i)
+        xo, _ = sim.state()
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < bound, (i, s.name)
+    alone = hobak.BATCH([mix[0]], hobak.solver_opts(precision=precision))
+    alone.step(10)
+    assert np.array_equal(alone.get_state(0)[0], b.get_state(0)[0])

@@ -11,8 +11,9 @@
   contact, 76 steps).  Contact makes the trajectory discontinuous in the
   state: a vertex crossing the detection distance adds or drops a spring.
   Mixed precision tracks FP64 within 1e-6 for as long as both runs find the
-  same vertex-face pairs; the first step where the pair sets differ is
-  recorded here (SPLIT_STEP) and checked."""
+  same vertex-face pairs on the same side of their faces; the first steps
+  where the contact branches and the pair sets differ are recorded here
+  (SPLIT_STEPS) and checked."""
 import numpy as np
 import pytest
 
@@ -21,9 +22,10 @@ from oracle import oracle
 
 pytestmark = pytest.mark.gpu
 
-# first step after which the mixed and FP64 runs of serving job 2 detect
-# different vertex-face pair sets
-SPLIT_STEP = 22
+# serving job 2: the first step whose contact response differs between the
+# mixed and FP64 runs (a pair's reversal branch), and the first step whose
+# vertex-face pair sets differ
+SPLIT_STEPS = (21, 22)
 
 
 def rel(a, b):
@@ -50,12 +52,21 @@ def test_mix256_subset_matches_oracle(precision, bound):
     b.close()
 
 
-def pair_set(b):
-    p, _ = b.collision_pairs(0)
-    return set(map(tuple, p.tolist()))
+def contact_branches(b, x_start, rest):
+    """{collision tet: reversal flag} of the last detection.  The flag is
+    VERTEX_FACE_SQRT_COLLISION::reverse (VERTEX_FACE_SQRT_COLLISION.cpp:73-86)
+    at the state the detection saw: the vertex behind the face switches the
+    spring from |t| - eps to |t| + eps, which makes the clamped Hessian jump
+    as the vertex crosses the face plane, with the pair set unchanged."""
+    tets, _, _ = b.collision_response(0)
+    p = (x_start + rest).reshape(-1, 3)
+    v = p[tets]  # [n, 4, 3]: vertex, face[2], face[1], face[0]
+    e0, e1, e2 = v[:, 3] - v[:, 2], v[:, 0] - v[:, 2], v[:, 1] - v[:, 2]
+    rev = np.einsum("ij,ij->i", np.cross(e2, e0), e1) < 0
+    return {tuple(t): bool(r) for t, r in zip(tets.tolist(), rev)}
 
 
-def test_serving_contact_job_mixed_tracks_fp64_until_pair_sets_split():
+def test_serving_contact_job_mixed_tracks_fp64_until_contact_splits():
     sc, nsteps, contact = scenes.config5_jobs(32)[2]
     assert sc.N == 26 and nsteps == 76 and contact is not None
     runs = {}
@@ -64,20 +75,28 @@ def test_serving_contact_job_mixed_tracks_fp64_until_pair_sets_split():
         b.set_collisions(0, True, *contact)
         runs[name] = b
     rest = sc.rest.reshape(-1)
-    split = None
+    start = {n: b.get_state(0)[0] for n, b in runs.items()}
+    split_pairs = split_branch = None
     worst_before = 0.0
     for k in range(1, nsteps + 1):
         for b in runs.values():
             b.step(1)
-        if pair_set(runs["mixed"]) != pair_set(runs["fp64"]):
-            split = k
+        br = {n: contact_branches(b, start[n], rest) for n, b in runs.items()}
+        if split_pairs is None and set(br["mixed"]) != set(br["fp64"]):
+            split_pairs = k
+        if split_branch is None and br["mixed"] != br["fp64"]:
+            split_branch = k
+        if split_branch is not None and split_pairs is not None:
             break
         xm, _ = runs["mixed"].get_state(0)
         xf, _ = runs["fp64"].get_state(0)
-        e = rel(xm + rest, xf + rest)
-        worst_before = max(worst_before, e)
-        assert e < 1e-6, (k, e)
+        if split_branch is None:
+            e = rel(xm + rest, xf + rest)
+            worst_before = max(worst_before, e)
+            assert e < 1e-6, (k, e)
+        start = {"mixed": xm, "fp64": xf}
     for b in runs.values():
         b.close()
-    print(f"serving job 2: pair sets split after step {split}; mixed vs FP64 before that <= {worst_before:.2e}")
-    assert split == SPLIT_STEP, split
+    print(f"serving job 2: contact branches split at step {split_branch}, pair sets at step {split_pairs}; "
+          f"mixed vs FP64 before that <= {worst_before:.2e}")
+    assert (split_branch, split_pairs) == SPLIT_STEPS, (split_branch, split_pairs)
