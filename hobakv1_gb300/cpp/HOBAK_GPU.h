@@ -144,6 +144,19 @@ class ANISOTROPIC_DIRICHLET : public ANISOTROPIC {
   std::string name() const override { return "ANISOTROPIC_DIRICHLET"; }
 };
 
+// VOLUME::GREEN_DAMPING(mu) (Damping/Volume/GREEN_DAMPING.h): the damping
+// of NEWMARK's energy-damped solve, P = mu F (F^T Fdot + Fdot^T F)
+// (GREEN_DAMPING.cpp:46-50); evaluated on the device inside the step.
+class GREEN_DAMPING {
+ public:
+  explicit GREEN_DAMPING(const REAL& mu) : _mu(mu) {}
+  std::string name() const { return "GREEN_DAMPING"; }
+  REAL mu() const { return _mu; }
+
+ private:
+  REAL _mu;
+};
+
 }  // namespace VOLUME
 
 // Rest mesh (TET_MESH.h): rest vertices and tets, plus the displacement the
@@ -400,10 +413,19 @@ class NEWMARK : public BACKWARD_EULER_VELOCITY {
     _name = "NEWMARK";
     _acceleration.assign(tetMesh.DOFs(), 0.0);
   }
+  // NEWMARK(tetMesh, hyperelastic, damping): the energy-damped solve
+  // (NEWMARK.cpp:344-420) with GREEN_DAMPING(mu)
+  NEWMARK(TET_MESH& tetMesh, VOLUME::HYPERELASTIC& hyperelastic, const VOLUME::GREEN_DAMPING& damping)
+      : NEWMARK(tetMesh, hyperelastic) {
+    _greenMu = damping.mu();
+  }
   VECTOR& acceleration() { return _acceleration; }
   int& maxNewtonIterations() { return _opts.max_newton; }
   bool solve(const bool verbose) {
-    if (!_handle && !build()) return false;
+    if (!_handle) {
+      if (!build()) return false;
+      if (_greenMu > 0.0 && hobak_batch_set_green_damping(_handle, 0, _greenMu) != HOBAK_OK) return fail();
+    }
     if (hobak_batch_set_acceleration(_handle, 0, _acceleration.data()) != HOBAK_OK) return fail();
     if (!BACKWARD_EULER_VELOCITY::solve(verbose)) return false;
     if (hobak_batch_get_acceleration(_handle, 0, _acceleration.data()) != HOBAK_OK) return fail();
@@ -412,6 +434,7 @@ class NEWMARK : public BACKWARD_EULER_VELOCITY {
 
  private:
   VECTOR _acceleration;
+  REAL _greenMu = 0.0;
 };
 
 }  // namespace TIMESTEPPER

@@ -698,12 +698,14 @@ long long solve_launches(const hobak_batch_t* B) {
 // Kernels of one Newton loop body (Newmark) outside the PCG loop bodies and
 // k_newton_continue: element, assembly, preconditioner, rhs, the solve, and
 // the update + test.
-long long newton_body_launches(const hobak_batch_t* B) { return 4 + solve_launches(B) + 2; }
+long long newton_body_launches(const hobak_batch_t* B) {
+  return 3 + element_launches(B->d) + (B->d.anyGreen ? 1 : 0) + solve_launches(B) + 2;
+}
 
 long long fixed_launches(const hobak_batch_t* B) {
   // begin, Newton begin, finish (+ the Newton loop's arming kernel in a graph)
   if (B->opts.integrator == HOBAK_INTEGRATOR_NEWMARK) return 3 + (B->opts.use_graph ? 1 : 0);
-  return 6 + solve_launches(B);
+  return 5 + element_launches(B->d) + solve_launches(B);
 }
 
 void drop_graphs(hobak_batch_t* B);
@@ -920,6 +922,7 @@ int enqueue_newton_body(hobak_batch_t* B, cudaStream_t s, bool capture, const Pc
   const DeviceBatch& d = B->d;
   if (sizeof(T) == sizeof(float)) launch_element_mixed(d, s);
   else launch_element(d, s);
+  launch_green_damping(d, s);
   launch_assemble<T>(d, v, s);
   launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
   launch_rhs(d, s);
@@ -1283,10 +1286,10 @@ int run_steps(hobak_batch_t* B, int nsteps) {
       if (rc) return rc;
     }
     B->launches += fixed_launches(B);
-    B->phaseLaunches[0] += 2;
+    B->phaseLaunches[0] += 1 + element_launches(B->d);
     B->phaseLaunches[1] += 2;
     B->phaseLaunches[2] += 1;
-    B->phaseLaunches[3] += fixed_launches(B) - 6;
+    B->phaseLaunches[3] += fixed_launches(B) - 5 - element_launches(B->d);
     B->phaseLaunches[4] += 1;
     if (timed) {
       CUDA_TRY(cudaEventSynchronize(B->ev[5]));
@@ -2015,6 +2018,24 @@ int hobak_batch_get_tuning(hobak_batch b, hobak_tuning* out) {
   out->cluster_pcg = b->clusterPcg ? 1 : 0;
   out->cluster_max = b->clusterMax;
   out->step_ms = 0.0;
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_green_damping(hobak_batch b, int scene, double mu) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  if (b->opts.integrator != HOBAK_INTEGRATOR_NEWMARK)
+    return fail(HOBAK_ERR_INVALID, "GREEN_DAMPING: only NEWMARK's energy-damped solve is defined");
+  if (!(mu >= 0.0) || !std::isfinite(mu)) return fail(HOBAK_ERR_INVALID, "damping mu must be finite and >= 0");
+  b->sceneParams[scene].greenMu = mu;
+  int any = 0;
+  for (const SceneParams& p : b->sceneParams) any |= p.greenMu > 0.0 ? 1 : 0;
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(cudaMemcpy(const_cast<SceneParams*>(b->d.scenes) + scene, &b->sceneParams[scene], sizeof(SceneParams),
+                      cudaMemcpyHostToDevice));
+  if (any != b->d.anyGreen) {  // the Newton body gains or loses a kernel
+    b->d.anyGreen = any;
+    drop_graphs(b);
+  }
   return HOBAK_OK;
 }
 

@@ -369,6 +369,67 @@ __device__ __forceinline__ void reduced_to_h9(const double* Hr, double* H) {
     for (int c = 0; c < 9; c++) H[r + 9 * c] = (r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)];
 }
 
+// NEWMARK's energy-damped solve (NEWMARK.cpp:344-420): the GREEN_DAMPING
+// force of every tet of a damped scene added to its element force, so the
+// right-hand side's R holds the elastic and damping forces
+// (TET_MESH::computeInternalForces).  The damping Hessian is passed to
+// computeCollisionResponse, which zeroes it (TIMESTEPPER.cpp:657), so the
+// system matrix is unchanged.  Per tet: the iterate's velocity
+// S (a3 (x - x_old) + a4 v_old + a5 a_old) of its four vertices (zero at
+// pins), Fdot = Vs DmInv (TET_MESH::computeFdots, TET_MESH.cpp:660-684),
+// P = mu F (F^T Fdot + Fdot^T F) (GREEN_DAMPING.cpp:46-50) and the force
+// -vol pFpx^T vec(P).  Runs after k_element, only in batches with a damped
+// scene, so the element kernel itself is unchanged.
+__global__ void __launch_bounds__(128) k_green_damping(DeviceBatch b) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.nt) return;
+  const int sc = b.tetScene[t];
+  const SceneParams& sp = b.scenes[sc];
+  if (!sp.active || !(sp.greenMu > 0.0) || b.solve[sc].newtonDone) return;
+  const int4 tv = b.tets[t];
+  const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
+  double Dinv[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) Dinv[k] = b.DmInv[9 * (size_t)t + k];
+  double X[4][3], vel[4][3];
+  load_tet(tv, b.rest, b.x, X);
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const bool free = b.freeMask[vid[a]] != 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const size_t q = 3 * (size_t)vid[a] + i;
+      vel[a][i] = free ? sp.nm[3] * (b.x[q] - b.xOld[q]) + sp.nm[4] * b.vOld[q] + sp.nm[5] * b.aOld[q] : 0.0;
+    }
+  }
+  double F[9], Fd[9];
+  deformation_gradient(X, Dinv, F);
+  deformation_gradient(vel, Dinv, Fd);
+  double G[9], P[9];  // G = F^T Fdot + Fdot^T F (symmetric), P = mu F G
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      double a = 0.0, c = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        a += F[k + 3 * i] * Fd[k + 3 * j];
+        c += Fd[k + 3 * i] * F[k + 3 * j];
+      }
+      G[i + 3 * j] = a + c;
+    }
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      P[i + 3 * j] = sp.greenMu * (F[i] * G[3 * j] + F[i + 3] * G[1 + 3 * j] + F[i + 6] * G[2 + 3 * j]);
+  double f[12];
+  element_force(P, Dinv, b.vol[t], f);
+  double* g = b.elemG + 12 * (size_t)t;
+#pragma unroll
+  for (int k = 0; k < 12; k++) g[k] += f[k];
+}
+
 // Standalone material terms of n elements (the VOLUME::HYPERELASTIC
 // interface): psi, PK1, clampedHessian and the unclamped hessian, from F
 // (svd_rv computed here) or, when Uin is given, from (U, Sigma, V) as the
@@ -536,6 +597,11 @@ void launch_element_mixed(const DeviceBatch& b, cudaStream_t s) {
   const int nt = b.elemThreads;
   k_element<float><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, 0, b.elemHf);
   if (b.anyAniso) k_element_aniso<float><<<(b.nt + 127) / 128, 128, 0, s>>>(b, 0, b.elemHf);
+}
+
+void launch_green_damping(const DeviceBatch& b, cudaStream_t s) {
+  if (b.nt == 0 || !b.anyGreen) return;
+  k_green_damping<<<(b.nt + 127) / 128, 128, 0, s>>>(b);
 }
 
 void launch_energy(const DeviceBatch& b, cudaStream_t s) {

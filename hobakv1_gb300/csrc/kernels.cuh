@@ -132,6 +132,7 @@ struct DeviceBatch {
   double* partial;      // [ntiles][kPartials]
   double* psi;          // [T] energy density scratch
   int anyAniso;          // some scene has an anisotropic energy (k_element_aniso)
+  int anyGreen;          // some Newmark scene has GREEN_DAMPING (k_green_damping)
   // vertex-face collisions (collOn = 0: none in this batch)
   int collOn;
   DeviceCollisions coll;
@@ -160,6 +161,12 @@ void launch_begin_step(const DeviceBatch& b, cudaStream_t s);
 // rawForces = 1 stores the element force f itself in elemG instead of dt (f + dt He v)
 void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces = 0);
 void launch_element_mixed(const DeviceBatch& b, cudaStream_t s);
+// NEWMARK energy-damped solve: adds each damped scene's GREEN_DAMPING element
+// forces to elemG (after the element kernel; no-op without damped scenes)
+void launch_green_damping(const DeviceBatch& b, cudaStream_t s);
+// element-phase kernel launches of a batch: k_element, plus k_element_aniso
+// and k_green_damping where the batch needs them
+inline int element_launches(const DeviceBatch& b) { return 1 + (b.anyAniso ? 1 : 0); }
 // K blocks (column major, un-masked, no mass) and R = sum of element forces, for inspection
 void launch_assemble_raw(const DeviceBatch& b, double* K, double* R, cudaStream_t s);
 template <typename T>

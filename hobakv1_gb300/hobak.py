@@ -563,6 +563,11 @@ class BATCH:
         check(_lib.load().hobak_batch_get_tuning(self.h, ctypes.byref(t)), "hobak_batch_get_tuning")
         return {k: getattr(t, k) for k in self.TUNING}
 
+    def set_green_damping(self, scene: int, mu: float):
+        """NEWMARK's energy-damped solve with GREEN_DAMPING(mu) for one scene
+        (NEWMARK batches only; mu = 0 turns it off)."""
+        check(_lib.load().hobak_batch_set_green_damping(self.h, scene, float(mu)), "hobak_batch_set_green_damping")
+
     def pcg_path(self) -> np.ndarray:
         """Per scene: CTAs of the cluster that solves its inner PCG (0: the tile path)."""
         out = np.zeros(len(self), dtype=np.int32)
@@ -817,6 +822,18 @@ class BACKWARD_EULER_POSITION(BACKWARD_EULER_VELOCITY):
 
 
 
+class GREEN_DAMPING:
+    """VOLUME::GREEN_DAMPING(mu) (Damping/Volume/GREEN_DAMPING.h): the damping
+    of NEWMARK's energy-damped solve; psi = mu |sym(Fdot^T F)|^2,
+    PK1 = mu F (F^T Fdot + Fdot^T F) (GREEN_DAMPING.cpp:36-50)."""
+
+    def __init__(self, mu: float):
+        self.mu = float(mu)
+
+    def name(self) -> str:
+        return "GREEN_DAMPING"
+
+
 class NEWMARK(BACKWARD_EULER_VELOCITY):
     """GPU drop-in for TIMESTEPPER::NEWMARK (Rayleigh-damped solve,
     NEWMARK.cpp:183-340: a Newton loop of at most maxNewtonIterations() solves,
@@ -824,10 +841,15 @@ class NEWMARK(BACKWARD_EULER_VELOCITY):
     host state that solve() uploads and downloads.  Vertex-face contact is not
     available with this integrator."""
 
-    def __init__(self, tetMesh: TET_MESH, hyperelastic: HYPERELASTIC, opts: Optional[HobakSolverOpts] = None):
+    def __init__(self, tetMesh: TET_MESH, hyperelastic: HYPERELASTIC, damping=None,
+                 opts: Optional[HobakSolverOpts] = None):
+        if isinstance(damping, HobakSolverOpts):  # NEWMARK(mesh, material, opts)
+            damping, opts = None, damping
         super().__init__(tetMesh, hyperelastic, None if opts is None else HobakSolverOpts.from_buffer_copy(opts))
         self._opts.integrator = INTEGRATOR_NEWMARK
         self._acceleration = np.zeros(tetMesh.DOFs())
+        # NEWMARK(mesh, material, damping): the energy-damped solve (NEWMARK.cpp:344-420)
+        self._damping = damping
 
     def acceleration(self):
         return self._acceleration
@@ -852,6 +874,8 @@ class NEWMARK(BACKWARD_EULER_VELOCITY):
     def solve(self, verbose: bool = False) -> bool:
         if self._batch is None:
             self._build()
+            if self._damping is not None:
+                self._batch.set_green_damping(0, self._damping.mu)
         self._batch.set_acceleration(0, self._acceleration)
         ok = super().solve(verbose)
         self._acceleration[:] = self._batch.get_acceleration(0)

@@ -159,6 +159,13 @@ int hobak_batch_get_state(hobak_batch b, int scene, double* x, double* v);
  * other integrators leave it untouched). */
 int hobak_batch_get_acceleration(hobak_batch b, int scene, double* a);
 int hobak_batch_set_acceleration(hobak_batch b, int scene, const double* a);
+/* NEWMARK's energy-damped solve for one scene: the damping of
+ * NEWMARK(mesh, material, GREEN_DAMPING(mu)) (NEWMARK.h constructor with a
+ * DAMPING; NEWMARK::solveEnergyDamped, NEWMARK.cpp:344-420;
+ * GREEN_DAMPING.cpp:46-50).  mu = 0 turns it off.  NEWMARK batches only: the
+ * reference's damped BACKWARD_EULER_VELOCITY solve reads a never-computed
+ * Fdot, so other integrators refuse it. */
+int hobak_batch_set_green_damping(hobak_batch b, int scene, double mu);
 /* Move one scene's pins: 3 target displacements (world - rest) per pinned
  * vertex, in the order hobak_scene_desc.pinned listed them.  Replaces
  * applyKinematicConstraints recomputing the targets from moved kinematic

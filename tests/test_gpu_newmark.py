@@ -127,3 +127,70 @@ def test_python_mirror_newmark_matches_oracle():
     assert rel(nm.position(), x) < 1e-9
     assert rel(nm.velocity(), v) < 1e-8
     assert rel(nm.acceleration(), sim.acceleration()) < 1e-7
+
+
+def test_green_damped_newmark_matches_reference_fixture():
+    """NEWMARK's energy-damped solve with GREEN_DAMPING(mu) (NEWMARK.cpp:
+    344-420): with the reference's Jacobi preconditioner, positions after
+    each of six steps within 1e-8 of the reference build's trajectories
+    (traj_kuhn5_snh_newmark_green.npz), at mu = 0.05 and 1.0."""
+    g = np.load(os.path.join(GOLDEN, "traj_kuhn5_snh_newmark_green.npz"))
+    s = scenes.config1_scene(5)
+    for mu in g["mus"]:
+        xr = g[f"x_mu{mu:g}".replace(".", "p")]
+        b = hobak.BATCH([s], hobak.solver_opts(preconditioner=hobak.PRECOND_JACOBI, integrator=NM))
+        b.set_green_damping(0, mu)
+        for k in range(int(g["steps"])):
+            b.step(1)
+            x, _ = b.get_state(0)
+            assert rel(x, xr[k + 1]) < 1e-8, (mu, k, rel(x, xr[k + 1]))
+        b.close()
+
+
+@pytest.mark.parametrize("precision,bound", [(hobak.PRECISION_FP64, 1e-10), (hobak.PRECISION_MIXED, 1e-6)],
+                         ids=["fp64", "mixed"])
+def test_green_damped_newmark_matches_oracle_and_batches(precision, bound):
+    """Block Jacobi against the oracle's energy-damped NEWMARK; a damped and
+    an undamped scene in one batch each match their own oracle run, and the
+    damped scene is the same alone and in the batch."""
+    mix = [scenes.config2_scene(6, "snh"), scenes.config1_scene(6)]
+    b = hobak.BATCH(mix, hobak.solver_opts(precision=precision, integrator=NM))
+    b.set_green_damping(0, 0.5)
+    b.step(8)
+    for i, s in enumerate(mix):
+        sim = oracle.Sim(s, precond=hobak.PRECOND_BLOCK_JACOBI, integrator="newmark")
+        if i == 0:
+            sim.set_green_damping(0.5)
+        sim.step(8)
+        x, _ = b.get_state(i)
+        xo, _ = sim.state()
+        assert rel(x, xo) < bound, (i, rel(x, xo))
+    alone = hobak.BATCH([mix[0]], hobak.solver_opts(precision=precision, integrator=NM))
+    alone.set_green_damping(0, 0.5)
+    alone.step(8)
+    assert np.array_equal(alone.get_state(0)[0], b.get_state(0)[0])
+
+
+def test_green_damping_refused_outside_newmark():
+    b = hobak.BATCH([scenes.config1_scene(3)])
+    with pytest.raises(_lib.HobakError):
+        b.set_green_damping(0, 0.1)
+
+
+def test_python_mirror_newmark_with_green_damping():
+    """NEWMARK(mesh, material, GREEN_DAMPING(mu)), as the reference constructs
+    the energy-damped integrator, against the oracle."""
+    s = scenes.config1_scene(5)
+    mesh = hobak.TET_MESH(s.rest, s.tets)
+    nm = hobak.NEWMARK(mesh, hobak.SNH(s.mu, s.lam), hobak.GREEN_DAMPING(1.0))
+    nm.scaleMass(s.density)
+    nm.attachKinematicConstraints(s.pinned)
+    sim = oracle.Sim(s, precond=hobak.PRECOND_BLOCK_JACOBI, integrator="newmark")
+    sim.set_green_damping(1.0)
+    for _ in range(4):
+        nm.externalForces()[:] = 0.0
+        nm.addGravity(np.array(s.gravity) * s.density)
+        nm.solve(False)
+    sim.step(4)
+    x, _ = sim.state()
+    assert rel(nm.position(), x) < 1e-9
