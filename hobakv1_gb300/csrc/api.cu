@@ -474,7 +474,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   // tiles: kTileV consecutive vertices of one scene (apply_tile_size changes
   // the size later; the tables are sized for kMinTileV)
   int ntilesCap = 0;
-  int anyAniso = 0;
+  int anyAniso = 0, anyArap = 0, anySvdFree = 0;
   for (int s = 0; s < n; s++) {
     SceneHost& H = B->scenes[s];
     ntilesCap += (H.nv + kMinTileV - 1) / kMinTileV;
@@ -500,6 +500,8 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     p.alpha = mp.alpha;
     for (int i = 0; i < 3; i++) p.fiber[i] = mp.a[i];
     if (is_anisotropic(mp.kind)) anyAniso = 1;
+    else if (mp.kind == MAT_ARAP) anyArap = 1;
+    else anySvdFree = 1;
     p.dt = H.dt;
     set_integrator(p, B->opts);
     p.active = 1;
@@ -607,6 +609,8 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.partial = carve<double>(base, oPart);
   d.psi = carve<double>(base, oPsi);
   d.anyAniso = anyAniso;
+  d.anyArap = anyArap;
+  d.anySvdFree = anySvdFree;
 
   auto up = [&](const void* dst, const void* src, size_t bytes) {
     return cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice);
@@ -699,13 +703,14 @@ long long solve_launches(const hobak_batch_t* B) {
 // k_newton_continue: element, assembly, preconditioner, rhs, the solve, and
 // the update + test.
 long long newton_body_launches(const hobak_batch_t* B) {
-  return 3 + element_launches(B->d) + (B->d.anyGreen ? 1 : 0) + solve_launches(B) + 2;
+  return 3 + element_launches(B->d, B->opts.precision == HOBAK_PRECISION_MIXED) + (B->d.anyGreen ? 1 : 0) +
+         solve_launches(B) + 2;
 }
 
 long long fixed_launches(const hobak_batch_t* B) {
   // begin, Newton begin, finish (+ the Newton loop's arming kernel in a graph)
   if (B->opts.integrator == HOBAK_INTEGRATOR_NEWMARK) return 3 + (B->opts.use_graph ? 1 : 0);
-  return 5 + element_launches(B->d) + solve_launches(B);
+  return 5 + element_launches(B->d, B->opts.precision == HOBAK_PRECISION_MIXED) + solve_launches(B);
 }
 
 void drop_graphs(hobak_batch_t* B);
@@ -1286,10 +1291,11 @@ int run_steps(hobak_batch_t* B, int nsteps) {
       if (rc) return rc;
     }
     B->launches += fixed_launches(B);
-    B->phaseLaunches[0] += 1 + element_launches(B->d);
+    const int elaunch = element_launches(B->d, B->opts.precision == HOBAK_PRECISION_MIXED);
+    B->phaseLaunches[0] += 1 + elaunch;
     B->phaseLaunches[1] += 2;
     B->phaseLaunches[2] += 1;
-    B->phaseLaunches[3] += fixed_launches(B) - 5 - element_launches(B->d);
+    B->phaseLaunches[3] += fixed_launches(B) - 5 - elaunch;
     B->phaseLaunches[4] += 1;
     if (timed) {
       CUDA_TRY(cudaEventSynchronize(B->ev[5]));
@@ -2002,7 +2008,7 @@ int hobak_batch_time_kernels(hobak_batch b, int reps, double* ms) {
     CUDA_TRY(cudaEventElapsedTime(&t, e0, e1));
     ms[k] = t / reps;
   }
-  b->launches += 4LL * reps + 1;
+  b->launches += (3LL + element_launches(d, mixed)) * reps + 1;
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpy(const_cast<SceneParams*>(d.scenes), b->sceneParams.data(), sizeof(SceneParams) * n,
                       cudaMemcpyHostToDevice));
@@ -2141,7 +2147,7 @@ int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out) {
       float ms = 0;
       int rc = elapsed(&ms);
       if (rc) return rc;
-      b->launches += reps;
+      b->launches += (long long)reps * element_launches(d, mixed);
       if (ms < bestMs) {
         bestMs = ms;
         best.element_threads = et;

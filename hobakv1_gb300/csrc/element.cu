@@ -26,9 +26,9 @@ __host__ __device__ __forceinline__ constexpr int sym9(int r, int c) { return r 
 // Returns in Hr[45].  U, B are the SVD's U and B = DmInv V.
 // clamp = false keeps negative eigenvalues: the unclamped hessian()
 // (HYPERELASTIC.h:44) from the same eigensystem.
-template <typename T>
-__device__ __forceinline__ void reduced_hessian(const MatParams& m, const double* Ud, const double* Sd,
-                                                const double* Vd, const double* Dinv, T* Hr, bool clamp = true) {
+template <typename T, typename IT = double>
+__device__ __forceinline__ void reduced_hessian(const MatParams& m, const IT* Ud, const IT* Sd, const IT* Vd,
+                                                const double* Dinv, T* Hr, bool clamp = true) {
 #pragma unroll
   for (int k = 0; k < 45; k++) Hr[k] = T(0);
   if (m.kind == MAT_LINEAR) {
@@ -50,7 +50,7 @@ __device__ __forceinline__ void reduced_hessian(const MatParams& m, const double
     return;
   }
   T L[9], A3[9], Q3[9];
-  const bool scalingMatrix = material_eigensystem<T>(m, Sd, L, A3);
+  const bool scalingMatrix = material_eigensystem<T, IT>(m, Sd, L, A3);
   if (scalingMatrix) {
     T L3[3];
     eig3sym<T>(A3, Q3, L3);
@@ -196,11 +196,19 @@ __device__ __forceinline__ void deformation_gradient(const double X[4][3], const
       F[i + 3 * j] = Ds[i] * Dinv[3 * j] + Ds[i + 3] * Dinv[1 + 3 * j] + Ds[i + 6] * Dinv[2 + 3 * j];
 }
 
+// Which tets an instantiation of k_element evaluates: every isotropic tet
+// (the FP64 path), or, in the mixed path, split by whether the stress reads
+// the SVD: ARAP's PK1 = 2 mu (F - U V^T) takes the FP64 SVD; the other
+// isotropic energies' PK1 is a function of F, so their SVD only feeds the
+// FP32 Hessian and runs in FP32 (svd3_rv_f32).
+constexpr int kElemAll = 0, kElemSvdFree = 1, kElemArap = 2;
+
 // Batched step kernel: element Hessian blocks and right-hand-side terms
 // g = dt (f + dt He v) for every tet of every scene.
 // HT is the Hessian's arithmetic/storage type: double (FP64 path) or float
-// (mixed path: F, SVD, stress and forces stay FP64).
-template <typename HT>
+// (mixed path: F, stress and forces stay FP64; the SVD is FP64 where the
+// stress reads it).
+template <typename HT, int KC>
 // FP32 Hessians fit 128 registers (4 CTAs per SM, a few bytes of spill); the
 // FP64 variant needs ~208 and spills heavily below that.
 __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
@@ -209,6 +217,7 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   if (t >= b.nt) return;
   const SceneParams& sp = b.scenes[b.tetScene[t]];
   if (!sp.active || is_anisotropic(sp.kind)) return;  // anisotropic energies: k_element_aniso
+  if ((KC == kElemSvdFree && sp.kind == MAT_ARAP) || (KC == kElemArap && sp.kind != MAT_ARAP)) return;
   // Newmark: a scene whose Newton loop is over needs no further element terms
   if (!rawForces && sp.integrator == kIntegratorNewmark && b.solve[b.tetScene[t]].newtonDone) return;
   const int4 tv = b.tets[t];
@@ -224,15 +233,23 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   const double vol = b.vol[t];
   double X[4][3];
   load_tet(tv, b.rest, b.x, X);
-  double F[9], U[9], S[3], V[9], P[9], f[12];
+  double F[9], P[9], f[12];
   deformation_gradient(X, Dinv, F);
-  svd3_rv_fast(F, U, S, V);
-  material_pk1(m, F, U, V, P);
-  // dt f directly (the force scaled by dt * vol instead of vol)
-  element_force(P, Dinv, velocityTerm ? dt * vol : vol, f);
-
   HT Hr[45];
-  reduced_hessian<HT>(m, U, S, V, Dinv, Hr);
+  if (KC == kElemSvdFree) {
+    float U[9], S[3], V[9];
+    svd3_rv_f32(F, U, S, V);
+    material_pk1_of_F(m, F, P);
+    // dt f directly (the force scaled by dt * vol instead of vol)
+    element_force(P, Dinv, velocityTerm ? dt * vol : vol, f);
+    reduced_hessian<HT, float>(m, U, S, V, Dinv, Hr);
+  } else {
+    double U[9], S[3], V[9];
+    svd3_rv_fast(F, U, S, V);
+    material_pk1(m, F, U, V, P);
+    element_force(P, Dinv, velocityTerm ? dt * vol : vol, f);
+    reduced_hessian<HT, double>(m, U, S, V, Dinv, Hr);
+  }
 
   double* g = b.elemG + 12 * (size_t)t;
   if (!velocityTerm) {
@@ -588,14 +605,15 @@ __global__ void k_energy(DeviceBatch b) {
 void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces) {
   if (b.nt == 0) return;
   const int nt = b.elemThreads;
-  k_element<double><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, rawForces, b.elemH);
+  k_element<double, kElemAll><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, rawForces, b.elemH);
   if (b.anyAniso) k_element_aniso<double><<<(b.nt + 127) / 128, 128, 0, s>>>(b, rawForces, b.elemH);
 }
 
 void launch_element_mixed(const DeviceBatch& b, cudaStream_t s) {
   if (b.nt == 0) return;
   const int nt = b.elemThreads;
-  k_element<float><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, 0, b.elemHf);
+  if (b.anySvdFree) k_element<float, kElemSvdFree><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, 0, b.elemHf);
+  if (b.anyArap) k_element<float, kElemArap><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, 0, b.elemHf);
   if (b.anyAniso) k_element_aniso<float><<<(b.nt + 127) / 128, 128, 0, s>>>(b, 0, b.elemHf);
 }
 

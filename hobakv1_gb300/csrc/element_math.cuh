@@ -234,6 +234,113 @@ __device__ __forceinline__ void svd3_rv_fast(const double* F, double* U, double*
   svd3_finish(A, U, S, V);
 }
 
+// The rotation-variant SVD in FP32 alone (stage 1 of svd3_rv_fast, then the
+// svd3_finish steps in FP32): for the mixed-precision path of the energies
+// whose stress needs no SVD (SNH, STVK, LINEAR, NEO_HOOKEAN_BW,
+// SNH_WITH_BARRIER: their PK1 is a function of F), where the factors only
+// feed the FP32 eigen-clamped Hessian.  The same svd_rv convention: S sorted
+// by magnitude, U and V rotations, a reflection carried by the sign of S[2].
+__device__ __forceinline__ void svd3_rv_f32(const double* F, float* U, float* S, float* V) {
+  float a[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    a[k] = float(F[k]);
+    V[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+  }
+  for (int sweep = 0; sweep < 10; sweep++) {
+    bool rotated = false;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const int p = (r == 2) ? 1 : 0;
+      const int q = (r == 0) ? 1 : 2;
+      const float al = a[3 * p] * a[3 * p] + a[3 * p + 1] * a[3 * p + 1] + a[3 * p + 2] * a[3 * p + 2];
+      const float be = a[3 * q] * a[3 * q] + a[3 * q + 1] * a[3 * q + 1] + a[3 * q + 2] * a[3 * q + 2];
+      const float ga = a[3 * p] * a[3 * q] + a[3 * p + 1] * a[3 * q + 1] + a[3 * p + 2] * a[3 * q + 2];
+      if (fabsf(ga) > 3e-7f * sqrtf(al * be)) {
+        rotated = true;
+        const float zeta = (be - al) / (2.0f * ga);
+        const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+        const float c = rsqrtf(1.0f + t * t), s = c * t;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const float x = a[3 * p + i], y = a[3 * q + i];
+          a[3 * p + i] = c * x - s * y;
+          a[3 * q + i] = s * x + c * y;
+          const float vx = V[3 * p + i], vy = V[3 * q + i];
+          V[3 * p + i] = c * vx - s * vy;
+          V[3 * q + i] = s * vx + c * vy;
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  // sort columns by norm, descending
+  float n[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) n[k] = a[3 * k] * a[3 * k] + a[3 * k + 1] * a[3 * k + 1] + a[3 * k + 2] * a[3 * k + 2];
+  auto swapcols = [&](int x, int y) {
+    float tn = n[x];
+    n[x] = n[y];
+    n[y] = tn;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      float t = a[3 * x + i];
+      a[3 * x + i] = a[3 * y + i];
+      a[3 * y + i] = t;
+      t = V[3 * x + i];
+      V[3 * x + i] = V[3 * y + i];
+      V[3 * y + i] = t;
+    }
+  };
+  if (n[0] < n[1]) swapcols(0, 1);
+  if (n[0] < n[2]) swapcols(0, 2);
+  if (n[1] < n[2]) swapcols(1, 2);
+  float rs[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    rs[k] = n[k] > 0.0f ? rsqrtf(n[k]) : 0.0f;
+    S[k] = n[k] * rs[k];
+  }
+  const float tiny = 1e-30f;
+  if (S[0] > tiny) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) U[i] = a[i] * rs[0];
+  } else {
+    U[0] = 1.0f; U[1] = 0.0f; U[2] = 0.0f;
+  }
+  if (S[1] > tiny) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) U[3 + i] = a[3 + i] * rs[1];
+  } else {
+    const float ax = fabsf(U[0]), ay = fabsf(U[1]), az = fabsf(U[2]);
+    float e0 = 0, e1 = 0, e2 = 0;
+    if (ax <= ay && ax <= az) e0 = 1; else if (ay <= az) e1 = 1; else e2 = 1;
+    const float w0 = U[1] * e2 - U[2] * e1, w1 = U[2] * e0 - U[0] * e2, w2 = U[0] * e1 - U[1] * e0;
+    const float rn = rsqrtf(w0 * w0 + w1 * w1 + w2 * w2);
+    U[3] = w0 * rn; U[4] = w1 * rn; U[5] = w2 * rn;
+  }
+  if (S[2] > tiny && S[1] > tiny) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) U[6 + i] = a[6 + i] * rs[2];
+  } else {
+    U[6] = U[1] * U[5] - U[2] * U[4];
+    U[7] = U[2] * U[3] - U[0] * U[5];
+    U[8] = U[0] * U[4] - U[1] * U[3];
+  }
+  auto det = [](const float* A) {
+    return A[0] * (A[4] * A[8] - A[7] * A[5]) - A[3] * (A[1] * A[8] - A[7] * A[2]) +
+           A[6] * (A[1] * A[5] - A[4] * A[2]);
+  };
+  if (det(U) < 0.0f) {
+    U[6] = -U[6]; U[7] = -U[7]; U[8] = -U[8];
+    S[2] = -S[2];
+  }
+  if (det(V) < 0.0f) {
+    V[6] = -V[6]; V[7] = -V[7]; V[8] = -V[8];
+    S[2] = -S[2];
+  }
+}
+
 // Symmetric 3x3 eigensystem by cyclic Jacobi: A = Q diag(L) Q^T.
 template <typename T>
 __device__ __forceinline__ void eig3sym(const T* Ain, T* Q, T* L) {
@@ -375,8 +482,26 @@ __device__ inline double material_psi(const MatParams& m, const double* F, const
 
 // PK1(F): SNH.cpp:45-50, ARAP.cpp:48-55 (P = R 2mu (S - I) = 2mu (F - U V^T)),
 // STVK.cpp PK1, LINEAR.cpp PK1, NEO_HOOKEAN_BW.cpp PK1, SNH_WITH_BARRIER.cpp PK1.
+__device__ inline void material_pk1_of_F(const MatParams& m, const double* F, double* P);
+
 __device__ inline void material_pk1(const MatParams& m, const double* F, const double* U, const double* V,
                                     double* P) {
+  if (m.kind == MAT_ARAP) {
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const double R = U[i] * V[j] + U[i + 3] * V[j + 3] + U[i + 6] * V[j + 6];
+        P[i + 3 * j] = 2.0 * m.mu * (F[i + 3 * j] - R);
+      }
+    return;
+  }
+  material_pk1_of_F(m, F, P);
+}
+
+// PK1 of the energies whose stress is a function of F alone (every isotropic
+// energy but ARAP).
+__device__ inline void material_pk1_of_F(const MatParams& m, const double* F, double* P) {
   switch (m.kind) {
     case MAT_SNH: {
       double G[9];
@@ -384,16 +509,6 @@ __device__ inline void material_pk1(const MatParams& m, const double* F, const d
       const double s = m.lambda * (det3(F) - m.alpha);
 #pragma unroll
       for (int k = 0; k < 9; k++) P[k] = m.mu * F[k] + s * G[k];
-      return;
-    }
-    case MAT_ARAP: {
-#pragma unroll
-      for (int j = 0; j < 3; j++)
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-          const double R = U[i] * V[j] + U[i + 3] * V[j + 3] + U[i + 6] * V[j + 6];
-          P[i + 3 * j] = 2.0 * m.mu * (F[i + 3 * j] - R);
-        }
       return;
     }
     case MAT_STVK: {
@@ -455,8 +570,8 @@ __device__ inline void material_pk1(const MatParams& m, const double* F, const d
 // coordinate axes (ARAP, MATRIX_UTIL.cpp:465-497 "jackpot" version).
 // SNH.cpp:94-144, ARAP.cpp:113-135, STVK.cpp buildEigensystem,
 // NEO_HOOKEAN_BW.cpp clampedHessian, SNH_WITH_BARRIER.cpp clampedHessian.
-template <typename T>
-__device__ inline bool material_eigensystem(const MatParams& mp, const double* Sd, T* L, T* A) {
+template <typename T, typename IT = double>
+__device__ inline bool material_eigensystem(const MatParams& mp, const IT* Sd, T* L, T* A) {
   const T mu = T(mp.mu), lambda = T(mp.lambda);
   const T s0 = T(Sd[0]), s1 = T(Sd[1]), s2 = T(Sd[2]);
   switch (mp.kind) {

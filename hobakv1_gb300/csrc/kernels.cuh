@@ -132,6 +132,7 @@ struct DeviceBatch {
   double* partial;      // [ntiles][kPartials]
   double* psi;          // [T] energy density scratch
   int anyAniso;          // some scene has an anisotropic energy (k_element_aniso)
+  int anyArap, anySvdFree;  // some scene has ARAP / another isotropic energy (mixed element kernels)
   int anyGreen;          // some Newmark scene has GREEN_DAMPING (k_green_damping)
   // vertex-face collisions (collOn = 0: none in this batch)
   int collOn;
@@ -166,7 +167,9 @@ void launch_element_mixed(const DeviceBatch& b, cudaStream_t s);
 void launch_green_damping(const DeviceBatch& b, cudaStream_t s);
 // element-phase kernel launches of a batch: k_element, plus k_element_aniso
 // and k_green_damping where the batch needs them
-inline int element_launches(const DeviceBatch& b) { return 1 + (b.anyAniso ? 1 : 0); }
+inline int element_launches(const DeviceBatch& b, bool mixed) {
+  return (mixed ? (b.anyArap ? 1 : 0) + (b.anySvdFree ? 1 : 0) : 1) + (b.anyAniso ? 1 : 0);
+}
 // K blocks (column major, un-masked, no mass) and R = sum of element forces, for inspection
 void launch_assemble_raw(const DeviceBatch& b, double* K, double* R, cudaStream_t s);
 template <typename T>
