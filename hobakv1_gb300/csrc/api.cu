@@ -532,6 +532,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oVtxptr = A.reserve(sizeof(int) * (nv + 1)), oVtxinc = A.reserve(sizeof(int) * 4 * (size_t)nt);
   const size_t oSliceRow = A.reserve(sizeof(int) * (nslices + 1)), oSlotSlice = A.reserve(sizeof(int) * nslotRows);
   const size_t oColS = A.reserve(sizeof(int) * kSlice * (size_t)nslotRows);
+  const size_t oGather = A.reserve(sizeof(int) * kSlice * (size_t)nslotRows);
 
   const size_t oTileS = A.reserve(sizeof(int) * ntilesCap), oTile0 = A.reserve(sizeof(int) * ntilesCap);
   const size_t oTile1 = A.reserve(sizeof(int) * ntilesCap);
@@ -594,6 +595,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.sliceRow = carve<int>(base, oSliceRow);
   d.slotSlice = carve<int>(base, oSlotSlice);
   d.colS = carve<int>(base, oColS);
+  d.clusterGather = carve<int>(base, oGather);
   d.nslotRows = nslotRows;
   d.tileScene = carve<int>(base, oTileS);
   d.tileV0 = carve<int>(base, oTile0);
@@ -774,6 +776,11 @@ int prepare_cluster_classes(hobak_batch_t* B) {
     CUDA_TRY(cudaMemcpy(B->clusterList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(const_cast<SceneParams*>(B->d.scenes), B->sceneParams.data(), sizeof(SceneParams) * n,
                       cudaMemcpyHostToDevice));
+  if (!list.empty()) {
+    launch_cluster_gather(B->d, B->stream);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(B->stream));
+  }
   if (changed) drop_graphs(B);
   B->clusterDirty = false;
   return HOBAK_OK;

@@ -34,14 +34,17 @@ namespace {
 
 __device__ __forceinline__ bool finite_d(double x) { return x == x && fabs(x) <= DBL_MAX; }
 
-// Shared memory of one CTA: [slots: 8 doubles][warp partials: 3 * kClusterWarps T]
-// [u, p, s, w, d, r: 3 * vpc T each].
-constexpr int kSlotBytes = 8 * sizeof(double) + 3 * kClusterWarps * sizeof(double);
+// Shared memory of one CTA:
+//   [slots: 8 doubles][warp partials: 3 * kClusterWarps doubles][ubase: 16 u32]
+//   [u: 4 * vpc T (x, y, z, 0 per vertex: one vector load per gather)]
+//   [p, s, w, d, r: 3 * vpc T each]
+constexpr int kSlotBytes = 8 * sizeof(double) + 3 * kClusterWarps * sizeof(double) + 16 * sizeof(uint32_t);
 
 template <typename T>
 struct ClusterSmem {
-  double* slots;  // [1] |r|^2, [2] (r, u), [3] delta (a barrier separates reuse)
-  T* warp;        // 3 * kClusterWarps
+  double* slots;     // [1..3] the loop's reductions, [4..6] the initial one (cluster_sum3)
+  T* warp;           // 3 * kClusterWarps warp partials
+  uint32_t* ubase;   // shared::cluster address of u in every CTA of the cluster
   T *u, *p, *s, *w, *d, *r;
 };
 
@@ -50,61 +53,56 @@ __device__ __forceinline__ ClusterSmem<T> carve_smem(unsigned char* base, int vp
   ClusterSmem<T> m;
   m.slots = reinterpret_cast<double*>(base);
   m.warp = reinterpret_cast<T*>(base + 8 * sizeof(double));
+  m.ubase = reinterpret_cast<uint32_t*>(base + 8 * sizeof(double) + 3 * kClusterWarps * sizeof(double));
   T* v = reinterpret_cast<T*>(base + kSlotBytes);
   const int n = 3 * vpc;
   m.u = v;
-  m.p = v + n;
-  m.s = v + 2 * n;
-  m.w = v + 3 * n;
-  m.d = v + 4 * n;
-  m.r = v + 5 * n;
+  m.p = v + 4 * vpc;
+  m.s = m.p + n;
+  m.w = m.s + n;
+  m.d = m.w + n;
+  m.r = m.d + n;
   return m;
 }
 
-// Sum over the CTA in T (fixed tree), written by thread 0 into this CTA's
-// slots as FP64, then a cluster barrier; thread 0 then adds the CL CTAs'
-// slots in rank order (sa, sb are valid in thread 0 only).  The scalar
-// recurrences that follow run in thread 0 alone and reach the other threads
-// through shared memory: 1024 threads redoing FP64 divisions would occupy
-// GB300's 2-lane FP64 pipe for tens of microseconds per iteration.
-template <int CL, typename T>
-__device__ __forceinline__ void cluster_sum2(cg::cluster_group& cluster, const ClusterSmem<T>& m, T a, T b,
-                                             int slot, double& sa, double& sb) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
-  }
-  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
-  if (lane == 0) {
-    m.warp[wid] = a;
-    m.warp[kClusterWarps + wid] = b;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    T ta = T(0), tb = T(0);
-#pragma unroll
-    for (int i = 0; i < kClusterWarps; i++) {
-      ta += m.warp[i];
-      tb += m.warp[kClusterWarps + i];
-    }
-    m.slots[slot] = double(ta);
-    m.slots[slot + 1] = double(tb);
-  }
-  cluster.sync();
-  sa = 0.0;
-  sb = 0.0;
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int rnk = 0; rnk < CL; rnk++) {
-      const double* rs = cluster.map_shared_rank(m.slots, rnk);
-      sa += rs[slot];
-      sb += rs[slot + 1];
-    }
-  }
+// The u of a vertex in any CTA of the cluster, by its shared::cluster address
+// (mapa of the owner's u plus the local offset): one vector load.
+__device__ __forceinline__ void ld_u(uint32_t a, float* x) {
+  float pad;
+  asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(x[0]), "=f"(x[1]), "=f"(x[2]), "=f"(pad)
+               : "r"(a));
+}
+__device__ __forceinline__ void ld_u(uint32_t a, double* x) {
+  double pad;
+  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(x[0]), "=d"(x[1]) : "r"(a));
+  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(x[2]), "=d"(pad) : "r"(a + 16));
+}
+__device__ __forceinline__ uint32_t map_cluster(const void* p, int rank) {
+  uint32_t out;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+               : "=r"(out)
+               : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(rank));
+  return out;
+}
+__device__ __forceinline__ double ld_cluster_f64(uint32_t a) {
+  double x;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(x) : "r"(a));
+  return x;
 }
 
-// Three sums as cluster_sum2 (slots slot .. slot + 2).
+// Three sums over the cluster: a warp tree, the CTA's warps summed by a tree
+// in warp 0 (in T, widened to FP64 once), a cluster barrier, then lanes
+// 0..CL-1 of warp 0 read the CL CTA sums through distributed shared memory
+// and a warp tree adds them.  Every tree is fixed, so results are
+// reproducible and independent of other scenes.  The sums are valid in warp 0
+// of every CTA (all its lanes).  The scalar recurrences that follow run in one
+// thread per CTA: 1024 threads redoing FP64 divisions would occupy GB300's
+// 2-lane FP64 pipe for tens of microseconds per iteration.
+// slot: the first of the three slots the CTA sums go to.  The loop's
+// reductions use slots 1..3 (the previous one's remote reads end before the
+// cluster barrier that closes its iteration); the initial one uses 4..6, so
+// no CTA overwrites a slot another may not have read yet.
 template <int CL, typename T>
 __device__ __forceinline__ void cluster_sum3(cg::cluster_group& cluster, const ClusterSmem<T>& m, T a, T b, T c,
                                              int slot, double (&out)[3]) {
@@ -116,33 +114,44 @@ __device__ __forceinline__ void cluster_sum3(cg::cluster_group& cluster, const C
   }
   const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (lane == 0) {
-    m.warp[wid] = a;
-    m.warp[kClusterWarps + wid] = b;
-    m.warp[2 * kClusterWarps + wid] = c;
+    m.warp[3 * wid] = a;
+    m.warp[3 * wid + 1] = b;
+    m.warp[3 * wid + 2] = c;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    T ta = T(0), tb = T(0), tc = T(0);
+  if (wid == 0) {
+    T ta = m.warp[3 * lane], tb = m.warp[3 * lane + 1], tc = m.warp[3 * lane + 2];
 #pragma unroll
-    for (int i = 0; i < kClusterWarps; i++) {
-      ta += m.warp[i];
-      tb += m.warp[kClusterWarps + i];
-      tc += m.warp[2 * kClusterWarps + i];
+    for (int o = 16; o > 0; o >>= 1) {
+      ta += __shfl_xor_sync(0xffffffffu, ta, o);
+      tb += __shfl_xor_sync(0xffffffffu, tb, o);
+      tc += __shfl_xor_sync(0xffffffffu, tc, o);
     }
-    m.slots[slot] = double(ta);
-    m.slots[slot + 1] = double(tb);
-    m.slots[slot + 2] = double(tc);
+    if (lane == 0) {
+      m.slots[slot] = double(ta);
+      m.slots[slot + 1] = double(tb);
+      m.slots[slot + 2] = double(tc);
+    }
   }
   cluster.sync();
   out[0] = out[1] = out[2] = 0.0;
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int rnk = 0; rnk < CL; rnk++) {
-      const double* rs = cluster.map_shared_rank(m.slots, rnk);
-      out[0] += rs[slot];
-      out[1] += rs[slot + 1];
-      out[2] += rs[slot + 2];
+  if (wid == 0) {
+    double sa = 0.0, sb = 0.0, sc = 0.0;
+    if (lane < CL) {
+      const uint32_t sl = map_cluster(m.slots + slot, lane);
+      sa = ld_cluster_f64(sl);
+      sb = ld_cluster_f64(sl + 8);
+      sc = ld_cluster_f64(sl + 16);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sa += __shfl_xor_sync(0xffffffffu, sa, o);
+      sb += __shfl_xor_sync(0xffffffffu, sb, o);
+      sc += __shfl_xor_sync(0xffffffffu, sc, o);
+    }
+    out[0] = sa;
+    out[1] = sb;
+    out[2] = sc;
   }
 }
 
@@ -153,9 +162,31 @@ struct Broadcast {
   int stop;
 };
 
+// Owner CTA and local vertex index of every slot's column for the scenes
+// solved in clusters (gather[slot] = owner << 20 | local index; the owner is
+// the CTA whose range [owner * vpc, (owner + 1) * vpc) holds the column), in
+// the sliced layout of colS.  Built when the cluster assignment changes.
+__global__ void k_cluster_gather(DeviceBatch b, int* __restrict__ gather) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)b.nslotRows * kSlice) return;
+  const int u = b.slotSlice[i / kSlice] * kSlice + (int)(i % kSlice);
+  int g = 0;
+  if (u < b.nv) {
+    const SceneParams& sp = b.scenes[b.vertexScene[u]];
+    if (sp.pcgCluster > 0) {
+      const int vpc = (sp.nv + sp.pcgCluster - 1) / sp.pcgCluster;
+      const int w = b.colS[i] - sp.v0;
+      const int owner = w / vpc;
+      g = (owner << 20) | (w - owner * vpc);
+    }
+  }
+  gather[i] = g;
+}
+
 template <int CL, typename T>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
-    k_pcg_cluster(DeviceBatch b, PcgVecs<T> v, const int* __restrict__ sceneList) {
+    k_pcg_cluster(DeviceBatch b, PcgVecs<T> v, const int* __restrict__ sceneList,
+                  const int* __restrict__ gather) {
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const int sc = sceneList[blockIdx.x / CL];
@@ -172,10 +203,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
   __shared__ Broadcast<T> bc;
   const int v0 = sp.v0, nvS = sp.nv;
   const int vpc = (nvS + CL - 1) / CL;  // the scene's own split: alone == in any batch
-  const float rvpc = 1.0f / float(vpc);
   const ClusterSmem<T> m = carve_smem<T>(smem, vpc);
   const int my0 = min(nvS, rank * vpc), my1 = min(nvS, (rank + 1) * vpc);
   const int nmine = my1 - my0;
+  constexpr int kUShift = sizeof(T) == 4 ? 4 : 5;  // bytes of one u entry: 16 (float4) or 32
+  if (threadIdx.x < CL) m.ubase[threadIdx.x] = map_cluster(m.u, threadIdx.x);
 
   // ---- init: r = rhs - A y (FP64, converted), u = Minv r, d = p = s = 0 ----
   const double rsc = (sizeof(T) != sizeof(double) && st.rScale > 0.0) ? st.rScale : 1.0;
@@ -197,12 +229,14 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
-      m.u[3 * lv + i] = ui;
+      m.u[4 * lv + i] = ui;
       ru += r3[i] * ui;
     }
+    m.u[4 * lv + 3] = T(0);
   }
-  double srr, sru;
-  cluster_sum2<CL, T>(cluster, m, rr, ru, 1, srr, sru);
+  double sums[3];
+  cluster_sum3<CL, T>(cluster, m, rr, ru, T(0), 4, sums);
+  double srr = sums[0];
   // the scene's scalar state, kept by thread 0 of every CTA (identical copies)
   double innerThr = 0.0, gamma = 0.0, gammaOld = 1.0, alpha = 1.0, beta = 0.0;
   int maxit = 0, totalIters = 0, iters = 0, converged = 0, outerDone = 0;
@@ -213,7 +247,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
     maxit = st.maxit;
     totalIters = st.totalIters;
     converged = st.converged;
-    gamma = sru;
+    gamma = sums[1];
     bc.stop = (srr == 0.0 || srr < innerThr) ? 1 : 0;
   }
   __syncthreads();
@@ -223,35 +257,33 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
     for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
       const int u = v0 + my0 + lv;
       T a0 = T(0), a1 = T(0), a2 = T(0);
-      const int k0 = b.rowptr[u], k1 = b.rowptr[u + 1];
-      // four blocks per trip, their column indices fetched one trip ahead;
-      // the owning CTA of a column from a float reciprocal (corrected by one
-      // step) instead of an integer division
-      int wn[4];
+      const int len = b.rowptr[u + 1] - b.rowptr[u];
+      const size_t srow = (size_t)b.sliceRow[u >> 5];
+      // the row's sliced 3x3 blocks (entry e of block j at (j * 288 + 32 e))
+      // and gather entries (j * 32), four blocks per trip with the next
+      // trip's gather entries fetched one trip ahead
+      const T* B = v.lhs + srow * kSlotVals + (u & (kSlice - 1));
+      const int* G = gather + srow * kSlice + (u & (kSlice - 1));
+      int gn[4];
 #pragma unroll
-      for (int q = 0; q < 4; q++) wn[q] = (k0 + q < k1) ? __ldg(&b.cols[k0 + q]) - v0 : 0;
-      for (int k = k0; k < k1; k += 4) {
-        int wl[4];
+      for (int q = 0; q < 4; q++) gn[q] = q < len ? __ldg(G + q * kSlice) : 0;
+      for (int j = 0; j < len; j += 4) {
+        int gq[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-          wl[q] = wn[q];
-          wn[q] = (k + 4 + q < k1) ? __ldg(&b.cols[k + 4 + q]) - v0 : 0;
+          gq[q] = gn[q];
+          gn[q] = (j + 4 + q < len) ? __ldg(G + (j + 4 + q) * kSlice) : 0;
         }
         T x[4][3];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-          int owner = min(CL - 1, (int)(float(wl[q]) * rvpc));
-          if (owner * vpc > wl[q]) owner--;
-          else if ((owner + 1) * vpc <= wl[q]) owner++;
-          const T* uw = (owner == rank ? m.u : cluster.map_shared_rank(m.u, owner)) + 3 * (wl[q] - owner * vpc);
-#pragma unroll
-          for (int i = 0; i < 3; i++) x[q][i] = (k + q < k1) ? uw[i] : T(0);
+          const uint32_t a = m.ubase[gq[q] >> 20] + ((uint32_t)(gq[q] & 0xFFFFF) << kUShift);
+          ld_u(a, x[q]);
         }
-        const T* B = v.lhs + lhs_slot(b, u, k - k0);  // sliced 3x3 blocks, entry e at kSlice * e
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-          if (k + q < k1) {
-            const T* Bq = B + (size_t)kSlotVals * q;
+          if (j + q < len) {
+            const T* Bq = B + (size_t)kSlotVals * (j + q);
             a0 = fma(Bq[0], x[q][0], fma(Bq[kSlice], x[q][1], fma(Bq[2 * kSlice], x[q][2], a0)));
             a1 = fma(Bq[3 * kSlice], x[q][0], fma(Bq[4 * kSlice], x[q][1], fma(Bq[5 * kSlice], x[q][2], a1)));
             a2 = fma(Bq[6 * kSlice], x[q][0], fma(Bq[7 * kSlice], x[q][1], fma(Bq[8 * kSlice], x[q][2], a2)));
@@ -261,13 +293,12 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
       m.w[3 * lv] = a0;
       m.w[3 * lv + 1] = a1;
       m.w[3 * lv + 2] = a2;
-      const T u0 = m.u[3 * lv], u1 = m.u[3 * lv + 1], u2 = m.u[3 * lv + 2];
+      const T u0 = m.u[4 * lv], u1 = m.u[4 * lv + 1], u2 = m.u[4 * lv + 2];
       const T r0 = m.r[3 * lv], r1 = m.r[3 * lv + 1], r2 = m.r[3 * lv + 2];
       dl += a0 * u0 + a1 * u1 + a2 * u2;
       gl += r0 * u0 + r1 * u1 + r2 * u2;
       rl += r0 * r0 + r1 * r1 + r2 * r2;
     }
-    double sums[3];
     cluster_sum3<CL, T>(cluster, m, rl, gl, dl, 1, sums);
     if (t0) {
       // after an update: the convergence test on its residual, then the
@@ -313,7 +344,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
 #pragma unroll
       for (int i = 0; i < 3; i++) {
         const int j = 3 * lv + i;
-        const T p = m.u[j] + tb * m.p[j];
+        const T p = m.u[4 * lv + i] + tb * m.p[j];
         const T sv = m.w[j] + tb * m.s[j];
         m.p[j] = p;
         m.s[j] = sv;
@@ -323,7 +354,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
       }
       const T* M = v.minv + 9 * (size_t)u;
 #pragma unroll
-      for (int i = 0; i < 3; i++) m.u[3 * lv + i] = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
+      for (int i = 0; i < 3; i++) m.u[4 * lv + i] = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
     }
     // the new u reaches the other CTAs' SpMV
     cluster.sync();
@@ -361,8 +392,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
 template <int CL, typename T>
 int launch_class(const DeviceBatch& b, const PcgVecs<T>& v, const ClusterClass& c, cudaStream_t s) {
   if (c.count == 0) return 0;
-  const size_t smem = kSlotBytes + (size_t)18 * c.vpcMax * sizeof(T);
-  k_pcg_cluster<CL, T><<<c.count * CL, kClusterThreads, smem, s>>>(b, v, c.scenes);
+  const size_t smem = kSlotBytes + cluster_vertex_bytes(sizeof(T) == 4) * c.vpcMax;
+  k_pcg_cluster<CL, T><<<c.count * CL, kClusterThreads, smem, s>>>(b, v, c.scenes, b.clusterGather);
   return 0;
 }
 
@@ -398,7 +429,14 @@ int configure_cluster_pcg() {
   return 0;
 }
 
-size_t cluster_vertex_bytes(bool mixed) { return (size_t)18 * (mixed ? sizeof(float) : sizeof(double)); }
+// u (4 wide) and p, s, w, d, r (3 wide) per vertex
+size_t cluster_vertex_bytes(bool mixed) { return (size_t)19 * (mixed ? sizeof(float) : sizeof(double)); }
+
+void launch_cluster_gather(const DeviceBatch& b, cudaStream_t s) {
+  const size_t n = (size_t)b.nslotRows * kSlice;
+  if (n == 0) return;
+  k_cluster_gather<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, b.clusterGather);
+}
 size_t cluster_fixed_bytes() { return kSlotBytes; }
 
 template <typename T>

@@ -100,6 +100,9 @@ struct DeviceBatch {
   const int* slotSlice;
   const int* colS;
   int nslotRows;
+  // cluster-resident PCG: per slot, the owner CTA and local index of its
+  // column (k_cluster_gather; scenes on the tile path: unused)
+  int* clusterGather;
   // clamped Hessian at zero displacement, CSR block order, 3x3 column major
   // (the position integrator's Rayleigh damping; null when unused)
   const double* K0;
@@ -230,6 +233,8 @@ void launch_element_eval(int nt, const int4* tets, const double* rest, const dou
 template <typename T>
 int launch_cluster_pcg(const DeviceBatch& b, const PcgVecs<T>& v, const ClusterClass* classes, int k,
                        cudaStream_t s);
+// Rebuilds the cluster kernels' gather table from the scenes' cluster sizes.
+void launch_cluster_gather(const DeviceBatch& b, cudaStream_t s);
 // Dynamic shared-memory opt-in of the cluster kernels (once, outside capture).
 int configure_cluster_pcg();
 // Shared memory a cluster CTA needs: fixed part + per-vertex part.
