@@ -18,6 +18,17 @@ keeps every admitted job's state resident on the GPU until it finishes:
 cohort of small fast scenes never waits for a cohort of large ones.
 `tick()` is the lock-step variant (all cohorts step, all are waited for).
 
+Merging (on by default): once a cohort's finished jobs hold at least
+`merge_fraction` of its jobs, or jobs are queued, the cohort is re-packed
+into a new batch of its running jobs plus the queued arrivals that fit the
+budget, built in the background while the old one keeps stepping.  At the
+old cohort's next step boundary the running jobs' state (displacement,
+velocity; acceleration for NEWMARK) is copied into the new batch, the old
+batch is freed, and the arrivals start stepping beside the jobs already
+running.  A job's trajectory carries no other state between steps, so its
+result is bitwise the same as run alone, whichever cohorts it passed
+through; finished jobs stop holding device memory.
+
 Within a cohort every scene keeps its own reduction tiles, so a job's result
 does not depend on which other jobs shared its batch or the device.
 
@@ -75,19 +86,27 @@ class Job:
 
 
 class Cohort:
+    """One batch of jobs.  Built on the builder thread; it takes ownership of
+    its jobs (attach) only when it joins the running set on the server's
+    thread, so a re-pack can be built while the jobs still step elsewhere."""
+
     def __init__(self, jobs: List[Job], opts, tuning: Optional[dict] = None):
         self.jobs = jobs
         self.batch = hobak.BATCH([j.scene for j in jobs], opts)
         if tuning:
             self.batch.set_tuning(**tuning)
         for k, j in enumerate(jobs):
-            j.cohort, j.slot = self, k
             if j.collisions is not None:
                 eps, mu, beta = j.collisions
                 self.batch.set_collisions(k, True, eps, mu, beta)
         self.bytes = self.batch.device_bytes()
         self.running = len(jobs)
         self.t_launch = None  # perf_counter() of the step in flight (pump mode)
+        self.replacement = None  # (future or Cohort, reserved bytes): its re-pack being built
+
+    def attach(self):
+        for k, j in enumerate(self.jobs):
+            j.cohort, j.slot = self, k
 
     def close(self):
         self.batch.close()
@@ -98,9 +117,16 @@ class Server:
 
     def __init__(self, budget_bytes: int, precision: int = hobak.PRECISION_MIXED,
                  max_admit_per_tick: int = 64, keep_results: bool = True, async_build: bool = False,
-                 tuning: Optional[dict] = None):
+                 tuning: Optional[dict] = None, merge: bool = True, merge_fraction: float = 0.5,
+                 max_cohort: int = 64):
         self.budget = int(budget_bytes)
         self.opts = hobak.solver_opts(precision=precision)
+        self.merge = merge
+        self.merge_fraction = merge_fraction
+        self.max_cohort = max_cohort
+        self.merges = 0  # re-packs swapped in
+        self.merged_arrivals = 0  # queued jobs that joined through a re-pack
+        self.used_history: List[tuple] = []  # (perf_counter, bytes in use) after each round
         self.tuning = tuning  # launch shapes for every cohort (hobak_batch_set_tuning)
         self.max_admit = max_admit_per_tick
         self.keep_results = keep_results
@@ -130,8 +156,76 @@ class Server:
         now = time.perf_counter()
         for j in c.jobs:
             j.admitted = now
+        c.attach()
         self.used += c.bytes - reserved
         self.cohorts.append(c)
+
+    def _build(self, jobs: List[Job]):
+        """A cohort built now, or a future of one built on the builder thread."""
+        if self._pool is None:
+            return Cohort(jobs, self.opts, self.tuning)
+        return self._pool.submit(Cohort, jobs, self.opts, self.tuning)
+
+    def _plan_merges(self):
+        """Start re-packing cohorts whose finished jobs hold memory (or when
+        arrivals wait): their running jobs plus the queued jobs that fit the
+        budget, which counts the old cohort until the swap frees it."""
+        if not self.merge:
+            return
+        for c in self.cohorts:
+            if c.replacement is not None or c.running == 0:
+                continue
+            parked = len(c.jobs) - c.running
+            if parked == 0:
+                continue
+            keep = [j for j in c.jobs if j.finished < 0]
+            est_keep = sum(footprint_bytes(j.scene, self.opts.precision) for j in keep)
+            take: List[Job] = []
+            est = 0
+            while self.queue and len(keep) + len(take) < self.max_cohort:
+                need = footprint_bytes(self.queue[0].scene, self.opts.precision)
+                if self.used + est_keep + est + need > self.budget:
+                    break
+                est += need
+                take.append(self.queue.popleft())
+            if parked < self.merge_fraction * len(c.jobs) and not take:
+                continue
+            if self.used + est_keep + est > self.budget:
+                self.queue.extendleft(reversed(take))  # no room for both batches at once yet
+                continue
+            self.used += est_keep + est
+            c.replacement = (self._build(keep + take), est_keep + est)
+
+    def _swap_ready(self, c: Cohort) -> Optional[Cohort]:
+        """At c's step boundary: its re-pack, if built, with the running jobs'
+        state copied in; c is freed.  None while the build is still running."""
+        if c.replacement is None or c.t_launch is not None:
+            return None
+        built, reserved = c.replacement
+        if isinstance(built, concurrent.futures.Future):
+            if not built.done():
+                return None
+            built = built.result()
+        newmark = self.opts.integrator == hobak.INTEGRATOR_NEWMARK
+        now = time.perf_counter()
+        for k, j in enumerate(built.jobs):
+            if j.cohort is c:  # carried over: continue from where it is
+                x, v = c.batch.get_state(j.slot)
+                built.batch.set_state(k, x, v)
+                if newmark:
+                    built.batch.set_acceleration(k, c.batch.get_acceleration(j.slot))
+                if j.finished >= 0:  # finished while the re-pack was built
+                    built.batch.set_active(k, False)
+                    built.running -= 1
+            else:  # a merged arrival
+                j.admitted = now
+                self.merged_arrivals += 1
+        built.attach()
+        self.used += built.bytes - reserved - c.bytes
+        c.close()
+        self.cohorts[self.cohorts.index(c)] = built
+        self.merges += 1
+        return built
 
     def _collect_built(self, block: bool = False):
         keep = []
@@ -145,6 +239,9 @@ class Server:
     def _admit(self):
         if self._pool is not None:
             self._collect_built(block=not self.cohorts)  # nothing running: wait for the build
+        # arrivals join running cohorts that have finished jobs first (a
+        # re-pack), the rest form a new cohort
+        self._plan_merges()
         take: List[Job] = []
         est = 0
         while self.queue and len(take) < self.max_admit:
@@ -183,9 +280,29 @@ class Server:
 
     def _retire(self):
         for c in [c for c in self.cohorts if c.running == 0 and c.t_launch is None]:
+            if c.replacement is not None:
+                # every carried job finished first: keep the re-pack for its arrivals, if any
+                nxt = self._finish_replacement(c)
+                if nxt is not None:
+                    continue
             self.used -= c.bytes
             c.close()
             self.cohorts.remove(c)
+        self.used_history.append((time.perf_counter(), self.used))
+
+    def _finish_replacement(self, c: Cohort) -> Optional[Cohort]:
+        """c has no running jobs left but its re-pack is being built: wait for
+        it and swap it in when it holds arrivals, else drop it."""
+        built, reserved = c.replacement
+        if isinstance(built, concurrent.futures.Future):
+            built = built.result()
+        c.replacement = (built, reserved)
+        if any(j.cohort is not c for j in built.jobs):
+            return self._swap_ready(c)
+        built.close()
+        self.used -= reserved
+        c.replacement = None
+        return None
 
     def tick(self) -> int:
         """One lock-step scheduling round: every running cohort advances one
@@ -205,6 +322,9 @@ class Server:
         now = time.perf_counter()
         done = sum(self._step_done(c, ms, now) for c in live)
         self._retire()
+        self._plan_merges()
+        for c in list(self.cohorts):
+            self._swap_ready(c)
         return done
 
     def pump(self) -> int:
@@ -226,10 +346,13 @@ class Server:
                 self.tick_ms.append(ms)
                 self.ticks += 1
                 done += self._step_done(c, ms, now)
+            if c.running > 0 and c.replacement is not None:
+                c = self._swap_ready(c) or c
             if c.running > 0:
                 c.batch.step_async(1)
                 c.t_launch = time.perf_counter()
         self._retire()
+        self._plan_merges()
         return done
 
     def drain(self, max_ticks: int = 1_000_000):
@@ -240,7 +363,11 @@ class Server:
     def close(self):
         if self._pool is not None:
             self._collect_built(block=True)
-            self._pool.shutdown()
         for c in self.cohorts:
+            if c.replacement is not None:
+                built = c.replacement[0]
+                (built.result() if isinstance(built, concurrent.futures.Future) else built).close()
             c.close()
+        if self._pool is not None:
+            self._pool.shutdown()
         self.cohorts.clear()

@@ -84,3 +84,53 @@ def test_event_driven_pump_matches_alone():
         assert j.done_steps == j.nsteps and len(j.step_ms) == j.nsteps
         x, v = alone(j, hobak.PRECISION_MIXED)
         assert np.array_equal(j.result_x, x) and np.array_equal(j.result_v, v), j.id
+
+
+@pytest.mark.parametrize("mode", ["tick", "pump"])
+def test_arrivals_merge_into_a_running_cohort_and_results_equal_alone(mode):
+    """Arrivals queued while a cohort has a finished (parked) job are merged
+    into it: the cohort is re-packed with its running jobs plus the arrivals
+    and swapped in at a step boundary.  Every result, of the jobs carried
+    across the re-pack and of the merged arrivals, is bitwise the same as the
+    job run alone."""
+    js = jobs()
+    a, b, c, d, e = js[2], js[3], js[0], js[1], js[5]  # 3, 11, 7, 9 (contact) and 6 steps
+    srv = Server(budget_bytes=1 << 34, precision=hobak.PRECISION_MIXED, merge_fraction=1.0,
+                 async_build=(mode == "pump"))
+    step = srv.tick if mode == "tick" else srv.pump
+    for j in (a, b, c):
+        srv.submit(j)
+    while a.finished < 0:
+        step()
+    assert srv.merges == 0  # nothing queued: merge_fraction 1 keeps the cohort as it is
+    srv.submit(d)
+    srv.submit(e)
+    while not srv.idle():
+        step()
+    srv.close()
+    assert srv.merges >= 1 and srv.merged_arrivals == 2
+    assert d.admitted > a.finished and e.admitted > a.finished
+    for j in (a, b, c, d, e):
+        assert j.done_steps == j.nsteps
+        x, v = alone(j, hobak.PRECISION_MIXED)
+        assert np.array_equal(j.result_x, x) and np.array_equal(j.result_v, v), j.id
+
+
+def test_finished_jobs_release_their_memory():
+    """With no arrivals, a cohort half of whose jobs finished is re-packed
+    without them: device memory in use falls, and the remaining job's result
+    is unchanged (bitwise equal to running it alone)."""
+    js = jobs()
+    short, longer = js[2], js[3]  # 3 and 11 steps
+    srv = Server(budget_bytes=1 << 34, precision=hobak.PRECISION_FP64, merge_fraction=0.5)
+    srv.submit(short)
+    srv.submit(longer)
+    srv.tick()
+    before = srv.used
+    while short.finished < 0:
+        srv.tick()
+    assert srv.merges == 1
+    assert srv.used < before
+    srv.drain()
+    x, v = alone(longer, hobak.PRECISION_FP64)
+    assert np.array_equal(longer.result_x, x) and np.array_equal(longer.result_v, v)
