@@ -383,7 +383,8 @@ class BACKWARD_EULER_VELOCITY {
 // GPU drop-in for BACKWARD_EULER_POSITION (Rayleigh damped,
 // BACKWARD_EULER_POSITION.cpp:138-330): the same host-state semantics; the
 // unknown of the solve is the position update, and C = alpha M + beta K at
-// rest.  Vertex-face contact is not available with this integrator.
+// rest.  Vertex-face and edge-edge contact as in the reference
+// (BACKWARD_EULER_POSITION.cpp:187-208).
 class BACKWARD_EULER_POSITION : public BACKWARD_EULER_VELOCITY {
  public:
   BACKWARD_EULER_POSITION(TET_MESH& tetMesh, VOLUME::HYPERELASTIC& hyperelastic)
@@ -404,8 +405,8 @@ class BACKWARD_EULER_POSITION : public BACKWARD_EULER_VELOCITY {
 
 // GPU drop-in for NEWMARK (Rayleigh-damped solve, NEWMARK.cpp:183-340): a
 // Newton loop of at most maxNewtonIterations() solves on the device;
-// acceleration() is host state like position() and velocity().  Vertex-face
-// contact is not available with this integrator.
+// acceleration() is host state like position() and velocity().  Contact is
+// detected and answered at every Newton iterate (NEWMARK.cpp:226-242).
 class NEWMARK : public BACKWARD_EULER_VELOCITY {
  public:
   NEWMARK(TET_MESH& tetMesh, VOLUME::HYPERELASTIC& hyperelastic) : BACKWARD_EULER_VELOCITY(tetMesh, hyperelastic) {

@@ -706,13 +706,14 @@ long long solve_launches(const hobak_batch_t* B) {
 // the update + test.
 long long newton_body_launches(const hobak_batch_t* B) {
   return 3 + element_launches(B->d, B->opts.precision == HOBAK_PRECISION_MIXED) + (B->d.anyGreen ? 1 : 0) +
-         solve_launches(B) + 2;
+         (B->d.collOn ? collision_launches(B->d.coll) : 0) + solve_launches(B) + 2;
 }
 
 long long fixed_launches(const hobak_batch_t* B) {
   // begin, Newton begin, finish (+ the Newton loop's arming kernel in a graph)
   if (B->opts.integrator == HOBAK_INTEGRATOR_NEWMARK) return 3 + (B->opts.use_graph ? 1 : 0);
-  return 5 + element_launches(B->d, B->opts.precision == HOBAK_PRECISION_MIXED) + solve_launches(B);
+  return 5 + element_launches(B->d, B->opts.precision == HOBAK_PRECISION_MIXED) +
+         (B->d.collOn ? collision_launches(B->d.coll) : 0) + solve_launches(B);
 }
 
 void drop_graphs(hobak_batch_t* B);
@@ -935,7 +936,10 @@ int enqueue_newton_body(hobak_batch_t* B, cudaStream_t s, bool capture, const Pc
   if (sizeof(T) == sizeof(float)) launch_element_mixed(d, s);
   else launch_element(d, s);
   launch_green_damping(d, s);
+  // contact at the iterate (NEWMARK.cpp:226-242)
+  if (d.collOn) launch_collisions(d, d.coll, s);
   launch_assemble<T>(d, v, s);
+  if (d.collOn) launch_collision_diag(d, d.coll, s);
   launch_diag_inverse<T>(d, v, B->opts.preconditioner, s);
   launch_rhs(d, s);
   if (int rc = enqueue_solve_t<T>(B, s, capture, v)) return rc;
@@ -1288,6 +1292,8 @@ int run_steps(hobak_batch_t* B, int nsteps) {
   cudaStream_t s = B->stream;
   const bool timed = B->timing;
   if (int rc = prepare_cluster_classes(B)) return rc;
+  // cleared once per call: an overflow in any step or Newton iteration is reported
+  if (B->d.collOn) CUDA_TRY(cudaMemsetAsync(B->d.coll.overflow, 0, sizeof(int), s));
   for (int k = 0; k < nsteps; k++) {
     if (B->opts.use_graph) {
       int rc = ensure_step_graph(B, timed);
@@ -1302,7 +1308,8 @@ int run_steps(hobak_batch_t* B, int nsteps) {
     B->phaseLaunches[0] += 1 + elaunch;
     B->phaseLaunches[1] += 2;
     B->phaseLaunches[2] += 1;
-    B->phaseLaunches[3] += fixed_launches(B) - 5 - elaunch;
+    B->phaseLaunches[3] += fixed_launches(B) - 5 - elaunch - (B->d.collOn ? collision_launches(B->d.coll) : 0);
+    if (B->d.collOn) B->phaseLaunches[0] += collision_launches(B->d.coll);
     B->phaseLaunches[4] += 1;
     if (timed) {
       CUDA_TRY(cudaEventSynchronize(B->ev[5]));
@@ -1724,9 +1731,6 @@ int hobak_batch_set_solver(hobak_batch b, const hobak_solver_opts* opts) {
   if (!b || !opts) return fail(HOBAK_ERR_INVALID, "bad arguments");
   int rc = check_opts(opts);
   if (rc) return rc;
-  if (opts->integrator == HOBAK_INTEGRATOR_NEWMARK)
-    for (const CollisionScene& cs : b->collScenes)
-      if (cs.vfOn || cs.eeOn) return fail(HOBAK_ERR_INVALID, "self collisions are not available with NEWMARK");
   b->opts = *opts;
   b->clusterDirty = true;
   drop_graphs(b);
@@ -1745,8 +1749,6 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
                                double damping_beta) {
   if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
   if (vf_on && !(eps > 0.0)) return fail(HOBAK_ERR_INVALID, "collision distance must be > 0");
-  if (vf_on && b->opts.integrator == HOBAK_INTEGRATOR_NEWMARK)
-    return fail(HOBAK_ERR_INVALID, "vertex-face contact is not available with NEWMARK");
   if (!b->collArena) {
     int rc = build_collisions(b);
     if (rc) return rc;
@@ -1768,8 +1770,6 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
 
 int hobak_batch_set_edge_collisions(hobak_batch b, int scene, int ee_on) {
   if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
-  if (ee_on && b->opts.integrator == HOBAK_INTEGRATOR_NEWMARK)
-    return fail(HOBAK_ERR_INVALID, "self collisions are not available with NEWMARK");
   if (!b->collArena) {
     int rc = build_collisions(b);
     if (rc) return rc;

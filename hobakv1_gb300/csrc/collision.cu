@@ -28,6 +28,7 @@
 #include <cfloat>
 
 #include "collision.cuh"
+#include <algorithm>
 #include "kernels.cuh"
 
 namespace hobak {
@@ -46,6 +47,21 @@ __device__ __forceinline__ D3 cross(D3 a, D3 b) {
 }
 __device__ __forceinline__ double norm(D3 a) { return sqrt(dot(a, a)); }
 __device__ __forceinline__ D3 unit(D3 a) { return (1.0 / norm(a)) * a; }
+
+// NEWMARK: beta G sum_b c_b (a3 (x_b - x_old_b) + a4 v_old_b + a5 a_old_b),
+// the pair's share of C times the Newmark velocity term (C = beta H_coll,
+// NEWMARK.cpp:244-255; G is the pair's 3x3 factor of H_coll, column major).
+__device__ __forceinline__ void newmark_coll_term(const DeviceBatch& b, int s, const int* id, const double* cvec,
+                                                  const double* G, double beta, double* out) {
+  const double* nm = b.scenes[s].nm;
+  double z[3] = {0.0, 0.0, 0.0};
+  for (int q = 0; q < 4; q++)
+    for (int k = 0; k < 3; k++) {
+      const size_t i = 3 * (size_t)id[q] + k;
+      z[k] += cvec[q] * (nm[3] * (b.x[i] - b.xOld[i]) + nm[4] * b.vOld[i] + nm[5] * b.aOld[i]);
+    }
+  for (int r = 0; r < 3; r++) out[r] = beta * (G[r] * z[0] + G[r + 3] * z[1] + G[r + 6] * z[2]);
+}
 
 __device__ __forceinline__ D3 pos(const DeviceBatch& b, int v) {
   return {b.rest[3 * v] + b.x[3 * v], b.rest[3 * v + 1] + b.x[3 * v + 1], b.rest[3 * v + 2] + b.x[3 * v + 2]};
@@ -378,12 +394,18 @@ __global__ void k_vf_pairs(DeviceBatch b, DeviceCollisions c) {
     const double tv[3] = {t.x, t.y, t.z};
     // right-hand side: dt (f + dt H v) for the velocity integrator; the
     // position integrator's b takes the force alone (collisionC and K stay
-    // out of it, BACKWARD_EULER_POSITION.cpp:196-203)
-    const bool position = b.scenes[s].integrator == kIntegratorPosition;
+    // out of it, BACKWARD_EULER_POSITION.cpp:196-203); NEWMARK's b subtracts
+    // f + beta H (a3 (x - x_old) + a4 v_old + a5 a_old) (C = beta H_coll,
+    // NEWMARK.cpp:244-255)
+    const int integ = b.scenes[s].integrator;
+    double Gn[3] = {0.0, 0.0, 0.0};
+    if (integ == kIntegratorNewmark) newmark_coll_term(b, s, id, cvec, G, cs.beta, Gn);
     for (int a = 0; a < 4; a++)
       for (int k = 0; k < 3; k++) {
         Fo[3 * a + k] = fs * cvec[a] * tv[k];
-        R[3 * a + k] = position ? fs * cvec[a] * tv[k] : dt * (fs * cvec[a] * tv[k] + dt * cvec[a] * Gz[k]);
+        R[3 * a + k] = integ == kIntegratorPosition ? fs * cvec[a] * tv[k]
+                       : integ == kIntegratorNewmark ? fs * cvec[a] * tv[k] + cvec[a] * Gn[k]
+                                                     : dt * (fs * cvec[a] * tv[k] + dt * cvec[a] * Gz[k]);
       }
   }
 }
@@ -741,12 +763,16 @@ __global__ void k_ee_pairs(DeviceBatch b, DeviceCollisions c) {
   double Gz[3];
   for (int i = 0; i < 3; i++) Gz[i] = G[i] * zv[0] + G[i + 3] * zv[1] + G[i + 6] * zv[2];
   const double dt = b.scenes[s].dt;
-  const bool position = b.scenes[s].integrator == kIntegratorPosition;
+  const int integ = b.scenes[s].integrator;
+  double Gn[3] = {0.0, 0.0, 0.0};
+  if (integ == kIntegratorNewmark) newmark_coll_term(b, s, id, cvec, G, c.scenes[s].beta, Gn);
   const double fs = gs * spring;
   for (int a = 0; a < 4; a++)
     for (int k = 0; k < 3; k++) {
       Fo[3 * a + k] = fs * cvec[a] * n3[k];
-      R[3 * a + k] = position ? Fo[3 * a + k] : dt * (Fo[3 * a + k] + dt * cvec[a] * Gz[k]);
+      R[3 * a + k] = integ == kIntegratorPosition ? Fo[3 * a + k]
+                     : integ == kIntegratorNewmark ? Fo[3 * a + k] + cvec[a] * Gn[k]
+                                                   : dt * (Fo[3 * a + k] + dt * cvec[a] * Gz[k]);
     }
 }
 
@@ -756,14 +782,44 @@ __global__ void k_add_total(const int* src, int* dst) {
 
 }  // namespace
 
+// Clears the detection's counters and tables (one kernel, so the detection
+// can sit inside a conditional graph body: NEWMARK's Newton loop).  The
+// overflow flag is not cleared here: it is cleared once per hobak_batch_step
+// call, so an overflow in any step or Newton iteration is reported.
+__global__ void k_coll_reset(DeviceCollisions c) {
+  const int n = max(max(c.nv + 1, c.hashSize + 1), max(c.eeHashSize + 1, c.nscenes));
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (i < c.nscenes) {
+      c.cellBits[i] = 0u;
+      if (c.nedge > 0) c.eeCellBits[i] = 0u;
+    }
+    if (i < c.nv) {
+      c.vInverted[i] = 0;
+      c.incCursor[i] = 0;
+    }
+    if (i <= c.nv) c.incCount[i] = 0;
+    if (i < c.hashSize) c.bucketCursor[i] = 0;
+    if (i <= c.hashSize) c.bucketCount[i] = 0;
+    if (c.nedge > 0) {
+      if (i < c.eeHashSize) c.eeBucketCursor[i] = 0;
+      if (i <= c.eeHashSize) c.eeBucketCount[i] = 0;
+    }
+  }
+}
+
+int collision_launches(const DeviceCollisions& c) {
+  // reset, inverted, triangles (prepare, 2 bucket passes, scan), vertex
+  // query, scan, total, pairs; edges (prepare, 2 bucket passes, scan,
+  // detect, scan, pairs, total); incidences (count, scan, fill, sort); the
+  // diagonal blocks
+  return 1 + 1 + (1 + 2 + 3) + 1 + 3 + 1 + 1 + (c.nedge > 0 ? 1 + 2 + 3 + 1 + 3 + 1 + 1 : 0) + (1 + 3 + 1 + 1) + 1;
+}
+
 void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStream_t s) {
-  cudaMemsetAsync(c.cellBits, 0, sizeof(unsigned) * c.nscenes, s);
-  cudaMemsetAsync(c.vInverted, 0, c.nv, s);
-  cudaMemsetAsync(c.bucketCount, 0, sizeof(int) * (c.hashSize + 1), s);
-  cudaMemsetAsync(c.bucketCursor, 0, sizeof(int) * c.hashSize, s);
-  cudaMemsetAsync(c.incCount, 0, sizeof(int) * (c.nv + 1), s);
-  cudaMemsetAsync(c.incCursor, 0, sizeof(int) * c.nv, s);
-  cudaMemsetAsync(c.overflow, 0, sizeof(int), s);
+  {
+    const int n = std::max(std::max(c.nv + 1, c.hashSize + 1), std::max(c.eeHashSize + 1, c.nscenes));
+    k_coll_reset<<<std::min((n + 255) / 256, 152 * 8), 256, 0, s>>>(c);
+  }
   k_mark_inverted<<<(b.nt + 255) / 256, 256, 0, s>>>(b, c);
   k_tri_prepare<<<(c.ntri + 255) / 256, 256, 0, s>>>(b, c);
   k_tri_bucket<false><<<(c.ntri + 255) / 256, 256, 0, s>>>(b, c);
@@ -774,9 +830,6 @@ void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStre
   k_copy_total<<<1, 32, 0, s>>>(c.svCount + c.nsv, c.npairs);
   k_vf_pairs<<<(c.nsv + 127) / 128, 128, 0, s>>>(b, c);
   if (c.nedge > 0) {  // edge-edge pairs follow the vertex-face ones (TIMESTEPPER.cpp:665-690)
-    cudaMemsetAsync(c.eeCellBits, 0, sizeof(unsigned) * c.nscenes, s);
-    cudaMemsetAsync(c.eeBucketCount, 0, sizeof(int) * (c.eeHashSize + 1), s);
-    cudaMemsetAsync(c.eeBucketCursor, 0, sizeof(int) * c.eeHashSize, s);
     k_edge_prepare<<<(c.nedge + 255) / 256, 256, 0, s>>>(b, c);
     k_edge_bucket<false><<<(c.nedge + 255) / 256, 256, 0, s>>>(b, c);
     scan_counts(c.eeBucketCount, c.eeHashSize, c.scanTmp, s);

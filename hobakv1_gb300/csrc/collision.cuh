@@ -83,5 +83,7 @@ void launch_collisions(const DeviceBatch& b, const DeviceCollisions& c, cudaStre
 // The vertices' own collision blocks (DeviceCollisions::diag, FP64), before
 // the preconditioner reads them.
 void launch_collision_diag(const DeviceBatch& b, const DeviceCollisions& c, cudaStream_t s);
+// kernels that launch_collisions and launch_collision_diag enqueue per detection
+int collision_launches(const DeviceCollisions& c);
 
 }  // namespace hobak

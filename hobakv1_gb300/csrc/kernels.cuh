@@ -155,10 +155,14 @@ __device__ __forceinline__ size_t col_slot(const DeviceBatch& b, int u, int j) {
 // K += H_coll and collision damping beta H_coll (TIMESTEPPER.cpp:645-720):
 // velocity integrator A = M - dt C - dt^2 K gives -(dt beta + dt^2);
 // position integrator A = M/dt^2 - (C + collisionC)/dt - K gives
-// -(beta/dt + 1) (BACKWARD_EULER_POSITION.cpp:187-208).
+// -(beta/dt + 1) (BACKWARD_EULER_POSITION.cpp:187-208); NEWMARK
+// A = a0 M - a3 C - K gives -(a3 beta + 1) (NEWMARK.cpp:257-262).
 __device__ __forceinline__ double collision_lhs_scale(const DeviceBatch& b, int s) {
   const double dt = b.scenes[s].dt, beta = b.coll.scenes[s].beta;
-  return b.scenes[s].integrator == kIntegratorPosition ? -(beta / dt + 1.0) : -(dt * beta + dt * dt);
+  const int integ = b.scenes[s].integrator;
+  return integ == kIntegratorPosition  ? -(beta / dt + 1.0)
+         : integ == kIntegratorNewmark ? -(b.scenes[s].nm[3] * beta + 1.0)
+                                       : -(dt * beta + dt * dt);
 }
 
 void launch_begin_step(const DeviceBatch& b, cudaStream_t s);

@@ -838,8 +838,9 @@ class NEWMARK(BACKWARD_EULER_VELOCITY):
     """GPU drop-in for TIMESTEPPER::NEWMARK (Rayleigh-damped solve,
     NEWMARK.cpp:183-340: a Newton loop of at most maxNewtonIterations() solves,
     beta = 1/4, gamma = 1/2).  position(), velocity() and acceleration() are
-    host state that solve() uploads and downloads.  Vertex-face contact is not
-    available with this integrator."""
+    host state that solve() uploads and downloads.  Vertex-face and edge-edge
+    contact run inside the Newton loop (NEWMARK.cpp:226-242), as in the
+    reference."""
 
     def __init__(self, tetMesh: TET_MESH, hyperelastic: HYPERELASTIC, damping=None,
                  opts: Optional[HobakSolverOpts] = None):
@@ -860,16 +861,6 @@ class NEWMARK(BACKWARD_EULER_VELOCITY):
     def setMaxNewtonIterations(self, n: int):
         self._require_unbuilt("setMaxNewtonIterations")
         self._opts.max_newton = int(n)
-
-    def setVertexFaceSelfCollisionsOn(self, on: bool):
-        if on:
-            raise ValueError("self collisions are not available with NEWMARK")
-        super().setVertexFaceSelfCollisionsOn(False)
-
-    def setEdgeEdgeSelfCollisionsOn(self, on: bool):
-        if on:
-            raise ValueError("self collisions are not available with NEWMARK")
-        super().setEdgeEdgeSelfCollisionsOn(False)
 
     def solve(self, verbose: bool = False) -> bool:
         if self._batch is None:

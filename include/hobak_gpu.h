@@ -104,7 +104,7 @@ typedef struct hobak_solver_opts {
   int use_graph;           /* capture each step as a CUDA graph (1) or launch eagerly (0) */
   int integrator;          /* HOBAK_INTEGRATOR_* (default VELOCITY) */
   double rayleigh_alpha;   /* POSITION: C = alpha M + beta K(rest) (defaults 0.01, 0.01: */
-  double rayleigh_beta;    /*   BACKWARD_EULER_POSITION.cpp:53-54); NEWMARK has no vertex-face contact */
+  double rayleigh_beta;    /*   BACKWARD_EULER_POSITION.cpp:53-54) */
   int max_newton;          /* NEWMARK: Newton iterations per step at most (default 10) */
   double newton_tolerance; /* NEWMARK: stop once |rhs|^2 <= this (default 1e-7, NEWMARK.cpp:43) */
 } hobak_solver_opts;
@@ -209,8 +209,8 @@ int hobak_batch_set_collisions(hobak_batch b, int scene, int vf_on, double eps, 
  * (TET_MESH_FASTER::computeEdgeEdgeCollisions, TET_MESH_FASTER.cpp:340-500)
  * with EDGE_SQRT_COLLISION forces and clamped Hessians, using the collision
  * distance, stiffness and damping set with hobak_batch_set_collisions (the
- * reference's defaults 0.01, 1, 0.001 when never set).  Velocity and
- * position integrators; off by default. */
+ * reference's defaults 0.01, 1, 0.001 when never set).  Every integrator
+ * (NEWMARK: at every Newton iterate, NEWMARK.cpp:226-242); off by default. */
 int hobak_batch_set_edge_collisions(hobak_batch b, int scene, int ee_on);
 /* The edge-edge pairs of the last detection as scene-local vertex quadruples
  * (edge0[0], edge0[1], edge1[0], edge1[1]), in surface edge order; *npairs

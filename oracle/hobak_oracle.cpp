@@ -1602,7 +1602,10 @@ void pcg(Sim& s, const std::vector<double>& A, const std::vector<double>& rhs, s
 // for a step whose A weighs the collision Hessian H_coll by collScale:
 // R += f_coll; the PCG adds collScale H_coll (in pair order) and its
 // diagonal blocks to the preconditioner; with collKv, also H_coll v.
-void collisionTerms(Sim& s, double collScale, std::vector<double>* collKv) {
+// vec: the vector H_coll multiplies for collKv (default: the velocity).
+void collisionTerms(Sim& s, double collScale, std::vector<double>* collKv,
+                    const std::vector<double>* vec = nullptr) {
+  const std::vector<double>& kvOf = vec ? *vec : s.v;
   const int nv = s.M.nv;
   Collisions& C = s.coll;
   C.weight.clear();
@@ -1633,7 +1636,7 @@ void collisionTerms(Sim& s, double collScale, std::vector<double>* collKv) {
         for (int i = 0; i < 3; i++)
           for (int j = 0; j < 3; j++) {
             const double h = H[(3 * a + i) + 12 * (3 * b + j)];
-            if (collKv) (*collKv)[3 * u + i] += h * s.v[3 * w + j];
+            if (collKv) (*collKv)[3 * u + i] += h * kvOf[3 * w + j];
             if (u == w && s.free[u]) s.collDiag[9 * (size_t)u + i + 3 * j] += s.collScale * h;
           }
       }
@@ -1760,13 +1763,16 @@ void stepPosition(Sim& s) {
     }
 }
 
-// One NEWMARK::solveRayleighDamped step (NEWMARK.cpp:183-340), collisions
-// off, no plane constraints (z = 0).  computeCollisionResponse receives the
-// Rayleigh C as its damping output and zeroes it (TIMESTEPPER.cpp:657) before
-// C is used, so C = 0 here.  beta = 1/4, gamma = 1/2 (NEWMARK.cpp:67-76).
-// Newton: while step < maxNewton and |rhs|^2 > eps (NEWMARK.cpp:212-318):
-//   b = M (a0 (x - x_old) - a2 a_old - a1 v_old) - R - f_ext
-//   A = a0 M - K;  LHS = S A S + (I - S), rhs = S b;  x -= y
+// One NEWMARK::solveRayleighDamped step (NEWMARK.cpp:183-340), no plane
+// constraints (z = 0).  computeCollisionResponse receives the Rayleigh C as
+// its damping output and overwrites it (TIMESTEPPER.cpp:645-720): C = 0
+// without contact, C = beta H_coll with it.  beta = 1/4, gamma = 1/2
+// (NEWMARK.cpp:67-76).  Newton: while step < maxNewton and |rhs|^2 > eps
+// (NEWMARK.cpp:212-318), detection and response at the iterate:
+//   b = M (a0 (x - x_old) - a2 a_old - a1 v_old)
+//       - C (a3 (x - x_old) + a4 v_old + a5 a_old) - R - f_ext
+//   A = a0 M - a3 C - K;  LHS = S A S + (I - S), rhs = S b;  x -= y
+// with R and K including the collision forces and Hessians.
 // then v = a3 (x - x_old) + a4 v_old + a5 a_old,
 //      a = a0 (x - x_old) - a1 v_old - a2 a_old, both filtered by S.
 void stepNewmark(Sim& s) {
@@ -1851,13 +1857,24 @@ void stepNewmark(Sim& s) {
           for (int i = 0; i < 3; i++) s.R[3 * u + i] += fd[12 * (size_t)t + 3 * a + i];
         }
     }
+    // contact: R += f_coll, K += H_coll, C = beta H_coll (A gains
+    // -(a3 beta + 1) H_coll; b gains -C times the Newmark velocity term)
+    std::vector<double> collKv;
+    if (s.coll.on || s.coll.ee) {
+      std::vector<double> vt(3 * (size_t)nv);
+      for (size_t q = 0; q < vt.size(); q++) vt[q] = al[3] * (s.x[q] - xOld[q]) + al[4] * vOld[q] + al[5] * aOld[q];
+      collisionTerms(s, -(al[3] * s.coll.beta + 1.0), &collKv, &vt);
+    } else {
+      collisionTerms(s, 0.0, nullptr);
+    }
     maxR = 0.0;
     for (int u = 0; u < nv; u++) {
       const double m = s.density * M.oneRing[u];
       for (int i = 0; i < 3; i++) {
         const size_t q = 3 * (size_t)u + i;
         const double t = m * (al[0] * (s.x[q] - xOld[q]) - al[2] * aOld[q] - al[1] * vOld[q]);
-        const double b = t - s.R[q] - s.fext[q];
+        double b = t - s.R[q] - s.fext[q];
+        if (!collKv.empty()) b -= s.coll.beta * collKv[q];
         rhs[q] = s.free[u] ? b : 0.0;
         maxR += rhs[q] * rhs[q];
       }
@@ -2059,7 +2076,7 @@ int oracle_set_green_damping(void* h, double mu) {
 int oracle_set_integrator(void* h, int integrator, double alpha, double beta) {
   Sim* s = static_cast<Sim*>(h);
   if (!s || integrator < 0 || integrator > 2) return -1;
-  if (integrator == 2 && s->coll.on) return -2;  // NEWMARK: no contact
+
   s->integrator = integrator;
   s->rayAlpha = alpha;
   s->rayBeta = beta;
@@ -2072,7 +2089,6 @@ int oracle_set_integrator(void* h, int integrator, double alpha, double beta) {
 int oracle_set_collisions(void* h, int vf_on, double eps, double mu, double beta) {
   Sim* s = static_cast<Sim*>(h);
   if (!s) return -1;
-  if (vf_on && s->integrator == 2) return -2;  // NEWMARK: no contact
   s->coll.on = (vf_on & 1) != 0;
   s->coll.ee = (vf_on & 2) != 0;  // bit 1: edge-edge collisions
   s->coll.eps = eps;

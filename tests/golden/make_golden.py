@@ -6,7 +6,7 @@ so this only runs where they are).  Inputs come from hobakv1_gb300.scenes, so
 they are regenerated bit-identically anywhere.  Usage:
 
     make -C oracle/ref REF=<reference checkout> -j8
-    python tests/golden/make_golden.py [elements] [trajectories] [aniso] [position] [newmark] [green] [collisions]
+    python tests/golden/make_golden.py [elements] [trajectories] [aniso] [position] [newmark] [green] [newmark_contact] [collisions]
 """
 from __future__ import annotations
 
@@ -125,6 +125,17 @@ def make_green_damping():
     print("green damping", s.name)
 
 
+def make_newmark_contact():
+    """NEWMARK with vertex-face contact (detection and response inside the
+    Newton loop, NEWMARK.cpp:226-242) on the two 6^3 cubes, collision distance
+    1e-3, stiffness 1e3, beta 1e-3, 40 steps."""
+    s = scenes.two_cubes_scene(6)
+    r = refrun.run(s, 40, stride=10, vf=True, coll_eps=1e-3, coll_mu=1e3, coll_beta=0.001, integrator="newmark")
+    np.savez_compressed(os.path.join(OUT, f"traj_{s.name}_newmark_vf.npz"), x=r["x"], v=r["v"], iters=r["iters"],
+                        steps=40, stride=10)
+    print("newmark contact", s.name, r["iters"].sum())
+
+
 def make_collisions():
     """Two cubes in contact: vertex-face pairs (reference AABB broad phase +
     narrow phase) at the start and along a 40-step trajectory with collisions."""
@@ -143,7 +154,8 @@ def make_collisions():
 if __name__ == "__main__":
     if not refrun.available():
         sys.exit("reference build missing: make -C oracle/ref REF=<reference checkout>")
-    which = set(sys.argv[1:]) or {"elements", "trajectories", "aniso", "position", "newmark", "green", "collisions"}
+    which = set(sys.argv[1:]) or {"elements", "trajectories", "aniso", "position", "newmark", "green",
+                                  "newmark_contact", "collisions"}
     if "elements" in which:
         make_elements()
     if "trajectories" in which:
@@ -156,5 +168,7 @@ if __name__ == "__main__":
         make_newmark_trajectories()
     if "green" in which:
         make_green_damping()
+    if "newmark_contact" in which:
+        make_newmark_contact()
     if "collisions" in which:
         make_collisions()

@@ -203,3 +203,17 @@ def test_oracle_green_damped_newmark_matches_the_reference_when_built():
             sim.step(1)
             x, _ = sim.state()
             assert np.linalg.norm(x - r["x"][k + 1]) / np.linalg.norm(r["x"][k + 1]) < 1e-12, (mu, k)
+
+
+def test_oracle_newmark_contact_matches_reference():
+    """NEWMARK with vertex-face contact inside the Newton loop (NEWMARK.cpp:
+    226-242): the restatement against the reference build's trajectory of two
+    6^3 cubes (traj_two_cubes6_snh_newmark_vf.npz)."""
+    g = np.load(os.path.join(GOLDEN, "traj_two_cubes6_snh_newmark_vf.npz"))
+    s = scenes.two_cubes_scene(6)
+    sim = oracle.Sim(s, precond=0, integrator="newmark")
+    sim.set_collisions(True, 1e-3, 1e3, 0.001)
+    for k in range(1, g["x"].shape[0]):
+        sim.step(int(g["stride"]))
+        x, _ = sim.state()
+        assert np.linalg.norm(x - g["x"][k]) / np.linalg.norm(g["x"][k]) < 1e-12, k
