@@ -198,9 +198,11 @@ __device__ __forceinline__ void deformation_gradient(const double X[4][3], const
 
 // Which tets an instantiation of k_element evaluates: every isotropic tet
 // (the FP64 path), or, in the mixed path, split by whether the stress reads
-// the SVD: ARAP's PK1 = 2 mu (F - U V^T) takes the FP64 SVD; the other
-// isotropic energies' PK1 is a function of F, so their SVD only feeds the
-// FP32 Hessian and runs in FP32 (svd3_rv_f32).
+// the SVD.  The other isotropic energies' PK1 is a function of F, so their
+// SVD only feeds the FP32 Hessian and runs in FP32 (svd3_rv_f32); ARAP's
+// PK1 = 2 mu (F - U V^T) reads the rotation in FP64, refined from the FP32
+// factors (arap_rotation_refined), or from the FP64 SVD where that
+// refinement is ill-conditioned.
 constexpr int kElemAll = 0, kElemSvdFree = 1, kElemArap = 2;
 
 // Batched step kernel: element Hessian blocks and right-hand-side terms
@@ -241,6 +243,25 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
     svd3_rv_f32(F, U, S, V);
     material_pk1_of_F(m, F, P);
     // dt f directly (the force scaled by dt * vol instead of vol)
+    element_force(P, Dinv, velocityTerm ? dt * vol : vol, f);
+    reduced_hessian<HT, float>(m, U, S, V, Dinv, Hr);
+  } else if (KC == kElemArap) {
+    // the FP32 factors feed the FP32 Hessian; the stress's rotation is
+    // refined to FP64 from them (the FP64 SVD near the twist singularity)
+    float U[9], S[3], V[9];
+    svd3_rv_f32(F, U, S, V);
+    double R[9];
+    if (!arap_rotation_refined(F, U, S, V, R)) {
+      double Ud[9], Sd[3], Vd[9];
+      svd3_rv_fast(F, Ud, Sd, Vd);
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) R[i + 3 * j] = Ud[i] * Vd[j] + Ud[i + 3] * Vd[j + 3] + Ud[i + 6] * Vd[j + 6];
+    }
+    // P = 2 mu (F - R) (ARAP.cpp:48-55)
+#pragma unroll
+    for (int k = 0; k < 9; k++) P[k] = 2.0 * m.mu * (F[k] - R[k]);
     element_force(P, Dinv, velocityTerm ? dt * vol : vol, f);
     reduced_hessian<HT, float>(m, U, S, V, Dinv, Hr);
   } else {

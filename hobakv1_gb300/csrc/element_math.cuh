@@ -341,6 +341,78 @@ __device__ __forceinline__ void svd3_rv_f32(const double* F, float* U, float* S,
   }
 }
 
+// ARAP's rotation R = U V^T (the rotation of F's polar decomposition in the
+// svd_rv convention) in FP64 from the FP32 factors of svd3_rv_f32:
+//   1. R0 = U V^T, re-orthonormalised in FP64 (Gram-Schmidt of two columns,
+//      the third their cross product, so det R0 = +1);
+//   2. one correction R = R0 Q, Q = I + W + W^2 / 2 with W = [w]x, where w
+//      solves (tr(S) I - S) w = (Y32 - Y23, Y13 - Y31, Y21 - Y12) for
+//      Y = R0^T F and S = sym(Y): the rotation that makes Q^T Y symmetric.
+// From R0 within ~1e-7 of R the result is within ~1e-14 while tr(S) I - S
+// (eigenvalues sigma_i + sigma_j) is well conditioned.  Returns false when
+// sigma_1 + sigma_2 is below 1e-2 sigma_0 (near ARAP's twist singularity, or
+// a collapsed tet): the caller then takes the FP64 SVD.
+__device__ __forceinline__ bool arap_rotation_refined(const double* F, const float* U, const float* S, const float* V,
+                                                      double* R) {
+  if (!(S[1] + S[2] > 1e-2f * S[0])) return false;
+  double c0[3], c1[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    c0[i] = double(U[i] * V[0] + U[i + 3] * V[3] + U[i + 6] * V[6]);
+    c1[i] = double(U[i] * V[1] + U[i + 3] * V[4] + U[i + 6] * V[7]);
+  }
+  const double n0 = rsqrt(c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2]);
+#pragma unroll
+  for (int i = 0; i < 3; i++) c0[i] *= n0;
+  const double d01 = c0[0] * c1[0] + c0[1] * c1[1] + c0[2] * c1[2];
+#pragma unroll
+  for (int i = 0; i < 3; i++) c1[i] -= d01 * c0[i];
+  const double n1 = rsqrt(c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2]);
+#pragma unroll
+  for (int i = 0; i < 3; i++) c1[i] *= n1;
+  double R0[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    R0[i] = c0[i];
+    R0[3 + i] = c1[i];
+  }
+  R0[6] = c0[1] * c1[2] - c0[2] * c1[1];
+  R0[7] = c0[2] * c1[0] - c0[0] * c1[2];
+  R0[8] = c0[0] * c1[1] - c0[1] * c1[0];
+  // Y = R0^T F
+  double Y[9];
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      Y[i + 3 * j] = R0[3 * i] * F[3 * j] + R0[3 * i + 1] * F[3 * j + 1] + R0[3 * i + 2] * F[3 * j + 2];
+  // K = tr(S) I - S, S = sym(Y); rhs = twice the axial vector of skew(Y)
+  const double tr = Y[0] + Y[4] + Y[8];
+  const double k00 = tr - Y[0], k11 = tr - Y[4], k22 = tr - Y[8];
+  const double k01 = -0.5 * (Y[3] + Y[1]), k02 = -0.5 * (Y[6] + Y[2]), k12 = -0.5 * (Y[7] + Y[5]);
+  const double b0 = Y[5] - Y[7], b1 = Y[6] - Y[2], b2 = Y[1] - Y[3];
+  // w = K^-1 b by cofactors (K symmetric)
+  const double a00 = k11 * k22 - k12 * k12, a01 = k02 * k12 - k01 * k22, a02 = k01 * k12 - k02 * k11;
+  const double a11 = k00 * k22 - k02 * k02, a12 = k01 * k02 - k00 * k12, a22 = k00 * k11 - k01 * k01;
+  const double det = k00 * a00 + k01 * a01 + k02 * a02;
+  const double id = 1.0 / det;
+  const double w0 = id * (a00 * b0 + a01 * b1 + a02 * b2);
+  const double w1 = id * (a01 * b0 + a11 * b1 + a12 * b2);
+  const double w2 = id * (a02 * b0 + a12 * b1 + a22 * b2);
+  // R = R0 (I + W + W^2 / 2), W^2 = w w^T - |w|^2 I
+  const double h = 1.0 - 0.5 * (w0 * w0 + w1 * w1 + w2 * w2);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const double r0 = R0[i], r1 = R0[i + 3], r2 = R0[i + 6];
+    const double rw = 0.5 * (r0 * w0 + r1 * w1 + r2 * w2);
+    // row i of R0 W: (r1 w2 - r2 w1, r2 w0 - r0 w2, r0 w1 - r1 w0)
+    R[i] = h * r0 + (r1 * w2 - r2 * w1) + rw * w0;
+    R[i + 3] = h * r1 + (r2 * w0 - r0 * w2) + rw * w1;
+    R[i + 6] = h * r2 + (r0 * w1 - r1 * w0) + rw * w2;
+  }
+  return true;
+}
+
 // Symmetric 3x3 eigensystem by cyclic Jacobi: A = Q diag(L) Q^T.
 template <typename T>
 __device__ __forceinline__ void eig3sym(const T* Ain, T* Q, T* L) {
