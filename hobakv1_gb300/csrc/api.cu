@@ -471,6 +471,24 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
     for (int t = 0; t < nt; t++)
       for (int e = 0; e < 16; e++) blksrc[fill[where[16 * (size_t)t + e]]++] = 16 * t + e;
   }
+  // element-kernel staging: per block of kStageTets consecutive tets, its
+  // distinct vertices (ascending) and each tet corner's index among them
+  const int nsb = (nt + kStageTets - 1) / kStageTets;
+  std::vector<int> stagePtr(nsb + 1, 0), stageVerts;
+  std::vector<unsigned char> stageLocal(4 * (size_t)nt);
+  {
+    std::vector<int> ids;
+    for (int sb = 0; sb < nsb; sb++) {
+      const int t0 = sb * kStageTets, t1 = std::min(nt, t0 + kStageTets);
+      ids.assign(B->tetsHost.begin() + 4 * (size_t)t0, B->tetsHost.begin() + 4 * (size_t)t1);
+      std::sort(ids.begin(), ids.end());
+      ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+      for (int k = 4 * t0; k < 4 * t1; k++)
+        stageLocal[k] = (unsigned char)(std::lower_bound(ids.begin(), ids.end(), B->tetsHost[k]) - ids.begin());
+      stageVerts.insert(stageVerts.end(), ids.begin(), ids.end());
+      stagePtr[sb + 1] = (int)stageVerts.size();
+    }
+  }
   // tiles: kTileV consecutive vertices of one scene (apply_tile_size changes
   // the size later; the tables are sized for kMinTileV)
   int ntilesCap = 0;
@@ -525,6 +543,8 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   const size_t oMass = A.reserve(sizeof(double) * nv), oFree = A.reserve(nv), oPin = A.reserve(V3);
   const size_t oVS = A.reserve(sizeof(int) * nv);
   const size_t oTets = A.reserve(sizeof(int4) * nt), oDm = A.reserve(sizeof(double) * 9 * (size_t)nt);
+  const size_t oStagePtr = A.reserve(sizeof(int) * (nsb + 1)), oStageVerts = A.reserve(sizeof(int) * stageVerts.size());
+  const size_t oStageLocal = A.reserve(4 * (size_t)nt);
   const size_t oVol = A.reserve(sizeof(double) * nt), oTS = A.reserve(sizeof(int) * nt);
   const size_t oRowptr = A.reserve(sizeof(int) * (nv + 1)), oCols = A.reserve(sizeof(int) * nblocks);
   const size_t oBlkRow = A.reserve(sizeof(int) * nblocks), oBlkptr = A.reserve(sizeof(int) * (nblocks + 1));
@@ -582,6 +602,12 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.pinTarget = carve<double>(base, oPin);
   d.vertexScene = carve<int>(base, oVS);
   d.tets = carve<int4>(base, oTets);
+  d.stagePtr = carve<int>(base, oStagePtr);
+  d.stageVerts = carve<int>(base, oStageVerts);
+  d.stageLocal = carve<uchar4>(base, oStageLocal);
+  d.stageMax = 1;
+  for (int sb = 0; sb < nsb; sb += 1)  // a 128-tet CTA stages blocks 2k and 2k + 1
+    d.stageMax = std::max(d.stageMax, stagePtr[std::min(nsb, sb + 2)] - stagePtr[sb]);
   d.DmInv = carve<double>(base, oDm);
   d.vol = carve<double>(base, oVol);
   d.tetScene = carve<int>(base, oTS);
@@ -629,6 +655,9 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   B->pinTargetHost = pinTarget;
   CUDA_TRY(up(d.vertexScene, vertexScene.data(), sizeof(int) * nv));
   CUDA_TRY(up(d.tets, B->tetsHost.data(), sizeof(int4) * nt));
+  CUDA_TRY(up(d.stagePtr, stagePtr.data(), sizeof(int) * (nsb + 1)));
+  CUDA_TRY(up(d.stageVerts, stageVerts.data(), sizeof(int) * stageVerts.size()));
+  CUDA_TRY(up(d.stageLocal, stageLocal.data(), 4 * (size_t)nt));
   CUDA_TRY(up(d.DmInv, DmInv.data(), sizeof(double) * 9 * (size_t)nt));
   CUDA_TRY(up(d.vol, vol.data(), sizeof(double) * nt));
   CUDA_TRY(up(d.tetScene, tetScene.data(), sizeof(int) * nt));

@@ -210,19 +210,53 @@ constexpr int kElemAll = 0, kElemSvdFree = 1, kElemArap = 2;
 // HT is the Hessian's arithmetic/storage type: double (FP64 path) or float
 // (mixed path: F, stress and forces stay FP64; the SVD is FP64 where the
 // stress reads it).
+// Whether an instantiation evaluates tets of a scene of this kind.
+template <int KC>
+__device__ __forceinline__ bool evaluates(int kind) {
+  if (is_anisotropic(kind)) return false;  // k_element_aniso
+  return KC == kElemAll || (KC == kElemSvdFree) == (kind != MAT_ARAP);
+}
+
 template <typename HT, int KC>
-// FP32 Hessians fit 128 registers (4 CTAs per SM, a few bytes of spill); the
-// FP64 variant needs ~208 and spills heavily below that.
+// FP32 Hessians fit 128 registers (4 CTAs per SM); the FP64 variant needs
+// ~208 and spills heavily below that.
 __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
     k_element(DeviceBatch b, int rawForces, HT* __restrict__ outH) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= b.nt) return;
+  // The CTA's tets read their corners from shared memory: the distinct
+  // vertices of its one or two staging blocks (host-built, ascending ids)
+  // are loaded once each, rest + x and v, so each vertex position is summed
+  // and fetched once per CTA instead of once per tet corner.
+  extern __shared__ double stage[];  // [n][6]: rest + x, v
+  const int tFirst = blockIdx.x * blockDim.x;
+  const int tLast = min(b.nt, tFirst + (int)blockDim.x) - 1;
+  // CTAs holding only scenes this instantiation does not evaluate (scenes
+  // are contiguous in tet order) leave before staging
+  {
+    bool any = false;
+    for (int sc = b.tetScene[tFirst]; sc <= b.tetScene[tLast] && !any; sc++) any = evaluates<KC>(b.scenes[sc].kind);
+    if (!any) return;
+  }
+  const int sb0 = tFirst / kStageTets;
+  const int s0 = b.stagePtr[sb0], s1 = b.stagePtr[tLast / kStageTets + 1];
+  for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) {
+    const int vid = b.stageVerts[s0 + i];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      stage[6 * i + k] = b.rest[3 * vid + k] + b.x[3 * vid + k];
+      stage[6 * i + 3 + k] = b.v[3 * vid + k];
+    }
+  }
+  __syncthreads();
+  const int t = tFirst + threadIdx.x;
+  if (t > tLast) return;
   const SceneParams& sp = b.scenes[b.tetScene[t]];
-  if (!sp.active || is_anisotropic(sp.kind)) return;  // anisotropic energies: k_element_aniso
-  if ((KC == kElemSvdFree && sp.kind == MAT_ARAP) || (KC == kElemArap && sp.kind != MAT_ARAP)) return;
+  if (!sp.active || !evaluates<KC>(sp.kind)) return;
   // Newmark: a scene whose Newton loop is over needs no further element terms
   if (!rawForces && sp.integrator == kIntegratorNewmark && b.solve[b.tetScene[t]].newtonDone) return;
-  const int4 tv = b.tets[t];
+  const uchar4 lc = b.stageLocal[t];
+  const int off = b.stagePtr[t / kStageTets] - s0;
+  const double* sx[4] = {stage + 6 * (off + lc.x), stage + 6 * (off + lc.y), stage + 6 * (off + lc.z),
+                         stage + 6 * (off + lc.w)};
   const MatParams m{sp.kind, sp.mu, sp.lambda, sp.alpha};
   // rhs term: dt (f + dt He v) for BACKWARD_EULER_VELOCITY; the force itself
   // for BACKWARD_EULER_POSITION (its rhs has no K v term: the Rayleigh part
@@ -234,7 +268,10 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   for (int k = 0; k < 9; k++) Dinv[k] = b.DmInv[9 * (size_t)t + k];
   const double vol = b.vol[t];
   double X[4][3];
-  load_tet(tv, b.rest, b.x, X);
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) X[a][i] = sx[a][i];
   double F[9], P[9], f[12];
   deformation_gradient(X, Dinv, F);
   HT Hr[45];
@@ -281,17 +318,11 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   }
   // He v = -vol D^T Hr (D v): D v = relative velocities of vertices 1..3
   // (in the mixed path He v is formed in FP32 like He itself)
-  const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
   HT dv[9];
-  {
-    double v0[3];
 #pragma unroll
-    for (int i = 0; i < 3; i++) v0[i] = b.v[3 * vid[0] + i];
+  for (int a = 0; a < 3; a++)
 #pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int i = 0; i < 3; i++) dv[3 * a + i] = HT(b.v[3 * vid[a + 1] + i] - v0[i]);
-  }
+    for (int i = 0; i < 3; i++) dv[3 * a + i] = HT(sx[a + 1][3 + i] - sx[0][3 + i]);
   // g = dt f + dt^2 He v: the He v rows carry the factor -vol dt^2 in HT
   // (one conversion and one add per entry on the FP64 pipe)
   const HT ch = HT(-vol * dt * dt);
@@ -623,18 +654,23 @@ __global__ void k_energy(DeviceBatch b) {
 
 // CTA size: the batch's autotuned elemThreads (64 or 128; the kernels are
 // bounded for 128).
+// dynamic shared memory of a k_element CTA: 6 doubles per staged vertex
+// (stageMax: the most distinct vertices of any pair of staging blocks)
+static size_t stage_bytes(const DeviceBatch& b) { return sizeof(double) * 6 * (size_t)b.stageMax; }
+
 void launch_element(const DeviceBatch& b, cudaStream_t s, int rawForces) {
   if (b.nt == 0) return;
   const int nt = b.elemThreads;
-  k_element<double, kElemAll><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, rawForces, b.elemH);
+  k_element<double, kElemAll><<<(b.nt + nt - 1) / nt, nt, stage_bytes(b), s>>>(b, rawForces, b.elemH);
   if (b.anyAniso) k_element_aniso<double><<<(b.nt + 127) / 128, 128, 0, s>>>(b, rawForces, b.elemH);
 }
 
 void launch_element_mixed(const DeviceBatch& b, cudaStream_t s) {
   if (b.nt == 0) return;
   const int nt = b.elemThreads;
-  if (b.anySvdFree) k_element<float, kElemSvdFree><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, 0, b.elemHf);
-  if (b.anyArap) k_element<float, kElemArap><<<(b.nt + nt - 1) / nt, nt, 0, s>>>(b, 0, b.elemHf);
+  if (b.anySvdFree)
+    k_element<float, kElemSvdFree><<<(b.nt + nt - 1) / nt, nt, stage_bytes(b), s>>>(b, 0, b.elemHf);
+  if (b.anyArap) k_element<float, kElemArap><<<(b.nt + nt - 1) / nt, nt, stage_bytes(b), s>>>(b, 0, b.elemHf);
   if (b.anyAniso) k_element_aniso<float><<<(b.nt + 127) / 128, 128, 0, s>>>(b, 0, b.elemHf);
 }
 

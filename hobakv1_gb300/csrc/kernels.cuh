@@ -20,6 +20,11 @@ struct PcgVecs {
   T* d;     // inner solution (the correction)
 };
 
+// Tets per staging block of the element kernel (a CTA of 64 or 128 threads
+// stages one or two blocks); at most 4 * kStageTets distinct vertices each,
+// so a one-byte corner index suffices.
+constexpr int kStageTets = 64;
+
 // Cluster-resident PCG (cluster_pcg.cu): scenes solved by clusters of
 // 1, 2, 4, 8 or 16 CTAs of kClusterThreads threads (one vertex per thread).
 constexpr int kClusterThreads = 1024;
@@ -81,6 +86,13 @@ struct DeviceBatch {
 
   // tets
   const int4* tets;
+  // element-kernel staging (k_element): per block of kStageTets consecutive
+  // tets, its distinct vertices (stageVerts[stagePtr[b] .. stagePtr[b + 1]),
+  // ascending) and each tet corner's index in that list
+  const int* stagePtr;
+  const int* stageVerts;
+  const uchar4* stageLocal;
+  int stageMax;  // most distinct vertices of any two consecutive staging blocks
   const double* DmInv;
   const double* vol;
   const int* tetScene;

@@ -10,10 +10,10 @@
   (job 2 of scenes.config5_jobs(32): two 26^3 SNH cubes in vertex-face
   contact, 76 steps).  Contact makes the trajectory discontinuous in the
   state: a vertex crossing the detection distance adds or drops a spring.
-  Mixed precision tracks FP64 within 1e-6 up to the impact step, where the
-  springs of many pairs engage at once; the first step past 1e-6 and the
-  first steps where the contact branches and the pair sets differ are
-  recorded here (SPLIT_STEPS) and checked."""
+  Mixed precision tracks FP64 within 1e-6 for as long as neither run's
+  contact branches or pair sets split from the other's; the first step past
+  1e-6 and the first steps where the contact branches and the pair sets
+  differ are recorded here (SPLIT_STEPS) and checked."""
 import numpy as np
 import pytest
 
@@ -22,10 +22,14 @@ from oracle import oracle
 
 pytestmark = pytest.mark.gpu
 
-# serving job 2: the first step whose mixed-vs-FP64 difference exceeds 1e-6
-# (the impact step), the first step whose contact branches (a pair's reversal
-# flag) differ, and the first step whose vertex-face pair sets differ
-SPLIT_STEPS = (21, 22, 22)
+# serving job 2: the first step whose mixed-vs-FP64 difference exceeds 1e-6,
+# the first step whose contact branches (a pair's reversal flag) differ, and
+# the first step whose vertex-face pair sets differ (None: not within the
+# job's 76 steps).  With the FP32 SVD of the SNH tets in mixed precision the
+# two runs stay within 2.4e-8 of each other through all 76 steps; a build
+# whose mixed element arithmetic differs may split at the impact step (21),
+# where 58 pairs engage at once.
+SPLIT_STEPS = (None, None, None)
 
 
 def rel(a, b):
@@ -108,7 +112,7 @@ def test_serving_contact_job_mixed_tracks_fp64_until_the_impact_step():
     for b in runs.values():
         b.close()
     at = rows[split_err - 1] if split_err else None
-    print(f"serving job 2: mixed vs FP64 <= {worst_before:.2e} through step {(split_err or nsteps + 1) - 1}; "
+    print(f"serving job 2: mixed vs FP64 <= {worst_before:.2e} through step {(split_err or len(rows) + 1) - 1}; "
           f"step {split_err}: {at[1] if at else '-'} pairs, mixed vs FP64 {at[2] if at else 0:.2e}, "
           f"FP64 tol 1e-8 vs 1e-12 {at[3] if at else 0:.2e}; contact branches split at step {split_branch}, "
           f"pair sets at step {split_pairs}")
