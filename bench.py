@@ -579,6 +579,8 @@ def run_ours(args, spec, scene_list):
     # this batch's data, before the warm-up; the state is left unchanged
     if args.no_autotune and args.cluster_pcg is not None:
         batch.set_tuning(cluster_pcg=args.cluster_pcg)
+    if args.no_autotune and args.cluster_max is not None:
+        batch.set_tuning(cluster_max=args.cluster_max)
     tuning = batch.get_tuning() if args.no_autotune else batch.autotune(reps=3)
 
     # ---- device-resident timed region ----
@@ -723,6 +725,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--cluster-pcg", type=int, choices=[0, 1], default=None,
                     help="PCG path of the serving cohorts (and of --no-autotune batches): 1 = cluster-resident")
+    ap.add_argument("--cluster-max", type=int, choices=[1, 2, 4, 8, 16], default=None,
+                    help="largest cluster of --no-autotune batches (the autotuner's choice on the default mix: 8)")
     ap.add_argument("--eager", action="store_true",
                     help="launch kernels one by one instead of the step graph (for per-kernel profilers)")
     args = ap.parse_args()
