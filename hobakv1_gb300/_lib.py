@@ -96,6 +96,7 @@ SIGNATURES = {
     "hobak_batch_kernel_bytes": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "hobak_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakTuning)]),
     "hobak_batch_pcg_path": (ctypes.c_int, [ctypes.c_void_p, _ip]),
+    "hobak_batch_set_scene_cluster": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "hobak_batch_set_green_damping": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
     "hobak_batch_get_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "hobak_batch_set_acceleration": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),

@@ -99,6 +99,7 @@ struct hobak_batch_t {
   bool clusterDirty = true;
   ClusterClass classes[kClusterClasses] = {};
   int* clusterList = nullptr;  // device, nscenes ids grouped by class
+  std::vector<int> sceneCluster;  // per scene: 0 by the tuning, > 0 a cluster size, -1 the tile path
   bool anyTileScene = true;
   cudaStream_t classStream[kClusterClasses] = {};  // classes run beside the tile path (fork/join)
   cudaEvent_t evFork = nullptr, evJoin[kClusterClasses] = {};
@@ -769,6 +770,13 @@ int prepare_cluster_classes(hobak_batch_t* B) {
         B->collArena && s < (int)B->collScenes.size() && (B->collScenes[s].vfOn || B->collScenes[s].eeOn);
     if (!B->clusterPcg || contact) continue;
     const int nv = B->scenes[s].nv;
+    const int force = s < (int)B->sceneCluster.size() ? B->sceneCluster[s] : 0;
+    if (force < 0) continue;  // this scene keeps the tile path
+    if (force > 0) {  // this scene's own cluster size, where its vectors fit
+      const int vpcF = (nv + force - 1) / force;
+      if (vpcF <= kClusterThreads || (force < 16 && vpcF <= vpcLimit)) cl[s] = force;
+      continue;
+    }
     // the smallest cluster that gives each thread one vertex at most; under
     // a cap below 16 CTAs, threads of a capped cluster take several vertices
     // as long as the CTA's vectors fit in its shared memory
@@ -2077,6 +2085,18 @@ int hobak_batch_set_green_damping(hobak_batch b, int scene, double mu) {
   if (any != b->d.anyGreen) {  // the Newton body gains or loses a kernel
     b->d.anyGreen = any;
     drop_graphs(b);
+  }
+  return HOBAK_OK;
+}
+
+int hobak_batch_set_scene_cluster(hobak_batch b, int scene, int ctas) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return fail(HOBAK_ERR_INVALID, "bad handle or scene");
+  if (!(ctas == -1 || ctas == 0 || ctas == 1 || ctas == 2 || ctas == 4 || ctas == 8 || ctas == 16))
+    return fail(HOBAK_ERR_INVALID, "ctas must be -1 (tile path), 0 (by the tuning), 1, 2, 4, 8 or 16");
+  if (b->sceneCluster.size() != b->scenes.size()) b->sceneCluster.assign(b->scenes.size(), 0);
+  if (b->sceneCluster[scene] != ctas) {
+    b->sceneCluster[scene] = ctas;
+    b->clusterDirty = true;
   }
   return HOBAK_OK;
 }

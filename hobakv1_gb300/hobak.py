@@ -574,6 +574,11 @@ class BATCH:
         check(_lib.load().hobak_batch_pcg_path(self.h, iptr(out)), "hobak_batch_pcg_path")
         return out
 
+    def set_scene_cluster(self, scene: int, ctas: int):
+        """Per-scene PCG path: a cluster of ctas CTAs (1..16), -1 the tile
+        path, 0 by the batch's tuning."""
+        check(_lib.load().hobak_batch_set_scene_cluster(self.h, scene, int(ctas)), "hobak_batch_set_scene_cluster")
+
     def blocks(self, scene: int) -> int:
         """3x3 blocks of one scene's system matrix (its BSR pattern)."""
         n = ctypes.c_int()

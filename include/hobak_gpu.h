@@ -356,6 +356,13 @@ int hobak_batch_get_tuning(hobak_batch b, hobak_tuning* out);
  * reference counterpart): cluster_ctas[s] = the CTAs of scene s's
  * thread-block cluster, or 0 for the batch-wide tile path. */
 int hobak_batch_pcg_path(hobak_batch b, int* cluster_ctas);
+/* Per-scene override of that choice (no reference counterpart): ctas = 1, 2,
+ * 4, 8 or 16 solves the scene in a cluster of that size when it fits (its
+ * vectors in the CTAs' shared memory), -1 keeps it on the tile path, 0 leaves
+ * it to the batch's tuning.  Applies from the next step; it depends only on
+ * the scene, so a scene given the same override alone and in a batch takes
+ * the same path. */
+int hobak_batch_set_scene_cluster(hobak_batch b, int scene, int ctas);
 int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t);
 /* Autotuner: times the element kernel per CTA size and the assembly kernel
  * per CTA size (reps launches each, CUDA events), then whole steps for every
