@@ -174,6 +174,52 @@ __device__ __forceinline__ void expand_blocks(const T* Hr, double vol, OutT* out
     for (int k = 0; k < 3; k++) out[3 * i + k] = OutT(nv * s00[3 * i + k]);
 }
 
+// The same 10 blocks as expand_blocks, with the same sums in the same order,
+// emitted in memory order two values per store (8-byte stores for FP32,
+// 16-byte for FP64): 45 store instructions per tet instead of 90, which
+// relieves the load/store queue the per-tet kernels saturate.  out is
+// 8-byte aligned (FP32, 360 B per tet) or 16-byte aligned (FP64, 720 B).
+template <typename T, typename OutT>
+__device__ __forceinline__ void store_blocks(const T* Hr, double vol, OutT* out) {
+  const T nv = T(-vol);
+  auto h = [&](int r, int c) -> T { return r <= c ? Hr[sym9(r, c)] : Hr[sym9(c, r)]; };
+  auto value = [&](int e) -> OutT {
+    const int ub = e / 9, i = (e % 9) / 3, k = e % 3;
+    const int A = ub < 4 ? 0 : ub < 7 ? 1 : ub < 9 ? 2 : 3;
+    const int B = ub < 4 ? ub : ub < 7 ? ub - 3 : ub < 9 ? ub - 5 : 3;
+    if (A >= 1) return OutT(nv * h(3 * (A - 1) + i, 3 * (B - 1) + k));
+    if (B >= 1) {
+      T s = T(0);
+#pragma unroll
+      for (int a = 0; a < 3; a++) s += h(3 * a + i, 3 * (B - 1) + k);
+      return OutT(-nv * s);
+    }
+    T s00 = T(0);
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+      T s = T(0);
+#pragma unroll
+      for (int a = 0; a < 3; a++) s += h(3 * a + i, 3 * b + k);
+      s00 += s;
+    }
+    return OutT(nv * s00);
+  };
+#pragma unroll
+  for (int e = 0; e < kElemHess; e += 2) {
+    if (sizeof(OutT) == 4) {
+      *reinterpret_cast<float2*>(out + e) = make_float2(float(value(e)), float(value(e + 1)));
+    } else {
+      *reinterpret_cast<double2*>(out + e) = make_double2(double(value(e)), double(value(e + 1)));
+    }
+  }
+}
+
+// 12 doubles (16-byte aligned) as six 16-byte stores
+__device__ __forceinline__ void store12(double* dst, const double* v) {
+#pragma unroll
+  for (int k = 0; k < 12; k += 2) *reinterpret_cast<double2*>(dst + k) = make_double2(v[k], v[k + 1]);
+}
+
 __device__ __forceinline__ void load_tet(const int4 tv, const double* rest, const double* x, double X[4][3]) {
   const int vid[4] = {tv.x, tv.y, tv.z, tv.w};
 #pragma unroll
@@ -311,9 +357,8 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
 
   double* g = b.elemG + 12 * (size_t)t;
   if (!velocityTerm) {
-#pragma unroll
-    for (int k = 0; k < 12; k++) g[k] = f[k];
-    expand_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
+    store12(g, f);
+    store_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
     return;
   }
   // He v = -vol D^T Hr (D v): D v = relative velocities of vertices 1..3
@@ -327,6 +372,7 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   // (one conversion and one add per entry on the FP64 pipe)
   const HT ch = HT(-vol * dt * dt);
   HT h0[3] = {HT(0), HT(0), HT(0)};
+  double gl[12];
 #pragma unroll
   for (int r = 0; r < 9; r++) {
     HT s = HT(0);
@@ -334,12 +380,12 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
     for (int c = 0; c < 9; c++) s += ((r <= c) ? Hr[sym9(r, c)] : Hr[sym9(c, r)]) * dv[c];
     s *= ch;
     h0[r % 3] += s;
-    g[3 + r] = f[3 + r] + double(s);
+    gl[3 + r] = f[3 + r] + double(s);
   }
 #pragma unroll
-  for (int i = 0; i < 3; i++) g[i] = f[i] - double(h0[i]);
-
-  expand_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
+  for (int i = 0; i < 3; i++) gl[i] = f[i] - double(h0[i]);
+  store12(g, gl);
+  store_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
 }
 
 // Element terms of the anisotropic energies (ANISOTROPIC_ARAP, STVK, FUNG,

@@ -119,15 +119,19 @@ def test_switching_integrator_matches_a_new_batch():
     assert np.array_equal(xb, xc) and np.array_equal(vb, vc)
 
 
-def test_contact_is_refused_for_newmark_only():
+def test_contact_switches_between_integrators():
+    """Contact is available with every integrator: a contact batch can switch
+    from the position integrator to NEWMARK and keep stepping."""
     two = scenes.two_cubes_scene(4)
     b = hobak.BATCH([two], hobak.solver_opts(integrator=hobak.INTEGRATOR_NEWMARK))
-    with pytest.raises(_lib.HobakError):
-        b.set_collisions(0, True, 1e-3, 1e3, 0.001)
+    b.set_collisions(0, True, 1e-3, 1e3, 0.001)
+    b.step(2)
     c = hobak.BATCH([two], hobak.solver_opts(integrator=POS))
     c.set_collisions(0, True, 1e-3, 1e3, 0.001)
-    with pytest.raises(_lib.HobakError):
-        c.set_solver(hobak.solver_opts(integrator=hobak.INTEGRATOR_NEWMARK))
+    c.step(1)
+    c.set_solver(hobak.solver_opts(integrator=hobak.INTEGRATOR_NEWMARK))
+    st = c.step(2)
+    assert st[0][1] == 1
 
 
 @pytest.mark.parametrize("precision,bound", [(hobak.PRECISION_FP64, 1e-8), (hobak.PRECISION_MIXED, 1e-6)],
