@@ -31,7 +31,8 @@ class HobakSolverOpts(ctypes.Structure):
                 ("preconditioner", ctypes.c_int), ("max_refinements", ctypes.c_int),
                 ("use_graph", ctypes.c_int), ("integrator", ctypes.c_int),
                 ("rayleigh_alpha", ctypes.c_double), ("rayleigh_beta", ctypes.c_double),
-                ("max_newton", ctypes.c_int), ("newton_tolerance", ctypes.c_double)]
+                ("max_newton", ctypes.c_int), ("newton_tolerance", ctypes.c_double),
+                ("inner_tolerance", ctypes.c_double)]
 
 
 class HobakTuning(ctypes.Structure):

@@ -688,6 +688,7 @@ int upload_solver_opts(hobak_batch_t* B) {
   for (auto& s : st) {
     std::memset(&s, 0, sizeof(s));
     s.tol = B->opts.tol;
+    s.innerFloor = B->opts.inner_tolerance;
     s.maxit = B->opts.max_iters;
     s.maxSweeps = sweeps_of(B->opts);
   }
@@ -708,6 +709,8 @@ int check_opts(const hobak_solver_opts* o) {
     return fail(HOBAK_ERR_INVALID, "unknown integrator");
   if (o->max_newton < 1 || o->max_newton > 100 || !(o->newton_tolerance >= 0.0))
     return fail(HOBAK_ERR_INVALID, "max_newton in 1..100 and newton_tolerance >= 0");
+  if (!(o->inner_tolerance >= 1e-7 && o->inner_tolerance < 1.0))
+    return fail(HOBAK_ERR_INVALID, "inner_tolerance in [1e-7, 1)");
   if (!(o->rayleigh_alpha >= 0.0) || !(o->rayleigh_beta >= 0.0) || !std::isfinite(o->rayleigh_alpha) ||
       !std::isfinite(o->rayleigh_beta))
     return fail(HOBAK_ERR_INVALID, "Rayleigh coefficients must be finite and >= 0");
@@ -1460,6 +1463,7 @@ void hobak_default_solver_opts(hobak_solver_opts* o) {
   o->rayleigh_beta = 0.01;
   o->max_newton = 10;           // NEWMARK.cpp:41
   o->newton_tolerance = 1e-7;   // NEWMARK.cpp:43
+  o->inner_tolerance = 1e-5;
 }
 
 int hobak_batch_create(const hobak_scene_desc* scenes, int nscenes, const hobak_solver_opts* opts,

@@ -242,7 +242,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
   int maxit = 0, totalIters = 0, iters = 0, converged = 0, outerDone = 0;
   if (t0) {
     double itol = st.tol;
-    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr * rsc * rsc, DBL_MIN)), 1e-5);
+    if (sizeof(T) != sizeof(double))
+      itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr * rsc * rsc, DBL_MIN)), st.innerFloor);
     innerThr = fmax(itol * itol * srr, DBL_MIN);
     maxit = st.maxit;
     totalIters = st.totalIters;

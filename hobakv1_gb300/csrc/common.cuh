@@ -72,6 +72,7 @@ struct SolveState {
   double rr64;         // |rhs - A y|^2 after the last refinement
   double rScale;       // mixed: the FP32 inner solve runs on r64 / rScale (a power of two near |r64|)
   double tol;
+  double innerFloor;   // mixed: tightest relative tolerance of an FP32 inner solve
   int outerDone;       // 1 when the step's linear solve is finished
   int sweep;           // refinement sweeps done
   int maxSweeps;       // 1 (FP64) or 1 + max_refinements (mixed)

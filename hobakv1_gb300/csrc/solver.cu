@@ -624,7 +624,8 @@ __global__ void k_set_active(DeviceBatch b) {
 
 // Start of one inner solve on r_T = (T) r64: d = 0, p = s = 0, u = Minv r,
 // gamma = (r, u), |r|^2.  Inner tolerance: the outer one for FP64; for FP32
-// the relative reduction still needed, floored at 1e-5 (FP32 stagnation).
+// the relative reduction still needed, floored at the inner tolerance
+// (default 1e-5: FP32 stagnation).
 template <int TV, typename T>
 __global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) {
   __shared__ double sh[TV / 32];
@@ -676,7 +677,7 @@ __global__ void __launch_bounds__(TV) k_inner_init(DeviceBatch b, PcgVecs<T> v) 
   const double sru = sum_partials<TV>(b.partial, sp.tile0, sp.ntiles, 1, sh);
   if (threadIdx.x == 0) {
     double itol = st.tol;
-    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr * sc * sc, DBL_MIN)), 1e-5);
+    if (sizeof(T) != sizeof(double)) itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr * sc * sc, DBL_MIN)), st.innerFloor);
     st.rr = srr;
     st.gamma = sru;
     st.gammaOld = 1.0;

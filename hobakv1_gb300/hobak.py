@@ -285,7 +285,7 @@ class TET_MESH:
 
 def solver_opts(tol=1e-8, max_iters=1000, precision=PRECISION_FP64, preconditioner=PRECOND_BLOCK_JACOBI,
                 max_refinements=3, use_graph=True, integrator=INTEGRATOR_VELOCITY,
-                rayleigh=(0.01, 0.01), max_newton=10, newton_tolerance=1e-7) -> HobakSolverOpts:
+                rayleigh=(0.01, 0.01), max_newton=10, newton_tolerance=1e-7, inner_tolerance=1e-5) -> HobakSolverOpts:
     """Solver options; integrator INTEGRATOR_VELOCITY (BACKWARD_EULER_VELOCITY),
     INTEGRATOR_POSITION (BACKWARD_EULER_POSITION, Rayleigh damped with
     alpha, beta = rayleigh) or INTEGRATOR_NEWMARK (NEWMARK, at most
@@ -296,6 +296,7 @@ def solver_opts(tol=1e-8, max_iters=1000, precision=PRECISION_FP64, precondition
     o.integrator = integrator
     o.rayleigh_alpha, o.rayleigh_beta = rayleigh
     o.max_newton, o.newton_tolerance = max_newton, newton_tolerance
+    o.inner_tolerance = inner_tolerance
     return o
 
 

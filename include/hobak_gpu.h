@@ -107,6 +107,8 @@ typedef struct hobak_solver_opts {
   double rayleigh_beta;    /*   BACKWARD_EULER_POSITION.cpp:53-54) */
   int max_newton;          /* NEWMARK: Newton iterations per step at most (default 10) */
   double newton_tolerance; /* NEWMARK: stop once |rhs|^2 <= this (default 1e-7, NEWMARK.cpp:43) */
+  double inner_tolerance;  /* MIXED: each FP32 inner solve stops at this relative residual at the
+                              tightest (default 1e-5; the FP64 test on the outer residual is unchanged) */
 } hobak_solver_opts;
 
 /* Per-scene statistics of the last step. */
