@@ -99,6 +99,8 @@ struct hobak_batch_t {
   bool clusterDirty = true;
   ClusterClass classes[kClusterClasses] = {};
   int* clusterList = nullptr;  // device, nscenes ids grouped by class
+  std::vector<int> hostClusterList;  // host copy of clusterList
+  bool clusterOrderStale = false;    // new iteration counts since the classes were last ordered
   std::vector<int> sceneCluster;  // per scene: 0 by the tuning, > 0 a cluster size, -1 the tile path
   bool anyTileScene = true;
   cudaStream_t classStream[kClusterClasses] = {};  // classes run beside the tile path (fork/join)
@@ -760,6 +762,40 @@ void drop_graphs(hobak_batch_t* B);
 // tile path, which spreads them wider.  The choice depends only on the scene itself, so
 // a scene takes the same path alone and in any batch.  Runs outside graph
 // capture (it uploads); drops the graphs when the assignment changed.
+// Longest first: within each class, the scenes that iterated most in the
+// last step (then the larger ones) come first, so that their clusters start
+// at the head of the launch and the short solves fill the SMs around them.
+// A scene's solve does not depend on where it sits in the list.
+void order_cluster_classes(const hobak_batch_t* B, std::vector<int>& list) {
+  const bool known = B->lastSolve.size() == B->scenes.size();
+  auto key = [&](int s) { return known ? B->lastSolve[s].totalIters : 0; };
+  size_t at = 0;
+  for (int k = 0; k < kClusterClasses; k++) {
+    const size_t end = at + B->classes[k].count;
+    std::stable_sort(list.begin() + at, list.begin() + end, [&](int a, int b) {
+      const int ka = key(a), kb = key(b);
+      if (ka != kb) return ka > kb;
+      return B->scenes[a].nv > B->scenes[b].nv;
+    });
+    at = end;
+  }
+}
+
+// Re-orders the classes after a step whose iteration counts were collected;
+// the graphs read the list at run time, so they stay valid.
+int reorder_cluster_classes(hobak_batch_t* B) {
+  if (!B->clusterOrderStale || B->hostClusterList.empty()) return HOBAK_OK;
+  B->clusterOrderStale = false;
+  std::vector<int> list = B->hostClusterList;
+  order_cluster_classes(B, list);
+  if (list == B->hostClusterList) return HOBAK_OK;
+  B->hostClusterList = list;
+  // from pageable memory: the call returns once the list is staged
+  CUDA_TRY(cudaMemcpyAsync(B->clusterList, B->hostClusterList.data(), sizeof(int) * list.size(),
+                           cudaMemcpyHostToDevice, B->stream));
+  return HOBAK_OK;
+}
+
 int prepare_cluster_classes(hobak_batch_t* B) {
   if (!B->clusterDirty) return HOBAK_OK;
   if (const int ce = configure_cluster_pcg())
@@ -804,6 +840,9 @@ int prepare_cluster_classes(hobak_batch_t* B) {
         c.vpcMax = std::max(c.vpcMax, (B->scenes[s].nv + sizes[k] - 1) / sizes[k]);
       }
   }
+  order_cluster_classes(B, list);
+  B->hostClusterList = list;
+  B->clusterOrderStale = false;
   for (int s = 0; s < n; s++) {
     if (B->sceneParams[s].pcgCluster != cl[s]) changed = true;
     B->sceneParams[s].pcgCluster = cl[s];
@@ -1332,6 +1371,7 @@ int run_steps(hobak_batch_t* B, int nsteps) {
   cudaStream_t s = B->stream;
   const bool timed = B->timing;
   if (int rc = prepare_cluster_classes(B)) return rc;
+  if (int rc = reorder_cluster_classes(B)) return rc;
   // cleared once per call: an overflow in any step or Newton iteration is reported
   if (B->d.collOn) CUDA_TRY(cudaMemsetAsync(B->d.coll.overflow, 0, sizeof(int), s));
   for (int k = 0; k < nsteps; k++) {
@@ -1569,6 +1609,7 @@ int hobak_batch_wait(hobak_batch b, hobak_step_stats* stats) {
   if (b->pending) {
     b->lastSolve.assign(b->solvePinned, b->solvePinned + n);
     b->pending = false;
+    b->clusterOrderStale = true;
   }
   if ((int)b->lastSolve.size() != n) return HOBAK_OK;  // nothing stepped yet
   int status = HOBAK_OK;
