@@ -730,10 +730,10 @@ long long solve_launches(const hobak_batch_t* B) {
   const bool mixed = B->opts.precision == HOBAK_PRECISION_MIXED;
   int cl = 0;
   for (const ClusterClass& c : B->classes) cl += c.count > 0 ? 1 : 0;
-  // per sweep: k_set_active, inner init (+ the loop's arming kernel in a
-  // graph), the cluster classes, the refinement
-  const int tile = B->anyTileScene ? (B->opts.use_graph ? 2 : 1) : 0;
-  return sweeps * (1 + tile + cl + (mixed ? 2 : 0));
+  // the cluster classes once; per sweep of the tile path: k_set_active,
+  // inner init (+ the loop's arming kernel in a graph), the refinement
+  if (!B->anyTileScene) return cl;
+  return cl + sweeps * (2 + (B->opts.use_graph ? 1 : 0) + (mixed ? 2 : 0));
 }
 
 // Kernels of one Newton loop body (Newmark) outside the PCG loop bodies and
@@ -753,15 +753,6 @@ long long fixed_launches(const hobak_batch_t* B) {
 
 void drop_graphs(hobak_batch_t* B);
 
-// Which scenes solve their inner PCG in a thread-block cluster, and in how
-// large a one, for the current precision: scenes without contact, in the
-// smallest cluster (1, 2, 4, 8 or 16 CTAs) that gives each thread at most one
-// vertex, or, with the cluster size capped below 16 (clusterMax), in a capped
-// cluster whose threads take several vertices while its vectors fit in shared
-// memory (fewer SMs per scene, more scenes at once); larger scenes keep the
-// tile path, which spreads them wider.  The choice depends only on the scene itself, so
-// a scene takes the same path alone and in any batch.  Runs outside graph
-// capture (it uploads); drops the graphs when the assignment changed.
 // Longest first: within each class, the scenes that iterated most in the
 // last step (then the larger ones) come first, so that their clusters start
 // at the head of the launch and the short solves fill the SMs around them.
@@ -796,6 +787,15 @@ int reorder_cluster_classes(hobak_batch_t* B) {
   return HOBAK_OK;
 }
 
+// Which scenes solve their inner PCG in a thread-block cluster, and in how
+// large a one, for the current precision: scenes without contact, in the
+// smallest cluster (1, 2, 4, 8 or 16 CTAs) that gives each thread at most one
+// vertex, or, with the cluster size capped below 16 (clusterMax), in a capped
+// cluster whose threads take several vertices while its vectors fit in shared
+// memory (fewer SMs per scene, more scenes at once); larger scenes keep the
+// tile path, which spreads them wider.  The choice depends only on the scene itself, so
+// a scene takes the same path alone and in any batch.  Runs outside graph
+// capture (it uploads); drops the graphs when the assignment changed.
 int prepare_cluster_classes(hobak_batch_t* B) {
   if (!B->clusterDirty) return HOBAK_OK;
   if (const int ce = configure_cluster_pcg())
@@ -974,35 +974,37 @@ int eager_pcg_loop(hobak_batch_t* B, cudaStream_t s, const PcgVecs<T>& v) {
   return HOBAK_OK;
 }
 
-// The linear solve of a step: per sweep an inner PCG (cluster classes on
-// their own streams beside the tile path, joined before the refinement: small
-// scenes solve while large ones iterate, and a class's long-running scenes do
-// not hold up the others) and, mixed, the FP64 refinement.
+// The linear solve of a step: the cluster classes on their own streams, each
+// launch solving its scenes to the end (mixed: every refinement sweep), beside
+// the tile path's sweeps (an inner PCG and, mixed, the FP64 refinement);
+// joined at the end.  Small scenes solve while large ones iterate, and a
+// class's long-running scenes hold up neither the other classes nor the
+// tile path's refinements.
 template <typename T>
 int enqueue_solve_t(hobak_batch_t* B, cudaStream_t s, bool capture, const PcgVecs<T>& v) {
   const DeviceBatch& d = B->d;
   const bool mixed = sizeof(T) == sizeof(float);
   const int sweeps = sweeps_of(B->opts);
-  for (int k = 0; k < sweeps; k++) {
+  // the cluster classes solve their scenes completely, every sweep included
+  // (cluster_pcg.cu), beside all of the tile path's sweeps
+  int forked = 0;
+  for (int c = kClusterClasses - 1; c >= 0; c--) {
+    if (B->classes[c].count == 0) continue;
+    if (!forked++) CUDA_TRY(cudaEventRecord(B->evFork, s));
+    CUDA_TRY(cudaStreamWaitEvent(B->classStream[c], B->evFork, 0));
+    const int ce = launch_cluster_pcg<T>(d, v, B->classes, c, B->classStream[c]);
+    if (ce) return fail(HOBAK_ERR_CUDA, std::string("cluster PCG launch: ") + cudaGetErrorString((cudaError_t)ce));
+    CUDA_TRY(cudaEventRecord(B->evJoin[c], B->classStream[c]));
+  }
+  for (int k = 0; k < sweeps && B->anyTileScene; k++) {
     launch_set_active(d, s);
-    int forked = 0;
-    for (int c = kClusterClasses - 1; c >= 0; c--) {
-      if (B->classes[c].count == 0) continue;
-      if (!forked++) CUDA_TRY(cudaEventRecord(B->evFork, s));
-      CUDA_TRY(cudaStreamWaitEvent(B->classStream[c], B->evFork, 0));
-      const int ce = launch_cluster_pcg<T>(d, v, B->classes, c, B->classStream[c]);
-      if (ce) return fail(HOBAK_ERR_CUDA, std::string("cluster PCG launch: ") + cudaGetErrorString((cudaError_t)ce));
-      CUDA_TRY(cudaEventRecord(B->evJoin[c], B->classStream[c]));
-    }
-    if (B->anyTileScene) {
-      launch_inner_init<T>(d, v, s);
-      int rc = capture ? capture_pcg_loop<T>(B, s, v) : eager_pcg_loop<T>(B, s, v);
-      if (rc) return rc;
-    }
-    for (int c = 0; c < kClusterClasses; c++)
-      if (B->classes[c].count) CUDA_TRY(cudaStreamWaitEvent(s, B->evJoin[c], 0));
+    launch_inner_init<T>(d, v, s);
+    int rc = capture ? capture_pcg_loop<T>(B, s, v) : eager_pcg_loop<T>(B, s, v);
+    if (rc) return rc;
     if (mixed) launch_refine(d, s);
   }
+  for (int c = 0; c < kClusterClasses; c++)
+    if (B->classes[c].count) CUDA_TRY(cudaStreamWaitEvent(s, B->evJoin[c], 0));
   return HOBAK_OK;
 }
 

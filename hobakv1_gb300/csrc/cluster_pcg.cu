@@ -155,11 +155,92 @@ __device__ __forceinline__ void cluster_sum3(cg::cluster_group& cluster, const C
   }
 }
 
+// One FP64 sum over the cluster (the residual's |r64|^2): the same trees as
+// cluster_sum3, on FP64 warp partials.  Valid in warp 0 of every CTA.
+template <int CL, typename T>
+__device__ __forceinline__ double cluster_sum_f64(cg::cluster_group& cluster, const ClusterSmem<T>& m, double a,
+                                                  int slot) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  double* warp = reinterpret_cast<double*>(m.warp);  // sized for 3 doubles per warp
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (lane == 0) warp[wid] = a;
+  __syncthreads();
+  if (wid == 0) {
+    double t = lane < kClusterWarps ? warp[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) m.slots[slot] = t;
+  }
+  cluster.sync();
+  double out = 0.0;
+  if (wid == 0) {
+    double sa = lane < CL ? ld_cluster_f64(map_cluster(m.slots + slot, lane)) : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sa += __shfl_xor_sync(0xffffffffu, sa, o);
+    out = sa;
+  }
+  return out;
+}
+
+// The end of a mixed-precision sweep for vertices [u0, u0 + n) of a scene:
+// y += rsc d (d from shared memory), a cluster barrier (every CTA's y is then
+// visible to the cluster: release / acquire), r64 = rhs - A y with the FP32
+// matrix entries promoted and FP64 sums in row order (as k_residual), and
+// |r64|^2 summed over the cluster, valid in warp 0.  Not inlined: its FP64
+// registers stay out of the PCG loop's allocation.
+template <int CL>
+__device__ __noinline__ double sweep_residual(cg::cluster_group& cluster, const ClusterSmem<float>& m, double* y,
+                                              double* r64, const double* rhs, const int* rowptr, const int* cols,
+                                              const int* sliceRow, const float* lhs, int u0, int n, double rsc) {
+  for (int lv = threadIdx.x; lv < n; lv += kClusterThreads) {
+    const int u = u0 + lv;
+#pragma unroll
+    for (int i = 0; i < 3; i++) y[3 * u + i] += rsc * double(m.d[3 * lv + i]);
+  }
+  cluster.sync();
+  double rl = 0.0;
+  for (int lv = threadIdx.x; lv < n; lv += kClusterThreads) {
+    const int u = u0 + lv;
+    const int k0 = rowptr[u], k1 = rowptr[u + 1];
+    const float* A = lhs + (size_t)sliceRow[u >> 5] * kSlotVals + (u & (kSlice - 1));
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int k = k0; k < k1; k++) {
+      const int w = cols[k];
+      const float* B = A + (size_t)kSlotVals * (k - k0);
+      const double y0 = y[3 * w], y1 = y[3 * w + 1], y2 = y[3 * w + 2];
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        acc[i] += double(B[3 * i * kSlice]) * y0 + double(B[(3 * i + 1) * kSlice]) * y1 +
+                  double(B[(3 * i + 2) * kSlice]) * y2;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const double ri = rhs[3 * u + i] - acc[i];
+      r64[3 * u + i] = ri;
+      rl += ri * ri;
+    }
+  }
+  return cluster_sum_f64<CL>(cluster, m, rl, 7);
+}
+template <int CL>
+__device__ double sweep_residual(cg::cluster_group&, const ClusterSmem<double>&, double*, double*, const double*,
+                                 const int*, const int*, const int*, const double*, int, int, double) {
+  return 0.0;  // FP64: one inner solve is the solve; never called
+}
+
+// The scene's PCG and sweep scalars, kept by thread 0 of each CTA.
+struct Scalars {
+  double innerThr = 0.0, gamma = 0.0, gammaOld = 1.0, alpha = 1.0, beta = 0.0, srr = 0.0;
+  int maxit = 0, totalIters = 0, iters = 0, converged = 0, outerDone = 0, sweep = 0;
+};
+
 // Values thread 0 hands to the CTA after each reduction.
 template <typename T>
 struct Broadcast {
+  double scale;  // mixed: the next sweep's residual scale
   T alpha, beta;
-  int stop;
+  int stop;      // 1: the inner solve (or the sweeps) ended; 2: non-finite, the step failed
 };
 
 // Owner CTA and local vertex index of every slot's column for the scenes
@@ -209,182 +290,234 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
   constexpr int kUShift = sizeof(T) == 4 ? 4 : 5;  // bytes of one u entry: 16 (float4) or 32
   if (threadIdx.x < CL) m.ubase[threadIdx.x] = map_cluster(m.u, threadIdx.x);
 
-  // ---- init: r = rhs - A y (FP64, converted), u = Minv r, d = p = s = 0 ----
-  const double rsc = (sizeof(T) != sizeof(double) && st.rScale > 0.0) ? st.rScale : 1.0;
-  const double inv = 1.0 / rsc;  // exact: rsc is a power of two
-  T rr = T(0), ru = T(0);
-  for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
-    const int u = v0 + my0 + lv;
-    T r3[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      r3[i] = T(b.r64[3 * u + i] * inv);
-      m.r[3 * lv + i] = r3[i];
-      m.d[3 * lv + i] = T(0);
-      m.p[3 * lv + i] = T(0);
-      m.s[3 * lv + i] = T(0);
-      rr += r3[i] * r3[i];
-    }
-    const T* M = v.minv + 9 * (size_t)u;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
-      m.u[4 * lv + i] = ui;
-      ru += r3[i] * ui;
-    }
-    m.u[4 * lv + 3] = T(0);
-  }
-  double sums[3];
-  cluster_sum3<CL, T>(cluster, m, rr, ru, T(0), 4, sums);
-  double srr = sums[0];
-  // the scene's scalar state, kept by thread 0 of every CTA (identical copies)
-  double innerThr = 0.0, gamma = 0.0, gammaOld = 1.0, alpha = 1.0, beta = 0.0;
-  int maxit = 0, totalIters = 0, iters = 0, converged = 0, outerDone = 0;
+  // The scene's scalar state, kept by thread 0 of every CTA in shared memory
+  // (identical copies, computed from the same cluster sums in the same
+  // order); registers stay with the SpMV.
+  __shared__ Scalars ss;
   if (t0) {
-    double itol = st.tol;
-    if (sizeof(T) != sizeof(double))
-      itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(srr * rsc * rsc, DBL_MIN)), st.innerFloor);
-    innerThr = fmax(itol * itol * srr, DBL_MIN);
-    maxit = st.maxit;
-    totalIters = st.totalIters;
-    converged = st.converged;
-    gamma = sums[1];
-    bc.stop = (srr == 0.0 || srr < innerThr) ? 1 : 0;
+    ss = Scalars{};
+    ss.maxit = st.maxit;
+    ss.totalIters = st.totalIters;
+    ss.converged = st.converged;
+    ss.sweep = st.sweep;
+    // mixed: the power-of-two scale of this sweep's r
+    bc.scale = (sizeof(T) != sizeof(double) && st.rScale > 0.0) ? st.rScale : 1.0;
   }
   __syncthreads();
-  while (!bc.stop) {
-    // ---- w = A u over my vertices; delta = (w, u), gamma = (r, u), |r|^2 ----
-    T dl = T(0), gl = T(0), rl = T(0);
-    for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
-      const int u = v0 + my0 + lv;
-      T a0 = T(0), a1 = T(0), a2 = T(0);
-      const int len = b.rowptr[u + 1] - b.rowptr[u];
-      const size_t srow = (size_t)b.sliceRow[u >> 5];
-      // the row's sliced 3x3 blocks (entry e of block j at (j * 288 + 32 e))
-      // and gather entries (j * 32), four blocks per trip with the next
-      // trip's gather entries fetched one trip ahead
-      const T* B = v.lhs + srow * kSlotVals + (u & (kSlice - 1));
-      const int* G = gather + srow * kSlice + (u & (kSlice - 1));
-      int gn[4];
-#pragma unroll
-      for (int q = 0; q < 4; q++) gn[q] = q < len ? __ldg(G + q * kSlice) : 0;
-      for (int j = 0; j < len; j += 4) {
-        int gq[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          gq[q] = gn[q];
-          gn[q] = (j + 4 + q < len) ? __ldg(G + (j + 4 + q) * kSlice) : 0;
-        }
-        T x[4][3];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const uint32_t a = m.ubase[gq[q] >> 20] + ((uint32_t)(gq[q] & 0xFFFFF) << kUShift);
-          ld_u(a, x[q]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (j + q < len) {
-            const T* Bq = B + (size_t)kSlotVals * (j + q);
-            a0 = fma(Bq[0], x[q][0], fma(Bq[kSlice], x[q][1], fma(Bq[2 * kSlice], x[q][2], a0)));
-            a1 = fma(Bq[3 * kSlice], x[q][0], fma(Bq[4 * kSlice], x[q][1], fma(Bq[5 * kSlice], x[q][2], a1)));
-            a2 = fma(Bq[6 * kSlice], x[q][0], fma(Bq[7 * kSlice], x[q][1], fma(Bq[8 * kSlice], x[q][2], a2)));
-          }
-        }
-      }
-      m.w[3 * lv] = a0;
-      m.w[3 * lv + 1] = a1;
-      m.w[3 * lv + 2] = a2;
-      const T u0 = m.u[4 * lv], u1 = m.u[4 * lv + 1], u2 = m.u[4 * lv + 2];
-      const T r0 = m.r[3 * lv], r1 = m.r[3 * lv + 1], r2 = m.r[3 * lv + 2];
-      dl += a0 * u0 + a1 * u1 + a2 * u2;
-      gl += r0 * u0 + r1 * u1 + r2 * u2;
-      rl += r0 * r0 + r1 * r1 + r2 * r2;
-    }
-    cluster_sum3<CL, T>(cluster, m, rl, gl, dl, 1, sums);
-    if (t0) {
-      // after an update: the convergence test on its residual, then the
-      // scalars of this iteration's update (tile path: spmv_decide)
-      int stop = 0;
-      if (iters > 0) {
-        srr = sums[0];
-        if (srr < innerThr) {
-          stop = 1;
-        } else if (!finite_d(srr) || !finite_d(sums[1]) || !finite_d(alpha)) {
-          stop = 1;
-          converged = -1;
-          outerDone = 1;
-        } else if (totalIters >= maxit) {
-          stop = 1;
-        }
-      }
-      if (!stop) {
-        const double g = sums[1], delta = sums[2];
-        if (iters == 0) {
-          beta = 0.0;
-          alpha = g / delta;
-        } else {
-          beta = g / gamma;
-          alpha = g / (delta - beta * g / alpha);
-        }
-        gammaOld = gamma;
-        gamma = g;
-        iters += 1;
-        totalIters += 1;
-      }
-      bc.alpha = T(alpha);
-      bc.beta = T(beta);
-      bc.stop = stop;
-    }
-    __syncthreads();
-    if (bc.stop) break;
-    const T ta = bc.alpha, tb = bc.beta;
-    // ---- p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s, u = Minv r ----
+  // Mixed precision: every refinement sweep runs here, back to back (the
+  // scene's own y, FP64 residual and outer test, as k_accumulate and
+  // k_residual do for the tile path), so a scene's sweeps never wait for
+  // the rest of the batch.
+  double sums[3];
+  for (;;) {
+    // ---- init: r = r64 / rsc (the FP64 residual, scaled and rounded), u = Minv r, d = p = s = 0 ----
+    const double rsc = bc.scale;
+    const double inv = 1.0 / rsc;  // exact: rsc is a power of two
+    T rr = T(0), ru = T(0);
     for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
       const int u = v0 + my0 + lv;
       T r3[3];
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        const int j = 3 * lv + i;
-        const T p = m.u[4 * lv + i] + tb * m.p[j];
-        const T sv = m.w[j] + tb * m.s[j];
-        m.p[j] = p;
-        m.s[j] = sv;
-        m.d[j] += ta * p;
-        r3[i] = m.r[j] - ta * sv;
-        m.r[j] = r3[i];
+        r3[i] = T(b.r64[3 * u + i] * inv);
+        m.r[3 * lv + i] = r3[i];
+        m.d[3 * lv + i] = T(0);
+        m.p[3 * lv + i] = T(0);
+        m.s[3 * lv + i] = T(0);
+        rr += r3[i] * r3[i];
       }
       const T* M = v.minv + 9 * (size_t)u;
 #pragma unroll
-      for (int i = 0; i < 3; i++) m.u[4 * lv + i] = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
+      for (int i = 0; i < 3; i++) {
+        const T ui = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
+        m.u[4 * lv + i] = ui;
+        ru += r3[i] * ui;
+      }
+      m.u[4 * lv + 3] = T(0);
     }
-    // the new u reaches the other CTAs' SpMV
-    cluster.sync();
+    cluster_sum3<CL, T>(cluster, m, rr, ru, T(0), 4, sums);
+    if (t0) {
+      ss.srr = sums[0];
+      double itol = st.tol;
+      if (sizeof(T) != sizeof(double))
+        itol = fmax(st.tol * sqrt(st.rhsNorm2 / fmax(ss.srr * rsc * rsc, DBL_MIN)), st.innerFloor);
+      ss.innerThr = fmax(itol * itol * ss.srr, DBL_MIN);
+      ss.gamma = sums[1];
+      ss.gammaOld = 1.0;
+      ss.alpha = 1.0;
+      ss.beta = 0.0;
+      ss.iters = 0;
+      bc.stop = (ss.srr == 0.0 || ss.srr < ss.innerThr) ? 1 : 0;
+    }
+    __syncthreads();
+    while (!bc.stop) {
+      // ---- w = A u over my vertices; delta = (w, u), gamma = (r, u), |r|^2 ----
+      T dl = T(0), gl = T(0), rl = T(0);
+      for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
+        const int u = v0 + my0 + lv;
+        T a0 = T(0), a1 = T(0), a2 = T(0);
+        const int len = b.rowptr[u + 1] - b.rowptr[u];
+        const size_t srow = (size_t)b.sliceRow[u >> 5];
+        // the row's sliced 3x3 blocks (entry e of block j at (j * 288 + 32 e))
+        // and gather entries (j * 32), four blocks per trip with the next
+        // trip's gather entries fetched one trip ahead
+        const T* B = v.lhs + srow * kSlotVals + (u & (kSlice - 1));
+        const int* G = gather + srow * kSlice + (u & (kSlice - 1));
+        int gn[4];
+  #pragma unroll
+        for (int q = 0; q < 4; q++) gn[q] = q < len ? __ldg(G + q * kSlice) : 0;
+        for (int j = 0; j < len; j += 4) {
+          int gq[4];
+  #pragma unroll
+          for (int q = 0; q < 4; q++) {
+            gq[q] = gn[q];
+            gn[q] = (j + 4 + q < len) ? __ldg(G + (j + 4 + q) * kSlice) : 0;
+          }
+          T x[4][3];
+  #pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const uint32_t a = m.ubase[gq[q] >> 20] + ((uint32_t)(gq[q] & 0xFFFFF) << kUShift);
+            ld_u(a, x[q]);
+          }
+  #pragma unroll
+          for (int q = 0; q < 4; q++) {
+            if (j + q < len) {
+              const T* Bq = B + (size_t)kSlotVals * (j + q);
+              a0 = fma(Bq[0], x[q][0], fma(Bq[kSlice], x[q][1], fma(Bq[2 * kSlice], x[q][2], a0)));
+              a1 = fma(Bq[3 * kSlice], x[q][0], fma(Bq[4 * kSlice], x[q][1], fma(Bq[5 * kSlice], x[q][2], a1)));
+              a2 = fma(Bq[6 * kSlice], x[q][0], fma(Bq[7 * kSlice], x[q][1], fma(Bq[8 * kSlice], x[q][2], a2)));
+            }
+          }
+        }
+        m.w[3 * lv] = a0;
+        m.w[3 * lv + 1] = a1;
+        m.w[3 * lv + 2] = a2;
+        const T u0 = m.u[4 * lv], u1 = m.u[4 * lv + 1], u2 = m.u[4 * lv + 2];
+        const T r0 = m.r[3 * lv], r1 = m.r[3 * lv + 1], r2 = m.r[3 * lv + 2];
+        dl += a0 * u0 + a1 * u1 + a2 * u2;
+        gl += r0 * u0 + r1 * u1 + r2 * u2;
+        rl += r0 * r0 + r1 * r1 + r2 * r2;
+      }
+      cluster_sum3<CL, T>(cluster, m, rl, gl, dl, 1, sums);
+      if (t0) {
+        // after an update: the convergence test on its residual, then the
+        // scalars of this iteration's update (tile path: spmv_decide)
+        int stop = 0;
+        if (ss.iters > 0) {
+          ss.srr = sums[0];
+          if (ss.srr < ss.innerThr) {
+            stop = 1;
+          } else if (!finite_d(ss.srr) || !finite_d(sums[1]) || !finite_d(ss.alpha)) {
+            stop = 2;  // the step fails: no further sweep
+            ss.converged = -1;
+            ss.outerDone = 1;
+          } else if (ss.totalIters >= ss.maxit) {
+            stop = 1;
+          }
+        }
+        if (!stop) {
+          const double g = sums[1], delta = sums[2];
+          if (ss.iters == 0) {
+            ss.beta = 0.0;
+            ss.alpha = g / delta;
+          } else {
+            ss.beta = g / ss.gamma;
+            ss.alpha = g / (delta - ss.beta * g / ss.alpha);
+          }
+          ss.gammaOld = ss.gamma;
+          ss.gamma = g;
+          ss.iters += 1;
+          ss.totalIters += 1;
+        }
+        bc.alpha = T(ss.alpha);
+        bc.beta = T(ss.beta);
+        bc.stop = stop;
+      }
+      __syncthreads();
+      if (bc.stop) break;
+      const T ta = bc.alpha, tb = bc.beta;
+      // ---- p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s, u = Minv r ----
+      for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
+        const int u = v0 + my0 + lv;
+        T r3[3];
+  #pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const int j = 3 * lv + i;
+          const T p = m.u[4 * lv + i] + tb * m.p[j];
+          const T sv = m.w[j] + tb * m.s[j];
+          m.p[j] = p;
+          m.s[j] = sv;
+          m.d[j] += ta * p;
+          r3[i] = m.r[j] - ta * sv;
+          m.r[j] = r3[i];
+        }
+        const T* M = v.minv + 9 * (size_t)u;
+  #pragma unroll
+        for (int i = 0; i < 3; i++) m.u[4 * lv + i] = M[3 * i] * r3[0] + M[3 * i + 1] * r3[1] + M[3 * i + 2] * r3[2];
+      }
+      // the new u reaches the other CTAs' SpMV
+      cluster.sync();
+    }
+    if (sizeof(T) == sizeof(double)) break;  // FP64: the inner solve is the solve
+    if (bc.stop == 2) break;                 // non-finite: the step has failed
+    // ---- mixed: y += rsc d, r64 = rhs - A y, |r64|^2 (FP64) ----
+    const double s64 = sweep_residual<CL>(cluster, m, b.y, b.r64, b.rhs, b.rowptr, b.cols, b.sliceRow, v.lhs,
+                                          v0 + my0, nmine, rsc);
+    if (t0) {
+      // the outer test (tile path: k_residual)
+      ss.sweep += 1;
+      int done = 0;
+      if (s64 < st.threshold) {
+        done = 1;
+        ss.converged = 1;
+      } else if (!finite_d(s64)) {
+        done = 1;
+        ss.converged = -1;
+      } else if (ss.sweep >= st.maxSweeps || ss.totalIters >= ss.maxit) {
+        done = 1;
+        ss.converged = 0;
+      }
+      ss.outerDone = done;
+      ss.srr = s64;
+      bc.scale = pow2_near_norm(s64);
+      bc.stop = done;
+    }
+    __syncthreads();
+    if (bc.stop) break;
   }
-  // ---- results: the correction d (FP64 path: the solution y itself) ----
-  for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
-    const int u = v0 + my0 + lv;
+  // ---- results: FP64 path, the solution y itself (the correction d) ----
+  if (sizeof(T) == sizeof(double)) {
+    for (int lv = threadIdx.x; lv < nmine; lv += kClusterThreads) {
+      const int u = v0 + my0 + lv;
 #pragma unroll
-    for (int i = 0; i < 3; i++) v.d[3 * u + i] = m.d[3 * lv + i];
+      for (int i = 0; i < 3; i++) v.d[3 * u + i] = m.d[3 * lv + i];
+    }
   }
   if (lead) {
-    st.rr = srr;
-    st.iters = iters;
-    st.totalIters = totalIters;
-    st.gamma = gamma;
-    st.gammaOld = gammaOld;
-    st.alpha = alpha;
-    st.beta = beta;
-    st.innerThreshold = innerThr;
+    st.rr = ss.srr;
+    st.iters = ss.iters;
+    st.totalIters = ss.totalIters;
+    st.gamma = ss.gamma;
+    st.gammaOld = ss.gammaOld;
+    st.alpha = ss.alpha;
+    st.beta = ss.beta;
+    st.innerThreshold = ss.innerThr;
     st.done = 1;
-    if (outerDone) {
-      st.converged = converged;
-      st.outerDone = 1;
-    } else if (sizeof(T) == sizeof(double)) {
-      // FP64 path: the recursive residual is the solver's verdict (Eigen)
-      st.rr64 = srr;
-      st.converged = srr < st.threshold ? 1 : 0;
-      st.outerDone = 1;
+    if (sizeof(T) == sizeof(double)) {
+      if (ss.outerDone) {
+        st.converged = ss.converged;
+      } else {
+        // FP64 path: the recursive residual is the solver's verdict (Eigen)
+        st.rr64 = ss.srr;
+        st.converged = ss.srr < st.threshold ? 1 : 0;
+      }
+    } else {
+      st.sweep = ss.sweep;
+      st.rr64 = ss.srr;
+      st.rScale = bc.scale;
+      st.converged = ss.converged;
     }
+    st.outerDone = 1;
   }
   // no CTA leaves while another may still read its shared memory
   cluster.sync();

@@ -1096,7 +1096,7 @@ __global__ void __launch_bounds__(1024) k_compact_tiles(DeviceBatch b, unsigned 
 __global__ void k_accumulate(DeviceBatch b) {
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
-  if (b.solve[s].outerDone) return;
+  if (b.solve[s].outerDone || b.scenes[s].pcgCluster) return;  // a cluster refines its own scene
   const int u = b.tileV0[tile] + threadIdx.x;
   if (u >= b.tileV1[tile]) return;
   const double sc = b.solve[s].rScale > 0.0 ? b.solve[s].rScale : 1.0;
@@ -1113,7 +1113,7 @@ __global__ void __launch_bounds__(3 * TV) k_residual(DeviceBatch b) {
   const int tile = blockIdx.x;
   const int s = b.tileScene[tile];
   SolveState& st = b.solve[s];
-  if (st.outerDone) return;
+  if (st.outerDone || b.scenes[s].pcgCluster) return;  // a cluster refines its own scene
   const int row = 3 * b.tileV0[tile] + threadIdx.x;
   double rr = 0.0;
   if (row < 3 * b.tileV1[tile]) {
