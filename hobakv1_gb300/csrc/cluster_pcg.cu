@@ -183,40 +183,66 @@ __device__ __forceinline__ double cluster_sum_f64(cg::cluster_group& cluster, co
   return out;
 }
 
-// The end of a mixed-precision sweep for vertices [u0, u0 + n) of a scene:
-// y += rsc d (d from shared memory), a cluster barrier (every CTA's y is then
-// visible to the cluster: release / acquire), r64 = rhs - A y with the FP32
-// matrix entries promoted and FP64 sums in row order (as k_residual), and
-// |r64|^2 summed over the cluster, valid in warp 0.  Not inlined: its FP64
-// registers stay out of the PCG loop's allocation.
+// a * x + (s, c): the exact product (TwoProduct: rounded product and its
+// error by an FMA) added to the running sum s with the addition's error
+// (TwoSum) and the product's error gathered in c.  Rounded operations only
+// (__fmul_rn / __fadd_rn are never contracted), so the error terms are exact.
+__device__ __forceinline__ void dot2_step(float a, float x, float& s, float& c) {
+  const float p = __fmul_rn(a, x);
+  const float pe = __fmaf_rn(a, x, -p);
+  const float t = __fadd_rn(s, p);
+  const float bp = __fsub_rn(t, s);
+  const float se = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(se, pe));
+}
+
+// The end of a mixed-precision sweep for vertices [u0, u0 + n) of a scene.
+// y += rsc d in FP64; the correction d is published four wide in u's place
+// (u is rebuilt by the next sweep's start); a cluster barrier (release /
+// acquire); then the residual is updated, r64 -= rsc (A d), with A d formed
+// from the FP32 blocks and the FP32 d by compensated dot products (Dot2 of
+// Ogita, Rump and Oishi: as accurate as FP64 sums of the exact products, on
+// the FP32 pipes rather than GB300's 2-lane FP64 pipe), and |r64|^2 summed
+// over the cluster (valid in warp 0).  r64 starts as rhs (y = 0), so it is
+// rhs - A y up to FP64 rounding of the updates.  Not inlined: its registers
+// stay out of the PCG loop's allocation.
 template <int CL>
 __device__ __noinline__ double sweep_residual(cg::cluster_group& cluster, const ClusterSmem<float>& m, double* y,
-                                              double* r64, const double* rhs, const int* rowptr, const int* cols,
-                                              const int* sliceRow, const float* lhs, int u0, int n, double rsc) {
+                                              double* r64, const int* gather, const int* sliceRow, const int* rowptr,
+                                              const float* lhs, int u0, int n, double rsc) {
   for (int lv = threadIdx.x; lv < n; lv += kClusterThreads) {
     const int u = u0 + lv;
 #pragma unroll
-    for (int i = 0; i < 3; i++) y[3 * u + i] += rsc * double(m.d[3 * lv + i]);
+    for (int i = 0; i < 3; i++) {
+      const float di = m.d[3 * lv + i];
+      y[3 * u + i] += rsc * double(di);
+      m.u[4 * lv + i] = di;
+    }
+    m.u[4 * lv + 3] = 0.0f;
   }
   cluster.sync();
   double rl = 0.0;
   for (int lv = threadIdx.x; lv < n; lv += kClusterThreads) {
     const int u = u0 + lv;
-    const int k0 = rowptr[u], k1 = rowptr[u + 1];
-    const float* A = lhs + (size_t)sliceRow[u >> 5] * kSlotVals + (u & (kSlice - 1));
-    double acc[3] = {0.0, 0.0, 0.0};
-    for (int k = k0; k < k1; k++) {
-      const int w = cols[k];
-      const float* B = A + (size_t)kSlotVals * (k - k0);
-      const double y0 = y[3 * w], y1 = y[3 * w + 1], y2 = y[3 * w + 2];
+    const int len = rowptr[u + 1] - rowptr[u];
+    const size_t srow = (size_t)sliceRow[u >> 5];
+    const float* B = lhs + srow * kSlotVals + (u & (kSlice - 1));
+    const int* G = gather + srow * kSlice + (u & (kSlice - 1));
+    float s[3] = {0.0f, 0.0f, 0.0f}, c[3] = {0.0f, 0.0f, 0.0f};
+    for (int j = 0; j < len; j++) {
+      const int g = __ldg(G + j * kSlice);
+      float x[3];
+      ld_u(m.ubase[g >> 20] + ((uint32_t)(g & 0xFFFFF) << 4), x);
+      const float* Bj = B + (size_t)kSlotVals * j;
 #pragma unroll
       for (int i = 0; i < 3; i++)
-        acc[i] += double(B[3 * i * kSlice]) * y0 + double(B[(3 * i + 1) * kSlice]) * y1 +
-                  double(B[(3 * i + 2) * kSlice]) * y2;
+#pragma unroll
+        for (int k = 0; k < 3; k++) dot2_step(Bj[(3 * i + k) * kSlice], x[k], s[i], c[i]);
     }
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const double ri = rhs[3 * u + i] - acc[i];
+      const double ri = r64[3 * u + i] - rsc * (double(s[i]) + double(c[i]));
       r64[3 * u + i] = ri;
       rl += ri * ri;
     }
@@ -224,8 +250,8 @@ __device__ __noinline__ double sweep_residual(cg::cluster_group& cluster, const 
   return cluster_sum_f64<CL>(cluster, m, rl, 7);
 }
 template <int CL>
-__device__ double sweep_residual(cg::cluster_group&, const ClusterSmem<double>&, double*, double*, const double*,
-                                 const int*, const int*, const int*, const double*, int, int, double) {
+__device__ double sweep_residual(cg::cluster_group&, const ClusterSmem<double>&, double*, double*, const int*,
+                                 const int*, const int*, const double*, int, int, double) {
   return 0.0;  // FP64: one inner solve is the solve; never called
 }
 
@@ -460,9 +486,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
     }
     if (sizeof(T) == sizeof(double)) break;  // FP64: the inner solve is the solve
     if (bc.stop == 2) break;                 // non-finite: the step has failed
-    // ---- mixed: y += rsc d, r64 = rhs - A y, |r64|^2 (FP64) ----
-    const double s64 = sweep_residual<CL>(cluster, m, b.y, b.r64, b.rhs, b.rowptr, b.cols, b.sliceRow, v.lhs,
-                                          v0 + my0, nmine, rsc);
+    // ---- mixed: y += rsc d, r64 -= rsc A d, |r64|^2 ----
+    const double s64 = sweep_residual<CL>(cluster, m, b.y, b.r64, gather, b.sliceRow, b.rowptr, v.lhs, v0 + my0,
+                                          nmine, rsc);
     if (t0) {
       // the outer test (tile path: k_residual)
       ss.sweep += 1;
