@@ -58,6 +58,8 @@ WORKLOADS = {
     "mix256_mixed": dict(kind="mix", count=256, material="snh/arap", precision=1),
     "mix256_fp64": dict(kind="mix", count=256, material="snh/arap", precision=0),
     "mix64_mixed": dict(kind="mix", count=64, material="snh/arap", precision=1),
+    # every third scene of the 256-scene mix (86 scenes, ~2 GB on the device): profiling case
+    "mix86_mixed": dict(kind="mix", count=256, stride=3, material="snh/arap", precision=1),
     # BACKWARD_EULER_POSITION (Rayleigh damped, alpha = beta = 0.01) on the same inputs
     "kuhn40_snh_twist_position": dict(kind="config2", N=40, material="snh", precision=0, integrator="position"),
     "kuhn40_snh_twist_position_mixed": dict(kind="config2", N=40, material="snh", precision=1,
@@ -92,7 +94,7 @@ def make_scenes(spec):
     if spec["kind"] == "config1":
         return [scenes.config1_scene(spec["N"], spec["material"])]
     if spec["kind"] == "mix":
-        return scenes.config4_scenes(spec["count"])
+        return scenes.config4_scenes(spec["count"])[::spec.get("stride", 1)]
     if spec["kind"] == "serve":
         return scenes.config5_jobs(spec["count"])
     if spec["kind"] == "contact":
