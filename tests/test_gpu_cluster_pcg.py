@@ -33,6 +33,10 @@ def test_cluster_path_matches_tile_path(precision):
     for k in range(len(mix)):
         assert rel(xc[k], xt[k]) < bound, (k, mix[k].nv, rel(xc[k], xt[k]))
         assert stc[k][1] == 1 and abs(stc[k][0] - stt[k][0]) <= 2, (stc[k], stt[k])
+        # mixed: the cluster runs the refinement sweeps itself (residual
+        # updated with compensated FP32 products) and ends on the same FP64
+        # test, after as many sweeps as the tile path's FP64 residual needs
+        assert stc[k][2] < 1e-8 and abs(stc[k][3] - stt[k][3]) <= 1, (stc[k], stt[k])
 
 
 def test_cluster_path_matches_oracle_with_jacobi_iterations():
