@@ -274,12 +274,13 @@ def port_vs_reference():
             "port_vs_reference_how": m.get("how")}
 
 
-def serve_once(job_specs, arrivals, precision, budget_bytes, tuning=None):
-    """Drive the continuous-batching server with jobs arriving at the given
-    times (seconds from start).  Returns (wall seconds, jobs, server)."""
+def serve_once(job_specs, arrivals, precision, budget_bytes, tuning=None, impl="native"):
+    """Drive the continuous-batching server (the library's own, or the Python
+    one) with jobs arriving at the given times (seconds from start).  Returns
+    (wall seconds, jobs, server)."""
     from hobakv1_gb300 import serving
-    srv = serving.Server(budget_bytes, precision=precision, async_build=True, max_admit_per_tick=8,
-                         tuning=tuning)
+    cls = serving.NativeServer if impl == "native" else serving.Server
+    srv = cls(budget_bytes, precision=precision, async_build=True, max_admit_per_tick=8, tuning=tuning)
     jobs = [serving.Job(k, sc, n, contact) for k, (sc, n, contact) in enumerate(job_specs)]
     t0 = time.perf_counter()
     i = 0
@@ -312,13 +313,13 @@ def run_serving(args, spec, job_specs):
     budget = int(float(spec.get("budget_gb", 64)) * (1 << 30))
     serve_tuning = None if args.cluster_pcg is None else {"cluster_pcg": args.cluster_pcg}
     # warm the library (module load, first graph capture) outside the timing
-    serve_once(job_specs[:2], [0.0, 0.0], hobak.PRECISION_MIXED, budget)
+    serve_once(job_specs[:2], [0.0, 0.0], hobak.PRECISION_MIXED, budget, impl=args.serve_impl)
     runs = {}
     finals = {}
     for prec_name, prec in (("mixed", hobak.PRECISION_MIXED), ("fp64", hobak.PRECISION_FP64)):
         for lam in spec["lambdas"]:
             arrivals = np.cumsum(gaps) / lam
-            wall, jobs, srv = serve_once(job_specs, arrivals, prec, budget, serve_tuning)
+            wall, jobs, srv = serve_once(job_specs, arrivals, prec, budget, serve_tuning, args.serve_impl)
             step_ms = [ms for j in jobs for ms in j.step_ms]
             job_s = [j.finished - j.submitted for j in jobs]
             runs[f"{prec_name}@{lam}"] = {
@@ -346,6 +347,8 @@ def run_serving(args, spec, job_specs):
                        "contact": "even jobs: two SNH cubes, vertex-face eps 1e-3, stiffness 1e3, beta 1e-3",
                        "tets_total": int(sum(sc.nt for sc, _, _ in job_specs)), "pcg_tol": 1e-8,
                        "budget_gb": budget / (1 << 30),
+                       "server": ("hobak_server_* (the library's native server)" if args.serve_impl == "native"
+                                  else "serving.Server (Python)"),
                        "timing": "wall clock from the first arrival to the last result on the host",
                        "pcg_path": "cluster-resident for small contact-free scenes" if args.cluster_pcg
                        else "tile path"},
@@ -359,7 +362,8 @@ def run_serving(args, spec, job_specs):
                 "per_job": [float(e) for e in errs]},
             "e2e": {"value": hi_m["job_steps_per_s"], "unit": "job-steps/s", "h2d_bytes_per_step":
                     nbytes_in / total_steps, "d2h_bytes_per_step": nbytes_out / total_steps,
-                    "api": "serving.Server over hobak_batch_create/step_async/wait/get_state"}}
+                    "api": ("hobak_server_submit/pump/job" if args.serve_impl == "native"
+                    else "serving.Server over hobak_batch_create/step_async/wait/get_state")}}
     print(json.dumps(line), flush=True)
 
 
@@ -725,6 +729,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the unbatched FP64 comparison on mixes")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--serve-impl", default="native", choices=["native", "python"],
+                    help="serving workloads: the library's server (hobak_server_*) or the Python one")
     ap.add_argument("--cluster-pcg", type=int, choices=[0, 1], default=None,
                     help="PCG path of the serving cohorts (and of --no-autotune batches): 1 = cluster-resident")
     ap.add_argument("--cluster-max", type=int, choices=[1, 2, 4, 8, 16], default=None,

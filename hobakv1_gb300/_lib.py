@@ -41,6 +41,24 @@ class HobakTuning(ctypes.Structure):
                 ("cluster_max", ctypes.c_int), ("step_ms", ctypes.c_double)]
 
 
+class HobakServerOpts(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_longlong), ("max_admit", ctypes.c_int), ("max_cohort", ctypes.c_int),
+                ("merge", ctypes.c_int), ("merge_fraction", ctypes.c_double), ("async_build", ctypes.c_int),
+                ("keep_results", ctypes.c_int), ("use_tuning", ctypes.c_int), ("tuning", HobakTuning)]
+
+
+class HobakServerStats(ctypes.Structure):
+    _fields_ = [("used_bytes", ctypes.c_longlong), ("cohorts", ctypes.c_int), ("queued", ctypes.c_int),
+                ("building", ctypes.c_int), ("merges", ctypes.c_int), ("merged_arrivals", ctypes.c_int),
+                ("finished", ctypes.c_int), ("ticks", ctypes.c_longlong), ("now_s", ctypes.c_double)]
+
+
+class HobakJobInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("done_steps", ctypes.c_int), ("nsteps", ctypes.c_int),
+                ("nv", ctypes.c_int), ("submitted_s", ctypes.c_double), ("admitted_s", ctypes.c_double),
+                ("finished_s", ctypes.c_double)]
+
+
 class HobakStepStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int),
                 ("rel_residual", ctypes.c_double), ("refinements", ctypes.c_int)]
@@ -48,6 +66,16 @@ class HobakStepStats(ctypes.Structure):
 
 # name -> (restype, argtypes); mirrors include/hobak_gpu.h
 SIGNATURES = {
+    "hobak_default_server_opts": (None, [ctypes.POINTER(HobakServerOpts)]),
+    "hobak_server_create": (ctypes.c_int, [ctypes.POINTER(HobakServerOpts), ctypes.POINTER(HobakSolverOpts),
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "hobak_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakSceneDesc), ctypes.c_int, _dp, _ip]),
+    "hobak_server_pump": (ctypes.c_int, [ctypes.c_void_p, _ip]),
+    "hobak_server_tick": (ctypes.c_int, [ctypes.c_void_p, _ip]),
+    "hobak_server_idle": (ctypes.c_int, [ctypes.c_void_p]),
+    "hobak_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(HobakServerStats)]),
+    "hobak_server_job": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(HobakJobInfo), _dp, _dp, _dp]),
+    "hobak_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "hobak_version": (ctypes.c_char_p, []),
     "hobak_last_error": (ctypes.c_char_p, []),
     "hobak_device_check": (ctypes.c_int, [_ip, _ip, _ip]),

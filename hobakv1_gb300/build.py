@@ -20,7 +20,7 @@ LIB = os.path.join(OUT, "libhobak_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-SOURCES = ["element.cu", "solver.cu", "cluster_pcg.cu", "collision.cu", "api.cu", "noalloc.cu"]
+SOURCES = ["element.cu", "solver.cu", "cluster_pcg.cu", "collision.cu", "api.cu", "noalloc.cu", "server.cu"]
 
 
 def nvcc() -> str:

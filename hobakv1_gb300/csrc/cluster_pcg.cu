@@ -22,6 +22,7 @@
 // branches and reaches every barrier.
 #include <cooperative_groups.h>
 
+#include <atomic>
 #include <cfloat>
 
 #include "kernels.cuh"
@@ -569,10 +570,11 @@ cudaError_t allow_smem() {
 }  // namespace
 
 // Opt every cluster kernel into kClusterSmemMax bytes of dynamic shared
-// memory (once per process; outside any stream capture).
+// memory (once per process; outside any stream capture; batches may be
+// created and stepped from several host threads).
 int configure_cluster_pcg() {
-  static int done = 0;
-  if (done) return 0;
+  static std::atomic<int> done{0};
+  if (done.load()) return 0;
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = allow_smem<1, float>();
   if (e == cudaSuccess) e = allow_smem<2, float>();
@@ -585,7 +587,7 @@ int configure_cluster_pcg() {
   if (e == cudaSuccess) e = allow_smem<8, double>();
   if (e == cudaSuccess) e = allow_smem<16, double>();
   if (e != cudaSuccess) return (int)e;
-  done = 1;
+  done.store(1);
   return 0;
 }
 

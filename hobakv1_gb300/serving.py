@@ -41,6 +41,7 @@ after it is built.  The memory budget is reserved at admission time.
 from __future__ import annotations
 
 import concurrent.futures
+import ctypes
 import dataclasses
 import time
 from collections import deque
@@ -371,3 +372,147 @@ class Server:
         if self._pool is not None:
             self._pool.shutdown()
         self.cohorts.clear()
+
+
+class NativeServer:
+    """The same server in the library (hobak_server_*: host C++ over the
+    batch ABI, a builder thread for async builds), with Server's interface:
+    submit Job objects, drive it with pump() or tick(), read the jobs back.
+    A C or C++ host uses the hobak_server_* calls directly."""
+
+    def __init__(self, budget_bytes: int, precision: int = hobak.PRECISION_MIXED,
+                 max_admit_per_tick: int = 64, keep_results: bool = True, async_build: bool = False,
+                 tuning: Optional[dict] = None, merge: bool = True, merge_fraction: float = 0.5,
+                 max_cohort: int = 64, solver_opts=None):
+        from . import _lib
+        self._lib = _lib
+        L = _lib.load()
+        o = _lib.HobakServerOpts()
+        L.hobak_default_server_opts(o)
+        o.budget_bytes = int(budget_bytes)
+        o.max_admit, o.max_cohort = int(max_admit_per_tick), int(max_cohort)
+        o.merge, o.merge_fraction = int(merge), float(merge_fraction)
+        o.async_build, o.keep_results = int(async_build), int(keep_results)
+        if tuning:
+            cur = dict(tile_vertices=128, element_threads=128, assembly_threads=256, pcg_chunk=8, cluster_pcg=0,
+                       cluster_max=16, step_ms=0.0)
+            cur.update(tuning)
+            o.use_tuning = 1
+            o.tuning = _lib.HobakTuning(*[cur[k] for k in hobak.BATCH.TUNING])
+        self.opts = solver_opts if solver_opts is not None else hobak.solver_opts(precision=precision)
+        self.budget = int(budget_bytes)
+        self.keep_results = keep_results
+        self.h = ctypes.c_void_p()
+        hobak.check(L.hobak_server_create(o, self.opts, ctypes.byref(self.h)), "hobak_server_create")
+        self.jobs: Dict[int, Job] = {}  # server job id -> Job
+        self.open: Dict[int, Job] = {}  # not finished yet
+        self.finished: Dict[int, Job] = {}
+        self.used_history: List[tuple] = []
+        self.tick_ms: List[float] = []
+        self.rejected = 0
+
+    def submit(self, job: Job):
+        a = hobak._SceneArrays(job.scene.rest, job.scene.tets,
+                               hobak.make_material(job.scene.material, job.scene.mu, job.scene.lam,
+                                                   getattr(job.scene, "fiber", None)),
+                               job.scene.density, job.scene.gravity, job.scene.dt, job.scene.pinned,
+                               job.scene.x0, job.scene.v0)
+        contact = (ctypes.c_double * 3)(*job.collisions) if job.collisions is not None else None
+        jid = ctypes.c_int()
+        rc = self._lib.load().hobak_server_submit(self.h, ctypes.byref(a.desc), int(job.nsteps), contact,
+                                                  ctypes.byref(jid))
+        if rc != 0:
+            self.rejected += 1
+            raise ValueError(f"job {job.id}: " + self._lib.load().hobak_last_error().decode())
+        self.jobs[jid.value] = job
+        self.open[jid.value] = job
+        info = self._info(jid.value)
+        job.submitted = info.submitted_s
+
+    def _info(self, jid: int, step_ms=None, x=None, v=None):
+        info = self._lib.HobakJobInfo()
+        hobak.check(self._lib.load().hobak_server_job(self.h, jid, ctypes.byref(info), hobak.dptr(step_ms),
+                                                      hobak.dptr(x), hobak.dptr(v)), "hobak_server_job")
+        return info
+
+    def _stats(self):
+        if not self.h.value:  # closed: the last figures
+            return self._final
+        st = self._lib.HobakServerStats()
+        hobak.check(self._lib.load().hobak_server_get_stats(self.h, ctypes.byref(st)), "hobak_server_get_stats")
+        return st
+
+    def _sync(self):
+        for jid, job in list(self.open.items()):
+            info = self._info(jid)
+            job.admitted = info.admitted_s
+            job.done_steps = info.done_steps
+            if info.state == 2:  # HOBAK_JOB_FINISHED
+                ms = np.zeros(info.done_steps)
+                x = v = None
+                if self.keep_results:
+                    x, v = np.zeros(3 * info.nv), np.zeros(3 * info.nv)
+                self._info(jid, ms, x, v)
+                job.step_ms = ms.tolist()
+                job.result_x, job.result_v = x, v
+                job.finished = info.finished_s
+                self.finished[job.id] = job
+                del self.open[jid]
+        st = self._stats()
+        self.used_history.append((st.now_s, st.used_bytes))
+        return st
+
+    def _round(self, fn) -> int:
+        n = ctypes.c_int()
+        t0 = time.perf_counter()
+        hobak.check(fn(self.h, ctypes.byref(n)), "hobak_server_round")
+        if n.value:
+            self.tick_ms.append((time.perf_counter() - t0) * 1e3)
+        self._sync()
+        return n.value
+
+    def pump(self) -> int:
+        return self._round(self._lib.load().hobak_server_pump)
+
+    def tick(self) -> int:
+        return self._round(self._lib.load().hobak_server_tick)
+
+    def idle(self) -> bool:
+        return bool(self._lib.load().hobak_server_idle(self.h))
+
+    def drain(self, max_ticks: int = 1_000_000):
+        while not self.idle() and max_ticks > 0:
+            self.tick()
+            max_ticks -= 1
+
+    @property
+    def used(self) -> int:
+        return int(self._stats().used_bytes)
+
+    @property
+    def cohorts(self) -> list:
+        return [None] * self._stats().cohorts
+
+    @property
+    def merges(self) -> int:
+        return int(self._stats().merges)
+
+    @property
+    def merged_arrivals(self) -> int:
+        return int(self._stats().merged_arrivals)
+
+    @property
+    def ticks(self) -> int:
+        return int(self._stats().ticks)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self._final = self._stats()
+            self._lib.load().hobak_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

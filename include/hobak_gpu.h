@@ -373,6 +373,62 @@ int hobak_batch_set_tuning(hobak_batch b, const hobak_tuning* t);
  * applies the fastest shape.  out may be NULL. */
 int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out);
 
+/* ---- continuous-batching server (no reference counterpart) ----
+ * Scene-timestep jobs admitted FIFO under a device-memory budget into
+ * batches ("cohorts", one per admission round) that step on their own
+ * streams; hobak_server_pump relaunches each cohort as soon as its own step
+ * has completed, hobak_server_tick steps all cohorts in lock step.  Finished
+ * jobs are parked and read back; a cohort whose finished jobs hold at least
+ * merge_fraction of it, or any cohort with a finished job while jobs are
+ * queued, is re-packed with the queued arrivals that fit (built on a host
+ * thread when async_build, swapped in at its next step boundary with the
+ * running jobs' state carried over), which frees the finished jobs' device
+ * memory.  Each job's result is bitwise the same as the job run alone in
+ * its own batch with the same solver options and tuning.  One host thread
+ * drives a server; its batches use the solver options given here. */
+#define HOBAK_JOB_QUEUED 0
+#define HOBAK_JOB_RUNNING 1    /* admitted: in a cohort, or in one being built */
+#define HOBAK_JOB_FINISHED 2
+typedef struct hobak_server_t* hobak_server;
+typedef struct hobak_server_opts {
+  long long budget_bytes;  /* device memory the server's batches may hold (estimates until built) */
+  int max_admit;           /* jobs per new cohort at most (default 64) */
+  int max_cohort;          /* jobs per re-packed cohort at most (default 64) */
+  int merge;               /* 1: re-pack cohorts (default 1) */
+  double merge_fraction;   /* re-pack once this share of a cohort's jobs finished (default 0.5) */
+  int async_build;         /* 1: build cohorts on a host thread (default 0) */
+  int keep_results;        /* 1: read back every finished job's x, v (default 1) */
+  int use_tuning;          /* 1: apply `tuning` to every cohort (default 0: the library's defaults) */
+  hobak_tuning tuning;
+} hobak_server_opts;
+typedef struct hobak_server_stats {
+  long long used_bytes;    /* device bytes held or reserved by the server's batches */
+  int cohorts, queued, building, merges, merged_arrivals, finished;
+  long long ticks;         /* cohort steps completed */
+  double now_s;            /* the server's clock (seconds), as in hobak_job_info */
+} hobak_server_stats;
+typedef struct hobak_job_info {
+  int state;               /* HOBAK_JOB_* */
+  int done_steps, nsteps, nv;
+  double submitted_s, admitted_s, finished_s;  /* server clock; -1 until then */
+} hobak_job_info;
+void hobak_default_server_opts(hobak_server_opts* opts);
+int hobak_server_create(const hobak_server_opts* opts, const hobak_solver_opts* solver, hobak_server* out);
+/* Copies the scene; contact = {eps, stiffness, beta} turns vertex-face
+ * contact on for this job (NULL: off).  Refuses a job whose estimated
+ * footprint exceeds the whole budget. */
+int hobak_server_submit(hobak_server s, const hobak_scene_desc* scene, int nsteps, const double* contact, int* job);
+/* One scheduling round; *job_steps = job-steps completed in it. */
+int hobak_server_pump(hobak_server s, int* job_steps);
+int hobak_server_tick(hobak_server s, int* job_steps);
+int hobak_server_idle(hobak_server s);  /* 1: nothing queued, building or running */
+int hobak_server_get_stats(hobak_server s, hobak_server_stats* out);
+/* A job's state; step_ms (done_steps values: each step's latency, launch to
+ * completion of its cohort's step), x and v (3 nv each, finished jobs with
+ * keep_results) may be NULL. */
+int hobak_server_job(hobak_server s, int job, hobak_job_info* info, double* step_ms, double* x, double* v);
+int hobak_server_destroy(hobak_server s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,3 +85,43 @@ def test_null_handles_are_errors_not_crashes():
     assert L.hobak_batch_step(None, 1, None) == -1
     assert L.hobak_batch_get_state(None, 0, None, None) == -1
     assert L.hobak_batch_destroy(None) == 0
+
+
+def test_server_options_and_admission_checks_without_a_device():
+    """hobak_server_*: defaults, refused options and jobs, and a queued job's
+    state, all before any batch is built (no device needed)."""
+    L = _lib.load()
+    o = _lib.HobakServerOpts()
+    L.hobak_default_server_opts(ctypes.byref(o))
+    assert o.max_admit == 64 and o.max_cohort == 64 and o.merge == 1 and o.merge_fraction == 0.5
+    assert o.keep_results == 1 and o.async_build == 0 and o.budget_bytes > 0
+    h = ctypes.c_void_p()
+    bad = _lib.HobakServerOpts()
+    L.hobak_default_server_opts(ctypes.byref(bad))
+    bad.merge_fraction = 1.5
+    assert L.hobak_server_create(ctypes.byref(bad), None, ctypes.byref(h)) == -1
+    assert "merge_fraction" in L.hobak_last_error().decode() and not h.value
+    assert L.hobak_server_create(ctypes.byref(o), None, ctypes.byref(h)) == 0 and h.value
+    a = _desc(scenes.config1_scene(2))
+    jid = ctypes.c_int(-1)
+    assert L.hobak_server_submit(h, ctypes.byref(a.desc), 0, None, ctypes.byref(jid)) == -1
+    assert L.hobak_server_submit(h, ctypes.byref(a.desc), 5, None, ctypes.byref(jid)) == 0 and jid.value == 0
+    info = _lib.HobakJobInfo()
+    assert L.hobak_server_job(h, 0, ctypes.byref(info), None, None, None) == 0
+    assert (info.state, info.done_steps, info.nsteps, info.nv) == (0, 0, 5, 27)
+    assert info.submitted_s > 0 and info.admitted_s == -1 and info.finished_s == -1
+    x = np.zeros(81)
+    assert L.hobak_server_job(h, 0, None, None, x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None) == -1
+    assert L.hobak_server_job(h, 7, ctypes.byref(info), None, None, None) == -1
+    assert L.hobak_server_idle(h) == 0
+    st = _lib.HobakServerStats()
+    assert L.hobak_server_get_stats(h, ctypes.byref(st)) == 0 and (st.queued, st.cohorts, st.used_bytes) == (1, 0, 0)
+    assert L.hobak_server_destroy(h) == 0
+    small = _lib.HobakServerOpts()
+    L.hobak_default_server_opts(ctypes.byref(small))
+    small.budget_bytes = 1024
+    h2 = ctypes.c_void_p()
+    assert L.hobak_server_create(ctypes.byref(small), None, ctypes.byref(h2)) == 0
+    assert L.hobak_server_submit(h2, ctypes.byref(a.desc), 5, None, ctypes.byref(jid)) == -1
+    assert "budget" in L.hobak_last_error().decode()
+    assert L.hobak_server_destroy(h2) == 0

@@ -5,10 +5,13 @@ import numpy as np
 import pytest
 
 from hobakv1_gb300 import hobak, scenes
-from hobakv1_gb300.serving import Job, Server, footprint_bytes
+from hobakv1_gb300.serving import Job, NativeServer, Server, footprint_bytes
 
 pytestmark = pytest.mark.gpu
 VF = (1e-3, 1e3, 0.001)
+# the Python server and the library's own (hobak_server_*), same tests
+IMPLS = {"python": Server, "native": NativeServer}
+impl = pytest.mark.parametrize("impl", sorted(IMPLS))
 
 
 def jobs():
@@ -26,10 +29,11 @@ def alone(job, precision):
     return b.get_state(0)
 
 
+@impl
 @pytest.mark.parametrize("precision", [hobak.PRECISION_FP64, hobak.PRECISION_MIXED], ids=["fp64", "mixed"])
-def test_results_equal_alone_and_in_the_mix(precision):
+def test_results_equal_alone_and_in_the_mix(precision, impl):
     js = jobs()
-    srv = Server(budget_bytes=1 << 34, precision=precision)
+    srv = IMPLS[impl](budget_bytes=1 << 34, precision=precision)
     # staggered arrivals: two jobs, a few ticks, then the rest while those run
     srv.submit(js[0])
     srv.submit(js[1])
@@ -47,10 +51,11 @@ def test_results_equal_alone_and_in_the_mix(precision):
         assert np.array_equal(j.result_x, x) and np.array_equal(j.result_v, v), j.id
 
 
-def test_admission_respects_the_memory_budget():
+@impl
+def test_admission_respects_the_memory_budget(impl):
     js = jobs()
     budget = max(footprint_bytes(j.scene, 1) for j in js) * 2  # about two jobs at a time
-    srv = Server(budget_bytes=budget, precision=hobak.PRECISION_MIXED)
+    srv = IMPLS[impl](budget_bytes=budget, precision=hobak.PRECISION_MIXED)
     for j in js:
         srv.submit(j)
     peak = 0
@@ -61,15 +66,16 @@ def test_admission_respects_the_memory_budget():
     assert len(srv.finished) == len(js)
     assert all(j.admitted >= j.submitted for j in js)
     with pytest.raises(ValueError):
-        Server(budget_bytes=1024).submit(js[0])
+        IMPLS[impl](budget_bytes=1024).submit(js[0])
 
 
-def test_event_driven_pump_matches_alone():
+@impl
+def test_event_driven_pump_matches_alone(impl):
     """pump(): cohorts relaunch independently (async builds, small cohorts);
     results stay bitwise equal to each job run alone."""
     js = jobs()
-    srv = Server(budget_bytes=1 << 34, precision=hobak.PRECISION_MIXED, async_build=True,
-                 max_admit_per_tick=2)
+    srv = IMPLS[impl](budget_bytes=1 << 34, precision=hobak.PRECISION_MIXED, async_build=True,
+                      max_admit_per_tick=2)
     srv.submit(js[0])
     for _ in range(3):
         srv.pump()
@@ -86,8 +92,9 @@ def test_event_driven_pump_matches_alone():
         assert np.array_equal(j.result_x, x) and np.array_equal(j.result_v, v), j.id
 
 
+@impl
 @pytest.mark.parametrize("mode", ["tick", "pump"])
-def test_arrivals_merge_into_a_running_cohort_and_results_equal_alone(mode):
+def test_arrivals_merge_into_a_running_cohort_and_results_equal_alone(mode, impl):
     """Arrivals queued while a cohort has a finished (parked) job are merged
     into it: the cohort is re-packed with its running jobs plus the arrivals
     and swapped in at a step boundary.  Every result, of the jobs carried
@@ -95,8 +102,8 @@ def test_arrivals_merge_into_a_running_cohort_and_results_equal_alone(mode):
     job run alone."""
     js = jobs()
     a, b, c, d, e = js[2], js[3], js[0], js[1], js[5]  # 3, 11, 7, 9 (contact) and 6 steps
-    srv = Server(budget_bytes=1 << 34, precision=hobak.PRECISION_MIXED, merge_fraction=1.0,
-                 async_build=(mode == "pump"))
+    srv = IMPLS[impl](budget_bytes=1 << 34, precision=hobak.PRECISION_MIXED, merge_fraction=1.0,
+                      async_build=(mode == "pump"))
     step = srv.tick if mode == "tick" else srv.pump
     for j in (a, b, c):
         srv.submit(j)
@@ -116,13 +123,14 @@ def test_arrivals_merge_into_a_running_cohort_and_results_equal_alone(mode):
         assert np.array_equal(j.result_x, x) and np.array_equal(j.result_v, v), j.id
 
 
-def test_finished_jobs_release_their_memory():
+@impl
+def test_finished_jobs_release_their_memory(impl):
     """With no arrivals, a cohort half of whose jobs finished is re-packed
     without them: device memory in use falls, and the remaining job's result
     is unchanged (bitwise equal to running it alone)."""
     js = jobs()
     short, longer = js[2], js[3]  # 3 and 11 steps
-    srv = Server(budget_bytes=1 << 34, precision=hobak.PRECISION_FP64, merge_fraction=0.5)
+    srv = IMPLS[impl](budget_bytes=1 << 34, precision=hobak.PRECISION_FP64, merge_fraction=0.5)
     srv.submit(short)
     srv.submit(longer)
     srv.tick()
