@@ -2261,8 +2261,12 @@ int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out) {
   // 2. assembly kernel CTA size
   {
     float bestMs = 3.4e38f;
-    for (int at : {128, 256, 512}) {
+    for (int at : {64, 128, 256, 512}) {
       d.asmThreads = at;
+      // one untimed launch first: the candidates are timed warm alike
+      if (mixed) launch_assemble<float>(d, d.v32, s);
+      else launch_assemble<double>(d, d.v64, s);
+      b->launches += 1;
       CUDA_TRY(cudaEventRecord(ev.e0, s));
       for (int r = 0; r < reps; r++) {
         if (mixed) launch_assemble<float>(d, d.v32, s);
