@@ -1,17 +1,20 @@
 // Cluster-resident PCG for small scenes.
 //
-// One thread-block cluster solves one scene's inner PCG from start to finish
-// in a single launch: the scene's vertices are split into CL contiguous
-// ranges, one per CTA; the Krylov vectors of a range live in that CTA's
-// shared memory, the SpMV gathers the search vector of neighbouring ranges
-// from the other CTAs' shared memory (distributed shared memory), and every
-// dot product is a CTA tree followed by a fixed-order sum of the CL CTA
+// One thread-block cluster solves one scene's linear system from start to
+// finish in a single launch: the scene's vertices are split into CL
+// contiguous ranges, one per CTA; the Krylov vectors of a range live in that
+// CTA's shared memory, the SpMV gathers the search vector of neighbouring
+// ranges from the other CTAs' shared memory (distributed shared memory), and
+// every dot product is a CTA tree followed by a fixed-order sum of the CL CTA
 // partials read through distributed shared memory.  An iteration is two
 // cluster barriers (the fused reduction after the SpMV, and the publication
-// of the new u after the update); the matrix and Minv stay in L2 across
-// iterations.  The
-// tile path (solver.cu: two grid-wide kernels per iteration, each ending in
-// a ticketed reduction) remains for scenes too large for a cluster and for
+// of the new u after the update); the matrix and Minv are read from L2 (or
+// DRAM, when a full batch's other scenes have evicted them) every iteration.
+// In mixed precision the launch also runs every refinement sweep: the FP64
+// y update, the residual update r -= A d in compensated FP32 and the outer
+// FP64 test, then the next inner solve, until the test passes.  The tile
+// path (solver.cu: two grid-wide kernels per iteration, each ending in a
+// ticketed reduction) remains for scenes too large for a cluster and for
 // scenes with contact.
 //
 // The iteration is the same Chronopoulos-Gear PCG as the tile path, with the
