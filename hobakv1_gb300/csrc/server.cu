@@ -77,6 +77,7 @@ struct Cohort {
 
 struct Built {
   std::unique_ptr<Cohort> cohort;
+  std::vector<Job*> jobs;  // the jobs it was built for
   int rc = HOBAK_OK;
   std::string error;
 };
@@ -158,6 +159,7 @@ struct hobak_server_t {
   // A cohort of `js` (their initial state), built now on this thread.
   std::shared_ptr<Built> build_now(const std::vector<Job*>& js) const {
     auto out = std::make_shared<Built>();
+    out->jobs = js;
     std::vector<hobak_scene_desc> descs;
     for (Job* j : js) descs.push_back(j->desc);
     auto c = std::make_unique<Cohort>();
@@ -216,19 +218,32 @@ struct hobak_server_t {
     c.reset();
   }
 
+  // A build that failed: its jobs will not run (HOBAK_JOB_FAILED) and the
+  // bytes reserved for it are returned; the error is reported once.
+  int drop_failed(const std::shared_ptr<Built>& b, long long reserved, bool arrivalsOnly, const Cohort* from) {
+    for (Job* j : b->jobs)
+      if (!arrivalsOnly || j->cohort != from) j->state = HOBAK_JOB_FAILED;
+    used -= reserved;
+    return fail(b->rc, "server: building a cohort: " + b->error);
+  }
+
   int collect_built(bool block) {
     std::vector<std::pair<std::shared_future<std::shared_ptr<Built>>, long long>> keep;
+    int err = HOBAK_OK;
     for (auto& b : building) {
       if (block || ready(b.first)) {
-        std::unique_ptr<Cohort> c;
-        if (int rc = take(b.first, &c)) return rc;
-        join(std::move(c), b.second);
+        std::shared_ptr<Built> r = b.first.get();
+        if (r->rc != HOBAK_OK) {
+          if (!err) err = drop_failed(r, b.second, false, nullptr);
+          continue;
+        }
+        join(std::move(r->cohort), b.second);
       } else {
         keep.push_back(b);
       }
     }
     building = std::move(keep);
-    return HOBAK_OK;
+    return err;
   }
 
   void plan_merges() {
@@ -275,6 +290,14 @@ struct hobak_server_t {
   Cohort* swap_ready(Cohort* c, int* rc) {
     *rc = HOBAK_OK;
     if (!c->hasRepl || c->inFlight || !ready(c->repl)) return nullptr;
+    {
+      std::shared_ptr<Built> r = c->repl.get();
+      if (r->rc != HOBAK_OK) {  // the carried jobs go on in c; the arrivals fail
+        c->hasRepl = false;
+        *rc = drop_failed(r, c->replReserved, true, c);
+        return nullptr;
+      }
+    }
     std::unique_ptr<Cohort> nb;
     if ((*rc = take(c->repl, &nb))) return nullptr;
     const bool newmark = solver.integrator == HOBAK_INTEGRATOR_NEWMARK;
@@ -367,7 +390,10 @@ struct hobak_server_t {
     *next = nullptr;
     c->repl.wait();
     std::shared_ptr<Built> b = c->repl.get();
-    if (b->rc != HOBAK_OK) return fail(b->rc, "server: building a cohort: " + b->error);
+    if (b->rc != HOBAK_OK) {
+      c->hasRepl = false;
+      return drop_failed(b, c->replReserved, true, c);
+    }
     bool arrivals = false;
     for (Job* j : b->cohort->jobs) arrivals = arrivals || j->cohort != c;
     if (arrivals) {

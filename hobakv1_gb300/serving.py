@@ -447,6 +447,10 @@ class NativeServer:
             info = self._info(jid)
             job.admitted = info.admitted_s
             job.done_steps = info.done_steps
+            if info.state == 3:  # HOBAK_JOB_FAILED: its cohort could not be built
+                job.failed = True
+                del self.open[jid]
+                continue
             if info.state == 2:  # HOBAK_JOB_FINISHED
                 ms = np.zeros(info.done_steps)
                 x = v = None

@@ -389,6 +389,7 @@ int hobak_batch_autotune(hobak_batch b, int reps, hobak_tuning* out);
 #define HOBAK_JOB_QUEUED 0
 #define HOBAK_JOB_RUNNING 1    /* admitted: in a cohort, or in one being built */
 #define HOBAK_JOB_FINISHED 2
+#define HOBAK_JOB_FAILED 3     /* its cohort could not be built (the round that found it returned the error) */
 typedef struct hobak_server_t* hobak_server;
 typedef struct hobak_server_opts {
   long long budget_bytes;  /* device memory the server's batches may hold (estimates until built) */

@@ -125,3 +125,29 @@ def test_server_options_and_admission_checks_without_a_device():
     assert L.hobak_server_submit(h2, ctypes.byref(a.desc), 5, None, ctypes.byref(jid)) == -1
     assert "budget" in L.hobak_last_error().decode()
     assert L.hobak_server_destroy(h2) == 0
+
+
+def test_server_reports_a_failed_build_once_and_marks_its_jobs():
+    """A job whose batch cannot be built (an unknown material, refused
+    before the device is touched): the round returns the error, the job is
+    marked failed, its reservation is returned and the server goes idle."""
+    L = _lib.load()
+    o = _lib.HobakServerOpts()
+    L.hobak_default_server_opts(ctypes.byref(o))
+    h = ctypes.c_void_p()
+    assert L.hobak_server_create(ctypes.byref(o), None, ctypes.byref(h)) == 0
+    a = _desc(scenes.config1_scene(2))
+    a.desc.material.kind = 42
+    jid = ctypes.c_int(-1)
+    assert L.hobak_server_submit(h, ctypes.byref(a.desc), 3, None, ctypes.byref(jid)) == 0
+    steps = ctypes.c_int(-1)
+    assert L.hobak_server_pump(h, ctypes.byref(steps)) == -1
+    msg = L.hobak_last_error().decode()
+    assert "building a cohort" in msg and "material" in msg, msg
+    info = _lib.HobakJobInfo()
+    assert L.hobak_server_job(h, jid.value, ctypes.byref(info), None, None, None) == 0 and info.state == 3
+    st = _lib.HobakServerStats()
+    assert L.hobak_server_get_stats(h, ctypes.byref(st)) == 0 and st.used_bytes == 0 and st.building == 0
+    assert L.hobak_server_pump(h, ctypes.byref(steps)) == 0 and steps.value == 0
+    assert L.hobak_server_idle(h) == 1
+    assert L.hobak_server_destroy(h) == 0
