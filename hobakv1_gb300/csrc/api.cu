@@ -788,7 +788,8 @@ int reorder_cluster_classes(hobak_batch_t* B) {
 }
 
 // Which scenes solve their inner PCG in a thread-block cluster, and in how
-// large a one, for the current precision: scenes without contact, in the
+// large a one, for the current precision (a scene in contact adds its
+// contact rows in the cluster as the tile path does): the
 // smallest cluster (1, 2, 4, 8 or 16 CTAs) that gives each thread at most one
 // vertex, or, with the cluster size capped below 16 (clusterMax), in a capped
 // cluster whose threads take several vertices while its vectors fit in shared
@@ -805,9 +806,7 @@ int prepare_cluster_classes(hobak_batch_t* B) {
   const int vpcLimit = (int)((kClusterSmemMax - cluster_fixed_bytes()) / cluster_vertex_bytes(mixed));
   std::vector<int> cl(n, 0);
   for (int s = 0; s < n; s++) {
-    const bool contact =
-        B->collArena && s < (int)B->collScenes.size() && (B->collScenes[s].vfOn || B->collScenes[s].eeOn);
-    if (!B->clusterPcg || contact) continue;
+    if (!B->clusterPcg) continue;
     const int nv = B->scenes[s].nv;
     const int force = s < (int)B->sceneCluster.size() ? B->sceneCluster[s] : 0;
     if (force < 0) continue;  // this scene keeps the tile path

@@ -95,6 +95,49 @@ __device__ __forceinline__ double ld_cluster_f64(uint32_t a) {
   return x;
 }
 
+// The contact rows of vertex u of w H_coll x (w = collision_lhs_scale of the
+// scene; H_coll = the sum over u's collision tets of (c c^T) (x) G, as
+// collision_row on the tile path), with x read four wide from the cluster's
+// shared memory: the scene's vertex id - v0 lies in the range of CTA
+// (id - v0) / vpc.  FP64 sums of the FP32 x (the contact blocks are not part
+// of the FP32 LHS).  Only free rows carry contact (pinned x are zero).
+// The per-step contact arrays contact_rows reads (DeviceCollisions).
+struct ContactRefs {
+  const int* incCount;
+  const int* incList;
+  const int4* pairTet;
+  const double* pairC;
+  const double* pairG;
+};
+
+template <typename T>
+__device__ __forceinline__ void contact_rows(const ContactRefs& c, int u, int v0, int vpc, double scale,
+                                             const uint32_t* ubase, double out[3]) {
+  constexpr int kUShift = sizeof(T) == 4 ? 4 : 5;
+  out[0] = out[1] = out[2] = 0.0;
+  const int k0 = c.incCount[u], k1 = c.incCount[u + 1];
+  for (int k = k0; k < k1; k++) {
+    const int e = c.incList[k], p = e >> 2, a = e & 3;
+    const int4 ct = c.pairTet[p];
+    const double* C = c.pairC + 4 * (size_t)p;
+    const double* G = c.pairG + 9 * (size_t)p;
+    const int id[4] = {ct.x, ct.y, ct.z, ct.w};
+    double z[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int w = id[q] - v0, owner = w / vpc;
+      T x[3];
+      ld_u(ubase[owner] + ((uint32_t)(w - owner * vpc) << kUShift), x);
+#pragma unroll
+      for (int j = 0; j < 3; j++) z[j] += C[q] * double(x[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) out[i] += C[a] * (G[i] * z[0] + G[i + 3] * z[1] + G[i + 6] * z[2]);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) out[i] *= scale;
+}
+
 // Three sums over the cluster: a warp tree, the CTA's warps summed by a tree
 // in warp 0 (in T, widened to FP64 once), a cluster barrier, then lanes
 // 0..CL-1 of warp 0 read the CL CTA sums through distributed shared memory
@@ -214,7 +257,9 @@ __device__ __forceinline__ void dot2_step(float a, float x, float& s, float& c) 
 template <int CL>
 __device__ __noinline__ double sweep_residual(cg::cluster_group& cluster, const ClusterSmem<float>& m, double* y,
                                               double* r64, const int* gather, const int* sliceRow, const int* rowptr,
-                                              const float* lhs, int u0, int n, double rsc) {
+                                              const float* lhs, int u0, int n, double rsc,
+                                              bool contact, ContactRefs coll, const unsigned char* freeMask,
+                                              int v0, int vpc, double collScale) {
   for (int lv = threadIdx.x; lv < n; lv += kClusterThreads) {
     const int u = u0 + lv;
 #pragma unroll
@@ -244,9 +289,11 @@ __device__ __noinline__ double sweep_residual(cg::cluster_group& cluster, const 
 #pragma unroll
         for (int k = 0; k < 3; k++) dot2_step(Bj[(3 * i + k) * kSlice], x[k], s[i], c[i]);
     }
+    double cr[3] = {0.0, 0.0, 0.0};
+    if (contact && freeMask[u]) contact_rows<float>(coll, u, v0, vpc, collScale, m.ubase, cr);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const double ri = r64[3 * u + i] - rsc * (double(s[i]) + double(c[i]));
+      const double ri = r64[3 * u + i] - rsc * (double(s[i]) + double(c[i]) + cr[i]);
       r64[3 * u + i] = ri;
       rl += ri * ri;
     }
@@ -255,7 +302,8 @@ __device__ __noinline__ double sweep_residual(cg::cluster_group& cluster, const 
 }
 template <int CL>
 __device__ double sweep_residual(cg::cluster_group&, const ClusterSmem<double>&, double*, double*, const int*,
-                                 const int*, const int*, const double*, int, int, double) {
+                                 const int*, const int*, const double*, int, int, double, bool, ContactRefs,
+                                 const unsigned char*, int, int, double) {
   return 0.0;  // FP64: one inner solve is the solve; never called
 }
 
@@ -317,6 +365,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
   const ClusterSmem<T> m = carve_smem<T>(smem, vpc);
   const int my0 = min(nvS, rank * vpc), my1 = min(nvS, (rank + 1) * vpc);
   const int nmine = my1 - my0;
+  // contact on this scene: its rows add w H_coll u (collision_lhs_scale)
+  const bool contact = b.collOn && (b.coll.scenes[sc].vfOn || b.coll.scenes[sc].eeOn);
   constexpr int kUShift = sizeof(T) == 4 ? 4 : 5;  // bytes of one u entry: 16 (float4) or 32
   if (threadIdx.x < CL) m.ubase[threadIdx.x] = map_cluster(m.u, threadIdx.x);
 
@@ -419,6 +469,14 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
             }
           }
         }
+        if (contact && b.freeMask[u]) {
+          const ContactRefs coll{b.coll.incCount, b.coll.incList, b.coll.pairTet, b.coll.pairC, b.coll.pairG};
+          double cr[3];
+          contact_rows<T>(coll, u, v0, vpc, collision_lhs_scale(b, sc), m.ubase, cr);
+          a0 += T(cr[0]);
+          a1 += T(cr[1]);
+          a2 += T(cr[2]);
+        }
         m.w[3 * lv] = a0;
         m.w[3 * lv + 1] = a1;
         m.w[3 * lv + 2] = a2;
@@ -492,7 +550,10 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kClusterThreads, 1)
     if (bc.stop == 2) break;                 // non-finite: the step has failed
     // ---- mixed: y += rsc d, r64 -= rsc A d, |r64|^2 ----
     const double s64 = sweep_residual<CL>(cluster, m, b.y, b.r64, gather, b.sliceRow, b.rowptr, v.lhs, v0 + my0,
-                                          nmine, rsc);
+                                          nmine, rsc, contact,
+                                          ContactRefs{b.coll.incCount, b.coll.incList, b.coll.pairTet, b.coll.pairC,
+                                                      b.coll.pairG},
+                                          b.freeMask, v0, vpc, contact ? collision_lhs_scale(b, sc) : 0.0);
     if (t0) {
       // the outer test (tile path: k_residual)
       ss.sweep += 1;

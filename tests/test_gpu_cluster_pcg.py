@@ -65,18 +65,60 @@ def test_large_and_small_scenes_share_a_batch(precision):
         assert np.array_equal(together[k], alone[0]), k
 
 
-def test_contact_scene_keeps_the_tile_path_beside_clusters():
-    two = scenes.two_cubes_scene(5)
+EPS, MU, BETA = 1e-3, 1e3, 0.001
+
+
+def as_set(p):
+    return sorted(map(tuple, np.asarray(p).tolist()))
+
+
+@pytest.mark.parametrize("ee", [False, True], ids=["vf", "vf+ee"])
+@pytest.mark.parametrize("precision,bound", [(hobak.PRECISION_FP64, 1e-8), (hobak.PRECISION_MIXED, 1e-6)],
+                         ids=["fp64", "mixed"])
+def test_contact_scene_in_a_cluster_matches_oracle_and_alone(precision, bound, ee):
+    """Self contact on the cluster path (a cluster adds its rows' contact
+    terms to the SpMV and to its residual update, as the tile path does):
+    two 8^3 cubes (1,458 vertices, a 2-CTA cluster) with vertex-face (and
+    edge-edge) contact beside clustered small scenes: positions within
+    `bound` of the FP64 oracle, the vertex-face pair sets equal the oracle's
+    (FP64), and the contact scene bitwise equal to itself alone.  FP64 runs
+    20 steps; mixed precision the first 10, the contact phase (the pairs
+    release by step 13): once the cubes separate with edge-edge springs
+    still engaged the trajectory becomes sensitive enough that mixed
+    precision departs from FP64 on the tile path as well (5e-6 by step 20,
+    from 1e-8 at step 13)."""
+    s = scenes.two_cubes_scene(8, gap=2e-4)
     small = scenes.config4_scenes(count=2, nmin=5, nmax=8)
-    b = hobak.BATCH([two] + small, hobak.solver_opts(precision=hobak.PRECISION_MIXED))
-    b.set_tuning(cluster_pcg=1)
-    b.set_collisions(0, True, 1e-3, 1e3, 0.001)
-    b.step(4)
-    a = hobak.BATCH([two], hobak.solver_opts(precision=hobak.PRECISION_MIXED))
-    a.set_tuning(cluster_pcg=1)
-    a.set_collisions(0, True, 1e-3, 1e3, 0.001)
-    a.step(4)
+
+    def batch(scene_list):
+        b = hobak.BATCH(scene_list, hobak.solver_opts(precision=precision))
+        b.set_tuning(cluster_pcg=1)
+        b.set_collisions(0, True, EPS, MU, BETA)
+        if ee:
+            b.set_edge_collisions(0, True)
+        return b
+
+    b = batch([s] + small)
+    sim = oracle.Sim(s, precond=hobak.PRECOND_BLOCK_JACOBI)
+    sim.set_collisions(True, EPS, MU, BETA, ee=ee)
+    chunks = 4 if precision == hobak.PRECISION_FP64 else 2
+    for k in range(chunks):
+        if precision == hobak.PRECISION_FP64:
+            gp, _ = b.collision_pairs(0, detect_now=True)
+            op, _ = sim.vf_pairs()
+            assert as_set(gp) == as_set(op), k
+        b.step(5)
+        sim.step(5)
+        assert b.pcg_path()[0] > 0  # the contact scene solves in a cluster
+        x, _ = b.get_state(0)
+        xo, _ = sim.state()
+        err = rel(x + s.rest.reshape(-1), xo + s.rest.reshape(-1))
+        assert err < bound, (k, err)
+    a = batch([s])
+    a.step(5 * chunks)
     assert np.array_equal(b.get_state(0)[0], a.get_state(0)[0])
+    b.close()
+    a.close()
 
 
 @pytest.mark.parametrize("precision", [hobak.PRECISION_FP64, hobak.PRECISION_MIXED], ids=["fp64", "mixed"])
