@@ -790,11 +790,13 @@ int reorder_cluster_classes(hobak_batch_t* B) {
 // Which scenes solve their inner PCG in a thread-block cluster, and in how
 // large a one, for the current precision (a scene in contact adds its
 // contact rows in the cluster as the tile path does): the
-// smallest cluster (1, 2, 4, 8 or 16 CTAs) that gives each thread at most one
-// vertex, or, with the cluster size capped below 16 (clusterMax), in a capped
-// cluster whose threads take several vertices while its vectors fit in shared
-// memory (fewer SMs per scene, more scenes at once); larger scenes keep the
-// tile path, which spreads them wider.  The choice depends only on the scene itself, so
+// smallest cluster (1, 2, 4, 8 or 16 CTAs, at most clusterMax) that gives
+// each thread at most one vertex, or else the largest allowed cluster, whose
+// threads then take several vertices, as long as its vectors fit in shared
+// memory (fewer SMs per scene, more scenes at once; for a scene of up to ~40 k
+// vertices in mixed precision, one 16-CTA cluster beats the tile path's two
+// grid-wide kernels per iteration); larger scenes keep the tile path, which
+// spreads them wider.  The choice depends only on the scene itself, so
 // a scene takes the same path alone and in any batch.  Runs outside graph
 // capture (it uploads); drops the graphs when the assignment changed.
 int prepare_cluster_classes(hobak_batch_t* B) {
@@ -812,16 +814,16 @@ int prepare_cluster_classes(hobak_batch_t* B) {
     if (force < 0) continue;  // this scene keeps the tile path
     if (force > 0) {  // this scene's own cluster size, where its vectors fit
       const int vpcF = (nv + force - 1) / force;
-      if (vpcF <= kClusterThreads || (force < 16 && vpcF <= vpcLimit)) cl[s] = force;
+      if (vpcF <= vpcLimit) cl[s] = force;
       continue;
     }
-    // the smallest cluster that gives each thread one vertex at most; under
-    // a cap below 16 CTAs, threads of a capped cluster take several vertices
-    // as long as the CTA's vectors fit in its shared memory
+    // the smallest cluster that gives each thread one vertex at most; else
+    // the cap, whose threads take several vertices as long as the CTA's
+    // vectors fit in its shared memory
     int c = 1;
     while (c < B->clusterMax && (nv + c - 1) / c > kClusterThreads) c *= 2;
     const int vpc = (nv + c - 1) / c;
-    if (vpc <= kClusterThreads || (B->clusterMax < 16 && vpc <= vpcLimit)) cl[s] = c;
+    if (vpc <= vpcLimit) cl[s] = c;
   }
   std::vector<int> list;
   bool changed = false;

@@ -57,12 +57,36 @@ def test_cluster_path_matches_oracle_with_jacobi_iterations():
 def test_large_and_small_scenes_share_a_batch(precision):
     """A scene too large for a cluster takes the tile path while the small
     ones solve in clusters beside it; each result equals the scene alone."""
-    big = scenes.config2_scene(30, "snh")  # 29,791 vertices: more than 16 x 1024
+    big = scenes.config2_scene(40, "snh")  # 68,921 vertices: more than 16 CTAs' shared memory holds
     small = scenes.config4_scenes(count=3, nmin=6, nmax=12)
     together, _ = run([big] + small, precision, 4, True)
+    b = hobak.BATCH([big] + small, hobak.solver_opts(precision=precision))
+    b.set_tuning(cluster_pcg=1)
+    paths = b.pcg_path()
+    b.close()
+    assert paths[0] == 0 and (paths[1:] > 0).all(), paths
     for k, sc in enumerate([big] + small):
         alone, _ = run([sc], precision, 4, True)
         assert np.array_equal(together[k], alone[0]), k
+
+
+def test_mid_size_scene_in_a_16_cta_cluster_matches_the_tile_path():
+    """Mixed precision: a scene of 29,791 vertices (more than one per thread
+    of 16 CTAs) solves in one 16-CTA cluster whose threads take two vertices
+    each, and agrees with the tile path to rounding (FP64 vectors would not
+    fit: the FP64 batch keeps it on the tile path)."""
+    s = scenes.config2_scene(30, "snh")
+    b = hobak.BATCH([s], hobak.solver_opts(precision=hobak.PRECISION_MIXED))
+    b.set_tuning(cluster_pcg=1)
+    assert b.pcg_path()[0] == 16
+    b.close()
+    b = hobak.BATCH([s], hobak.solver_opts(precision=hobak.PRECISION_FP64))
+    b.set_tuning(cluster_pcg=1)
+    assert b.pcg_path()[0] == 0
+    b.close()
+    xc, stc = run([s], hobak.PRECISION_MIXED, 6, True)
+    xt, stt = run([s], hobak.PRECISION_MIXED, 6, False)
+    assert rel(xc[0], xt[0]) < 1e-6 and stc[0][1] == 1 and stc[0][2] < 1e-8, (rel(xc[0], xt[0]), stc, stt)
 
 
 EPS, MU, BETA = 1e-3, 1e3, 0.001
