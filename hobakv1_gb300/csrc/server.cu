@@ -26,6 +26,8 @@
 #include <thread>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "hobak_gpu.h"
 
 namespace hobak {
@@ -94,10 +96,14 @@ long long footprint_bytes(const hobak_scene_desc& s, int precision) {
   return nt * perTet + nb * perBlock + nv * perVertex + (1LL << 20);
 }
 
-// One builder thread running build tasks in submission order.
+// One builder thread running build tasks in submission order, on the
+// device that was current where the server was created.
 class Builder {
  public:
-  Builder() : worker_([this] { run(); }) {}
+  Builder() {
+    if (cudaGetDevice(&device_) != cudaSuccess) device_ = 0;
+    worker_ = std::thread([this] { run(); });
+  }
   ~Builder() {
     {
       std::lock_guard<std::mutex> lk(m_);
@@ -119,6 +125,7 @@ class Builder {
 
  private:
   void run() {
+    cudaSetDevice(device_);
     for (;;) {
       std::function<void()> f;
       {
@@ -135,6 +142,7 @@ class Builder {
   std::condition_variable cv_;
   std::deque<std::function<void()>> q_;
   bool stop_ = false;
+  int device_ = 0;
   std::thread worker_;
 };
 
