@@ -536,11 +536,16 @@ def step_rooflines(batch, spec, scene_list, phases, phase_steps, iters_by_scene,
                   else "k_spmv + k_update (tile path)",
                   "step_ms": pcg_ms, "algorithmic_bytes_per_step": pcg_bytes, "GB/s": gbs(pcg_bytes, pcg_ms),
                   "frac_hbm": gbs(pcg_bytes, pcg_ms) / peak, "traffic": traffic.get("pcg"),
+                  "dram_GB/s": gbs(traffic["pcg"], pcg_ms) if traffic.get("pcg") else None,
+                  "dram_frac_hbm": gbs(traffic["pcg"], pcg_ms) / peak if traffic.get("pcg") else None,
                   "scenes_cluster_path": int(len(paths) - n_tile), "scenes_tile_path": n_tile,
                   "iterations_slowest_scene": slow,
                   "us_per_iteration_slowest_scene": 1e3 * pcg_ms / slow if slow else None,
                   "how": "sum over scenes of PCG iterations x (SpMV + update bytes of the scene), over the "
-                         "phase's CUDA-event time per step (all refinement sweeps)"}
+                         "phase's CUDA-event time per step (all refinement sweeps); in a cluster the vectors "
+                         "stay in shared memory and the matrix comes from L2 or DRAM, so this is an "
+                         "HBM-equivalent rate; traffic and dram_GB/s: the DRAM bytes ncu counts for a step's "
+                         "cluster launches (profiles/traffic.json) over the same time"}
     for k in ("spmv", "pcg_update"):
         a = gbs(kbytes[k], kms[k])
         ent[k] = {"kernel": "k_spmv" if k == "spmv" else "k_update", "launch_ms": kms[k],
