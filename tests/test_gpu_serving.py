@@ -142,3 +142,20 @@ def test_finished_jobs_release_their_memory(impl):
     srv.drain()
     x, v = alone(longer, hobak.PRECISION_FP64)
     assert np.array_equal(longer.result_x, x) and np.array_equal(longer.result_v, v)
+
+
+@pytest.mark.parametrize("precision", [hobak.PRECISION_FP64, hobak.PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_admission_estimate_bounds_the_device_bytes(precision):
+    """The footprint both servers admit by is an upper bound of what a batch
+    of those scenes holds on the device (so the budget is never exceeded),
+    with and without contact."""
+    sc = scenes.config4_scenes(count=3, nmin=5, nmax=14) + [scenes.two_cubes_scene(6)]
+    for s in sc:
+        b = hobak.BATCH([s], hobak.solver_opts(precision=precision))
+        assert footprint_bytes(s, precision) >= b.device_bytes(), s.name
+        b.close()
+    b = hobak.BATCH(sc, hobak.solver_opts(precision=precision))
+    b.set_collisions(len(sc) - 1, True, *VF)
+    b.step(1)
+    assert sum(footprint_bytes(s, precision) for s in sc) >= b.device_bytes()
+    b.close()
