@@ -12,10 +12,10 @@
 // DRAM, when a full batch's other scenes have evicted them) every iteration.
 // In mixed precision the launch also runs every refinement sweep: the FP64
 // y update, the residual update r -= A d in compensated FP32 and the outer
-// FP64 test, then the next inner solve, until the test passes.  The tile
+// FP64 test, then the next inner solve, until the test passes.  A scene in
+// contact adds its rows' contact terms from the step's pair lists.  The tile
 // path (solver.cu: two grid-wide kernels per iteration, each ending in a
-// ticketed reduction) remains for scenes too large for a cluster and for
-// scenes with contact.
+// ticketed reduction) remains for scenes too large for a cluster.
 //
 // The iteration is the same Chronopoulos-Gear PCG as the tile path, with the
 // same scalars, stopping rules and iteration accounting (ConjugateGradient.h

@@ -336,11 +336,13 @@ int hobak_batch_kernel_bytes(hobak_batch b, double* bytes);
  * (64 or 128; one CTA of the SpMV/update/reduction kernels), CTA sizes of the
  * element kernel (64 or 128) and of the assembly kernel (64..1024, multiple of
  * 32), PCG iterations per graph loop body / host poll (1..64), and whether
- * scenes of at most 16 x 1024 vertices without contact solve their inner PCG
- * inside one thread-block cluster (1; beside the tile path for the others) or
- * on the batch-wide tile path (0, the default), and the largest cluster such
- * a scene may use (cluster_max: 1, 2, 4, 8 or 16 CTAs; larger scenes keep the
- * tile path, which spreads them over the whole GPU).  step_ms is the measured
+ * scenes whose vectors fit the shared memory of at most cluster_max CTAs
+ * (one vertex per thread, or several in the largest cluster; contact scenes
+ * included) solve their linear system inside one thread-block cluster (1;
+ * beside the tile path for the others) or on the batch-wide tile path (0,
+ * the default), and the largest cluster such a scene may use (cluster_max:
+ * 1, 2, 4, 8 or 16 CTAs; larger scenes keep the tile path, which spreads them
+ * over the whole GPU).  step_ms is the measured
  * step time of the chosen shape (autotune only; 0 otherwise).  The tile size and
  * the PCG path change results, and only by FP rounding (they change the shape
  * of the dot-product reduction trees). */
