@@ -171,3 +171,26 @@ def test_capped_clusters_match_the_tile_path_and_the_scene_alone(precision, cap)
         c.set_tuning(cluster_pcg=1)
         c.step(4)
         assert np.array_equal(b.get_state(k)[0], c.get_state(0)[0]), k
+
+
+@pytest.mark.parametrize("integrator", [hobak.INTEGRATOR_POSITION, hobak.INTEGRATOR_NEWMARK],
+                         ids=["position", "newmark"])
+def test_contact_in_a_cluster_with_the_other_integrators(integrator):
+    """The contact rows' scale follows the integrator (collision_lhs_scale:
+    BACKWARD_EULER_POSITION's -(beta/dt + 1), NEWMARK's -(a3 beta + 1)):
+    two 7^3 cubes in vertex-face contact, FP64, 10 steps, the cluster path
+    within 1e-9 of the tile path."""
+    s = scenes.two_cubes_scene(7, gap=2e-4)
+
+    def run_path(cluster):
+        b = hobak.BATCH([s], hobak.solver_opts(integrator=integrator))
+        b.set_tuning(cluster_pcg=int(cluster))
+        b.set_collisions(0, True, EPS, MU, BETA)
+        b.step(10)
+        assert (b.pcg_path()[0] > 0) == cluster
+        x = b.get_state(0)[0] + s.rest.reshape(-1)
+        b.close()
+        return x
+
+    xc, xt = run_path(True), run_path(False)
+    assert rel(xc, xt) < 1e-9, rel(xc, xt)
