@@ -239,7 +239,7 @@ int rest_hessian(hobak_batch_t* B) {
   if (B->K0) return HOBAK_OK;
   const size_t kBytes = sizeof(double) * 9 * (size_t)std::max(B->nblocks, 1);
   CUDA_TRY(cudaMalloc(&B->K0, kBytes));
-  const size_t ehBytes = sizeof(double) * kElemHess * (size_t)B->nt, xBytes = sizeof(double) * 3 * (size_t)B->nv;
+  const size_t ehBytes = sizeof(double) * kElemHessStride * (size_t)B->nt, xBytes = sizeof(double) * 3 * (size_t)B->nv;
   void* scratch = nullptr;
   CUDA_TRY(cudaMalloc(&scratch, ehBytes + 2 * xBytes));
   cudaStream_t s = B->stream;
@@ -285,7 +285,7 @@ int alloc_precision(hobak_batch_t* B) {
   const bool mixed = B->opts.precision == HOBAK_PRECISION_MIXED;
   const size_t w = mixed ? sizeof(float) : sizeof(double);
   Arena A;
-  const size_t oEH = A.reserve(w * kElemHess * nt);
+  const size_t oEH = A.reserve(w * kElemHessStride * nt);
   const size_t oLhs = A.reserve(w * vals);
   const size_t oMinv = A.reserve(w * 9 * nv);
   size_t oVec[6];
@@ -2493,7 +2493,7 @@ int hobak_batch_assemble(hobak_batch b, int scene, int* nblocks, int* rowptr, in
   // Hessians in scratch of this call), then the device gathers K (CSR
   // order, scratch) and R (into the per-step rhs buffer)
   DeviceScratch scratch;
-  const size_t ehBytes = sizeof(double) * kElemHess * (size_t)b->nt;
+  const size_t ehBytes = sizeof(double) * kElemHessStride * (size_t)b->nt;
   CUDA_TRY(cudaMalloc(&scratch.p, ehBytes + sizeof(double) * 9 * (size_t)std::max(b->nblocks, 1)));
   DeviceBatch d = b->d;
   d.elemH = static_cast<double*>(scratch.p);

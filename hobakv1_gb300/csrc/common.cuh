@@ -29,6 +29,7 @@ constexpr int kTileV = 128;       // default vertices per PCG tile (one CTA)
 constexpr int kMinTileV = 64;     // smallest tile size; tile tables are sized for it
 //       // vertices per PCG tile (one CTA)
 constexpr int kElemHess = 90;     // 10 upper blocks x 9
+constexpr int kElemHessStride = 92;  // per-tet stride: each tet's blocks start on a 16-byte boundary
 constexpr int kPartials = 4;      // per-tile partial sums slots
 // Timesteppers: BACKWARD_EULER_VELOCITY::solve (unknown: the velocity update)
 // and BACKWARD_EULER_POSITION::solveRayleighDamped (unknown: the position

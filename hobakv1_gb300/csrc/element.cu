@@ -177,8 +177,9 @@ __device__ __forceinline__ void expand_blocks(const T* Hr, double vol, OutT* out
 // The same 10 blocks as expand_blocks, with the same sums in the same order,
 // emitted in memory order two values per store (8-byte stores for FP32,
 // 16-byte for FP64): 45 store instructions per tet instead of 90, which
-// relieves the load/store queue the per-tet kernels saturate.  out is
-// 8-byte aligned (FP32, 360 B per tet) or 16-byte aligned (FP64, 720 B).
+// relieves the load/store queue the per-tet kernels saturate.  out is the
+// tet's record, 16-byte aligned so that the assembly reads each block with
+// 16-byte loads: 92 values per tet, the last two padding written as zeros.
 template <typename T, typename OutT>
 __device__ __forceinline__ void store_blocks(const T* Hr, double vol, OutT* out) {
   const T nv = T(-vol);
@@ -212,6 +213,11 @@ __device__ __forceinline__ void store_blocks(const T* Hr, double vol, OutT* out)
       *reinterpret_cast<double2*>(out + e) = make_double2(double(value(e)), double(value(e + 1)));
     }
   }
+  // the padding too: a partly written sector costs a DRAM read on eviction
+  if (sizeof(OutT) == 4)
+    *reinterpret_cast<float2*>(out + kElemHess) = make_float2(0.f, 0.f);
+  else
+    *reinterpret_cast<double2*>(out + kElemHess) = make_double2(0.0, 0.0);
 }
 
 // 12 doubles (16-byte aligned) as six 16-byte stores
@@ -358,7 +364,7 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
   double* g = b.elemG + 12 * (size_t)t;
   if (!velocityTerm) {
     store12(g, f);
-    store_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
+    store_blocks<HT, HT>(Hr, vol, outH + kElemHessStride * (size_t)t);
     return;
   }
   // He v = -vol D^T Hr (D v): D v = relative velocities of vertices 1..3
@@ -385,7 +391,7 @@ __global__ void __launch_bounds__(128, sizeof(HT) == 4 ? 4 : 1)
 #pragma unroll
   for (int i = 0; i < 3; i++) gl[i] = f[i] - double(h0[i]);
   store12(g, gl);
-  store_blocks<HT, HT>(Hr, vol, outH + kElemHess * (size_t)t);
+  store_blocks<HT, HT>(Hr, vol, outH + kElemHessStride * (size_t)t);
 }
 
 // Element terms of the anisotropic energies (ANISOTROPIC_ARAP, STVK, FUNG,
@@ -443,7 +449,7 @@ __global__ void __launch_bounds__(128) k_element_aniso(DeviceBatch b, int rawFor
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int k = 0; k < 3; k++) G[3 * i + k] = HT((i == k ? al : 0.0) + be * g[i] * g[k]);
-  HT* out = outH + kElemHess * (size_t)t;
+  HT* out = outH + kElemHessStride * (size_t)t;
   const HT nv = HT(-vol);
 #pragma unroll
   for (int A = 0; A < 4; A++)
@@ -453,6 +459,8 @@ __global__ void __launch_bounds__(128) k_element_aniso(DeviceBatch b, int rawFor
 #pragma unroll
       for (int e = 0; e < 9; e++) out[9 * upper_block(A, B) + e] = cc * G[e];
     }
+  out[kElemHess] = HT(0);
+  out[kElemHess + 1] = HT(0);
   double* gout = b.elemG + 12 * (size_t)t;
   if (!velocityTerm) {
 #pragma unroll

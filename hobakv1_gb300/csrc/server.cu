@@ -90,7 +90,7 @@ struct Built {
 long long footprint_bytes(const hobak_scene_desc& s, int precision) {
   const long long nv = s.nv, nt = s.nt, nb = 16 * nv;
   const long long w = precision == HOBAK_PRECISION_MIXED ? 4 : 8;
-  const long long perTet = 16 + 72 + 8 + 4 + 96 + 64 + 16 + 8 + 90 * w;
+  const long long perTet = 16 + 72 + 8 + 4 + 96 + 64 + 16 + 8 + 92 * w;  // element Hessians: 92 values per tet
   const long long perBlock = 4 + 4 + 4 + 4 + 9 * w;
   const long long perVertex = 5 * 24 + 8 + 1 + 4 + 4 + 4 + 3 * 24 + 9 * w + (w == 4 ? 6 : 4) * 3 * w;
   return nt * perTet + nb * perBlock + nv * perVertex + (1LL << 20);

@@ -284,7 +284,7 @@ __device__ __forceinline__ HT gather_block_entry(const DeviceBatch& b, const HT*
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int t = src[q] >> 4, ea = (src[q] >> 2) & 3, eb = src[q] & 3;
-      const HT* H = elemH + (size_t)kElemHess * t;
+      const HT* H = elemH + (size_t)kElemHessStride * t;
       val[q] = (k + q >= k1) ? HT(0)
                : (ea <= eb)  ? H[9 * upper_block(ea, eb) + 3 * r + c]
                              : H[9 * upper_block(eb, ea) + 3 * c + r];
@@ -375,9 +375,30 @@ __global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __res
 #pragma unroll
         for (int q = 0; q < kQ; q++) {
           const int t = src[q] >> 4, ea = (src[q] >> 2) & 3, eb = src[q] & 3;
-          const HT* H = elemH + (size_t)kElemHess * t + 9 * ((ea <= eb) ? upper_block(ea, eb) : upper_block(eb, ea));
+          const int off = 9 * ((ea <= eb) ? upper_block(ea, eb) : upper_block(eb, ea));
+          if (sizeof(HT) == sizeof(float)) {
+            // the block's 9 values from the three 16-byte words that cover
+            // them (the tet's record starts on a 16-byte boundary), then
+            // shifted down by the block's offset within the first word
+            const float4* W = reinterpret_cast<const float4*>(elemH + (size_t)kElemHessStride * t + (off & ~3));
+            float4 w0 = make_float4(0.f, 0.f, 0.f, 0.f), w1 = w0, w2 = w0;
+            if (k + q < k1) {
+              w0 = __ldg(W);
+              w1 = __ldg(W + 1);
+              w2 = __ldg(W + 2);
+            }
+            const float win[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+            const int sh = off & 3;
+            float mid[11];
 #pragma unroll
-          for (int e = 0; e < 9; e++) val[q][e] = (k + q < k1) ? H[e] : HT(0);
+            for (int e = 0; e < 11; e++) mid[e] = (sh & 1) ? win[e + 1] : win[e];
+#pragma unroll
+            for (int e = 0; e < 9; e++) val[q][e] = HT((sh & 2) ? mid[e + 2] : mid[e]);
+          } else {
+            const HT* H = elemH + (size_t)kElemHessStride * t + off;
+#pragma unroll
+            for (int e = 0; e < 9; e++) val[q][e] = (k + q < k1) ? H[e] : HT(0);
+          }
           if (ea > eb) {  // lower-triangle block: the stored upper block transposed
             HT tmp;
             tmp = val[q][1]; val[q][1] = val[q][3]; val[q][3] = tmp;

@@ -60,7 +60,8 @@ def footprint_bytes(scene, precision: int) -> int:
     nb = 16 * nv
     w = 4 if precision == hobak.PRECISION_MIXED else 8
     # tets, DmInv, vol, scene id, element g, contribution map, incidences, psi; element Hessians
-    per_tet = 16 + 72 + 8 + 4 + 96 + 64 + 16 + 8 + 90 * w
+    # (90 values padded to 92 per tet)
+    per_tet = 16 + 72 + 8 + 4 + 96 + 64 + 16 + 8 + 92 * w
     # cols, block row, contribution ranges, sliced column; sliced LHS values
     per_block = 4 + 4 + 4 + 4 + 9 * w
     # rest, x, v, f_ext, pin target, mass, mask, scene id, rowptr, incidences,
