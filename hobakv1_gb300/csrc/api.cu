@@ -585,7 +585,7 @@ int build_batch(hobak_batch_t* B, const hobak_scene_desc* descs, int n) {
   d.ntiles = ntiles;
   d.tileV = kTileV;
   d.elemThreads = 128;
-  d.asmThreads = 256;
+  d.asmThreads = 64;  // the fastest measured on the 7.2 M-tet mix (1.48 ms; 256 threads: 1.70)
   d.scenes = carve<SceneParams>(base, oScenes);
   d.solve = carve<SolveState>(base, oSolve);
   d.active = carve<int>(base, oActive);

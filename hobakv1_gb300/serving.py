@@ -395,7 +395,7 @@ class NativeServer:
         o.merge, o.merge_fraction = int(merge), float(merge_fraction)
         o.async_build, o.keep_results = int(async_build), int(keep_results)
         if tuning:
-            cur = dict(tile_vertices=128, element_threads=128, assembly_threads=256, pcg_chunk=8, cluster_pcg=0,
+            cur = dict(tile_vertices=128, element_threads=128, assembly_threads=64, pcg_chunk=8, cluster_pcg=0,
                        cluster_max=16, step_ms=0.0)
             cur.update(tuning)
             o.use_tuning = 1
