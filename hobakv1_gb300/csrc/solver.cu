@@ -351,9 +351,11 @@ __global__ void k_assemble_entry(DeviceBatch b, const HT* __restrict__ elemH, T*
 // contribution is 9 contiguous values: a 3x3 block of one element Hessian,
 // transposed for the lower triangle), then LHS block = S(M - dt^2 K)S + (I - S)
 // written entry by entry, each entry of the warp's 32 slots one 128-byte line.
-// Blocks of parked scenes keep their old values.
+// Blocks of parked scenes keep their old values.  The gathers are latency
+// bound, so registers are capped at 64 (no spills) for 32 resident warps per
+// SM instead of 28.
 template <typename HT, typename T>
-__global__ void k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
+__global__ void __maxnreg__(64) k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= (size_t)kSlice * b.nslotRows) return;
   const int r = (int)(g / kSlice), lane = (int)(g % kSlice);
