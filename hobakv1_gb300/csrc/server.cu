@@ -198,14 +198,6 @@ struct hobak_server_t {
     return builder->submit([this, js] { return build_now(js); });
   }
 
-  // The built cohort, or the build's error reported on this thread.
-  static int take(const std::shared_future<std::shared_ptr<Built>>& f, std::unique_ptr<Cohort>* out) {
-    std::shared_ptr<Built> b = f.get();
-    if (b->rc != HOBAK_OK) return fail(b->rc, "server: building a cohort: " + b->error);
-    *out = std::move(b->cohort);
-    return HOBAK_OK;
-  }
-
   static void attach(Cohort* c) {
     for (size_t k = 0; k < c->jobs.size(); k++) {
       c->jobs[k]->cohort = c;
@@ -292,47 +284,59 @@ struct hobak_server_t {
     }
   }
 
-  // At c's step boundary: its re-pack, if built, with the carried jobs'
-  // state copied in; c is freed.  Returns the new cohort, or null while the
-  // build is still running (or on error, with *rc set).
-  Cohort* swap_ready(Cohort* c, int* rc) {
-    *rc = HOBAK_OK;
-    if (!c->hasRepl || c->inFlight || !ready(c->repl)) return nullptr;
-    {
-      std::shared_ptr<Built> r = c->repl.get();
-      if (r->rc != HOBAK_OK) {  // the carried jobs go on in c; the arrivals fail
-        c->hasRepl = false;
-        *rc = drop_failed(r, c->replReserved, true, c);
-        return nullptr;
-      }
-    }
-    std::unique_ptr<Cohort> nb;
-    if ((*rc = take(c->repl, &nb))) return nullptr;
+  // The carried jobs' state (x, v and NEWMARK's acceleration) copied from c
+  // into its re-pack nb; the jobs that finished meanwhile parked there.
+  int carry_over(Cohort* c, Cohort* nb) {
     const bool newmark = solver.integrator == HOBAK_INTEGRATOR_NEWMARK;
-    const double t = now_s();
     std::vector<double> x, v, a;
     for (size_t k = 0; k < nb->jobs.size(); k++) {
       Job* j = nb->jobs[k];
-      if (j->cohort == c) {  // carried over: continue from where it is
-        const size_t n = 3 * (size_t)j->desc.nv;
-        x.resize(n);
-        v.resize(n);
-        if ((*rc = hobak_batch_get_state(c->batch, j->slot, x.data(), v.data()))) return nullptr;
-        if ((*rc = hobak_batch_set_state(nb->batch, (int)k, x.data(), v.data()))) return nullptr;
-        if (newmark) {
-          a.resize(n);
-          if ((*rc = hobak_batch_get_acceleration(c->batch, j->slot, a.data()))) return nullptr;
-          if ((*rc = hobak_batch_set_acceleration(nb->batch, (int)k, a.data()))) return nullptr;
-        }
-        if (j->state == HOBAK_JOB_FINISHED) {  // finished while the re-pack was built
-          if ((*rc = hobak_batch_set_active(nb->batch, (int)k, 0))) return nullptr;
-          nb->running -= 1;
-        }
-      } else {  // a merged arrival
+      if (j->cohort != c) continue;  // a merged arrival starts from its initial state
+      const size_t n = 3 * (size_t)j->desc.nv;
+      x.resize(n);
+      v.resize(n);
+      if (int rc = hobak_batch_get_state(c->batch, j->slot, x.data(), v.data())) return rc;
+      if (int rc = hobak_batch_set_state(nb->batch, (int)k, x.data(), v.data())) return rc;
+      if (newmark) {
+        a.resize(n);
+        if (int rc = hobak_batch_get_acceleration(c->batch, j->slot, a.data())) return rc;
+        if (int rc = hobak_batch_set_acceleration(nb->batch, (int)k, a.data())) return rc;
+      }
+      if (j->state == HOBAK_JOB_FINISHED) {  // finished while the re-pack was built
+        if (int rc = hobak_batch_set_active(nb->batch, (int)k, 0)) return rc;
+        nb->running -= 1;
+      }
+    }
+    return HOBAK_OK;
+  }
+
+  // At c's step boundary: its re-pack, if built, with the carried jobs'
+  // state copied in; c is freed.  Returns the new cohort, or null while the
+  // build is still running, or on error (*rc set): then the carried jobs go
+  // on in c, the merged arrivals fail and the re-pack is freed.
+  Cohort* swap_ready(Cohort* c, int* rc) {
+    *rc = HOBAK_OK;
+    if (!c->hasRepl || c->inFlight || !ready(c->repl)) return nullptr;
+    std::shared_ptr<Built> r = c->repl.get();
+    c->hasRepl = false;
+    if (r->rc != HOBAK_OK) {
+      *rc = drop_failed(r, c->replReserved, true, c);
+      return nullptr;
+    }
+    std::unique_ptr<Cohort> nb = std::move(r->cohort);
+    if ((*rc = carry_over(c, nb.get()))) {
+      for (Job* j : nb->jobs)
+        if (j->cohort != c) j->state = HOBAK_JOB_FAILED;
+      destroy(nb);
+      used -= c->replReserved;
+      return nullptr;
+    }
+    const double t = now_s();
+    for (Job* j : nb->jobs)
+      if (j->cohort != c) {  // a merged arrival
         j->admitted = t;
         mergedArrivals += 1;
       }
-    }
     attach(nb.get());
     used += nb->bytes - c->replReserved - c->bytes;
     Cohort* out = nb.get();
