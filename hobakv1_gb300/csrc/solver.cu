@@ -353,7 +353,8 @@ __global__ void k_assemble_entry(DeviceBatch b, const HT* __restrict__ elemH, T*
 // written entry by entry, each entry of the warp's 32 slots one 128-byte line.
 // Blocks of parked scenes keep their old values.  The gathers are latency
 // bound, so registers are capped at 64 (no spills) for 32 resident warps per
-// SM instead of 28.
+// SM instead of 28; the cap also keeps every tunable CTA size (up to 1024
+// threads) within the SM's 65,536 registers.
 template <typename HT, typename T>
 __global__ void __maxnreg__(64) k_assemble(DeviceBatch b, const HT* __restrict__ elemH, T* __restrict__ lhs) {
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
