@@ -32,6 +32,7 @@ def test_cta_sizes_and_chunk_do_not_change_results(precision):
     sc = mix()
     ref = run(sc, precision)
     for shape in (dict(element_threads=64), dict(assembly_threads=128), dict(assembly_threads=512),
+                  dict(assembly_threads=1024),
                   dict(pcg_chunk=4), dict(pcg_chunk=16), dict(cluster_max=4)):
         got = run(sc, precision, **shape)
         for (x, v), (xr, vr) in zip(got, ref):
